@@ -1,0 +1,199 @@
+/*
+ * pmgpu.h — C ABI of the GB300 (sm_103a) saddle-point multigrid solver for
+ * Q2/P1disc Oseen systems (NSTYPE 4: nine velocity blocks A11..A33 sharing one
+ * CSR pattern, B1..B3, B1T..B3T).
+ *
+ * The entry points replace, one for one, the solver objects that ParMooN's
+ * NSE3D/TNSE3D programs build when SC_SOLVER_SADDLE=16 (FGMRES),
+ * SC_PRECONDITIONER_SADDLE=5 (multigrid) and SC_SMOOTHER_SADDLE=2 (cell Vanka):
+ *
+ *   pm_create            TNSE_MultiGrid::TNSE_MultiGrid  (include/FE/NSE_MultiGrid.h:193)
+ *                        + TFgmresIte ctor parameters    (src/FE/FgmresIte.C:75-176)
+ *   pm_add_level         TNSE_MultiGrid::AddLevel        (src/FE/NSE_MultiGrid.C:81-102)
+ *                        with the arrays a TNSE_MGLevel4 captures in its ctor
+ *                        (src/FE/NSE_MGLevel4.C:119-328)
+ *   pm_setup             TNSE_MultiGrid::InitGPU         (src/FE/NSE_MultiGrid.C:105-185)
+ *                        (upload, colour, factor all local Vanka blocks once,
+ *                        factor the coarse dense system once)
+ *   pm_defect            TNSE_MGLevel4::Defect           (src/FE/NSE_MGLevel4.C:465-539)
+ *   pm_coupled_defect    Defect_NSE4 / CoupledDefect     (src/FE/MGComponents3D.C:3038-3231)
+ *   pm_matvec            MatVect_NSE4 / CoupledMatVect   (src/FE/MGComponents3D.C:2872-3035)
+ *   pm_cell_vanka        TNSE_MGLevel4::CellVanka        (src/FE/NSE_MGLevel4.C:1653-2087;
+ *                        colour-block semantics of CellVanka_GPU, src/FE/NSE_CellVanka.cu:1748-2555)
+ *   pm_restrict          DefectRestriction (vector+scalar) (src/FE/MGComponents3D.C:711-1242)
+ *   pm_prolongate        Prolongate (vector+scalar)      (src/FE/MGComponents3D.C:184-708)
+ *   pm_solve_exact       TNSE_MGLevel4::SolveExact       (src/FE/NSE_MGLevel4.C:5728-5847)
+ *   pm_vcycle            TMultiGridIte::Iterate          (src/FE/MultiGridIte.C:76-132)
+ *                        -> TNSE_MultiGrid::Cycle        (src/FE/NSE_MultiGrid.C:434-1779)
+ *   pm_solve             TFgmresIte::Iterate (flexible)  (src/FE/FgmresIte.C:250-677)
+ *   pm_destroy           destructors
+ *
+ * All host pointers are plain C arrays in the reference's own layouts:
+ * solution/rhs vectors are [u1 | u2 | u3 | p] of length 3*N_U + N_P, CSR
+ * arrays are exactly those of TSquareMatrix3D / TMatrix3D.  The *_device
+ * variants take device pointers (cudaMalloc'd, same layout) and run without
+ * any host<->device copy of the vectors.
+ *
+ * Errors are returned as pm_status; nothing in the library calls exit().
+ * A handle is not thread-safe; it owns one CUDA stream.
+ */
+#ifndef PMGPU_H
+#define PMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PM_OK = 0,
+  PM_MAXIT = 1,        /* FGMRES stopped at maxit without meeting the test   */
+  PM_DIVERGED = 2,     /* res > SC_DIV_FACTOR * res0 (reference: exit(4711)) */
+  PM_NAN = 3,          /* non-finite residual                                */
+  PM_TIMEOUT = 4,      /* a bounded device wait ran out                      */
+  PM_OOM = 5,          /* device allocation failed                          */
+  PM_BADARG = 6,       /* invalid argument / unsupported configuration       */
+  PM_CUDA_ERROR = 7,   /* CUDA runtime error                                 */
+  PM_NOT_SETUP = 8,    /* pm_setup has not run (or failed)                   */
+  PM_NO_DEVICE = 9     /* no CUDA device / extension cannot run              */
+} pm_status;
+
+/* Precision of the V-cycle.  FGMRES, Arnoldi, Givens and the coarse direct
+ * solve are FP64 in both modes; the local LU factorisations are computed in
+ * FP64 (factor_fp32 = 0) and stored in the V-cycle precision. */
+enum { PM_PREC_FP64 = 0, PM_PREC_MIXED = 1 };
+
+typedef struct {
+  int precision;          /* PM_PREC_FP64 | PM_PREC_MIXED                          */
+  int factor_fp32;        /* 1: compute local LU in FP32 (mixed only); default 0   */
+  /* multigrid (TDatabase::ParamDB names) */
+  int pre_smooth;         /* SC_PRE_SMOOTH_SADDLE   (default 2)                    */
+  int post_smooth;        /* SC_POST_SMOOTH_SADDLE  (default 2)                    */
+  double smooth_damp;     /* SC_SMOOTH_DAMP_FACTOR_COARSE_SADDLE (default 1.0)     */
+  double alpha;           /* level relaxation al[0] (default 1.0)                 */
+  double beta;            /* SC_GMG_DAMP_FACTOR_SADDLE, level al[1] (default 1.0) */
+  int project_pressure;   /* INTERNAL_PROJECT_PRESSURE (default 1)                 */
+  /* FGMRES */
+  int restart;            /* SC_GMRES_RESTART                                      */
+  int maxit;              /* SC_LIN_MAXIT_SADDLE                                   */
+  int minit;              /* SC_MINIT                                              */
+  double red_factor;      /* SC_LIN_RED_FACTOR_SADDLE (relative to res0 of the current restart cycle) */
+  double res_norm_min;    /* SC_LIN_RES_NORM_MIN_SADDLE (absolute)                  */
+  double div_factor;      /* SC_DIV_FACTOR                                          */
+  /* runtime */
+  int device;             /* CUDA device ordinal                                    */
+  int use_graphs;         /* capture the V-cycle in a CUDA graph (default 1)        */
+  int verbose;
+} pm_options;
+
+/* One multigrid level in the reference's data layout.  Levels are added
+ * coarsest first, as TNSE_MultiGrid::AddLevel is called in
+ * TSystemNSE3D::Init (src/System/SystemNSE3D.C:806-876). */
+typedef struct {
+  int n_udof;            /* N_U: scalar velocity DOFs (rows of A11)             */
+  int n_pdof;            /* N_P: pressure DOFs                                   */
+  int n_active;          /* N_Active = USpace->GetActiveBound()                  */
+  int hanging_bound;     /* HangingNodeBound (== n_active: no hanging nodes)     */
+  int n_dirichlet;       /* N_Dirichlet                                          */
+  /* velocity blocks: shared pattern (ARowPtr/AKCol, sorted columns) */
+  int a_nnz;
+  const int *a_rowptr;   /* n_udof+1 */
+  const int *a_col;      /* a_nnz    */
+  const double *a[9];    /* A11,A12,A13,A21,A22,A23,A31,A32,A33 entries */
+  /* B blocks: N_P x N_U */
+  int b_nnz;
+  const int *b_rowptr;   /* n_pdof+1 */
+  const int *b_col;
+  const double *b[3];
+  /* BT blocks: N_U x N_P */
+  int bt_nnz;
+  const int *bt_rowptr;  /* n_udof+1 */
+  const int *bt_col;
+  const double *bt[3];
+  /* cells: local DOF maps (UGlobalNumbers+UBeginIndex[c], PGlobalNumbers+PBeginIndex[c]) */
+  int n_cells;
+  int n_ulocal;          /* 27 for Q2 hexahedra */
+  int n_plocal;          /* 4 for P1disc        */
+  const int *cell_udofs; /* n_cells*n_ulocal    */
+  const int *cell_pdofs; /* n_cells*n_plocal    */
+  /* grid hierarchy (ignored on the coarsest level): parent cell on the next
+   * coarser level and child number 0..7 with offset (c&1, (c>>1)&1, (c>>2)&1)
+   * in the parent's reference coordinates (regular hexahedral refinement). */
+  const int *cell_parent;
+  const int *cell_child;
+  /* optional cell colouring (no two cells of a colour share a DOF); NULL: the
+   * library colours greedily, as TParFEMapper3D::colorCell does. */
+  const int *cell_colour;
+} pm_level_desc;
+
+typedef struct {
+  int iterations;        /* FGMRES iterations (return value of Iterate)          */
+  double res0;           /* ||b - K x0||                                         */
+  double res;            /* final ||b - K x|| estimate (|s[i+1]| or true at restart) */
+  double true_res;       /* ||b - K x|| recomputed at exit (FP64)                */
+  double setup_ms;       /* factorisation time of the last pm_setup / refactor   */
+  double solve_ms;       /* device time of the FGMRES solve                      */
+  int vcycles;           /* preconditioner applications                          */
+  int status;            /* pm_status of the solve                               */
+} pm_result;
+
+typedef struct pm_handle pm_handle;
+
+void        pm_default_options(pm_options *opt);
+const char *pm_status_string(int status);
+const char *pm_last_error(pm_handle *h);
+int         pm_device_count(void);
+
+pm_status pm_create(pm_handle **h, const pm_options *opt);
+pm_status pm_add_level(pm_handle *h, const pm_level_desc *lvl);
+/* Uploads every level, colours, factors the local blocks and the coarse
+ * system.  Host arrays of the level descriptors are read here and may be
+ * freed afterwards. */
+pm_status pm_setup(pm_handle *h);
+/* Replace the matrix values of every level (same patterns) and refactor. */
+pm_status pm_update_matrices(pm_handle *h, const pm_level_desc *levels, int n_levels);
+pm_status pm_destroy(pm_handle *h);
+int       pm_n_levels(pm_handle *h);
+int       pm_level_ndof(pm_handle *h, int level);
+
+/* Level operators (FP64 on host vectors of length ndof(level)). */
+pm_status pm_coupled_defect(pm_handle *h, int level, const double *x, const double *b,
+                            double *r, int project_pressure);
+pm_status pm_defect(pm_handle *h, int level, const double *u, const double *f,
+                    double *d, double *res);
+pm_status pm_matvec(pm_handle *h, int level, const double *x, double *y);
+/* `sweeps` cell-Vanka sweeps on `level` in the handle's V-cycle precision. */
+pm_status pm_cell_vanka(pm_handle *h, int level, double *u, const double *rhs, int sweeps);
+/* Coarse rhs of level-1 from the fine defect of `level` (u and p parts). */
+pm_status pm_restrict(pm_handle *h, int level, const double *fine, double *coarse);
+/* Fine correction on `level` from a coarse vector of level-1. */
+pm_status pm_prolongate(pm_handle *h, int level, const double *coarse, double *fine);
+pm_status pm_solve_exact(pm_handle *h, const double *rhs, double *u);
+
+/* One preconditioner application z = V-cycle(v) on the finest level. */
+pm_status pm_vcycle(pm_handle *h, double *z, const double *v);
+/* FGMRES(restart) + V-cycle to the tolerances in the options.
+ * sol holds the initial guess on entry, the solution on exit. */
+pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out);
+/* Same with device pointers (no vector copies); the matrices must be set up. */
+pm_status pm_solve_device(pm_handle *h, double *d_sol, const double *d_rhs, pm_result *out);
+/* Re-run the local-block and coarse factorisations on the device (timed into
+ * out->setup_ms); used to time factor+solve with inputs resident in HBM. */
+pm_status pm_refactor(pm_handle *h, double *ms);
+
+/* Diagnostics: launches of this library's kernels since the handle was
+ * created, and device bytes held. */
+long long pm_kernel_launches(pm_handle *h);
+long long pm_device_bytes(pm_handle *h);
+/* Average duration (ms) of the Vanka residual/solve kernel over the last
+ * pm_solve (CUDA events on the handle's stream; 0 when not recorded). */
+pm_status pm_profile_enable(pm_handle *h, int enable);
+pm_status pm_profile_read(pm_handle *h, double *vanka_ms_total, long long *vanka_launches,
+                          double *vanka_bytes_total);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMGPU_H */

@@ -1,0 +1,60 @@
+"""CPU tests of the boundary: libpmgpu.so builds for sm_103a, loads, and
+exports every entry point include/pmgpu.h declares (no compute calls)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "pmgpu.h").read_text()
+    return sorted(set(re.findall(r"\b(pm_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_and_binding_agree():
+    from to_merge_master_parmoon_gb300._lib import GPU_SYMBOLS
+    assert declared_symbols() == sorted(GPU_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol():
+    from to_merge_master_parmoon_gb300._lib import gpu_lib
+    lib = gpu_lib()
+    for sym in declared_symbols():
+        assert hasattr(lib, sym), sym
+
+
+def test_library_is_built_for_sm_103a():
+    import subprocess
+    so = ROOT / "to_merge_master_parmoon_gb300" / "_build" / "libpmgpu.so"
+    assert so.exists()
+    out = subprocess.run(["cuobjdump", "--list-elf", str(so)], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_options_defaults_mirror_reference_database():
+    """Defaults of pm_default_options are the TDatabase::ParamDB defaults
+    (src/General/Database.C:640-871) that the path uses."""
+    from to_merge_master_parmoon_gb300._lib import PmOptions, gpu_lib
+    o = PmOptions()
+    gpu_lib().pm_default_options(C.byref(o))
+    assert (o.pre_smooth, o.post_smooth) == (2, 2)
+    assert o.smooth_damp == 1.0 and o.beta == 1.0 and o.alpha == 1.0
+    assert o.red_factor == 0.0 and o.res_norm_min == 1e-10 and o.div_factor == 1e10
+    assert o.project_pressure == 1
+
+
+def test_no_device_is_reported_not_faked(monkeypatch):
+    """Without a GPU the library refuses to create a handle (no CPU fallback)."""
+    from to_merge_master_parmoon_gb300._lib import gpu_lib
+    lib = gpu_lib()
+    if lib.pm_device_count() > 0:
+        pytest.skip("a GPU is present")
+    from to_merge_master_parmoon_gb300 import PmError, PmSolver
+    with pytest.raises(PmError) as e:
+        PmSolver()
+    assert e.value.status == 9  # PM_NO_DEVICE

@@ -1,0 +1,1048 @@
+// pm_api.cu — host side of libpmgpu: the C ABI declared in include/pmgpu.h.
+//
+// Orchestrates, on one CUDA stream, the reference's solver path:
+//   TFgmresIte::Iterate (flexible, src/FE/FgmresIte.C:250-677)
+//     -> TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132)
+//        -> TNSE_MultiGrid::Cycle, V-cycle (src/FE/NSE_MultiGrid.C:434-1779)
+//           -> TNSE_MGLevel4 Defect / CorrectNodes / CellVanka / SolveExact
+// with every numerical step on the GPU.  The V-cycle is captured once into a
+// CUDA graph and replayed for every preconditioner application.  FGMRES keeps
+// its vectors, Arnoldi and Gram-Schmidt on the device; only the (restart+2)
+// Hessenberg entries of the current column travel to the host, where the
+// Givens rotations run exactly as in the reference.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pm_kernels.h"
+#include "pm_setup_host.h"
+#include "pmgpu.h"
+
+using namespace pm;
+
+namespace {
+
+struct CsrStore {
+  int rows = 0, cols = 0, nnz = 0;
+  int *rowptr = nullptr, *col = nullptr;
+  double *v64 = nullptr;
+  float *v32 = nullptr;
+  template <typename T>
+  DevCsr<T> view() const;
+};
+template <>
+DevCsr<double> CsrStore::view<double>() const {
+  return DevCsr<double>{rows, cols, rowptr, col, v64};
+}
+template <>
+DevCsr<float> CsrStore::view<float>() const {
+  return DevCsr<float>{rows, cols, rowptr, col, v32};
+}
+
+struct LevelDev {
+  int nu = 0, np = 0, ndof = 0, nact = 0, hb = 0, ndir = 0, ncells = 0;
+  int a_nnz = 0, b_nnz = 0, bt_nnz = 0;
+  std::vector<int> h_udofs, h_pdofs, h_parent, h_child, h_colour;
+  bool has_colour = false;
+  int *a_rowptr = nullptr, *a_col = nullptr, *b_rowptr = nullptr, *b_col = nullptr;
+  int *bt_rowptr = nullptr, *bt_col = nullptr;
+  double *a64[9] = {}, *b64[3] = {}, *bt64[3] = {};
+  float *a32[9] = {}, *b32[3] = {}, *bt32[3] = {};
+  int *udofs = nullptr, *pdofs = nullptr;
+  Colouring colouring;
+  int *colour_cells = nullptr;
+  void *factors = nullptr;
+  uint8_t *perm = nullptr;
+  CsrStore Pu, Ru, Pp, Rp;
+  void *sol = nullptr, *rhs = nullptr, *def = nullptr, *uold = nullptr, *dbuf = nullptr;
+  double *x64 = nullptr, *y64 = nullptr, *z64 = nullptr;
+  // unique bytes of one Vanka sweep per cell: matrix (values + indices +
+  // row pointers) once, u read+write and rhs read, stored factors and
+  // permutation, divided by the number of cells
+  double vanka_unit_bytes = 0.0;
+
+  template <typename T>
+  DevOp<T> op() const;
+  DevCells cells() const { return DevCells{ncells, udofs, pdofs}; }
+};
+template <>
+DevOp<double> LevelDev::op<double>() const {
+  DevOp<double> o;
+  o.nu = nu;
+  o.np = np;
+  o.nact = nact;
+  o.a_rowptr = a_rowptr;
+  o.a_col = a_col;
+  for (int k = 0; k < 9; ++k) o.a[k] = a64[k];
+  o.b_rowptr = b_rowptr;
+  o.b_col = b_col;
+  o.bt_rowptr = bt_rowptr;
+  o.bt_col = bt_col;
+  for (int k = 0; k < 3; ++k) {
+    o.b[k] = b64[k];
+    o.bt[k] = bt64[k];
+  }
+  return o;
+}
+template <>
+DevOp<float> LevelDev::op<float>() const {
+  DevOp<float> o;
+  o.nu = nu;
+  o.np = np;
+  o.nact = nact;
+  o.a_rowptr = a_rowptr;
+  o.a_col = a_col;
+  for (int k = 0; k < 9; ++k) o.a[k] = a32[k];
+  o.b_rowptr = b_rowptr;
+  o.b_col = b_col;
+  o.bt_rowptr = bt_rowptr;
+  o.bt_col = bt_col;
+  for (int k = 0; k < 3; ++k) {
+    o.b[k] = b32[k];
+    o.bt[k] = bt32[k];
+  }
+  return o;
+}
+
+}  // namespace
+
+struct pm_handle {
+  pm_options opt;
+  cudaStream_t stream = nullptr;
+  std::vector<LevelDev> L;
+  bool setup_done = false;
+  std::string err;
+  long long launches = 0;
+  long long bytes = 0;
+  std::vector<void *> allocs;
+  // reductions and scalars
+  double *partials = nullptr;
+  unsigned int *counter = nullptr;
+  double *hcol = nullptr;
+  double *ydev = nullptr;
+  int *status_d = nullptr;
+  // coarse direct solve
+  int coarse_n = 0;
+  double *coarse_lu = nullptr, *coarse_b = nullptr, *coarse_x = nullptr;
+  int *coarse_ipiv = nullptr;
+  // FGMRES storage
+  int restart = 0;
+  double *V = nullptr, *Z = nullptr, *w = nullptr, *xd = nullptr, *bd = nullptr;
+  // V-cycle graph
+  cudaGraphExec_t vgraph = nullptr;
+  long long vgraph_kernels = 0;
+  // profiling of the Vanka solve kernel
+  bool prof = false;
+  std::vector<cudaEvent_t> evpool;
+  size_t evused = 0;
+  std::vector<double> prof_bytes;
+  double vanka_ms = 0.0, vanka_bytes = 0.0;
+  long long vanka_launches = 0;
+  double last_factor_ms = 0.0;
+};
+
+namespace {
+
+pm_status fail(pm_handle *h, pm_status s, const std::string &msg) {
+  if (h) h->err = msg;
+  return s;
+}
+
+pm_status cuda_fail(pm_handle *h, const char *what) {
+  cudaError_t e = cudaGetLastError();
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (h) h->err = m;
+  return (e == cudaErrorMemoryAllocation) ? PM_OOM : PM_CUDA_ERROR;
+}
+
+template <typename T>
+pm_status dalloc(pm_handle *h, T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    h->err = "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed: " +
+             cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? PM_OOM : PM_CUDA_ERROR;
+  }
+  h->allocs.push_back(q);
+  h->bytes += (long long)(count * sizeof(T));
+  *p = static_cast<T *>(q);
+  return PM_OK;
+}
+
+template <typename T>
+pm_status upload(pm_handle *h, T **dst, const T *src, size_t count) {
+  pm_status s = dalloc(h, dst, count);
+  if (s != PM_OK) return s;
+  if (count && cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice, h->stream) !=
+                   cudaSuccess)
+    return cuda_fail(h, "upload");
+  return PM_OK;
+}
+
+#define PM_TRY(expr)                  \
+  do {                                \
+    pm_status _s = (expr);            \
+    if (_s != PM_OK) return _s;       \
+  } while (0)
+
+#define PM_LAUNCH(expr)                                      \
+  do {                                                       \
+    int _n = (expr);                                         \
+    if (_n < 0) return cuda_fail(h, #expr);                  \
+    h->launches += _n;                                       \
+  } while (0)
+
+bool mixed(const pm_handle *h) { return h->opt.precision == PM_PREC_MIXED; }
+
+pm_status sync(pm_handle *h, const char *what) {
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return cuda_fail(h, what);
+  return PM_OK;
+}
+
+// ------------------------------------------------------------ level ops ---
+template <typename T>
+pm_status l20(pm_handle *h, T *p, int np) {
+  if (!h->opt.project_pressure) return PM_OK;
+  PM_LAUNCH(launch_l20_project<T>(p, np, h->partials, h->counter, h->stream));
+  return PM_OK;
+}
+
+// TNSE_MGLevel4::Defect: CoupledDefect, L2_0 of the pressure part, zero
+// non-active velocity rows.
+template <typename T>
+pm_status level_defect(pm_handle *h, const LevelDev &Lv, const T *u, const T *f, T *d) {
+  PM_LAUNCH(launch_coupled<T>(Lv.op<T>(), u, f, d, true, true, h->stream));
+  return l20<T>(h, d + 3 * Lv.nu, Lv.np);
+}
+
+template <typename T>
+pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
+  const T damp = (T)h->opt.smooth_damp;
+  const bool relax = std::fabs(1.0 - h->opt.alpha) > 1e-3;
+  PM_LAUNCH(launch_dirichlet<T>(u, rhs, Lv.nu, Lv.hb, Lv.ndir, h->stream));
+  if (relax &&
+      cudaMemcpyAsync(Lv.uold, u, sizeof(T) * Lv.ndof, cudaMemcpyDeviceToDevice, h->stream) !=
+          cudaSuccess)
+    return cuda_fail(h, "uold copy");
+  const DevOp<T> op = Lv.op<T>();
+  const DevCells cells = Lv.cells();
+  const int ncol = (int)Lv.colouring.ptr.size() - 1;
+  for (int k = 0; k < ncol; ++k) {
+    const int b = Lv.colouring.ptr[k], n = Lv.colouring.ptr[k + 1] - b;
+    if (n == 0) continue;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (h->prof && h->evused + 2 <= h->evpool.size()) {
+      e0 = h->evpool[h->evused];
+      e1 = h->evpool[h->evused + 1];
+      h->evused += 2;
+      cudaEventRecord(e0, h->stream);
+    }
+    PM_LAUNCH(launch_vanka_solve<T>(op, cells, Lv.colour_cells + b, n,
+                                    static_cast<const T *>(Lv.factors), Lv.perm, u, rhs,
+                                    static_cast<T *>(Lv.dbuf), h->stream));
+    if (e1) {
+      cudaEventRecord(e1, h->stream);
+      // algorithmic bytes of this launch: the level's unique Vanka-sweep
+      // bytes per cell times the cells of this colour
+      const double per_cell = Lv.vanka_unit_bytes;
+      h->prof_bytes.push_back(per_cell * n);
+    }
+    PM_LAUNCH(launch_vanka_update<T>(cells, Lv.nu, Lv.colour_cells + b, n,
+                                     static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
+  }
+  if (relax) PM_LAUNCH(launch_relax<T>(u, static_cast<const T *>(Lv.uold), (T)h->opt.alpha, Lv.ndof, h->stream));
+  PM_LAUNCH(launch_dirichlet<T>(u, rhs, Lv.nu, Lv.hb, Lv.ndir, h->stream));
+  return PM_OK;
+}
+
+template <typename T>
+pm_status coarse_solve(pm_handle *h, LevelDev &Lv, const T *rhs, T *u) {
+  const int pin = h->opt.project_pressure ? 3 * Lv.nu : -1;
+  if (sizeof(T) == sizeof(double)) {
+    PM_LAUNCH(launch_dense_solve(h->coarse_lu, h->coarse_ipiv, h->coarse_n,
+                                 reinterpret_cast<const double *>(rhs), reinterpret_cast<double *>(u),
+                                 pin, h->stream));
+  } else {
+    PM_LAUNCH((launch_convert<double, T>(h->coarse_b, rhs, h->coarse_n, h->stream)));
+    PM_LAUNCH(launch_dense_solve(h->coarse_lu, h->coarse_ipiv, h->coarse_n, h->coarse_b,
+                                 h->coarse_x, pin, h->stream));
+    PM_LAUNCH((launch_convert<T, double>(u, h->coarse_x, h->coarse_n, h->stream)));
+  }
+  return PM_OK;
+}
+
+// TNSE_MultiGrid::Cycle (V-cycle, cell Vanka, coarse SolveExact)
+template <typename T>
+pm_status cycle(pm_handle *h, int i) {
+  LevelDev &C = h->L[i];
+  T *u = static_cast<T *>(C.sol), *f = static_cast<T *>(C.rhs);
+  // CorrectNodes + SetDirichletNodes
+  PM_LAUNCH(launch_dirichlet<T>(u, f, C.nu, C.hb, C.ndir, h->stream));
+  if (i == 0) return coarse_solve<T>(h, C, f, u);
+  LevelDev &K = h->L[i - 1];
+  T *d = static_cast<T *>(C.def);
+  T *cu = static_cast<T *>(K.sol), *cf = static_cast<T *>(K.rhs);
+  for (int s = 0; s < h->opt.pre_smooth; ++s) PM_TRY(vanka_sweep<T>(h, C, u, f));
+  PM_LAUNCH(launch_dirichlet<T>(u, (const T *)nullptr, C.nu, C.hb, C.ndir, h->stream));
+  PM_TRY(level_defect<T>(h, C, u, f, d));
+  // DefectRestriction (u and p) + CorrectDefect + Reset
+  PM_LAUNCH(launch_csr_apply<T>(C.Ru.view<T>(), 3, d, C.nu, cf, K.nu, h->stream));
+  PM_LAUNCH(launch_csr_apply<T>(C.Rp.view<T>(), 1, d + 3 * C.nu, C.np, cf + 3 * K.nu, K.np, h->stream));
+  PM_LAUNCH(launch_zero_nonactive<T>(cf, K.nu, K.nact, h->stream));
+  PM_TRY(l20<T>(h, cf + 3 * K.nu, K.np));
+  PM_LAUNCH(launch_fill<T>(cu, T(0), K.ndof, h->stream));
+  PM_TRY(cycle<T>(h, i - 1));
+  // Prolongate, CorrectNodes(defect), Update, CorrectNodes(u)
+  PM_LAUNCH(launch_csr_apply<T>(C.Pu.view<T>(), 3, cu, K.nu, d, C.nu, h->stream));
+  PM_LAUNCH(launch_csr_apply<T>(C.Pp.view<T>(), 1, cu + 3 * K.nu, K.np, d + 3 * C.nu, C.np, h->stream));
+  PM_LAUNCH(launch_dirichlet<T>(d, (const T *)nullptr, C.nu, C.hb, C.ndir, h->stream));
+  PM_LAUNCH(launch_axpy<T>(u, (T)h->opt.beta, d, C.ndof, h->stream));
+  PM_LAUNCH(launch_dirichlet<T>(u, (const T *)nullptr, C.nu, C.hb, C.ndir, h->stream));
+  for (int s = 0; s < h->opt.post_smooth; ++s) PM_TRY(vanka_sweep<T>(h, C, u, f));
+  return PM_OK;
+}
+
+// TMultiGridIte::Iterate body after rhs is in place: zero start,
+// SetDirichletNodes, one cycle.
+template <typename T>
+pm_status vcycle_core(pm_handle *h) {
+  LevelDev &F = h->L.back();
+  PM_LAUNCH(launch_fill<T>(static_cast<T *>(F.sol), T(0), F.ndof, h->stream));
+  PM_LAUNCH(launch_dirichlet<T>(static_cast<T *>(F.sol), static_cast<const T *>(F.rhs), F.nu, F.hb,
+                                F.ndir, h->stream));
+  return cycle<T>(h, (int)h->L.size() - 1);
+}
+
+pm_status run_vcycle_core(pm_handle *h) {
+  if (h->opt.use_graphs && !h->prof) {
+    if (!h->vgraph) {
+      cudaGraph_t g = nullptr;
+      const long long before = h->launches;
+      if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return cuda_fail(h, "begin capture");
+      pm_status s = mixed(h) ? vcycle_core<float>(h) : vcycle_core<double>(h);
+      cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+      if (s != PM_OK) {
+        if (g) cudaGraphDestroy(g);
+        return s;
+      }
+      if (e != cudaSuccess) return cuda_fail(h, "end capture");
+      h->vgraph_kernels = h->launches - before;
+      h->launches = before;
+      if (cudaGraphInstantiate(&h->vgraph, g, 0) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(h, "graph instantiate");
+      }
+      cudaGraphDestroy(g);
+    }
+    if (cudaGraphLaunch(h->vgraph, h->stream) != cudaSuccess) return cuda_fail(h, "graph launch");
+    h->launches += h->vgraph_kernels;
+    return PM_OK;
+  }
+  return mixed(h) ? vcycle_core<float>(h) : vcycle_core<double>(h);
+}
+
+// z = M v (FP64 in/out)
+pm_status precondition(pm_handle *h, double *z, const double *v) {
+  LevelDev &F = h->L.back();
+  if (mixed(h))
+    PM_LAUNCH((launch_convert<float, double>(static_cast<float *>(F.rhs), v, F.ndof, h->stream)));
+  else if (cudaMemcpyAsync(F.rhs, v, sizeof(double) * F.ndof, cudaMemcpyDeviceToDevice,
+                           h->stream) != cudaSuccess)
+    return cuda_fail(h, "rhs copy");
+  PM_TRY(run_vcycle_core(h));
+  if (mixed(h))
+    PM_LAUNCH((launch_convert<double, float>(z, static_cast<const float *>(F.sol), F.ndof, h->stream)));
+  else if (cudaMemcpyAsync(z, F.sol, sizeof(double) * F.ndof, cudaMemcpyDeviceToDevice,
+                           h->stream) != cudaSuccess)
+    return cuda_fail(h, "sol copy");
+  return PM_OK;
+}
+
+// Defect_NSE4 on the finest level in FP64
+pm_status defect_nse4(pm_handle *h, const double *x, const double *b, double *r) {
+  LevelDev &F = h->L.back();
+  PM_LAUNCH(launch_coupled<double>(F.op<double>(), x, b, r, true, false, h->stream));
+  return l20<double>(h, r + 3 * F.nu, F.np);
+}
+
+pm_status read_scalars(pm_handle *h, double *dst, const double *src, int n) {
+  if (cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream) !=
+      cudaSuccess)
+    return cuda_fail(h, "scalar read");
+  return sync(h, "scalar read");
+}
+
+pm_status norm2(pm_handle *h, const double *x, int n, double *out) {
+  PM_LAUNCH(launch_dot(x, x, n, h->partials, h->counter, h->hcol, h->stream));
+  PM_TRY(read_scalars(h, out, h->hcol, 1));
+  *out = std::sqrt(*out);
+  return PM_OK;
+}
+
+void gen_rot(double dx, double dy, double *cs, double *sn) {
+  if (dy == 0.0) {
+    *cs = 1.0;
+    *sn = 0.0;
+  } else if (std::fabs(dy) > std::fabs(dx)) {
+    double t = dx / dy;
+    *sn = 1.0 / std::sqrt(1.0 + t * t);
+    *cs = t * *sn;
+  } else {
+    double t = dy / dx;
+    *cs = 1.0 / std::sqrt(1.0 + t * t);
+    *sn = t * *cs;
+  }
+}
+void apply_rot(double *dx, double *dy, double cs, double sn) {
+  double t = cs * *dx + sn * *dy;
+  *dy = -sn * *dx + cs * *dy;
+  *dx = t;
+}
+
+// TFgmresIte::Iterate, flexible branch
+pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
+  LevelDev &F = h->L.back();
+  const int N = F.ndof;
+  int restart = h->opt.restart;
+  const int maxit = h->opt.maxit, minit = h->opt.minit;
+  if (restart > maxit) restart = maxit;
+  if (restart <= 0) restart = 10;
+  if (restart > h->restart) return fail(h, PM_BADARG, "restart larger than allocated");
+  const double red = h->opt.red_factor, resmin = h->opt.res_norm_min, divf = h->opt.div_factor;
+  std::vector<double> s(restart + 1), cs(restart + 1), sn(restart + 1), y(restart + 1);
+  std::vector<double> H((size_t)(restart + 1) * restart, 0.0), col(restart + 2);
+  auto hh = [&](int r, int c) -> double & { return H[(size_t)r * restart + c]; };
+  double *V = h->V, *Z = h->Z, *w = h->w;
+  auto v = [&](int k) { return V + (size_t)k * N; };
+  auto z = [&](int k) { return Z + (size_t)k * N; };
+  res->vcycles = 0;
+
+  PM_TRY(defect_nse4(h, x, b, v(0)));
+  double r0;
+  PM_TRY(norm2(h, v(0), N, &r0));
+  double resv = r0, res0 = r0, beta = r0;
+  res->res0 = r0;
+  if (!std::isfinite(r0)) {
+    res->res = r0;
+    return fail(h, PM_NAN, "non-finite initial residual");
+  }
+  int maxite = maxit;
+  if (beta <= resmin) {
+    if (minit == 0 || beta < 1e-20) {
+      res->iterations = 0;
+      res->res = resv;
+      return PM_OK;
+    }
+    maxite = minit;
+  }
+  int j = 1;
+  while (j <= maxite) {
+    PM_LAUNCH(launch_scale(v(0), 1.0 / beta, N, h->stream));
+    std::fill(s.begin(), s.end(), 0.0);
+    s[0] = beta;
+    int i;
+    for (i = 0; i < restart && j <= maxite; i++, j++) {
+      PM_TRY(precondition(h, z(i), v(i)));
+      res->vcycles++;
+      PM_LAUNCH(launch_coupled<double>(F.op<double>(), z(i), nullptr, w, false, false, h->stream));
+      // modified Gram-Schmidt, each step fused with the next dot product
+      PM_LAUNCH(launch_mgs_step(w, nullptr, nullptr, v(0), N, h->partials, h->counter, h->hcol,
+                                h->stream));
+      for (int k = 1; k <= i; ++k)
+        PM_LAUNCH(launch_mgs_step(w, v(k - 1), h->hcol + (k - 1), v(k), N, h->partials,
+                                  h->counter, h->hcol + k, h->stream));
+      PM_LAUNCH(launch_mgs_step(w, v(i), h->hcol + i, nullptr, N, h->partials, h->counter,
+                                h->hcol + i + 1, h->stream));
+      PM_LAUNCH(launch_scale_copy(v(i + 1), w, h->hcol + i + 1, N, h->stream));
+      PM_TRY(read_scalars(h, col.data(), h->hcol, i + 2));
+      for (int k = 0; k <= i + 1; ++k) hh(k, i) = col[k];
+      for (int k = 0; k <= i + 1; ++k)
+        if (!std::isfinite(col[k])) {
+          res->iterations = j;
+          res->res = col[k];
+          return fail(h, PM_NAN, "non-finite Arnoldi coefficient");
+        }
+      for (int k = 0; k < i; ++k) apply_rot(&hh(k, i), &hh(k + 1, i), cs[k], sn[k]);
+      gen_rot(hh(i, i), hh(i + 1, i), &cs[i], &sn[i]);
+      apply_rot(&hh(i, i), &hh(i + 1, i), cs[i], sn[i]);
+      apply_rot(&s[i], &s[i + 1], cs[i], sn[i]);
+      resv = std::fabs(s[i + 1]);
+      if (j >= minit && (resv < resmin || resv < red * res0)) {
+        for (int k = 0; k <= i; ++k) y[k] = s[k];
+        for (int r = i; r >= 0; --r) {
+          y[r] /= hh(r, r);
+          for (int q = r - 1; q >= 0; --q) y[q] -= hh(q, r) * y[r];
+        }
+        if (cudaMemcpyAsync(h->ydev, y.data(), sizeof(double) * (i + 1), cudaMemcpyHostToDevice,
+                            h->stream) != cudaSuccess)
+          return cuda_fail(h, "y upload");
+        PM_LAUNCH(launch_multi_axpy(x, Z, (size_t)N, h->ydev, i + 1, N, h->stream));
+        PM_TRY(sync(h, "fgmres final"));
+        res->iterations = j;
+        res->res = resv;
+        return PM_OK;
+      }
+      if (resv > divf * res0) {
+        res->iterations = j;
+        res->res = resv;
+        return fail(h, PM_DIVERGED, "FGMRES residual exceeded SC_DIV_FACTOR * res0");
+      }
+    }
+    // restart (src/FE/FgmresIte.C:574-590); only the i columns of this cycle
+    for (int k = 0; k < i; ++k) y[k] = s[k];
+    for (int r = i - 1; r >= 0; --r) {
+      y[r] /= hh(r, r);
+      for (int q = r - 1; q >= 0; --q) y[q] -= hh(q, r) * y[r];
+    }
+    if (cudaMemcpyAsync(h->ydev, y.data(), sizeof(double) * i, cudaMemcpyHostToDevice,
+                        h->stream) != cudaSuccess)
+      return cuda_fail(h, "y upload");
+    PM_LAUNCH(launch_multi_axpy(x, Z, (size_t)N, h->ydev, i, N, h->stream));
+    PM_TRY(defect_nse4(h, x, b, v(0)));
+    PM_TRY(norm2(h, v(0), N, &resv));
+    res0 = beta = resv;
+    if (!std::isfinite(resv)) return fail(h, PM_NAN, "non-finite residual at restart");
+  }
+  if (j > maxite) j = maxite;
+  res->iterations = j;
+  res->res = resv;
+  return PM_MAXIT;
+}
+
+// ------------------------------------------------------------- setup ------
+pm_status factor_all(pm_handle *h) {
+  if (cudaMemsetAsync(h->status_d, 0, sizeof(int), h->stream) != cudaSuccess)
+    return cuda_fail(h, "status reset");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, h->stream);
+  for (size_t l = 1; l < h->L.size(); ++l) {
+    LevelDev &Lv = h->L[l];
+    if (mixed(h))
+      PM_LAUNCH(launch_vanka_factor<float>(Lv.op<double>(), Lv.cells(), static_cast<float *>(Lv.factors),
+                                           Lv.perm, h->opt.factor_fp32 != 0, h->status_d, h->stream));
+    else
+      PM_LAUNCH(launch_vanka_factor<double>(Lv.op<double>(), Lv.cells(), static_cast<double *>(Lv.factors),
+                                            Lv.perm, false, h->status_d, h->stream));
+  }
+  LevelDev &C = h->L[0];
+  PM_LAUNCH(launch_coarse_assemble(C.op<double>(), h->coarse_lu, h->opt.project_pressure, h->stream));
+  PM_LAUNCH(launch_dense_lu(h->coarse_lu, h->coarse_n, h->coarse_ipiv, h->status_d, h->stream));
+  cudaEventRecord(e1, h->stream);
+  int st = 0;
+  if (cudaMemcpyAsync(&st, h->status_d, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    return cuda_fail(h, "status read");
+  PM_TRY(sync(h, "factorisation"));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  h->last_factor_ms = ms;
+  if (st & 1) return fail(h, PM_BADARG, "singular local Vanka block (zero pivot)");
+  if (st & 2) return fail(h, PM_BADARG, "singular coarse system (zero pivot)");
+  return PM_OK;
+}
+
+pm_status upload_values(pm_handle *h, LevelDev &Lv, const pm_level_desc *d, bool first) {
+  for (int k = 0; k < 9; ++k) {
+    if (!d->a[k]) return fail(h, PM_BADARG, "missing A block");
+    if (first) PM_TRY(dalloc(h, &Lv.a64[k], Lv.a_nnz));
+    if (cudaMemcpyAsync(Lv.a64[k], d->a[k], sizeof(double) * Lv.a_nnz, cudaMemcpyHostToDevice,
+                        h->stream) != cudaSuccess)
+      return cuda_fail(h, "A upload");
+  }
+  for (int k = 0; k < 3; ++k) {
+    if (!d->b[k] || !d->bt[k]) return fail(h, PM_BADARG, "missing B/BT block");
+    if (first) {
+      PM_TRY(dalloc(h, &Lv.b64[k], Lv.b_nnz));
+      PM_TRY(dalloc(h, &Lv.bt64[k], Lv.bt_nnz));
+    }
+    if (cudaMemcpyAsync(Lv.b64[k], d->b[k], sizeof(double) * Lv.b_nnz, cudaMemcpyHostToDevice,
+                        h->stream) != cudaSuccess ||
+        cudaMemcpyAsync(Lv.bt64[k], d->bt[k], sizeof(double) * Lv.bt_nnz, cudaMemcpyHostToDevice,
+                        h->stream) != cudaSuccess)
+      return cuda_fail(h, "B upload");
+  }
+  PM_LAUNCH(launch_zero_dirichlet_offdiag(Lv.a64, Lv.a_rowptr, Lv.nu, Lv.nact, h->stream));
+  if (mixed(h)) {
+    for (int k = 0; k < 9; ++k) {
+      if (first) PM_TRY(dalloc(h, &Lv.a32[k], Lv.a_nnz));
+      PM_LAUNCH((launch_convert<float, double>(Lv.a32[k], Lv.a64[k], Lv.a_nnz, h->stream)));
+    }
+    for (int k = 0; k < 3; ++k) {
+      if (first) {
+        PM_TRY(dalloc(h, &Lv.b32[k], Lv.b_nnz));
+        PM_TRY(dalloc(h, &Lv.bt32[k], Lv.bt_nnz));
+      }
+      PM_LAUNCH((launch_convert<float, double>(Lv.b32[k], Lv.b64[k], Lv.b_nnz, h->stream)));
+      PM_LAUNCH((launch_convert<float, double>(Lv.bt32[k], Lv.bt64[k], Lv.bt_nnz, h->stream)));
+    }
+  }
+  return PM_OK;
+}
+
+pm_status upload_csr(pm_handle *h, CsrStore &c, const HostCsr &m) {
+  c.rows = m.rows;
+  c.cols = m.cols;
+  c.nnz = (int)m.col.size();
+  PM_TRY(upload(h, &c.rowptr, m.rowptr.data(), m.rowptr.size()));
+  PM_TRY(upload(h, &c.col, m.col.data(), m.col.size()));
+  PM_TRY(upload(h, &c.v64, m.val.data(), m.val.size()));
+  if (mixed(h)) {
+    PM_TRY(dalloc(h, &c.v32, m.val.size()));
+    PM_LAUNCH((launch_convert<float, double>(c.v32, c.v64, c.nnz, h->stream)));
+  }
+  return PM_OK;
+}
+
+bool check_desc(pm_handle *h, const pm_level_desc *d) {
+  if (!d) return fail(h, PM_BADARG, "null level"), false;
+  if (d->n_udof <= 0 || d->n_pdof <= 0 || d->n_active < 0 || d->n_active > d->n_udof)
+    return fail(h, PM_BADARG, "bad level sizes"), false;
+  if (d->hanging_bound != d->n_active)
+    return fail(h, PM_BADARG, "hanging nodes are not supported (hanging_bound != n_active)"), false;
+  if (d->hanging_bound + d->n_dirichlet != d->n_udof)
+    return fail(h, PM_BADARG, "n_dirichlet inconsistent with n_udof"), false;
+  if (d->n_ulocal != NU_LOC || d->n_plocal != NP_LOC)
+    return fail(h, PM_BADARG, "only Q2/P1disc hexahedra (27+4 local DOFs) are supported"), false;
+  if (!d->a_rowptr || !d->a_col || !d->b_rowptr || !d->b_col || !d->bt_rowptr || !d->bt_col ||
+      !d->cell_udofs || !d->cell_pdofs)
+    return fail(h, PM_BADARG, "missing arrays"), false;
+  if (d->a_rowptr[d->n_udof] != d->a_nnz || d->b_rowptr[d->n_pdof] != d->b_nnz ||
+      d->bt_rowptr[d->n_udof] != d->bt_nnz)
+    return fail(h, PM_BADARG, "row pointer totals do not match nnz"), false;
+  return true;
+}
+
+}  // namespace
+
+// ===================================================================== ABI ==
+extern "C" {
+
+void pm_default_options(pm_options *o) {
+  std::memset(o, 0, sizeof(*o));
+  o->precision = PM_PREC_FP64;
+  o->factor_fp32 = 0;
+  o->pre_smooth = 2;
+  o->post_smooth = 2;
+  o->smooth_damp = 1.0;
+  o->alpha = 1.0;
+  o->beta = 1.0;
+  o->project_pressure = 1;
+  o->restart = 20;
+  o->maxit = 100;
+  o->minit = 0;
+  o->red_factor = 0.0;
+  o->res_norm_min = 1e-10;
+  o->div_factor = 1e10;
+  o->device = 0;
+  o->use_graphs = 1;
+  o->verbose = 0;
+}
+
+const char *pm_status_string(int s) {
+  switch (s) {
+    case PM_OK: return "ok";
+    case PM_MAXIT: return "maximum iterations reached";
+    case PM_DIVERGED: return "diverged";
+    case PM_NAN: return "non-finite residual";
+    case PM_TIMEOUT: return "device wait timed out";
+    case PM_OOM: return "out of device memory";
+    case PM_BADARG: return "bad argument";
+    case PM_CUDA_ERROR: return "CUDA error";
+    case PM_NOT_SETUP: return "not set up";
+    case PM_NO_DEVICE: return "no CUDA device";
+    default: return "unknown";
+  }
+}
+
+const char *pm_last_error(pm_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+int pm_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+pm_status pm_create(pm_handle **out, const pm_options *opt) {
+  if (!out) return PM_BADARG;
+  *out = nullptr;
+  pm_options o;
+  if (opt)
+    o = *opt;
+  else
+    pm_default_options(&o);
+  if (o.precision != PM_PREC_FP64 && o.precision != PM_PREC_MIXED) return PM_BADARG;
+  if (o.factor_fp32 && o.precision != PM_PREC_MIXED) return PM_BADARG;
+  if (o.pre_smooth < 0 || o.post_smooth < 0 || o.restart <= 0 || o.maxit <= 0) return PM_BADARG;
+  if (pm_device_count() <= 0) return PM_NO_DEVICE;
+  if (cudaSetDevice(o.device) != cudaSuccess) {
+    cudaGetLastError();
+    return PM_NO_DEVICE;
+  }
+  pm_handle *h = new pm_handle();
+  h->opt = o;
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return PM_CUDA_ERROR;
+  }
+  *out = h;
+  return PM_OK;
+}
+
+pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
+  if (!h) return PM_BADARG;
+  if (h->setup_done) return fail(h, PM_BADARG, "levels must be added before pm_setup");
+  if (!check_desc(h, d)) return PM_BADARG;
+  if (cudaSetDevice(h->opt.device) != cudaSuccess) return cuda_fail(h, "set device");
+  h->L.emplace_back();
+  LevelDev &Lv = h->L.back();
+  Lv.nu = d->n_udof;
+  Lv.np = d->n_pdof;
+  Lv.ndof = 3 * Lv.nu + Lv.np;
+  Lv.nact = d->n_active;
+  Lv.hb = d->hanging_bound;
+  Lv.ndir = d->n_dirichlet;
+  Lv.ncells = d->n_cells;
+  Lv.a_nnz = d->a_nnz;
+  Lv.b_nnz = d->b_nnz;
+  Lv.bt_nnz = d->bt_nnz;
+  Lv.h_udofs.assign(d->cell_udofs, d->cell_udofs + (size_t)Lv.ncells * NU_LOC);
+  Lv.h_pdofs.assign(d->cell_pdofs, d->cell_pdofs + (size_t)Lv.ncells * NP_LOC);
+  if (d->cell_parent && d->cell_child) {
+    Lv.h_parent.assign(d->cell_parent, d->cell_parent + Lv.ncells);
+    Lv.h_child.assign(d->cell_child, d->cell_child + Lv.ncells);
+  }
+  Lv.has_colour = d->cell_colour != nullptr;
+  if (Lv.has_colour) Lv.h_colour.assign(d->cell_colour, d->cell_colour + Lv.ncells);
+  PM_TRY(upload(h, &Lv.a_rowptr, d->a_rowptr, (size_t)Lv.nu + 1));
+  PM_TRY(upload(h, &Lv.a_col, d->a_col, (size_t)Lv.a_nnz));
+  PM_TRY(upload(h, &Lv.b_rowptr, d->b_rowptr, (size_t)Lv.np + 1));
+  PM_TRY(upload(h, &Lv.b_col, d->b_col, (size_t)Lv.b_nnz));
+  PM_TRY(upload(h, &Lv.bt_rowptr, d->bt_rowptr, (size_t)Lv.nu + 1));
+  PM_TRY(upload(h, &Lv.bt_col, d->bt_col, (size_t)Lv.bt_nnz));
+  PM_TRY(upload_values(h, Lv, d, true));
+  PM_TRY(upload(h, &Lv.udofs, Lv.h_udofs.data(), Lv.h_udofs.size()));
+  PM_TRY(upload(h, &Lv.pdofs, Lv.h_pdofs.data(), Lv.h_pdofs.size()));
+  return sync(h, "add level");
+}
+
+pm_status pm_setup(pm_handle *h) {
+  if (!h) return PM_BADARG;
+  if (h->L.empty()) return fail(h, PM_BADARG, "no levels");
+  if (h->setup_done) return fail(h, PM_BADARG, "pm_setup called twice");
+  const size_t es = mixed(h) ? sizeof(float) : sizeof(double);
+  // colouring, transfers, buffers
+  size_t maxcol = 0;
+  for (size_t l = 0; l < h->L.size(); ++l) {
+    LevelDev &Lv = h->L[l];
+    std::string err;
+    if (!make_colouring(Lv.ncells, NU_LOC, NP_LOC, Lv.h_udofs.data(), Lv.h_pdofs.data(), Lv.nu,
+                        Lv.np, Lv.has_colour ? Lv.h_colour.data() : nullptr, Lv.colouring, err))
+      return fail(h, PM_BADARG, "level " + std::to_string(l) + ": " + err);
+    PM_TRY(upload(h, &Lv.colour_cells, Lv.colouring.order.data(), Lv.colouring.order.size()));
+    maxcol = std::max(maxcol, (size_t)Lv.colouring.max_size);
+    if (l > 0) {
+      LevelDev &K = h->L[l - 1];
+      if (Lv.h_parent.empty()) return fail(h, PM_BADARG, "fine level without cell_parent/cell_child");
+      HostCsr Pu, Ru, Pp, Rp;
+      if (!build_transfers(K.ncells, K.h_udofs.data(), K.h_pdofs.data(), K.nu, K.np, Lv.ncells,
+                           Lv.h_udofs.data(), Lv.h_pdofs.data(), Lv.nu, Lv.np,
+                           Lv.h_parent.data(), Lv.h_child.data(), Pu, Ru, Pp, Rp, err))
+        return fail(h, PM_BADARG, "level " + std::to_string(l) + ": " + err);
+      PM_TRY(upload_csr(h, Lv.Pu, Pu));
+      PM_TRY(upload_csr(h, Lv.Ru, Ru));
+      PM_TRY(upload_csr(h, Lv.Pp, Pp));
+      PM_TRY(upload_csr(h, Lv.Rp, Rp));
+      // local factors (FP64 or FP32 storage) and permutations
+      PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
+                    (size_t)Lv.ncells * NLOC * NLOC * es));
+      PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * NLOC));
+      PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.dbuf),
+                    (size_t)Lv.colouring.max_size * NLOC * es));
+      if (std::fabs(1.0 - h->opt.alpha) > 1e-3)
+        PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.uold), (size_t)Lv.ndof * es));
+    }
+    {
+      const double sv = (double)es;
+      const double mat = 9.0 * sv * Lv.a_nnz + 4.0 * Lv.a_nnz + 4.0 * (Lv.nu + 1) +
+                         (3.0 * sv + 4.0) * ((double)Lv.b_nnz + Lv.bt_nnz) + 4.0 * (Lv.np + 1) +
+                         4.0 * (Lv.nu + 1);
+      const double total = mat + 3.0 * sv * Lv.ndof +
+                           (double)Lv.ncells * ((double)NLOC * NLOC * sv + NLOC);
+      Lv.vanka_unit_bytes = Lv.ncells > 0 ? total / Lv.ncells : 0.0;
+    }
+    PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.sol), (size_t)Lv.ndof * es));
+    PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.rhs), (size_t)Lv.ndof * es));
+    PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.def), (size_t)Lv.ndof * es));
+    PM_TRY(dalloc(h, &Lv.x64, (size_t)Lv.ndof));
+    PM_TRY(dalloc(h, &Lv.y64, (size_t)Lv.ndof));
+    PM_TRY(dalloc(h, &Lv.z64, (size_t)Lv.ndof));
+  }
+  (void)maxcol;
+  PM_TRY(dalloc(h, &h->partials, 8 * 152 + 64));
+  PM_TRY(dalloc(h, &h->counter, 4));
+  if (cudaMemsetAsync(h->counter, 0, 4 * sizeof(unsigned int), h->stream) != cudaSuccess)
+    return cuda_fail(h, "counter reset");
+  PM_TRY(dalloc(h, &h->status_d, 4));
+  h->restart = std::max(1, std::min(h->opt.restart, h->opt.maxit));
+  PM_TRY(dalloc(h, &h->hcol, (size_t)h->restart + 4));
+  PM_TRY(dalloc(h, &h->ydev, (size_t)h->restart + 4));
+  LevelDev &C = h->L[0];
+  h->coarse_n = C.ndof;
+  PM_TRY(dalloc(h, &h->coarse_lu, (size_t)C.ndof * C.ndof));
+  PM_TRY(dalloc(h, &h->coarse_ipiv, (size_t)C.ndof));
+  PM_TRY(dalloc(h, &h->coarse_b, (size_t)C.ndof));
+  PM_TRY(dalloc(h, &h->coarse_x, (size_t)C.ndof));
+  const size_t N = h->L.back().ndof;
+  PM_TRY(dalloc(h, &h->V, (size_t)(h->restart + 1) * N));
+  PM_TRY(dalloc(h, &h->Z, (size_t)(h->restart + 1) * N));
+  PM_TRY(dalloc(h, &h->w, N));
+  PM_TRY(dalloc(h, &h->xd, N));
+  PM_TRY(dalloc(h, &h->bd, N));
+  PM_TRY(factor_all(h));
+  h->setup_done = true;
+  return PM_OK;
+}
+
+pm_status pm_update_matrices(pm_handle *h, const pm_level_desc *levels, int n) {
+  if (!h || !levels) return PM_BADARG;
+  if (!h->setup_done) return PM_NOT_SETUP;
+  if (n != (int)h->L.size()) return fail(h, PM_BADARG, "level count mismatch");
+  for (int l = 0; l < n; ++l) {
+    LevelDev &Lv = h->L[l];
+    const pm_level_desc *d = &levels[l];
+    if (d->n_udof != Lv.nu || d->n_pdof != Lv.np || d->a_nnz != Lv.a_nnz || d->b_nnz != Lv.b_nnz ||
+        d->bt_nnz != Lv.bt_nnz)
+      return fail(h, PM_BADARG, "pattern changed");
+    PM_TRY(upload_values(h, Lv, d, false));
+  }
+  return factor_all(h);
+}
+
+pm_status pm_refactor(pm_handle *h, double *ms) {
+  if (!h) return PM_BADARG;
+  if (!h->setup_done) return PM_NOT_SETUP;
+  PM_TRY(factor_all(h));
+  if (ms) *ms = h->last_factor_ms;
+  return PM_OK;
+}
+
+pm_status pm_destroy(pm_handle *h) {
+  if (!h) return PM_OK;
+  cudaSetDevice(h->opt.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->vgraph) cudaGraphExecDestroy(h->vgraph);
+  for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
+  for (void *p : h->allocs) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return PM_OK;
+}
+
+int pm_n_levels(pm_handle *h) { return h ? (int)h->L.size() : 0; }
+int pm_level_ndof(pm_handle *h, int l) {
+  return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].ndof : -1;
+}
+
+#define PM_CHECK_LEVEL(h, level)                                           \
+  do {                                                                     \
+    if (!(h)) return PM_BADARG;                                            \
+    if (!(h)->setup_done) return PM_NOT_SETUP;                             \
+    if ((level) < 0 || (level) >= (int)(h)->L.size())                      \
+      return fail((h), PM_BADARG, "level out of range");                   \
+  } while (0)
+
+static pm_status h2d(pm_handle *h, double *d, const double *s, size_t n) {
+  if (cudaMemcpyAsync(d, s, n * sizeof(double), cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+    return cuda_fail(h, "H2D");
+  return PM_OK;
+}
+static pm_status d2h(pm_handle *h, double *d, const double *s, size_t n) {
+  if (cudaMemcpyAsync(d, s, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    return cuda_fail(h, "D2H");
+  return sync(h, "D2H");
+}
+
+pm_status pm_coupled_defect(pm_handle *h, int level, const double *x, const double *b, double *r,
+                            int project) {
+  PM_CHECK_LEVEL(h, level);
+  LevelDev &Lv = h->L[level];
+  PM_TRY(h2d(h, Lv.x64, x, Lv.ndof));
+  PM_TRY(h2d(h, Lv.y64, b, Lv.ndof));
+  PM_LAUNCH(launch_coupled<double>(Lv.op<double>(), Lv.x64, Lv.y64, Lv.z64, true, false, h->stream));
+  if (project) PM_LAUNCH(launch_l20_project<double>(Lv.z64 + 3 * Lv.nu, Lv.np, h->partials, h->counter, h->stream));
+  return d2h(h, r, Lv.z64, Lv.ndof);
+}
+
+pm_status pm_defect(pm_handle *h, int level, const double *u, const double *f, double *d,
+                    double *res) {
+  PM_CHECK_LEVEL(h, level);
+  LevelDev &Lv = h->L[level];
+  PM_TRY(h2d(h, Lv.x64, u, Lv.ndof));
+  PM_TRY(h2d(h, Lv.y64, f, Lv.ndof));
+  PM_TRY(level_defect<double>(h, Lv, Lv.x64, Lv.y64, Lv.z64));
+  if (res) {
+    double r;
+    PM_TRY(norm2(h, Lv.z64, Lv.ndof, &r));
+    *res = r;
+  }
+  return d2h(h, d, Lv.z64, Lv.ndof);
+}
+
+pm_status pm_matvec(pm_handle *h, int level, const double *x, double *y) {
+  PM_CHECK_LEVEL(h, level);
+  LevelDev &Lv = h->L[level];
+  PM_TRY(h2d(h, Lv.x64, x, Lv.ndof));
+  PM_LAUNCH(launch_coupled<double>(Lv.op<double>(), Lv.x64, nullptr, Lv.z64, false, false, h->stream));
+  return d2h(h, y, Lv.z64, Lv.ndof);
+}
+
+pm_status pm_cell_vanka(pm_handle *h, int level, double *u, const double *rhs, int sweeps) {
+  PM_CHECK_LEVEL(h, level);
+  if (level == 0) return fail(h, PM_BADARG, "the coarsest level is solved exactly");
+  LevelDev &Lv = h->L[level];
+  PM_TRY(h2d(h, Lv.x64, u, Lv.ndof));
+  PM_TRY(h2d(h, Lv.y64, rhs, Lv.ndof));
+  if (mixed(h)) {
+    float *uu = static_cast<float *>(Lv.sol), *ff = static_cast<float *>(Lv.rhs);
+    PM_LAUNCH((launch_convert<float, double>(uu, Lv.x64, Lv.ndof, h->stream)));
+    PM_LAUNCH((launch_convert<float, double>(ff, Lv.y64, Lv.ndof, h->stream)));
+    for (int s = 0; s < sweeps; ++s) PM_TRY(vanka_sweep<float>(h, Lv, uu, ff));
+    PM_LAUNCH((launch_convert<double, float>(Lv.x64, uu, Lv.ndof, h->stream)));
+  } else {
+    for (int s = 0; s < sweeps; ++s) PM_TRY(vanka_sweep<double>(h, Lv, Lv.x64, Lv.y64));
+  }
+  return d2h(h, u, Lv.x64, Lv.ndof);
+}
+
+pm_status pm_restrict(pm_handle *h, int level, const double *fine, double *coarse) {
+  PM_CHECK_LEVEL(h, level);
+  if (level == 0) return fail(h, PM_BADARG, "no coarser level");
+  LevelDev &Fl = h->L[level], &Cl = h->L[level - 1];
+  PM_TRY(h2d(h, Fl.x64, fine, Fl.ndof));
+  PM_LAUNCH(launch_csr_apply<double>(Fl.Ru.view<double>(), 3, Fl.x64, Fl.nu, Cl.z64, Cl.nu, h->stream));
+  PM_LAUNCH(launch_csr_apply<double>(Fl.Rp.view<double>(), 1, Fl.x64 + 3 * Fl.nu, Fl.np,
+                                     Cl.z64 + 3 * Cl.nu, Cl.np, h->stream));
+  return d2h(h, coarse, Cl.z64, Cl.ndof);
+}
+
+pm_status pm_prolongate(pm_handle *h, int level, const double *coarse, double *fine) {
+  PM_CHECK_LEVEL(h, level);
+  if (level == 0) return fail(h, PM_BADARG, "no coarser level");
+  LevelDev &Fl = h->L[level], &Cl = h->L[level - 1];
+  PM_TRY(h2d(h, Cl.x64, coarse, Cl.ndof));
+  PM_LAUNCH(launch_csr_apply<double>(Fl.Pu.view<double>(), 3, Cl.x64, Cl.nu, Fl.z64, Fl.nu, h->stream));
+  PM_LAUNCH(launch_csr_apply<double>(Fl.Pp.view<double>(), 1, Cl.x64 + 3 * Cl.nu, Cl.np,
+                                     Fl.z64 + 3 * Fl.nu, Fl.np, h->stream));
+  return d2h(h, fine, Fl.z64, Fl.ndof);
+}
+
+pm_status pm_solve_exact(pm_handle *h, const double *rhs, double *u) {
+  PM_CHECK_LEVEL(h, 0);
+  LevelDev &C = h->L[0];
+  PM_TRY(h2d(h, C.x64, rhs, C.ndof));
+  PM_LAUNCH(launch_dense_solve(h->coarse_lu, h->coarse_ipiv, h->coarse_n, C.x64, C.z64,
+                               h->opt.project_pressure ? 3 * C.nu : -1, h->stream));
+  return d2h(h, u, C.z64, C.ndof);
+}
+
+pm_status pm_vcycle(pm_handle *h, double *z, const double *v) {
+  PM_CHECK_LEVEL(h, 0);
+  LevelDev &F = h->L.back();
+  PM_TRY(h2d(h, h->bd, v, F.ndof));
+  PM_TRY(precondition(h, h->xd, h->bd));
+  return d2h(h, z, h->xd, F.ndof);
+}
+
+pm_status pm_solve_device(pm_handle *h, double *d_sol, const double *d_rhs, pm_result *out) {
+  PM_CHECK_LEVEL(h, 0);
+  pm_result r;
+  std::memset(&r, 0, sizeof(r));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  if (h->prof) {
+    h->evused = 0;
+    h->prof_bytes.clear();
+  }
+  cudaEventRecord(e0, h->stream);
+  pm_status st = fgmres(h, d_sol, d_rhs, &r);
+  cudaEventRecord(e1, h->stream);
+  if (st == PM_OK || st == PM_MAXIT) {
+    // true residual of the returned iterate (FP64)
+    pm_status s2 = defect_nse4(h, d_sol, d_rhs, h->w);
+    if (s2 == PM_OK) s2 = norm2(h, h->w, h->L.back().ndof, &r.true_res);
+    if (s2 != PM_OK) st = s2;
+  }
+  cudaStreamSynchronize(h->stream);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  r.solve_ms = ms;
+  r.setup_ms = h->last_factor_ms;
+  r.status = st;
+  if (h->prof) {
+    for (size_t k = 0; k + 1 < h->evused; k += 2) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, h->evpool[k], h->evpool[k + 1]);
+      h->vanka_ms += t;
+      h->vanka_launches++;
+      h->vanka_bytes += h->prof_bytes[k / 2];
+    }
+  }
+  if (out) *out = r;
+  return st;
+}
+
+pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out) {
+  PM_CHECK_LEVEL(h, 0);
+  LevelDev &F = h->L.back();
+  PM_TRY(h2d(h, h->xd, sol, F.ndof));
+  PM_TRY(h2d(h, h->bd, rhs, F.ndof));
+  pm_status st = pm_solve_device(h, h->xd, h->bd, out);
+  pm_status s2 = d2h(h, sol, h->xd, F.ndof);
+  return st != PM_OK ? st : s2;
+}
+
+long long pm_kernel_launches(pm_handle *h) { return h ? h->launches : 0; }
+long long pm_device_bytes(pm_handle *h) { return h ? h->bytes : 0; }
+
+pm_status pm_profile_enable(pm_handle *h, int enable) {
+  if (!h) return PM_BADARG;
+  h->prof = enable != 0;
+  h->vanka_ms = 0.0;
+  h->vanka_bytes = 0.0;
+  h->vanka_launches = 0;
+  if (h->prof && h->evpool.empty()) {
+    h->evpool.resize(1 << 15);
+    for (auto &e : h->evpool) cudaEventCreate(&e);
+  }
+  return PM_OK;
+}
+
+pm_status pm_profile_read(pm_handle *h, double *ms, long long *launches, double *bytes) {
+  if (!h) return PM_BADARG;
+  if (ms) *ms = h->vanka_ms;
+  if (launches) *launches = h->vanka_launches;
+  if (bytes) *bytes = h->vanka_bytes;
+  return PM_OK;
+}
+
+}  // extern "C"

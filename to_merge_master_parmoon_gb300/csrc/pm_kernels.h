@@ -1,0 +1,130 @@
+// pm_kernels.h — host-callable launchers of the sm_103a kernels of libpmgpu.
+// Every launcher enqueues on the given stream and returns the number of
+// kernels it launched (for the launch counter), or -1 on a launch error.
+#ifndef PM_KERNELS_H
+#define PM_KERNELS_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pm {
+
+constexpr int NU_LOC = 27;                 // Q2 local velocity nodes
+constexpr int NP_LOC = 4;                  // P1disc local pressure DOFs
+constexpr int NLOC = 3 * NU_LOC + NP_LOC;  // 85: local Vanka block size
+
+// One level's operator in precision T (device pointers).  The nine velocity
+// blocks share the CSR pattern; off-diagonal blocks are zero on Dirichlet rows
+// (the reference ignores them there, src/FE/MGComponents3D.C:3143-3162).
+template <typename T>
+struct DevOp {
+  int nu, np, nact;
+  const int *a_rowptr, *a_col;
+  const T *a[9];
+  const int *b_rowptr, *b_col;
+  const T *b[3];
+  const int *bt_rowptr, *bt_col;
+  const T *bt[3];
+};
+
+// Scalar CSR (transfer operators).
+template <typename T>
+struct DevCsr {
+  int rows, cols;
+  const int *rowptr, *col;
+  const T *val;
+};
+
+// Local-block data of one level for the Vanka kernels.
+struct DevCells {
+  int ncells;
+  const int *udofs;   // ncells x 27
+  const int *pdofs;   // ncells x 4
+};
+
+// ---------------------------------------------------------------- sparse ---
+// r = b - K x (defect = true) or y = K x; optionally zero non-active velocity
+// rows (TNSE_MGLevel4::Defect).
+template <typename T>
+int launch_coupled(const DevOp<T> &op, const T *x, const T *b, T *r, bool defect,
+                   bool zero_nonactive, cudaStream_t s);
+// y_c = M x_c for ncomp components stored with strides (x_stride, y_stride);
+// beta_accumulate: y += M x instead of y = M x.
+template <typename T>
+int launch_csr_apply(const DevCsr<T> &m, int ncomp, const T *x, int x_stride, T *y, int y_stride,
+                     cudaStream_t s);
+
+// ---------------------------------------------------------------- vectors ---
+// Deterministic sums: partial sums per block, reduced in fixed order by the
+// last block to finish (no waiting).  `counter` must be zero on entry and is
+// reset to zero by the last block.
+template <typename T>
+int launch_l20_project(T *p, int np, double *scratch, unsigned int *counter, cudaStream_t s);
+int launch_dot(const double *a, const double *b, int n, double *partials, unsigned int *counter,
+               double *result, cudaStream_t s);
+// w -= h[k_axpy]*v_axpy (if v_axpy), then result = <w, v_dot> (if v_dot) or
+// <w, w> (if v_dot == nullptr and norm == true).
+int launch_mgs_step(double *w, const double *v_axpy, const double *h_axpy, const double *v_dot,
+                    int n, double *partials, unsigned int *counter, double *result,
+                    cudaStream_t s);
+// v = w / *h (h read on device)
+int launch_scale_copy(double *v, const double *w, const double *h, int n, cudaStream_t s);
+int launch_scale(double *v, double alpha, int n, cudaStream_t s);
+// x += sum_{k<nk} y[k] * Z[k*ld + :]
+int launch_multi_axpy(double *x, const double *Z, size_t ld, const double *y, int nk, int n,
+                      cudaStream_t s);
+template <typename TD, typename TS>
+int launch_convert(TD *dst, const TS *src, int n, cudaStream_t s);
+template <typename T>
+int launch_fill(T *x, T v, int n, cudaStream_t s);
+template <typename T>
+int launch_axpy(T *y, T a, const T *x, int n, cudaStream_t s);
+// u[c*nu + hb + i] = src ? src[c*nu + hb + i] : 0 for the Dirichlet block of
+// the three velocity components.
+template <typename T>
+int launch_dirichlet(T *u, const T *src, int nu, int hb, int ndir, cudaStream_t s);
+// zero velocity rows >= nact of the three components
+template <typename T>
+int launch_zero_nonactive(T *v, int nu, int nact, cudaStream_t s);
+// u = uold + alpha (u - uold)
+template <typename T>
+int launch_relax(T *u, const T *uold, T alpha, int n, cudaStream_t s);
+// zero off-diagonal velocity blocks on rows >= nact
+int launch_zero_dirichlet_offdiag(double *const a[9], const int *rowptr, int nu, int nact,
+                                  cudaStream_t s);
+// non-finite check: flag[0] |= 1 if any entry is not finite
+int launch_check_finite(const double *x, int n, int *flag, cudaStream_t s);
+
+// ---------------------------------------------------------------- Vanka ----
+// Gather every cell's 85x85 block from the FP64 CSR, LU with partial
+// pivoting (FP64, or FP32 with factor_fp32), store the factors column-major
+// in TF with the reciprocal of U's diagonal on the diagonal, and the row
+// permutation as uint8 (row i of PA = row perm[i] of A).
+template <typename TF>
+int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *factors,
+                        uint8_t *perm, bool factor_fp32, int *status, cudaStream_t s);
+// For the ncol cells listed in cell_list: local residual (full rows) from the
+// current u, local solve with the stored factors, delta -> dbuf[slot*85 + i].
+template <typename T>
+int launch_vanka_solve(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
+                       const T *factors, const uint8_t *perm, const T *u, const T *rhs, T *dbuf,
+                       cudaStream_t s);
+// u[dofs of cell_list[slot]] += damp * dbuf[slot*85 + i]
+template <typename T>
+int launch_vanka_update(const DevCells &cells, int nu, const int *cell_list, int ncol,
+                        const T *dbuf, T damp, T *u, cudaStream_t s);
+
+// ----------------------------------------------------------------- coarse --
+// Dense column-major N x N coarse saddle matrix of SolveExact
+// (src/FE/NSE_MGLevel4.C:5728-5830) from the FP64 CSR.
+int launch_coarse_assemble(const DevOp<double> &op, double *dense, int project_pressure,
+                           cudaStream_t s);
+// In-place LU with partial pivoting (one CTA), ipiv as in dgetrf.
+int launch_dense_lu(double *a, int n, int *ipiv, int *status, cudaStream_t s);
+// x = A^{-1} b with the factors (one CTA); b[first_p] = 0 when project.
+int launch_dense_solve(const double *lu, const int *ipiv, int n, const double *b, double *x,
+                       int pin_row, cudaStream_t s);
+
+}  // namespace pm
+
+#endif

@@ -1,0 +1,45 @@
+// pm_setup_host.h — host-side setup algorithms of libpmgpu (run once per
+// pm_setup; no numerical results of the solve are computed here).
+#ifndef PM_SETUP_HOST_H
+#define PM_SETUP_HOST_H
+
+#include <string>
+#include <vector>
+
+namespace pm {
+
+struct HostCsr {
+  int rows = 0, cols = 0;
+  std::vector<int> rowptr, col;
+  std::vector<double> val;
+};
+
+// Cells grouped by colour: cells of colour k are order[ptr[k]..ptr[k+1]).
+struct Colouring {
+  std::vector<int> ptr, order;
+  int max_size = 0;
+};
+
+// Validate a caller-provided colouring (no velocity or pressure DOF shared
+// by two cells of one colour) or, if colour == nullptr, colour greedily in
+// cell order (smallest colour unused by any cell sharing a DOF), as
+// TParFEMapper3D::colorCell does (src/Parallel/ParFEMapper3D.C:750).
+bool make_colouring(int ncells, int nulocal, int nplocal, const int *udofs, const int *pdofs,
+                    int nu, int np, const int *colour, Colouring &out, std::string &err);
+
+// Prolongation from the coarse to the fine level, P[i][k] =
+// (1/m_i) sum over fine cells containing node i of QQ_child[i_loc][k_loc]
+// (Prolongate, src/FE/MGComponents3D.C:468-708, with the multiplicity
+// division of :692-707), for Q2 (velocity, continuous) and P1disc
+// (pressure).  Restriction is its transpose (DefectRestriction divides by the
+// same multiplicity before applying QQ^T, :1036-1235).
+bool build_transfers(int nc_cells, const int *c_udofs, const int *c_pdofs, int c_nu, int c_np,
+                     int nf_cells, const int *f_udofs, const int *f_pdofs, int f_nu, int f_np,
+                     const int *f_parent, const int *f_child, HostCsr &Pu, HostCsr &Ru,
+                     HostCsr &Pp, HostCsr &Rp, std::string &err);
+
+HostCsr transpose(const HostCsr &a);
+
+}  // namespace pm
+
+#endif

@@ -1,0 +1,142 @@
+"""Python view of the host-side Oseen problem builder (libpmhost.so).
+
+An :class:`OseenProblem` owns the multigrid hierarchy that ParMooN's
+TSystemNSE3D would hand to its saddle-point solver: per level the NSTYPE-4
+CSR matrices (A11..A33 on one pattern, B1..B3, B1T..B3T), the Q2/P1disc cell
+DOF maps and the parent/child relation; plus the finest-level right-hand side.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import PmhParams, PmLevelDesc, host_lib
+
+EXAMPLES = {"random": 0, "quadlin_stokes": 1, "quadlin_oseen": 2}
+
+
+class OseenProblem:
+    """Steady Oseen problem on a box with ``n_levels`` uniform refinements.
+
+    The coarsest level has ``(nx0, ny0, nz0)`` hexahedra; level ``l`` has
+    ``2**l`` times as many per direction.  ``example`` selects the seeded
+    random Oseen problem (divergence-free Fourier convection, smooth forcing,
+    u = 0 on the walls) or the known-answer polynomial solution of the
+    reference's Examples/NSE_3D/AnsatzQuadLin.h (Stokes, or Oseen with b := u).
+    """
+
+    def __init__(self, n_levels: int = 4, nu: float = 1e-2, seed: int = 0,
+                 example: str = "random", nx0: int = 2, ny0: int = 2, nz0: int = 2,
+                 box=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), n_modes: int = 8, nthreads: int = 0):
+        lib = host_lib()
+        p = PmhParams()
+        lib.pmh_default_params(C.byref(p))
+        p.nx0, p.ny0, p.nz0, p.n_levels = nx0, ny0, nz0, n_levels
+        p.x0, p.x1, p.y0, p.y1, p.z0, p.z1 = box
+        p.nu = nu
+        p.seed = seed
+        p.example = EXAMPLES[example]
+        p.n_modes = n_modes
+        p.nthreads = nthreads
+        self._lib = lib
+        self.params = p
+        self.nu = nu
+        self.example = example
+        self._h = lib.pmh_build(C.byref(p))
+        if not self._h:
+            raise ValueError("pmh_build rejected the parameters")
+        self.n_levels = lib.pmh_n_levels(self._h)
+        self._descs = (PmLevelDesc * self.n_levels)()
+        for level in range(self.n_levels):
+            lib.pmh_level_desc(self._h, level, C.byref(self._descs[level]))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.pmh_free(h)
+            self._h = None
+
+    @property
+    def descs(self):
+        """ctypes array of pm_level_desc, coarsest first (valid while self lives)."""
+        return self._descs
+
+    def desc(self, level: int) -> PmLevelDesc:
+        return self._descs[level]
+
+    def ndof(self, level: int = -1) -> int:
+        level = level % self.n_levels
+        return self._lib.pmh_ndof(self._h, level)
+
+    def rhs(self) -> np.ndarray:
+        n = self.ndof(-1)
+        return np.ctypeslib.as_array(self._lib.pmh_rhs(self._h), shape=(n,)).copy()
+
+    def exact(self):
+        ptr = self._lib.pmh_exact(self._h)
+        if not ptr:
+            return None
+        return np.ctypeslib.as_array(ptr, shape=(self.ndof(-1),)).copy()
+
+    def arrays(self, level: int) -> dict:
+        """Numpy views of one level's arrays (no copies)."""
+        d = self._descs[level % self.n_levels]
+
+        def iv(ptr, n):
+            return np.ctypeslib.as_array(ptr, shape=(n,)) if n > 0 and ptr else np.zeros(0, np.int32)
+
+        def dv(ptr, n):
+            return np.ctypeslib.as_array(ptr, shape=(n,))
+
+        out = {
+            "n_udof": d.n_udof, "n_pdof": d.n_pdof, "n_active": d.n_active,
+            "n_cells": d.n_cells,
+            "a_rowptr": iv(d.a_rowptr, d.n_udof + 1), "a_col": iv(d.a_col, d.a_nnz),
+            "a": [dv(d.a[k], d.a_nnz) for k in range(9)],
+            "b_rowptr": iv(d.b_rowptr, d.n_pdof + 1), "b_col": iv(d.b_col, d.b_nnz),
+            "b": [dv(d.b[k], d.b_nnz) for k in range(3)],
+            "bt_rowptr": iv(d.bt_rowptr, d.n_udof + 1), "bt_col": iv(d.bt_col, d.bt_nnz),
+            "bt": [dv(d.bt[k], d.bt_nnz) for k in range(3)],
+            "cell_udofs": iv(d.cell_udofs, 27 * d.n_cells).reshape(d.n_cells, 27),
+            "cell_pdofs": iv(d.cell_pdofs, 4 * d.n_cells).reshape(d.n_cells, 4),
+            "cell_colour": iv(d.cell_colour, d.n_cells),
+        }
+        if d.cell_parent:
+            out["cell_parent"] = iv(d.cell_parent, d.n_cells)
+            out["cell_child"] = iv(d.cell_child, d.n_cells)
+        return out
+
+    def scipy_matrix(self, level: int = -1):
+        """Assembled saddle-point matrix K of one level as scipy CSR, with the
+        reference's conventions (Dirichlet rows: diagonal blocks only; BT on
+        active rows only).  Test helper."""
+        import scipy.sparse as sp
+        a = self.arrays(level)
+        nu, np_, na = a["n_udof"], a["n_pdof"], a["n_active"]
+        rows = np.repeat(np.arange(nu), np.diff(a["a_rowptr"]))
+        cols = a["a_col"]
+        blocks = []
+        act = rows < na
+        for bi in range(3):
+            for bj in range(3):
+                v = a["a"][3 * bi + bj].copy()
+                if bi != bj:
+                    v[~act] = 0.0
+                blocks.append(sp.csr_matrix((v, (rows + bi * nu, cols + bj * nu)),
+                                            shape=(3 * nu + np_, 3 * nu + np_)))
+        brow = np.repeat(np.arange(np_), np.diff(a["b_rowptr"]))
+        for k in range(3):
+            blocks.append(sp.csr_matrix((a["b"][k], (brow + 3 * nu, a["b_col"] + k * nu)),
+                                        shape=(3 * nu + np_, 3 * nu + np_)))
+        btrow = np.repeat(np.arange(nu), np.diff(a["bt_rowptr"]))
+        bact = btrow < na
+        for k in range(3):
+            v = a["bt"][k].copy()
+            v[~bact] = 0.0
+            blocks.append(sp.csr_matrix((v, (btrow + k * nu, a["bt_col"] + 3 * nu)),
+                                        shape=(3 * nu + np_, 3 * nu + np_)))
+        K = blocks[0]
+        for b in blocks[1:]:
+            K = K + b
+        return K.tocsr()

@@ -1,0 +1,191 @@
+"""Python handle on libpmgpu (include/pmgpu.h).
+
+``PmSolver`` mirrors the objects the reference builds for
+SC_SOLVER_SADDLE=16 / SC_PRECONDITIONER_SADDLE=5 / SC_SMOOTHER_SADDLE=2:
+``add_level`` is TNSE_MultiGrid::AddLevel, ``defect`` TNSE_MGLevel4::Defect,
+``coupled_defect`` Defect_NSE4, ``matvec`` MatVect_NSE4, ``cell_vanka``
+TNSE_MGLevel4::CellVanka, ``restrict``/``prolongate`` DefectRestriction /
+Prolongate, ``solve_exact`` TNSE_MGLevel4::SolveExact, ``vcycle``
+TMultiGridIte::Iterate and ``iterate`` TFgmresIte::Iterate.  Every call goes
+through the C ABI into CUDA kernels; a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import PM_STATUS, PmOptions, PmResult, gpu_lib
+
+OPTION_NAMES = [f for f, _ in PmOptions._fields_]
+
+
+class PmError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{PM_STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class PmSolver:
+    def __init__(self, levels=None, **options):
+        self._lib = gpu_lib()
+        opt = PmOptions()
+        self._lib.pm_default_options(C.byref(opt))
+        for k, v in options.items():
+            if k == "precision" and isinstance(v, str):
+                v = {"fp64": 0, "mixed": 1}[v]
+            if k not in OPTION_NAMES:
+                raise KeyError(f"unknown option {k}")
+            setattr(opt, k, v)
+        self.options = opt
+        h = C.c_void_p()
+        st = self._lib.pm_create(C.byref(h), C.byref(opt))
+        if st != 0:
+            raise PmError(st, "pm_create failed")
+        self._h = h
+        self._ndof = []
+        if levels is not None:
+            for d in levels:
+                self.add_level(d)
+            self.setup()
+
+    # ---------------------------------------------------------------- admin
+    def _check(self, st: int, what: str) -> int:
+        if st not in (0,):
+            msg = self._lib.pm_last_error(self._h)
+            raise PmError(st, f"{what}: {msg.decode() if msg else ''}")
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def add_level(self, desc):
+        self._check(self._lib.pm_add_level(self._h, C.byref(desc)), "pm_add_level")
+        self._ndof.append(3 * desc.n_udof + desc.n_pdof)
+
+    def setup(self):
+        self._check(self._lib.pm_setup(self._h), "pm_setup")
+
+    def update_matrices(self, descs):
+        self._check(self._lib.pm_update_matrices(self._h, descs, len(descs)), "pm_update_matrices")
+
+    def refactor(self) -> float:
+        ms = C.c_double()
+        self._check(self._lib.pm_refactor(self._h, C.byref(ms)), "pm_refactor")
+        return ms.value
+
+    @property
+    def n_levels(self) -> int:
+        return self._lib.pm_n_levels(self._h)
+
+    def ndof(self, level: int = -1) -> int:
+        return self._ndof[level]
+
+    @property
+    def kernel_launches(self) -> int:
+        return self._lib.pm_kernel_launches(self._h)
+
+    @property
+    def device_bytes(self) -> int:
+        return self._lib.pm_device_bytes(self._h)
+
+    def profile(self, enable: bool = True):
+        self._check(self._lib.pm_profile_enable(self._h, int(enable)), "pm_profile_enable")
+
+    def profile_read(self) -> dict:
+        ms, n, b = C.c_double(), C.c_longlong(), C.c_double()
+        self._check(self._lib.pm_profile_read(self._h, C.byref(ms), C.byref(n), C.byref(b)),
+                    "pm_profile_read")
+        return {"vanka_ms": ms.value, "vanka_launches": n.value, "vanka_bytes": b.value}
+
+    # ------------------------------------------------------------ level ops
+    def coupled_defect(self, level, x, b, project=True):
+        x, b = _f64(x), _f64(b)
+        r = np.empty_like(x)
+        self._check(self._lib.pm_coupled_defect(self._h, level, _dp(x), _dp(b), _dp(r), int(project)),
+                    "pm_coupled_defect")
+        return r
+
+    def defect(self, level, u, f):
+        u, f = _f64(u), _f64(f)
+        d = np.empty_like(u)
+        res = C.c_double()
+        self._check(self._lib.pm_defect(self._h, level, _dp(u), _dp(f), _dp(d), C.byref(res)),
+                    "pm_defect")
+        return d, res.value
+
+    def matvec(self, level, x):
+        x = _f64(x)
+        y = np.empty_like(x)
+        self._check(self._lib.pm_matvec(self._h, level, _dp(x), _dp(y)), "pm_matvec")
+        return y
+
+    def cell_vanka(self, level, u, rhs, sweeps=1):
+        u = _f64(u).copy()
+        rhs = _f64(rhs)
+        self._check(self._lib.pm_cell_vanka(self._h, level, _dp(u), _dp(rhs), sweeps), "pm_cell_vanka")
+        return u
+
+    def restrict(self, level, fine):
+        fine = _f64(fine)
+        coarse = np.empty(self._ndof[level - 1])
+        self._check(self._lib.pm_restrict(self._h, level, _dp(fine), _dp(coarse)), "pm_restrict")
+        return coarse
+
+    def prolongate(self, level, coarse):
+        coarse = _f64(coarse)
+        fine = np.empty(self._ndof[level])
+        self._check(self._lib.pm_prolongate(self._h, level, _dp(coarse), _dp(fine)), "pm_prolongate")
+        return fine
+
+    def solve_exact(self, rhs):
+        rhs = _f64(rhs)
+        u = np.empty_like(rhs)
+        self._check(self._lib.pm_solve_exact(self._h, _dp(rhs), _dp(u)), "pm_solve_exact")
+        return u
+
+    def vcycle(self, v):
+        v = _f64(v)
+        z = np.empty_like(v)
+        self._check(self._lib.pm_vcycle(self._h, _dp(z), _dp(v)), "pm_vcycle")
+        return z
+
+    # ---------------------------------------------------------------- solve
+    def iterate(self, sol, rhs, allow=(0,)):
+        """TFgmresIte::Iterate on host vectors; returns (solution, result dict)."""
+        sol = _f64(sol).copy()
+        rhs = _f64(rhs)
+        r = PmResult()
+        st = self._lib.pm_solve(self._h, _dp(sol), _dp(rhs), C.byref(r))
+        if st not in allow:
+            self._check(st, "pm_solve")
+        out = r.as_dict()
+        out["status_name"] = PM_STATUS.get(st, str(st))
+        return sol, out
+
+    def iterate_device(self, d_sol_ptr: int, d_rhs_ptr: int, allow=(0,)):
+        """TFgmresIte::Iterate on device vectors (raw CUDA pointers)."""
+        r = PmResult()
+        st = self._lib.pm_solve_device(self._h, C.c_void_p(d_sol_ptr), C.c_void_p(d_rhs_ptr), C.byref(r))
+        if st not in allow:
+            self._check(st, "pm_solve_device")
+        out = r.as_dict()
+        out["status_name"] = PM_STATUS.get(st, str(st))
+        return out
+
+
+def device_count() -> int:
+    return gpu_lib().pm_device_count()
