@@ -1,0 +1,330 @@
+"""Benchmark: time-to-1e-8 relative residual of the 3D Oseen saddle-point
+solve (Q2/P1disc, 64^3 cells, 6 levels from 2^3, nu = 1e-2) on one GB300.
+
+One step = one complete linear solve with the matrices already resident in
+HBM: factor every local 85x85 Vanka block and the coarse system, then
+FGMRES(20) preconditioned by one V(2,2) cycle with cell Vanka until
+||b - K x|| <= 1e-8 ||b||.  ``value`` is the mean step time (CUDA events on
+the library's stream) of the mixed-precision path; the plain FP64 GPU path
+is timed beside it.  ``e2e`` times the same solve through the C ABI with
+host buffers: per step the matrix values are copied host->device
+(pm_update_matrices), refactored, and the rhs/solution travel through
+pm_solve.
+
+``--impl reference`` times the CPU restatement of the reference solver
+(oracle/, FP64, every Vanka block refactored in every sweep as in
+src/FE/NSE_MGLevel4.C:1653-2087) on all host cores, on a bounded sample:
+one FGMRES iteration per step, scaled by the iteration count of the solve.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "3D Oseen time-to-1e-8 residual: mixed+learned vs plain FP64 GMG on one GB300"
+RTOL = 1e-8
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--levels", type=int, default=6)
+    ap.add_argument("--nu", type=float, default=1e-2)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the Vanka solve kernel from the committed ncu
+    summary (profiles/vanka_solve_64cube.json), or None."""
+    p = ROOT / "profiles" / "vanka_solve_64cube.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get("dram_bytes_per_launch")
+        except ValueError:
+            return None
+    return None
+
+
+def cpu_baseline(P, iterations, levels, threads):
+    """Oracle (FP64, per-sweep refactorisation as the reference) on the host
+    cores: one FGMRES iteration at the full size, scaled by `iterations`."""
+    import numpy as np
+    from oracle.pyoracle import Oracle
+    b = P.rhs()
+    O = Oracle(P, restart=20, maxit=1, res_norm_min=0.0, nthreads=threads)
+    t = time.perf_counter()
+    O.iterate(np.zeros_like(b), b)
+    dt = time.perf_counter() - t
+    return dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle.pyoracle import Oracle
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    threads = os.cpu_count() or 1
+    P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed, nthreads=threads)
+    b = P.rhs()
+    O = Oracle(P, restart=20, maxit=1, res_norm_min=0.0, nthreads=threads)
+    iters = FGMRES_ITERATIONS.get((args.levels, args.nu), 10)
+    times = []
+    for s in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        O.iterate(np.zeros_like(b), b)
+        dt = time.perf_counter() - t
+        if s >= args.warmup:
+            times.append(dt)
+    per_it = sum(times) / len(times)
+    value = per_it * iters
+    n = args.levels
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_it * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded divergence-free Fourier convection, smooth forcing)",
+        "config": {"workload": f"steady 3D Oseen, Q2/P1disc, {2 ** n}^3 cells, {n} levels from 2^3, "
+                               f"nu={args.nu}, FGMRES(20)+V(2,2) cell Vanka, rtol 1e-8",
+                   "ndof": P.ndof(-1)},
+        "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                         "sample": f"one FGMRES iteration (V(2,2) + mat-vec + MGS) per step at "
+                                   f"the full size, x {iters} iterations to 1e-8"},
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# FGMRES iterations to 1e-8 of this workload (measured on the GPU FP64 path,
+# which runs the same algorithm as the reference; used to scale the CPU sample)
+FGMRES_ITERATIONS = {(6, 1e-2): 10, (5, 1e-2): 10, (4, 1e-2): 9}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_env()
+    import numpy as np
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+
+    threads = os.cpu_count() or 1
+    P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed + rank, nthreads=threads)
+    b = P.rhs()
+    n = P.ndof(-1)
+    d_b = torch.from_numpy(b).cuda()
+    d_x = torch.zeros(n, dtype=torch.float64, device="cuda")
+
+    # ||b - K 0|| with the pressure part projected (Defect_NSE4 of x0 = 0)
+    bp = b.copy()
+    nu3 = 3 * P.desc(args.levels - 1).n_udof
+    bp[nu3::4] -= bp[nu3::4].mean()
+    r0 = float(np.linalg.norm(bp))
+    solvers = {}
+    for prec in ("mixed", "fp64"):
+        solvers[prec] = PmSolver(P.descs, precision=prec, device=local, restart=20, maxit=200,
+                                 res_norm_min=RTOL * r0, pin_host=int(prec == "mixed"))
+
+    def step(S):
+        d_x.zero_()
+        torch.cuda.synchronize()
+        fms = S.refactor()
+        info = S.iterate_device(d_x.data_ptr(), d_b.data_ptr())
+        return fms, info
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    results = {}
+    for prec, S in solvers.items():
+        for _ in range(args.warmup):
+            step(S)
+        barrier()
+        profile = prec == "mixed"
+        if profile:
+            S.profile(True)
+        launches0 = S.kernel_launches
+        t_dev = []
+        iters = []
+        with Clocks(local) as clk:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                fms, info = step(S)
+                t_dev.append(fms + info["solve_ms"])
+                iters.append(info["iterations"])
+            barrier()
+            wall = time.perf_counter() - t0
+        results[prec] = {
+            "ms": sum(t_dev) / len(t_dev), "wall_ms": wall * 1e3 / args.steps,
+            "factor_ms": fms, "solve_ms": info["solve_ms"], "iterations": iters[-1],
+            "rel_res": info["true_res"] / info["res0"], "launches": S.kernel_launches - launches0,
+            "clocks": clk.summary(),
+        }
+        if profile:
+            results[prec]["profile"] = S.profile_read()
+            S.profile(False)
+
+    # reduce: max over ranks
+    ms = results["mixed"]["ms"]
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        S = solvers["mixed"]
+        x = np.zeros(n)
+        h2d = 0
+        for lv in range(P.n_levels):
+            d = P.desc(lv)
+            h2d += 8 * (9 * d.a_nnz + 3 * d.b_nnz + 3 * d.bt_nnz)
+        h2d += 16 * n
+        times = []
+        for s in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            S.update_matrices(P.descs)
+            xs, info = S.iterate(x, b)
+            times.append(time.perf_counter() - t)
+        times = times[args.warmup:]
+        e2e = {"value": sum(times) / len(times), "unit": "s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": 8 * n}
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    prof = results["mixed"].get("profile", {})
+    achieved = None
+    if prof.get("vanka_ms"):
+        achieved = prof["vanka_bytes"] / (prof["vanka_ms"] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(),
+            "kernel": "k_vanka_solve<float> (local residual + stored-LU apply, one colour)",
+            "peak_kind": peak_kind,
+            "avg_launch_ms": prof["vanka_ms"] / prof["vanka_launches"] if prof.get("vanka_launches") else None,
+            "bytes_per_launch": prof["vanka_bytes"] / prof["vanka_launches"] if prof.get("vanka_launches") else None}
+    cpu = None
+    if not args.no_cpu_baseline:
+        per_it = cpu_baseline(P, results["fp64"]["iterations"], args.levels, threads)
+        its = results["fp64"]["iterations"]
+        cpu = {"value": per_it * its, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"oracle: one FGMRES iteration (V(2,2) with per-sweep refactorisation, "
+                         f"mat-vec, MGS) at the full size = {per_it:.2f} s, x {its} iterations"}
+    nlev = args.levels
+    line = {
+        "metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded divergence-free Fourier convection, smooth forcing)",
+        "config": {"workload": f"steady 3D Oseen, Q2/P1disc, {2 ** nlev}^3 cells, {nlev} levels "
+                               f"from 2^3, nu={args.nu}, FGMRES(20)+V(2,2) cell Vanka, rtol 1e-8",
+                   "ndof": n, "precision": "mixed: FP32 V-cycle + FP32-stored FP64-computed "
+                                           "local LU, FP64 FGMRES/coarse",
+                   "l2": "inputs (11.7 GB of matrices) larger than L2", "parallelism": "replicas"},
+        "fp64": {"value": results["fp64"]["ms"] * 1e-3, "iterations": results["fp64"]["iterations"],
+                 "factor_ms": results["fp64"]["factor_ms"], "solve_ms": results["fp64"]["solve_ms"],
+                 "rel_res": results["fp64"]["rel_res"]},
+        "mixed": {k: results["mixed"][k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res", "wall_ms")},
+        "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": results["mixed"]["launches"],
+        "clocks": {k: results["mixed"]["clocks"][k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

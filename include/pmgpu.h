@@ -86,6 +86,11 @@ typedef struct {
   int device;             /* CUDA device ordinal                                    */
   int use_graphs;         /* capture the V-cycle in a CUDA graph (default 1)        */
   int verbose;
+  int pin_host;           /* 1: page-lock the caller's matrix value arrays in
+                             pm_add_level (cudaHostRegister, as the TNSE_MGLevel4
+                             ctor does, src/FE/NSE_MGLevel4.C:168-188) so that
+                             pm_update_matrices copies at full link speed; the
+                             arrays stay registered until pm_destroy          */
 } pm_options;
 
 /* One multigrid level in the reference's data layout.  Levels are added

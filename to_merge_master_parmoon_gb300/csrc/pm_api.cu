@@ -145,6 +145,7 @@ struct pm_handle {
   double vanka_ms = 0.0, vanka_bytes = 0.0;
   long long vanka_launches = 0;
   double last_factor_ms = 0.0;
+  std::vector<void *> pinned;
 };
 
 namespace {
@@ -650,6 +651,7 @@ void pm_default_options(pm_options *o) {
   o->device = 0;
   o->use_graphs = 1;
   o->verbose = 0;
+  o->pin_host = 0;
 }
 
 const char *pm_status_string(int s) {
@@ -736,6 +738,20 @@ pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
   PM_TRY(upload(h, &Lv.b_col, d->b_col, (size_t)Lv.b_nnz));
   PM_TRY(upload(h, &Lv.bt_rowptr, d->bt_rowptr, (size_t)Lv.nu + 1));
   PM_TRY(upload(h, &Lv.bt_col, d->bt_col, (size_t)Lv.bt_nnz));
+  if (h->opt.pin_host) {
+    auto pin = [h](const void *p, size_t bytes) {
+      if (!p || bytes < (1u << 20)) return;
+      if (cudaHostRegister(const_cast<void *>(p), bytes, cudaHostRegisterPortable) == cudaSuccess)
+        h->pinned.push_back(const_cast<void *>(p));
+      else
+        cudaGetLastError();  // already registered / not registrable: copy unpinned
+    };
+    for (int k = 0; k < 9; ++k) pin(d->a[k], sizeof(double) * (size_t)Lv.a_nnz);
+    for (int k = 0; k < 3; ++k) {
+      pin(d->b[k], sizeof(double) * (size_t)Lv.b_nnz);
+      pin(d->bt[k], sizeof(double) * (size_t)Lv.bt_nnz);
+    }
+  }
   PM_TRY(upload_values(h, Lv, d, true));
   PM_TRY(upload(h, &Lv.udofs, Lv.h_udofs.data(), Lv.h_udofs.size()));
   PM_TRY(upload(h, &Lv.pdofs, Lv.h_pdofs.data(), Lv.h_pdofs.size()));
@@ -850,6 +866,7 @@ pm_status pm_destroy(pm_handle *h) {
   if (h->vgraph) cudaGraphExecDestroy(h->vgraph);
   for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
   for (void *p : h->allocs) cudaFree(p);
+  for (void *p : h->pinned) cudaHostUnregister(p);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return PM_OK;
