@@ -285,15 +285,22 @@ def main():
         return
     peak, peak_kind = measured_peaks()
     prof = results["mixed"].get("profile", {})
-    achieved = None
-    if prof.get("vanka_ms"):
-        achieved = prof["vanka_bytes"] / (prof["vanka_ms"] * 1e-3) / 1e9
+
+    def kernel_roof(d):
+        if not d or not d.get("ms"):
+            return None, None, None
+        return (d["bytes"] / (d["ms"] * 1e-3) / 1e9, d["ms"] / d["launches"],
+                d["bytes"] / d["launches"])
+
+    achieved, avg_ms, per_launch = kernel_roof(prof.get("residual"))
+    a_ach, a_ms, a_bytes = kernel_roof(prof.get("apply"))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(),
-            "kernel": "k_vanka_solve<float> (local residual + stored-LU apply, one colour)",
-            "peak_kind": peak_kind,
-            "avg_launch_ms": prof["vanka_ms"] / prof["vanka_launches"] if prof.get("vanka_launches") else None,
-            "bytes_per_launch": prof["vanka_bytes"] / prof["vanka_launches"] if prof.get("vanka_launches") else None}
+            "kernel": "k_vanka_residual<float,4> (cell-local residuals over full CSR rows, one colour)",
+            "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "bytes_per_launch": per_launch,
+            "apply_kernel": {"name": "k_vanka_apply<float> (stored-LU solve + update)",
+                             "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,
+                             "avg_launch_ms": a_ms, "bytes_per_launch": a_bytes}}
     cpu = None
     if not args.no_cpu_baseline:
         per_it = cpu_baseline(P, results["fp64"]["iterations"], args.levels, threads)

@@ -192,11 +192,14 @@ pm_status pm_refactor(pm_handle *h, double *ms);
  * created, and device bytes held. */
 long long pm_kernel_launches(pm_handle *h);
 long long pm_device_bytes(pm_handle *h);
-/* Average duration (ms) of the Vanka residual/solve kernel over the last
- * pm_solve (CUDA events on the handle's stream; 0 when not recorded). */
+/* Per-kernel timing of the two Vanka sweep kernels while profiling is
+ * enabled: CUDA events on the handle's stream bracket every launch (the
+ * V-cycle then runs without graph capture).  kernel 0 = local residual,
+ * 1 = factor apply + update.  Totals since pm_profile_enable: device time
+ * (ms), launches and algorithmic (unique) bytes of those launches. */
 pm_status pm_profile_enable(pm_handle *h, int enable);
-pm_status pm_profile_read(pm_handle *h, double *vanka_ms_total, long long *vanka_launches,
-                          double *vanka_bytes_total);
+pm_status pm_profile_read(pm_handle *h, int kernel, double *ms_total, long long *launches,
+                          double *bytes_total);
 
 #ifdef __cplusplus
 }

@@ -94,7 +94,7 @@ GPU_SYMBOLS = {
     "pm_kernel_launches": (C.c_longlong, [_P]),
     "pm_device_bytes": (C.c_longlong, [_P]),
     "pm_profile_enable": (C.c_int, [_P, C.c_int]),
-    "pm_profile_read": (C.c_int, [_P, c_double_p, C.POINTER(C.c_longlong), c_double_p]),
+    "pm_profile_read": (C.c_int, [_P, C.c_int, c_double_p, C.POINTER(C.c_longlong), c_double_p]),
 }
 
 HOST_SYMBOLS = {

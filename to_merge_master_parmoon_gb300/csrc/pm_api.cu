@@ -62,10 +62,8 @@ struct LevelDev {
   CsrStore Pu, Ru, Pp, Rp;
   void *sol = nullptr, *rhs = nullptr, *def = nullptr, *uold = nullptr, *dbuf = nullptr;
   double *x64 = nullptr, *y64 = nullptr, *z64 = nullptr;
-  // unique bytes of one Vanka sweep per cell: matrix (values + indices +
-  // row pointers) once, u read+write and rhs read, stored factors and
-  // permutation, divided by the number of cells
-  double vanka_unit_bytes = 0.0;
+  // unique bytes of one Vanka sweep per cell, split by kernel (see pm_setup)
+  double vanka_res_bytes = 0.0, vanka_apply_bytes = 0.0;
 
   template <typename T>
   DevOp<T> op() const;
@@ -129,7 +127,7 @@ struct pm_handle {
   int *status_d = nullptr;
   // coarse direct solve
   int coarse_n = 0;
-  double *coarse_lu = nullptr, *coarse_b = nullptr, *coarse_x = nullptr;
+  double *coarse_lu = nullptr, *coarse_inv = nullptr, *coarse_b = nullptr, *coarse_x = nullptr;
   int *coarse_ipiv = nullptr;
   // FGMRES storage
   int restart = 0;
@@ -142,8 +140,9 @@ struct pm_handle {
   std::vector<cudaEvent_t> evpool;
   size_t evused = 0;
   std::vector<double> prof_bytes;
-  double vanka_ms = 0.0, vanka_bytes = 0.0;
-  long long vanka_launches = 0;
+  // [0] = k_vanka_residual, [1] = k_vanka_apply
+  double prof_ms[2] = {0.0, 0.0}, prof_sum_bytes[2] = {0.0, 0.0};
+  long long prof_launches[2] = {0, 0};
   double last_factor_ms = 0.0;
   std::vector<void *> pinned;
 };
@@ -241,25 +240,28 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
   for (int k = 0; k < ncol; ++k) {
     const int b = Lv.colouring.ptr[k], n = Lv.colouring.ptr[k + 1] - b;
     if (n == 0) continue;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (h->prof && h->evused + 2 <= h->evpool.size()) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    if (h->prof && h->evused + 3 <= h->evpool.size()) {
       e0 = h->evpool[h->evused];
       e1 = h->evpool[h->evused + 1];
-      h->evused += 2;
+      e2 = h->evpool[h->evused + 2];
+      h->evused += 3;
       cudaEventRecord(e0, h->stream);
     }
-    PM_LAUNCH(launch_vanka_solve<T>(op, cells, Lv.colour_cells + b, n,
-                                    static_cast<const T *>(Lv.factors), Lv.perm, u, rhs,
-                                    static_cast<T *>(Lv.dbuf), h->stream));
-    if (e1) {
-      cudaEventRecord(e1, h->stream);
-      // algorithmic bytes of this launch: the level's unique Vanka-sweep
-      // bytes per cell times the cells of this colour
-      const double per_cell = Lv.vanka_unit_bytes;
-      h->prof_bytes.push_back(per_cell * n);
+    PM_LAUNCH(launch_vanka_residual<T>(op, cells, Lv.colour_cells + b, n, u, rhs,
+                                       static_cast<T *>(Lv.dbuf), h->stream));
+    if (e1) cudaEventRecord(e1, h->stream);
+    PM_LAUNCH(launch_vanka_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
+                                    static_cast<const T *>(Lv.factors), Lv.perm,
+                                    static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
+    if (e2) {
+      cudaEventRecord(e2, h->stream);
+      // algorithmic bytes of this colour: the level's unique Vanka-sweep
+      // bytes per cell (split into the residual part and the factor part)
+      // times the cells of this colour
+      h->prof_bytes.push_back(Lv.vanka_res_bytes * n);
+      h->prof_bytes.push_back(Lv.vanka_apply_bytes * n);
     }
-    PM_LAUNCH(launch_vanka_update<T>(cells, Lv.nu, Lv.colour_cells + b, n,
-                                     static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
   }
   if (relax) PM_LAUNCH(launch_relax<T>(u, static_cast<const T *>(Lv.uold), (T)h->opt.alpha, Lv.ndof, h->stream));
   PM_LAUNCH(launch_dirichlet<T>(u, rhs, Lv.nu, Lv.hb, Lv.ndir, h->stream));
@@ -268,17 +270,9 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
 
 template <typename T>
 pm_status coarse_solve(pm_handle *h, LevelDev &Lv, const T *rhs, T *u) {
+  // SolveExact with the inverse of the (pinned) coarse matrix, FP64 arithmetic
   const int pin = h->opt.project_pressure ? 3 * Lv.nu : -1;
-  if (sizeof(T) == sizeof(double)) {
-    PM_LAUNCH(launch_dense_solve(h->coarse_lu, h->coarse_ipiv, h->coarse_n,
-                                 reinterpret_cast<const double *>(rhs), reinterpret_cast<double *>(u),
-                                 pin, h->stream));
-  } else {
-    PM_LAUNCH((launch_convert<double, T>(h->coarse_b, rhs, h->coarse_n, h->stream)));
-    PM_LAUNCH(launch_dense_solve(h->coarse_lu, h->coarse_ipiv, h->coarse_n, h->coarse_b,
-                                 h->coarse_x, pin, h->stream));
-    PM_LAUNCH((launch_convert<T, double>(u, h->coarse_x, h->coarse_n, h->stream)));
-  }
+  PM_LAUNCH((launch_dense_gemv<T, T>(h->coarse_inv, h->coarse_n, rhs, u, pin, h->stream)));
   return PM_OK;
 }
 
@@ -541,6 +535,7 @@ pm_status factor_all(pm_handle *h) {
   LevelDev &C = h->L[0];
   PM_LAUNCH(launch_coarse_assemble(C.op<double>(), h->coarse_lu, h->opt.project_pressure, h->stream));
   PM_LAUNCH(launch_dense_lu(h->coarse_lu, h->coarse_n, h->coarse_ipiv, h->status_d, h->stream));
+  PM_LAUNCH(launch_dense_inverse(h->coarse_lu, h->coarse_ipiv, h->coarse_n, h->coarse_inv, h->stream));
   cudaEventRecord(e1, h->stream);
   int st = 0;
   if (cudaMemcpyAsync(&st, h->status_d, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
@@ -790,18 +785,21 @@ pm_status pm_setup(pm_handle *h) {
                     (size_t)Lv.ncells * NLOC * NLOC * es));
       PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * NLOC));
       PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.dbuf),
-                    (size_t)Lv.colouring.max_size * NLOC * es));
+                    (size_t)Lv.colouring.max_size * kRStride * es));
       if (std::fabs(1.0 - h->opt.alpha) > 1e-3)
         PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.uold), (size_t)Lv.ndof * es));
     }
-    {
+    if (Lv.ncells > 0) {
+      // unique bytes of one sweep (each stored element counted once):
+      // residual kernel = matrix values + column indices + row pointers, u
+      // and rhs read; apply kernel = factors + permutation, u read+write
       const double sv = (double)es;
       const double mat = 9.0 * sv * Lv.a_nnz + 4.0 * Lv.a_nnz + 4.0 * (Lv.nu + 1) +
                          (3.0 * sv + 4.0) * ((double)Lv.b_nnz + Lv.bt_nnz) + 4.0 * (Lv.np + 1) +
                          4.0 * (Lv.nu + 1);
-      const double total = mat + 3.0 * sv * Lv.ndof +
-                           (double)Lv.ncells * ((double)NLOC * NLOC * sv + NLOC);
-      Lv.vanka_unit_bytes = Lv.ncells > 0 ? total / Lv.ncells : 0.0;
+      Lv.vanka_res_bytes = (mat + 2.0 * sv * Lv.ndof) / Lv.ncells;
+      Lv.vanka_apply_bytes =
+          ((double)Lv.ncells * ((double)NLOC * NLOC * sv + NLOC) + 2.0 * sv * Lv.ndof) / Lv.ncells;
     }
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.sol), (size_t)Lv.ndof * es));
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.rhs), (size_t)Lv.ndof * es));
@@ -822,6 +820,7 @@ pm_status pm_setup(pm_handle *h) {
   LevelDev &C = h->L[0];
   h->coarse_n = C.ndof;
   PM_TRY(dalloc(h, &h->coarse_lu, (size_t)C.ndof * C.ndof));
+  PM_TRY(dalloc(h, &h->coarse_inv, (size_t)C.ndof * C.ndof));
   PM_TRY(dalloc(h, &h->coarse_ipiv, (size_t)C.ndof));
   PM_TRY(dalloc(h, &h->coarse_b, (size_t)C.ndof));
   PM_TRY(dalloc(h, &h->coarse_x, (size_t)C.ndof));
@@ -1016,12 +1015,16 @@ pm_status pm_solve_device(pm_handle *h, double *d_sol, const double *d_rhs, pm_r
   r.setup_ms = h->last_factor_ms;
   r.status = st;
   if (h->prof) {
-    for (size_t k = 0; k + 1 < h->evused; k += 2) {
-      float t = 0.f;
-      cudaEventElapsedTime(&t, h->evpool[k], h->evpool[k + 1]);
-      h->vanka_ms += t;
-      h->vanka_launches++;
-      h->vanka_bytes += h->prof_bytes[k / 2];
+    for (size_t k = 0; k + 2 < h->evused; k += 3) {
+      float t0 = 0.f, t1 = 0.f;
+      cudaEventElapsedTime(&t0, h->evpool[k], h->evpool[k + 1]);
+      cudaEventElapsedTime(&t1, h->evpool[k + 1], h->evpool[k + 2]);
+      h->prof_ms[0] += t0;
+      h->prof_ms[1] += t1;
+      h->prof_launches[0]++;
+      h->prof_launches[1]++;
+      h->prof_sum_bytes[0] += h->prof_bytes[2 * (k / 3)];
+      h->prof_sum_bytes[1] += h->prof_bytes[2 * (k / 3) + 1];
     }
   }
   if (out) *out = r;
@@ -1044,21 +1047,24 @@ long long pm_device_bytes(pm_handle *h) { return h ? h->bytes : 0; }
 pm_status pm_profile_enable(pm_handle *h, int enable) {
   if (!h) return PM_BADARG;
   h->prof = enable != 0;
-  h->vanka_ms = 0.0;
-  h->vanka_bytes = 0.0;
-  h->vanka_launches = 0;
+  for (int k = 0; k < 2; ++k) {
+    h->prof_ms[k] = 0.0;
+    h->prof_sum_bytes[k] = 0.0;
+    h->prof_launches[k] = 0;
+  }
   if (h->prof && h->evpool.empty()) {
-    h->evpool.resize(1 << 15);
+    h->evpool.resize(3 << 14);
     for (auto &e : h->evpool) cudaEventCreate(&e);
   }
   return PM_OK;
 }
 
-pm_status pm_profile_read(pm_handle *h, double *ms, long long *launches, double *bytes) {
-  if (!h) return PM_BADARG;
-  if (ms) *ms = h->vanka_ms;
-  if (launches) *launches = h->vanka_launches;
-  if (bytes) *bytes = h->vanka_bytes;
+pm_status pm_profile_read(pm_handle *h, int kernel, double *ms, long long *launches,
+                          double *bytes) {
+  if (!h || kernel < 0 || kernel > 1) return PM_BADARG;
+  if (ms) *ms = h->prof_ms[kernel];
+  if (launches) *launches = h->prof_launches[kernel];
+  if (bytes) *bytes = h->prof_sum_bytes[kernel];
   return PM_OK;
 }
 

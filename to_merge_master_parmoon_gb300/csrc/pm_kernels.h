@@ -12,6 +12,7 @@ namespace pm {
 constexpr int NU_LOC = 27;                 // Q2 local velocity nodes
 constexpr int NP_LOC = 4;                  // P1disc local pressure DOFs
 constexpr int NLOC = 3 * NU_LOC + NP_LOC;  // 85: local Vanka block size
+constexpr int kRStride = 88;               // per-cell stride of the residual buffer
 
 // One level's operator in precision T (device pointers).  The nine velocity
 // blocks share the CSR pattern; off-diagonal blocks are zero on Dirichlet rows
@@ -103,16 +104,17 @@ int launch_check_finite(const double *x, int n, int *flag, cudaStream_t s);
 template <typename TF>
 int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *factors,
                         uint8_t *perm, bool factor_fp32, int *status, cudaStream_t s);
-// For the ncol cells listed in cell_list: local residual (full rows) from the
-// current u, local solve with the stored factors, delta -> dbuf[slot*85 + i].
+// For the ncol cells listed in cell_list: local residual r = f - K u over the
+// full rows of the cell's 85 DOFs -> rbuf[slot*kRStride + i].
 template <typename T>
-int launch_vanka_solve(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
-                       const T *factors, const uint8_t *perm, const T *u, const T *rhs, T *dbuf,
+int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
+                          const T *u, const T *rhs, T *rbuf, cudaStream_t s);
+// Local solve with the stored factors and u[dofs] += damp * delta, for the
+// same cells (run after launch_vanka_residual of the whole colour).
+template <typename T>
+int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
+                       const T *factors, const uint8_t *perm, const T *rbuf, T damp, T *u,
                        cudaStream_t s);
-// u[dofs of cell_list[slot]] += damp * dbuf[slot*85 + i]
-template <typename T>
-int launch_vanka_update(const DevCells &cells, int nu, const int *cell_list, int ncol,
-                        const T *dbuf, T damp, T *u, cudaStream_t s);
 
 // ----------------------------------------------------------------- coarse --
 // Dense column-major N x N coarse saddle matrix of SolveExact
@@ -124,6 +126,11 @@ int launch_dense_lu(double *a, int n, int *ipiv, int *status, cudaStream_t s);
 // x = A^{-1} b with the factors (one CTA); b[first_p] = 0 when project.
 int launch_dense_solve(const double *lu, const int *ipiv, int n, const double *b, double *x,
                        int pin_row, cudaStream_t s);
+// A^{-1} (column-major) from the LU factors, one CTA per column.
+int launch_dense_inverse(const double *lu, const int *ipiv, int n, double *inv, cudaStream_t s);
+// x = A^{-1} b in FP64 arithmetic (b[pin_row] = 0 when pin_row >= 0).
+template <typename TB, typename TX>
+int launch_dense_gemv(const double *inv, int n, const TB *b, TX *x, int pin_row, cudaStream_t s);
 
 }  // namespace pm
 

@@ -7,12 +7,12 @@
 // change during a linear solve, so here they are gathered and factored once
 // per matrix (k_vanka_factor) and every sweep only
 //   1. forms each cell's local residual from the full CSR rows (the same
-//      rows the reference reads, :1810-1941),
-//   2. applies the stored factors (forward/back substitution),
-//   3. adds damp * delta to the cell's DOFs (:2044-2059),
+//      rows the reference reads, :1810-1941) -> k_vanka_residual,
+//   2. applies the stored factors (forward/back substitution) and adds
+//      damp * delta to the cell's DOFs (:2044-2059) -> k_vanka_apply,
 // colour by colour: cells of one colour share no DOF; their residuals are
 // all taken from the state before the colour (CellVanka_GPU semantics,
-// src/FE/NSE_CellVanka.cu:2181-2365), so step 3 runs after step 1-2 of the
+// src/FE/NSE_CellVanka.cu:2181-2365), so step 2 runs after step 1 of the
 // whole colour in a separate launch.
 #include <cuda_runtime.h>
 
@@ -190,129 +190,278 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
 }
 
 // ------------------------------------------------------------------ apply ---
-// One warp per cell of the colour.  Lane l owns local rows l, l+32, l+64 of
-// the permuted system during the substitutions.
-constexpr int kSolveWarps = 8;
+// Sweep of one colour = two launches:
+//  k_vanka_residual: one warp per cell forms the local residual
+//    r = f - K u on the cell's 85 DOFs from the full CSR rows.  The cell's
+//    27 A rows, 27 BT rows and 4 B rows are walked as one flattened entry
+//    stream, U x 32 entries per iteration with all their loads issued
+//    together (memory-level parallelism), and summed per row with a
+//    deterministic segmented warp reduction.  r goes to a small buffer.
+//  k_vanka_apply: one warp per cell solves P A = L U with the stored
+//    factors (factor columns prefetched a block ahead in registers) and adds
+//    damp * delta to the cell's DOFs.  Cells of one colour share no DOF and
+//    every residual of the colour was taken before this launch, so the
+//    in-place update is race-free.
+constexpr int kResWarps = 4;
+constexpr int kApplyWarps = 8;
 
-template <typename T>
-__global__ void __launch_bounds__(kSolveWarps * 32) k_vanka_solve(
-    DevOp<T> op, DevCells cells, const int *__restrict__ list, int ncol, const T *__restrict__ F,
-    const uint8_t *__restrict__ perm, const T *__restrict__ u, const T *__restrict__ rhs,
-    T *__restrict__ dbuf) {
-  __shared__ T sres[kSolveWarps][NLOC + 3];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int slot = blockIdx.x * kSolveWarps + warp;
-  if (slot >= ncol) return;  // whole warp leaves; no block-wide barrier below
-  const int cell = list[slot];
-  const int nu = op.nu;
-  const int my_ud = lane < NU_LOC ? cells.udofs[(size_t)cell * NU_LOC + lane] : 0;
-  const int my_pd = lane < NP_LOC ? cells.pdofs[(size_t)cell * NP_LOC + lane] : 0;
-  T *R = sres[warp];
-  const T *u1 = u, *u2 = u + nu, *u3 = u + 2 * nu, *p = u + 3 * nu;
+__device__ __forceinline__ int warp_excl_scan(int v, int lane, int &total) {
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  total = __shfl_sync(kFull, x, 31);
+  return x - v;
+}
 
-  // 1. local residual over the full rows of the cell's 85 DOFs
-  for (int a = 0; a < NU_LOC; ++a) {
-    const int r = __shfl_sync(kFull, my_ud, a);
-    T s1 = 0, s2 = 0, s3 = 0;
-    const int rs = op.a_rowptr[r], re = op.a_rowptr[r + 1];
-    for (int j = rs + lane; j < re; j += 32) {
-      const int c = __ldg(op.a_col + j);
-      const T x1 = u1[c], x2 = u2[c], x3 = u3[c];
-      s1 += ld_stream(op.a[0] + j) * x1 + ld_stream(op.a[1] + j) * x2 + ld_stream(op.a[2] + j) * x3;
-      s2 += ld_stream(op.a[3] + j) * x1 + ld_stream(op.a[4] + j) * x2 + ld_stream(op.a[5] + j) * x3;
-      s3 += ld_stream(op.a[6] + j) * x1 + ld_stream(op.a[7] + j) * x2 + ld_stream(op.a[8] + j) * x3;
-    }
-    if (r < op.nact) {
-      const int bs = op.bt_rowptr[r], be = op.bt_rowptr[r + 1];
-      for (int j = bs + lane; j < be; j += 32) {
-        const T pv = p[__ldg(op.bt_col + j)];
-        s1 += ld_stream(op.bt[0] + j) * pv;
-        s2 += ld_stream(op.bt[1] + j) * pv;
-        s3 += ld_stream(op.bt[2] + j) * pv;
-      }
-    }
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
-    s3 = warp_sum(s3);
-    if (lane == 0) {
-      R[a] = rhs[r] - s1;
-      R[a + NU_LOC] = rhs[nu + r] - s2;
-      R[a + 2 * NU_LOC] = rhs[2 * nu + r] - s3;
+// segment of entry e: the last a in [0,n) with off[a] <= e (empty segments
+// share their offset with the next one and are skipped).
+__device__ __forceinline__ int find_seg(const int *off, int n, int e) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= e) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Segmented warp sum of NO values keyed by seg (contiguous keys, -1 = none);
+// the first lane of each segment adds the sums to acc[seg + k*stride].
+template <typename T, int NO>
+__device__ __forceinline__ void seg_accumulate(int seg, T (&v)[NO], T *acc, int stride, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int so = __shfl_down_sync(kFull, seg, o);
+#pragma unroll
+    for (int k = 0; k < NO; ++k) {
+      const T w = __shfl_down_sync(kFull, v[k], o);
+      if (lane + o < 32 && so == seg) v[k] += w;
     }
   }
-  for (int k = 0; k < NP_LOC; ++k) {
-    const int r = __shfl_sync(kFull, my_pd, k);
-    T s = 0;
-    for (int j = op.b_rowptr[r] + lane; j < op.b_rowptr[r + 1]; j += 32) {
-      const int c = __ldg(op.b_col + j);
-      s += ld_stream(op.b[0] + j) * u1[c] + ld_stream(op.b[1] + j) * u2[c] +
-           ld_stream(op.b[2] + j) * u3[c];
-    }
-    s = warp_sum(s);
-    if (lane == 0) R[3 * NU_LOC + k] = rhs[3 * nu + r] - s;
+  const int sp = __shfl_up_sync(kFull, seg, 1);
+  if (seg >= 0 && (lane == 0 || sp != seg)) {
+#pragma unroll
+    for (int k = 0; k < NO; ++k) acc[seg + k * stride] += v[k];
   }
   __syncwarp();
+}
 
-  // 2. P A = L U: y = P r, L y' = y, U x = y'
-  const uint8_t *pc = perm + (size_t)cell * NLOC;
-  const T *Fc = F + (size_t)cell * NLOC * NLOC;
-  const bool has2 = lane + 64 < NLOC;
-  T y0 = R[__ldg(pc + lane)];
-  T y1 = R[__ldg(pc + lane + 32)];
-  T y2 = has2 ? R[__ldg(pc + lane + 64)] : T(0);
-  for (int j = 0; j < NLOC - 1; ++j) {
-    const T *col = Fc + (size_t)j * NLOC;
-    const T l0 = (lane > j) ? ld_stream(col + lane) : T(0);
-    const T l1 = (lane + 32 > j) ? ld_stream(col + lane + 32) : T(0);
-    const T l2 = (has2 && lane + 64 > j) ? ld_stream(col + lane + 64) : T(0);
-    const int owner = j & 31;
-    const T ysel = (j < 32) ? y0 : ((j < 64) ? y1 : y2);
-    const T yj = __shfl_sync(kFull, ysel, owner);
-    y0 -= l0 * yj;
-    y1 -= l1 * yj;
-    y2 -= l2 * yj;
-  }
-  for (int j = NLOC - 1; j >= 0; --j) {
-    const T *col = Fc + (size_t)j * NLOC;
-    const T u0 = (lane <= j) ? ld_stream(col + lane) : T(0);
-    const T u1v = (lane + 32 <= j) ? ld_stream(col + lane + 32) : T(0);
-    const T u2v = (has2 && lane + 64 <= j) ? ld_stream(col + lane + 64) : T(0);
-    const int owner = j & 31;
-    // diagonal holds 1/U_jj
-    if (lane == owner) {
-      if (j < 32)
-        y0 *= u0;
-      else if (j < 64)
-        y1 *= u1v;
-      else
-        y2 *= u2v;
+// Walk nseg row segments (start st[a], length off[a+1]-off[a]) of a CSR
+// matrix with NV value arrays; each entry contributes NO products.
+// MODE 0: A rows (9 values, gather u1,u2,u3 -> 3 outputs)
+// MODE 1: BT rows (3 values, gather p -> 3 outputs)
+// MODE 2: B rows (3 values, gather u1,u2,u3 -> 1 output)
+template <typename T, int MODE, int U>
+__device__ __forceinline__ void flat_rows(const int *st, const int *off, int nseg, int total,
+                                          const int *__restrict__ col, const T *const *vals,
+                                          const T *__restrict__ x0, const T *__restrict__ x1,
+                                          const T *__restrict__ x2, T *acc, int lane) {
+  constexpr int NV = MODE == 0 ? 9 : 3;
+  constexpr int NO = MODE == 2 ? 1 : 3;
+  for (int base = 0; base < total; base += 32 * U) {
+    int seg[U], gi[U], c[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const int e = base + q * 32 + lane;
+      if (e < total) {
+        seg[q] = find_seg(off, nseg, e);
+        gi[q] = st[seg[q]] + (e - off[seg[q]]);
+      } else {
+        seg[q] = -1;
+        gi[q] = -1;
+      }
     }
-    const T ysel = (j < 32) ? y0 : ((j < 64) ? y1 : y2);
-    const T xj = __shfl_sync(kFull, ysel, owner);
-    if (lane < j) y0 -= u0 * xj;
-    if (lane + 32 < j) y1 -= u1v * xj;
-    if (has2 && lane + 64 < j) y2 -= u2v * xj;
+#pragma unroll
+    for (int q = 0; q < U; ++q) c[q] = gi[q] >= 0 ? __ldg(col + gi[q]) : 0;
+    T v[U][NV];
+#pragma unroll
+    for (int q = 0; q < U; ++q)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) v[q][k] = gi[q] >= 0 ? ld_stream(vals[k] + gi[q]) : T(0);
+    T g[U][3];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      if (MODE == 1) {
+        g[q][0] = __ldg(x0 + c[q]);
+        g[q][1] = g[q][2] = T(0);
+      } else {
+        g[q][0] = __ldg(x0 + c[q]);
+        g[q][1] = __ldg(x1 + c[q]);
+        g[q][2] = __ldg(x2 + c[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      T s[NO];
+      if (MODE == 0) {
+        s[0] = v[q][0] * g[q][0] + v[q][1] * g[q][1] + v[q][2] * g[q][2];
+        s[1 % NO] = v[q][3] * g[q][0] + v[q][4] * g[q][1] + v[q][5] * g[q][2];
+        s[2 % NO] = v[q][6] * g[q][0] + v[q][7] * g[q][1] + v[q][8] * g[q][2];
+      } else if (MODE == 1) {
+        s[0] = v[q][0] * g[q][0];
+        s[1 % NO] = v[q][1] * g[q][0];
+        s[2 % NO] = v[q][2] * g[q][0];
+      } else {
+        s[0] = v[q][0] * g[q][0] + v[q][1] * g[q][1] + v[q][2] * g[q][2];
+      }
+      seg_accumulate<T, NO>(seg[q], s, acc, NU_LOC, lane);
+    }
   }
-  T *D = dbuf + (size_t)slot * NLOC;
-  D[lane] = y0;
-  D[lane + 32] = y1;
-  if (has2) D[lane + 64] = y2;
+}
+
+template <typename T, int U>
+__global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual(
+    DevOp<T> op, DevCells cells, const int *__restrict__ list, int ncol, const T *__restrict__ u,
+    const T *__restrict__ rhs, T *__restrict__ rbuf) {
+  __shared__ int s_st[kResWarps][32];
+  __shared__ int s_off[kResWarps][32];
+  __shared__ T s_acc[kResWarps][kRStride];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = blockIdx.x * kResWarps + warp;
+  if (slot >= ncol) return;  // whole warp; no block-wide barrier in this kernel
+  const int cell = list[slot];
+  const int nu = op.nu;
+  const T *u1 = u, *u2 = u + nu, *u3 = u + 2 * nu, *p = u + 3 * nu;
+  int *st = s_st[warp], *off = s_off[warp];
+  T *acc = s_acc[warp];
+  for (int i = lane; i < kRStride; i += 32) acc[i] = T(0);
+  const int my_r = lane < NU_LOC ? cells.udofs[(size_t)cell * NU_LOC + lane] : 0;
+  const int my_p = lane < NP_LOC ? cells.pdofs[(size_t)cell * NP_LOC + lane] : 0;
+  int start, len, total;
+  // A rows: nine blocks
+  start = lane < NU_LOC ? op.a_rowptr[my_r] : 0;
+  len = lane < NU_LOC ? op.a_rowptr[my_r + 1] - start : 0;
+  off[lane] = warp_excl_scan(len, lane, total);
+  st[lane] = start;
+  __syncwarp();
+  flat_rows<T, 0, U>(st, off, NU_LOC, total, op.a_col, op.a, u1, u2, u3, acc, lane);
+  __syncwarp();
+  // BT rows of active velocity DOFs
+  const bool act = lane < NU_LOC && my_r < op.nact;
+  start = act ? op.bt_rowptr[my_r] : 0;
+  len = act ? op.bt_rowptr[my_r + 1] - start : 0;
+  off[lane] = warp_excl_scan(len, lane, total);
+  st[lane] = start;
+  __syncwarp();
+  flat_rows<T, 1, U>(st, off, NU_LOC, total, op.bt_col, op.bt, p, p, p, acc, lane);
+  __syncwarp();
+  // B rows of the cell's pressure DOFs
+  start = lane < NP_LOC ? op.b_rowptr[my_p] : 0;
+  len = lane < NP_LOC ? op.b_rowptr[my_p + 1] - start : 0;
+  off[lane] = warp_excl_scan(len, lane, total);
+  st[lane] = start;
+  __syncwarp();
+  flat_rows<T, 2, U>(st, off, NP_LOC, total, op.b_col, op.b, u1, u2, u3, acc + 3 * NU_LOC, lane);
+  __syncwarp();
+  T *R = rbuf + (size_t)slot * kRStride;
+  if (lane < NU_LOC) {
+    R[lane] = rhs[my_r] - acc[lane];
+    R[lane + NU_LOC] = rhs[nu + my_r] - acc[lane + NU_LOC];
+    R[lane + 2 * NU_LOC] = rhs[2 * nu + my_r] - acc[lane + 2 * NU_LOC];
+  }
+  if (lane < NP_LOC) R[3 * NU_LOC + lane] = rhs[3 * nu + my_p] - acc[3 * NU_LOC + lane];
 }
 
 template <typename T>
-__global__ void k_vanka_update(DevCells cells, int nu, const int *__restrict__ list, int ncol,
-                               const T *__restrict__ dbuf, T damp, T *__restrict__ u) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)ncol * NLOC) return;
-  const int slot = (int)(t / NLOC), i = (int)(t % NLOC);
-  const int cell = list[slot];
-  const T d = damp * dbuf[t];
+__device__ __forceinline__ void scatter_local(int i, T v, const int *ud, const int *pd, int nu,
+                                              T *u) {
   if (i < 3 * NU_LOC) {
-    const int comp = i / NU_LOC, a = i % NU_LOC;
-    u[(size_t)comp * nu + cells.udofs[(size_t)cell * NU_LOC + a]] += d;
+    const int comp = i / NU_LOC, a = i - comp * NU_LOC;
+    u[(size_t)comp * nu + ud[a]] += v;
   } else {
-    u[(size_t)3 * nu + cells.pdofs[(size_t)cell * NP_LOC + (i - 3 * NU_LOC)]] += d;
+    u[(size_t)3 * nu + pd[i - 3 * NU_LOC]] += v;
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
+    DevCells cells, int nu, const int *__restrict__ list, int ncol, const T *__restrict__ F,
+    const uint8_t *__restrict__ perm, const T *__restrict__ rbuf, T damp, T *__restrict__ u) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = blockIdx.x * kApplyWarps + warp;
+  if (slot >= ncol) return;
+  const int cell = list[slot];
+  const bool has2 = lane + 64 < NLOC;
+  const uint8_t *pc = perm + (size_t)cell * NLOC;
+  const T *R = rbuf + (size_t)slot * kRStride;
+  T y0 = R[__ldg(pc + lane)];
+  T y1 = R[__ldg(pc + lane + 32)];
+  T y2 = has2 ? R[__ldg(pc + lane + 64)] : T(0);
+  const T *Fc = F + (size_t)cell * NLOC * NLOC;
+  // forward substitution with the unit lower factor, columns 0..83 in blocks
+  // of 4, the next block's column entries loaded while this one is used
+  T cur[4][3], nxt[4][3];
+  auto load_l = [&](T(&b)[4][3], int j0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = j0 + q;
+      const T *col = Fc + (size_t)j * NLOC;
+      b[q][0] = (lane > j) ? ld_stream(col + lane) : T(0);
+      b[q][1] = (lane + 32 > j) ? ld_stream(col + lane + 32) : T(0);
+      b[q][2] = (has2 && lane + 64 > j) ? ld_stream(col + lane + 64) : T(0);
+    }
+  };
+  load_l(cur, 0);
+  for (int j0 = 0; j0 < NLOC - 1; j0 += 4) {
+    if (j0 + 4 < NLOC - 1) load_l(nxt, j0 + 4);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = j0 + q;
+      const T ysel = (j < 32) ? y0 : ((j < 64) ? y1 : y2);
+      const T yj = __shfl_sync(kFull, ysel, j & 31);
+      y0 -= cur[q][0] * yj;
+      y1 -= cur[q][1] * yj;
+      y2 -= cur[q][2] * yj;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) cur[q][k] = nxt[q][k];
+  }
+  // back substitution with U (diagonal stores 1/U_jj), columns 84..0
+  auto load_u = [&](T(&b)[4][3], int jt) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = jt - q;
+      const T *col = Fc + (size_t)(j < 0 ? 0 : j) * NLOC;
+      b[q][0] = (j >= 0 && lane <= j) ? ld_stream(col + lane) : T(0);
+      b[q][1] = (j >= 0 && lane + 32 <= j) ? ld_stream(col + lane + 32) : T(0);
+      b[q][2] = (j >= 0 && has2 && lane + 64 <= j) ? ld_stream(col + lane + 64) : T(0);
+    }
+  };
+  load_u(cur, NLOC - 1);
+  for (int jt = NLOC - 1; jt >= 0; jt -= 4) {
+    if (jt - 4 >= 0) load_u(nxt, jt - 4);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = jt - q;
+      if (j >= 0) {
+        const int owner = j & 31;
+        if (lane == owner) {
+          if (j < 32) y0 *= cur[q][0];
+          else if (j < 64) y1 *= cur[q][1];
+          else y2 *= cur[q][2];
+        }
+        const T ysel = (j < 32) ? y0 : ((j < 64) ? y1 : y2);
+        const T xj = __shfl_sync(kFull, ysel, owner);
+        if (lane < j) y0 -= cur[q][0] * xj;
+        if (lane + 32 < j) y1 -= cur[q][1] * xj;
+        if (has2 && lane + 64 < j) y2 -= cur[q][2] * xj;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) cur[q][k] = nxt[q][k];
+  }
+  // u += damp * delta on the cell's DOFs (local order: u1 nodes, u2, u3, p)
+  const int *ud = cells.udofs + (size_t)cell * NU_LOC;
+  const int *pd = cells.pdofs + (size_t)cell * NP_LOC;
+  scatter_local(lane, damp * y0, ud, pd, nu, u);
+  scatter_local(lane + 32, damp * y1, ud, pd, nu, u);
+  if (has2) scatter_local(lane + 64, damp * y2, ud, pd, nu, u);
 }
 
 // ----------------------------------------------------------------- coarse ---
@@ -480,6 +629,62 @@ __global__ void __launch_bounds__(kDenseSolveThreads) k_dense_solve(const double
   for (int i = tid; i < N; i += kDenseSolveThreads) x[i] = xs[i];
 }
 
+// Column j of A^{-1} from the LU factors (P A = L U): one CTA per column,
+// forward and back substitution of P e_j with barriers per step.  Runs once
+// per factorisation; every coarse solve is then one GEMV.
+constexpr int kInvThreads = 256;
+__global__ void __launch_bounds__(kInvThreads) k_dense_inverse(const double *lu, const int *ipiv,
+                                                               int N, double *inv) {
+  extern __shared__ double xs[];
+  const int j = blockIdx.x, tid = threadIdx.x;
+  for (int i = tid; i < N; i += kInvThreads) xs[i] = (i == j) ? 1.0 : 0.0;
+  __syncthreads();
+  if (tid == 0)
+    for (int k = 0; k < N; ++k) {
+      const int p = ipiv[k];
+      if (p != k) {
+        const double t = xs[k];
+        xs[k] = xs[p];
+        xs[p] = t;
+      }
+    }
+  __syncthreads();
+  for (int k = 0; k < N; ++k) {
+    const double xk = xs[k];
+    if (xk != 0.0)
+      for (int i = k + 1 + tid; i < N; i += kInvThreads) xs[i] -= lu[(size_t)k * N + i] * xk;
+    __syncthreads();
+  }
+  for (int k = N - 1; k >= 0; --k) {
+    if (tid == 0) xs[k] /= lu[(size_t)k * N + k];
+    __syncthreads();
+    const double xk = xs[k];
+    if (xk != 0.0)
+      for (int i = tid; i < k; i += kInvThreads) xs[i] -= lu[(size_t)k * N + i] * xk;
+    __syncthreads();
+  }
+  for (int i = tid; i < N; i += kInvThreads) inv[(size_t)j * N + i] = xs[i];
+}
+
+// x = A^{-1} b (A^{-1} column-major), b[pin_row] = 0 when pin_row >= 0
+template <typename TB, typename TX>
+__global__ void k_dense_gemv(const double *__restrict__ inv, int N, const TB *__restrict__ b,
+                             TX *__restrict__ x, int pin_row) {
+  extern __shared__ double bs[];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) bs[i] = (i == pin_row) ? 0.0 : (double)b[i];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double s0 = 0.0, s1 = 0.0;
+  int j = 0;
+  for (; j + 1 < N; j += 2) {
+    s0 += inv[(size_t)j * N + i] * bs[j];
+    s1 += inv[(size_t)(j + 1) * N + i] * bs[j + 1];
+  }
+  if (j < N) s0 += inv[(size_t)j * N + i] * bs[j];
+  x[i] = (TX)(s0 + s1);
+}
+
 inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 
 }  // namespace
@@ -505,23 +710,23 @@ int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *fact
 }
 
 template <typename T>
-int launch_vanka_solve(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
-                       const T *factors, const uint8_t *perm, const T *u, const T *rhs, T *dbuf,
-                       cudaStream_t s) {
+int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
+                          const T *u, const T *rhs, T *rbuf, cudaStream_t s) {
   if (ncol <= 0) return 0;
-  const int grid = (ncol + kSolveWarps - 1) / kSolveWarps;
-  k_vanka_solve<T><<<grid, kSolveWarps * 32, 0, s>>>(op, cells, cell_list, ncol, factors, perm, u,
-                                                    rhs, dbuf);
+  constexpr int U = sizeof(T) == 4 ? 4 : 2;
+  const int grid = (ncol + kResWarps - 1) / kResWarps;
+  k_vanka_residual<T, U><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list, ncol, u, rhs, rbuf);
   return ok() < 0 ? -1 : 1;
 }
 
 template <typename T>
-int launch_vanka_update(const DevCells &cells, int nu, const int *cell_list, int ncol,
-                        const T *dbuf, T damp, T *u, cudaStream_t s) {
+int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
+                       const T *factors, const uint8_t *perm, const T *rbuf, T damp, T *u,
+                       cudaStream_t s) {
   if (ncol <= 0) return 0;
-  const long long n = (long long)ncol * NLOC;
-  k_vanka_update<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(cells, nu, cell_list, ncol, dbuf,
-                                                                damp, u);
+  const int grid = (ncol + kApplyWarps - 1) / kApplyWarps;
+  k_vanka_apply<T><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors, perm,
+                                                    rbuf, damp, u);
   return ok() < 0 ? -1 : 1;
 }
 
@@ -544,6 +749,27 @@ int launch_dense_lu(double *a, int n, int *ipiv, int *status, cudaStream_t s) {
   return ok() < 0 ? -1 : 1;
 }
 
+int launch_dense_inverse(const double *lu, const int *ipiv, int n, double *inv, cudaStream_t s) {
+  const size_t sm = sizeof(double) * n;
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_dense_inverse<<<n, kInvThreads, sm, s>>>(lu, ipiv, n, inv);
+  return ok() < 0 ? -1 : 1;
+}
+
+template <typename TB, typename TX>
+int launch_dense_gemv(const double *inv, int n, const TB *b, TX *x, int pin_row, cudaStream_t s) {
+  const size_t sm = sizeof(double) * n;
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_dense_gemv<TB, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_dense_gemv<TB, TX><<<(n + 127) / 128, 128, sm, s>>>(inv, n, b, x, pin_row);
+  return ok() < 0 ? -1 : 1;
+}
+template int launch_dense_gemv<double, double>(const double *, int, const double *, double *, int,
+                                               cudaStream_t);
+template int launch_dense_gemv<float, float>(const double *, int, const float *, float *, int,
+                                             cudaStream_t);
+
 int launch_dense_solve(const double *lu, const int *ipiv, int n, const double *b, double *x,
                        int pin_row, cudaStream_t s) {
   const size_t sm = sizeof(double) * n;
@@ -557,15 +783,13 @@ template int launch_vanka_factor<double>(const DevOp<double> &, const DevCells &
                                          uint8_t *, bool, int *, cudaStream_t);
 template int launch_vanka_factor<float>(const DevOp<double> &, const DevCells &, float *,
                                         uint8_t *, bool, int *, cudaStream_t);
-template int launch_vanka_solve<double>(const DevOp<double> &, const DevCells &, const int *, int,
-                                        const double *, const uint8_t *, const double *,
-                                        const double *, double *, cudaStream_t);
-template int launch_vanka_solve<float>(const DevOp<float> &, const DevCells &, const int *, int,
-                                       const float *, const uint8_t *, const float *,
-                                       const float *, float *, cudaStream_t);
-template int launch_vanka_update<double>(const DevCells &, int, const int *, int, const double *,
-                                         double, double *, cudaStream_t);
-template int launch_vanka_update<float>(const DevCells &, int, const int *, int, const float *,
-                                        float, float *, cudaStream_t);
+#define PM_VINST(T)                                                                                 \
+  template int launch_vanka_residual<T>(const DevOp<T> &, const DevCells &, const int *, int,      \
+                                        const T *, const T *, T *, cudaStream_t);                  \
+  template int launch_vanka_apply<T>(const DevCells &, int, const int *, int, const T *,           \
+                                     const uint8_t *, const T *, T, T *, cudaStream_t);
+PM_VINST(double)
+PM_VINST(float)
+#undef PM_VINST
 
 }  // namespace pm

@@ -106,10 +106,15 @@ class PmSolver:
         self._check(self._lib.pm_profile_enable(self._h, int(enable)), "pm_profile_enable")
 
     def profile_read(self) -> dict:
-        ms, n, b = C.c_double(), C.c_longlong(), C.c_double()
-        self._check(self._lib.pm_profile_read(self._h, C.byref(ms), C.byref(n), C.byref(b)),
-                    "pm_profile_read")
-        return {"vanka_ms": ms.value, "vanka_launches": n.value, "vanka_bytes": b.value}
+        """Totals of the two Vanka sweep kernels since profile(True):
+        {"residual": {...}, "apply": {...}} with ms, launches, bytes."""
+        out = {}
+        for k, name in enumerate(("residual", "apply")):
+            ms, n, b = C.c_double(), C.c_longlong(), C.c_double()
+            self._check(self._lib.pm_profile_read(self._h, k, C.byref(ms), C.byref(n), C.byref(b)),
+                        "pm_profile_read")
+            out[name] = {"ms": ms.value, "launches": n.value, "bytes": b.value}
+        return out
 
     # ------------------------------------------------------------ level ops
     def coupled_defect(self, level, x, b, project=True):
