@@ -201,6 +201,21 @@ pm_status pm_profile_enable(pm_handle *h, int enable);
 pm_status pm_profile_read(pm_handle *h, int kernel, double *ms_total, long long *launches,
                           double *bytes_total);
 
+/* Allocation-free L2_0 projection of a P1disc pressure vector on the device
+ * (subtract the mean of the constant modes d_p[0], d_p[4], ...), for callers
+ * that cannot allocate device memory where they need it: code inside CUDA
+ * stream capture, solvers confined to an application-owned memory pool, MPI
+ * ranks whose GPU memory is partitioned before the time loop.  No counterpart
+ * in the reference (there the projection is host code, IntoL20Vector3D); it
+ * computes what pm_coupled_defect's projection computes, without a handle.
+ * Its reduction scratch is a 64 KB file-scope device array held by every GPU
+ * that loads the library until exit; n_p must be a multiple of 4 and at most
+ * 8,388,608 (else PM_BADARG).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race.  stream may be NULL (default stream).  Nothing is allocated. */
+pm_status pm_l20_project_noalloc(double *d_p, int n_p, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
