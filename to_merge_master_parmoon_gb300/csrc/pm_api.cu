@@ -179,6 +179,28 @@ pm_status dalloc(pm_handle *h, T **p, size_t count) {
   return PM_OK;
 }
 
+// CSR value / column arrays: padded by 8 zero entries so that the Vanka
+// residual kernel's aligned 4-entry vector loads never leave the allocation.
+constexpr size_t kCsrPad = 8;
+template <typename T>
+pm_status dalloc_padded(pm_handle *h, T **p, size_t count) {
+  pm_status s = dalloc(h, p, count + kCsrPad);
+  if (s != PM_OK) return s;
+  if (cudaMemsetAsync(*p, 0, (count + kCsrPad) * sizeof(T), h->stream) != cudaSuccess)
+    return cuda_fail(h, "padded alloc");
+  return PM_OK;
+}
+
+template <typename T>
+pm_status upload_padded(pm_handle *h, T **dst, const T *src, size_t count) {
+  pm_status s = dalloc_padded(h, dst, count);
+  if (s != PM_OK) return s;
+  if (count && cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice, h->stream) !=
+                   cudaSuccess)
+    return cuda_fail(h, "upload");
+  return PM_OK;
+}
+
 template <typename T>
 pm_status upload(pm_handle *h, T **dst, const T *src, size_t count) {
   pm_status s = dalloc(h, dst, count);
@@ -554,7 +576,7 @@ pm_status factor_all(pm_handle *h) {
 pm_status upload_values(pm_handle *h, LevelDev &Lv, const pm_level_desc *d, bool first) {
   for (int k = 0; k < 9; ++k) {
     if (!d->a[k]) return fail(h, PM_BADARG, "missing A block");
-    if (first) PM_TRY(dalloc(h, &Lv.a64[k], Lv.a_nnz));
+    if (first) PM_TRY(dalloc_padded(h, &Lv.a64[k], Lv.a_nnz));
     if (cudaMemcpyAsync(Lv.a64[k], d->a[k], sizeof(double) * Lv.a_nnz, cudaMemcpyHostToDevice,
                         h->stream) != cudaSuccess)
       return cuda_fail(h, "A upload");
@@ -562,8 +584,8 @@ pm_status upload_values(pm_handle *h, LevelDev &Lv, const pm_level_desc *d, bool
   for (int k = 0; k < 3; ++k) {
     if (!d->b[k] || !d->bt[k]) return fail(h, PM_BADARG, "missing B/BT block");
     if (first) {
-      PM_TRY(dalloc(h, &Lv.b64[k], Lv.b_nnz));
-      PM_TRY(dalloc(h, &Lv.bt64[k], Lv.bt_nnz));
+      PM_TRY(dalloc_padded(h, &Lv.b64[k], Lv.b_nnz));
+      PM_TRY(dalloc_padded(h, &Lv.bt64[k], Lv.bt_nnz));
     }
     if (cudaMemcpyAsync(Lv.b64[k], d->b[k], sizeof(double) * Lv.b_nnz, cudaMemcpyHostToDevice,
                         h->stream) != cudaSuccess ||
@@ -574,13 +596,13 @@ pm_status upload_values(pm_handle *h, LevelDev &Lv, const pm_level_desc *d, bool
   PM_LAUNCH(launch_zero_dirichlet_offdiag(Lv.a64, Lv.a_rowptr, Lv.nu, Lv.nact, h->stream));
   if (mixed(h)) {
     for (int k = 0; k < 9; ++k) {
-      if (first) PM_TRY(dalloc(h, &Lv.a32[k], Lv.a_nnz));
+      if (first) PM_TRY(dalloc_padded(h, &Lv.a32[k], Lv.a_nnz));
       PM_LAUNCH((launch_convert<float, double>(Lv.a32[k], Lv.a64[k], Lv.a_nnz, h->stream)));
     }
     for (int k = 0; k < 3; ++k) {
       if (first) {
-        PM_TRY(dalloc(h, &Lv.b32[k], Lv.b_nnz));
-        PM_TRY(dalloc(h, &Lv.bt32[k], Lv.bt_nnz));
+        PM_TRY(dalloc_padded(h, &Lv.b32[k], Lv.b_nnz));
+        PM_TRY(dalloc_padded(h, &Lv.bt32[k], Lv.bt_nnz));
       }
       PM_LAUNCH((launch_convert<float, double>(Lv.b32[k], Lv.b64[k], Lv.b_nnz, h->stream)));
       PM_LAUNCH((launch_convert<float, double>(Lv.bt32[k], Lv.bt64[k], Lv.bt_nnz, h->stream)));
@@ -728,11 +750,11 @@ pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
   Lv.has_colour = d->cell_colour != nullptr;
   if (Lv.has_colour) Lv.h_colour.assign(d->cell_colour, d->cell_colour + Lv.ncells);
   PM_TRY(upload(h, &Lv.a_rowptr, d->a_rowptr, (size_t)Lv.nu + 1));
-  PM_TRY(upload(h, &Lv.a_col, d->a_col, (size_t)Lv.a_nnz));
+  PM_TRY(upload_padded(h, &Lv.a_col, d->a_col, (size_t)Lv.a_nnz));
   PM_TRY(upload(h, &Lv.b_rowptr, d->b_rowptr, (size_t)Lv.np + 1));
-  PM_TRY(upload(h, &Lv.b_col, d->b_col, (size_t)Lv.b_nnz));
+  PM_TRY(upload_padded(h, &Lv.b_col, d->b_col, (size_t)Lv.b_nnz));
   PM_TRY(upload(h, &Lv.bt_rowptr, d->bt_rowptr, (size_t)Lv.nu + 1));
-  PM_TRY(upload(h, &Lv.bt_col, d->bt_col, (size_t)Lv.bt_nnz));
+  PM_TRY(upload_padded(h, &Lv.bt_col, d->bt_col, (size_t)Lv.bt_nnz));
   if (h->opt.pin_host) {
     auto pin = [h](const void *p, size_t bytes) {
       if (!p || bytes < (1u << 20)) return;

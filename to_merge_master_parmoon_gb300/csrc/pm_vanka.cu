@@ -248,75 +248,139 @@ __device__ __forceinline__ void seg_accumulate(int seg, T (&v)[NO], T *acc, int 
   __syncwarp();
 }
 
-// Walk nseg row segments (start st[a], length off[a+1]-off[a]) of a CSR
-// matrix with NV value arrays; each entry contributes NO products.
+// Aligned vector loads of VEC consecutive CSR entries (value and column
+// arrays are padded to a multiple of 4 entries at upload).
+template <typename T, int VEC>
+struct VecLd;
+template <>
+struct VecLd<float, 4> {
+  static __device__ __forceinline__ void val(const float *p, float (&o)[4]) {
+    const float4 v = __ldcs(reinterpret_cast<const float4 *>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+  static __device__ __forceinline__ void idx(const int *p, int (&o)[4]) {
+    const int4 v = __ldg(reinterpret_cast<const int4 *>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+};
+template <>
+struct VecLd<double, 2> {
+  static __device__ __forceinline__ void val(const double *p, double (&o)[2]) {
+    const double2 v = __ldcs(reinterpret_cast<const double2 *>(p));
+    o[0] = v.x; o[1] = v.y;
+  }
+  static __device__ __forceinline__ void idx(const int *p, int (&o)[2]) {
+    const int2 v = __ldg(reinterpret_cast<const int2 *>(p));
+    o[0] = v.x; o[1] = v.y;
+  }
+};
+
+// Row segments of one warp: row a spans entries [rs[a], re[a]) and the
+// aligned VEC-entry groups qs[a] .. qs[a] + (off[a+1]-off[a]) - 1, which are
+// flattened across rows (group offset off[a]).
+struct SegTab {
+  int *qs, *off, *rs, *re;
+};
+
+template <int VEC>
+__device__ __forceinline__ int seg_setup(const SegTab &t, int lane, bool valid, int rs, int re) {
+  int nq = 0, qs = 0;
+  if (valid && re > rs) {
+    qs = rs / VEC;
+    nq = (re - 1) / VEC - qs + 1;
+  }
+  int total;
+  t.off[lane] = warp_excl_scan(nq, lane, total);
+  t.qs[lane] = qs;
+  t.rs[lane] = valid ? rs : 0;
+  t.re[lane] = valid ? re : 0;
+  __syncwarp();
+  return total;
+}
+
+// Walk the groups of nseg row segments of a CSR matrix with NV value
+// arrays; each entry contributes NO products.
 // MODE 0: A rows (9 values, gather u1,u2,u3 -> 3 outputs)
 // MODE 1: BT rows (3 values, gather p -> 3 outputs)
 // MODE 2: B rows (3 values, gather u1,u2,u3 -> 1 output)
-template <typename T, int MODE, int U>
-__device__ __forceinline__ void flat_rows(const int *st, const int *off, int nseg, int total,
+template <typename T, int MODE, int VEC, int U>
+__device__ __forceinline__ void flat_rows(const SegTab &t, int nseg, int total,
                                           const int *__restrict__ col, const T *const *vals,
                                           const T *__restrict__ x0, const T *__restrict__ x1,
                                           const T *__restrict__ x2, T *acc, int lane) {
   constexpr int NV = MODE == 0 ? 9 : 3;
   constexpr int NO = MODE == 2 ? 1 : 3;
   for (int base = 0; base < total; base += 32 * U) {
-    int seg[U], gi[U], c[U];
+    int seg[U];
+    long long gq[U];
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      const int e = base + q * 32 + lane;
-      if (e < total) {
-        seg[q] = find_seg(off, nseg, e);
-        gi[q] = st[seg[q]] + (e - off[seg[q]]);
-      } else {
-        seg[q] = -1;
-        gi[q] = -1;
+      const int g = base + q * 32 + lane;
+      seg[q] = -1;
+      gq[q] = 0;
+      if (g < total) {
+        seg[q] = find_seg(t.off, nseg, g);
+        gq[q] = (long long)t.qs[seg[q]] + (g - t.off[seg[q]]);
       }
     }
-#pragma unroll
-    for (int q = 0; q < U; ++q) c[q] = gi[q] >= 0 ? __ldg(col + gi[q]) : 0;
-    T v[U][NV];
-#pragma unroll
-    for (int q = 0; q < U; ++q)
-#pragma unroll
-      for (int k = 0; k < NV; ++k) v[q][k] = gi[q] >= 0 ? ld_stream(vals[k] + gi[q]) : T(0);
-    T g[U][3];
+    int ci[U][VEC];
+    T v[U][NV][VEC];
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      if (MODE == 1) {
-        g[q][0] = __ldg(x0 + c[q]);
-        g[q][1] = g[q][2] = T(0);
+      if (seg[q] >= 0) {
+        VecLd<T, VEC>::idx(col + gq[q] * VEC, ci[q]);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) VecLd<T, VEC>::val(vals[k] + gq[q] * VEC, v[q][k]);
       } else {
-        g[q][0] = __ldg(x0 + c[q]);
-        g[q][1] = __ldg(x1 + c[q]);
-        g[q][2] = __ldg(x2 + c[q]);
+#pragma unroll
+        for (int m = 0; m < VEC; ++m) {
+          ci[q][m] = 0;
+#pragma unroll
+          for (int k = 0; k < NV; ++k) v[q][k][m] = T(0);
+        }
       }
     }
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       T s[NO];
-      if (MODE == 0) {
-        s[0] = v[q][0] * g[q][0] + v[q][1] * g[q][1] + v[q][2] * g[q][2];
-        s[1 % NO] = v[q][3] * g[q][0] + v[q][4] * g[q][1] + v[q][5] * g[q][2];
-        s[2 % NO] = v[q][6] * g[q][0] + v[q][7] * g[q][1] + v[q][8] * g[q][2];
-      } else if (MODE == 1) {
-        s[0] = v[q][0] * g[q][0];
-        s[1 % NO] = v[q][1] * g[q][0];
-        s[2 % NO] = v[q][2] * g[q][0];
-      } else {
-        s[0] = v[q][0] * g[q][0] + v[q][1] * g[q][1] + v[q][2] * g[q][2];
+#pragma unroll
+      for (int k = 0; k < NO; ++k) s[k] = T(0);
+      if (seg[q] >= 0) {
+        const long long e0 = gq[q] * VEC;
+        const int lo = t.rs[seg[q]], hi = t.re[seg[q]];
+#pragma unroll
+        for (int m = 0; m < VEC; ++m) {
+          const long long e = e0 + m;
+          if (e >= lo && e < hi) {
+            const int c = ci[q][m];
+            if (MODE == 1) {
+              const T g0 = __ldg(x0 + c);
+              s[0] += v[q][0][m] * g0;
+              s[1 % NO] += v[q][1][m] * g0;
+              s[2 % NO] += v[q][2][m] * g0;
+            } else {
+              const T g0 = __ldg(x0 + c), g1 = __ldg(x1 + c), g2 = __ldg(x2 + c);
+              if (MODE == 0) {
+                s[0] += v[q][0][m] * g0 + v[q][1][m] * g1 + v[q][2][m] * g2;
+                s[1 % NO] += v[q][3][m] * g0 + v[q][4][m] * g1 + v[q][5][m] * g2;
+                s[2 % NO] += v[q][6][m] * g0 + v[q][7][m] * g1 + v[q][8][m] * g2;
+              } else {
+                s[0] += v[q][0][m] * g0 + v[q][1][m] * g1 + v[q][2][m] * g2;
+              }
+            }
+          }
+        }
       }
       seg_accumulate<T, NO>(seg[q], s, acc, NU_LOC, lane);
     }
   }
 }
 
-template <typename T, int U>
+template <typename T, int VEC, int U>
 __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual(
     DevOp<T> op, DevCells cells, const int *__restrict__ list, int ncol, const T *__restrict__ u,
     const T *__restrict__ rhs, T *__restrict__ rbuf) {
-  __shared__ int s_st[kResWarps][32];
-  __shared__ int s_off[kResWarps][32];
+  __shared__ int s_tab[kResWarps][4][32];
   __shared__ T s_acc[kResWarps][kRStride];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int slot = blockIdx.x * kResWarps + warp;
@@ -324,44 +388,32 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual(
   const int cell = list[slot];
   const int nu = op.nu;
   const T *u1 = u, *u2 = u + nu, *u3 = u + 2 * nu, *p = u + 3 * nu;
-  int *st = s_st[warp], *off = s_off[warp];
+  const SegTab tab{s_tab[warp][0], s_tab[warp][1], s_tab[warp][2], s_tab[warp][3]};
   T *acc = s_acc[warp];
   for (int i = lane; i < kRStride; i += 32) acc[i] = T(0);
-  const int my_r = lane < NU_LOC ? cells.udofs[(size_t)cell * NU_LOC + lane] : 0;
-  const int my_p = lane < NP_LOC ? cells.pdofs[(size_t)cell * NP_LOC + lane] : 0;
-  int start, len, total;
+  const bool vu = lane < NU_LOC, vp = lane < NP_LOC;
+  const int my_r = vu ? cells.udofs[(size_t)cell * NU_LOC + lane] : 0;
+  const int my_p = vp ? cells.pdofs[(size_t)cell * NP_LOC + lane] : 0;
   // A rows: nine blocks
-  start = lane < NU_LOC ? op.a_rowptr[my_r] : 0;
-  len = lane < NU_LOC ? op.a_rowptr[my_r + 1] - start : 0;
-  off[lane] = warp_excl_scan(len, lane, total);
-  st[lane] = start;
-  __syncwarp();
-  flat_rows<T, 0, U>(st, off, NU_LOC, total, op.a_col, op.a, u1, u2, u3, acc, lane);
-  __syncwarp();
+  int total = seg_setup<VEC>(tab, lane, vu, vu ? op.a_rowptr[my_r] : 0,
+                             vu ? op.a_rowptr[my_r + 1] : 0);
+  flat_rows<T, 0, VEC, U>(tab, NU_LOC, total, op.a_col, op.a, u1, u2, u3, acc, lane);
   // BT rows of active velocity DOFs
-  const bool act = lane < NU_LOC && my_r < op.nact;
-  start = act ? op.bt_rowptr[my_r] : 0;
-  len = act ? op.bt_rowptr[my_r + 1] - start : 0;
-  off[lane] = warp_excl_scan(len, lane, total);
-  st[lane] = start;
-  __syncwarp();
-  flat_rows<T, 1, U>(st, off, NU_LOC, total, op.bt_col, op.bt, p, p, p, acc, lane);
-  __syncwarp();
+  const bool act = vu && my_r < op.nact;
+  total = seg_setup<VEC>(tab, lane, act, act ? op.bt_rowptr[my_r] : 0,
+                         act ? op.bt_rowptr[my_r + 1] : 0);
+  flat_rows<T, 1, VEC, U>(tab, NU_LOC, total, op.bt_col, op.bt, p, p, p, acc, lane);
   // B rows of the cell's pressure DOFs
-  start = lane < NP_LOC ? op.b_rowptr[my_p] : 0;
-  len = lane < NP_LOC ? op.b_rowptr[my_p + 1] - start : 0;
-  off[lane] = warp_excl_scan(len, lane, total);
-  st[lane] = start;
-  __syncwarp();
-  flat_rows<T, 2, U>(st, off, NP_LOC, total, op.b_col, op.b, u1, u2, u3, acc + 3 * NU_LOC, lane);
+  total = seg_setup<VEC>(tab, lane, vp, vp ? op.b_rowptr[my_p] : 0, vp ? op.b_rowptr[my_p + 1] : 0);
+  flat_rows<T, 2, VEC, U>(tab, NP_LOC, total, op.b_col, op.b, u1, u2, u3, acc + 3 * NU_LOC, lane);
   __syncwarp();
   T *R = rbuf + (size_t)slot * kRStride;
-  if (lane < NU_LOC) {
+  if (vu) {
     R[lane] = rhs[my_r] - acc[lane];
     R[lane + NU_LOC] = rhs[nu + my_r] - acc[lane + NU_LOC];
     R[lane + 2 * NU_LOC] = rhs[2 * nu + my_r] - acc[lane + 2 * NU_LOC];
   }
-  if (lane < NP_LOC) R[3 * NU_LOC + lane] = rhs[3 * nu + my_p] - acc[3 * NU_LOC + lane];
+  if (vp) R[3 * NU_LOC + lane] = rhs[3 * nu + my_p] - acc[3 * NU_LOC + lane];
 }
 
 template <typename T>
@@ -713,9 +765,11 @@ template <typename T>
 int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
                           const T *u, const T *rhs, T *rbuf, cudaStream_t s) {
   if (ncol <= 0) return 0;
-  constexpr int U = sizeof(T) == 4 ? 4 : 2;
+  constexpr int VEC = sizeof(T) == 4 ? 4 : 2;
+  constexpr int U = sizeof(T) == 4 ? 1 : 2;
   const int grid = (ncol + kResWarps - 1) / kResWarps;
-  k_vanka_residual<T, U><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list, ncol, u, rhs, rbuf);
+  k_vanka_residual<T, VEC, U><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list, ncol, u, rhs,
+                                                             rbuf);
   return ok() < 0 ? -1 : 1;
 }
 
