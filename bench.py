@@ -228,7 +228,7 @@ def main():
         for _ in range(args.warmup):
             step(S)
         barrier()
-        profile = prec == "mixed"
+        profile = True
         if profile:
             S.profile(True)
         launches0 = S.kernel_launches
@@ -321,7 +321,10 @@ def main():
                    "l2": "inputs (11.7 GB of matrices) larger than L2", "parallelism": "replicas"},
         "fp64": {"value": results["fp64"]["ms"] * 1e-3, "iterations": results["fp64"]["iterations"],
                  "factor_ms": results["fp64"]["factor_ms"], "solve_ms": results["fp64"]["solve_ms"],
-                 "rel_res": results["fp64"]["rel_res"]},
+                 "rel_res": results["fp64"]["rel_res"],
+                 "sweep_kernels": {k: {"ms_total": v["ms"], "launches": v["launches"],
+                                       "achieved_gbs": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] else None}
+                                   for k, v in results["fp64"].get("profile", {}).items()}},
         "mixed": {k: results["mixed"][k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res", "wall_ms")},
         "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "roofline": roof,

@@ -91,6 +91,10 @@ typedef struct {
                              ctor does, src/FE/NSE_MGLevel4.C:168-188) so that
                              pm_update_matrices copies at full link speed; the
                              arrays stay registered until pm_destroy          */
+  int vanka_inverse;      /* mixed only: store each local block as its FP32
+                             inverse (computed from the FP64 LU) so that the
+                             sweep applies it as a GEMV; 0 (default) keeps
+                             the FP32 LU factors and substitution            */
 } pm_options;
 
 /* One multigrid level in the reference's data layout.  Levels are added

@@ -38,7 +38,7 @@ class PmOptions(C.Structure):
         ("restart", C.c_int), ("maxit", C.c_int), ("minit", C.c_int),
         ("red_factor", C.c_double), ("res_norm_min", C.c_double), ("div_factor", C.c_double),
         ("device", C.c_int), ("use_graphs", C.c_int), ("verbose", C.c_int),
-        ("pin_host", C.c_int),
+        ("pin_host", C.c_int), ("vanka_inverse", C.c_int),
     ]
 
 

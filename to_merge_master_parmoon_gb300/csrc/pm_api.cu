@@ -225,6 +225,8 @@ pm_status upload(pm_handle *h, T **dst, const T *src, size_t count) {
   } while (0)
 
 bool mixed(const pm_handle *h) { return h->opt.precision == PM_PREC_MIXED; }
+// mixed mode stores each local block's FP32 inverse unless told otherwise
+bool use_inverse(const pm_handle *h) { return mixed(h) && h->opt.vanka_inverse != 0; }
 
 pm_status sync(pm_handle *h, const char *what) {
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return cuda_fail(h, what);
@@ -274,7 +276,7 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
                                        static_cast<T *>(Lv.dbuf), h->stream));
     if (e1) cudaEventRecord(e1, h->stream);
     PM_LAUNCH(launch_vanka_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
-                                    static_cast<const T *>(Lv.factors), Lv.perm,
+                                    static_cast<const T *>(Lv.factors), Lv.perm, use_inverse(h),
                                     static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
     if (e2) {
       cudaEventRecord(e2, h->stream);
@@ -549,10 +551,11 @@ pm_status factor_all(pm_handle *h) {
     LevelDev &Lv = h->L[l];
     if (mixed(h))
       PM_LAUNCH(launch_vanka_factor<float>(Lv.op<double>(), Lv.cells(), static_cast<float *>(Lv.factors),
-                                           Lv.perm, h->opt.factor_fp32 != 0, h->status_d, h->stream));
+                                           Lv.perm, h->opt.factor_fp32 != 0, use_inverse(h),
+                                           h->status_d, h->stream));
     else
       PM_LAUNCH(launch_vanka_factor<double>(Lv.op<double>(), Lv.cells(), static_cast<double *>(Lv.factors),
-                                            Lv.perm, false, h->status_d, h->stream));
+                                            Lv.perm, false, false, h->status_d, h->stream));
   }
   LevelDev &C = h->L[0];
   PM_LAUNCH(launch_coarse_assemble(C.op<double>(), h->coarse_lu, h->opt.project_pressure, h->stream));
@@ -669,6 +672,7 @@ void pm_default_options(pm_options *o) {
   o->use_graphs = 1;
   o->verbose = 0;
   o->pin_host = 0;
+  o->vanka_inverse = 0;
 }
 
 const char *pm_status_string(int s) {

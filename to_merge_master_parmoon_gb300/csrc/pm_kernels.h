@@ -101,9 +101,12 @@ int launch_check_finite(const double *x, int n, int *flag, cudaStream_t s);
 // pivoting (FP64, or FP32 with factor_fp32), store the factors column-major
 // in TF with the reciprocal of U's diagonal on the diagonal, and the row
 // permutation as uint8 (row i of PA = row perm[i] of A).
+// With inverse (FP32 storage only) the stored block is A^{-1} (column-major),
+// computed in FP32 from the LU factors; perm is still written.
 template <typename TF>
 int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *factors,
-                        uint8_t *perm, bool factor_fp32, int *status, cudaStream_t s);
+                        uint8_t *perm, bool factor_fp32, bool inverse, int *status,
+                        cudaStream_t s);
 // For the ncol cells listed in cell_list: local residual r = f - K u over the
 // full rows of the cell's 85 DOFs -> rbuf[slot*kRStride + i].
 template <typename T>
@@ -113,8 +116,8 @@ int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *
 // same cells (run after launch_vanka_residual of the whole colour).
 template <typename T>
 int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
-                       const T *factors, const uint8_t *perm, const T *rbuf, T damp, T *u,
-                       cudaStream_t s);
+                       const T *factors, const uint8_t *perm, bool inverse, const T *rbuf,
+                       T damp, T *u, cudaStream_t s);
 
 // ----------------------------------------------------------------- coarse --
 // Dense column-major N x N coarse saddle matrix of SolveExact

@@ -43,8 +43,12 @@ __device__ __forceinline__ T ld_stream(const T *p) {
 // exactly the reference's System layout.  Right-looking LU with partial
 // pivoting (first maximal |pivot|, dgetrf's choice).
 constexpr int kFactorThreads = 256;
+// float offset of the inverse's workspace (16-byte aligned, after the float
+// copy of the factors); 2 * (85*85+3) floats = 57,824 bytes of shared memory
+constexpr int kInvYOffset = NLOC * NLOC + 3;
+constexpr size_t kInvSmem = sizeof(float) * 2 * kInvYOffset;
 
-template <typename TC, typename TF>
+template <typename TC, typename TF, bool INV>
 __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> op, DevCells cells,
                                                                  TF *__restrict__ factors,
                                                                  uint8_t *__restrict__ perm,
@@ -179,11 +183,58 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
     __syncthreads();
   }
   TF *F = factors + (size_t)cell * NLOC * NLOC;
-  for (int t = tid; t < NLOC * NLOC; t += kFactorThreads) {
-    const int i = t % NLOC, j = t / NLOC;
-    TC v = S[t];
-    if (i == j) v = (v != TC(0)) ? TC(1) / v : TC(0);
-    F[t] = (TF)v;
+  if (INV) {
+    // A^{-1} = U^{-1} L^{-1} P in FP32 from the factors, all 85 right-hand
+    // sides at once: a float copy of L\U overlays S, Y holds P then A^{-1}
+    // (column-major), both inside the same 57.8 KB of shared memory.
+    float *Lf = reinterpret_cast<float *>(smem_raw);
+    float *Y = reinterpret_cast<float *>(smem_raw) + kInvYOffset;
+    constexpr int PER = (NLOC * NLOC + kFactorThreads - 1) / kFactorThreads;
+    float tmp[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int t = tid + q * kFactorThreads;
+      tmp[q] = t < NLOC * NLOC ? (float)S[t] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int t = tid + q * kFactorThreads;
+      if (t < NLOC * NLOC) Lf[t] = tmp[q];
+    }
+    for (int t = tid; t < NLOC * NLOC; t += kFactorThreads) {
+      const int i = t % NLOC, j = t / NLOC;
+      Y[t] = (pm[i] == j) ? 1.f : 0.f;
+    }
+    __syncthreads();
+    for (int k = 0; k < NLOC - 1; ++k) {  // unit lower triangle
+      for (int j = warp; j < NLOC; j += nwarps) {
+        const float ykj = Y[j * NLOC + k];
+        if (ykj != 0.f)
+          for (int i = k + 1 + lane; i < NLOC; i += 32) Y[j * NLOC + i] -= Lf[k * NLOC + i] * ykj;
+      }
+      __syncthreads();
+    }
+    for (int k = NLOC - 1; k >= 0; --k) {  // upper triangle
+      const float d = Lf[k * NLOC + k];
+      const float rd = d != 0.f ? 1.f / d : 0.f;
+      for (int j = tid; j < NLOC; j += kFactorThreads) Y[j * NLOC + k] *= rd;
+      __syncthreads();
+      for (int j = warp; j < NLOC; j += nwarps) {
+        const float xkj = Y[j * NLOC + k];
+        if (xkj != 0.f)
+          for (int i = lane; i < k; i += 32) Y[j * NLOC + i] -= Lf[k * NLOC + i] * xkj;
+      }
+      __syncthreads();
+    }
+    for (int t = tid; t < NLOC * NLOC; t += kFactorThreads) F[t] = (TF)Y[t];
+  } else {
+    for (int t = tid; t < NLOC * NLOC; t += kFactorThreads) {
+      const int i = t % NLOC, j = t / NLOC;
+      TC v = S[t];
+      if (i == j) v = (v != TC(0)) ? TC(1) / v : TC(0);
+      F[t] = (TF)v;
+    }
   }
   if (tid < NLOC) perm[(size_t)cell * NLOC + tid] = pm[tid];
   if (tid == 0 && singular) atomicOr(status, 1);
@@ -425,6 +476,39 @@ __device__ __forceinline__ void scatter_local(int i, T v, const int *ud, const i
   } else {
     u[(size_t)3 * nu + pd[i - 3 * NU_LOC]] += v;
   }
+}
+
+// Mixed-precision apply with the stored FP32 inverse: delta = A^{-1} r, a
+// dense 85x85 GEMV whose column loads are all independent (no substitution
+// chain), then u[dofs] += damp * delta.
+template <typename T>
+__global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply_inv(
+    DevCells cells, int nu, const int *__restrict__ list, int ncol, const T *__restrict__ X,
+    const T *__restrict__ rbuf, T damp, T *__restrict__ u) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = blockIdx.x * kApplyWarps + warp;
+  if (slot >= ncol) return;
+  const int cell = list[slot];
+  const bool has2 = lane + 64 < NLOC;
+  const T *R = rbuf + (size_t)slot * kRStride;
+  const T r0 = R[lane], r1 = R[lane + 32], r2 = has2 ? R[lane + 64] : T(0);
+  const T *Xc = X + (size_t)cell * NLOC * NLOC;
+  T a0 = 0, a1 = 0, a2 = 0;
+#pragma unroll 17
+  for (int j = 0; j < NLOC; ++j) {
+    const T *col = Xc + (size_t)j * NLOC;
+    const T x0 = ld_stream(col + lane), x1 = ld_stream(col + lane + 32);
+    const T x2 = has2 ? ld_stream(col + lane + 64) : T(0);
+    const T rj = __shfl_sync(kFull, (j < 32) ? r0 : ((j < 64) ? r1 : r2), j & 31);
+    a0 += x0 * rj;
+    a1 += x1 * rj;
+    a2 += x2 * rj;
+  }
+  const int *ud = cells.udofs + (size_t)cell * NU_LOC;
+  const int *pd = cells.pdofs + (size_t)cell * NP_LOC;
+  scatter_local(lane, damp * a0, ud, pd, nu, u);
+  scatter_local(lane + 32, damp * a1, ud, pd, nu, u);
+  if (has2) scatter_local(lane + 64, damp * a2, ud, pd, nu, u);
 }
 
 template <typename T>
@@ -741,24 +825,28 @@ inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 
 }  // namespace
 
+template <typename TC, typename TF, bool INV>
+int launch_factor_impl(const DevOp<double> &op, const DevCells &cells, TF *factors, uint8_t *perm,
+                       int *status, cudaStream_t s) {
+  size_t sm = sizeof(TC) * NLOC * NLOC;
+  if (INV && sm < kInvSmem) sm = kInvSmem;
+  cudaFuncSetAttribute(k_vanka_factor<TC, TF, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sm);
+  k_vanka_factor<TC, TF, INV><<<cells.ncells, kFactorThreads, sm, s>>>(op, cells, factors, perm,
+                                                                      status);
+  return ok() < 0 ? -1 : 1;
+}
+
 template <typename TF>
 int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, uint8_t *perm,
-                        bool factor_fp32, int *status, cudaStream_t s) {
+                        bool factor_fp32, bool inverse, int *status, cudaStream_t s) {
   if (cells.ncells <= 0) return 0;
-  if (factor_fp32) {
-    const size_t sm = sizeof(float) * NLOC * NLOC;
-    cudaFuncSetAttribute(k_vanka_factor<float, TF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
-    k_vanka_factor<float, TF><<<cells.ncells, kFactorThreads, sm, s>>>(op, cells, factors, perm,
-                                                                      status);
-  } else {
-    const size_t sm = sizeof(double) * NLOC * NLOC;
-    cudaFuncSetAttribute(k_vanka_factor<double, TF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
-    k_vanka_factor<double, TF><<<cells.ncells, kFactorThreads, sm, s>>>(op, cells, factors, perm,
-                                                                       status);
+  if (inverse && sizeof(TF) == sizeof(float)) {
+    return factor_fp32 ? launch_factor_impl<float, TF, true>(op, cells, factors, perm, status, s)
+                       : launch_factor_impl<double, TF, true>(op, cells, factors, perm, status, s);
   }
-  return ok() < 0 ? -1 : 1;
+  return factor_fp32 ? launch_factor_impl<float, TF, false>(op, cells, factors, perm, status, s)
+                     : launch_factor_impl<double, TF, false>(op, cells, factors, perm, status, s);
 }
 
 template <typename T>
@@ -775,12 +863,16 @@ int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *
 
 template <typename T>
 int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
-                       const T *factors, const uint8_t *perm, const T *rbuf, T damp, T *u,
-                       cudaStream_t s) {
+                       const T *factors, const uint8_t *perm, bool inverse, const T *rbuf, T damp,
+                       T *u, cudaStream_t s) {
   if (ncol <= 0) return 0;
   const int grid = (ncol + kApplyWarps - 1) / kApplyWarps;
-  k_vanka_apply<T><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors, perm,
-                                                    rbuf, damp, u);
+  if (inverse)
+    k_vanka_apply_inv<T><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors,
+                                                          rbuf, damp, u);
+  else
+    k_vanka_apply<T><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors, perm,
+                                                      rbuf, damp, u);
   return ok() < 0 ? -1 : 1;
 }
 
@@ -834,14 +926,14 @@ int launch_dense_solve(const double *lu, const int *ipiv, int n, const double *b
 }
 
 template int launch_vanka_factor<double>(const DevOp<double> &, const DevCells &, double *,
-                                         uint8_t *, bool, int *, cudaStream_t);
+                                         uint8_t *, bool, bool, int *, cudaStream_t);
 template int launch_vanka_factor<float>(const DevOp<double> &, const DevCells &, float *,
-                                        uint8_t *, bool, int *, cudaStream_t);
+                                        uint8_t *, bool, bool, int *, cudaStream_t);
 #define PM_VINST(T)                                                                                 \
   template int launch_vanka_residual<T>(const DevOp<T> &, const DevCells &, const int *, int,      \
                                         const T *, const T *, T *, cudaStream_t);                  \
   template int launch_vanka_apply<T>(const DevCells &, int, const int *, int, const T *,           \
-                                     const uint8_t *, const T *, T, T *, cudaStream_t);
+                                     const uint8_t *, bool, const T *, T, T *, cudaStream_t);
 PM_VINST(double)
 PM_VINST(float)
 #undef PM_VINST
