@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--train-problems", type=int, default=8)
     return ap.parse_args()
 
 
@@ -174,6 +175,44 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def train_network(device, args, log=None):
+    """The learned smoother's network: (residual, error) pairs harvested from
+    plain FP64 solves of 32^3 problems with nu log-uniform in [1e-3, 1e-1]
+    (seeds 1000+k), AdamW lr 1e-3, 20 epochs, all on the GPU.  Cached in the
+    package's build folder keyed by the training configuration."""
+    import hashlib
+
+    import numpy as np
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    from to_merge_master_parmoon_gb300.learned import Mlp, harvest_pairs, relative_loss, train
+    cfg = dict(levels=5, problems=args.train_problems, cycles=8, epochs=20, batch=4096, lr=1e-3,
+               seed=0, nu_range=(1e-3, 1e-1))
+    key = hashlib.sha1(json.dumps(cfg, sort_keys=True).encode()).hexdigest()[:12]
+    cache = ROOT / "to_merge_master_parmoon_gb300" / "_build" / f"mlp_{key}.npy"
+    net = Mlp(device=device, seed=cfg["seed"], max_batch=cfg["batch"])
+    info = {"config": cfg, "cached": cache.exists()}
+    if cache.exists():
+        net.set_params(np.load(cache))
+        return net, info
+    rng = np.random.default_rng(cfg["seed"])
+    lo, hi = np.log10(cfg["nu_range"][0]), np.log10(cfg["nu_range"][1])
+    t = time.perf_counter()
+    probs = [OseenProblem(n_levels=cfg["levels"], nu=float(10 ** rng.uniform(lo, hi)), seed=1000 + k)
+             for k in range(cfg["problems"])]
+    X, T = harvest_pairs(probs, n_cycles=cfg["cycles"], device=device, log=log)
+    info["harvest_s"] = time.perf_counter() - t
+    info["pairs"] = int(X.shape[0])
+    t = time.perf_counter()
+    hist = train(net, X, T, epochs=cfg["epochs"], batch=cfg["batch"], lr=cfg["lr"], seed=cfg["seed"])
+    info["train_s"] = time.perf_counter() - t
+    info["loss_first_last"] = [hist[0], hist[-1]]
+    info["relative_loss"] = relative_loss(net, X, T)
+    cache.parent.mkdir(parents=True, exist_ok=True)
+    np.save(cache, net.params())
+    del X, T
+    return net, info
+
+
 # FGMRES iterations to 1e-8 of this workload (measured on the GPU FP64 path,
 # which runs the same algorithm as the reference; used to scale the CPU sample)
 FGMRES_ITERATIONS = {(6, 1e-2): 10, (5, 1e-2): 10, (4, 1e-2): 9}
@@ -205,10 +244,14 @@ def main():
     nu3 = 3 * P.desc(args.levels - 1).n_udof
     bp[nu3::4] -= bp[nu3::4].mean()
     r0 = float(np.linalg.norm(bp))
+    # learned smoother: trained once (harvest on 32^3 problems, GPU training),
+    # outside the timed region; cached by configuration in the build folder
+    net, learned_info = train_network(local, args, log=lambda *a: print(*a, file=sys.stderr))
     solvers = {}
-    for prec in ("mixed", "fp64"):
-        solvers[prec] = PmSolver(P.descs, precision=prec, device=local, restart=20, maxit=200,
-                                 res_norm_min=RTOL * r0, pin_host=int(prec == "mixed"))
+    for name, prec in (("mixed_learned", "mixed"), ("mixed", "mixed"), ("fp64", "fp64")):
+        solvers[name] = PmSolver(P.descs, precision=prec, device=local, restart=20, maxit=200,
+                                 res_norm_min=RTOL * r0, pin_host=int(name == "mixed_learned"))
+    solvers["mixed_learned"].attach_learned(net, omega=1.0, fallback_ratio=0.5)
 
     def step(S):
         d_x.zero_()
@@ -251,9 +294,11 @@ def main():
         if profile:
             results[prec]["profile"] = S.profile_read()
             S.profile(False)
+        if prec == "mixed_learned":
+            results[prec]["learned"] = S.learned_status()
 
     # reduce: max over ranks
-    ms = results["mixed"]["ms"]
+    ms = results["mixed_learned"]["ms"]
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device="cuda")
@@ -263,7 +308,7 @@ def main():
     # end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
-        S = solvers["mixed"]
+        S = solvers["mixed_learned"]
         x = np.zeros(n)
         h2d = 0
         for lv in range(P.n_levels):
@@ -317,7 +362,8 @@ def main():
         "config": {"workload": f"steady 3D Oseen, Q2/P1disc, {2 ** nlev}^3 cells, {nlev} levels "
                                f"from 2^3, nu={args.nu}, FGMRES(20)+V(2,2) cell Vanka, rtol 1e-8",
                    "ndof": n, "precision": "mixed: FP32 V-cycle + FP32-stored FP64-computed "
-                                           "local LU, FP64 FGMRES/coarse",
+                                           "local LU, FP64 FGMRES/coarse; learned: BF16 MLP "
+                                           "post-smoothing step on every level",
                    "l2": "inputs (11.7 GB of matrices) larger than L2", "parallelism": "replicas"},
         "fp64": {"value": results["fp64"]["ms"] * 1e-3, "iterations": results["fp64"]["iterations"],
                  "factor_ms": results["fp64"]["factor_ms"], "solve_ms": results["fp64"]["solve_ms"],
@@ -325,13 +371,19 @@ def main():
                  "sweep_kernels": {k: {"ms_total": v["ms"], "launches": v["launches"],
                                        "achieved_gbs": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] else None}
                                    for k, v in results["fp64"].get("profile", {}).items()}},
-        "mixed": {k: results["mixed"][k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res", "wall_ms")},
+        "mixed": {"value": results["mixed"]["ms"] * 1e-3,
+                  **{k: results["mixed"][k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res")}},
+        "mixed_learned": {**{k: results["mixed_learned"][k]
+                             for k in ("factor_ms", "solve_ms", "iterations", "rel_res", "wall_ms")},
+                          "learned_status": results["mixed_learned"].get("learned"),
+                          "training": learned_info},
+        "speedup_vs_fp64": results["fp64"]["ms"] / results["mixed_learned"]["ms"],
         "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": results["mixed"]["launches"],
-        "clocks": {k: results["mixed"]["clocks"][k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
+        "gpu_launches": results["mixed_learned"]["launches"],
+        "clocks": {k: results["mixed_learned"]["clocks"][k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
     }
     print(json.dumps(line), flush=True)
 

@@ -205,6 +205,53 @@ pm_status pm_profile_enable(pm_handle *h, int enable);
 pm_status pm_profile_read(pm_handle *h, int kernel, double *ms_total, long long *launches,
                           double *bytes_total);
 
+/* ---------------------------------------------------------------------------
+ * Learned smoother (no counterpart in the reference: an addition to
+ * TNSE_MultiGrid::Cycle's post-smoothing, src/FE/NSE_MultiGrid.C:1608-1742).
+ * A per-cell MLP 397 -> 256 -> 256 -> 85 (GELU; BF16 weights/activations,
+ * FP32 accumulation on the tensor cores) maps a cell's scaled local residual
+ * plus 26 neighbour residual summaries (12 each) to a correction of the
+ * cell's 85 DOFs.  Attached to a handle, it runs as one extra post-smoothing
+ * step on every level; FGMRES switches it off for the rest of a solve when
+ * the residual reduction of an iteration is worse than fallback_ratio, so
+ * plain cell Vanka is the fallback.
+ * Feature vector of cell c (divided by s_c = rms of its 85 local residual
+ * entries): [local residual in local DOF order (u1 nodes, u2, u3, p modes)] then,
+ * for each neighbour slot n = 0..25 (offsets (dx,dy,dz) in {-1,0,1}^3 \ 0,
+ * slot order dx fastest), the neighbour's summary: mean r_u1, r_u2, r_u3
+ * over its 27 nodes, rms of each, its 4 pressure residuals, rms of all 85,
+ * mean |r_u|.  Targets: the error at the cell's 85 DOFs divided by s_c. */
+typedef struct pm_mlp pm_mlp;
+enum { PM_MLP_IN = 397, PM_MLP_HIDDEN = 256, PM_MLP_OUT = 85 };
+
+pm_status pm_mlp_create(pm_mlp **m, int device, unsigned long long seed, int max_batch);
+pm_status pm_mlp_destroy(pm_mlp *m);
+long long pm_mlp_num_params(void);  /* FP32 parameter vector length (padded layout) */
+pm_status pm_mlp_get_params(pm_mlp *m, float *host, long long n);
+pm_status pm_mlp_set_params(pm_mlp *m, const float *host, long long n);
+/* d_X [M x 397] FP32 (device) -> d_Y [M x 85] FP32 (device), BF16 compute */
+pm_status pm_mlp_forward(pm_mlp *m, const float *d_X, int M, float *d_Y);
+/* MSE loss of the batch and its gradient (kept in the object; copied to
+ * host_grad when non-NULL, length pm_mlp_num_params()) */
+pm_status pm_mlp_loss_grad(pm_mlp *m, const float *d_X, const float *d_T, int M, double *loss,
+                           float *host_grad);
+/* one AdamW step with the last gradient (bias-corrected moments, decoupled
+ * weight decay on weights, not biases) */
+pm_status pm_mlp_adamw_step(pm_mlp *m, float lr, float beta1, float beta2, float eps,
+                            float weight_decay);
+/* attach (m != NULL) or detach the network; omega scales the correction */
+pm_status pm_learned_attach(pm_handle *h, pm_mlp *m, double omega, double fallback_ratio);
+/* Training pairs from the plain solver on the finest level: starting from
+ * u = 0 it runs n_cycles iterations u += Vcycle(b - K u) (the post-smoothed
+ * state of the cycle) and after each stores every cell's features and
+ * scaled error (sol_exact - u) into d_X [.. x 397] / d_T [.. x 85] from row
+ * *n_pairs on (capacity rows); *n_pairs is advanced. */
+pm_status pm_learned_harvest(pm_handle *h, const double *sol_exact, const double *rhs,
+                             int n_cycles, float *d_X, float *d_T, long long capacity,
+                             long long *n_pairs);
+/* learned step enabled now (1/0) and fallbacks since attach */
+pm_status pm_learned_status(pm_handle *h, int *enabled, int *fallbacks);
+
 /* Allocation-free L2_0 projection of a P1disc pressure vector on the device
  * (subtract the mean of the constant modes d_p[0], d_p[4], ...), for callers
  * that cannot allocate device memory where they need it: code inside CUDA

@@ -1,0 +1,142 @@
+"""Learned smoother on the GPU: the network's forward pass and gradients
+against the numpy oracle (same BF16 operand rounding; tolerance 2e-3
+relative for FP32-accumulation order), training on harvested
+(residual, error) pairs, and the solve with the learned post-smoothing step
+(parity with the plain solver's solution, fallback to plain Vanka)."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def mlp():
+    from to_merge_master_parmoon_gb300.learned import Mlp
+    m = Mlp(device=0, seed=7, max_batch=512)
+    yield m
+    m.close()
+
+
+def test_forward_and_gradients_match_oracle(mlp):
+    import torch
+    rng = np.random.default_rng(3)
+    M = 96
+    X = rng.standard_normal((M, mo.N_IN)).astype(np.float32)
+    T = rng.standard_normal((M, mo.N_OUT)).astype(np.float32)
+    P = mlp.params().astype(np.float64)
+    Xd, Td = torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda()
+    y_gpu = mlp.forward(Xd).cpu().numpy()
+    y_ref, _ = mo.forward(P, X.astype(np.float64))
+    assert rel(y_gpu, y_ref) < 2e-3
+    loss, g = mlp.loss_grad(Xd, Td, want_grad=True)
+    loss_ref, g_ref = mo.loss_grad(P, X.astype(np.float64), T.astype(np.float64))
+    assert abs(loss - loss_ref) < 1e-4 * loss_ref
+    blocks = [(mo.OFF_W1, mo.OFF_B1), (mo.OFF_B1, mo.OFF_W2), (mo.OFF_W2, mo.OFF_B2),
+              (mo.OFF_B2, mo.OFF_W3), (mo.OFF_W3, mo.OFF_B3), (mo.OFF_B3, mo.N_PARAMS)]
+    for a, b in blocks:
+        assert rel(g[a:b], g_ref[a:b]) < 2e-3, (a, rel(g[a:b], g_ref[a:b]))
+
+
+def test_adamw_step_matches_formula(mlp):
+    import torch
+    rng = np.random.default_rng(4)
+    X = torch.from_numpy(rng.standard_normal((64, mo.N_IN)).astype(np.float32)).cuda()
+    T = torch.from_numpy(rng.standard_normal((64, mo.N_OUT)).astype(np.float32)).cuda()
+    from to_merge_master_parmoon_gb300.learned import Mlp
+    m = Mlp(device=0, seed=11, max_batch=64)
+    p0 = m.params().astype(np.float64)
+    _, g = m.loss_grad(X, T, want_grad=True)
+    m.adamw(lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=1e-2)
+    p1 = m.params().astype(np.float64)
+    g = g.astype(np.float64)
+    mhat = g  # first step: bias-corrected moments equal g and g^2
+    vhat = g * g
+    bias = np.zeros(mo.N_PARAMS, bool)
+    bias[mo.OFF_B1:mo.OFF_W2] = bias[mo.OFF_B2:mo.OFF_W3] = bias[mo.OFF_B3:] = True
+    want = p0 - 1e-3 * (mhat / (np.sqrt(vhat) + 1e-8) + np.where(bias, 0.0, 1e-2 * p0))
+    assert np.max(np.abs(p1 - want)) < 1e-6
+    m.close()
+
+
+@pytest.fixture(scope="module")
+def trained(problems):
+    from to_merge_master_parmoon_gb300.learned import Mlp, harvest_pairs, relative_loss, train
+    Ps = [problems(3, nu, seed) for nu, seed in ((1e-2, 21), (3e-2, 22), (5e-3, 23))]
+    X, T = harvest_pairs(Ps, n_cycles=6)
+    m = Mlp(device=0, seed=5, max_batch=1024)
+    before = relative_loss(m, X, T)
+    hist = train(m, X, T, epochs=40, batch=512, lr=2e-3)
+    after = relative_loss(m, X, T)
+    yield m, X, T, before, after, hist
+    m.close()
+
+
+def test_harvest_and_training_reduce_loss(trained):
+    m, X, T, before, after, hist = trained
+    assert X.shape[1] == mo.N_IN and T.shape[1] == mo.N_OUT
+    assert 0.9 * 3 * 512 * 6 <= X.shape[0] <= 3 * 512 * 6  # a few outlier rows may be dropped
+    assert np.isfinite(hist).all()
+    assert hist[-1] < 0.7 * hist[0], hist
+    assert after < before, (before, after)
+
+
+def test_learned_gain_over_plain(problems, trained):
+    """What the trained network gains: FGMRES iterations and the mean
+    residual reduction per iteration with and without the learned step
+    (printed; the learned solve must still reach the tolerance)."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    m = trained[0]
+    P = problems(3, 2e-2, 31)
+    b = P.rhs()
+    nu3 = 3 * P.desc(2).n_udof
+    bp = b.copy()
+    bp[nu3::4] -= bp[nu3::4].mean()
+    r0 = np.linalg.norm(bp)
+    out = {}
+    for name, net in (("plain", None), ("learned", m)):
+        S = PmSolver(P.descs, precision="mixed", restart=20, maxit=80, res_norm_min=1e-10 * r0)
+        if net is not None:
+            S.attach_learned(net, omega=1.0, fallback_ratio=0.5)
+        x, info = S.iterate(np.zeros_like(b), b)
+        out[name] = (info["iterations"], (info["true_res"] / r0) ** (1.0 / info["iterations"]))
+        assert info["true_res"] <= 1.05e-10 * r0
+        S.close()
+    print(f"learned-smoother gain on 8^3, nu=2e-2: iterations {out['plain'][0]} -> "
+          f"{out['learned'][0]}, mean reduction/iteration {out['plain'][1]:.3f} -> "
+          f"{out['learned'][1]:.3f}")
+    assert out["learned"][0] <= out["plain"][0] + 2
+
+
+def test_learned_solve_matches_plain_solution_and_falls_back(problems, trained):
+    from to_merge_master_parmoon_gb300 import PmSolver
+    m = trained[0]
+    P = problems(3, 1e-2, 0)
+    b = P.rhs()
+    nu3 = 3 * P.desc(2).n_udof
+    bp = b.copy()
+    bp[nu3::4] -= bp[nu3::4].mean()
+    tol = 1e-10 * np.linalg.norm(bp)
+    plain = PmSolver(P.descs, precision="mixed", restart=20, maxit=80, res_norm_min=tol)
+    x0, i0 = plain.iterate(np.zeros_like(b), b)
+    S = PmSolver(P.descs, precision="mixed", restart=20, maxit=80, res_norm_min=tol)
+    S.attach_learned(m, omega=1.0, fallback_ratio=0.5)
+    x1, i1 = S.iterate(np.zeros_like(b), b)
+    assert i1["true_res"] <= 1.05 * tol
+    for v in (x0, x1):
+        v[nu3::4] -= v[nu3::4].mean()
+    assert rel(x1, x0) < 1e-6
+    # a fallback ratio of 0 switches the learned step off after the first iteration
+    S.attach_learned(m, omega=1.0, fallback_ratio=0.0)
+    x2, i2 = S.iterate(np.zeros_like(b), b)
+    st = S.learned_status()
+    assert st["fallbacks"] >= 1 and st["enabled"] == 0
+    assert i2["true_res"] <= 1.05 * tol
+    S.attach_learned(None)
+    S.close()
+    plain.close()

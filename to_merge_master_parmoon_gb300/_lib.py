@@ -96,6 +96,19 @@ GPU_SYMBOLS = {
     "pm_profile_enable": (C.c_int, [_P, C.c_int]),
     "pm_profile_read": (C.c_int, [_P, C.c_int, c_double_p, C.POINTER(C.c_longlong), c_double_p]),
     "pm_l20_project_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "pm_mlp_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_ulonglong, C.c_int]),
+    "pm_mlp_destroy": (C.c_int, [_P]),
+    "pm_mlp_num_params": (C.c_longlong, []),
+    "pm_mlp_get_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong]),
+    "pm_mlp_set_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong]),
+    "pm_mlp_forward": (C.c_int, [_P, C.c_void_p, C.c_int, C.c_void_p]),
+    "pm_mlp_loss_grad": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_int, c_double_p,
+                                   C.POINTER(C.c_float)]),
+    "pm_mlp_adamw_step": (C.c_int, [_P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
+    "pm_learned_attach": (C.c_int, [_P, _P, C.c_double, C.c_double]),
+    "pm_learned_harvest": (C.c_int, [_P, c_double_p, c_double_p, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_longlong, C.POINTER(C.c_longlong)]),
+    "pm_learned_status": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
 }
 
 HOST_SYMBOLS = {

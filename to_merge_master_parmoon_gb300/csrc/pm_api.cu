@@ -21,8 +21,13 @@
 #include <vector>
 
 #include "pm_kernels.h"
+#include "pm_learned.h"
 #include "pm_setup_host.h"
 #include "pmgpu.h"
+
+struct pm_mlp {
+  pm::Mlp m;
+};
 
 using namespace pm;
 
@@ -64,6 +69,13 @@ struct LevelDev {
   double *x64 = nullptr, *y64 = nullptr, *z64 = nullptr;
   // unique bytes of one Vanka sweep per cell, split by kernel (see pm_setup)
   double vanka_res_bytes = 0.0, vanka_apply_bytes = 0.0;
+  // learned smoother buffers (allocated on first attach / harvest)
+  bool l_ready = false;
+  int *l_nbr = nullptr;
+  float *l_inv_mult = nullptr, *l_summary = nullptr, *l_Y = nullptr, *l_scale = nullptr;
+  __nv_bfloat16 *l_X = nullptr, *l_H1 = nullptr, *l_H2 = nullptr;
+  void *l_corr = nullptr, *l_q = nullptr, *l_zero = nullptr;  // V-cycle precision
+  double *l_omega = nullptr;                                   // step length (device)
 
   template <typename T>
   DevOp<T> op() const;
@@ -132,9 +144,10 @@ struct pm_handle {
   // FGMRES storage
   int restart = 0;
   double *V = nullptr, *Z = nullptr, *w = nullptr, *xd = nullptr, *bd = nullptr;
-  // V-cycle graph
-  cudaGraphExec_t vgraph = nullptr;
-  long long vgraph_kernels = 0;
+  // V-cycle graphs: [0] plain, [1] with the learned step
+  cudaGraphExec_t vgraph_g[2] = {nullptr, nullptr};
+  long long vgraph_kernels_g[2] = {0, 0};
+  bool l_active = false;  // the cycle being run / captured includes the learned step
   // profiling of the Vanka solve kernel
   bool prof = false;
   std::vector<cudaEvent_t> evpool;
@@ -145,6 +158,12 @@ struct pm_handle {
   long long prof_launches[2] = {0, 0};
   double last_factor_ms = 0.0;
   std::vector<void *> pinned;
+  // learned smoother (borrowed network), device on/off flag read by its kernels
+  pm::Mlp *mlp = nullptr;
+  double l_omega = 1.0, l_fallback = 0.5;
+  int *d_on = nullptr;
+  int l_on_host = 0;
+  int l_fallbacks = 0;
 };
 
 namespace {
@@ -300,6 +319,67 @@ pm_status coarse_solve(pm_handle *h, LevelDev &Lv, const T *rhs, T *u) {
   return PM_OK;
 }
 
+// Per-level buffers of the learned step: neighbour slots, inverse node
+// multiplicities, cell summaries, BF16 features and activations, outputs.
+pm_status ensure_learned_buffers(pm_handle *h, LevelDev &Lv) {
+  if (Lv.l_ready || Lv.ncells == 0) return PM_OK;
+  std::vector<int> nbr;
+  build_neighbours(Lv.ncells, Lv.h_udofs.data(), Lv.nu, nbr);
+  std::vector<float> inv;
+  node_inverse_multiplicity(Lv.ncells, Lv.h_udofs.data(), Lv.nu, inv);
+  PM_TRY(upload(h, &Lv.l_nbr, nbr.data(), nbr.size()));
+  PM_TRY(upload(h, &Lv.l_inv_mult, inv.data(), inv.size()));
+  const size_t nc = (size_t)Lv.ncells;
+  PM_TRY(dalloc(h, &Lv.l_summary, nc * kSummary));
+  PM_TRY(dalloc(h, &Lv.l_scale, nc));
+  PM_TRY(dalloc(h, &Lv.l_Y, nc * kMlpOutPad));
+  PM_TRY(dalloc(h, &Lv.l_X, nc * kMlpInPad));
+  PM_TRY(dalloc(h, &Lv.l_H1, nc * kMlpHidden));
+  PM_TRY(dalloc(h, &Lv.l_H2, nc * kMlpHidden));
+  const size_t es = mixed(h) ? sizeof(float) : sizeof(double);
+  PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.l_corr), (size_t)Lv.ndof * es));
+  PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.l_q), (size_t)Lv.ndof * es));
+  PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.l_zero), (size_t)Lv.ndof * es));
+  PM_TRY(dalloc(h, &Lv.l_omega, 1));
+  if (cudaMemsetAsync(Lv.l_zero, 0, (size_t)Lv.ndof * es, h->stream) != cudaSuccess)
+    return cuda_fail(h, "zero vector");
+  PM_TRY(sync(h, "learned buffers"));
+  Lv.l_ready = true;
+  return PM_OK;
+}
+
+// Learned post-smoothing step on one level: d = f - K u, cell features,
+// MLP, u += omega * (cell corrections averaged over the cells sharing a DOF)
+// colour by colour (no two cells of a colour share a DOF).  All kernels read
+// the device flag h->d_on and do nothing when it is 0.
+template <typename T>
+pm_status learned_step(pm_handle *h, LevelDev &C, T *u, const T *f) {
+  T *d = static_cast<T *>(C.def);
+  PM_TRY(level_defect<T>(h, C, u, f, d));
+  const DevCells cells = C.cells();
+  PM_LAUNCH(launch_cell_summary<T>(cells, C.nu, d, C.l_summary, h->d_on, h->stream));
+  PM_LAUNCH(launch_cell_features<T>(cells, C.nu, d, C.l_summary, C.l_nbr, C.l_X, nullptr,
+                                    C.l_scale, h->d_on, h->stream));
+  PM_LAUNCH(mlp_forward(*h->mlp, C.l_X, C.ncells, C.l_H1, C.l_H2, C.l_Y, h->stream, h->d_on));
+  // correction c = cell predictions averaged over the cells sharing a DOF
+  T *c = static_cast<T *>(C.l_corr), *q = static_cast<T *>(C.l_q);
+  PM_LAUNCH(launch_fill<T>(c, T(0), C.ndof, h->stream));
+  const int ncol = (int)C.colouring.ptr.size() - 1;
+  for (int k = 0; k < ncol; ++k) {
+    const int b = C.colouring.ptr[k], n = C.colouring.ptr[k + 1] - b;
+    PM_LAUNCH(launch_learned_apply<T>(cells, C.nu, C.nact, C.colour_cells + b, n, C.l_Y,
+                                      C.l_scale, C.l_inv_mult, T(1), c, h->d_on, h->stream));
+  }
+  // minimal-residual step length (as TNSE_MGLevel4::StepLengthControl
+  // damps a correction, src/FE/NSE_MGLevel4.C:5878): q = P(0 - K c),
+  // omega = argmin ||d + omega q|| in [0, omega_max], u += omega c
+  PM_TRY(level_defect<T>(h, C, c, static_cast<const T *>(C.l_zero), q));
+  PM_LAUNCH(launch_mr_step<T>(d, q, C.ndof, h->partials, h->counter, h->l_omega, C.l_omega,
+                              h->d_on, h->stream));
+  PM_LAUNCH(launch_axpy_dev<T>(u, C.l_omega, c, C.ndof, h->d_on, h->stream));
+  return PM_OK;
+}
+
 // TNSE_MultiGrid::Cycle (V-cycle, cell Vanka, coarse SolveExact)
 template <typename T>
 pm_status cycle(pm_handle *h, int i) {
@@ -328,6 +408,7 @@ pm_status cycle(pm_handle *h, int i) {
   PM_LAUNCH(launch_axpy<T>(u, (T)h->opt.beta, d, C.ndof, h->stream));
   PM_LAUNCH(launch_dirichlet<T>(u, (const T *)nullptr, C.nu, C.hb, C.ndir, h->stream));
   for (int s = 0; s < h->opt.post_smooth; ++s) PM_TRY(vanka_sweep<T>(h, C, u, f));
+  if (h->l_active) PM_TRY(learned_step<T>(h, C, u, f));
   return PM_OK;
 }
 
@@ -342,9 +423,22 @@ pm_status vcycle_core(pm_handle *h) {
   return cycle<T>(h, (int)h->L.size() - 1);
 }
 
+void drop_graphs(pm_handle *h) {
+  for (int k = 0; k < 2; ++k)
+    if (h->vgraph_g[k]) {
+      cudaGraphExecDestroy(h->vgraph_g[k]);
+      h->vgraph_g[k] = nullptr;
+    }
+}
+
+// One V-cycle; with a network attached and enabled the cycle includes the
+// learned post-smoothing step.  The plain and the learned cycle are each
+// captured once into their own graph.
 pm_status run_vcycle_core(pm_handle *h) {
+  h->l_active = h->mlp != nullptr && h->l_on_host != 0;
+  const int gi = h->l_active ? 1 : 0;
   if (h->opt.use_graphs && !h->prof) {
-    if (!h->vgraph) {
+    if (!h->vgraph_g[gi]) {
       cudaGraph_t g = nullptr;
       const long long before = h->launches;
       if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
@@ -356,16 +450,17 @@ pm_status run_vcycle_core(pm_handle *h) {
         return s;
       }
       if (e != cudaSuccess) return cuda_fail(h, "end capture");
-      h->vgraph_kernels = h->launches - before;
+      h->vgraph_kernels_g[gi] = h->launches - before;
       h->launches = before;
-      if (cudaGraphInstantiate(&h->vgraph, g, 0) != cudaSuccess) {
+      if (cudaGraphInstantiate(&h->vgraph_g[gi], g, 0) != cudaSuccess) {
         cudaGraphDestroy(g);
         return cuda_fail(h, "graph instantiate");
       }
       cudaGraphDestroy(g);
     }
-    if (cudaGraphLaunch(h->vgraph, h->stream) != cudaSuccess) return cuda_fail(h, "graph launch");
-    h->launches += h->vgraph_kernels;
+    if (cudaGraphLaunch(h->vgraph_g[gi], h->stream) != cudaSuccess)
+      return cuda_fail(h, "graph launch");
+    h->launches += h->vgraph_kernels_g[gi];
     return PM_OK;
   }
   return mixed(h) ? vcycle_core<float>(h) : vcycle_core<double>(h);
@@ -385,6 +480,15 @@ pm_status precondition(pm_handle *h, double *z, const double *v) {
   else if (cudaMemcpyAsync(z, F.sol, sizeof(double) * F.ndof, cudaMemcpyDeviceToDevice,
                            h->stream) != cudaSuccess)
     return cuda_fail(h, "sol copy");
+  return PM_OK;
+}
+
+pm_status set_learned_flag(pm_handle *h, int on) {
+  h->l_on_host = on;
+  static const int kValues[2] = {0, 1};
+  if (cudaMemcpyAsync(h->d_on, &kValues[on ? 1 : 0], sizeof(int), cudaMemcpyHostToDevice,
+                      h->stream) != cudaSuccess)
+    return cuda_fail(h, "learned flag");
   return PM_OK;
 }
 
@@ -465,6 +569,10 @@ pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
     }
     maxite = minit;
   }
+  // learned step on at the start of every solve; off for the rest of the
+  // solve once an iteration reduces the residual by less than l_fallback
+  if (h->mlp) PM_TRY(set_learned_flag(h, 1));
+  double prev_res = r0;
   int j = 1;
   while (j <= maxite) {
     PM_LAUNCH(launch_scale(v(0), 1.0 / beta, N, h->stream));
@@ -497,6 +605,11 @@ pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
       apply_rot(&hh(i, i), &hh(i + 1, i), cs[i], sn[i]);
       apply_rot(&s[i], &s[i + 1], cs[i], sn[i]);
       resv = std::fabs(s[i + 1]);
+      if (h->mlp && h->l_on_host && prev_res > 0.0 && resv > h->l_fallback * prev_res) {
+        PM_TRY(set_learned_flag(h, 0));
+        h->l_fallbacks++;
+      }
+      prev_res = resv;
       if (j >= minit && (resv < resmin || resv < red * res0)) {
         for (int k = 0; k <= i; ++k) y[k] = s[k];
         for (int r = i; r >= 0; --r) {
@@ -888,7 +1001,7 @@ pm_status pm_destroy(pm_handle *h) {
   if (!h) return PM_OK;
   cudaSetDevice(h->opt.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  if (h->vgraph) cudaGraphExecDestroy(h->vgraph);
+  drop_graphs(h);
   for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
   for (void *p : h->allocs) cudaFree(p);
   for (void *p : h->pinned) cudaHostUnregister(p);
@@ -1083,6 +1196,153 @@ pm_status pm_profile_enable(pm_handle *h, int enable) {
     for (auto &e : h->evpool) cudaEventCreate(&e);
   }
   return PM_OK;
+}
+
+// ------------------------------------------------------ learned smoother --
+pm_status pm_mlp_create(pm_mlp **out, int device, unsigned long long seed, int max_batch) {
+  if (!out || max_batch <= 0) return PM_BADARG;
+  *out = nullptr;
+  if (pm_device_count() <= 0) return PM_NO_DEVICE;
+  pm_mlp *m = new pm_mlp();
+  const cudaError_t e = mlp_create(m->m, device, seed, max_batch);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    mlp_destroy(m->m);
+    delete m;
+    return e == cudaErrorMemoryAllocation ? PM_OOM : PM_CUDA_ERROR;
+  }
+  *out = m;
+  return PM_OK;
+}
+
+pm_status pm_mlp_destroy(pm_mlp *m) {
+  if (!m) return PM_OK;
+  mlp_destroy(m->m);
+  delete m;
+  return PM_OK;
+}
+
+long long pm_mlp_num_params(void) { return kNumParams; }
+
+pm_status pm_mlp_get_params(pm_mlp *m, float *host, long long n) {
+  if (!m || !host || n != kNumParams) return PM_BADARG;
+  cudaSetDevice(m->m.device);
+  if (cudaMemcpyAsync(host, m->m.P, sizeof(float) * kNumParams, cudaMemcpyDeviceToHost,
+                      m->m.stream) != cudaSuccess ||
+      cudaStreamSynchronize(m->m.stream) != cudaSuccess)
+    return PM_CUDA_ERROR;
+  return PM_OK;
+}
+
+pm_status pm_mlp_set_params(pm_mlp *m, const float *host, long long n) {
+  if (!m || !host || n != kNumParams) return PM_BADARG;
+  cudaSetDevice(m->m.device);
+  if (cudaMemcpyAsync(m->m.P, host, sizeof(float) * kNumParams, cudaMemcpyHostToDevice,
+                      m->m.stream) != cudaSuccess ||
+      mlp_sync_bf16(m->m, m->m.stream) < 0 || cudaStreamSynchronize(m->m.stream) != cudaSuccess)
+    return PM_CUDA_ERROR;
+  return PM_OK;
+}
+
+pm_status pm_mlp_forward(pm_mlp *m, const float *d_X, int M, float *d_Y) {
+  if (!m || !d_X || !d_Y || M <= 0 || M > m->m.max_batch) return PM_BADARG;
+  cudaSetDevice(m->m.device);
+  if (mlp_forward_f32(m->m, d_X, M, d_Y, m->m.stream) < 0 ||
+      cudaStreamSynchronize(m->m.stream) != cudaSuccess)
+    return PM_CUDA_ERROR;
+  return PM_OK;
+}
+
+pm_status pm_mlp_loss_grad(pm_mlp *m, const float *d_X, const float *d_T, int M, double *loss,
+                           float *host_grad) {
+  if (!m || !d_X || !d_T || M <= 0 || M > m->m.max_batch) return PM_BADARG;
+  cudaSetDevice(m->m.device);
+  if (mlp_loss_grad(m->m, d_X, d_T, M, m->m.stream) < 0) return PM_CUDA_ERROR;
+  double l = 0.0;
+  if (cudaMemcpyAsync(&l, m->m.loss, sizeof(double), cudaMemcpyDeviceToHost, m->m.stream) !=
+      cudaSuccess)
+    return PM_CUDA_ERROR;
+  if (host_grad && cudaMemcpyAsync(host_grad, m->m.G, sizeof(float) * kNumParams,
+                                   cudaMemcpyDeviceToHost, m->m.stream) != cudaSuccess)
+    return PM_CUDA_ERROR;
+  if (cudaStreamSynchronize(m->m.stream) != cudaSuccess) return PM_CUDA_ERROR;
+  if (loss) *loss = l;
+  return std::isfinite(l) ? PM_OK : PM_NAN;
+}
+
+pm_status pm_mlp_adamw_step(pm_mlp *m, float lr, float beta1, float beta2, float eps, float wd) {
+  if (!m) return PM_BADARG;
+  cudaSetDevice(m->m.device);
+  if (mlp_adamw(m->m, lr, beta1, beta2, eps, wd, m->m.stream) < 0) return PM_CUDA_ERROR;
+  return PM_OK;
+}
+
+pm_status pm_learned_attach(pm_handle *h, pm_mlp *m, double omega, double fallback_ratio) {
+  if (!h) return PM_BADARG;
+  if (!h->setup_done) return PM_NOT_SETUP;
+  if (m && m->m.device != h->opt.device) return fail(h, PM_BADARG, "network on another device");
+  drop_graphs(h);  // the captured V-cycles change
+  if (!m) {
+    h->mlp = nullptr;
+    return PM_OK;
+  }
+  // the network's weights are written on its own stream; make them visible
+  if (cudaStreamSynchronize(m->m.stream) != cudaSuccess) return cuda_fail(h, "network sync");
+  for (size_t l = 1; l < h->L.size(); ++l) PM_TRY(ensure_learned_buffers(h, h->L[l]));
+  if (!h->d_on) PM_TRY(dalloc(h, &h->d_on, 1));
+  h->mlp = &m->m;
+  h->l_omega = omega;
+  h->l_fallback = fallback_ratio;
+  h->l_fallbacks = 0;
+  PM_TRY(set_learned_flag(h, 1));
+  return sync(h, "attach");
+}
+
+pm_status pm_learned_status(pm_handle *h, int *enabled, int *fallbacks) {
+  if (!h) return PM_BADARG;
+  if (enabled) *enabled = h->mlp ? h->l_on_host : 0;
+  if (fallbacks) *fallbacks = h->l_fallbacks;
+  return PM_OK;
+}
+
+pm_status pm_learned_harvest(pm_handle *h, const double *sol_exact, const double *rhs,
+                             int n_cycles, float *d_X, float *d_T, long long capacity,
+                             long long *n_pairs) {
+  PM_CHECK_LEVEL(h, 0);
+  if (!sol_exact || !rhs || !d_X || !d_T || !n_pairs || n_cycles <= 0) return PM_BADARG;
+  LevelDev &F = h->L.back();
+  if (*n_pairs < 0 || *n_pairs + (long long)n_cycles * F.ncells > capacity)
+    return fail(h, PM_BADARG, "harvest capacity exceeded");
+  if (h->L.size() < 2) return fail(h, PM_BADARG, "harvest needs at least two levels");
+  PM_TRY(ensure_learned_buffers(h, F));
+  const int N = F.ndof;
+  double *u = h->xd, *b = h->bd, *ue = h->V, *e = h->V + N, *z = h->Z, *r = h->w;
+  PM_TRY(h2d(h, b, rhs, N));
+  PM_TRY(h2d(h, ue, sol_exact, N));
+  PM_LAUNCH(launch_fill<double>(u, 0.0, N, h->stream));
+  const int was_on = h->l_on_host;
+  if (h->mlp) PM_TRY(set_learned_flag(h, 0));  // pairs of the plain solver
+  const DevCells cells = F.cells();
+  for (int k = 0; k < n_cycles; ++k) {
+    PM_TRY(defect_nse4(h, u, b, r));
+    PM_TRY(precondition(h, z, r));
+    PM_LAUNCH(launch_axpy<double>(u, 1.0, z, N, h->stream));
+    PM_TRY(level_defect<double>(h, F, u, b, r));
+    if (cudaMemcpyAsync(e, ue, sizeof(double) * N, cudaMemcpyDeviceToDevice, h->stream) !=
+        cudaSuccess)
+      return cuda_fail(h, "harvest copy");
+    PM_LAUNCH(launch_axpy<double>(e, -1.0, u, N, h->stream));
+    PM_TRY(l20<double>(h, e + 3 * F.nu, F.np));
+    float *Xrow = d_X + (size_t)(*n_pairs) * kMlpIn;
+    float *Trow = d_T + (size_t)(*n_pairs) * kMlpOut;
+    PM_LAUNCH(launch_cell_summary<double>(cells, F.nu, r, F.l_summary, nullptr, h->stream));
+    PM_LAUNCH(launch_cell_features<double>(cells, F.nu, r, F.l_summary, F.l_nbr, nullptr, Xrow,
+                                           F.l_scale, nullptr, h->stream));
+    PM_LAUNCH(launch_cell_targets<double>(cells, F.nu, e, F.l_scale, Trow, h->stream));
+    *n_pairs += F.ncells;
+  }
+  if (h->mlp) PM_TRY(set_learned_flag(h, was_on));
+  return sync(h, "harvest");
 }
 
 pm_status pm_profile_read(pm_handle *h, int kernel, double *ms, long long *launches,

@@ -126,6 +126,59 @@ bool build_one(int nf_cells, int nloc, const int *f_dofs, int f_n, const int *c_
 
 }  // namespace
 
+void build_neighbours(int ncells, const int *udofs, int nu, std::vector<int> &nbr) {
+  std::vector<int> ptr, ent;
+  incidence(ncells, 27, udofs, nu, ptr, ent);
+  nbr.assign((size_t)ncells * 26, -1);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int c = 0; c < ncells; ++c) {
+    // neighbour cell -> bitmask of c's local nodes it shares
+    int cand[64];
+    unsigned int mask[64];
+    int nc = 0;
+    for (int k = 0; k < 27; ++k) {
+      const int d = udofs[(size_t)c * 27 + k];
+      for (int e = ptr[d]; e < ptr[d + 1]; ++e) {
+        const int o = ent[e] / 27;
+        if (o == c) continue;
+        int q = 0;
+        while (q < nc && cand[q] != o) ++q;
+        if (q == nc) {
+          if (nc == 64) continue;
+          cand[nc] = o;
+          mask[nc] = 0;
+          ++nc;
+        }
+        mask[q] |= 1u << k;
+      }
+    }
+    for (int q = 0; q < nc; ++q) {
+      int off[3];
+      for (int axis = 0; axis < 3; ++axis) {
+        bool all0 = true, all2 = true;
+        for (int k = 0; k < 27; ++k)
+          if (mask[q] & (1u << k)) {
+            const int idx = axis == 0 ? k % 3 : (axis == 1 ? (k / 3) % 3 : k / 9);
+            all0 = all0 && idx == 0;
+            all2 = all2 && idx == 2;
+          }
+        off[axis] = all2 ? 1 : (all0 ? -1 : 0);
+      }
+      int slot = (off[0] + 1) + 3 * (off[1] + 1) + 9 * (off[2] + 1);
+      if (slot == 13) continue;
+      if (slot > 13) --slot;
+      nbr[(size_t)c * 26 + slot] = cand[q];
+    }
+  }
+}
+
+void node_inverse_multiplicity(int ncells, const int *udofs, int nu, std::vector<float> &inv) {
+  std::vector<int> cnt(nu, 0);
+  for (long long t = 0; t < (long long)ncells * 27; ++t) cnt[udofs[t]]++;
+  inv.resize(nu);
+  for (int i = 0; i < nu; ++i) inv[i] = cnt[i] > 0 ? 1.0f / (float)cnt[i] : 0.0f;
+}
+
 HostCsr transpose(const HostCsr &a) {
   HostCsr t;
   t.rows = a.cols;

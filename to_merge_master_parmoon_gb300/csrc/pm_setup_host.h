@@ -40,6 +40,14 @@ bool build_transfers(int nc_cells, const int *c_udofs, const int *c_pdofs, int c
 
 HostCsr transpose(const HostCsr &a);
 
+// 26 neighbour slots per cell (-1 = none) for Q2 hexahedra, from the shared
+// nodes alone: along each axis the neighbour lies at +1 if all shared nodes
+// have local index 2 on that axis, -1 if all have 0, else 0; slot =
+// (dx+1) + 3(dy+1) + 9(dz+1) with the centre (13) removed.
+void build_neighbours(int ncells, const int *udofs, int nu, std::vector<int> &nbr);
+// 1 / (number of cells containing each velocity node)
+void node_inverse_multiplicity(int ncells, const int *udofs, int nu, std::vector<float> &inv);
+
 }  // namespace pm
 
 #endif

@@ -1,0 +1,155 @@
+"""Learned per-cell smoother: network handle, training-pair harvest and the
+training loop (AdamW, mini-batches) around the library's GPU kernels.
+
+The network (397 -> 256 -> 256 -> 85, GELU, BF16 tensor-core GEMMs with FP32
+accumulation) and every forward/backward/update step run in libpmgpu; this
+module only orders the calls.  Device buffers for the training set are torch
+tensors (plumbing).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+
+import numpy as np
+
+from ._lib import gpu_lib
+from .solver import PmError, PmSolver
+
+N_IN, N_HIDDEN, N_OUT = 397, 256, 85
+
+
+class Mlp:
+    def __init__(self, device: int = 0, seed: int = 0, max_batch: int = 8192):
+        self._lib = gpu_lib()
+        h = C.c_void_p()
+        st = self._lib.pm_mlp_create(C.byref(h), device, seed, max_batch)
+        if st != 0:
+            raise PmError(st, "pm_mlp_create")
+        self._h = h
+        self.max_batch = max_batch
+        self.n_params = self._lib.pm_mlp_num_params()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pm_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.n_params, np.float32)
+        st = self._lib.pm_mlp_get_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float)), p.size)
+        if st != 0:
+            raise PmError(st, "pm_mlp_get_params")
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        st = self._lib.pm_mlp_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float)), p.size)
+        if st != 0:
+            raise PmError(st, "pm_mlp_set_params")
+
+    def forward(self, X):
+        """X: torch float32 cuda tensor [M, 397] -> [M, 85]."""
+        import torch
+        Y = torch.empty((X.shape[0], N_OUT), dtype=torch.float32, device=X.device)
+        st = self._lib.pm_mlp_forward(self._h, C.c_void_p(X.data_ptr()), X.shape[0],
+                                      C.c_void_p(Y.data_ptr()))
+        if st != 0:
+            raise PmError(st, "pm_mlp_forward")
+        return Y
+
+    def loss_grad(self, X, T, want_grad: bool = False):
+        loss = C.c_double()
+        g = np.empty(self.n_params, np.float32) if want_grad else None
+        st = self._lib.pm_mlp_loss_grad(self._h, C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr()),
+                                        X.shape[0], C.byref(loss),
+                                        g.ctypes.data_as(C.POINTER(C.c_float)) if g is not None else None)
+        if st != 0:
+            raise PmError(st, "pm_mlp_loss_grad")
+        return (loss.value, g) if want_grad else loss.value
+
+    def adamw(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=1e-2):
+        st = self._lib.pm_mlp_adamw_step(self._h, lr, beta1, beta2, eps, weight_decay)
+        if st != 0:
+            raise PmError(st, "pm_mlp_adamw_step")
+
+
+def harvest_pairs(problems, n_cycles: int = 8, device: int = 0, precision: str = "fp64",
+                  max_target_rms: float = 1e4, log=None):
+    """(features, scaled error) pairs from the plain solver on each problem's
+    finest level: exact solution by FGMRES to 1e-11, then n_cycles V-cycle
+    iterations from zero.  Rows that are not finite or whose scaled error has
+    an rms above max_target_rms (the plain iteration diverging on strongly
+    convective problems) are dropped.  Returns torch tensors X [n, 397],
+    T [n, 85]."""
+    import torch
+    total = sum(P.desc(P.n_levels - 1).n_cells * n_cycles for P in problems)
+    X = torch.empty((total, N_IN), dtype=torch.float32, device=f"cuda:{device}")
+    T = torch.empty((total, N_OUT), dtype=torch.float32, device=f"cuda:{device}")
+    n = 0
+    for P in problems:
+        b = P.rhs()
+        nu3 = 3 * P.desc(P.n_levels - 1).n_udof
+        bp = b.copy()
+        bp[nu3::4] -= bp[nu3::4].mean()
+        r0 = float(np.linalg.norm(bp))
+        S = PmSolver(P.descs, precision=precision, device=device, restart=30, maxit=300,
+                     res_norm_min=1e-11 * r0)
+        xs, info = S.iterate(np.zeros_like(b), b, allow=(0, 1))
+        n0 = n
+        converged = info["true_res"] <= 1e-9 * r0
+        if converged:  # the targets are errors against this solution
+            n = S.harvest(xs, b, n_cycles, X.data_ptr(), T.data_ptr(), total, n)
+        S.close()
+        if log:
+            log(f"harvest nu={P.nu:.2e}: exact solve {info['iterations']} it "
+                f"(rel {info['true_res'] / r0:.1e}), {n - n0} rows"
+                + ("" if converged else " (skipped: not converged)"))
+    X, T = X[:n], T[:n]
+    keep = torch.isfinite(X).all(1) & torch.isfinite(T).all(1)
+    keep &= T.pow(2).mean(1).sqrt() <= max_target_rms
+    return X[keep].contiguous(), T[keep].contiguous()
+
+
+def train(mlp: Mlp, X, T, epochs: int = 20, batch: int = 4096, lr: float = 1e-3,
+          weight_decay: float = 1e-2, seed: int = 0, log=None):
+    """AdamW mini-batch training on device tensors; returns per-epoch mean loss."""
+    import torch
+    g = torch.Generator(device=X.device)
+    g.manual_seed(seed)
+    n = X.shape[0]
+    batch = min(batch, mlp.max_batch)
+    hist = []
+    t0 = time.time()
+    for ep in range(epochs):
+        perm = torch.randperm(n, device=X.device, generator=g)
+        tot, cnt = 0.0, 0
+        for s in range(0, n - batch + 1, batch):
+            idx = perm[s:s + batch]
+            xb = X.index_select(0, idx).contiguous()
+            tb = T.index_select(0, idx).contiguous()
+            loss = mlp.loss_grad(xb, tb)
+            mlp.adamw(lr=lr, weight_decay=weight_decay)
+            tot += loss
+            cnt += 1
+        hist.append(tot / max(cnt, 1))
+        if log:
+            log(f"epoch {ep}: loss {hist[-1]:.4e} ({time.time() - t0:.1f}s)")
+    return hist
+
+
+def relative_loss(mlp: Mlp, X, T, batch: int = 8192) -> float:
+    """||pred - T||^2 / ||T||^2 over a data set (1.0 = predicting zero)."""
+    num = den = 0.0
+    batch = min(batch, mlp.max_batch)
+    for s in range(0, X.shape[0], batch):
+        xb = X[s:s + batch].contiguous()
+        y = mlp.forward(xb)
+        tb = T[s:s + batch]
+        num += float(((y - tb) ** 2).sum())
+        den += float((tb ** 2).sum())
+    return num / max(den, 1e-300)

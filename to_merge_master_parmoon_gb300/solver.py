@@ -168,6 +168,30 @@ class PmSolver:
         self._check(self._lib.pm_vcycle(self._h, _dp(z), _dp(v)), "pm_vcycle")
         return z
 
+    # ------------------------------------------------------ learned smoother
+    def attach_learned(self, mlp, omega=1.0, fallback_ratio=0.5):
+        """Insert the network as an extra post-smoothing step on every level
+        (None detaches)."""
+        self._check(self._lib.pm_learned_attach(self._h, mlp._h if mlp is not None else None,
+                                                omega, fallback_ratio), "pm_learned_attach")
+        self._mlp = mlp
+
+    def learned_status(self):
+        on, fb = C.c_int(), C.c_int()
+        self._check(self._lib.pm_learned_status(self._h, C.byref(on), C.byref(fb)),
+                    "pm_learned_status")
+        return {"enabled": on.value, "fallbacks": fb.value}
+
+    def harvest(self, sol_exact, rhs, n_cycles, d_X_ptr, d_T_ptr, capacity, n_pairs):
+        """(residual, error) training pairs of the plain V-cycle iteration on
+        the finest level; returns the new row count."""
+        sol_exact, rhs = _f64(sol_exact), _f64(rhs)
+        n = C.c_longlong(n_pairs)
+        self._check(self._lib.pm_learned_harvest(self._h, _dp(sol_exact), _dp(rhs), n_cycles,
+                                                 C.c_void_p(d_X_ptr), C.c_void_p(d_T_ptr),
+                                                 capacity, C.byref(n)), "pm_learned_harvest")
+        return n.value
+
     # ---------------------------------------------------------------- solve
     def iterate(self, sol, rhs, allow=(0,)):
         """TFgmresIte::Iterate on host vectors; returns (solution, result dict)."""
