@@ -315,16 +315,20 @@ def main():
             d = P.desc(lv)
             h2d += 8 * (9 * d.a_nnz + 3 * d.b_nnz + 3 * d.bt_nnz)
         h2d += 16 * n
-        times = []
+        times, t_upd = [], []
         for s in range(args.warmup + args.steps):
             torch.cuda.synchronize()
             t = time.perf_counter()
             S.update_matrices(P.descs)
+            t1 = time.perf_counter()
             xs, info = S.iterate(x, b)
             times.append(time.perf_counter() - t)
-        times = times[args.warmup:]
+            t_upd.append(t1 - t)
+        times, t_upd = times[args.warmup:], t_upd[args.warmup:]
         e2e = {"value": sum(times) / len(times), "unit": "s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": 8 * n}
+               "d2h_bytes_per_step": 8 * n,
+               "update_matrices_s": sum(t_upd) / len(t_upd),
+               "pinned_host_bytes": S._lib.pm_pinned_bytes(S._h)}
 
     if rank != 0:
         return

@@ -196,6 +196,8 @@ pm_status pm_refactor(pm_handle *h, double *ms);
  * created, and device bytes held. */
 long long pm_kernel_launches(pm_handle *h);
 long long pm_device_bytes(pm_handle *h);
+/* Host bytes page-locked by pm_add_level under pin_host (0 if none took). */
+long long pm_pinned_bytes(pm_handle *h);
 /* Per-kernel timing of the two Vanka sweep kernels while profiling is
  * enabled: CUDA events on the handle's stream bracket every launch (the
  * V-cycle then runs without graph capture).  kernel 0 = local residual,

@@ -93,6 +93,7 @@ GPU_SYMBOLS = {
     "pm_refactor": (C.c_int, [_P, c_double_p]),
     "pm_kernel_launches": (C.c_longlong, [_P]),
     "pm_device_bytes": (C.c_longlong, [_P]),
+    "pm_pinned_bytes": (C.c_longlong, [_P]),
     "pm_profile_enable": (C.c_int, [_P, C.c_int]),
     "pm_profile_read": (C.c_int, [_P, C.c_int, c_double_p, C.POINTER(C.c_longlong), c_double_p]),
     "pm_l20_project_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),

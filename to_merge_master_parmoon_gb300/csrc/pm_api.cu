@@ -53,6 +53,7 @@ DevCsr<float> CsrStore::view<float>() const {
 struct LevelDev {
   int nu = 0, np = 0, ndof = 0, nact = 0, hb = 0, ndir = 0, ncells = 0;
   int a_nnz = 0, b_nnz = 0, bt_nnz = 0;
+  int structured = 0;  // velocity blocks: A12..A32 = 0 and A11 = A22 = A33 (exactly)
   std::vector<int> h_udofs, h_pdofs, h_parent, h_child, h_colour;
   bool has_colour = false;
   int *a_rowptr = nullptr, *a_col = nullptr, *b_rowptr = nullptr, *b_col = nullptr;
@@ -85,6 +86,7 @@ template <>
 DevOp<double> LevelDev::op<double>() const {
   DevOp<double> o;
   o.nu = nu;
+  o.structured = structured;
   o.np = np;
   o.nact = nact;
   o.a_rowptr = a_rowptr;
@@ -104,6 +106,7 @@ template <>
 DevOp<float> LevelDev::op<float>() const {
   DevOp<float> o;
   o.nu = nu;
+  o.structured = structured;
   o.np = np;
   o.nact = nact;
   o.a_rowptr = a_rowptr;
@@ -158,6 +161,7 @@ struct pm_handle {
   long long prof_launches[2] = {0, 0};
   double last_factor_ms = 0.0;
   std::vector<void *> pinned;
+  long long pinned_bytes = 0;
   // learned smoother (borrowed network), device on/off flag read by its kernels
   pm::Mlp *mlp = nullptr;
   double l_omega = 1.0, l_fallback = 0.5;
@@ -875,9 +879,10 @@ pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
   if (h->opt.pin_host) {
     auto pin = [h](const void *p, size_t bytes) {
       if (!p || bytes < (1u << 20)) return;
-      if (cudaHostRegister(const_cast<void *>(p), bytes, cudaHostRegisterPortable) == cudaSuccess)
+      if (cudaHostRegister(const_cast<void *>(p), bytes, cudaHostRegisterPortable) == cudaSuccess) {
         h->pinned.push_back(const_cast<void *>(p));
-      else
+        h->pinned_bytes += (long long)bytes;
+      } else
         cudaGetLastError();  // already registered / not registrable: copy unpinned
     };
     for (int k = 0; k < 9; ++k) pin(d->a[k], sizeof(double) * (size_t)Lv.a_nnz);
@@ -1182,6 +1187,7 @@ pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out)
 
 long long pm_kernel_launches(pm_handle *h) { return h ? h->launches : 0; }
 long long pm_device_bytes(pm_handle *h) { return h ? h->bytes : 0; }
+long long pm_pinned_bytes(pm_handle *h) { return h ? h->pinned_bytes : 0; }
 
 pm_status pm_profile_enable(pm_handle *h, int enable) {
   if (!h) return PM_BADARG;

@@ -20,6 +20,9 @@ constexpr int kRStride = 88;               // per-cell stride of the residual bu
 template <typename T>
 struct DevOp {
   int nu, np, nact;
+  // 1: A12..A32 are zero and A11 = A22 = A33 (checked exactly at set-up);
+  // only a[0] is read
+  int structured;
   const int *a_rowptr, *a_col;
   const T *a[9];
   const int *b_rowptr, *b_col;

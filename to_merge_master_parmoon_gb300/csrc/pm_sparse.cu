@@ -60,12 +60,22 @@ __global__ void __launch_bounds__(kBlock) k_coupled_velocity(DevOp<T> op, const 
   T s1 = 0, s2 = 0, s3 = 0;
   if (!skip) {
     const int rs = op.a_rowptr[i], re = op.a_rowptr[i + 1];
-    for (int j = rs + lane; j < re; j += G) {
-      const int c = __ldg(op.a_col + j);
-      const T x1 = __ldg(u1 + c), x2 = __ldg(u2 + c), x3 = __ldg(u3 + c);
-      s1 += ld_stream(op.a[0] + j) * x1 + ld_stream(op.a[1] + j) * x2 + ld_stream(op.a[2] + j) * x3;
-      s2 += ld_stream(op.a[3] + j) * x1 + ld_stream(op.a[4] + j) * x2 + ld_stream(op.a[5] + j) * x3;
-      s3 += ld_stream(op.a[6] + j) * x1 + ld_stream(op.a[7] + j) * x2 + ld_stream(op.a[8] + j) * x3;
+    if (op.structured) {  // one block value per entry, same for the three components
+      for (int j = rs + lane; j < re; j += G) {
+        const int c = __ldg(op.a_col + j);
+        const T a = ld_stream(op.a[0] + j);
+        s1 += a * __ldg(u1 + c);
+        s2 += a * __ldg(u2 + c);
+        s3 += a * __ldg(u3 + c);
+      }
+    } else {
+      for (int j = rs + lane; j < re; j += G) {
+        const int c = __ldg(op.a_col + j);
+        const T x1 = __ldg(u1 + c), x2 = __ldg(u2 + c), x3 = __ldg(u3 + c);
+        s1 += ld_stream(op.a[0] + j) * x1 + ld_stream(op.a[1] + j) * x2 + ld_stream(op.a[2] + j) * x3;
+        s2 += ld_stream(op.a[3] + j) * x1 + ld_stream(op.a[4] + j) * x2 + ld_stream(op.a[5] + j) * x3;
+        s3 += ld_stream(op.a[6] + j) * x1 + ld_stream(op.a[7] + j) * x2 + ld_stream(op.a[8] + j) * x3;
+      }
     }
     if (i < op.nact) {
       const int bs = op.bt_rowptr[i], be = op.bt_rowptr[i + 1];
