@@ -252,6 +252,15 @@ def main():
         solvers[name] = PmSolver(P.descs, precision=prec, device=local, restart=20, maxit=200,
                                  res_norm_min=RTOL * r0, pin_host=int(name == "mixed_learned"))
     solvers["mixed_learned"].attach_learned(net, omega=1.0, fallback_ratio=0.5)
+    # the same system as NSTYPE-2 levels (one velocity block; the Galerkin
+    # Oseen form has A12..A32 = 0 and A11 = A22 = A33), smoothed by the exact
+    # block solve of the cell systems: reported beside the headline
+    one_block = P.is_one_block()
+    D1 = P.descs_one_block() if one_block else None
+    if one_block:
+        for name, prec in (("mixed_one_block", "mixed"), ("fp64_one_block", "fp64")):
+            solvers[name] = PmSolver(D1, precision=prec, device=local, restart=20, maxit=200,
+                                     res_norm_min=RTOL * r0, pin_host=int(name == "mixed_one_block"))
 
     def step(S):
         d_x.zero_()
@@ -305,30 +314,36 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
 
-    # end to end through the C ABI with host buffers
-    e2e = None
-    if not args.no_e2e:
-        S = solvers["mixed_learned"]
+    # end to end through the C ABI with host buffers: every step uploads the
+    # level matrices (pm_update_matrices, which refactors) and solves from
+    # host vectors (pm_solve copies b in and x out)
+    def e2e_run(S, descs, nblk):
         x = np.zeros(n)
         h2d = 0
         for lv in range(P.n_levels):
             d = P.desc(lv)
-            h2d += 8 * (9 * d.a_nnz + 3 * d.b_nnz + 3 * d.bt_nnz)
+            h2d += 8 * (nblk * d.a_nnz + 3 * d.b_nnz + 3 * d.bt_nnz)
         h2d += 16 * n
         times, t_upd = [], []
         for s in range(args.warmup + args.steps):
             torch.cuda.synchronize()
             t = time.perf_counter()
-            S.update_matrices(P.descs)
+            S.update_matrices(descs)
             t1 = time.perf_counter()
             xs, info = S.iterate(x, b)
             times.append(time.perf_counter() - t)
             t_upd.append(t1 - t)
         times, t_upd = times[args.warmup:], t_upd[args.warmup:]
-        e2e = {"value": sum(times) / len(times), "unit": "s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": 8 * n,
-               "update_matrices_s": sum(t_upd) / len(t_upd),
-               "pinned_host_bytes": S._lib.pm_pinned_bytes(S._h)}
+        return {"value": sum(times) / len(times), "unit": "s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": 8 * n,
+                "update_matrices_s": sum(t_upd) / len(t_upd),
+                "pinned_host_bytes": S._lib.pm_pinned_bytes(S._h)}
+
+    e2e = e2e1 = None
+    if not args.no_e2e:
+        e2e = e2e_run(solvers["mixed_learned"], P.descs, 9)
+        if one_block:
+            e2e1 = e2e_run(solvers["mixed_one_block"], D1, 1)
 
     if rank != 0:
         return
@@ -350,6 +365,21 @@ def main():
             "apply_kernel": {"name": "k_vanka_apply<float> (stored-LU solve + update)",
                              "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,
                              "avg_launch_ms": a_ms, "bytes_per_launch": a_bytes}}
+    one = None
+    if one_block:
+        one = {"note": "same system as NSTYPE-2 levels (a[0] only); exact block solve of the "
+                       "cell systems (A^-1 + 4x4 Schur complement, 1393 stored values per cell); "
+                       "byte counts of its own (1 A array, 1393 values per cell)"}
+        for name in ("mixed_one_block", "fp64_one_block"):
+            r = results[name]
+            one[name] = {"value": r["ms"] * 1e-3,
+                         **{k: r[k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res")},
+                         "sweep_kernels": {
+                             k: {"ms_total": v["ms"], "launches": v["launches"],
+                                 "achieved_gbs": kernel_roof(v)[0],
+                                 "frac": (kernel_roof(v)[0] / peak) if v["ms"] else None}
+                             for k, v in r.get("profile", {}).items()}}
+        one["e2e"] = e2e1
     cpu = None
     if not args.no_cpu_baseline:
         per_it = cpu_baseline(P, results["fp64"]["iterations"], args.levels, threads)
@@ -384,6 +414,7 @@ def main():
         "speedup_vs_fp64": results["fp64"]["ms"] / results["mixed_learned"]["ms"],
         "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "roofline": roof,
+        "one_block": one,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": results["mixed_learned"]["launches"],

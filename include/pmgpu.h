@@ -110,7 +110,12 @@ typedef struct {
   int a_nnz;
   const int *a_rowptr;   /* n_udof+1 */
   const int *a_col;      /* a_nnz    */
-  const double *a[9];    /* A11,A12,A13,A21,A22,A23,A31,A32,A33 entries */
+  /* A11,A12,A13,A21,A22,A23,A31,A32,A33 entries (NSTYPE 4, TNSE_MGLevel4);
+   * or a[0] alone with a[1..8] NULL: one block A shared by the three
+   * components and no velocity coupling (NSTYPE 2, TNSE_MGLevel2,
+   * src/FE/NSE_MGLevel2.C:54-110), smoothed by the exact block solve of the
+   * local system (A^{-1}, 4x4 Schur complement) */
+  const double *a[9];
   /* B blocks: N_P x N_U */
   int b_nnz;
   const int *b_rowptr;   /* n_pdof+1 */
@@ -166,6 +171,8 @@ pm_status pm_update_matrices(pm_handle *h, const pm_level_desc *levels, int n_le
 pm_status pm_destroy(pm_handle *h);
 int       pm_n_levels(pm_handle *h);
 int       pm_level_ndof(pm_handle *h, int level);
+/* velocity blocks of a level: 9 (NSTYPE 4) or 1 (NSTYPE 2); -1 if no such level */
+int       pm_level_blocks(pm_handle *h, int level);
 
 /* Level operators (FP64 on host vectors of length ndof(level)). */
 pm_status pm_coupled_defect(pm_handle *h, int level, const double *x, const double *b,

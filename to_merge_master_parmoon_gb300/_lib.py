@@ -80,6 +80,7 @@ GPU_SYMBOLS = {
     "pm_destroy": (C.c_int, [_P]),
     "pm_n_levels": (C.c_int, [_P]),
     "pm_level_ndof": (C.c_int, [_P, C.c_int]),
+    "pm_level_blocks": (C.c_int, [_P, C.c_int]),
     "pm_coupled_defect": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, c_double_p, C.c_int]),
     "pm_defect": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, c_double_p, c_double_p]),
     "pm_matvec": (C.c_int, [_P, C.c_int, c_double_p, c_double_p]),

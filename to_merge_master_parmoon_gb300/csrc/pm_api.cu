@@ -298,9 +298,14 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
     PM_LAUNCH(launch_vanka_residual<T>(op, cells, Lv.colour_cells + b, n, u, rhs,
                                        static_cast<T *>(Lv.dbuf), h->stream));
     if (e1) cudaEventRecord(e1, h->stream);
-    PM_LAUNCH(launch_vanka_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
-                                    static_cast<const T *>(Lv.factors), Lv.perm, use_inverse(h),
-                                    static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
+    if (Lv.structured)
+      PM_LAUNCH(launch_schur_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
+                                      static_cast<const T *>(Lv.factors),
+                                      static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
+    else
+      PM_LAUNCH(launch_vanka_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
+                                      static_cast<const T *>(Lv.factors), Lv.perm, use_inverse(h),
+                                      static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
     if (e2) {
       cudaEventRecord(e2, h->stream);
       // algorithmic bytes of this colour: the level's unique Vanka-sweep
@@ -666,7 +671,15 @@ pm_status factor_all(pm_handle *h) {
   cudaEventRecord(e0, h->stream);
   for (size_t l = 1; l < h->L.size(); ++l) {
     LevelDev &Lv = h->L[l];
-    if (mixed(h))
+    if (Lv.structured) {
+      if (mixed(h))
+        PM_LAUNCH(launch_schur_factor<float>(Lv.op<double>(), Lv.cells(),
+                                             static_cast<float *>(Lv.factors), h->status_d, h->stream));
+      else
+        PM_LAUNCH(launch_schur_factor<double>(Lv.op<double>(), Lv.cells(),
+                                              static_cast<double *>(Lv.factors), h->status_d,
+                                              h->stream));
+    } else if (mixed(h))
       PM_LAUNCH(launch_vanka_factor<float>(Lv.op<double>(), Lv.cells(), static_cast<float *>(Lv.factors),
                                            Lv.perm, h->opt.factor_fp32 != 0, use_inverse(h),
                                            h->status_d, h->stream));
@@ -693,9 +706,22 @@ pm_status factor_all(pm_handle *h) {
   return PM_OK;
 }
 
+// Number of A value arrays of a level descriptor: 9 (NSTYPE 4) or 1 (NSTYPE 2:
+// a[0] is the block of all three components, a[1..8] are NULL); 0 if mixed.
+int desc_blocks(const pm_level_desc *d) {
+  int given = 0;
+  for (int k = 1; k < 9; ++k) given += d->a[k] != nullptr;
+  if (!d->a[0]) return 0;
+  return given == 8 ? 9 : (given == 0 ? 1 : 0);
+}
+
 pm_status upload_values(pm_handle *h, LevelDev &Lv, const pm_level_desc *d, bool first) {
-  for (int k = 0; k < 9; ++k) {
-    if (!d->a[k]) return fail(h, PM_BADARG, "missing A block");
+  const int nblk = desc_blocks(d);
+  if (nblk == 0) return fail(h, PM_BADARG, "A blocks: give all nine or only a[0]");
+  if (first) Lv.structured = nblk == 1;
+  if ((nblk == 1) != (Lv.structured != 0))
+    return fail(h, PM_BADARG, "A block count differs from the level's first upload");
+  for (int k = 0; k < nblk; ++k) {
     if (first) PM_TRY(dalloc_padded(h, &Lv.a64[k], Lv.a_nnz));
     if (cudaMemcpyAsync(Lv.a64[k], d->a[k], sizeof(double) * Lv.a_nnz, cudaMemcpyHostToDevice,
                         h->stream) != cudaSuccess)
@@ -713,9 +739,10 @@ pm_status upload_values(pm_handle *h, LevelDev &Lv, const pm_level_desc *d, bool
                         h->stream) != cudaSuccess)
       return cuda_fail(h, "B upload");
   }
-  PM_LAUNCH(launch_zero_dirichlet_offdiag(Lv.a64, Lv.a_rowptr, Lv.nu, Lv.nact, h->stream));
+  if (!Lv.structured)
+    PM_LAUNCH(launch_zero_dirichlet_offdiag(Lv.a64, Lv.a_rowptr, Lv.nu, Lv.nact, h->stream));
   if (mixed(h)) {
-    for (int k = 0; k < 9; ++k) {
+    for (int k = 0; k < nblk; ++k) {
       if (first) PM_TRY(dalloc_padded(h, &Lv.a32[k], Lv.a_nnz));
       PM_LAUNCH((launch_convert<float, double>(Lv.a32[k], Lv.a64[k], Lv.a_nnz, h->stream)));
     }
@@ -758,6 +785,8 @@ bool check_desc(pm_handle *h, const pm_level_desc *d) {
   if (!d->a_rowptr || !d->a_col || !d->b_rowptr || !d->b_col || !d->bt_rowptr || !d->bt_col ||
       !d->cell_udofs || !d->cell_pdofs)
     return fail(h, PM_BADARG, "missing arrays"), false;
+  if (desc_blocks(d) == 0)
+    return fail(h, PM_BADARG, "A blocks: give all nine or only a[0]"), false;
   if (d->a_rowptr[d->n_udof] != d->a_nnz || d->b_rowptr[d->n_pdof] != d->b_nnz ||
       d->bt_rowptr[d->n_udof] != d->bt_nnz)
     return fail(h, PM_BADARG, "row pointer totals do not match nnz"), false;
@@ -924,10 +953,16 @@ pm_status pm_setup(pm_handle *h) {
       PM_TRY(upload_csr(h, Lv.Ru, Ru));
       PM_TRY(upload_csr(h, Lv.Pp, Pp));
       PM_TRY(upload_csr(h, Lv.Rp, Rp));
-      // local factors (FP64 or FP32 storage) and permutations
-      PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
-                    (size_t)Lv.ncells * NLOC * NLOC * es));
-      PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * NLOC));
+      // local factors (FP64 or FP32 storage) and permutations, or the
+      // block-solve data of a one-block level
+      if (Lv.structured) {
+        PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
+                      (size_t)Lv.ncells * kSchurStride * es));
+      } else {
+        PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
+                      (size_t)Lv.ncells * NLOC * NLOC * es));
+        PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * NLOC));
+      }
       PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.dbuf),
                     (size_t)Lv.colouring.max_size * kRStride * es));
       if (std::fabs(1.0 - h->opt.alpha) > 1e-3)
@@ -938,12 +973,14 @@ pm_status pm_setup(pm_handle *h) {
       // residual kernel = matrix values + column indices + row pointers, u
       // and rhs read; apply kernel = factors + permutation, u read+write
       const double sv = (double)es;
-      const double mat = 9.0 * sv * Lv.a_nnz + 4.0 * Lv.a_nnz + 4.0 * (Lv.nu + 1) +
+      const double nblk = Lv.structured ? 1.0 : 9.0;
+      const double mat = nblk * sv * Lv.a_nnz + 4.0 * Lv.a_nnz + 4.0 * (Lv.nu + 1) +
                          (3.0 * sv + 4.0) * ((double)Lv.b_nnz + Lv.bt_nnz) + 4.0 * (Lv.np + 1) +
                          4.0 * (Lv.nu + 1);
       Lv.vanka_res_bytes = (mat + 2.0 * sv * Lv.ndof) / Lv.ncells;
-      Lv.vanka_apply_bytes =
-          ((double)Lv.ncells * ((double)NLOC * NLOC * sv + NLOC) + 2.0 * sv * Lv.ndof) / Lv.ncells;
+      const double per_cell =
+          Lv.structured ? (double)kSchurValues * sv : (double)NLOC * NLOC * sv + NLOC;
+      Lv.vanka_apply_bytes = ((double)Lv.ncells * per_cell + 2.0 * sv * Lv.ndof) / Lv.ncells;
     }
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.sol), (size_t)Lv.ndof * es));
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.rhs), (size_t)Lv.ndof * es));
@@ -1018,6 +1055,9 @@ pm_status pm_destroy(pm_handle *h) {
 int pm_n_levels(pm_handle *h) { return h ? (int)h->L.size() : 0; }
 int pm_level_ndof(pm_handle *h, int l) {
   return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].ndof : -1;
+}
+int pm_level_blocks(pm_handle *h, int l) {
+  return (h && l >= 0 && l < (int)h->L.size()) ? (h->L[l].structured ? 1 : 9) : -1;
 }
 
 #define PM_CHECK_LEVEL(h, level)                                           \

@@ -122,6 +122,21 @@ int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int 
                        const T *factors, const uint8_t *perm, bool inverse, const T *rbuf,
                        T damp, T *u, cudaStream_t s);
 
+// Block (Schur-complement) local solve for structured operators: per cell
+// A^{-1} (27x27, column-major), D (4x3x27), W = A^{-1} G (4x3x27) and S^{-1}
+// (4x4, column-major), kSchurStride values of the storage precision.
+constexpr int kSchurOffD = NU_LOC * NU_LOC;                    // 729
+constexpr int kSchurOffW = kSchurOffD + NP_LOC * 3 * NU_LOC;   // 1053
+constexpr int kSchurOffS = kSchurOffW + NP_LOC * 3 * NU_LOC;   // 1377
+constexpr int kSchurValues = kSchurOffS + NP_LOC * NP_LOC;     // 1393
+constexpr int kSchurStride = 1396;                             // 16-byte multiple per cell
+template <typename TF>
+int launch_schur_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,
+                        cudaStream_t s);
+template <typename T>
+int launch_schur_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
+                       const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s);
+
 // ----------------------------------------------------------------- coarse --
 // Dense column-major N x N coarse saddle matrix of SolveExact
 // (src/FE/NSE_MGLevel4.C:5728-5830) from the FP64 CSR.

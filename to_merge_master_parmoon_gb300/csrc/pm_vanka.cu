@@ -83,6 +83,13 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
         }
       if (m < 0) continue;
       const int c1 = m * NLOC, c2 = (m + NU_LOC) * NLOC, c3 = (m + 2 * NU_LOC) * NLOC;
+      if (op.structured) {  // one block for the three components, no coupling
+        const TC v = (TC)op.a[0][j];
+        S[c1 + a] = v;
+        S[c2 + a + NU_LOC] = v;
+        S[c3 + a + 2 * NU_LOC] = v;
+        continue;
+      }
       S[c1 + a] = (TC)op.a[0][j];
       S[c2 + a + NU_LOC] = (TC)op.a[4][j];
       S[c3 + a + 2 * NU_LOC] = (TC)op.a[8][j];
@@ -354,12 +361,13 @@ __device__ __forceinline__ int seg_setup(const SegTab &t, int lane, bool valid, 
 // MODE 0: A rows (9 values, gather u1,u2,u3 -> 3 outputs)
 // MODE 1: BT rows (3 values, gather p -> 3 outputs)
 // MODE 2: B rows (3 values, gather u1,u2,u3 -> 1 output)
+// MODE 3: A rows of a one-block operator (1 value, gather u1,u2,u3 -> 3 outputs)
 template <typename T, int MODE, int VEC, int U>
 __device__ __forceinline__ void flat_rows(const SegTab &t, int nseg, int total,
                                           const int *__restrict__ col, const T *const *vals,
                                           const T *__restrict__ x0, const T *__restrict__ x1,
                                           const T *__restrict__ x2, T *acc, int lane) {
-  constexpr int NV = MODE == 0 ? 9 : 3;
+  constexpr int NV = MODE == 0 ? 9 : (MODE == 3 ? 1 : 3);
   constexpr int NO = MODE == 2 ? 1 : 3;
   for (int base = 0; base < total; base += 32 * U) {
     int seg[U];
@@ -404,14 +412,19 @@ __device__ __forceinline__ void flat_rows(const SegTab &t, int nseg, int total,
           const long long e = e0 + m;
           if (e >= lo && e < hi) {
             const int c = ci[q][m];
-            if (MODE == 1) {
+            if constexpr (MODE == 1) {
               const T g0 = __ldg(x0 + c);
               s[0] += v[q][0][m] * g0;
               s[1 % NO] += v[q][1][m] * g0;
               s[2 % NO] += v[q][2][m] * g0;
+            } else if constexpr (MODE == 3) {
+              const T a = v[q][0][m];
+              s[0] += a * __ldg(x0 + c);
+              s[1 % NO] += a * __ldg(x1 + c);
+              s[2 % NO] += a * __ldg(x2 + c);
             } else {
               const T g0 = __ldg(x0 + c), g1 = __ldg(x1 + c), g2 = __ldg(x2 + c);
-              if (MODE == 0) {
+              if constexpr (MODE == 0) {
                 s[0] += v[q][0][m] * g0 + v[q][1][m] * g1 + v[q][2][m] * g2;
                 s[1 % NO] += v[q][3][m] * g0 + v[q][4][m] * g1 + v[q][5][m] * g2;
                 s[2 % NO] += v[q][6][m] * g0 + v[q][7][m] * g1 + v[q][8][m] * g2;
@@ -445,10 +458,13 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual(
   const bool vu = lane < NU_LOC, vp = lane < NP_LOC;
   const int my_r = vu ? cells.udofs[(size_t)cell * NU_LOC + lane] : 0;
   const int my_p = vp ? cells.pdofs[(size_t)cell * NP_LOC + lane] : 0;
-  // A rows: nine blocks
+  // A rows: nine blocks, or the one block of a structured operator
   int total = seg_setup<VEC>(tab, lane, vu, vu ? op.a_rowptr[my_r] : 0,
                              vu ? op.a_rowptr[my_r + 1] : 0);
-  flat_rows<T, 0, VEC, U>(tab, NU_LOC, total, op.a_col, op.a, u1, u2, u3, acc, lane);
+  if (op.structured)
+    flat_rows<T, 3, VEC, U>(tab, NU_LOC, total, op.a_col, op.a, u1, u2, u3, acc, lane);
+  else
+    flat_rows<T, 0, VEC, U>(tab, NU_LOC, total, op.a_col, op.a, u1, u2, u3, acc, lane);
   // BT rows of active velocity DOFs
   const bool act = vu && my_r < op.nact;
   total = seg_setup<VEC>(tab, lane, act, act ? op.bt_rowptr[my_r] : 0,
@@ -609,6 +625,13 @@ __global__ void k_coarse_scatter(DevOp<double> op, double *a, int N) {
     const int i = t;
     for (int j = op.a_rowptr[i]; j < op.a_rowptr[i + 1]; ++j) {
       const size_t idx = op.a_col[j];
+      if (op.structured) {
+        const double v = op.a[0][j];
+        a[idx * N + i] = v;
+        a[(idx + nu) * N + i + nu] = v;
+        a[(idx + nu2) * N + i + nu2] = v;
+        continue;
+      }
       a[idx * N + i] = op.a[0][j];
       a[(idx + nu) * N + i] = op.a[1][j];
       a[idx * N + i + nu] = op.a[3][j];
@@ -629,9 +652,10 @@ __global__ void k_coarse_scatter(DevOp<double> op, double *a, int N) {
     const int i = t;
     for (int j = op.a_rowptr[i]; j < op.a_rowptr[i + 1]; ++j) {
       const size_t idx = op.a_col[j];
+      const int k4 = op.structured ? 0 : 4, k8 = op.structured ? 0 : 8;
       a[i + N * idx] = op.a[0][j];
-      a[(idx + nu) * N + i + nu] = op.a[4][j];
-      a[(idx + nu2) * N + i + nu2] = op.a[8][j];
+      a[(idx + nu) * N + i + nu] = op.a[k4][j];
+      a[(idx + nu2) * N + i + nu2] = op.a[k8][j];
     }
   } else if (t < nu + op.np) {
     const int i = t - nu;

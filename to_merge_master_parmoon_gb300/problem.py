@@ -65,6 +65,33 @@ class OseenProblem:
     def desc(self, level: int) -> PmLevelDesc:
         return self._descs[level]
 
+    def is_one_block(self) -> bool:
+        """True when every level has A12..A32 = 0 on the active rows and
+        A11 = A22 = A33 exactly (the Galerkin Oseen/Stokes forms with the
+        gradient Laplacian), i.e. the system is also an NSTYPE-2 system."""
+        for level in range(self.n_levels):
+            d = self.arrays(level)
+            a, nact = d["a"], d["n_active"]
+            act = np.repeat(np.arange(d["n_udof"]) < nact, np.diff(d["a_rowptr"]))
+            if not (np.array_equal(a[0], a[4]) and np.array_equal(a[0], a[8])):
+                return False
+            if any(np.any(a[k][act] != 0.0) for k in (1, 2, 3, 5, 6, 7)):
+                return False
+        return True
+
+    def descs_one_block(self):
+        """The same levels as NSTYPE-2 descriptors: a[0] carries the block of
+        all three components, a[1..8] are NULL (TNSE_MGLevel2's one A
+        matrix).  Valid only when is_one_block(); shares this problem's arrays."""
+        if not self.is_one_block():
+            raise ValueError("the velocity blocks are coupled or differ: not an NSTYPE-2 system")
+        out = (PmLevelDesc * self.n_levels)()
+        for level in range(self.n_levels):
+            C.pointer(out[level])[0] = self._descs[level]
+            for k in range(1, 9):
+                out[level].a[k] = None
+        return out
+
     def ndof(self, level: int = -1) -> int:
         level = level % self.n_levels
         return self._lib.pmh_ndof(self._h, level)
