@@ -186,7 +186,7 @@ def train_network(device, args, log=None):
     from to_merge_master_parmoon_gb300 import OseenProblem
     from to_merge_master_parmoon_gb300.learned import Mlp, harvest_pairs, relative_loss, train
     cfg = dict(levels=5, problems=args.train_problems, cycles=8, epochs=20, batch=4096, lr=1e-3,
-               seed=0, nu_range=(1e-3, 1e-1))
+               seed=0, nu_range=(1e-3, 1e-1), features="neighbourhood-max-rms")
     key = hashlib.sha1(json.dumps(cfg, sort_keys=True).encode()).hexdigest()[:12]
     cache = ROOT / "to_merge_master_parmoon_gb300" / "_build" / f"mlp_{key}.npy"
     net = Mlp(device=device, seed=cfg["seed"], max_batch=cfg["batch"])
@@ -231,6 +231,7 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    from to_merge_master_parmoon_gb300.solver import PmError
 
     threads = os.cpu_count() or 1
     P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed + rank, nthreads=threads)
@@ -247,10 +248,21 @@ def main():
     # learned smoother: trained once (harvest on 32^3 problems, GPU training),
     # outside the timed region; cached by configuration in the build folder
     net, learned_info = train_network(local, args, log=lambda *a: print(*a, file=sys.stderr))
+    # matrix values move by SM loads of the caller's (pageable) arrays where
+    # the GPU can read host memory (Grace-coupled), else by copy-engine
+    # copies.  The arrays are not page-locked: on the GB300 machine copies from
+    # cudaHostRegister'ed memory fell to 5-10 GB/s after sustained GPU load
+    # while pageable memory kept 175-190 GB/s.
+    def make(descs, prec):
+        kw = dict(precision=prec, device=local, restart=20, maxit=200, res_norm_min=RTOL * r0)
+        try:
+            return PmSolver(descs, upload_mode=1, **kw)
+        except PmError:
+            return PmSolver(descs, upload_mode=0, **kw)
+
     solvers = {}
     for name, prec in (("mixed_learned", "mixed"), ("mixed", "mixed"), ("fp64", "fp64")):
-        solvers[name] = PmSolver(P.descs, precision=prec, device=local, restart=20, maxit=200,
-                                 res_norm_min=RTOL * r0, pin_host=int(name == "mixed_learned"))
+        solvers[name] = make(P.descs, prec)
     solvers["mixed_learned"].attach_learned(net, omega=1.0, fallback_ratio=0.5)
     # the same system as NSTYPE-2 levels (one velocity block; the Galerkin
     # Oseen form has A12..A32 = 0 and A11 = A22 = A33), smoothed by the exact
@@ -259,8 +271,7 @@ def main():
     D1 = P.descs_one_block() if one_block else None
     if one_block:
         for name, prec in (("mixed_one_block", "mixed"), ("fp64_one_block", "fp64")):
-            solvers[name] = PmSolver(D1, precision=prec, device=local, restart=20, maxit=200,
-                                     res_norm_min=RTOL * r0, pin_host=int(name == "mixed_one_block"))
+            solvers[name] = make(D1, prec)
 
     def step(S):
         d_x.zero_()
@@ -337,7 +348,7 @@ def main():
         return {"value": sum(times) / len(times), "unit": "s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": 8 * n,
                 "update_matrices_s": sum(t_upd) / len(t_upd),
-                "pinned_host_bytes": S._lib.pm_pinned_bytes(S._h)}
+                "upload_mode": S.options.upload_mode}
 
     e2e = e2e1 = None
     if not args.no_e2e:
@@ -360,9 +371,11 @@ def main():
     a_ach, a_ms, a_bytes = kernel_roof(prof.get("apply"))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(),
-            "kernel": "k_vanka_residual<float,4> (cell-local residuals over full CSR rows, one colour)",
+            "kernel": "k_vanka_residual_rows<float,4,false,1> (cell-local residuals over full CSR "
+                      "rows, one colour; 8 lanes per row)",
             "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "bytes_per_launch": per_launch,
-            "apply_kernel": {"name": "k_vanka_apply<float> (stored-LU solve + update)",
+            "apply_kernel": {"name": "k_vanka_apply_tma (stored FP32 LU staged in shared memory "
+                                     "by bulk copies, substitution + update)",
                              "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,
                              "avg_launch_ms": a_ms, "bytes_per_launch": a_bytes}}
     one = None

@@ -88,13 +88,33 @@ typedef struct {
   int verbose;
   int pin_host;           /* 1: page-lock the caller's matrix value arrays in
                              pm_add_level (cudaHostRegister, as the TNSE_MGLevel4
-                             ctor does, src/FE/NSE_MGLevel4.C:168-188) so that
-                             pm_update_matrices copies at full link speed; the
-                             arrays stay registered until pm_destroy          */
+                             ctor does, src/FE/NSE_MGLevel4.C:168-188); the
+                             arrays stay registered until pm_destroy.  Off by
+                             default: on Grace-coupled GPUs pageable arrays
+                             copy as fast, and copies from registered memory
+                             were seen to slow to 5-10 GB/s after sustained
+                             GPU load                                        */
   int vanka_inverse;      /* mixed only: store each local block as its FP32
                              inverse (computed from the FP64 LU) so that the
                              sweep applies it as a GEMV; 0 (default) keeps
                              the FP32 LU factors and substitution            */
+  int residual_variant;   /* local-residual kernel of the Vanka sweep:
+                             0 (default) row groups, 8 lanes per CSR row;
+                             1 one flattened entry stream per cell with
+                             segmented sums; -1 time both on every level at
+                             pm_setup and keep the faster (the choice is
+                             reported by pm_level_variant)                   */
+  int apply_variant;      /* mixed, nine-block levels: 0 (default) the LU
+                             factors of each cell are staged in shared memory
+                             by bulk copies; 1 loaded directly; -1 time both
+                             at pm_setup per level                           */
+  int upload_mode;        /* how pm_add_level / pm_update_matrices move matrix
+                             values: 0 (default) copy-engine copies
+                             (cudaMemcpyAsync) then device conversions; 1 the
+                             SMs read the caller's arrays directly and write
+                             the FP64 and FP32 copies in one pass (needs a
+                             device that reads pageable host memory, e.g. a
+                             Grace-coupled GPU; PM_BADARG otherwise)         */
 } pm_options;
 
 /* One multigrid level in the reference's data layout.  Levels are added
@@ -173,6 +193,9 @@ int       pm_n_levels(pm_handle *h);
 int       pm_level_ndof(pm_handle *h, int level);
 /* velocity blocks of a level: 9 (NSTYPE 4) or 1 (NSTYPE 2); -1 if no such level */
 int       pm_level_blocks(pm_handle *h, int level);
+/* kernel variants a level runs: residual variant + 2 * apply variant (see
+ * pm_options.residual_variant / apply_variant); -1 if no such level */
+int       pm_level_variant(pm_handle *h, int level);
 
 /* Level operators (FP64 on host vectors of length ndof(level)). */
 pm_status pm_coupled_defect(pm_handle *h, int level, const double *x, const double *b,

@@ -86,6 +86,24 @@ def test_cell_vanka_mixed(P, gpu32, oracle):
     assert rel(gpu32.cell_vanka(2, u, f, 1), oracle.cell_vanka(2, u, f, 1)) < 5e-4
 
 
+@pytest.mark.parametrize("variant", [1, -1])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_residual_variants(P, oracle, variant, precision):
+    """The flattened-stream residual kernel and the direct-load apply
+    (variant 1) and the per-level choice of the tuner (-1) give the same
+    sweeps as the defaults (row groups, bulk-staged factors)."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    S = PmSolver(P.descs, precision=precision, residual_variant=variant, apply_variant=variant)
+    chosen = [S._lib.pm_level_variant(S._h, l) for l in range(3)]
+    assert all(v in (0, 1, 2, 3) for v in chosen)
+    if variant == 1:
+        assert chosen[1:] == [3, 3]
+    tol = 1e-9 if precision == "fp64" else 5e-4
+    for level in (1, 2):
+        u, f = 0.1 * rand(P, level, 6), rand(P, level, 7)
+        assert rel(S.cell_vanka(level, u, f, 2), oracle.cell_vanka(level, u, f, 2)) < tol
+
+
 def test_vcycle(P, gpu64, gpu32, oracle):
     v = rand(P, 2, 8)
     z_o = oracle.vcycle(v)

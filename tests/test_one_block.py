@@ -209,3 +209,24 @@ def test_coupled_blocks_fgmres(P, precision):
     assert rel(normalise_p(xg, nu), normalise_p(xo, nu)) < 1e-6
     if precision == "fp64":
         assert ig["iterations"] == io["iterations"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_upload_by_host_reads_matches_copies(P, precision):
+    """upload_mode=1 (the SMs read the caller's arrays, FP32 copies and the
+    Dirichlet-row zeroing of A12..A32 in the same pass) stores exactly what
+    the copy-engine path stores: identical operator, sweeps and V-cycle."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    Q = Coupled(P, 0.01, 11)
+    for descs in (Q.descs, P.descs_one_block()):
+        S0 = PmSolver(descs, precision=precision, upload_mode=0)
+        S1 = PmSolver(descs, precision=precision, upload_mode=1)
+        for level in (0, 1, 2):
+            x = rand(P, level, 31)
+            assert np.array_equal(S0.matvec(level, x), S1.matvec(level, x))
+        u, f = 0.1 * rand(P, 2, 32), rand(P, 2, 33)
+        assert np.array_equal(S0.cell_vanka(2, u, f, 1), S1.cell_vanka(2, u, f, 1))
+        v = rand(P, 2, 34)
+        assert np.array_equal(S0.vcycle(v), S1.vcycle(v))
+        S1.update_matrices(descs)
+        assert np.array_equal(S0.vcycle(v), S1.vcycle(v))

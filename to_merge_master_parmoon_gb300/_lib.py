@@ -38,7 +38,8 @@ class PmOptions(C.Structure):
         ("restart", C.c_int), ("maxit", C.c_int), ("minit", C.c_int),
         ("red_factor", C.c_double), ("res_norm_min", C.c_double), ("div_factor", C.c_double),
         ("device", C.c_int), ("use_graphs", C.c_int), ("verbose", C.c_int),
-        ("pin_host", C.c_int), ("vanka_inverse", C.c_int),
+        ("pin_host", C.c_int), ("vanka_inverse", C.c_int), ("residual_variant", C.c_int),
+        ("apply_variant", C.c_int), ("upload_mode", C.c_int),
     ]
 
 
@@ -81,6 +82,7 @@ GPU_SYMBOLS = {
     "pm_n_levels": (C.c_int, [_P]),
     "pm_level_ndof": (C.c_int, [_P, C.c_int]),
     "pm_level_blocks": (C.c_int, [_P, C.c_int]),
+    "pm_level_variant": (C.c_int, [_P, C.c_int]),
     "pm_coupled_defect": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, c_double_p, C.c_int]),
     "pm_defect": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, c_double_p, c_double_p]),
     "pm_matvec": (C.c_int, [_P, C.c_int, c_double_p, c_double_p]),

@@ -32,6 +32,12 @@ struct pm_mlp {
 using namespace pm;
 
 namespace {
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+namespace {
 
 struct CsrStore {
   int rows = 0, cols = 0, nnz = 0;
@@ -54,6 +60,8 @@ struct LevelDev {
   int nu = 0, np = 0, ndof = 0, nact = 0, hb = 0, ndir = 0, ncells = 0;
   int a_nnz = 0, b_nnz = 0, bt_nnz = 0;
   int structured = 0;  // velocity blocks: A12..A32 = 0 and A11 = A22 = A33 (exactly)
+  int res_variant = 0;  // local-residual kernel of the sweep (0 row groups, 1 stream)
+  int apply_variant = 0;  // FP32 LU apply: 0 bulk-staged factors, 1 direct loads
   std::vector<int> h_udofs, h_pdofs, h_parent, h_child, h_colour;
   bool has_colour = false;
   int *a_rowptr = nullptr, *a_col = nullptr, *b_rowptr = nullptr, *b_col = nullptr;
@@ -127,6 +135,7 @@ DevOp<float> LevelDev::op<float>() const {
 
 struct pm_handle {
   pm_options opt;
+  double t_update0 = 0.0;  // host clock at pm_update_matrices entry (verbose timing)
   cudaStream_t stream = nullptr;
   std::vector<LevelDev> L;
   bool setup_done = false;
@@ -140,6 +149,8 @@ struct pm_handle {
   double *hcol = nullptr;
   double *ydev = nullptr;
   int *status_d = nullptr;
+  int *sweep_err = nullptr;  // device flags of bounded waits inside sweep kernels
+  int num_sms = 0;
   // coarse direct solve
   int coarse_n = 0;
   double *coarse_lu = nullptr, *coarse_inv = nullptr, *coarse_b = nullptr, *coarse_x = nullptr;
@@ -253,6 +264,16 @@ bool use_inverse(const pm_handle *h) { return mixed(h) && h->opt.vanka_inverse !
 
 pm_status sync(pm_handle *h, const char *what) {
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return cuda_fail(h, what);
+  if (h->sweep_err) {  // bounded device waits that gave up (bulk-copy barriers)
+    int e = 0;
+    if (cudaMemcpy(&e, h->sweep_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return cuda_fail(h, what);
+    if (e) {
+      cudaMemset(h->sweep_err, 0, sizeof(int));
+      return fail(h, PM_TIMEOUT, std::string(what) + ": a bulk copy into shared memory did not "
+                                 "complete within the wait limit (sweep result invalid)");
+    }
+  }
   return PM_OK;
 }
 
@@ -296,12 +317,18 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
       cudaEventRecord(e0, h->stream);
     }
     PM_LAUNCH(launch_vanka_residual<T>(op, cells, Lv.colour_cells + b, n, u, rhs,
-                                       static_cast<T *>(Lv.dbuf), h->stream));
+                                       static_cast<T *>(Lv.dbuf), Lv.res_variant, h->stream));
     if (e1) cudaEventRecord(e1, h->stream);
     if (Lv.structured)
       PM_LAUNCH(launch_schur_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
                                       static_cast<const T *>(Lv.factors),
                                       static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
+    else if (sizeof(T) == sizeof(float) && !use_inverse(h) && Lv.apply_variant == 0)
+      PM_LAUNCH(launch_vanka_apply_tma(cells, Lv.nu, Lv.colour_cells + b, n,
+                                       static_cast<const float *>(Lv.factors), Lv.perm,
+                                       reinterpret_cast<const float *>(Lv.dbuf), (float)damp,
+                                       reinterpret_cast<float *>(u), h->sweep_err, h->num_sms,
+                                       h->stream));
     else
       PM_LAUNCH(launch_vanka_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
                                       static_cast<const T *>(Lv.factors), Lv.perm, use_inverse(h),
@@ -662,6 +689,77 @@ pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
 }
 
 // ------------------------------------------------------------- setup ------
+// Kernel choice per level (pm_options.residual_variant / apply_variant = -1):
+// both variants timed with CUDA events on the level's largest colour (zeroed
+// vectors, 3 launches after one warm-up launch), the faster one kept.
+template <typename T>
+pm_status tune_level(pm_handle *h, LevelDev &Lv) {
+  Lv.res_variant = h->opt.residual_variant > 0 ? 1 : 0;
+  Lv.apply_variant = h->opt.apply_variant > 0 ? 1 : 0;
+  const bool tune_res = h->opt.residual_variant < 0;
+  const bool tune_apply = h->opt.apply_variant < 0 && sizeof(T) == sizeof(float) &&
+                          !use_inverse(h) && !Lv.structured;
+  if ((!tune_res && !tune_apply) || Lv.ncells == 0) return PM_OK;
+  int kb = 0, nb = 0;
+  for (size_t k = 0; k + 1 < Lv.colouring.ptr.size(); ++k) {
+    const int n = Lv.colouring.ptr[k + 1] - Lv.colouring.ptr[k];
+    if (n > nb) {
+      nb = n;
+      kb = (int)k;
+    }
+  }
+  if (nb == 0) return PM_OK;
+  if (cudaMemsetAsync(Lv.sol, 0, sizeof(T) * Lv.ndof, h->stream) != cudaSuccess ||
+      cudaMemsetAsync(Lv.rhs, 0, sizeof(T) * Lv.ndof, h->stream) != cudaSuccess)
+    return cuda_fail(h, "tuning buffers");
+  const DevOp<T> op = Lv.op<T>();
+  const int *list = Lv.colour_cells + Lv.colouring.ptr[kb];
+  T *u = static_cast<T *>(Lv.sol), *rb = static_cast<T *>(Lv.dbuf);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto time_it = [&](auto &&launch, float &ms) -> pm_status {
+    for (int rep = 0; rep < 4; ++rep) {
+      if (rep == 1) cudaEventRecord(e0, h->stream);
+      PM_LAUNCH(launch());
+    }
+    cudaEventRecord(e1, h->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return cuda_fail(h, "tuning");
+    cudaEventElapsedTime(&ms, e0, e1);
+    return PM_OK;
+  };
+  pm_status st = PM_OK;
+  if (tune_res) {
+    float t[2] = {0.f, 0.f};
+    for (int v = 0; v < 2 && st == PM_OK; ++v)
+      st = time_it([&] {
+        return launch_vanka_residual<T>(op, Lv.cells(), list, nb, u,
+                                        static_cast<const T *>(Lv.rhs), rb, v, h->stream);
+      }, t[v]);
+    Lv.res_variant = t[1] < t[0] ? 1 : 0;
+  }
+  if (tune_apply && st == PM_OK) {
+    float t[2] = {0.f, 0.f};
+    float *uf = reinterpret_cast<float *>(u);
+    const float *F = static_cast<const float *>(Lv.factors);
+    const float *rf = reinterpret_cast<const float *>(rb);
+    st = time_it([&] {
+      return launch_vanka_apply_tma(Lv.cells(), Lv.nu, list, nb, F, Lv.perm, rf, 1.f, uf,
+                                    h->sweep_err, h->num_sms, h->stream);
+    }, t[0]);
+    if (st == PM_OK)
+      st = time_it([&] {
+        return launch_vanka_apply<float>(Lv.cells(), Lv.nu, list, nb, F, Lv.perm, false, rf, 1.f,
+                                         uf, h->stream);
+      }, t[1]);
+    Lv.apply_variant = t[1] < t[0] ? 1 : 0;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st == PM_OK) st = sync(h, "tuning");
+  return st;
+}
+
 pm_status factor_all(pm_handle *h) {
   if (cudaMemsetAsync(h->status_d, 0, sizeof(int), h->stream) != cudaSuccess)
     return cuda_fail(h, "status reset");
@@ -721,6 +819,36 @@ pm_status upload_values(pm_handle *h, LevelDev &Lv, const pm_level_desc *d, bool
   if (first) Lv.structured = nblk == 1;
   if ((nblk == 1) != (Lv.structured != 0))
     return fail(h, PM_BADARG, "A block count differs from the level's first upload");
+  if (h->opt.upload_mode == 1) {
+    // the SMs read the caller's arrays and write the FP64 (and FP32) copies
+    // in one pass; off-diagonal blocks are zeroed on the Dirichlet rows
+    for (int k = 0; k < nblk; ++k) {
+      if (first) {
+        PM_TRY(dalloc_padded(h, &Lv.a64[k], Lv.a_nnz));
+        if (mixed(h)) PM_TRY(dalloc_padded(h, &Lv.a32[k], Lv.a_nnz));
+      }
+      const bool offdiag = nblk == 9 && k != 0 && k != 4 && k != 8;
+      const long long zero_from = offdiag ? (long long)d->a_rowptr[Lv.nact] : (long long)Lv.a_nnz;
+      PM_LAUNCH(launch_host_upload(d->a[k], Lv.a64[k], mixed(h) ? Lv.a32[k] : nullptr, Lv.a_nnz,
+                                   zero_from, h->num_sms, h->stream));
+    }
+    for (int k = 0; k < 3; ++k) {
+      if (!d->b[k] || !d->bt[k]) return fail(h, PM_BADARG, "missing B/BT block");
+      if (first) {
+        PM_TRY(dalloc_padded(h, &Lv.b64[k], Lv.b_nnz));
+        PM_TRY(dalloc_padded(h, &Lv.bt64[k], Lv.bt_nnz));
+        if (mixed(h)) {
+          PM_TRY(dalloc_padded(h, &Lv.b32[k], Lv.b_nnz));
+          PM_TRY(dalloc_padded(h, &Lv.bt32[k], Lv.bt_nnz));
+        }
+      }
+      PM_LAUNCH(launch_host_upload(d->b[k], Lv.b64[k], mixed(h) ? Lv.b32[k] : nullptr, Lv.b_nnz,
+                                   Lv.b_nnz, h->num_sms, h->stream));
+      PM_LAUNCH(launch_host_upload(d->bt[k], Lv.bt64[k], mixed(h) ? Lv.bt32[k] : nullptr,
+                                   Lv.bt_nnz, Lv.bt_nnz, h->num_sms, h->stream));
+    }
+    return PM_OK;
+  }
   for (int k = 0; k < nblk; ++k) {
     if (first) PM_TRY(dalloc_padded(h, &Lv.a64[k], Lv.a_nnz));
     if (cudaMemcpyAsync(Lv.a64[k], d->a[k], sizeof(double) * Lv.a_nnz, cudaMemcpyHostToDevice,
@@ -819,6 +947,9 @@ void pm_default_options(pm_options *o) {
   o->verbose = 0;
   o->pin_host = 0;
   o->vanka_inverse = 0;
+  o->residual_variant = 0;
+  o->apply_variant = 0;
+  o->upload_mode = 0;
 }
 
 const char *pm_status_string(int s) {
@@ -859,6 +990,9 @@ pm_status pm_create(pm_handle **out, const pm_options *opt) {
   if (o.precision != PM_PREC_FP64 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.factor_fp32 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.pre_smooth < 0 || o.post_smooth < 0 || o.restart <= 0 || o.maxit <= 0) return PM_BADARG;
+  if (o.residual_variant < -1 || o.residual_variant > 1) return PM_BADARG;
+  if (o.apply_variant < -1 || o.apply_variant > 1) return PM_BADARG;
+  if (o.upload_mode < 0 || o.upload_mode > 1) return PM_BADARG;
   if (pm_device_count() <= 0) return PM_NO_DEVICE;
   if (cudaSetDevice(o.device) != cudaSuccess) {
     cudaGetLastError();
@@ -866,6 +1000,16 @@ pm_status pm_create(pm_handle **out, const pm_options *opt) {
   }
   pm_handle *h = new pm_handle();
   h->opt = o;
+  cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, o.device);
+  if (h->num_sms <= 0) h->num_sms = 1;
+  if (o.upload_mode == 1) {
+    int pageable = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, o.device);
+    if (!pageable) {
+      delete h;
+      return PM_BADARG;  // the SMs cannot read the caller's host arrays on this system
+    }
+  }
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return PM_CUDA_ERROR;
@@ -960,7 +1104,7 @@ pm_status pm_setup(pm_handle *h) {
                       (size_t)Lv.ncells * kSchurStride * es));
       } else {
         PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
-                      (size_t)Lv.ncells * NLOC * NLOC * es));
+                      (size_t)Lv.ncells * kFacStride * es));
         PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * NLOC));
       }
       PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.dbuf),
@@ -995,6 +1139,10 @@ pm_status pm_setup(pm_handle *h) {
   if (cudaMemsetAsync(h->counter, 0, 4 * sizeof(unsigned int), h->stream) != cudaSuccess)
     return cuda_fail(h, "counter reset");
   PM_TRY(dalloc(h, &h->status_d, 4));
+  PM_TRY(dalloc(h, &h->sweep_err, 4));
+  if (cudaMemsetAsync(h->sweep_err, 0, sizeof(int), h->stream) != cudaSuccess)
+    return cuda_fail(h, "flag reset");
+  if (mixed(h) && launch_vanka_apply_tma_init() < 0) return cuda_fail(h, "bulk-copy apply set-up");
   h->restart = std::max(1, std::min(h->opt.restart, h->opt.maxit));
   PM_TRY(dalloc(h, &h->hcol, (size_t)h->restart + 4));
   PM_TRY(dalloc(h, &h->ydev, (size_t)h->restart + 4));
@@ -1012,6 +1160,12 @@ pm_status pm_setup(pm_handle *h) {
   PM_TRY(dalloc(h, &h->xd, N));
   PM_TRY(dalloc(h, &h->bd, N));
   PM_TRY(factor_all(h));
+  for (size_t l = 1; l < h->L.size(); ++l) {
+    if (mixed(h))
+      PM_TRY(tune_level<float>(h, h->L[l]));
+    else
+      PM_TRY(tune_level<double>(h, h->L[l]));
+  }
   h->setup_done = true;
   return PM_OK;
 }
@@ -1019,6 +1173,7 @@ pm_status pm_setup(pm_handle *h) {
 pm_status pm_update_matrices(pm_handle *h, const pm_level_desc *levels, int n) {
   if (!h || !levels) return PM_BADARG;
   if (!h->setup_done) return PM_NOT_SETUP;
+  h->t_update0 = now_s();
   if (n != (int)h->L.size()) return fail(h, PM_BADARG, "level count mismatch");
   for (int l = 0; l < n; ++l) {
     LevelDev &Lv = h->L[l];
@@ -1027,6 +1182,19 @@ pm_status pm_update_matrices(pm_handle *h, const pm_level_desc *levels, int n) {
         d->bt_nnz != Lv.bt_nnz)
       return fail(h, PM_BADARG, "pattern changed");
     PM_TRY(upload_values(h, Lv, d, false));
+  }
+  if (h->opt.verbose) {
+    // host timing of the two phases (the sync separates them)
+    PM_TRY(sync(h, "upload"));
+    const double t1 = now_s();
+    PM_TRY(factor_all(h));
+    const double t2 = now_s();
+    double bytes = 0.0;
+    for (const LevelDev &Lv : h->L)
+      bytes += 8.0 * ((Lv.structured ? 1.0 : 9.0) * Lv.a_nnz + 3.0 * (Lv.b_nnz + Lv.bt_nnz));
+    std::fprintf(stderr, "pm_update_matrices: upload %.4f s (%.1f GB/s), factor %.4f s\n",
+                 t1 - h->t_update0, bytes / (t1 - h->t_update0) / 1e9, t2 - t1);
+    return PM_OK;
   }
   return factor_all(h);
 }
@@ -1055,6 +1223,10 @@ pm_status pm_destroy(pm_handle *h) {
 int pm_n_levels(pm_handle *h) { return h ? (int)h->L.size() : 0; }
 int pm_level_ndof(pm_handle *h, int l) {
   return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].ndof : -1;
+}
+int pm_level_variant(pm_handle *h, int l) {
+  return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].res_variant + 2 * h->L[l].apply_variant
+                                                : -1;
 }
 int pm_level_blocks(pm_handle *h, int l) {
   return (h && l >= 0 && l < (int)h->L.size()) ? (h->L[l].structured ? 1 : 9) : -1;

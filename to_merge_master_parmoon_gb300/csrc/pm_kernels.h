@@ -13,6 +13,9 @@ constexpr int NU_LOC = 27;                 // Q2 local velocity nodes
 constexpr int NP_LOC = 4;                  // P1disc local pressure DOFs
 constexpr int NLOC = 3 * NU_LOC + NP_LOC;  // 85: local Vanka block size
 constexpr int kRStride = 88;               // per-cell stride of the residual buffer
+// per-cell stride (values) of the stored 85x85 factors: 7225 rounded up so
+// every cell's block starts on a 16-byte boundary in FP32 and FP64 (bulk copies)
+constexpr int kFacStride = 7228;
 
 // One level's operator in precision T (device pointers).  The nine velocity
 // blocks share the CSR pattern; off-diagonal blocks are zero on Dirichlet rows
@@ -96,6 +99,10 @@ int launch_relax(T *u, const T *uold, T alpha, int n, cudaStream_t s);
 // zero off-diagonal velocity blocks on rows >= nact
 int launch_zero_dirichlet_offdiag(double *const a[9], const int *rowptr, int nu, int nact,
                                   cudaStream_t s);
+// d64 = src (host memory read by the SMs), d32 = (float)src if d32; entries
+// from zero_from on are zero.  Needs cudaDevAttrPageableMemoryAccess.
+int launch_host_upload(const double *src, double *d64, float *d32, long long n,
+                       long long zero_from, int num_sms, cudaStream_t s);
 // non-finite check: flag[0] |= 1 if any entry is not finite
 int launch_check_finite(const double *x, int n, int *flag, cudaStream_t s);
 
@@ -112,15 +119,29 @@ int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *fact
                         cudaStream_t s);
 // For the ncol cells listed in cell_list: local residual r = f - K u over the
 // full rows of the cell's 85 DOFs -> rbuf[slot*kRStride + i].
+// variant 0: row groups (8 lanes per row); 1: flattened row stream with
+// segmented sums.  Same result up to summation order.
 template <typename T>
 int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
-                          const T *u, const T *rhs, T *rbuf, cudaStream_t s);
+                          const T *u, const T *rhs, T *rbuf, int variant, cudaStream_t s);
 // Local solve with the stored factors and u[dofs] += damp * delta, for the
 // same cells (run after launch_vanka_residual of the whole colour).
 template <typename T>
 int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                        const T *factors, const uint8_t *perm, bool inverse, const T *rbuf,
                        T damp, T *u, cudaStream_t s);
+
+// Error bits of bounded device waits (sweep kernels, `err` arguments)
+constexpr int PM_ERR_BULK_TIMEOUT = 1;
+// Mixed-precision apply with the FP32 LU factors staged in shared memory by
+// bulk copies (two cell buffers per warp, three warps per CTA, at most
+// num_sms CTAs walking the colour's cells with a stride).  Same arithmetic
+// as launch_vanka_apply.  _init sets the kernel's shared-memory limit (call
+// once before any launch, outside stream capture).
+int launch_vanka_apply_tma_init();
+int launch_vanka_apply_tma(const DevCells &cells, int nu, const int *cell_list, int ncol,
+                           const float *factors, const uint8_t *perm, const float *rbuf, float damp,
+                           float *u, int *err, int num_sms, cudaStream_t s);
 
 // Block (Schur-complement) local solve for structured operators: per cell
 // A^{-1} (27x27, column-major), D (4x3x27), W = A^{-1} G (4x3x27) and S^{-1}

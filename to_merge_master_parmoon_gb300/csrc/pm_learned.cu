@@ -325,7 +325,16 @@ __global__ void k_cell_features(DevCells cells, int nu, const T *d, const float 
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-  const float sc = sqrtf(ss / NLOC);
+  // scale: the largest residual RMS of the cell and its 26 neighbours, so
+  // every feature is O(1) even where the cell's own residual is small
+  float sc = sqrtf(ss / NLOC);
+  {
+    const int nb = lane < kNeighbours ? nbr[(size_t)c * kNeighbours + lane] : -1;
+    float m = nb >= 0 ? summary[(size_t)nb * kSummary + 10] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    sc = fmaxf(sc, m);
+  }
   const float inv = sc > 0.f ? 1.f / sc : 0.f;
   if (lane == 0) scale[c] = sc;
   for (int i = lane; i < kMlpInPad; i += 32) {
@@ -337,6 +346,9 @@ __global__ void k_cell_features(DevCells cells, int nu, const T *d, const float 
       const int nb = nbr[(size_t)c * kNeighbours + n];
       v = nb >= 0 ? summary[(size_t)nb * kSummary + q] * inv : 0.f;
     }
+    // a cell whose own residual is tiny against its neighbours' would give
+    // unbounded features (and BF16 GEMM overflow): clamp
+    v = fminf(fmaxf(v, -kFeatureClamp), kFeatureClamp);
     if (Xb) Xb[(size_t)c * kMlpInPad + i] = __float2bfloat16(v);
     if (Xf && i < kMlpIn) Xf[(size_t)c * kMlpIn + i] = v;
   }

@@ -20,6 +20,7 @@ constexpr int kMlpOut = 85;
 constexpr int kMlpOutPad = 96;
 constexpr int kSummary = 12;
 constexpr int kNeighbours = 26;
+constexpr float kFeatureClamp = 1.0e3f;  // |feature| bound (features are O(1) residual ratios)
 
 // offsets of the parameter blocks in the flat FP32 parameter vector
 constexpr long long kOffW1 = 0;

@@ -327,6 +327,34 @@ __global__ void k_zero_dirichlet_offdiag(Ptr9 a, const int *rowptr, int nu, int 
   }
 }
 
+// Upload by SM loads of the caller's host array (through the CPU-GPU link;
+// the device must be able to read pageable host memory): d64 = src, and
+// d32 = (float)src when d32 is given; entries i >= zero_from are written as
+// zero (off-diagonal velocity blocks on the Dirichlet rows, which are
+// numbered last).  Four independent 8-byte loads per thread and iteration.
+__global__ void k_host_upload(const double *__restrict__ src, double *__restrict__ d64,
+                              float *__restrict__ d32, long long n, long long zero_from) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    double v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = src[i + q * stride];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long k = i + q * stride;
+      const double w = k < zero_from ? v[q] : 0.0;
+      d64[k] = w;
+      if (d32) d32[k] = (float)w;
+    }
+  }
+  for (; i < n; i += stride) {
+    const double w = i < zero_from ? src[i] : 0.0;
+    d64[i] = w;
+    if (d32) d32[i] = (float)w;
+  }
+}
+
 __global__ void k_check_finite(const double *x, int n, int *flag) {
   int bad = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -449,6 +477,16 @@ int launch_zero_dirichlet_offdiag(double *const a[9], const int *rowptr, int nu,
   Ptr9 p;
   for (int k = 0; k < 9; ++k) p.p[k] = a[k];
   k_zero_dirichlet_offdiag<<<grid_for(nu - nact), kBlock, 0, s>>>(p, rowptr, nu, nact);
+  return ok() < 0 ? -1 : 1;
+}
+int launch_host_upload(const double *src, double *d64, float *d32, long long n,
+                       long long zero_from, int num_sms, cudaStream_t s) {
+  if (n <= 0) return 0;
+  long long g = (n + 4LL * kBlock - 1) / (4LL * kBlock);
+  const long long cap = 8LL * num_sms;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  k_host_upload<<<(unsigned)g, kBlock, 0, s>>>(src, d64, d32, n, zero_from);
   return ok() < 0 ? -1 : 1;
 }
 int launch_check_finite(const double *x, int n, int *flag, cudaStream_t s) {

@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
     }
     __syncthreads();
   }
-  TF *F = factors + (size_t)cell * NLOC * NLOC;
+  TF *F = factors + (size_t)cell * kFacStride;
   if (INV) {
     // A^{-1} = U^{-1} L^{-1} P in FP32 from the factors, all 85 right-hand
     // sides at once: a float copy of L\U overlays S, Y holds P then A^{-1}
@@ -483,6 +483,126 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual(
   if (vp) R[3 * NU_LOC + lane] = rhs[3 * nu + my_p] - acc[3 * NU_LOC + lane];
 }
 
+// Row-group variant of the local residual: one warp per cell, the warp's
+// four 8-lane groups each own one row at a time (its A entries, then its BT
+// entries), VEC entries per lane per load, a fixed 3-step butterfly per row.
+// The cell's 27 velocity rows are taken in order of stencil size (8 Q2
+// vertices, 12 edge midpoints, 6 face centres, the centre: 125/75/45/27
+// entries on interior cells) so the four rows of a step have similar
+// lengths; the order only balances work, any local numbering is correct.
+__constant__ unsigned char c_row_order[NU_LOC] = {0, 2, 6, 8, 18, 20, 24, 26, 1, 3, 5, 7, 9, 11,
+                                                  15, 17, 19, 21, 23, 25, 4, 10, 12, 14, 16, 22,
+                                                  13};
+
+template <typename T, int VEC, int NV, int UR>
+__device__ __forceinline__ void row_group_sum(const int *__restrict__ col, const T *const *vals,
+                                              int rs, int re, int sl, const T *__restrict__ x0,
+                                              const T *__restrict__ x1, const T *__restrict__ x2,
+                                              bool gather3, T (&s)[3]) {
+  for (int g = rs / VEC + sl; g * VEC < re; g += 8 * UR) {
+    int ci[UR][VEC];
+    T v[UR][NV][VEC];
+#pragma unroll
+    for (int q = 0; q < UR; ++q) {
+      const int gq = g + 8 * q;
+      if (gq * VEC < re) {
+        VecLd<T, VEC>::idx(col + (size_t)gq * VEC, ci[q]);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) VecLd<T, VEC>::val(vals[k] + (size_t)gq * VEC, v[q][k]);
+      } else {
+#pragma unroll
+        for (int m = 0; m < VEC; ++m) {
+          ci[q][m] = 0;
+#pragma unroll
+          for (int k = 0; k < NV; ++k) v[q][k][m] = T(0);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < UR; ++q) {
+      const int e0 = (g + 8 * q) * VEC;
+#pragma unroll
+      for (int m = 0; m < VEC; ++m) {
+        const int e = e0 + m;
+        if (e >= rs && e < re) {
+          const int c = ci[q][m];
+          if (gather3) {
+            const T g0 = __ldg(x0 + c), g1 = __ldg(x1 + c), g2 = __ldg(x2 + c);
+            if constexpr (NV == 1) {
+              s[0] += v[q][0][m] * g0;
+              s[1] += v[q][0][m] * g1;
+              s[2] += v[q][0][m] * g2;
+            } else if constexpr (NV == 9) {
+              s[0] += v[q][0][m] * g0 + v[q][1][m] * g1 + v[q][2][m] * g2;
+              s[1] += v[q][3][m] * g0 + v[q][4][m] * g1 + v[q][5][m] * g2;
+              s[2] += v[q][6][m] * g0 + v[q][7][m] * g1 + v[q][8][m] * g2;
+            } else {  // B row: one output
+              s[0] += v[q][0][m] * g0 + v[q][1][m] * g1 + v[q][2][m] * g2;
+            }
+          } else {  // BT row: gather p, three outputs
+            const T pc = __ldg(x0 + c);
+            s[0] += v[q][0][m] * pc;
+            if constexpr (NV >= 3) {
+              s[1] += v[q][1][m] * pc;
+              s[2] += v[q][2][m] * pc;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+template <typename T, int VEC, bool ONE, int URA>
+__global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual_rows(
+    DevOp<T> op, DevCells cells, const int *__restrict__ list, int ncol, const T *__restrict__ u,
+    const T *__restrict__ rhs, T *__restrict__ rbuf) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = blockIdx.x * kResWarps + warp;
+  if (slot >= ncol) return;  // whole warp; no block-wide barrier in this kernel
+  const int cell = list[slot];
+  const int sub = lane >> 3, sl = lane & 7;
+  const int nu = op.nu;
+  const T *u1 = u, *u2 = u + nu, *u3 = u + 2 * nu, *p = u + 3 * nu;
+  const int *ud = cells.udofs + (size_t)cell * NU_LOC;
+  T *R = rbuf + (size_t)slot * kRStride;
+  // velocity rows: A (one or nine blocks) and, on active rows, BT
+  for (int step = 0; step < (NU_LOC + 3) / 4; ++step) {
+    const int k = step * 4 + sub;
+    const bool valid = k < NU_LOC;
+    const int a = valid ? c_row_order[k] : 0;
+    const int r = valid ? __ldg(ud + a) : 0;
+    T s[3] = {T(0), T(0), T(0)};
+    if (valid) {
+      row_group_sum<T, VEC, ONE ? 1 : 9, URA>(op.a_col, op.a, op.a_rowptr[r], op.a_rowptr[r + 1],
+                                              sl, u1, u2, u3, true, s);
+      if (r < op.nact)
+        row_group_sum<T, VEC, 3, 1>(op.bt_col, op.bt, op.bt_rowptr[r], op.bt_rowptr[r + 1], sl, p,
+                                    p, p, false, s);
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(kFull, s[c], o);
+    }
+    if (valid && sl == 0) {
+      R[a] = rhs[r] - s[0];
+      R[NU_LOC + a] = rhs[(size_t)nu + r] - s[1];
+      R[2 * NU_LOC + a] = rhs[(size_t)2 * nu + r] - s[2];
+    }
+  }
+  // pressure rows (B): group `sub` owns the cell's pressure DOF `sub`
+  {
+    const int r = cells.pdofs[(size_t)cell * NP_LOC + sub];
+    T s[3] = {T(0), T(0), T(0)};
+    row_group_sum<T, VEC, 3, 1>(op.b_col, op.b, op.b_rowptr[r], op.b_rowptr[r + 1], sl, u1, u2, u3,
+                                true, s);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) s[0] += __shfl_xor_sync(kFull, s[0], o);
+    if (sl == 0) R[3 * NU_LOC + sub] = rhs[(size_t)3 * nu + r] - s[0];
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void scatter_local(int i, T v, const int *ud, const int *pd, int nu,
                                               T *u) {
@@ -508,7 +628,7 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply_inv(
   const bool has2 = lane + 64 < NLOC;
   const T *R = rbuf + (size_t)slot * kRStride;
   const T r0 = R[lane], r1 = R[lane + 32], r2 = has2 ? R[lane + 64] : T(0);
-  const T *Xc = X + (size_t)cell * NLOC * NLOC;
+  const T *Xc = X + (size_t)cell * kFacStride;
   T a0 = 0, a1 = 0, a2 = 0;
 #pragma unroll 17
   for (int j = 0; j < NLOC; ++j) {
@@ -541,7 +661,7 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
   T y0 = R[__ldg(pc + lane)];
   T y1 = R[__ldg(pc + lane + 32)];
   T y2 = has2 ? R[__ldg(pc + lane + 64)] : T(0);
-  const T *Fc = F + (size_t)cell * NLOC * NLOC;
+  const T *Fc = F + (size_t)cell * kFacStride;
   // forward substitution with the unit lower factor, columns 0..83 in blocks
   // of 4, the next block's column entries loaded while this one is used
   T cur[4][3], nxt[4][3];
@@ -875,13 +995,21 @@ int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *fact
 
 template <typename T>
 int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
-                          const T *u, const T *rhs, T *rbuf, cudaStream_t s) {
+                          const T *u, const T *rhs, T *rbuf, int variant, cudaStream_t s) {
   if (ncol <= 0) return 0;
   constexpr int VEC = sizeof(T) == 4 ? 4 : 2;
   constexpr int U = sizeof(T) == 4 ? 1 : 2;
   const int grid = (ncol + kResWarps - 1) / kResWarps;
-  k_vanka_residual<T, VEC, U><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list, ncol, u, rhs,
-                                                             rbuf);
+  if (variant == 1) {
+    k_vanka_residual<T, VEC, U><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list, ncol, u, rhs,
+                                                               rbuf);
+  } else if (op.structured) {
+    k_vanka_residual_rows<T, VEC, true, 2><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list,
+                                                                          ncol, u, rhs, rbuf);
+  } else {
+    k_vanka_residual_rows<T, VEC, false, 1><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list,
+                                                                           ncol, u, rhs, rbuf);
+  }
   return ok() < 0 ? -1 : 1;
 }
 
@@ -955,7 +1083,7 @@ template int launch_vanka_factor<float>(const DevOp<double> &, const DevCells &,
                                         uint8_t *, bool, bool, int *, cudaStream_t);
 #define PM_VINST(T)                                                                                 \
   template int launch_vanka_residual<T>(const DevOp<T> &, const DevCells &, const int *, int,      \
-                                        const T *, const T *, T *, cudaStream_t);                  \
+                                        const T *, const T *, T *, int, cudaStream_t);             \
   template int launch_vanka_apply<T>(const DevCells &, int, const int *, int, const T *,           \
                                      const uint8_t *, bool, const T *, T, T *, cudaStream_t);
 PM_VINST(double)

@@ -18,6 +18,7 @@ from ._lib import gpu_lib
 from .solver import PmError, PmSolver
 
 N_IN, N_HIDDEN, N_OUT = 397, 256, 85
+FEATURE_CLAMP = 1.0e3  # |feature| bound of the feature kernel (kFeatureClamp)
 
 
 class Mlp:
@@ -112,6 +113,8 @@ def harvest_pairs(problems, n_cycles: int = 8, device: int = 0, precision: str =
     X, T = X[:n], T[:n]
     keep = torch.isfinite(X).all(1) & torch.isfinite(T).all(1)
     keep &= T.pow(2).mean(1).sqrt() <= max_target_rms
+    # cells at the feature clamp (own residual ~0 against their neighbours')
+    keep &= X.abs().amax(1) < 0.999 * FEATURE_CLAMP
     return X[keep].contiguous(), T[keep].contiguous()
 
 
