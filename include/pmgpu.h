@@ -99,15 +99,23 @@ typedef struct {
                              sweep applies it as a GEMV; 0 (default) keeps
                              the FP32 LU factors and substitution            */
   int residual_variant;   /* local-residual kernel of the Vanka sweep:
-                             0 (default) row groups, 8 lanes per CSR row;
-                             1 one flattened entry stream per cell with
-                             segmented sums; -1 time both on every level at
-                             pm_setup and keep the faster (the choice is
-                             reported by pm_level_variant)                   */
-  int apply_variant;      /* mixed, nine-block levels: 0 (default) the LU
-                             factors of each cell are staged in shared memory
-                             by bulk copies; 1 loaded directly; -1 time both
-                             at pm_setup per level                           */
+                             0 (default) per level: row groups (8 lanes per
+                             CSR row), except the flattened entry stream with
+                             segmented sums on FP32 nine-block levels (faster
+                             there); 1 row groups everywhere; 2 the stream
+                             everywhere; -1 time both on every level at
+                             pm_setup and keep the faster                    */
+  int apply_variant;      /* LU apply of nine-block levels, factor columns
+                             loaded from HBM with register prefetch: 0
+                             (default) per level: two cells per warp (half a
+                             warp per cell) in FP64, one cell per warp in
+                             FP32 (each measured faster there); 1 (FP32
+                             only; FP64 levels use pairs) each cell's factors
+                             staged in shared memory by bulk copies; 2 one
+                             cell per warp; -1 time them per level at
+                             pm_setup.  pm_level_variant reports residual
+                             kernel (0 rows, 1 stream) + 2 * apply kernel
+                             (0 pairs, 1 bulk, 2 single)                     */
   int upload_mode;        /* how pm_add_level / pm_update_matrices move matrix
                              values: 0 (default) copy-engine copies
                              (cudaMemcpyAsync) then device conversions; 1 the
@@ -193,8 +201,9 @@ int       pm_n_levels(pm_handle *h);
 int       pm_level_ndof(pm_handle *h, int level);
 /* velocity blocks of a level: 9 (NSTYPE 4) or 1 (NSTYPE 2); -1 if no such level */
 int       pm_level_blocks(pm_handle *h, int level);
-/* kernel variants a level runs: residual variant + 2 * apply variant (see
- * pm_options.residual_variant / apply_variant); -1 if no such level */
+/* kernels a level runs: residual kernel (0 row groups, 1 stream) + 2 * apply
+ * kernel (0 two cells per warp, 1 bulk-staged, 2 one cell per warp); -1 if
+ * no such level */
 int       pm_level_variant(pm_handle *h, int level);
 
 /* Level operators (FP64 on host vectors of length ndof(level)). */

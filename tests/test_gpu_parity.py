@@ -86,22 +86,46 @@ def test_cell_vanka_mixed(P, gpu32, oracle):
     assert rel(gpu32.cell_vanka(2, u, f, 1), oracle.cell_vanka(2, u, f, 1)) < 5e-4
 
 
-@pytest.mark.parametrize("variant", [1, -1])
+@pytest.mark.parametrize("variant", [1, 2, -1])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_residual_variants(P, oracle, variant, precision):
-    """The flattened-stream residual kernel and the direct-load apply
-    (variant 1) and the per-level choice of the tuner (-1) give the same
-    sweeps as the defaults (row groups, bulk-staged factors)."""
+def test_kernel_variants(P, oracle, variant, precision):
+    """Every residual kernel (1 row groups, 2 flattened stream), every LU
+    apply (1 bulk-staged or two cells per warp, 2 one cell per warp) and the
+    tuner's per-level choice (-1) give the same sweeps as the oracle."""
     from to_merge_master_parmoon_gb300 import PmSolver
     S = PmSolver(P.descs, precision=precision, residual_variant=variant, apply_variant=variant)
     chosen = [S._lib.pm_level_variant(S._h, l) for l in range(3)]
-    assert all(v in (0, 1, 2, 3) for v in chosen)
+    assert all(0 <= v <= 5 for v in chosen)
+    bulk = 2 if precision == "mixed" else 0  # the bulk-staged apply is FP32 only
     if variant == 1:
-        assert chosen[1:] == [3, 3]
+        assert chosen[1:] == [bulk, bulk]  # row groups, bulk-staged (FP32) or two cells per warp
+    if variant == 2:
+        assert chosen[1:] == [5, 5]  # flattened stream, one cell per warp
     tol = 1e-9 if precision == "fp64" else 5e-4
     for level in (1, 2):
         u, f = 0.1 * rand(P, level, 6), rand(P, level, 7)
         assert rel(S.cell_vanka(level, u, f, 2), oracle.cell_vanka(level, u, f, 2)) < tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_default_kernels(P, gpu64, gpu32, precision):
+    """The per-level defaults: stream residual + one cell per warp in FP32,
+    row groups + two cells per warp in FP64 (coarsest level: no cells)."""
+    S = gpu64 if precision == "fp64" else gpu32
+    want = 0 if precision == "fp64" else 1 + 2 * 2
+    assert [S._lib.pm_level_variant(S._h, l) for l in range(1, 3)] == [want, want]
+
+
+def test_inverse_apply(P, oracle):
+    """vanka_inverse=1: the FP32 inverse of every local block (computed from
+    the FP32 LU factors by a separate kernel) applied as a GEMV."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    S = PmSolver(P.descs, precision="mixed", vanka_inverse=1)
+    for level in (1, 2):
+        u, f = 0.1 * rand(P, level, 6), rand(P, level, 7)
+        assert rel(S.cell_vanka(level, u, f, 2), oracle.cell_vanka(level, u, f, 2)) < 5e-4
+    v = rand(P, 2, 8)
+    assert rel(S.vcycle(v), oracle.vcycle(v)) < 5e-4
 
 
 def test_vcycle(P, gpu64, gpu32, oracle):

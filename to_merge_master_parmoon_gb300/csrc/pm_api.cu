@@ -60,8 +60,8 @@ struct LevelDev {
   int nu = 0, np = 0, ndof = 0, nact = 0, hb = 0, ndir = 0, ncells = 0;
   int a_nnz = 0, b_nnz = 0, bt_nnz = 0;
   int structured = 0;  // velocity blocks: A12..A32 = 0 and A11 = A22 = A33 (exactly)
-  int res_variant = 0;  // local-residual kernel of the sweep (0 row groups, 1 stream)
-  int apply_variant = 0;  // FP32 LU apply: 0 bulk-staged factors, 1 direct loads
+  int res_variant = 0;    // local-residual kernel of the sweep (0 row groups, 1 stream)
+  int apply_variant = 0;  // LU apply: 0 two cells per warp, 1 bulk-staged (FP32), 2 one cell per warp
   std::vector<int> h_udofs, h_pdofs, h_parent, h_child, h_colour;
   bool has_colour = false;
   int *a_rowptr = nullptr, *a_col = nullptr, *b_rowptr = nullptr, *b_col = nullptr;
@@ -323,7 +323,7 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
       PM_LAUNCH(launch_schur_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
                                       static_cast<const T *>(Lv.factors),
                                       static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
-    else if (sizeof(T) == sizeof(float) && !use_inverse(h) && Lv.apply_variant == 0)
+    else if (sizeof(T) == sizeof(float) && !use_inverse(h) && Lv.apply_variant == 1)
       PM_LAUNCH(launch_vanka_apply_tma(cells, Lv.nu, Lv.colour_cells + b, n,
                                        static_cast<const float *>(Lv.factors), Lv.perm,
                                        reinterpret_cast<const float *>(Lv.dbuf), (float)damp,
@@ -332,7 +332,8 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
     else
       PM_LAUNCH(launch_vanka_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
                                       static_cast<const T *>(Lv.factors), Lv.perm, use_inverse(h),
-                                      static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
+                                      static_cast<const T *>(Lv.dbuf), damp, u,
+                                      Lv.apply_variant == 0, h->stream));
     if (e2) {
       cudaEventRecord(e2, h->stream);
       // algorithmic bytes of this colour: the level's unique Vanka-sweep
@@ -694,11 +695,18 @@ pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
 // vectors, 3 launches after one warm-up launch), the faster one kept.
 template <typename T>
 pm_status tune_level(pm_handle *h, LevelDev &Lv) {
-  Lv.res_variant = h->opt.residual_variant > 0 ? 1 : 0;
-  Lv.apply_variant = h->opt.apply_variant > 0 ? 1 : 0;
+  // defaults (option 0): row groups except on FP32 nine-block levels, where
+  // the flattened stream measured faster; LU apply with two cells per warp
+  // in FP64 (the FP64 chain is the bound), one cell per warp in FP32
+  const int rule_res = (sizeof(T) == sizeof(float) && !Lv.structured) ? 1 : 0;
+  const int ro = h->opt.residual_variant;
+  Lv.res_variant = ro == 0 ? rule_res : (ro == 2 ? 1 : 0);
+  const bool can_bulk = sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured;
+  const int ao = h->opt.apply_variant;
+  const int rule_apply = sizeof(T) == sizeof(double) ? 0 : 2;
+  Lv.apply_variant = ao == 0 ? rule_apply : (ao == 2 ? 2 : (can_bulk ? 1 : 0));
   const bool tune_res = h->opt.residual_variant < 0;
-  const bool tune_apply = h->opt.apply_variant < 0 && sizeof(T) == sizeof(float) &&
-                          !use_inverse(h) && !Lv.structured;
+  const bool tune_apply = h->opt.apply_variant < 0 && !use_inverse(h) && !Lv.structured;
   if ((!tune_res && !tune_apply) || Lv.ncells == 0) return PM_OK;
   int kb = 0, nb = 0;
   for (size_t k = 0; k + 1 < Lv.colouring.ptr.size(); ++k) {
@@ -736,23 +744,33 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
         return launch_vanka_residual<T>(op, Lv.cells(), list, nb, u,
                                         static_cast<const T *>(Lv.rhs), rb, v, h->stream);
       }, t[v]);
-    Lv.res_variant = t[1] < t[0] ? 1 : 0;
+    Lv.res_variant = t[1] < t[0] ? 1 : 0;  // kernel index: 0 row groups, 1 stream
   }
   if (tune_apply && st == PM_OK) {
-    float t[2] = {0.f, 0.f};
-    float *uf = reinterpret_cast<float *>(u);
-    const float *F = static_cast<const float *>(Lv.factors);
-    const float *rf = reinterpret_cast<const float *>(rb);
-    st = time_it([&] {
-      return launch_vanka_apply_tma(Lv.cells(), Lv.nu, list, nb, F, Lv.perm, rf, 1.f, uf,
-                                    h->sweep_err, h->num_sms, h->stream);
-    }, t[0]);
-    if (st == PM_OK)
-      st = time_it([&] {
-        return launch_vanka_apply<float>(Lv.cells(), Lv.nu, list, nb, F, Lv.perm, false, rf, 1.f,
-                                         uf, h->stream);
-      }, t[1]);
-    Lv.apply_variant = t[1] < t[0] ? 1 : 0;
+    // kernel index: 0 two cells per warp, 1 bulk-staged (FP32 only), 2 one cell per warp
+    float t[3] = {0.f, 1e30f, 0.f};
+    const T *F = static_cast<const T *>(Lv.factors);
+    for (int v = 0; v < 3 && st == PM_OK; ++v) {
+      if (v == 1) {
+        if (!can_bulk) continue;
+        st = time_it([&] {
+          return launch_vanka_apply_tma(Lv.cells(), Lv.nu, list, nb,
+                                        reinterpret_cast<const float *>(F), Lv.perm,
+                                        reinterpret_cast<const float *>(rb), 1.f,
+                                        reinterpret_cast<float *>(u), h->sweep_err, h->num_sms,
+                                        h->stream);
+        }, t[1]);
+      } else {
+        st = time_it([&] {
+          return launch_vanka_apply<T>(Lv.cells(), Lv.nu, list, nb, F, Lv.perm, false, rb, T(1), u,
+                                       v == 0, h->stream);
+        }, t[v]);
+      }
+    }
+    int best = 0;
+    for (int v = 1; v < 3; ++v)
+      if (t[v] < t[best]) best = v;
+    Lv.apply_variant = best;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -990,8 +1008,8 @@ pm_status pm_create(pm_handle **out, const pm_options *opt) {
   if (o.precision != PM_PREC_FP64 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.factor_fp32 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.pre_smooth < 0 || o.post_smooth < 0 || o.restart <= 0 || o.maxit <= 0) return PM_BADARG;
-  if (o.residual_variant < -1 || o.residual_variant > 1) return PM_BADARG;
-  if (o.apply_variant < -1 || o.apply_variant > 1) return PM_BADARG;
+  if (o.residual_variant < -1 || o.residual_variant > 2) return PM_BADARG;
+  if (o.apply_variant < -1 || o.apply_variant > 2) return PM_BADARG;
   if (o.upload_mode < 0 || o.upload_mode > 1) return PM_BADARG;
   if (pm_device_count() <= 0) return PM_NO_DEVICE;
   if (cudaSetDevice(o.device) != cudaSuccess) {
@@ -1240,6 +1258,25 @@ int pm_level_blocks(pm_handle *h, int l) {
       return fail((h), PM_BADARG, "level out of range");                   \
   } while (0)
 
+// Sweep-kernel timings recorded since the last collection (events of the
+// residual and apply launches, after a synchronisation) into the totals.
+static void collect_profile(pm_handle *h) {
+  if (!h->prof) return;
+  for (size_t k = 0; k + 2 < h->evused; k += 3) {
+    float t0 = 0.f, t1 = 0.f;
+    cudaEventElapsedTime(&t0, h->evpool[k], h->evpool[k + 1]);
+    cudaEventElapsedTime(&t1, h->evpool[k + 1], h->evpool[k + 2]);
+    h->prof_ms[0] += t0;
+    h->prof_ms[1] += t1;
+    h->prof_launches[0]++;
+    h->prof_launches[1]++;
+    h->prof_sum_bytes[0] += h->prof_bytes[2 * (k / 3)];
+    h->prof_sum_bytes[1] += h->prof_bytes[2 * (k / 3) + 1];
+  }
+  h->evused = 0;
+  h->prof_bytes.clear();
+}
+
 static pm_status h2d(pm_handle *h, double *d, const double *s, size_t n) {
   if (cudaMemcpyAsync(d, s, n * sizeof(double), cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
     return cuda_fail(h, "H2D");
@@ -1300,7 +1337,9 @@ pm_status pm_cell_vanka(pm_handle *h, int level, double *u, const double *rhs, i
   } else {
     for (int s = 0; s < sweeps; ++s) PM_TRY(vanka_sweep<double>(h, Lv, Lv.x64, Lv.y64));
   }
-  return d2h(h, u, Lv.x64, Lv.ndof);
+  const pm_status st = d2h(h, u, Lv.x64, Lv.ndof);
+  collect_profile(h);
+  return st;
 }
 
 pm_status pm_restrict(pm_handle *h, int level, const double *fine, double *coarse) {
@@ -1370,19 +1409,7 @@ pm_status pm_solve_device(pm_handle *h, double *d_sol, const double *d_rhs, pm_r
   r.solve_ms = ms;
   r.setup_ms = h->last_factor_ms;
   r.status = st;
-  if (h->prof) {
-    for (size_t k = 0; k + 2 < h->evused; k += 3) {
-      float t0 = 0.f, t1 = 0.f;
-      cudaEventElapsedTime(&t0, h->evpool[k], h->evpool[k + 1]);
-      cudaEventElapsedTime(&t1, h->evpool[k + 1], h->evpool[k + 2]);
-      h->prof_ms[0] += t0;
-      h->prof_ms[1] += t1;
-      h->prof_launches[0]++;
-      h->prof_launches[1]++;
-      h->prof_sum_bytes[0] += h->prof_bytes[2 * (k / 3)];
-      h->prof_sum_bytes[1] += h->prof_bytes[2 * (k / 3) + 1];
-    }
-  }
+  collect_profile(h);
   if (out) *out = r;
   return st;
 }

@@ -112,7 +112,8 @@ int launch_check_finite(const double *x, int n, int *flag, cudaStream_t s);
 // in TF with the reciprocal of U's diagonal on the diagonal, and the row
 // permutation as uint8 (row i of PA = row perm[i] of A).
 // With inverse (FP32 storage only) the stored block is A^{-1} (column-major),
-// computed in FP32 from the LU factors; perm is still written.
+// computed in FP32 from the stored LU factors by a second kernel; perm is
+// still written.
 template <typename TF>
 int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *factors,
                         uint8_t *perm, bool factor_fp32, bool inverse, int *status,
@@ -125,11 +126,12 @@ template <typename T>
 int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
                           const T *u, const T *rhs, T *rbuf, int variant, cudaStream_t s);
 // Local solve with the stored factors and u[dofs] += damp * delta, for the
-// same cells (run after launch_vanka_residual of the whole colour).
+// same cells (run after launch_vanka_residual of the whole colour).  pairs:
+// two cells per warp (half-warp per cell) instead of one.
 template <typename T>
 int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                        const T *factors, const uint8_t *perm, bool inverse, const T *rbuf,
-                       T damp, T *u, cudaStream_t s);
+                       T damp, T *u, bool pairs, cudaStream_t s);
 
 // Error bits of bounded device waits (sweep kernels, `err` arguments)
 constexpr int PM_ERR_BULK_TIMEOUT = 1;

@@ -43,12 +43,8 @@ __device__ __forceinline__ T ld_stream(const T *p) {
 // exactly the reference's System layout.  Right-looking LU with partial
 // pivoting (first maximal |pivot|, dgetrf's choice).
 constexpr int kFactorThreads = 256;
-// float offset of the inverse's workspace (16-byte aligned, after the float
-// copy of the factors); 2 * (85*85+3) floats = 57,824 bytes of shared memory
-constexpr int kInvYOffset = NLOC * NLOC + 3;
-constexpr size_t kInvSmem = sizeof(float) * 2 * kInvYOffset;
 
-template <typename TC, typename TF, bool INV>
+template <typename TC, typename TF>
 __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> op, DevCells cells,
                                                                  TF *__restrict__ factors,
                                                                  uint8_t *__restrict__ perm,
@@ -190,61 +186,56 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
     __syncthreads();
   }
   TF *F = factors + (size_t)cell * kFacStride;
-  if (INV) {
-    // A^{-1} = U^{-1} L^{-1} P in FP32 from the factors, all 85 right-hand
-    // sides at once: a float copy of L\U overlays S, Y holds P then A^{-1}
-    // (column-major), both inside the same 57.8 KB of shared memory.
-    float *Lf = reinterpret_cast<float *>(smem_raw);
-    float *Y = reinterpret_cast<float *>(smem_raw) + kInvYOffset;
-    constexpr int PER = (NLOC * NLOC + kFactorThreads - 1) / kFactorThreads;
-    float tmp[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int t = tid + q * kFactorThreads;
-      tmp[q] = t < NLOC * NLOC ? (float)S[t] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int t = tid + q * kFactorThreads;
-      if (t < NLOC * NLOC) Lf[t] = tmp[q];
-    }
-    for (int t = tid; t < NLOC * NLOC; t += kFactorThreads) {
-      const int i = t % NLOC, j = t / NLOC;
-      Y[t] = (pm[i] == j) ? 1.f : 0.f;
-    }
-    __syncthreads();
-    for (int k = 0; k < NLOC - 1; ++k) {  // unit lower triangle
-      for (int j = warp; j < NLOC; j += nwarps) {
-        const float ykj = Y[j * NLOC + k];
-        if (ykj != 0.f)
-          for (int i = k + 1 + lane; i < NLOC; i += 32) Y[j * NLOC + i] -= Lf[k * NLOC + i] * ykj;
-      }
-      __syncthreads();
-    }
-    for (int k = NLOC - 1; k >= 0; --k) {  // upper triangle
-      const float d = Lf[k * NLOC + k];
-      const float rd = d != 0.f ? 1.f / d : 0.f;
-      for (int j = tid; j < NLOC; j += kFactorThreads) Y[j * NLOC + k] *= rd;
-      __syncthreads();
-      for (int j = warp; j < NLOC; j += nwarps) {
-        const float xkj = Y[j * NLOC + k];
-        if (xkj != 0.f)
-          for (int i = lane; i < k; i += 32) Y[j * NLOC + i] -= Lf[k * NLOC + i] * xkj;
-      }
-      __syncthreads();
-    }
-    for (int t = tid; t < NLOC * NLOC; t += kFactorThreads) F[t] = (TF)Y[t];
-  } else {
-    for (int t = tid; t < NLOC * NLOC; t += kFactorThreads) {
-      const int i = t % NLOC, j = t / NLOC;
-      TC v = S[t];
-      if (i == j) v = (v != TC(0)) ? TC(1) / v : TC(0);
-      F[t] = (TF)v;
-    }
+  for (int t = tid; t < NLOC * NLOC; t += kFactorThreads) {
+    const int i = t % NLOC, j = t / NLOC;
+    TC v = S[t];
+    if (i == j) v = (v != TC(0)) ? TC(1) / v : TC(0);
+    F[t] = (TF)v;
   }
   if (tid < NLOC) perm[(size_t)cell * NLOC + tid] = pm[tid];
   if (tid == 0 && singular) atomicOr(status, 1);
+}
+
+// ---------------------------------------------------------------- inverse ---
+// A^{-1} = U^{-1} L^{-1} P in FP32 from the stored FP32 factors of one cell
+// (column-major, unit L below the diagonal, 1/U_jj on it), written over
+// them.  One CTA per cell; thread j < 85 computes column j: y = P e_j, then
+// column-oriented forward (y_i -= L_ik y_k, i > k) and backward
+// (x_k = y_k / U_kk, y_i -= U_ik x_k, i < k) substitution, the factor
+// columns read from shared memory as broadcasts.  85^3 FMA per cell.
+constexpr int kInvThreadsLU = 96;
+__global__ void __launch_bounds__(kInvThreadsLU) k_lu_inverse_f32(float *__restrict__ factors,
+                                                                  const uint8_t *__restrict__ perm) {
+  __shared__ float LU[NLOC * NLOC];
+  __shared__ unsigned char pm[NLOC];
+  const int cell = blockIdx.x, j = threadIdx.x;
+  float *F = factors + (size_t)cell * kFacStride;
+  for (int t = threadIdx.x; t < NLOC * NLOC; t += kInvThreadsLU) LU[t] = F[t];
+  if (threadIdx.x < NLOC) pm[threadIdx.x] = perm[(size_t)cell * NLOC + threadIdx.x];
+  __syncthreads();
+  float y[NLOC];
+#pragma unroll
+  for (int i = 0; i < NLOC; ++i) y[i] = (j < NLOC && pm[i] == j) ? 1.f : 0.f;
+#pragma unroll
+  for (int k = 0; k < NLOC - 1; ++k) {
+    const float yk = y[k];
+#pragma unroll
+    for (int i = k + 1; i < NLOC; ++i) y[i] -= LU[k * NLOC + i] * yk;
+  }
+#pragma unroll
+  for (int k = NLOC - 1; k >= 0; --k) {
+    const float xk = y[k] * LU[k * NLOC + k];
+    y[k] = xk;
+#pragma unroll
+    for (int i = 0; i < k; ++i) y[i] -= LU[k * NLOC + i] * xk;
+  }
+  __syncthreads();  // every thread is done with the factors
+  if (j < NLOC) {
+#pragma unroll
+    for (int i = 0; i < NLOC; ++i) LU[j * NLOC + i] = y[i];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < NLOC * NLOC; t += kInvThreadsLU) F[t] = LU[t];
 }
 
 // ------------------------------------------------------------------ apply ---
@@ -736,6 +727,105 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
   if (has2) scatter_local(lane + 64, damp * y2, ud, pd, nu, u);
 }
 
+// Two cells per warp: each half-warp owns one cell of the colour and each of
+// its lanes rows hl, hl+16, ..., hl+80 (six per lane), so a warp keeps the
+// factor columns of two cells in flight (the substitution chain, not the
+// bandwidth, bounds one cell per warp).  Columns are processed in blocks of
+// four, the next block's entries loaded while the current one is used; the
+// row owning column j is held by half-lane j & 15 in slot j >> 4, so every
+// index below is a compile-time constant after unrolling.
+template <typename T>
+__device__ __forceinline__ void load_cols(T (&b)[4][6], const T *Fc, int hl, int j0, int dir,
+                                          bool lower) {
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int j = j0 + dir * t;
+    const bool jok = j >= 0 && j < NLOC;
+    const T *col = Fc + (size_t)(jok ? j : 0) * NLOC;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const int r = hl + 16 * q;
+      const bool want = jok && r < NLOC && (lower ? r > j : r <= j);
+      b[t][q] = want ? ld_stream(col + r) : T(0);
+    }
+  }
+}
+
+template <typename T, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_vanka_apply2(
+    DevCells cells, int nu, const int *__restrict__ list, int ncol, const T *__restrict__ F,
+    const uint8_t *__restrict__ perm, const T *__restrict__ rbuf, T damp, T *__restrict__ u) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pair = blockIdx.x * WARPS + warp;
+  if (2 * pair >= ncol) return;  // whole warp
+  const int half = lane >> 4, hl = lane & 15;
+  const int slot = 2 * pair + half;
+  const bool live = slot < ncol;
+  const int cslot = live ? slot : slot - 1;  // an idle half repeats its partner's cell
+  const int cell = list[cslot];
+  const uint8_t *pc = perm + (size_t)cell * NLOC;
+  const T *R = rbuf + (size_t)cslot * kRStride;
+  T y[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int r = hl + 16 * q;
+    y[q] = r < NLOC ? R[__ldg(pc + r)] : T(0);
+  }
+  const T *Fc = F + (size_t)cell * kFacStride;
+  T cur[4][6], nxt[4][6];
+  // forward substitution with the unit lower factor, columns 0..83
+  load_cols(cur, Fc, hl, 0, 1, true);
+#pragma unroll
+  for (int blk = 0; blk < (NLOC - 1) / 4; ++blk) {  // 21 blocks of 4 columns
+    const int j0 = 4 * blk;
+    if (blk + 1 < (NLOC - 1) / 4) load_cols(nxt, Fc, hl, j0 + 4, 1, true);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int j = j0 + t;
+      const T yj = __shfl_sync(kFull, y[j >> 4], j & 15, 16);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) y[q] -= cur[t][q] * yj;
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) cur[t][q] = nxt[t][q];
+  }
+  // back substitution with U (diagonal stores 1/U_jj), columns 84..0 in
+  // blocks 87..84 (only 84 real), 83..80, ..., 3..0
+  load_cols(cur, Fc, hl, 87, -1, false);
+#pragma unroll
+  for (int blk = 21; blk >= 0; --blk) {
+    const int jt = 4 * blk + 3;
+    if (blk > 0) load_cols(nxt, Fc, hl, jt - 4, -1, false);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int j = jt - t;
+      if (j < NLOC) {
+        const int qb = j >> 4, owner = j & 15;
+        if (hl == owner) y[qb] *= cur[t][qb];
+        const T xj = __shfl_sync(kFull, y[qb], owner, 16);
+#pragma unroll
+        for (int q = 0; q < 6; ++q)
+          if (hl + 16 * q < j) y[q] -= cur[t][q] * xj;
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) cur[t][q] = nxt[t][q];
+  }
+  if (live) {
+    const int *ud = cells.udofs + (size_t)cell * NU_LOC;
+    const int *pd = cells.pdofs + (size_t)cell * NP_LOC;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const int r = hl + 16 * q;
+      if (r < NLOC) scatter_local(r, damp * y[q], ud, pd, nu, u);
+    }
+  }
+}
+
 // ----------------------------------------------------------------- coarse ---
 // Dense column-major coarse matrix a[col*N + row] (SolveExact layout).
 __global__ void k_coarse_scatter(DevOp<double> op, double *a, int N) {
@@ -969,15 +1059,13 @@ inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 
 }  // namespace
 
-template <typename TC, typename TF, bool INV>
+template <typename TC, typename TF>
 int launch_factor_impl(const DevOp<double> &op, const DevCells &cells, TF *factors, uint8_t *perm,
                        int *status, cudaStream_t s) {
-  size_t sm = sizeof(TC) * NLOC * NLOC;
-  if (INV && sm < kInvSmem) sm = kInvSmem;
-  cudaFuncSetAttribute(k_vanka_factor<TC, TF, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const size_t sm = sizeof(TC) * NLOC * NLOC;
+  cudaFuncSetAttribute(k_vanka_factor<TC, TF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sm);
-  k_vanka_factor<TC, TF, INV><<<cells.ncells, kFactorThreads, sm, s>>>(op, cells, factors, perm,
-                                                                      status);
+  k_vanka_factor<TC, TF><<<cells.ncells, kFactorThreads, sm, s>>>(op, cells, factors, perm, status);
   return ok() < 0 ? -1 : 1;
 }
 
@@ -985,12 +1073,14 @@ template <typename TF>
 int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, uint8_t *perm,
                         bool factor_fp32, bool inverse, int *status, cudaStream_t s) {
   if (cells.ncells <= 0) return 0;
-  if (inverse && sizeof(TF) == sizeof(float)) {
-    return factor_fp32 ? launch_factor_impl<float, TF, true>(op, cells, factors, perm, status, s)
-                       : launch_factor_impl<double, TF, true>(op, cells, factors, perm, status, s);
+  const int n = factor_fp32 ? launch_factor_impl<float, TF>(op, cells, factors, perm, status, s)
+                            : launch_factor_impl<double, TF>(op, cells, factors, perm, status, s);
+  if (n < 0 || !inverse) return n;
+  if constexpr (sizeof(TF) == sizeof(float)) {
+    k_lu_inverse_f32<<<cells.ncells, kInvThreadsLU, 0, s>>>(factors, perm);
+    return ok() < 0 ? -1 : n + 1;
   }
-  return factor_fp32 ? launch_factor_impl<float, TF, false>(op, cells, factors, perm, status, s)
-                     : launch_factor_impl<double, TF, false>(op, cells, factors, perm, status, s);
+  return -1;  // the inverse is stored in FP32 only
 }
 
 template <typename T>
@@ -1016,13 +1106,18 @@ int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *
 template <typename T>
 int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                        const T *factors, const uint8_t *perm, bool inverse, const T *rbuf, T damp,
-                       T *u, cudaStream_t s) {
+                       T *u, bool pairs, cudaStream_t s) {
   if (ncol <= 0) return 0;
   const int grid = (ncol + kApplyWarps - 1) / kApplyWarps;
   if (inverse)
     k_vanka_apply_inv<T><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors,
                                                           rbuf, damp, u);
-  else
+  else if (pairs) {
+    constexpr int W = sizeof(T) == 4 ? 8 : 4;  // FP64 holds twice the registers
+    const int g2 = (ncol + 2 * W - 1) / (2 * W);
+    k_vanka_apply2<T, W><<<g2, W * 32, 0, s>>>(cells, nu, cell_list, ncol, factors, perm, rbuf,
+                                               damp, u);
+  } else
     k_vanka_apply<T><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors, perm,
                                                       rbuf, damp, u);
   return ok() < 0 ? -1 : 1;
@@ -1085,7 +1180,7 @@ template int launch_vanka_factor<float>(const DevOp<double> &, const DevCells &,
   template int launch_vanka_residual<T>(const DevOp<T> &, const DevCells &, const int *, int,      \
                                         const T *, const T *, T *, int, cudaStream_t);             \
   template int launch_vanka_apply<T>(const DevCells &, int, const int *, int, const T *,           \
-                                     const uint8_t *, bool, const T *, T, T *, cudaStream_t);
+                                     const uint8_t *, bool, const T *, T, T *, bool, cudaStream_t);
 PM_VINST(double)
 PM_VINST(float)
 #undef PM_VINST
