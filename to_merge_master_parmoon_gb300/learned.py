@@ -21,6 +21,15 @@ N_IN, N_HIDDEN, N_OUT = 397, 256, 85
 FEATURE_CLAMP = 1.0e3  # |feature| bound of the feature kernel (kFeatureClamp)
 
 
+def _torch_done(t):
+    """Wait for the work torch has queued on its current stream of t's device:
+    the library runs on its own stream, so tensors that torch has just
+    written (index_select, randperm, empty from recycled memory) must be
+    complete before a library kernel reads or writes them."""
+    import torch
+    torch.cuda.current_stream(t.device).synchronize()
+
+
 class Mlp:
     def __init__(self, device: int = 0, seed: int = 0, max_batch: int = 8192):
         self._lib = gpu_lib()
@@ -57,6 +66,7 @@ class Mlp:
         """X: torch float32 cuda tensor [M, 397] -> [M, 85]."""
         import torch
         Y = torch.empty((X.shape[0], N_OUT), dtype=torch.float32, device=X.device)
+        _torch_done(X)
         st = self._lib.pm_mlp_forward(self._h, C.c_void_p(X.data_ptr()), X.shape[0],
                                       C.c_void_p(Y.data_ptr()))
         if st != 0:
@@ -66,6 +76,7 @@ class Mlp:
     def loss_grad(self, X, T, want_grad: bool = False):
         loss = C.c_double()
         g = np.empty(self.n_params, np.float32) if want_grad else None
+        _torch_done(X)
         st = self._lib.pm_mlp_loss_grad(self._h, C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr()),
                                         X.shape[0], C.byref(loss),
                                         g.ctypes.data_as(C.POINTER(C.c_float)) if g is not None else None)
@@ -104,6 +115,7 @@ def harvest_pairs(problems, n_cycles: int = 8, device: int = 0, precision: str =
         n0 = n
         converged = info["true_res"] <= 1e-9 * r0
         if converged:  # the targets are errors against this solution
+            _torch_done(X)
             n = S.harvest(xs, b, n_cycles, X.data_ptr(), T.data_ptr(), total, n)
         S.close()
         if log:
