@@ -42,65 +42,127 @@ __device__ __forceinline__ T group_sum(T v) {
 }
 
 // ---------------------------------------------------------------------------
-// Velocity rows: G lanes per row.  Dirichlet rows (>= nact) carry only the
-// diagonal-block values (off-diagonal blocks are zeroed at upload) and no BT.
-template <typename T, int G>
-__global__ void __launch_bounds__(kBlock) k_coupled_velocity(DevOp<T> op, const T *__restrict__ x,
-                                                             const T *__restrict__ b,
-                                                             T *__restrict__ r, int defect,
-                                                             int zero_nonactive) {
+// Velocity rows with 8 lanes per row (four rows per warp) and aligned vector
+// loads: each lane takes VEC consecutive entries of the column and value
+// arrays (arrays are padded to a multiple of 8 entries at upload), UR such
+// groups in flight, then a fixed 3-step butterfly per row.  Dirichlet rows
+// (>= nact) carry only the diagonal-block values (off-diagonal blocks are
+// zeroed at upload) and no BT; with zero_nonactive they are set to zero.
+template <typename T, int VEC>
+struct VLd;
+template <>
+struct VLd<float, 4> {
+  static __device__ __forceinline__ void val(const float *p, float (&o)[4]) {
+    const float4 v = __ldcs(reinterpret_cast<const float4 *>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+  static __device__ __forceinline__ void idx(const int *p, int (&o)[4]) {
+    const int4 v = __ldg(reinterpret_cast<const int4 *>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+};
+template <>
+struct VLd<double, 2> {
+  static __device__ __forceinline__ void val(const double *p, double (&o)[2]) {
+    const double2 v = __ldcs(reinterpret_cast<const double2 *>(p));
+    o[0] = v.x; o[1] = v.y;
+  }
+  static __device__ __forceinline__ void idx(const int *p, int (&o)[2]) {
+    const int2 v = __ldg(reinterpret_cast<const int2 *>(p));
+    o[0] = v.x; o[1] = v.y;
+  }
+};
+
+// s[0..2] += the row's products; NV = 9 (A blocks) and 1 (one-block A)
+// gather x0..x2; NV = 3 (BT) gathers x0 only
+template <typename T, int VEC, int NV, int UR>
+__device__ __forceinline__ void rows8_sum(const int *__restrict__ col, const T *const *vals, int rs,
+                                          int re, int sl, const T *__restrict__ x0,
+                                          const T *__restrict__ x1, const T *__restrict__ x2,
+                                          T (&s)[3]) {
+  for (int g = rs / VEC + sl; g * VEC < re; g += 8 * UR) {
+    int ci[UR][VEC];
+    T v[UR][NV][VEC];
+#pragma unroll
+    for (int q = 0; q < UR; ++q) {
+      const int gq = g + 8 * q;
+      if (gq * VEC < re) {
+        VLd<T, VEC>::idx(col + (size_t)gq * VEC, ci[q]);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) VLd<T, VEC>::val(vals[k] + (size_t)gq * VEC, v[q][k]);
+      } else {
+#pragma unroll
+        for (int m = 0; m < VEC; ++m) {
+          ci[q][m] = 0;
+#pragma unroll
+          for (int k = 0; k < NV; ++k) v[q][k][m] = T(0);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < UR; ++q) {
+      const int e0 = (g + 8 * q) * VEC;
+#pragma unroll
+      for (int m = 0; m < VEC; ++m) {
+        const int e = e0 + m;
+        if (e >= rs && e < re) {
+          const int c = ci[q][m];
+          if constexpr (NV == 3) {
+            const T pc = __ldg(x0 + c);
+            s[0] += v[q][0][m] * pc;
+            s[1] += v[q][1][m] * pc;
+            s[2] += v[q][2][m] * pc;
+          } else if constexpr (NV == 1) {
+            const T a = v[q][0][m];
+            s[0] += a * __ldg(x0 + c);
+            s[1] += a * __ldg(x1 + c);
+            s[2] += a * __ldg(x2 + c);
+          } else {
+            const T g0 = __ldg(x0 + c), g1 = __ldg(x1 + c), g2 = __ldg(x2 + c);
+            s[0] += v[q][0][m] * g0 + v[q][1][m] * g1 + v[q][2][m] * g2;
+            s[1] += v[q][3][m] * g0 + v[q][4][m] * g1 + v[q][5][m] * g2;
+            s[2] += v[q][6][m] * g0 + v[q][7][m] * g1 + v[q][8][m] * g2;
+          }
+        }
+      }
+    }
+  }
+}
+
+template <typename T, int VEC, bool ONE, int UR>
+__global__ void __launch_bounds__(kBlock) k_coupled_velocity8(DevOp<T> op, const T *__restrict__ x,
+                                                              const T *__restrict__ b,
+                                                              T *__restrict__ r, int defect,
+                                                              int zero_nonactive) {
   // no early return before the group shuffles: every lane of the warp joins
-  const int lane = threadIdx.x & (G - 1);
-  const long long row = ((long long)blockIdx.x * kBlock + threadIdx.x) / G;
+  const int sl = threadIdx.x & 7;
+  const long long row = ((long long)blockIdx.x * kBlock + threadIdx.x) >> 3;
   const int nu = op.nu;
   const bool valid = row < nu;
   const int i = valid ? (int)row : 0;
   const bool skip = !valid || (zero_nonactive && i >= op.nact);
   const T *u1 = x, *u2 = x + nu, *u3 = x + 2 * nu, *p = x + 3 * nu;
-  T s1 = 0, s2 = 0, s3 = 0;
+  T s[3] = {T(0), T(0), T(0)};
   if (!skip) {
-    const int rs = op.a_rowptr[i], re = op.a_rowptr[i + 1];
-    if (op.structured) {  // one block value per entry, same for the three components
-      for (int j = rs + lane; j < re; j += G) {
-        const int c = __ldg(op.a_col + j);
-        const T a = ld_stream(op.a[0] + j);
-        s1 += a * __ldg(u1 + c);
-        s2 += a * __ldg(u2 + c);
-        s3 += a * __ldg(u3 + c);
-      }
-    } else {
-      for (int j = rs + lane; j < re; j += G) {
-        const int c = __ldg(op.a_col + j);
-        const T x1 = __ldg(u1 + c), x2 = __ldg(u2 + c), x3 = __ldg(u3 + c);
-        s1 += ld_stream(op.a[0] + j) * x1 + ld_stream(op.a[1] + j) * x2 + ld_stream(op.a[2] + j) * x3;
-        s2 += ld_stream(op.a[3] + j) * x1 + ld_stream(op.a[4] + j) * x2 + ld_stream(op.a[5] + j) * x3;
-        s3 += ld_stream(op.a[6] + j) * x1 + ld_stream(op.a[7] + j) * x2 + ld_stream(op.a[8] + j) * x3;
-      }
-    }
-    if (i < op.nact) {
-      const int bs = op.bt_rowptr[i], be = op.bt_rowptr[i + 1];
-      for (int j = bs + lane; j < be; j += G) {
-        const T pv = __ldg(p + __ldg(op.bt_col + j));
-        s1 += ld_stream(op.bt[0] + j) * pv;
-        s2 += ld_stream(op.bt[1] + j) * pv;
-        s3 += ld_stream(op.bt[2] + j) * pv;
-      }
-    }
+    rows8_sum<T, VEC, ONE ? 1 : 9, UR>(op.a_col, op.a, op.a_rowptr[i], op.a_rowptr[i + 1], sl, u1,
+                                       u2, u3, s);
+    if (i < op.nact)
+      rows8_sum<T, VEC, 3, 1>(op.bt_col, op.bt, op.bt_rowptr[i], op.bt_rowptr[i + 1], sl, p, p,
+                              p, s);
   }
-  s1 = group_sum<G>(s1);
-  s2 = group_sum<G>(s2);
-  s3 = group_sum<G>(s3);
-  if (valid && lane == 0) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) s[c] = group_sum<8>(s[c]);
+  if (valid && sl == 0) {
     if (skip) {
       r[i] = r[nu + i] = r[2 * nu + i] = T(0);
     } else if (defect) {
-      r[i] = b[i] - s1;
-      r[nu + i] = b[nu + i] - s2;
-      r[2 * nu + i] = b[2 * nu + i] - s3;
+      r[i] = b[i] - s[0];
+      r[nu + i] = b[nu + i] - s[1];
+      r[2 * nu + i] = b[2 * nu + i] - s[2];
     } else {
-      r[i] = s1;
-      r[nu + i] = s2;
-      r[2 * nu + i] = s3;
+      r[i] = s[0];
+      r[nu + i] = s[1];
+      r[2 * nu + i] = s[2];
     }
   }
 }
@@ -380,9 +442,15 @@ inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 template <typename T>
 int launch_coupled(const DevOp<T> &op, const T *x, const T *b, T *r, bool defect,
                    bool zero_nonactive, cudaStream_t s) {
-  constexpr int GV = 32, GP = 16;
-  k_coupled_velocity<T, GV><<<grid_for((long long)op.nu * GV), kBlock, 0, s>>>(
-      op, x, b, r, defect ? 1 : 0, zero_nonactive ? 1 : 0);
+  constexpr int GP = 16;
+  constexpr int VEC = sizeof(T) == 4 ? 4 : 2;
+  const unsigned gv = grid_for((long long)op.nu * 8);
+  if (op.structured)
+    k_coupled_velocity8<T, VEC, true, 2><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+                                                              zero_nonactive ? 1 : 0);
+  else
+    k_coupled_velocity8<T, VEC, false, 1><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+                                                               zero_nonactive ? 1 : 0);
   if (ok() < 0) return -1;
   k_coupled_pressure<T, GP><<<grid_for((long long)op.np * GP), kBlock, 0, s>>>(op, x, b, r,
                                                                                defect ? 1 : 0);
