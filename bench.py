@@ -112,16 +112,24 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the Vanka solve kernel from the committed ncu
-    summary (profiles/vanka_solve_64cube.json), or None."""
-    p = ROOT / "profiles" / "vanka_solve_64cube.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text()).get("dram_bytes_per_launch")
-        except ValueError:
-            return None
-    return None
+def ncu_traffic(P):
+    """DRAM bytes per average residual launch: the per-cell traffic of one
+    32^3 colour launch from the committed ncu summary
+    (profiles/vanka_kernels_32cube_level.md), times the average number of
+    cells per residual launch of this workload (all smoothed cells / (8
+    colours x smoothed levels)); None without the summary."""
+    p = ROOT / "profiles" / "vanka_kernels_32cube_level.md"
+    if not p.exists():
+        return None
+    per_cell = None
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if len(parts) == 2 and parts[0] == "residual_dram_bytes_per_cell":
+            per_cell = float(parts[1])
+    if per_cell is None:
+        return None
+    cells = [P.desc(l).n_cells for l in range(1, P.n_levels)]
+    return per_cell * sum(cells) / (8 * len(cells))
 
 
 def cpu_baseline(P, iterations, levels, threads):
@@ -373,7 +381,7 @@ def main():
     achieved, avg_ms, per_launch = kernel_roof(prof.get("residual"))
     a_ach, a_ms, a_bytes = kernel_roof(prof.get("apply"))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(),
+            "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(P),
             "kernel": "k_vanka_residual<float,4,1> (cell-local residuals over full CSR rows, "
                       "one colour; flattened entry stream)",
             "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "bytes_per_launch": per_launch,
