@@ -43,6 +43,33 @@ def test_forward_and_gradients_match_oracle(mlp):
         assert rel(g[a:b], g_ref[a:b]) < 2e-3, (a, rel(g[a:b], g_ref[a:b]))
 
 
+@pytest.mark.parametrize("M", [96, 300, 512])
+def test_tcgen05_and_mma_sync_paths_agree(mlp, M):
+    """The forward layers on tcgen05 (TMEM accumulators, the default) and on
+    mma.sync give the same outputs, loss and gradients (FP32 accumulation of
+    the same BF16 products in another order; tile edges at M not a multiple
+    of 128), and both match the oracle."""
+    import torch
+    rng = np.random.default_rng(M)
+    X = rng.standard_normal((M, mo.N_IN)).astype(np.float32)
+    T = rng.standard_normal((M, mo.N_OUT)).astype(np.float32)
+    Xd, Td = torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda()
+    P = mlp.params().astype(np.float64)
+    y_ref, _ = mo.forward(P, X.astype(np.float64))
+    out = {}
+    for path in (True, False):
+        mlp.set_tensor_path(path)
+        y = mlp.forward(Xd).cpu().numpy()
+        loss, g = mlp.loss_grad(Xd, Td, want_grad=True)
+        out[path] = (y, loss, g)
+        assert rel(y, y_ref) < 2e-3
+    mlp.set_tensor_path(True)
+    (y1, l1, g1), (y0, l0, g0) = out[True], out[False]
+    assert rel(y1, y0) < 2e-3
+    assert abs(l1 - l0) < 1e-4 * l0
+    assert rel(g1, g0) < 2e-3
+
+
 def test_adamw_step_matches_formula(mlp):
     import torch
     rng = np.random.default_rng(4)

@@ -106,6 +106,7 @@ GPU_SYMBOLS = {
     "pm_mlp_get_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong]),
     "pm_mlp_set_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong]),
     "pm_mlp_forward": (C.c_int, [_P, C.c_void_p, C.c_int, C.c_void_p]),
+    "pm_mlp_set_tensor_path": (C.c_int, [_P, C.c_int]),
     "pm_mlp_loss_grad": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_int, c_double_p,
                                    C.POINTER(C.c_float)]),
     "pm_mlp_adamw_step": (C.c_int, [_P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),

@@ -397,7 +397,8 @@ pm_status learned_step(pm_handle *h, LevelDev &C, T *u, const T *f) {
   PM_LAUNCH(launch_cell_summary<T>(cells, C.nu, d, C.l_summary, h->d_on, h->stream));
   PM_LAUNCH(launch_cell_features<T>(cells, C.nu, d, C.l_summary, C.l_nbr, C.l_X, nullptr,
                                     C.l_scale, h->d_on, h->stream));
-  PM_LAUNCH(mlp_forward(*h->mlp, C.l_X, C.ncells, C.l_H1, C.l_H2, C.l_Y, h->stream, h->d_on));
+  PM_LAUNCH(mlp_forward(*h->mlp, C.l_X, C.ncells, C.l_H1, C.l_H2, C.l_Y, h->stream, h->d_on,
+                        h->sweep_err));
   // correction c = cell predictions averaged over the cells sharing a DOF
   T *c = static_cast<T *>(C.l_corr), *q = static_cast<T *>(C.l_q);
   PM_LAUNCH(launch_fill<T>(c, T(0), C.ndof, h->stream));
@@ -1489,12 +1490,30 @@ pm_status pm_mlp_set_params(pm_mlp *m, const float *host, long long n) {
   return PM_OK;
 }
 
+// bounded waits of the tcgen05 layers that gave up (flag read and cleared)
+static pm_status mlp_err(pm_mlp *m) {
+  int e = 0;
+  if (cudaMemcpy(&e, m->m.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return PM_CUDA_ERROR;
+  if (e) {
+    cudaMemset(m->m.err, 0, sizeof(int));
+    return PM_TIMEOUT;
+  }
+  return PM_OK;
+}
+
 pm_status pm_mlp_forward(pm_mlp *m, const float *d_X, int M, float *d_Y) {
   if (!m || !d_X || !d_Y || M <= 0 || M > m->m.max_batch) return PM_BADARG;
   cudaSetDevice(m->m.device);
   if (mlp_forward_f32(m->m, d_X, M, d_Y, m->m.stream) < 0 ||
       cudaStreamSynchronize(m->m.stream) != cudaSuccess)
     return PM_CUDA_ERROR;
+  return mlp_err(m);
+}
+
+pm_status pm_mlp_set_tensor_path(pm_mlp *m, int tcgen05) {
+  if (!m) return PM_BADARG;
+  m->m.tc = tcgen05 != 0;
   return PM_OK;
 }
 
@@ -1512,6 +1531,8 @@ pm_status pm_mlp_loss_grad(pm_mlp *m, const float *d_X, const float *d_T, int M,
     return PM_CUDA_ERROR;
   if (cudaStreamSynchronize(m->m.stream) != cudaSuccess) return PM_CUDA_ERROR;
   if (loss) *loss = l;
+  const pm_status es = mlp_err(m);
+  if (es != PM_OK) return es;
   return std::isfinite(l) ? PM_OK : PM_NAN;
 }
 

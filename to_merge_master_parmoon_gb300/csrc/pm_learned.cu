@@ -507,6 +507,9 @@ cudaError_t mlp_create(Mlp &m, int device, unsigned long long seed, int max_batc
   A((void **)&m.dY, sizeof(float) * B * kMlpOutPad);
   A((void **)&m.dH, sizeof(float) * B * kMlpHidden);
   A((void **)&m.loss, sizeof(double));
+  A((void **)&m.err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(m.err, 0, sizeof(int));
+  if (e == cudaSuccess && mlp_tc_init() < 0) e = cudaErrorInvalidValue;
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m.stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return e;
   cudaMemsetAsync(m.Mo, 0, np, m.stream);
@@ -522,7 +525,7 @@ void mlp_destroy(Mlp &m) {
   cudaSetDevice(m.device);
   if (m.stream) cudaStreamSynchronize(m.stream);
   void *ptrs[] = {m.P,  m.G,    m.Mo,   m.Vo,   m.W1,   m.W2, m.W3, m.X, m.H1, m.H2,
-                  m.dYb, m.dA2b, m.dA1b, m.pre1, m.pre2, m.Y,  m.dY, m.dH, m.loss};
+                  m.dYb, m.dA2b, m.dA1b, m.pre1, m.pre2, m.Y,  m.dY, m.dH, m.loss, m.err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (m.stream) cudaStreamDestroy(m.stream);
@@ -535,9 +538,21 @@ int mlp_sync_bf16(const Mlp &m, cudaStream_t s) {
 }
 
 int mlp_forward(const Mlp &m, const __nv_bfloat16 *X, int M, __nv_bfloat16 *H1, __nv_bfloat16 *H2,
-                float *Y, cudaStream_t s, const int *on) {
+                float *Y, cudaStream_t s, const int *on, int *err) {
   if (M <= 0) return 0;
   int n = 0, r;
+  if (m.tc) {
+    int *e = err ? err : m.err;
+    if ((r = mlp_layer_tc(1, X, M, m.W1, m.P + kOffB1, 1, nullptr, nullptr, H1, on, e, s)) < 0)
+      return -1;
+    n += r;
+    if ((r = mlp_layer_tc(2, H1, M, m.W2, m.P + kOffB2, 1, nullptr, nullptr, H2, on, e, s)) < 0)
+      return -1;
+    n += r;
+    if ((r = mlp_layer_tc(3, H2, M, m.W3, m.P + kOffB3, 0, nullptr, Y, nullptr, on, e, s)) < 0)
+      return -1;
+    return n + r;
+  }
   GemmArgs g{};
   // layer 1: H1 = GELU(X W1^T + b1)
   g = GemmArgs{M, kMlpHidden, kMlpInPad, X, kMlpInPad, 1, m.W1, 1, kMlpInPad, 1.f,
@@ -577,18 +592,33 @@ int mlp_loss_grad(Mlp &m, const float *X, const float *T, int M, cudaStream_t s)
   n++;
   GemmArgs g{};
   // forward, keeping pre-activations
-  g = GemmArgs{M, kMlpHidden, kMlpInPad, m.X, kMlpInPad, 1, m.W1, 1, kMlpInPad, 1.f,
-               m.P + kOffB1, 1, m.pre1, nullptr, m.H1, kMlpHidden};
-  if ((r = gemm(g, s)) < 0) return -1;
-  n += r;
-  g = GemmArgs{M, kMlpHidden, kMlpHidden, m.H1, kMlpHidden, 1, m.W2, 1, kMlpHidden, 1.f,
-               m.P + kOffB2, 1, m.pre2, nullptr, m.H2, kMlpHidden};
-  if ((r = gemm(g, s)) < 0) return -1;
-  n += r;
-  g = GemmArgs{M, kMlpOutPad, kMlpHidden, m.H2, kMlpHidden, 1, m.W3, 1, kMlpHidden, 1.f,
-               m.P + kOffB3, 0, nullptr, m.Y, nullptr, kMlpOutPad};
-  if ((r = gemm(g, s)) < 0) return -1;
-  n += r;
+  if (m.tc) {
+    if ((r = mlp_layer_tc(1, m.X, M, m.W1, m.P + kOffB1, 1, m.pre1, nullptr, m.H1, nullptr, m.err,
+                          s)) < 0)
+      return -1;
+    n += r;
+    if ((r = mlp_layer_tc(2, m.H1, M, m.W2, m.P + kOffB2, 1, m.pre2, nullptr, m.H2, nullptr,
+                          m.err, s)) < 0)
+      return -1;
+    n += r;
+    if ((r = mlp_layer_tc(3, m.H2, M, m.W3, m.P + kOffB3, 0, nullptr, m.Y, nullptr, nullptr,
+                          m.err, s)) < 0)
+      return -1;
+    n += r;
+  } else {
+    g = GemmArgs{M, kMlpHidden, kMlpInPad, m.X, kMlpInPad, 1, m.W1, 1, kMlpInPad, 1.f,
+                 m.P + kOffB1, 1, m.pre1, nullptr, m.H1, kMlpHidden};
+    if ((r = gemm(g, s)) < 0) return -1;
+    n += r;
+    g = GemmArgs{M, kMlpHidden, kMlpHidden, m.H1, kMlpHidden, 1, m.W2, 1, kMlpHidden, 1.f,
+                 m.P + kOffB2, 1, m.pre2, nullptr, m.H2, kMlpHidden};
+    if ((r = gemm(g, s)) < 0) return -1;
+    n += r;
+    g = GemmArgs{M, kMlpOutPad, kMlpHidden, m.H2, kMlpHidden, 1, m.W3, 1, kMlpHidden, 1.f,
+                 m.P + kOffB3, 0, nullptr, m.Y, nullptr, kMlpOutPad};
+    if ((r = gemm(g, s)) < 0) return -1;
+    n += r;
+  }
   k_mse_grad<<<blocks_for((long long)M * kMlpOutPad), 256, 0, s>>>(m.Y, T, M, m.dY, m.dYb, m.loss);
   n++;
   // layer 3: dW3 = dY^T H2, db3, dH2 = dY W3

@@ -1,6 +1,7 @@
 // pm_learned.h — learned per-cell smoother (no counterpart in the reference):
 // a 397 -> 256 -> 256 -> 85 MLP with GELU, BF16 weights and activations and
-// FP32 accumulation on the tensor cores (mma.sync m16n8k16), trained on the
+// FP32 accumulation on the tensor cores (forward layers: tcgen05.mma with
+// TMEM accumulators; training gradients: mma.sync m16n8k16), trained on the
 // GPU from (residual, error) pairs of the plain solver.
 #ifndef PM_LEARNED_H
 #define PM_LEARNED_H
@@ -42,8 +43,19 @@ struct Mlp {
                 *dA1b = nullptr;
   float *pre1 = nullptr, *pre2 = nullptr, *Y = nullptr, *dY = nullptr, *dH = nullptr;
   double *loss = nullptr;
+  int *err = nullptr;   // device flags of bounded waits in the tcgen05 layers
+  bool tc = true;       // forward layers on tcgen05 (else mma.sync)
   cudaStream_t stream = nullptr;
 };
+
+// tcgen05 forward layer (pm_mlp_tc.cu): layer 1 (X [M x 400] -> [M x 256]),
+// 2 ([M x 256] -> [M x 256]) or 3 ([M x 256] -> [M x 96]) with bias and, if
+// act, GELU; outputs pre-activation (FP32), FP32 and/or BF16 rows.
+int mlp_layer_tc(int layer, const __nv_bfloat16 *A, int M, const __nv_bfloat16 *W,
+                 const float *bias, int act, float *pre, float *Cf, __nv_bfloat16 *Cb,
+                 const int *on, int *err, cudaStream_t s);
+// sets the layers' shared-memory limits (once, outside stream capture)
+int mlp_tc_init();
 
 // allocate / free (returns cudaError_t)
 cudaError_t mlp_create(Mlp &m, int device, unsigned long long seed, int max_batch);
@@ -52,7 +64,8 @@ void mlp_destroy(Mlp &m);
 int mlp_sync_bf16(const Mlp &m, cudaStream_t s);
 // Inference: X [M x 400] BF16 (padded) -> Y [M x 96] FP32; H1/H2 workspaces [M x 256].
 int mlp_forward(const Mlp &m, const __nv_bfloat16 *X, int M, __nv_bfloat16 *H1,
-                __nv_bfloat16 *H2, float *Y, cudaStream_t s, const int *on = nullptr);
+                __nv_bfloat16 *H2, float *Y, cudaStream_t s, const int *on = nullptr,
+                int *err = nullptr);
 // Inference on unpadded FP32 rows: X [M x 397] -> Yout [M x 85] (M <= max_batch)
 int mlp_forward_f32(Mlp &m, const float *X, int M, float *Yout, cudaStream_t s);
 // Training: X [M x 397] FP32, T [M x 85] FP32 -> loss (device double), grads in m.G

@@ -62,6 +62,12 @@ class Mlp:
         if st != 0:
             raise PmError(st, "pm_mlp_set_params")
 
+    def set_tensor_path(self, tcgen05: bool):
+        """Forward layers on tcgen05 (True, the default) or mma.sync (False)."""
+        st = self._lib.pm_mlp_set_tensor_path(self._h, int(tcgen05))
+        if st != 0:
+            raise PmError(st, "pm_mlp_set_tensor_path")
+
     def forward(self, X):
         """X: torch float32 cuda tensor [M, 397] -> [M, 85]."""
         import torch
