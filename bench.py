@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-systems", type=int, default=48)
     ap.add_argument("--train-problems", type=int, default=8)
     return ap.parse_args()
 
@@ -226,6 +228,57 @@ def train_network(device, args, log=None):
 FGMRES_ITERATIONS = {(6, 1e-2): 10, (5, 1e-2): 10, (4, 1e-2): 9}
 
 
+def batch_run(args, device, log=None):
+    """Batched independent systems of uneven size: hexahedral systems with
+    sizes drawn uniformly from {8^3, 16^3, 32^3} cells, nu log-uniform in
+    [1e-3, 1e-1], seeds 100+s, mixed precision, FGMRES(20)+V(2,2) to 1e-8
+    (at most 100 iterations).  Timed once through pm_solve_batch (host
+    vectors, concurrent host threads, one stream per system) and once as the
+    same pm_solve calls one after another; both after one untimed pass."""
+    import numpy as np
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver, solve_batch
+    rng = np.random.default_rng(2)
+    probs, solvers, rhss = [], [], []
+    t0 = time.perf_counter()
+    for k in range(args.batch_systems):
+        levels = int(rng.integers(3, 6))
+        nu = float(10 ** rng.uniform(-3, -1))
+        P = OseenProblem(n_levels=levels, nu=nu, seed=100 + k, nthreads=os.cpu_count() or 1)
+        b = P.rhs()
+        nu3 = 3 * P.desc(levels - 1).n_udof
+        bp = b.copy()
+        bp[nu3::4] -= bp[nu3::4].mean()
+        solvers.append(PmSolver(P.descs, precision="mixed", device=device, restart=20, maxit=100,
+                                res_norm_min=RTOL * float(np.linalg.norm(bp))))
+        probs.append(P)
+        rhss.append(b)
+    build_s = time.perf_counter() - t0
+    zeros = [np.zeros_like(b) for b in rhss]
+    solve_batch(solvers, zeros, rhss, allow=(0, 1, 2))  # untimed pass
+    t = time.perf_counter()
+    _, infos = solve_batch(solvers, zeros, rhss, allow=(0, 1, 2))
+    t_batch = time.perf_counter() - t
+    t = time.perf_counter()
+    for S, b in zip(solvers, rhss):
+        S.iterate(np.zeros_like(b), b, allow=(0, 1, 2))
+    t_seq = time.perf_counter() - t
+    conv = sum(1 for i in infos if i["status"] == 0)
+    dofs = sum(P.ndof(-1) for P in probs)
+    if log:
+        log(f"batch: {len(solvers)} systems, {conv} converged, batch {t_batch:.3f} s, "
+            f"one after another {t_seq:.3f} s")
+    out = {"systems": len(solvers), "converged_to_1e-8": conv, "total_dof": dofs,
+           "cells": sorted({P.desc(P.n_levels - 1).n_cells for P in probs}),
+           "iterations": [i["iterations"] for i in infos],
+           "batch_s": t_batch, "sequential_s": t_seq, "speedup": t_seq / t_batch,
+           "build_s": build_s,
+           "note": "hexahedral Q2/P1disc systems only; the tetrahedral P2+bubble systems "
+                   "of this workload are not built"}
+    for S in solvers:
+        S.close()
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -367,6 +420,10 @@ def main():
         if one_block:
             e2e1 = e2e_run(solvers["mixed_one_block"], D1, 1)
 
+    batch = None
+    if not args.no_batch and rank == 0:
+        batch = batch_run(args, local, log=lambda *a: print(*a, file=sys.stderr))
+
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -439,6 +496,7 @@ def main():
         "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "roofline": roof,
         "one_block": one,
+        "batch": batch,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": results["mixed_learned"]["launches"],

@@ -227,6 +227,15 @@ pm_status pm_vcycle(pm_handle *h, double *z, const double *v);
 pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out);
 /* Same with device pointers (no vector copies); the matrices must be set up. */
 pm_status pm_solve_device(pm_handle *h, double *d_sol, const double *d_rhs, pm_result *out);
+/* Batched solves of independent systems (a batch of Oseen systems of uneven
+ * size, each in its own set-up handle): pm_solve for every i < n, run
+ * concurrently from up to nthreads host threads (0: one per system), so the
+ * handles' streams overlap on the GPU.  The handles must be distinct.  Each
+ * result equals the one pm_solve gives alone (same kernels, same order on
+ * the handle's stream).  results may be NULL; returns the first non-PM_OK
+ * status in index order, PM_OK if none. */
+pm_status pm_solve_batch(pm_handle *const *hs, int n, double *const *sols,
+                         const double *const *rhss, pm_result *results, int nthreads);
 /* Re-run the local-block and coarse factorisations on the device (timed into
  * out->setup_ms); used to time factor+solve with inputs resident in HBM. */
 pm_status pm_refactor(pm_handle *h, double *ms);

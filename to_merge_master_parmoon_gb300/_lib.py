@@ -93,6 +93,8 @@ GPU_SYMBOLS = {
     "pm_vcycle": (C.c_int, [_P, c_double_p, c_double_p]),
     "pm_solve": (C.c_int, [_P, c_double_p, c_double_p, C.POINTER(PmResult)]),
     "pm_solve_device": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.POINTER(PmResult)]),
+    "pm_solve_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(c_double_p),
+                                 C.POINTER(c_double_p), C.POINTER(PmResult), C.c_int]),
     "pm_refactor": (C.c_int, [_P, c_double_p]),
     "pm_kernel_launches": (C.c_longlong, [_P]),
     "pm_device_bytes": (C.c_longlong, [_P]),

@@ -13,11 +13,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "pm_kernels.h"
@@ -1423,6 +1425,41 @@ pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out)
   pm_status st = pm_solve_device(h, h->xd, h->bd, out);
   pm_status s2 = d2h(h, sol, h->xd, F.ndof);
   return st != PM_OK ? st : s2;
+}
+
+pm_status pm_solve_batch(pm_handle *const *hs, int n, double *const *sols,
+                         const double *const *rhss, pm_result *results, int nthreads) {
+  if (!hs || !sols || !rhss || n <= 0) return PM_BADARG;
+  for (int i = 0; i < n; ++i) {
+    if (!hs[i] || !sols[i] || !rhss[i]) return PM_BADARG;
+    if (!hs[i]->setup_done) return PM_NOT_SETUP;
+    for (int j = 0; j < i; ++j)
+      if (hs[j] == hs[i]) return PM_BADARG;  // a handle is not thread-safe
+  }
+  std::vector<pm_status> st((size_t)n, PM_OK);
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    for (;;) {
+      const int i = next.fetch_add(1);
+      if (i >= n) break;
+      pm_result r;
+      std::memset(&r, 0, sizeof(r));
+      if (cudaSetDevice(hs[i]->opt.device) != cudaSuccess) {
+        st[(size_t)i] = PM_CUDA_ERROR;
+      } else {
+        st[(size_t)i] = pm_solve(hs[i], sols[i], rhss[i], &r);
+      }
+      if (results) results[i] = r;
+    }
+  };
+  const int T = std::max(1, std::min(nthreads > 0 ? nthreads : n, n));
+  std::vector<std::thread> pool;
+  pool.reserve((size_t)T);
+  for (int t = 0; t < T; ++t) pool.emplace_back(worker);
+  for (auto &th : pool) th.join();
+  for (int i = 0; i < n; ++i)
+    if (st[(size_t)i] != PM_OK) return st[(size_t)i];
+  return PM_OK;
 }
 
 long long pm_kernel_launches(pm_handle *h) { return h ? h->launches : 0; }

@@ -218,3 +218,22 @@ class PmSolver:
 
 def device_count() -> int:
     return gpu_lib().pm_device_count()
+
+
+def solve_batch(solvers, sols, rhss, nthreads=0, allow=(0,)):
+    """pm_solve_batch: independent systems, one set-up PmSolver each, solved
+    concurrently (each handle's stream overlaps the others on the GPU).
+    Returns (solutions, list of result dicts)."""
+    n = len(solvers)
+    lib = solvers[0]._lib
+    sols = [_f64(x).copy() for x in sols]
+    rhss = [_f64(b) for b in rhss]
+    H = (C.c_void_p * n)(*[S._h for S in solvers])
+    X = (C.POINTER(C.c_double) * n)(*[_dp(x) for x in sols])
+    B = (C.POINTER(C.c_double) * n)(*[_dp(b) for b in rhss])
+    R = (PmResult * n)()
+    st = lib.pm_solve_batch(H, n, X, B, R, nthreads)
+    if st not in allow:
+        raise PmError(st, "pm_solve_batch")
+    return sols, [R[i].as_dict() for i in range(n)]
+
