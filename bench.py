@@ -254,13 +254,13 @@ def batch_run(args, device, log=None):
         rhss.append(b)
     build_s = time.perf_counter() - t0
     zeros = [np.zeros_like(b) for b in rhss]
-    solve_batch(solvers, zeros, rhss, allow=(0, 1, 2))  # untimed pass
+    solve_batch(solvers, zeros, rhss, allow=(0, 1, 2, 3))  # untimed pass
     t = time.perf_counter()
-    _, infos = solve_batch(solvers, zeros, rhss, allow=(0, 1, 2))
+    _, infos = solve_batch(solvers, zeros, rhss, allow=(0, 1, 2, 3))
     t_batch = time.perf_counter() - t
     t = time.perf_counter()
     for S, b in zip(solvers, rhss):
-        S.iterate(np.zeros_like(b), b, allow=(0, 1, 2))
+        S.iterate(np.zeros_like(b), b, allow=(0, 1, 2, 3))
     t_seq = time.perf_counter() - t
     conv = sum(1 for i in infos if i["status"] == 0)
     dofs = sum(P.ndof(-1) for P in probs)
