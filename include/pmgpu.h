@@ -227,6 +227,20 @@ pm_status pm_vcycle(pm_handle *h, double *z, const double *v);
 pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out);
 /* Same with device pointers (no vector copies); the matrices must be set up. */
 pm_status pm_solve_device(pm_handle *h, double *d_sol, const double *d_rhs, pm_result *out);
+/* Galerkin Oseen assembly of one level on the device, replacing the level's
+ * matrix values (NSType4Galerkin3D, src/FE/NSE3D_FixPo.C:1919-2071, in the
+ * cell loop of TAssembleMat3D::Assemble3D, src/System/AssembleMat3D.C:230):
+ * A11 = A22 = A33 = nu (grad u, grad v) + ((b . grad) u, v), A12..A32 = 0,
+ * B and BT from -(p, div v), Q2/P1disc, 4-point Gauss rule per direction;
+ * Dirichlet rows get 1 on the diagonal.  Cells must be axis-aligned boxes:
+ * cell_h = (hx, hy, hz) per cell (n_cells x 3), conv = [b1|b2|b3] at the
+ * velocity nodes (3 x n_udof).  The level's sparsity pattern is kept; call
+ * pm_refactor after assembling the levels. */
+pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const double *conv,
+                            double nu);
+/* Same with device pointers (e.g. the current velocity on the device). */
+pm_status pm_assemble_level_device(pm_handle *h, int level, const double *d_cell_h,
+                                   const double *d_conv, double nu);
 /* Batched solves of independent systems (a batch of Oseen systems of uneven
  * size, each in its own set-up handle): pm_solve for every i < n, run
  * concurrently from up to nthreads host threads (0: one per system), so the

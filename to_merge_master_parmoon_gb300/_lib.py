@@ -93,6 +93,8 @@ GPU_SYMBOLS = {
     "pm_vcycle": (C.c_int, [_P, c_double_p, c_double_p]),
     "pm_solve": (C.c_int, [_P, c_double_p, c_double_p, C.POINTER(PmResult)]),
     "pm_solve_device": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.POINTER(PmResult)]),
+    "pm_assemble_level": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, C.c_double]),
+    "pm_assemble_level_device": (C.c_int, [_P, C.c_int, C.c_void_p, C.c_void_p, C.c_double]),
     "pm_solve_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(c_double_p),
                                  C.POINTER(c_double_p), C.POINTER(PmResult), C.c_int]),
     "pm_refactor": (C.c_int, [_P, c_double_p]),
@@ -129,6 +131,8 @@ HOST_SYMBOLS = {
     "pmh_exact": (c_double_p, [C.c_void_p]),
     "pmh_q2_basis": (None, [C.c_double, C.c_double, C.c_double, c_double_p, c_double_p]),
     "pmh_max_convection": (C.c_double, [C.c_void_p]),
+    "pmh_cell_sizes": (C.c_int, [C.c_void_p, C.c_int, c_double_p]),
+    "pmh_convection_nodal": (C.c_int, [C.c_void_p, C.c_int, c_double_p]),
 }
 
 _cache: dict[str, C.CDLL] = {}

@@ -625,6 +625,32 @@ int pmh_ndof(const pmh_problem *p, int level) {
 }
 double pmh_max_convection(const pmh_problem *p) { return p ? p->bmax : 0.0; }
 
+int pmh_cell_sizes(const pmh_problem *p, int level, double *out) {
+  if (!p || level < 0 || level >= (int)p->levels.size() || !out) return -1;
+  const PMLevelData &L = p->levels[level];
+  for (int c = 0; c < L.n_cells; ++c) {
+    const int cx = c % L.nx, cy = (c / L.nx) % L.ny, cz = c / (L.nx * L.ny);
+    out[3 * c] = L.xs[cx + 1] - L.xs[cx];
+    out[3 * c + 1] = L.ys[cy + 1] - L.ys[cy];
+    out[3 * c + 2] = L.zs[cz + 1] - L.zs[cz];
+  }
+  return 0;
+}
+
+int pmh_convection_nodal(const pmh_problem *p, int level, double *out) {
+  if (!p || level < 0 || level >= (int)p->levels.size() || !out) return -1;
+  const PMLevelData &L = p->levels[level];
+  const int gx = L.gx(), gy = L.gy();
+  for (int r = 0; r < L.n_udof; ++r) {
+    const int g = L.dof2grid[r];
+    const int i = g % gx, j = (g / gx) % gy, k = g / (gx * gy);
+    double b[3];
+    convection(*p, L.node_x(i), L.node_y(j), L.node_z(k), b);
+    for (int d = 0; d < 3; ++d) out[(size_t)d * L.n_udof + r] = b[d];
+  }
+  return 0;
+}
+
 int pmh_level_desc(const pmh_problem *p, int level, pm_level_desc *o) {
   if (!p || !o || level < 0 || level >= (int)p->levels.size()) return -1;
   const PMLevelData &L = p->levels[level];

@@ -58,6 +58,10 @@ const double *pmh_exact(const pmh_problem *p);
  * (d/dxi, d/deta, d/dzeta per function). */
 void pmh_q2_basis(double xi, double eta, double zeta, double *values, double *derivs);
 double pmh_max_convection(const pmh_problem *p);
+/* (hx, hy, hz) of every cell of a level (n_cells x 3); 0 or -1 */
+int pmh_cell_sizes(const pmh_problem *p, int level, double *out);
+/* the convection field at the level's velocity nodes, [b1|b2|b3]; 0 or -1 */
+int pmh_convection_nodal(const pmh_problem *p, int level, double *out);
 
 #ifdef __cplusplus
 }

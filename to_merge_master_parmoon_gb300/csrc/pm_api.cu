@@ -87,6 +87,8 @@ struct LevelDev {
   __nv_bfloat16 *l_X = nullptr, *l_H1 = nullptr, *l_H2 = nullptr;
   void *l_corr = nullptr, *l_q = nullptr, *l_zero = nullptr;  // V-cycle precision
   double *l_omega = nullptr;                                   // step length (device)
+  // device assembly inputs (allocated on first pm_assemble_level)
+  double *asm_h = nullptr, *asm_conv = nullptr;
 
   template <typename T>
   DevOp<T> op() const;
@@ -152,6 +154,7 @@ struct pm_handle {
   double *ydev = nullptr;
   int *status_d = nullptr;
   int *sweep_err = nullptr;  // device flags of bounded waits inside sweep kernels
+  bool asm_tables = false;   // assembly reference tables on the device
   int num_sms = 0;
   // coarse direct solve
   int coarse_n = 0;
@@ -1425,6 +1428,65 @@ pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out)
   pm_status st = pm_solve_device(h, h->xd, h->bd, out);
   pm_status s2 = d2h(h, sol, h->xd, F.ndof);
   return st != PM_OK ? st : s2;
+}
+
+pm_status pm_assemble_level_device(pm_handle *h, int level, const double *d_cell_h,
+                                   const double *d_conv, double nu) {
+  PM_CHECK_LEVEL(h, level);
+  if (!d_cell_h || !d_conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
+  LevelDev &Lv = h->L[level];
+  if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
+  if (!h->asm_tables) {
+    if (assemble_tables_init() < 0) return cuda_fail(h, "assembly tables");
+    h->asm_tables = true;
+  }
+  AsmOp op{};
+  op.nu = Lv.nu;
+  op.np = Lv.np;
+  op.nact = Lv.nact;
+  op.a_nnz = Lv.a_nnz;
+  op.b_nnz = Lv.b_nnz;
+  op.bt_nnz = Lv.bt_nnz;
+  op.a_rowptr = Lv.a_rowptr;
+  op.a_col = Lv.a_col;
+  op.b_rowptr = Lv.b_rowptr;
+  op.b_col = Lv.b_col;
+  op.bt_rowptr = Lv.bt_rowptr;
+  op.bt_col = Lv.bt_col;
+  const int nblk = Lv.structured ? 1 : 9;
+  for (int k = 0; k < nblk; ++k) op.a[k] = Lv.a64[k];
+  for (int k = 0; k < 3; ++k) {
+    op.b[k] = Lv.b64[k];
+    op.bt[k] = Lv.bt64[k];
+  }
+  PM_LAUNCH(launch_assemble_level(op, Lv.cells(), Lv.colour_cells, Lv.colouring.ptr.data(),
+                                  (int)Lv.colouring.ptr.size() - 1, d_cell_h, d_conv, nu,
+                                  h->stream));
+  if (mixed(h)) {
+    for (int k = 0; k < nblk; ++k)
+      PM_LAUNCH((launch_convert<float, double>(Lv.a32[k], Lv.a64[k], Lv.a_nnz, h->stream)));
+    for (int k = 0; k < 3; ++k) {
+      PM_LAUNCH((launch_convert<float, double>(Lv.b32[k], Lv.b64[k], Lv.b_nnz, h->stream)));
+      PM_LAUNCH((launch_convert<float, double>(Lv.bt32[k], Lv.bt64[k], Lv.bt_nnz, h->stream)));
+    }
+  }
+  return sync(h, "assembly");
+}
+
+pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const double *conv,
+                            double nu) {
+  PM_CHECK_LEVEL(h, level);
+  if (!cell_h || !conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
+  LevelDev &Lv = h->L[level];
+  if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
+  if (!Lv.asm_h) PM_TRY(dalloc(h, &Lv.asm_h, (size_t)Lv.ncells * 3));
+  if (!Lv.asm_conv) PM_TRY(dalloc(h, &Lv.asm_conv, (size_t)Lv.nu * 3));
+  if (cudaMemcpyAsync(Lv.asm_h, cell_h, sizeof(double) * Lv.ncells * 3, cudaMemcpyHostToDevice,
+                      h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(Lv.asm_conv, conv, sizeof(double) * Lv.nu * 3, cudaMemcpyHostToDevice,
+                      h->stream) != cudaSuccess)
+    return cuda_fail(h, "assembly inputs");
+  return pm_assemble_level_device(h, level, Lv.asm_h, Lv.asm_conv, nu);
 }
 
 pm_status pm_solve_batch(pm_handle *const *hs, int n, double *const *sols,

@@ -1,0 +1,243 @@
+// pm_assemble.cu — Oseen matrix assembly of one level on the device.
+//
+// The reference assembles the Galerkin Oseen blocks of NSTYPE 4 cell by cell
+// on the host (NSType4Galerkin3D, src/FE/NSE3D_FixPo.C:1919-2071, called
+// from TAssembleMat3D::Assemble3D, src/System/AssembleMat3D.C:230) with the
+// gradient form nu (grad u, grad v) + ((b . grad) u, v) on the three diagonal
+// velocity blocks and -(p, div v) / -(q, div u) in B and BT; with Q2 velocity,
+// P1disc pressure and the 4-point Gauss rule per direction (64 points).  A
+// time-dependent run re-assembles these for every new convection field.
+//
+// Here one CTA of 128 threads assembles one cell of a colour and adds into
+// the level's CSR values in place; cells of one colour share no DOF, so the
+// additions need no atomics and the order of the sums is fixed.  Cells are
+// axis-aligned boxes (the Jacobian is diag(hx, hy, hz) / 2), as in the
+// uniform and stretched box meshes of the workloads.  Per cell:
+//   diffusion  nu * detJ * sum_d s_d^2 Kref_d           (reference tables)
+//   convection detJ * sum_q w_q phi_i(q) (b(q) . grad phi_j(q)),
+//              b(q) = sum_m b_m phi_m(q) from the nodal convection b_m
+//   B_d[m][j]  = -detJ * s_d * Bref_d[m][j]             (= BT_d[j][m])
+// with s_d = 2 / h_d and detJ = hx hy hz / 8.  Dirichlet rows get 1 on the
+// diagonal of A11, A22, A33 and nothing else.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "pm_kernels.h"
+
+namespace pm {
+
+namespace {
+
+constexpr int kNq = 64;          // 4 x 4 x 4 Gauss points
+constexpr int kAsmThreads = 128;
+
+// reference tables on the unit cube [-1, 1]^3, local Q2 order a + 3b + 9c
+__constant__ double c_Kref[3][NU_LOC][NU_LOC];   // sum_q w dphi_i,d dphi_j,d
+__constant__ double c_Bref[3][NP_LOC][NU_LOC];   // sum_q w psi_m dphi_j,d
+__device__ double g_wphi[kNq][NU_LOC];           // w_q phi_i(q)
+__device__ double g_phi[kNq][NU_LOC];
+__device__ double g_dphi[kNq][NU_LOC][3];
+
+struct HostTables {
+  double K[3][NU_LOC][NU_LOC];
+  double B[3][NP_LOC][NU_LOC];
+  double wphi[kNq][NU_LOC];
+  double phi[kNq][NU_LOC];
+  double dphi[kNq][NU_LOC][3];
+};
+
+void lagrange2(double t, double *v, double *d) {
+  v[0] = 0.5 * t * (t - 1.0);
+  v[1] = 1.0 - t * t;
+  v[2] = 0.5 * t * (t + 1.0);
+  d[0] = t - 0.5;
+  d[1] = -2.0 * t;
+  d[2] = t + 0.5;
+}
+
+void make_tables(HostTables &T) {
+  // Gauss-Legendre, 4 points on [-1, 1]
+  const double gp[4] = {-0.86113631159405257522, -0.33998104358485626480,
+                        0.33998104358485626480, 0.86113631159405257522};
+  const double gw[4] = {0.34785484513745385737, 0.65214515486254614263,
+                        0.65214515486254614263, 0.34785484513745385737};
+  std::memset(&T, 0, sizeof(T));
+  for (int qc = 0; qc < 4; ++qc)
+    for (int qb = 0; qb < 4; ++qb)
+      for (int qa = 0; qa < 4; ++qa) {
+        const int q = qa + 4 * qb + 16 * qc;
+        const double w = gw[qa] * gw[qb] * gw[qc];
+        double vx[3], vy[3], vz[3], dx[3], dy[3], dz[3];
+        lagrange2(gp[qa], vx, dx);
+        lagrange2(gp[qb], vy, dy);
+        lagrange2(gp[qc], vz, dz);
+        const double psi[4] = {1.0, gp[qa], gp[qb], gp[qc]};
+        for (int c = 0; c < 3; ++c)
+          for (int b = 0; b < 3; ++b)
+            for (int a = 0; a < 3; ++a) {
+              const int i = a + 3 * b + 9 * c;
+              T.phi[q][i] = vx[a] * vy[b] * vz[c];
+              T.wphi[q][i] = w * T.phi[q][i];
+              T.dphi[q][i][0] = dx[a] * vy[b] * vz[c];
+              T.dphi[q][i][1] = vx[a] * dy[b] * vz[c];
+              T.dphi[q][i][2] = vx[a] * vy[b] * dz[c];
+            }
+        for (int d = 0; d < 3; ++d) {
+          for (int i = 0; i < NU_LOC; ++i)
+            for (int j = 0; j < NU_LOC; ++j) T.K[d][i][j] += w * T.dphi[q][i][d] * T.dphi[q][j][d];
+          for (int m = 0; m < NP_LOC; ++m)
+            for (int j = 0; j < NU_LOC; ++j) T.B[d][m][j] += w * psi[m] * T.dphi[q][j][d];
+        }
+      }
+}
+
+// position of column key in the sorted row [lo, hi), or -1 if absent (a
+// pattern that lacks a coupling of the cell: the entry is left out)
+__device__ __forceinline__ int find_pos(const int *cols, int lo, int hi, int key) {
+  const int end = hi;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (cols[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return (lo < end && cols[lo] == key) ? lo : -1;
+}
+
+__global__ void __launch_bounds__(kAsmThreads) k_assemble_cells(
+    AsmOp op, DevCells cells, const int *__restrict__ list, int ncol,
+    const double *__restrict__ cell_h, const double *__restrict__ conv, double nu) {
+  __shared__ int ud[NU_LOC], pd[NP_LOC];
+  __shared__ double bl[NU_LOC][3];   // nodal convection of the cell
+  __shared__ double bq[kNq][3];      // convection at the Gauss points
+  __shared__ double G[kNq][NU_LOC];  // b(q) . grad phi_j(q)
+  const int slot = blockIdx.x, tid = threadIdx.x;
+  if (slot >= ncol) return;  // whole block
+  const int cell = list[slot];
+  const int nu_ = op.nu;
+  if (tid < NU_LOC) ud[tid] = cells.udofs[(size_t)cell * NU_LOC + tid];
+  if (tid < NP_LOC) pd[tid] = cells.pdofs[(size_t)cell * NP_LOC + tid];
+  const double hx = cell_h[(size_t)cell * 3], hy = cell_h[(size_t)cell * 3 + 1],
+               hz = cell_h[(size_t)cell * 3 + 2];
+  const double s[3] = {2.0 / hx, 2.0 / hy, 2.0 / hz};
+  const double detJ = hx * hy * hz * 0.125;
+  __syncthreads();
+  for (int t = tid; t < NU_LOC * 3; t += kAsmThreads) {
+    const int m = t / 3, d = t - 3 * m;
+    bl[m][d] = conv[(size_t)d * nu_ + ud[m]];
+  }
+  __syncthreads();
+  for (int t = tid; t < kNq * 3; t += kAsmThreads) {
+    const int q = t / 3, d = t - 3 * q;
+    double v = 0.0;
+#pragma unroll 9
+    for (int m = 0; m < NU_LOC; ++m) v += bl[m][d] * g_phi[q][m];
+    bq[q][d] = v;
+  }
+  __syncthreads();
+  for (int t = tid; t < kNq * NU_LOC; t += kAsmThreads) {
+    const int q = t / NU_LOC, j = t - NU_LOC * q;
+    G[q][j] = s[0] * bq[q][0] * g_dphi[q][j][0] + s[1] * bq[q][1] * g_dphi[q][j][1] +
+              s[2] * bq[q][2] * g_dphi[q][j][2];
+  }
+  __syncthreads();
+  // A entries (active rows only)
+  for (int t = tid; t < NU_LOC * NU_LOC; t += kAsmThreads) {
+    const int i = t / NU_LOC, j = t - NU_LOC * i;
+    const int r = ud[i];
+    if (r >= op.nact) continue;
+    double conv_ij = 0.0;
+#pragma unroll 8
+    for (int q = 0; q < kNq; ++q) conv_ij += g_wphi[q][i] * G[q][j];
+    const double v = nu * detJ *
+                         (s[0] * s[0] * c_Kref[0][i][j] + s[1] * s[1] * c_Kref[1][i][j] +
+                          s[2] * s[2] * c_Kref[2][i][j]) +
+                     detJ * conv_ij;
+    const int pos = find_pos(op.a_col, op.a_rowptr[r], op.a_rowptr[r + 1], ud[j]);
+    if (pos < 0) continue;
+    op.a[0][pos] += v;
+    if (op.a[4]) op.a[4][pos] += v;
+    if (op.a[8]) op.a[8][pos] += v;
+  }
+  // B rows of the cell's pressure DOFs and BT entries of its active velocity rows
+  for (int t = tid; t < NP_LOC * NU_LOC; t += kAsmThreads) {
+    const int m = t / NU_LOC, j = t - NU_LOC * m;
+    double v[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] = -detJ * s[d] * c_Bref[d][m][j];
+    const int p = pd[m];
+    const int bpos = find_pos(op.b_col, op.b_rowptr[p], op.b_rowptr[p + 1], ud[j]);
+    if (bpos >= 0) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) op.b[d][bpos] += v[d];
+    }
+    const int r = ud[j];
+    if (r < op.nact) {
+      const int tpos = find_pos(op.bt_col, op.bt_rowptr[r], op.bt_rowptr[r + 1], p);
+      if (tpos >= 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) op.bt[d][tpos] += v[d];
+      }
+    }
+  }
+}
+
+__global__ void k_assemble_dirichlet(AsmOp op) {
+  const int r = op.nact + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= op.nu) return;
+  const int pos = find_pos(op.a_col, op.a_rowptr[r], op.a_rowptr[r + 1], r);
+  if (pos < 0) return;
+  op.a[0][pos] = 1.0;
+  if (op.a[4]) op.a[4][pos] = 1.0;
+  if (op.a[8]) op.a[8][pos] = 1.0;
+}
+
+inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
+
+}  // namespace
+
+int assemble_tables_init() {
+  static HostTables T;
+  static bool made = false;
+  if (!made) {
+    make_tables(T);
+    made = true;
+  }
+  if (cudaMemcpyToSymbol(c_Kref, T.K, sizeof(T.K)) != cudaSuccess ||
+      cudaMemcpyToSymbol(c_Bref, T.B, sizeof(T.B)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_wphi, T.wphi, sizeof(T.wphi)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_phi, T.phi, sizeof(T.phi)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_dphi, T.dphi, sizeof(T.dphi)) != cudaSuccess)
+    return -1;
+  return 0;
+}
+
+int launch_assemble_level(const AsmOp &op, const DevCells &cells, const int *colour_cells,
+                          const int *colour_ptr, int ncolours, const double *cell_h,
+                          const double *conv, double nu, cudaStream_t s) {
+  int n = 0;
+  for (int k = 0; k < 9; ++k)
+    if (op.a[k] &&
+        cudaMemsetAsync(op.a[k], 0, sizeof(double) * (size_t)op.a_nnz, s) != cudaSuccess)
+      return -1;
+  for (int k = 0; k < 3; ++k)
+    if (cudaMemsetAsync(op.b[k], 0, sizeof(double) * (size_t)op.b_nnz, s) != cudaSuccess ||
+        cudaMemsetAsync(op.bt[k], 0, sizeof(double) * (size_t)op.bt_nnz, s) != cudaSuccess)
+      return -1;
+  for (int k = 0; k < ncolours; ++k) {
+    const int b = colour_ptr[k], m = colour_ptr[k + 1] - b;
+    if (m <= 0) continue;
+    k_assemble_cells<<<m, kAsmThreads, 0, s>>>(op, cells, colour_cells + b, m, cell_h, conv, nu);
+    if (ok() < 0) return -1;
+    ++n;
+  }
+  if (op.nu > op.nact) {
+    k_assemble_dirichlet<<<(op.nu - op.nact + 255) / 256, 256, 0, s>>>(op);
+    if (ok() < 0) return -1;
+    ++n;
+  }
+  return n;
+}
+
+}  // namespace pm

@@ -160,6 +160,25 @@ template <typename T>
 int launch_schur_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                        const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s);
 
+// --------------------------------------------------------------- assembly --
+// Writable view of a level's FP64 values for device assembly: NSTYPE 4 fills
+// a[0], a[4], a[8] and zeroes the other blocks; a one-block level has a[0]
+// only (a[1..8] null).
+struct AsmOp {
+  int nu, np, nact, a_nnz, b_nnz, bt_nnz;
+  const int *a_rowptr, *a_col, *b_rowptr, *b_col, *bt_rowptr, *bt_col;
+  double *a[9];
+  double *b[3], *bt[3];
+};
+// reference tables into the current device's constant / global memory
+int assemble_tables_init();
+// Galerkin Oseen blocks of one level (pm_assemble.cu): zero the values, then
+// colour by colour one CTA per cell; cell_h = (hx, hy, hz) per cell, conv =
+// [b1|b2|b3] at the velocity nodes.  Returns the number of kernels launched.
+int launch_assemble_level(const AsmOp &op, const DevCells &cells, const int *colour_cells,
+                          const int *colour_ptr, int ncolours, const double *cell_h,
+                          const double *conv, double nu, cudaStream_t s);
+
 // ----------------------------------------------------------------- coarse --
 // Dense column-major N x N coarse saddle matrix of SolveExact
 // (src/FE/NSE_MGLevel4.C:5728-5830) from the FP64 CSR.

@@ -65,6 +65,24 @@ class OseenProblem:
     def desc(self, level: int) -> PmLevelDesc:
         return self._descs[level]
 
+    def cell_sizes(self, level: int) -> np.ndarray:
+        """(hx, hy, hz) of every cell of a level, shape (n_cells, 3)."""
+        d = self._descs[level % self.n_levels]
+        out = np.empty((d.n_cells, 3))
+        if self._lib.pmh_cell_sizes(self._h, level % self.n_levels,
+                                    out.ctypes.data_as(C.POINTER(C.c_double))) != 0:
+            raise ValueError("bad level")
+        return out
+
+    def convection_nodal(self, level: int) -> np.ndarray:
+        """The convection field at the level's velocity nodes, [b1|b2|b3]."""
+        d = self._descs[level % self.n_levels]
+        out = np.empty(3 * d.n_udof)
+        if self._lib.pmh_convection_nodal(self._h, level % self.n_levels,
+                                          out.ctypes.data_as(C.POINTER(C.c_double))) != 0:
+            raise ValueError("bad level")
+        return out
+
     def is_one_block(self) -> bool:
         """True when every level has A12..A32 = 0 on the active rows and
         A11 = A22 = A33 exactly (the Galerkin Oseen/Stokes forms with the

@@ -116,6 +116,13 @@ class PmSolver:
             out[name] = {"ms": ms.value, "launches": n.value, "bytes": b.value}
         return out
 
+    def assemble_level(self, level, cell_h, conv, nu):
+        """pm_assemble_level: Galerkin Oseen blocks of one level on the device
+        from cell sizes (n_cells x 3) and nodal convection [b1|b2|b3]."""
+        cell_h, conv = _f64(cell_h), _f64(conv)
+        self._check(self._lib.pm_assemble_level(self._h, level, _dp(cell_h), _dp(conv), float(nu)),
+                    "pm_assemble_level")
+
     # ------------------------------------------------------------ level ops
     def coupled_defect(self, level, x, b, project=True):
         x, b = _f64(x), _f64(b)
