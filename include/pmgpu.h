@@ -241,6 +241,28 @@ pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const
 /* Same with device pointers (e.g. the current velocity on the device). */
 pm_status pm_assemble_level_device(pm_handle *h, int level, const double *d_cell_h,
                                    const double *d_conv, double nu);
+/* Time-dependent system of one level (the theta scheme of
+ * TSystemTNSE3D::AssembleSystMat, src/System/SystemTNSE3D.C:1118-1274):
+ * velocity blocks c_mass * M + c_a * A with the Q2 mass matrix M and the
+ * Oseen block A of pm_assemble_level (A11 = A22 = A33, A12..A32 = 0), B
+ * scaled by b_scale and BT by bt_scale; M and A are kept for
+ * pm_system_rhs.  The reference's system matrix is c_mass = 1,
+ * c_a = tau * theta1, bt_scale = scale (and b_scale = scale * the divergence
+ * scaling when that is on).  Call pm_refactor after the levels. */
+pm_status pm_assemble_system_level(pm_handle *h, int level, const double *cell_h,
+                                   const double *conv, double nu, double c_mass, double c_a,
+                                   double b_scale, double bt_scale);
+pm_status pm_assemble_system_level_device(pm_handle *h, int level, const double *d_cell_h,
+                                          const double *d_conv, double nu, double c_mass,
+                                          double c_a, double b_scale, double bt_scale);
+/* Working right-hand side of the theta scheme on the finest level (host
+ * vectors of its size): out = c_old * old_rhs + c_new * rhs + (M - c2 A) sol
+ * on the active velocity rows, rhs on the Dirichlet rows, 0 on the pressure
+ * rows; the reference uses c_old = tau theta3, c_new = tau theta4,
+ * c2 = tau theta2 (SystemTNSE3D.C:1132-1202).  Needs the finest level
+ * assembled by pm_assemble_system_level. */
+pm_status pm_system_rhs(pm_handle *h, const double *old_rhs, const double *rhs, const double *sol,
+                        double c_old, double c_new, double c2, double *out);
 /* Batched solves of independent systems (a batch of Oseen systems of uneven
  * size, each in its own set-up handle): pm_solve for every i < n, run
  * concurrently from up to nthreads host threads (0: one per system), so the

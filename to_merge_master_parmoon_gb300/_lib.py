@@ -95,6 +95,13 @@ GPU_SYMBOLS = {
     "pm_solve_device": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.POINTER(PmResult)]),
     "pm_assemble_level": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, C.c_double]),
     "pm_assemble_level_device": (C.c_int, [_P, C.c_int, C.c_void_p, C.c_void_p, C.c_double]),
+    "pm_assemble_system_level": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, C.c_double,
+                                           C.c_double, C.c_double, C.c_double, C.c_double]),
+    "pm_assemble_system_level_device": (C.c_int, [_P, C.c_int, C.c_void_p, C.c_void_p, C.c_double,
+                                                  C.c_double, C.c_double, C.c_double,
+                                                  C.c_double]),
+    "pm_system_rhs": (C.c_int, [_P, c_double_p, c_double_p, c_double_p, C.c_double, C.c_double,
+                                C.c_double, c_double_p]),
     "pm_solve_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(c_double_p),
                                  C.POINTER(c_double_p), C.POINTER(PmResult), C.c_int]),
     "pm_refactor": (C.c_int, [_P, c_double_p]),

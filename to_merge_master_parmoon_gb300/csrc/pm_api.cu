@@ -89,6 +89,7 @@ struct LevelDev {
   double *l_omega = nullptr;                                   // step length (device)
   // device assembly inputs (allocated on first pm_assemble_level)
   double *asm_h = nullptr, *asm_conv = nullptr;
+  double *asm_A = nullptr, *asm_M = nullptr;  // Oseen block and mass matrix (system assembly)
 
   template <typename T>
   DevOp<T> op() const;
@@ -1430,16 +1431,7 @@ pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out)
   return st != PM_OK ? st : s2;
 }
 
-pm_status pm_assemble_level_device(pm_handle *h, int level, const double *d_cell_h,
-                                   const double *d_conv, double nu) {
-  PM_CHECK_LEVEL(h, level);
-  if (!d_cell_h || !d_conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
-  LevelDev &Lv = h->L[level];
-  if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
-  if (!h->asm_tables) {
-    if (assemble_tables_init() < 0) return cuda_fail(h, "assembly tables");
-    h->asm_tables = true;
-  }
+static AsmOp asm_op(LevelDev &Lv) {
   AsmOp op{};
   op.nu = Lv.nu;
   op.np = Lv.np;
@@ -1459,10 +1451,38 @@ pm_status pm_assemble_level_device(pm_handle *h, int level, const double *d_cell
     op.b[k] = Lv.b64[k];
     op.bt[k] = Lv.bt64[k];
   }
+  op.c_mass = 0.0;
+  op.c_a = 1.0;
+  op.b_scale = 1.0;
+  op.bt_scale = 1.0;
+  op.Aonly = Lv.asm_A;
+  op.Monly = Lv.asm_M;
+  return op;
+}
+
+pm_status pm_assemble_system_level_device(pm_handle *h, int level, const double *d_cell_h,
+                                          const double *d_conv, double nu, double c_mass,
+                                          double c_a, double b_scale, double bt_scale) {
+  PM_CHECK_LEVEL(h, level);
+  if (!d_cell_h || !d_conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
+  LevelDev &Lv = h->L[level];
+  if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
+  if (!h->asm_tables) {
+    if (assemble_tables_init() < 0) return cuda_fail(h, "assembly tables");
+    h->asm_tables = true;
+  }
+  if (!Lv.asm_A) PM_TRY(dalloc(h, &Lv.asm_A, (size_t)Lv.a_nnz));
+  if (!Lv.asm_M) PM_TRY(dalloc(h, &Lv.asm_M, (size_t)Lv.a_nnz));
+  AsmOp op = asm_op(Lv);
+  op.c_mass = c_mass;
+  op.c_a = c_a;
+  op.b_scale = b_scale;
+  op.bt_scale = bt_scale;
   PM_LAUNCH(launch_assemble_level(op, Lv.cells(), Lv.colour_cells, Lv.colouring.ptr.data(),
                                   (int)Lv.colouring.ptr.size() - 1, d_cell_h, d_conv, nu,
                                   h->stream));
   if (mixed(h)) {
+    const int nblk = Lv.structured ? 1 : 9;
     for (int k = 0; k < nblk; ++k)
       PM_LAUNCH((launch_convert<float, double>(Lv.a32[k], Lv.a64[k], Lv.a_nnz, h->stream)));
     for (int k = 0; k < 3; ++k) {
@@ -1473,12 +1493,14 @@ pm_status pm_assemble_level_device(pm_handle *h, int level, const double *d_cell
   return sync(h, "assembly");
 }
 
-pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const double *conv,
-                            double nu) {
-  PM_CHECK_LEVEL(h, level);
-  if (!cell_h || !conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
-  LevelDev &Lv = h->L[level];
-  if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
+pm_status pm_assemble_level_device(pm_handle *h, int level, const double *d_cell_h,
+                                   const double *d_conv, double nu) {
+  return pm_assemble_system_level_device(h, level, d_cell_h, d_conv, nu, 0.0, 1.0, 1.0, 1.0);
+}
+
+// host inputs into the level's assembly buffers
+static pm_status stage_assembly_inputs(pm_handle *h, LevelDev &Lv, const double *cell_h,
+                                       const double *conv) {
   if (!Lv.asm_h) PM_TRY(dalloc(h, &Lv.asm_h, (size_t)Lv.ncells * 3));
   if (!Lv.asm_conv) PM_TRY(dalloc(h, &Lv.asm_conv, (size_t)Lv.nu * 3));
   if (cudaMemcpyAsync(Lv.asm_h, cell_h, sizeof(double) * Lv.ncells * 3, cudaMemcpyHostToDevice,
@@ -1486,7 +1508,41 @@ pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const
       cudaMemcpyAsync(Lv.asm_conv, conv, sizeof(double) * Lv.nu * 3, cudaMemcpyHostToDevice,
                       h->stream) != cudaSuccess)
     return cuda_fail(h, "assembly inputs");
-  return pm_assemble_level_device(h, level, Lv.asm_h, Lv.asm_conv, nu);
+  return PM_OK;
+}
+
+pm_status pm_assemble_system_level(pm_handle *h, int level, const double *cell_h,
+                                   const double *conv, double nu, double c_mass, double c_a,
+                                   double b_scale, double bt_scale) {
+  PM_CHECK_LEVEL(h, level);
+  if (!cell_h || !conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
+  LevelDev &Lv = h->L[level];
+  if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
+  PM_TRY(stage_assembly_inputs(h, Lv, cell_h, conv));
+  return pm_assemble_system_level_device(h, level, Lv.asm_h, Lv.asm_conv, nu, c_mass, c_a,
+                                         b_scale, bt_scale);
+}
+
+pm_status pm_system_rhs(pm_handle *h, const double *old_rhs, const double *rhs, const double *sol,
+                        double c_old, double c_new, double c2, double *out) {
+  PM_CHECK_LEVEL(h, 0);
+  if (!old_rhs || !rhs || !sol || !out) return PM_BADARG;
+  LevelDev &F = h->L.back();
+  if (!F.asm_A || !F.asm_M)
+    return fail(h, PM_BADARG, "the finest level has no assembled Oseen and mass blocks");
+  const size_t n = (size_t)F.ndof;
+  // three staging vectors of the level (FP64)
+  PM_TRY(h2d(h, F.x64, old_rhs, n));
+  PM_TRY(h2d(h, F.y64, rhs, n));
+  PM_TRY(h2d(h, F.z64, sol, n));
+  double *o = h->xd;  // finest-level sized FP64 buffer of the solver
+  PM_LAUNCH(launch_system_rhs(asm_op(F), F.x64, F.y64, F.z64, c_old, c_new, c2, o, h->stream));
+  return d2h(h, out, o, n);
+}
+
+pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const double *conv,
+                            double nu) {
+  return pm_assemble_system_level(h, level, cell_h, conv, nu, 0.0, 1.0, 1.0, 1.0);
 }
 
 pm_status pm_solve_batch(pm_handle *const *hs, int n, double *const *sols,

@@ -37,11 +37,13 @@ constexpr int kAsmThreads = 128;
 // reference tables on the unit cube [-1, 1]^3, local Q2 order a + 3b + 9c
 __constant__ double c_Kref[3][NU_LOC][NU_LOC];   // sum_q w dphi_i,d dphi_j,d
 __constant__ double c_Bref[3][NP_LOC][NU_LOC];   // sum_q w psi_m dphi_j,d
+__constant__ double c_Mref[NU_LOC][NU_LOC];      // sum_q w phi_i phi_j
 __device__ double g_wphi[kNq][NU_LOC];           // w_q phi_i(q)
 __device__ double g_phi[kNq][NU_LOC];
 __device__ double g_dphi[kNq][NU_LOC][3];
 
 struct HostTables {
+  double M[NU_LOC][NU_LOC];
   double K[3][NU_LOC][NU_LOC];
   double B[3][NP_LOC][NU_LOC];
   double wphi[kNq][NU_LOC];
@@ -85,6 +87,8 @@ void make_tables(HostTables &T) {
               T.dphi[q][i][1] = vx[a] * dy[b] * vz[c];
               T.dphi[q][i][2] = vx[a] * vy[b] * dz[c];
             }
+        for (int i = 0; i < NU_LOC; ++i)
+          for (int j = 0; j < NU_LOC; ++j) T.M[i][j] += w * T.phi[q][i] * T.phi[q][j];
         for (int d = 0; d < 3; ++d) {
           for (int i = 0; i < NU_LOC; ++i)
             for (int j = 0; j < NU_LOC; ++j) T.K[d][i][j] += w * T.dphi[q][i][d] * T.dphi[q][j][d];
@@ -150,15 +154,19 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble_cells(
     double conv_ij = 0.0;
 #pragma unroll 8
     for (int q = 0; q < kNq; ++q) conv_ij += g_wphi[q][i] * G[q][j];
-    const double v = nu * detJ *
-                         (s[0] * s[0] * c_Kref[0][i][j] + s[1] * s[1] * c_Kref[1][i][j] +
-                          s[2] * s[2] * c_Kref[2][i][j]) +
-                     detJ * conv_ij;
+    const double va = nu * detJ *
+                          (s[0] * s[0] * c_Kref[0][i][j] + s[1] * s[1] * c_Kref[1][i][j] +
+                           s[2] * s[2] * c_Kref[2][i][j]) +
+                      detJ * conv_ij;
+    const double vm = detJ * c_Mref[i][j];
+    const double v = op.c_mass * vm + op.c_a * va;
     const int pos = find_pos(op.a_col, op.a_rowptr[r], op.a_rowptr[r + 1], ud[j]);
     if (pos < 0) continue;
     op.a[0][pos] += v;
     if (op.a[4]) op.a[4][pos] += v;
     if (op.a[8]) op.a[8][pos] += v;
+    if (op.Aonly) op.Aonly[pos] += va;
+    if (op.Monly) op.Monly[pos] += vm;
   }
   // B rows of the cell's pressure DOFs and BT entries of its active velocity rows
   for (int t = tid; t < NP_LOC * NU_LOC; t += kAsmThreads) {
@@ -170,14 +178,14 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble_cells(
     const int bpos = find_pos(op.b_col, op.b_rowptr[p], op.b_rowptr[p + 1], ud[j]);
     if (bpos >= 0) {
 #pragma unroll
-      for (int d = 0; d < 3; ++d) op.b[d][bpos] += v[d];
+      for (int d = 0; d < 3; ++d) op.b[d][bpos] += op.b_scale * v[d];
     }
     const int r = ud[j];
     if (r < op.nact) {
       const int tpos = find_pos(op.bt_col, op.bt_rowptr[r], op.bt_rowptr[r + 1], p);
       if (tpos >= 0) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) op.bt[d][tpos] += v[d];
+        for (int d = 0; d < 3; ++d) op.bt[d][tpos] += op.bt_scale * v[d];
       }
     }
   }
@@ -193,6 +201,41 @@ __global__ void k_assemble_dirichlet(AsmOp op) {
   if (op.a[8]) op.a[8][pos] = 1.0;
 }
 
+// one warp per velocity row: the working right-hand side of the theta scheme
+__global__ void k_system_rhs(AsmOp op, const double *__restrict__ old_rhs,
+                             const double *__restrict__ rhs, const double *__restrict__ sol,
+                             double c_old, double c_new, double c2, double *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nu = op.nu;
+  if (row >= nu) return;  // whole warp
+  const int i = (int)row;
+  if (i >= op.nact) {
+    if (lane < 3) out[(size_t)lane * nu + i] = rhs[(size_t)lane * nu + i];
+    return;
+  }
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int e = op.a_rowptr[i] + lane; e < op.a_rowptr[i + 1]; e += 32) {
+    const int j = op.a_col[e];
+    const double m = op.Monly[e] - c2 * op.Aonly[e];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] += m * sol[(size_t)c * nu + j];
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  if (lane < 3) {
+    const size_t k = (size_t)lane * nu + i;
+    out[k] = c_old * old_rhs[k] + c_new * rhs[k] + acc[lane];
+  }
+}
+
+__global__ void k_zero_pressure(double *p, int np) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < np) p[k] = 0.0;
+}
+
 inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 
 }  // namespace
@@ -206,6 +249,7 @@ int assemble_tables_init() {
   }
   if (cudaMemcpyToSymbol(c_Kref, T.K, sizeof(T.K)) != cudaSuccess ||
       cudaMemcpyToSymbol(c_Bref, T.B, sizeof(T.B)) != cudaSuccess ||
+      cudaMemcpyToSymbol(c_Mref, T.M, sizeof(T.M)) != cudaSuccess ||
       cudaMemcpyToSymbol(g_wphi, T.wphi, sizeof(T.wphi)) != cudaSuccess ||
       cudaMemcpyToSymbol(g_phi, T.phi, sizeof(T.phi)) != cudaSuccess ||
       cudaMemcpyToSymbol(g_dphi, T.dphi, sizeof(T.dphi)) != cudaSuccess)
@@ -220,6 +264,9 @@ int launch_assemble_level(const AsmOp &op, const DevCells &cells, const int *col
   for (int k = 0; k < 9; ++k)
     if (op.a[k] &&
         cudaMemsetAsync(op.a[k], 0, sizeof(double) * (size_t)op.a_nnz, s) != cudaSuccess)
+      return -1;
+  for (double *q : {op.Aonly, op.Monly})
+    if (q && cudaMemsetAsync(q, 0, sizeof(double) * (size_t)op.a_nnz, s) != cudaSuccess)
       return -1;
   for (int k = 0; k < 3; ++k)
     if (cudaMemsetAsync(op.b[k], 0, sizeof(double) * (size_t)op.b_nnz, s) != cudaSuccess ||
@@ -238,6 +285,18 @@ int launch_assemble_level(const AsmOp &op, const DevCells &cells, const int *col
     ++n;
   }
   return n;
+}
+
+int launch_system_rhs(const AsmOp &op, const double *old_rhs, const double *rhs,
+                      const double *sol, double c_old, double c_new, double c2, double *out,
+                      cudaStream_t s) {
+  if (!op.Aonly || !op.Monly) return -1;
+  const long long threads = (long long)op.nu * 32;
+  k_system_rhs<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(op, old_rhs, rhs, sol, c_old,
+                                                                 c_new, c2, out);
+  if (ok() < 0) return -1;
+  k_zero_pressure<<<(op.np + 255) / 256, 256, 0, s>>>(out + (size_t)3 * op.nu, op.np);
+  return ok() < 0 ? -1 : 2;
 }
 
 }  // namespace pm

@@ -169,10 +169,21 @@ struct AsmOp {
   const int *a_rowptr, *a_col, *b_rowptr, *b_col, *bt_rowptr, *bt_col;
   double *a[9];
   double *b[3], *bt[3];
+  // system values c_mass * M + c_a * A in a[], b_scale * B, bt_scale * BT;
+  // the Oseen block A and the mass matrix M also into Aonly / Monly if given
+  double c_mass, c_a, b_scale, bt_scale;
+  double *Aonly, *Monly;
 };
+// out = c_old * old_rhs + c_new * rhs + (M - c2 A) sol on the active velocity
+// rows of the three components (one block for all three), rhs on the
+// Dirichlet rows, zero pressure rows (TSystemTNSE3D::AssembleSystMat's
+// working right-hand side).
+int launch_system_rhs(const AsmOp &op, const double *old_rhs, const double *rhs,
+                      const double *sol, double c_old, double c_new, double c2, double *out,
+                      cudaStream_t s);
 // reference tables into the current device's constant / global memory
 int assemble_tables_init();
-// Galerkin Oseen blocks of one level (pm_assemble.cu): zero the values, then
+// Galerkin Oseen (and mass) blocks of one level (pm_assemble.cu): zero the values, then
 // colour by colour one CTA per cell; cell_h = (hx, hy, hz) per cell, conv =
 // [b1|b2|b3] at the velocity nodes.  Returns the number of kernels launched.
 int launch_assemble_level(const AsmOp &op, const DevCells &cells, const int *colour_cells,

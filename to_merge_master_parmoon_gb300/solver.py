@@ -123,6 +123,24 @@ class PmSolver:
         self._check(self._lib.pm_assemble_level(self._h, level, _dp(cell_h), _dp(conv), float(nu)),
                     "pm_assemble_level")
 
+    def assemble_system_level(self, level, cell_h, conv, nu, c_mass, c_a, b_scale=1.0,
+                              bt_scale=1.0):
+        """pm_assemble_system_level: c_mass M + c_a A in the velocity blocks,
+        scaled B and BT (theta-scheme system of TSystemTNSE3D)."""
+        cell_h, conv = _f64(cell_h), _f64(conv)
+        self._check(self._lib.pm_assemble_system_level(self._h, level, _dp(cell_h), _dp(conv),
+                                                       float(nu), float(c_mass), float(c_a),
+                                                       float(b_scale), float(bt_scale)),
+                    "pm_assemble_system_level")
+
+    def system_rhs(self, old_rhs, rhs, sol, c_old, c_new, c2):
+        """pm_system_rhs: working right-hand side of the theta scheme."""
+        old_rhs, rhs, sol = _f64(old_rhs), _f64(rhs), _f64(sol)
+        out = np.empty_like(rhs)
+        self._check(self._lib.pm_system_rhs(self._h, _dp(old_rhs), _dp(rhs), _dp(sol), float(c_old),
+                                            float(c_new), float(c2), _dp(out)), "pm_system_rhs")
+        return out
+
     # ------------------------------------------------------------ level ops
     def coupled_defect(self, level, x, b, project=True):
         x, b = _f64(x), _f64(b)
