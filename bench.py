@@ -35,6 +35,13 @@ METRIC = "3D Oseen time-to-1e-8 residual: mixed+learned vs plain FP64 GMG on one
 RTOL = 1e-8
 
 
+# FP64 flops of k_assemble_cells per cell: the convection field at the 64
+# Gauss points (64 x 3 x 27 FMA), b . grad phi_j there (64 x 27 x 3 FMA), the
+# convection integrals (27 x 27 x 64 FMA) and the diffusion/mass sums (27 x 27
+# x 8): 2 x 57,024 + 5,832
+ASSEMBLY_FLOP_PER_CELL = 2 * (64 * 3 * 27 * 2 + 27 * 27 * 64) + 27 * 27 * 8
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -48,6 +55,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-systems", type=int, default=48)
+    ap.add_argument("--no-assembly", action="store_true")
     ap.add_argument("--train-problems", type=int, default=8)
     return ap.parse_args()
 
@@ -183,6 +191,95 @@ def run_reference(args):
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def assembly_run(P, S, args, threads, S1=None):
+    """Device re-assembly of the Galerkin Oseen blocks of every level
+    (pm_assemble_level_device from device cell sizes and nodal convection)
+    against the host builder's assembly of the same levels on all host
+    threads, then Crank-Nicolson steps (tau = 1e-2) of the time-dependent
+    Oseen system with the convection field held fixed, every step on the
+    device: the system M + tau/2 A, B, tau BT on every level, the
+    refactorisation, the working right-hand side and the FGMRES solve; on
+    one-block (NSTYPE-2) levels when the problem has them (S1), as the theta
+    system keeps A11 = A22 = A33 and A12..A32 = 0, and on the nine-block
+    levels of S."""
+    import numpy as np
+    import torch
+    dev = [(torch.from_numpy(P.cell_sizes(l)).cuda(),
+            torch.from_numpy(P.convection_nodal(l)).cuda()) for l in range(P.n_levels)]
+    cells = [P.desc(l).n_cells for l in range(P.n_levels)]
+
+    def assemble_all():
+        t0 = time.perf_counter()
+        for l, (h, c) in enumerate(dev):
+            S.assemble_level_device(l, h.data_ptr(), c.data_ptr(), P.nu)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        assemble_all()
+    gpu = [assemble_all() for _ in range(args.steps)]
+    cpu = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        P.reassemble()
+        cpu.append(time.perf_counter() - t0)
+    # the device-assembled levels solve as the host-built ones do
+    n = P.ndof(-1)
+    d_b = torch.from_numpy(P.rhs()).cuda()
+    d_x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    f0 = S.refactor()
+    info0 = S.iterate_device(d_x.data_ptr(), d_b.data_ptr())
+
+    tau, theta = 1e-2, 0.5
+    sysm = (1.0, tau * theta, 1.0, tau)
+
+    def theta_steps(T):
+        d_u = torch.zeros(n, dtype=torch.float64, device="cuda")
+        d_w = torch.empty_like(d_u)
+        d_v = torch.empty_like(d_u)
+        rows = []
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            for l, (h, c) in enumerate(dev):
+                T.assemble_system_level_device(l, h.data_ptr(), c.data_ptr(), P.nu, *sysm)
+            t_asm = time.perf_counter() - t0
+            f_ms = T.refactor()
+            t0 = time.perf_counter()
+            T.system_rhs_device(d_b.data_ptr(), d_b.data_ptr(), d_u.data_ptr(), tau * (1 - theta),
+                                tau * theta, tau * (1 - theta), d_w.data_ptr())
+            t_rhs = time.perf_counter() - t0
+            d_v.copy_(d_u)
+            torch.cuda.synchronize()
+            info = T.iterate_device(d_v.data_ptr(), d_w.data_ptr())
+            d_u.copy_(d_v)
+            torch.cuda.synchronize()
+            rows.append({"assembly_ms": t_asm * 1e3, "factor_ms": f_ms, "rhs_ms": t_rhs * 1e3,
+                         "solve_ms": info["solve_ms"], "iterations": info["iterations"],
+                         "rel_res": info["true_res"] / max(float(torch.linalg.norm(d_w)), 1e-300)})
+        rows = rows[args.warmup:]
+
+        def mean(key):
+            return sum(r[key] for r in rows) / len(rows)
+
+        out = {k: mean(k) for k in ("assembly_ms", "factor_ms", "rhs_ms", "solve_ms",
+                                    "iterations")}
+        out["step_ms"] = sum(out[k] for k in ("assembly_ms", "factor_ms", "rhs_ms", "solve_ms"))
+        out["max_rel_res"] = max(r["rel_res"] for r in rows)
+        out["steps"] = len(rows)
+        return out
+
+    g = sum(gpu) / len(gpu)
+    return {
+        "cells": sum(cells), "levels": P.n_levels,
+        "gpu_ms": g * 1e3, "cpu_ms": min(cpu) * 1e3, "cpu_threads": threads,
+        "speedup": min(cpu) / g,
+        "fp64_gflops": ASSEMBLY_FLOP_PER_CELL * sum(cells) / g / 1e9,
+        "iterations_after": info0["iterations"], "factor_ms_after": f0,
+        "theta_steps": {"tau": tau, "theta": theta, "convection": "fixed (time-dependent Oseen)",
+                        "nine_block": theta_steps(S),
+                        "one_block": theta_steps(S1) if S1 is not None else None},
+    }
 
 
 def train_network(device, args, log=None):
@@ -424,6 +521,11 @@ def main():
     if not args.no_batch and rank == 0:
         batch = batch_run(args, local, log=lambda *a: print(*a, file=sys.stderr))
 
+    assembly = None
+    if not args.no_assembly and rank == 0:
+        assembly = assembly_run(P, solvers["mixed"], args, threads,
+                                solvers.get("mixed_one_block"))
+
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -497,6 +599,7 @@ def main():
         "roofline": roof,
         "one_block": one,
         "batch": batch,
+        "assembly": assembly,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": results["mixed_learned"]["launches"],

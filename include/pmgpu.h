@@ -263,6 +263,11 @@ pm_status pm_assemble_system_level_device(pm_handle *h, int level, const double 
  * assembled by pm_assemble_system_level. */
 pm_status pm_system_rhs(pm_handle *h, const double *old_rhs, const double *rhs, const double *sol,
                         double c_old, double c_new, double c2, double *out);
+/* Same with device vectors of the finest level's size (out may not alias
+ * the inputs). */
+pm_status pm_system_rhs_device(pm_handle *h, const double *d_old_rhs, const double *d_rhs,
+                               const double *d_sol, double c_old, double c_new, double c2,
+                               double *d_out);
 /* Batched solves of independent systems (a batch of Oseen systems of uneven
  * size, each in its own set-up handle): pm_solve for every i < n, run
  * concurrently from up to nthreads host threads (0: one per system), so the

@@ -7,7 +7,9 @@ Oseen blocks and a host Q2 mass matrix (4-point Gauss rule):
 * pm_system_rhs: c_old old + c_new rhs + (M - c2 A) sol on active rows,
   rhs on Dirichlet rows, 0 on pressure rows (1e-13);
 * three Crank-Nicolson steps with the device system: every step's solution
-  satisfies the host-assembled system to the solver tolerance."""
+  satisfies the host-assembled system to the solver tolerance.
+Each on nine-block (NSTYPE 4) and one-block (NSTYPE 2) levels: the theta
+system keeps A11 = A22 = A33 and A12..A32 = 0."""
 import ctypes as C
 
 import numpy as np
@@ -91,11 +93,12 @@ def assemble_system(S, P, c_mass, c_a, b_scale, bt_scale):
     S.refactor()
 
 
-def test_system_operator_and_rhs(problems):
+@pytest.mark.parametrize("one_block", [False, True])
+def test_system_operator_and_rhs(problems, one_block):
     from to_merge_master_parmoon_gb300 import PmSolver
     P = problems(3, 1e-2, 0)
     tau, theta = 1e-2, 0.5
-    S = PmSolver(P.descs, precision="fp64")
+    S = PmSolver(P.descs_one_block() if one_block else P.descs, precision="fp64")
     assemble_system(S, P, 1.0, tau * theta, 1.0, tau)
     rng = np.random.default_rng(9)
     for level in range(P.n_levels):
@@ -115,14 +118,21 @@ def test_system_operator_and_rhs(problems):
         w[na:] = rhs[sl][na:]
         want[sl] = w
     assert rel(out, want) < 1e-13
+    torch = pytest.importorskip("torch")
+    d_old, d_rhs, d_sol = (torch.from_numpy(v).cuda() for v in (old, rhs, sol))
+    d_out = torch.empty_like(d_rhs)
+    S.system_rhs_device(d_old.data_ptr(), d_rhs.data_ptr(), d_sol.data_ptr(), tau * theta,
+                        tau * theta, tau * (1 - theta), d_out.data_ptr())
+    assert np.array_equal(d_out.cpu().numpy(), out)
 
 
-def test_crank_nicolson_steps(problems):
+@pytest.mark.parametrize("one_block", [False, True])
+def test_crank_nicolson_steps(problems, one_block):
     from to_merge_master_parmoon_gb300 import PmSolver
     P = problems(3, 1e-2, 0)
     tau, theta = 1e-2, 0.5
     f = P.rhs()                      # forcing (Dirichlet rows carry the boundary values)
-    S = PmSolver(P.descs, precision="mixed", restart=20, maxit=80, res_norm_min=1e-30,
+    S = PmSolver(P.descs_one_block() if one_block else P.descs, precision="mixed", restart=20, maxit=80, res_norm_min=1e-30,
                  red_factor=1e-10)
     assemble_system(S, P, 1.0, tau * theta, 1.0, tau)
     K = host_system(P, 2, 1.0, tau * theta, 1.0, tau)

@@ -102,6 +102,8 @@ GPU_SYMBOLS = {
                                                   C.c_double]),
     "pm_system_rhs": (C.c_int, [_P, c_double_p, c_double_p, c_double_p, C.c_double, C.c_double,
                                 C.c_double, c_double_p]),
+    "pm_system_rhs_device": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                       C.c_double, C.c_double, C.c_void_p]),
     "pm_solve_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(c_double_p),
                                  C.POINTER(c_double_p), C.POINTER(PmResult), C.c_int]),
     "pm_refactor": (C.c_int, [_P, c_double_p]),
@@ -140,6 +142,7 @@ HOST_SYMBOLS = {
     "pmh_max_convection": (C.c_double, [C.c_void_p]),
     "pmh_cell_sizes": (C.c_int, [C.c_void_p, C.c_int, c_double_p]),
     "pmh_convection_nodal": (C.c_int, [C.c_void_p, C.c_int, c_double_p]),
+    "pmh_reassemble": (C.c_int, [C.c_void_p]),
 }
 
 _cache: dict[str, C.CDLL] = {}

@@ -651,6 +651,19 @@ int pmh_convection_nodal(const pmh_problem *p, int level, double *out) {
   return 0;
 }
 
+int pmh_reassemble(pmh_problem *p) {
+  if (!p) return -1;
+  const int n = (int)p->levels.size();
+  for (int l = 0; l < n; ++l) {
+    PMLevelData &L = p->levels[l];
+    for (auto &v : L.a) std::fill(v.begin(), v.end(), 0.0);
+    for (auto &v : L.b) std::fill(v.begin(), v.end(), 0.0);
+    for (auto &v : L.bt) std::fill(v.begin(), v.end(), 0.0);
+    assemble_level(*p, L, l == n - 1);
+  }
+  return 0;
+}
+
 int pmh_level_desc(const pmh_problem *p, int level, pm_level_desc *o) {
   if (!p || !o || level < 0 || level >= (int)p->levels.size()) return -1;
   const PMLevelData &L = p->levels[level];

@@ -62,6 +62,9 @@ double pmh_max_convection(const pmh_problem *p);
 int pmh_cell_sizes(const pmh_problem *p, int level, double *out);
 /* the convection field at the level's velocity nodes, [b1|b2|b3]; 0 or -1 */
 int pmh_convection_nodal(const pmh_problem *p, int level, double *out);
+/* Assemble the matrix values of every level again (the same cell loop as the
+ * build, on the build's threads): the host timing of a re-assembly; 0 or -1 */
+int pmh_reassemble(pmh_problem *p);
 
 #ifdef __cplusplus
 }

@@ -1540,6 +1540,21 @@ pm_status pm_system_rhs(pm_handle *h, const double *old_rhs, const double *rhs, 
   return d2h(h, out, o, n);
 }
 
+pm_status pm_system_rhs_device(pm_handle *h, const double *d_old_rhs, const double *d_rhs,
+                               const double *d_sol, double c_old, double c_new, double c2,
+                               double *d_out) {
+  PM_CHECK_LEVEL(h, 0);
+  if (!d_old_rhs || !d_rhs || !d_sol || !d_out) return PM_BADARG;
+  if (d_out == d_old_rhs || d_out == d_rhs || d_out == d_sol)
+    return fail(h, PM_BADARG, "out aliases an input");
+  LevelDev &F = h->L.back();
+  if (!F.asm_A || !F.asm_M)
+    return fail(h, PM_BADARG, "the finest level has no assembled Oseen and mass blocks");
+  PM_LAUNCH(launch_system_rhs(asm_op(F), d_old_rhs, d_rhs, d_sol, c_old, c_new, c2, d_out,
+                              h->stream));
+  return sync(h, "system rhs");
+}
+
 pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const double *conv,
                             double nu) {
   return pm_assemble_system_level(h, level, cell_h, conv, nu, 0.0, 1.0, 1.0, 1.0);

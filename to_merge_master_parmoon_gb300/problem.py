@@ -83,6 +83,12 @@ class OseenProblem:
             raise ValueError("bad level")
         return out
 
+    def reassemble(self):
+        """Assemble every level's matrix values again on the host (the build's
+        cell loop and threads); the arrays behind ``descs`` are rewritten."""
+        if self._lib.pmh_reassemble(self._h) != 0:
+            raise ValueError("pmh_reassemble failed")
+
     def is_one_block(self) -> bool:
         """True when every level has A12..A32 = 0 on the active rows and
         A11 = A22 = A33 exactly (the Galerkin Oseen/Stokes forms with the

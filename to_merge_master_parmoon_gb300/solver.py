@@ -123,6 +123,19 @@ class PmSolver:
         self._check(self._lib.pm_assemble_level(self._h, level, _dp(cell_h), _dp(conv), float(nu)),
                     "pm_assemble_level")
 
+    def assemble_level_device(self, level, d_cell_h: int, d_conv: int, nu):
+        """pm_assemble_level_device: the same from device arrays (addresses)."""
+        self._check(self._lib.pm_assemble_level_device(self._h, level, C.c_void_p(d_cell_h),
+                                                       C.c_void_p(d_conv), float(nu)),
+                    "pm_assemble_level_device")
+
+    def assemble_system_level_device(self, level, d_cell_h: int, d_conv: int, nu, c_mass, c_a,
+                                     b_scale=1.0, bt_scale=1.0):
+        """pm_assemble_system_level_device: the theta-scheme system from device arrays."""
+        self._check(self._lib.pm_assemble_system_level_device(
+            self._h, level, C.c_void_p(d_cell_h), C.c_void_p(d_conv), float(nu), float(c_mass),
+            float(c_a), float(b_scale), float(bt_scale)), "pm_assemble_system_level_device")
+
     def assemble_system_level(self, level, cell_h, conv, nu, c_mass, c_a, b_scale=1.0,
                               bt_scale=1.0):
         """pm_assemble_system_level: c_mass M + c_a A in the velocity blocks,
@@ -140,6 +153,13 @@ class PmSolver:
         self._check(self._lib.pm_system_rhs(self._h, _dp(old_rhs), _dp(rhs), _dp(sol), float(c_old),
                                             float(c_new), float(c2), _dp(out)), "pm_system_rhs")
         return out
+
+    def system_rhs_device(self, d_old: int, d_rhs: int, d_sol: int, c_old, c_new, c2, d_out: int):
+        """pm_system_rhs_device: the same on device vectors (addresses)."""
+        self._check(self._lib.pm_system_rhs_device(self._h, C.c_void_p(d_old), C.c_void_p(d_rhs),
+                                                   C.c_void_p(d_sol), float(c_old), float(c_new),
+                                                   float(c2), C.c_void_p(d_out)),
+                    "pm_system_rhs_device")
 
     # ------------------------------------------------------------ level ops
     def coupled_defect(self, level, x, b, project=True):
