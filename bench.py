@@ -35,11 +35,13 @@ METRIC = "3D Oseen time-to-1e-8 residual: mixed+learned vs plain FP64 GMG on one
 RTOL = 1e-8
 
 
-# FP64 flops of k_assemble_cells per cell: the convection field at the 64
-# Gauss points (64 x 3 x 27 FMA), b . grad phi_j there (64 x 27 x 3 FMA), the
-# convection integrals (27 x 27 x 64 FMA) and the diffusion/mass sums (27 x 27
-# x 8): 2 x 57,024 + 5,832
-ASSEMBLY_FLOP_PER_CELL = 2 * (64 * 3 * 27 * 2 + 27 * 27 * 64) + 27 * 27 * 8
+# FP64 flops of k_assemble_cells per cell (sum factorisation): the convection
+# at the Gauss points one direction at a time (108 x 3 + 144 x 3 + 192 x 3 FMA),
+# b . grad phi_j at the 64 points (1728 x 3 FMA), the convection integrals
+# contracted over qa, qb, qc (1296 x 4 + 972 x 4 + 729 x 4 FMA) and the
+# diffusion/mass combination (729 x 6)
+ASSEMBLY_FLOP_PER_CELL = 2 * (108 * 3 + 144 * 3 + 192 * 3 + 1728 * 3 + 1296 * 4 + 972 * 4
+                              + 729 * 4) + 729 * 6
 
 
 def parse():
