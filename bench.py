@@ -35,13 +35,12 @@ METRIC = "3D Oseen time-to-1e-8 residual: mixed+learned vs plain FP64 GMG on one
 RTOL = 1e-8
 
 
-# FP64 flops of k_assemble_cells per cell (sum factorisation): the convection
-# at the Gauss points one direction at a time (108 x 3 + 144 x 3 + 192 x 3 FMA),
-# b . grad phi_j at the 64 points (1728 x 3 FMA), the convection integrals
-# contracted over qa, qb, qc (1296 x 4 + 972 x 4 + 729 x 4 FMA) and the
-# diffusion/mass combination (729 x 6)
-ASSEMBLY_FLOP_PER_CELL = 2 * (108 * 3 + 144 * 3 + 192 * 3 + 1728 * 3 + 1296 * 4 + 972 * 4
-                              + 729 * 4) + 729 * 6
+# FP64 flops of k_assemble_cells<false> per cell: scaled nodal convection
+# (81 x 2), the diffusion/mass y-z factors (81 x 13), the z and y contractions
+# of the convection integrals (243 x 3 and 243 x 9 FMA), the x contraction
+# with diffusion per A entry (729 x 8 FMA) and its addition into the CSR
+# value (729), the B/BT entries (108 x 15)
+ASSEMBLY_FLOP_PER_CELL = 81 * 2 + 81 * 13 + 2 * (243 * 3 + 243 * 9) + 729 * 16 + 729 + 108 * 15
 
 
 def parse():

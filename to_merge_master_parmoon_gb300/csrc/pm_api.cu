@@ -90,6 +90,7 @@ struct LevelDev {
   // device assembly inputs (allocated on first pm_assemble_level)
   double *asm_h = nullptr, *asm_conv = nullptr;
   double *asm_A = nullptr, *asm_M = nullptr;  // Oseen block and mass matrix (system assembly)
+  bool asm_theta = false;  // asm_A / asm_M hold the last system assembly
 
   template <typename T>
   DevOp<T> op() const;
@@ -1460,9 +1461,11 @@ static AsmOp asm_op(LevelDev &Lv) {
   return op;
 }
 
-pm_status pm_assemble_system_level_device(pm_handle *h, int level, const double *d_cell_h,
-                                          const double *d_conv, double nu, double c_mass,
-                                          double c_a, double b_scale, double bt_scale) {
+// SYS: the theta-scheme system (A and M kept for pm_system_rhs); otherwise
+// the Oseen blocks alone
+static pm_status assemble_impl(pm_handle *h, int level, const double *d_cell_h,
+                               const double *d_conv, double nu, double c_mass, double c_a,
+                               double b_scale, double bt_scale, bool sys) {
   PM_CHECK_LEVEL(h, level);
   if (!d_cell_h || !d_conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
   LevelDev &Lv = h->L[level];
@@ -1471,13 +1474,17 @@ pm_status pm_assemble_system_level_device(pm_handle *h, int level, const double 
     if (assemble_tables_init() < 0) return cuda_fail(h, "assembly tables");
     h->asm_tables = true;
   }
-  if (!Lv.asm_A) PM_TRY(dalloc(h, &Lv.asm_A, (size_t)Lv.a_nnz));
-  if (!Lv.asm_M) PM_TRY(dalloc(h, &Lv.asm_M, (size_t)Lv.a_nnz));
+  if (sys) {
+    if (!Lv.asm_A) PM_TRY(dalloc(h, &Lv.asm_A, (size_t)Lv.a_nnz));
+    if (!Lv.asm_M) PM_TRY(dalloc(h, &Lv.asm_M, (size_t)Lv.a_nnz));
+  }
   AsmOp op = asm_op(Lv);
   op.c_mass = c_mass;
   op.c_a = c_a;
   op.b_scale = b_scale;
   op.bt_scale = bt_scale;
+  if (!sys) op.Aonly = op.Monly = nullptr;
+  Lv.asm_theta = false;
   PM_LAUNCH(launch_assemble_level(op, Lv.cells(), Lv.colour_cells, Lv.colouring.ptr.data(),
                                   (int)Lv.colouring.ptr.size() - 1, d_cell_h, d_conv, nu,
                                   h->stream));
@@ -1490,12 +1497,20 @@ pm_status pm_assemble_system_level_device(pm_handle *h, int level, const double 
       PM_LAUNCH((launch_convert<float, double>(Lv.bt32[k], Lv.bt64[k], Lv.bt_nnz, h->stream)));
     }
   }
-  return sync(h, "assembly");
+  PM_TRY(sync(h, "assembly"));
+  Lv.asm_theta = sys;
+  return PM_OK;
+}
+
+pm_status pm_assemble_system_level_device(pm_handle *h, int level, const double *d_cell_h,
+                                          const double *d_conv, double nu, double c_mass,
+                                          double c_a, double b_scale, double bt_scale) {
+  return assemble_impl(h, level, d_cell_h, d_conv, nu, c_mass, c_a, b_scale, bt_scale, true);
 }
 
 pm_status pm_assemble_level_device(pm_handle *h, int level, const double *d_cell_h,
                                    const double *d_conv, double nu) {
-  return pm_assemble_system_level_device(h, level, d_cell_h, d_conv, nu, 0.0, 1.0, 1.0, 1.0);
+  return assemble_impl(h, level, d_cell_h, d_conv, nu, 0.0, 1.0, 1.0, 1.0, false);
 }
 
 // host inputs into the level's assembly buffers
@@ -1528,8 +1543,8 @@ pm_status pm_system_rhs(pm_handle *h, const double *old_rhs, const double *rhs, 
   PM_CHECK_LEVEL(h, 0);
   if (!old_rhs || !rhs || !sol || !out) return PM_BADARG;
   LevelDev &F = h->L.back();
-  if (!F.asm_A || !F.asm_M)
-    return fail(h, PM_BADARG, "the finest level has no assembled Oseen and mass blocks");
+  if (!F.asm_theta)
+    return fail(h, PM_BADARG, "the finest level has no system assembly (Oseen and mass blocks)");
   const size_t n = (size_t)F.ndof;
   // three staging vectors of the level (FP64)
   PM_TRY(h2d(h, F.x64, old_rhs, n));
@@ -1548,8 +1563,8 @@ pm_status pm_system_rhs_device(pm_handle *h, const double *d_old_rhs, const doub
   if (d_out == d_old_rhs || d_out == d_rhs || d_out == d_sol)
     return fail(h, PM_BADARG, "out aliases an input");
   LevelDev &F = h->L.back();
-  if (!F.asm_A || !F.asm_M)
-    return fail(h, PM_BADARG, "the finest level has no assembled Oseen and mass blocks");
+  if (!F.asm_theta)
+    return fail(h, PM_BADARG, "the finest level has no system assembly (Oseen and mass blocks)");
   PM_LAUNCH(launch_system_rhs(asm_op(F), d_old_rhs, d_rhs, d_sol, c_old, c_new, c2, d_out,
                               h->stream));
   return sync(h, "system rhs");
@@ -1557,7 +1572,12 @@ pm_status pm_system_rhs_device(pm_handle *h, const double *d_old_rhs, const doub
 
 pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const double *conv,
                             double nu) {
-  return pm_assemble_system_level(h, level, cell_h, conv, nu, 0.0, 1.0, 1.0, 1.0);
+  PM_CHECK_LEVEL(h, level);
+  if (!cell_h || !conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
+  LevelDev &Lv = h->L[level];
+  if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
+  PM_TRY(stage_assembly_inputs(h, Lv, cell_h, conv));
+  return pm_assemble_level_device(h, level, Lv.asm_h, Lv.asm_conv, nu);
 }
 
 pm_status pm_solve_batch(pm_handle *const *hs, int n, double *const *sols,

@@ -11,10 +11,17 @@
 // Here one CTA of 256 threads assembles one cell of a colour and adds into
 // the level's CSR values in place; cells of one colour share no DOF, so the
 // additions need no atomics and the order of the sums is fixed.  The
-// quadrature sums use the tensor-product structure of the Q2 basis and the
-// Gauss rule (sum factorisation): b(q) from the nodal values and the
-// convection integrals contract one direction at a time, 1.9e4 FMA per cell
-// instead of 5.7e4 for the plain 64-point sums.  Cells are
+// convection integrals use the tensor-product structure: with b the Q2
+// interpolant (b_m at the nodes),
+//   int phi_i (b_x d_x phi_j) = sum_m b_m,x X1(a,am,aj) Y0(b,bm,bj) Y0(c,cm,cj)
+// with the 1D integrals Y0 = int l l l and X1 = int l l l' over [-1, 1]
+// (likewise for y and z), which the 4-point Gauss rule integrates exactly, as
+// it does the 3D integrand; the sum over m contracts one direction at a time
+// (7.3e3 FMA per cell instead of 5.7e4 for the plain 64-point sums; the y and
+// z terms share their x factor Y0 and are summed before the last step).
+// Diffusion and mass are Kronecker products of the 1D matrices
+// D1 = int l' l' and M1 = int l l, e.g. M = M1 (x) M1 (x) M1, combined per
+// cell in the y-z factors so that an entry costs two FMA.  Cells are
 // axis-aligned boxes (the Jacobian is diag(hx, hy, hz) / 2), as in the
 // uniform and stretched box meshes of the workloads.  Per cell:
 //   diffusion  nu * detJ * sum_d s_d^2 Kref_d           (reference tables)
@@ -37,27 +44,19 @@ namespace {
 
 constexpr int kNq = 64;          // 4 x 4 x 4 Gauss points, q = qa + 4 qb + 16 qc
 constexpr int kAsmThreads = 256;
-// padded row strides (odd) of the per-basis-function shared arrays: the
-// threads of a warp take consecutive j
-constexpr int kGS = 65, kT1S = 49, kT2S = 37;
 
 // reference tables on the unit cube [-1, 1]^3, local Q2 order a + 3b + 9c.
 // Global memory read through L1 (the threads of a warp read different
 // entries, which constant memory would serialise).
-__device__ double g_Kref[3][NU_LOC][NU_LOC];   // sum_q w dphi_i,d dphi_j,d
 __device__ double g_Bref[3][NP_LOC][NU_LOC];   // sum_q w psi_m dphi_j,d
-__device__ double g_Mref[NU_LOC][NU_LOC];      // sum_q w phi_i phi_j
-__device__ double g_dphi[kNq][NU_LOC][3];      // grad phi_j(q) on the unit cube
-__device__ double g_l1[4][3];                  // 1D quadratic Lagrange l_a(x_q)
-__device__ double g_wl1[4][3];                 // w_q l_a(x_q)
+__device__ double g_tri[2][3][3][3];           // [0]: int l_a l_m l_j, [1]: int l_a l_m l_j'
+__device__ double g_dm[2][3][3];               // [0]: int l_a' l_j', [1]: int l_a l_j
 
 struct HostTables {
-  double M[NU_LOC][NU_LOC];
-  double K[3][NU_LOC][NU_LOC];
   double B[3][NP_LOC][NU_LOC];
-  double phi[kNq][NU_LOC];
   double dphi[kNq][NU_LOC][3];
-  double l1[4][3], wl1[4][3];
+  double tri[2][3][3][3];
+  double dm[2][3][3];
 };
 
 void lagrange2(double t, double *v, double *d) {
@@ -79,10 +78,17 @@ void make_tables(HostTables &T) {
   for (int q = 0; q < 4; ++q) {
     double v[3], d[3];
     lagrange2(gp[q], v, d);
-    for (int a = 0; a < 3; ++a) {
-      T.l1[q][a] = v[a];
-      T.wl1[q][a] = gw[q] * v[a];
-    }
+    for (int a = 0; a < 3; ++a)
+      for (int m = 0; m < 3; ++m)
+        for (int j = 0; j < 3; ++j) {
+          T.tri[0][a][m][j] += gw[q] * v[a] * v[m] * v[j];
+          T.tri[1][a][m][j] += gw[q] * v[a] * v[m] * d[j];
+        }
+    for (int a = 0; a < 3; ++a)
+      for (int j = 0; j < 3; ++j) {
+        T.dm[0][a][j] += gw[q] * d[a] * d[j];
+        T.dm[1][a][j] += gw[q] * v[a] * v[j];
+      }
   }
   for (int qc = 0; qc < 4; ++qc)
     for (int qb = 0; qb < 4; ++qb)
@@ -98,19 +104,13 @@ void make_tables(HostTables &T) {
           for (int b = 0; b < 3; ++b)
             for (int a = 0; a < 3; ++a) {
               const int i = a + 3 * b + 9 * c;
-              T.phi[q][i] = vx[a] * vy[b] * vz[c];
               T.dphi[q][i][0] = dx[a] * vy[b] * vz[c];
               T.dphi[q][i][1] = vx[a] * dy[b] * vz[c];
               T.dphi[q][i][2] = vx[a] * vy[b] * dz[c];
             }
-        for (int i = 0; i < NU_LOC; ++i)
-          for (int j = 0; j < NU_LOC; ++j) T.M[i][j] += w * T.phi[q][i] * T.phi[q][j];
-        for (int d = 0; d < 3; ++d) {
-          for (int i = 0; i < NU_LOC; ++i)
-            for (int j = 0; j < NU_LOC; ++j) T.K[d][i][j] += w * T.dphi[q][i][d] * T.dphi[q][j][d];
+        for (int d = 0; d < 3; ++d)
           for (int m = 0; m < NP_LOC; ++m)
             for (int j = 0; j < NU_LOC; ++j) T.B[d][m][j] += w * psi[m] * T.dphi[q][j][d];
-        }
       }
 }
 
@@ -125,111 +125,104 @@ __device__ __forceinline__ int find_pos(const int *cols, int lo, int hi, int key
   return (lo < end && cols[lo] == key) ? lo : -1;
 }
 
+// SYS: the system c_mass M + c_a A, with A and M also stored (Aonly, Monly);
+// otherwise the Oseen block A alone
+template <bool SYS>
 __global__ void __launch_bounds__(kAsmThreads) k_assemble_cells(
     AsmOp op, DevCells cells, const int *__restrict__ list, int ncol,
     const double *__restrict__ cell_h, const double *__restrict__ conv, double nu) {
   __shared__ int ud[NU_LOC], pd[NP_LOC];
-  __shared__ double l1[4][3], wl1[4][3];
-  __shared__ double bl[3][NU_LOC];        // nodal convection of the cell [d][m]
-  __shared__ double S1[3][9][4];          // [d][ia + 3 ib][qc]
-  __shared__ double S2[3][3][16];         // [d][ia][qb + 4 qc]
-  __shared__ double bq[3][kNq];           // convection at the Gauss points
-  __shared__ double G[NU_LOC * kGS];      // [j][16 qa + qb + 4 qc]: b(q) . grad phi_j(q)
-  __shared__ double T1[NU_LOC * kT1S];    // [j][16 ia + qb + 4 qc]: qa contracted
-  __shared__ double T2[NU_LOC * kT2S];    // [j][4 (ia + 3 ib) + qc]: qb contracted
+  __shared__ double F[2][27];             // 1D triple-product integrals [Y0 | X1][a][m][j]
+  __shared__ double DM[2][9];             // 1D [D1 | M1][a][j]
+  __shared__ double sb[3][NU_LOC];        // detJ s_d b_m,d: scaled nodal convection
+  __shared__ double W1[3][9][9];          // [d][am + 3 bm][3 c + cj]: cm contracted
+  __shared__ double W2x[3][81];           // [am][w], w = 9 (3 b + bj) + 3 c + cj: d = x
+  __shared__ double W2yz[3][81];          // the same, d = y and z summed
+  __shared__ double Pyz[81], Qyz[81], Myz[81];  // diffusion and mass y-z factors
+  __shared__ double cs[4];                // s0, s1, s2, detJ
   const int slot = blockIdx.x, tid = threadIdx.x;
   if (slot >= ncol) return;  // whole block
   const int cell = list[slot];
   const int nu_ = op.nu;
   if (tid < NU_LOC) ud[tid] = cells.udofs[(size_t)cell * NU_LOC + tid];
   if (tid < NP_LOC) pd[tid] = cells.pdofs[(size_t)cell * NP_LOC + tid];
-  if (tid < 12) {
-    l1[tid / 3][tid % 3] = g_l1[tid / 3][tid % 3];
-    wl1[tid / 3][tid % 3] = g_wl1[tid / 3][tid % 3];
-  }
-  const double hx = cell_h[(size_t)cell * 3], hy = cell_h[(size_t)cell * 3 + 1],
-               hz = cell_h[(size_t)cell * 3 + 2];
-  const double s0 = 2.0 / hx, s1 = 2.0 / hy, s2 = 2.0 / hz;
-  const double detJ = hx * hy * hz * 0.125;
+  if (tid < 54) F[tid / 27][tid % 27] = (&g_tri[0][0][0][0])[tid];
+  if (tid >= 64 && tid < 82) DM[(tid - 64) / 9][(tid - 64) % 9] = (&g_dm[0][0][0])[tid - 64];
+  // s_d = 2 / h_d and detJ = hx hy hz / 8, once per cell (an FP64 division
+  // is a sequence of FMA: not on every thread)
+  if (tid < 3) cs[tid] = 2.0 / cell_h[(size_t)cell * 3 + tid];
+  if (tid == 3)
+    cs[3] = cell_h[(size_t)cell * 3] * cell_h[(size_t)cell * 3 + 1] *
+            cell_h[(size_t)cell * 3 + 2] * 0.125;
   __syncthreads();
+  const double s0 = cs[0], s1 = cs[1], s2 = cs[2], detJ = cs[3];
   for (int t = tid; t < 3 * NU_LOC; t += kAsmThreads) {
     const int d = t / NU_LOC, m = t - NU_LOC * d;
-    bl[d][m] = conv[(size_t)d * nu_ + ud[m]];
+    sb[d][m] = detJ * cs[d] * conv[(size_t)d * nu_ + ud[m]];
+  }
+  if (tid >= 128 && tid < 128 + 81) {
+    const int w = tid - 128;
+    const int bbj = w / 9, ccj = w - 9 * bbj;
+    const double mb = DM[1][bbj], mc = DM[1][ccj], db = DM[0][bbj], dc = DM[0][ccj];
+    const double nd = nu * detJ;
+    Pyz[w] = nd * s0 * s0 * mb * mc;
+    Qyz[w] = nd * (s1 * s1 * db * mc + s2 * s2 * mb * dc);
+    Myz[w] = detJ * mb * mc;
   }
   __syncthreads();
-  // b(q) = sum_m b_m phi_m(q), one direction at a time: c, b, a
-  for (int t = tid; t < 3 * 9 * 4; t += kAsmThreads) {
-    const int qc = t & 3, ab = (t >> 2) % 9, d = t / 36;
-    S1[d][ab][qc] = bl[d][ab] * l1[qc][0] + bl[d][ab + 9] * l1[qc][1] + bl[d][ab + 18] * l1[qc][2];
+  // direction z (cm): the derivative factor X1 for d = 2, else Y0
+  for (int t = tid; t < 3 * 81; t += kAsmThreads) {
+    const int d = t / 81, u = t - 81 * d;
+    const int ab = u / 9, ccj = u - 9 * ab;
+    const double *f = &F[d == 2][(ccj / 3) * 9 + (ccj % 3)];  // [c][cm][cj], stride 3 in cm
+    W1[d][ab][ccj] = sb[d][ab] * f[0] + sb[d][ab + 9] * f[3] + sb[d][ab + 18] * f[6];
   }
   __syncthreads();
-  for (int t = tid; t < 3 * 3 * 16; t += kAsmThreads) {
-    const int r = t & 15, ia = (t >> 4) % 3, d = t / 48;
-    const int qb = r & 3, qc = r >> 2;
-    S2[d][ia][r] = S1[d][ia][qc] * l1[qb][0] + S1[d][ia + 3][qc] * l1[qb][1] +
-                   S1[d][ia + 6][qc] * l1[qb][2];
+  // direction y (bm): X1 for d = 1, else Y0; d = y and z summed
+  for (int t = tid; t < 3 * 81; t += kAsmThreads) {
+    const int am = t / 81, w = t - 81 * am;
+    const int bbj = w / 9, ccj = w - 9 * bbj;
+    const int fo = (bbj / 3) * 9 + (bbj % 3);  // [b][bm][bj]
+    const double *y0 = &F[0][fo], *x1 = &F[1][fo];
+    W2x[am][w] = W1[0][am][ccj] * y0[0] + W1[0][am + 3][ccj] * y0[3] + W1[0][am + 6][ccj] * y0[6];
+    W2yz[am][w] = W1[1][am][ccj] * x1[0] + W1[1][am + 3][ccj] * x1[3] +
+                  W1[1][am + 6][ccj] * x1[6] + W1[2][am][ccj] * y0[0] +
+                  W1[2][am + 3][ccj] * y0[3] + W1[2][am + 6][ccj] * y0[6];
   }
   __syncthreads();
-  for (int t = tid; t < 3 * kNq; t += kAsmThreads) {
-    const int q = t & 63, d = t >> 6;
-    const int qa = q & 3, r = q >> 2;
-    bq[d][q] = S2[d][0][r] * l1[qa][0] + S2[d][1][r] * l1[qa][1] + S2[d][2][r] * l1[qa][2];
-  }
-  __syncthreads();
-  for (int t = tid; t < kNq * NU_LOC; t += kAsmThreads) {
-    const int q = t / NU_LOC, j = t - NU_LOC * q;
-    const int qa = q & 3, r = q >> 2;
-    G[j * kGS + 16 * qa + r] = s0 * bq[0][q] * g_dphi[q][j][0] + s1 * bq[1][q] * g_dphi[q][j][1] +
-                               s2 * bq[2][q] * g_dphi[q][j][2];
-  }
-  __syncthreads();
-  // conv_ij = sum_q w_q phi_i(q) G_j(q): contract qa, then qb, then qc
-  for (int t = tid; t < 48 * NU_LOC; t += kAsmThreads) {
-    const int u = t / NU_LOC, j = t - NU_LOC * u;
-    const int ia = u % 3, r = u / 3;
-    const double *g = &G[j * kGS + r];
-    T1[j * kT1S + 16 * ia + r] =
-        wl1[0][ia] * g[0] + wl1[1][ia] * g[16] + wl1[2][ia] * g[32] + wl1[3][ia] * g[48];
-  }
-  __syncthreads();
-  for (int t = tid; t < 36 * NU_LOC; t += kAsmThreads) {
-    const int u = t / NU_LOC, j = t - NU_LOC * u;
-    const int qc = u & 3, ab = u >> 2;
-    const int ia = ab % 3, ib = ab / 3;
-    const double *g = &T1[j * kT1S + 16 * ia + 4 * qc];
-    T2[j * kT2S + 4 * ab + qc] =
-        wl1[0][ib] * g[0] + wl1[1][ib] * g[1] + wl1[2][ib] * g[2] + wl1[3][ib] * g[3];
-  }
-  __syncthreads();
-  const double k0 = nu * detJ * s0 * s0, k1 = nu * detJ * s1 * s1, k2 = nu * detJ * s2 * s2;
-  // A entries (active rows only), j fastest over the threads
+  // A entries (active rows only), j fastest over the threads: direction x (am)
   for (int t = tid; t < NU_LOC * NU_LOC; t += kAsmThreads) {
     const int i = t / NU_LOC, j = t - NU_LOC * i;
     const int r = ud[i];
     if (r >= op.nact) continue;
-    const int ab = i % 9, ic = i / 9;
-    const double *g = &T2[j * kT2S + 4 * ab];
-    const double conv_ij =
-        wl1[0][ic] * g[0] + wl1[1][ic] * g[1] + wl1[2][ic] * g[2] + wl1[3][ic] * g[3];
-    const double va = k0 * g_Kref[0][i][j] + k1 * g_Kref[1][i][j] + k2 * g_Kref[2][i][j] +
-                      detJ * conv_ij;
-    const double vm = detJ * g_Mref[i][j];
-    const double v = op.c_mass * vm + op.c_a * va;
+    const int ia = i % 3, ib = (i / 3) % 3, ic = i / 9;
+    const int ja = j % 3, jb = (j / 3) % 3, jc = j / 9;
+    const int w = 9 * (3 * ib + jb) + 3 * ic + jc;
+    const int fo = ia * 9 + ja;  // [a][am][aj]
+    const double va = F[1][fo] * W2x[0][w] + F[1][fo + 3] * W2x[1][w] + F[1][fo + 6] * W2x[2][w] +
+                      F[0][fo] * W2yz[0][w] + F[0][fo + 3] * W2yz[1][w] +
+                      F[0][fo + 6] * W2yz[2][w] + DM[0][3 * ia + ja] * Pyz[w] +
+                      DM[1][3 * ia + ja] * Qyz[w];
     const int pos = find_pos(op.a_col, op.a_rowptr[r], op.a_rowptr[r + 1], ud[j]);
     if (pos < 0) continue;
+    double v = va;
+    if (SYS) {
+      const double vm = DM[1][3 * ia + ja] * Myz[w];
+      v = op.c_mass * vm + op.c_a * va;
+      op.Aonly[pos] += va;
+      op.Monly[pos] += vm;
+    }
     op.a[0][pos] += v;
     if (op.a[4]) op.a[4][pos] += v;
     if (op.a[8]) op.a[8][pos] += v;
-    if (op.Aonly) op.Aonly[pos] += va;
-    if (op.Monly) op.Monly[pos] += vm;
   }
   // B rows of the cell's pressure DOFs and BT entries of its active velocity rows
-  const double s[3] = {s0, s1, s2};
+  const double nb[3] = {-detJ * s0, -detJ * s1, -detJ * s2};
   for (int t = tid; t < NP_LOC * NU_LOC; t += kAsmThreads) {
     const int m = t / NU_LOC, j = t - NU_LOC * m;
     double v[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) v[d] = -detJ * s[d] * g_Bref[d][m][j];
+    for (int d = 0; d < 3; ++d) v[d] = nb[d] * g_Bref[d][m][j];
     const int p = pd[m];
     const int bpos = find_pos(op.b_col, op.b_rowptr[p], op.b_rowptr[p + 1], ud[j]);
     if (bpos >= 0) {
@@ -303,12 +296,9 @@ int assemble_tables_init() {
     make_tables(T);
     made = true;
   }
-  if (cudaMemcpyToSymbol(g_Kref, T.K, sizeof(T.K)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_Bref, T.B, sizeof(T.B)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_Mref, T.M, sizeof(T.M)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_dphi, T.dphi, sizeof(T.dphi)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_l1, T.l1, sizeof(T.l1)) != cudaSuccess ||
-      cudaMemcpyToSymbol(g_wl1, T.wl1, sizeof(T.wl1)) != cudaSuccess)
+  if (cudaMemcpyToSymbol(g_Bref, T.B, sizeof(T.B)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_tri, T.tri, sizeof(T.tri)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_dm, T.dm, sizeof(T.dm)) != cudaSuccess)
     return -1;
   return 0;
 }
@@ -331,7 +321,12 @@ int launch_assemble_level(const AsmOp &op, const DevCells &cells, const int *col
   for (int k = 0; k < ncolours; ++k) {
     const int b = colour_ptr[k], m = colour_ptr[k + 1] - b;
     if (m <= 0) continue;
-    k_assemble_cells<<<m, kAsmThreads, 0, s>>>(op, cells, colour_cells + b, m, cell_h, conv, nu);
+    if (op.Aonly && op.Monly)
+      k_assemble_cells<true><<<m, kAsmThreads, 0, s>>>(op, cells, colour_cells + b, m, cell_h,
+                                                       conv, nu);
+    else
+      k_assemble_cells<false><<<m, kAsmThreads, 0, s>>>(op, cells, colour_cells + b, m, cell_h,
+                                                        conv, nu);
     if (ok() < 0) return -1;
     ++n;
   }
