@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-systems", type=int, default=48)
     ap.add_argument("--no-assembly", action="store_true")
+    ap.add_argument("--only-assembly", action="store_true",
+                    help="device assembly of every level only (one-block FP64 levels, "
+                         "warm-up + steps passes): the case profiled for k_assemble_cells")
     ap.add_argument("--train-problems", type=int, default=8)
     return ap.parse_args()
 
@@ -283,6 +286,30 @@ def assembly_run(P, S, args, threads, S1=None):
     }
 
 
+def only_assembly(args):
+    """pm_assemble_level_device on every level of one-block FP64 levels,
+    args.warmup + args.steps passes; prints the mean time of a pass."""
+    import torch
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed, nthreads=os.cpu_count() or 1)
+    S = PmSolver(P.descs_one_block() if P.is_one_block() else P.descs, precision="fp64")
+    dev = [(torch.from_numpy(P.cell_sizes(l)).cuda(),
+            torch.from_numpy(P.convection_nodal(l)).cuda()) for l in range(P.n_levels)]
+    times = []
+    for k in range(args.warmup + args.steps):
+        n0 = S.kernel_launches
+        t0 = time.perf_counter()
+        for l, (h, c) in enumerate(dev):
+            S.assemble_level_device(l, h.data_ptr(), c.data_ptr(), P.nu)
+        times.append(time.perf_counter() - t0)
+        launches = S.kernel_launches - n0
+    times = times[args.warmup:]
+    print(json.dumps({"only_assembly": True, "levels": P.n_levels,
+                      "cells": sum(P.desc(l).n_cells for l in range(P.n_levels)),
+                      "ms_per_pass": 1e3 * sum(times) / len(times),
+                      "kernel_launches_per_pass": launches}), flush=True)
+
+
 def train_network(device, args, log=None):
     """The learned smoother's network: (residual, error) pairs harvested from
     plain FP64 solves of 32^3 problems with nu log-uniform in [1e-3, 1e-1]
@@ -381,6 +408,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.only_assembly:
+        only_assembly(args)
         return
     rank, world, local = dist_env()
     import numpy as np
