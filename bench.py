@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-systems", type=int, default=48)
     ap.add_argument("--no-assembly", action="store_true")
+    ap.add_argument("--no-channel", action="store_true")
+    ap.add_argument("--channel-steps", type=int, default=10,
+                    help="timed Crank-Nicolson steps per variant of the channel run "
+                         "(a bounded sample of its 200 steps)")
     ap.add_argument("--only-assembly", action="store_true",
                     help="device assembly of every level only (one-block FP64 levels, "
                          "warm-up + steps passes): the case profiled for k_assemble_cells")
@@ -284,6 +288,90 @@ def assembly_run(P, S, args, threads, S1=None):
                         "nine_block": theta_steps(S),
                         "one_block": theta_steps(S1) if S1 is not None else None},
     }
+
+
+def channel_run(args, threads, net):
+    """Time-dependent channel (TNSE3D): box [0, 2pi] x [-1, 1] x [0, pi],
+    64 x 64 x 32 hexahedra (5 levels from 4 x 4 x 2), periodic in x and z,
+    no-slip at y = +-1, y = tanh(2.5 eta)/tanh(2.5), Q2/P1disc, nu = 1/180,
+    body force 2 nu e_x, initial velocity 1 - y^2 plus a 5 % seeded
+    divergence-free perturbation; Crank-Nicolson (theta = 1/2), dt = 1e-3,
+    one Oseen linearisation per step on the current velocity, solved to a
+    1e-8 residual reduction.  Every step on the device: the velocity at the
+    coarse nodes (pm_interpolate_coarse), the system M + dt/2 A(u), B, dt BT
+    on every level (pm_assemble_system_level_device), the refactorisation,
+    the working right-hand side (pm_system_rhs_device) and the FGMRES solve
+    from u.  NSTYPE-2 levels (the system keeps A11 = A22 = A33, A12..A32 = 0).
+    Variants: FP64, mixed, mixed + learned smoother; 2 untimed steps, then
+    args.channel_steps timed steps from the same initial state each."""
+    import numpy as np
+    import torch
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    from to_merge_master_parmoon_gb300.solver import PmError
+    P = OseenProblem(n_levels=5, nu=1.0 / 180.0, seed=args.seed, example="channel", nx0=4, ny0=4,
+                     nz0=2, box=(0.0, 2 * np.pi, -1.0, 1.0, 0.0, np.pi), periodic="xz",
+                     stretch_y=2.5, perturb=0.05, nthreads=threads)
+    L = P.n_levels
+    D1 = P.descs_one_block()
+    tau, theta = 1e-3, 0.5
+    n3 = 3 * P.desc(L - 1).n_udof
+    d_h = [torch.from_numpy(P.cell_sizes(l)).cuda() for l in range(L)]
+    d_conv = [torch.empty(3 * P.desc(l).n_udof, dtype=torch.float64, device="cuda")
+              for l in range(L - 1)]
+    d_f = torch.from_numpy(P.rhs()).cuda()
+    u0 = torch.zeros_like(d_f)
+    u0[:n3] = torch.from_numpy(P.convection_nodal(L - 1)).cuda()
+    d_w = torch.empty_like(d_f)
+    out = {"workload": "channel 64x64x32 (tanh 2.5 in y), periodic x/z, Q2/P1disc, nu=1/180, "
+                       "CN dt=1e-3, one Oseen linearisation per step to 1e-8 reduction",
+           "ndof": P.ndof(-1), "levels": L, "timed_steps": args.channel_steps}
+    for name, prec, learned in (("fp64", "fp64", False), ("mixed", "mixed", False),
+                                ("mixed_learned", "mixed", True)):
+        kw = dict(precision=prec, restart=20, maxit=100, res_norm_min=1e-300, red_factor=1e-8,
+                  red_initial=1)
+        try:
+            S = PmSolver(D1, upload_mode=1, **kw)
+        except PmError:
+            S = PmSolver(D1, upload_mode=0, **kw)
+        if learned:
+            S.attach_learned(net, omega=1.0, fallback_ratio=0.5)
+        d_u = u0.clone()
+        rows = []
+        for k in range(2 + args.channel_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            conv = [None] * L
+            conv[L - 1] = d_u[:n3]
+            for l in range(L - 1, 0, -1):
+                S.interpolate_coarse(l, conv[l].data_ptr(), d_conv[l - 1].data_ptr())
+                conv[l - 1] = d_conv[l - 1]
+            for l in range(L):
+                S.assemble_system_level_device(l, d_h[l].data_ptr(), conv[l].data_ptr(), P.nu,
+                                               1.0, tau * theta, 1.0, tau)
+            t1 = time.perf_counter()
+            f_ms = S.refactor()
+            t2 = time.perf_counter()
+            S.system_rhs_device(d_f.data_ptr(), d_f.data_ptr(), d_u.data_ptr(), tau * (1 - theta),
+                                tau * theta, tau * (1 - theta), d_w.data_ptr())
+            info = S.iterate_device(d_u.data_ptr(), d_w.data_ptr(), allow=(0, 1))
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            rows.append({"assembly_ms": (t1 - t0) * 1e3, "factor_ms": f_ms,
+                         "solve_ms": (t3 - t2) * 1e3, "step_ms": (t3 - t0) * 1e3,
+                         "iterations": info["iterations"],
+                         "reduction": info["true_res"] / max(info["res0"], 1e-300)})
+        rows = rows[2:]
+        mean = lambda key: sum(r[key] for r in rows) / len(rows)
+        out[name] = {k: mean(k) for k in ("step_ms", "assembly_ms", "factor_ms", "solve_ms",
+                                           "iterations")}
+        out[name]["max_reduction"] = max(r["reduction"] for r in rows)
+        out[name]["s_per_200_steps"] = mean("step_ms") * 200 / 1e3
+        if learned:
+            out[name]["learned_status"] = S.learned_status()
+        umax = float(d_u[:n3].abs().max())
+        out[name]["max_abs_u"] = umax
+        S.close()
+    return out
 
 
 def only_assembly(args):
@@ -557,6 +645,10 @@ def main():
         assembly = assembly_run(P, solvers["mixed"], args, threads,
                                 solvers.get("mixed_one_block"))
 
+    channel = None
+    if not args.no_channel and rank == 0:
+        channel = channel_run(args, threads, net)
+
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -631,6 +723,7 @@ def main():
         "one_block": one,
         "batch": batch,
         "assembly": assembly,
+        "channel": channel,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": results["mixed_learned"]["launches"],

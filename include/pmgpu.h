@@ -123,6 +123,11 @@ typedef struct {
                              the FP64 and FP32 copies in one pass (needs a
                              device that reads pageable host memory, e.g. a
                              Grace-coupled GPU; PM_BADARG otherwise)         */
+  int red_initial;        /* 0 (default, the reference's rule): red_factor
+                             applies to res0 of the current restart cycle;
+                             1: to the residual at the start of the solve, so
+                             that "reduce by red_factor" holds across
+                             restarts (e.g. one time step solved to 1e-8)  */
 } pm_options;
 
 /* One multigrid level in the reference's data layout.  Levels are added
@@ -268,6 +273,15 @@ pm_status pm_system_rhs(pm_handle *h, const double *old_rhs, const double *rhs, 
 pm_status pm_system_rhs_device(pm_handle *h, const double *d_old_rhs, const double *d_rhs,
                                const double *d_sol, double c_old, double c_new, double c2,
                                double *d_out);
+/* Nodal values of a velocity field [u1|u2|u3] of `level` at the velocity
+ * nodes of level-1 (each coarse node is a node of the nested fine mesh):
+ * the convection field of the coarser levels for the assembly entry points,
+ * e.g. from the current velocity in a time step.  Device vectors of
+ * 3 n_udof(level) and 3 n_udof(level-1); needs cell_parent / cell_child.
+ * ParMooN's RestrictFunction (src/FE/MGComponents3D.C:1243-1506) averages
+ * child-wise L2 projections instead; both return the coarse function itself
+ * when the fine function lies in the coarse space. */
+pm_status pm_interpolate_coarse(pm_handle *h, int level, const double *d_fine, double *d_coarse);
 /* Batched solves of independent systems (a batch of Oseen systems of uneven
  * size, each in its own set-up handle): pm_solve for every i < n, run
  * concurrently from up to nthreads host threads (0: one per system), so the

@@ -39,7 +39,7 @@ class PmOptions(C.Structure):
         ("red_factor", C.c_double), ("res_norm_min", C.c_double), ("div_factor", C.c_double),
         ("device", C.c_int), ("use_graphs", C.c_int), ("verbose", C.c_int),
         ("pin_host", C.c_int), ("vanka_inverse", C.c_int), ("residual_variant", C.c_int),
-        ("apply_variant", C.c_int), ("upload_mode", C.c_int),
+        ("apply_variant", C.c_int), ("upload_mode", C.c_int), ("red_initial", C.c_int),
     ]
 
 
@@ -60,6 +60,7 @@ class PmhParams(C.Structure):
         ("x0", C.c_double), ("x1", C.c_double), ("y0", C.c_double), ("y1", C.c_double),
         ("z0", C.c_double), ("z1", C.c_double), ("nu", C.c_double), ("seed", C.c_uint64),
         ("example", C.c_int), ("n_modes", C.c_int), ("nthreads", C.c_int),
+        ("periodic", C.c_int), ("stretch_y", C.c_double), ("perturb", C.c_double),
     ]
 
 
@@ -104,6 +105,7 @@ GPU_SYMBOLS = {
                                 C.c_double, c_double_p]),
     "pm_system_rhs_device": (C.c_int, [_P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                        C.c_double, C.c_double, C.c_void_p]),
+    "pm_interpolate_coarse": (C.c_int, [_P, C.c_int, C.c_void_p, C.c_void_p]),
     "pm_solve_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(c_double_p),
                                  C.POINTER(c_double_p), C.POINTER(PmResult), C.c_int]),
     "pm_refactor": (C.c_int, [_P, c_double_p]),

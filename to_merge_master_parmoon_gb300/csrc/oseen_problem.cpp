@@ -183,9 +183,38 @@ void quadlin_grad(double x, double y, double z, double g[3][3]) {
   g[2][0] = -2 * z; g[2][1] = 10 * y; g[2][2] = -2 * x;
 }
 
+// Channel perturbation: sum_m curl(a_m sin(theta_m) w(y)) with the wall
+// factor w = (1 - eta^2)^2 (w = w' = 0 at the walls), wavenumbers that are
+// periodic in x and z: curl(a s w) = w cos(theta) (k x a) + s w' (e_y x a).
+void channel_perturbation(const pmh_problem &P, double x, double y, double z, double *p) {
+  const pmh_params &q = P.prm;
+  const double Lx = q.x1 - q.x0, Ly = q.y1 - q.y0, Lz = q.z1 - q.z0;
+  const double eta = (2.0 * y - q.y0 - q.y1) / Ly, e2 = 1.0 - eta * eta;
+  const double w = e2 * e2, dw = -4.0 * eta * e2 * (2.0 / Ly);
+  p[0] = p[1] = p[2] = 0.0;
+  for (const Mode &m : P.bmodes) {
+    const double kx = 2.0 * M_PI * m.k[0] / Lx, ky = M_PI * m.k[1] / Ly,
+                 kz = 2.0 * M_PI * m.k[2] / Lz;
+    const double th = kx * (x - q.x0) + ky * (y - q.y0) + kz * (z - q.z0) + m.phase;
+    const double c = w * std::cos(th), sn = dw * std::sin(th);
+    p[0] += c * (ky * m.a[2] - kz * m.a[1]) + sn * m.a[2];
+    p[1] += c * (kz * m.a[0] - kx * m.a[2]);
+    p[2] += c * (kx * m.a[1] - ky * m.a[0]) - sn * m.a[0];
+  }
+}
+
 void convection(const pmh_problem &P, double x, double y, double z, double *b) {
   b[0] = b[1] = b[2] = 0.0;
   if (P.prm.example == PMH_EXAMPLE_QUADLIN_STOKES) return;
+  if (P.prm.example == PMH_EXAMPLE_CHANNEL) {
+    const double eta = (2.0 * y - P.prm.y0 - P.prm.y1) / (P.prm.y1 - P.prm.y0);
+    double p[3];
+    channel_perturbation(P, x, y, z, p);
+    b[0] = (1.0 - eta * eta) + P.bscale * p[0];
+    b[1] = P.bscale * p[1];
+    b[2] = P.bscale * p[2];
+    return;
+  }
   if (P.prm.example == PMH_EXAMPLE_QUADLIN_OSEEN) {
     quadlin_u(x, y, z, b);
     return;
@@ -220,6 +249,12 @@ void forcing(const pmh_problem &P, double x, double y, double z, double *f) {
       f[k] = -nu * lap[k] + u[0] * g[k][0] + u[1] * g[k][1] + u[2] * g[k][2] + gp[k];
     return;
   }
+  if (P.prm.example == PMH_EXAMPLE_CHANNEL) {
+    const double s = 2.0 / (P.prm.y1 - P.prm.y0);
+    f[0] = 2.0 * nu * s * s;  // -nu d2/dy2 (1 - eta^2)
+    f[1] = f[2] = 0.0;
+    return;
+  }
   f[0] = f[1] = f[2] = 0.0;
   for (const Mode &m : P.fmodes) {
     double s = std::sin(2.0 * M_PI * (m.k[0] * x + m.k[1] * y + m.k[2] * z) + m.phase);
@@ -230,7 +265,7 @@ void forcing(const pmh_problem &P, double x, double y, double z, double *f) {
 }
 
 bool boundary_value(const pmh_problem &P, double x, double y, double z, double *u) {
-  if (P.prm.example == PMH_EXAMPLE_RANDOM_OSEEN) {
+  if (P.prm.example == PMH_EXAMPLE_RANDOM_OSEEN || P.prm.example == PMH_EXAMPLE_CHANNEL) {
     u[0] = u[1] = u[2] = 0.0;
     return false;
   }
@@ -238,46 +273,73 @@ bool boundary_value(const pmh_problem &P, double x, double y, double z, double *
   return true;
 }
 
-// per-dimension coupling ranges of a Q2 node index (nodes of all cells that
-// contain the node)
-inline void node_range(int i, int gmax, int &lo, int &hi) {
-  if (i & 1) {
-    lo = i - 1;
-    hi = i + 1;
+// per-dimension coupling lists of a Q2 node index i on a line of g = 2n + 1
+// grid nodes (the nodes of all cells that contain it); a periodic direction
+// identifies node 2n with node 0, so indices wrap modulo 2n (duplicates, for
+// n = 2, are removed by the caller)
+inline int node_list(int i, int g, bool per, int *out) {
+  const int lo = (i & 1) ? i - 1 : i - 2, hi = (i & 1) ? i + 1 : i + 2;
+  int n = 0;
+  if (per) {
+    const int m = g - 1;
+    for (int t = lo; t <= hi; ++t) out[n++] = ((t % m) + m) % m;
   } else {
-    lo = std::max(i - 2, 0);
-    hi = std::min(i + 2, gmax - 1);
+    for (int t = std::max(lo, 0); t <= std::min(hi, g - 1); ++t) out[n++] = t;
   }
+  return n;
 }
-inline void cell_range(int i, int ncells, int &lo, int &hi) {
-  if (i & 1) {
-    lo = hi = (i - 1) / 2;
-  } else {
-    lo = std::max(i / 2 - 1, 0);
-    hi = std::min(i / 2, ncells - 1);
+// cells (per direction) that contain node i; nc cells on the line
+inline int cell_list(int i, int nc, bool per, int *out) {
+  const int lo = (i & 1) ? (i - 1) / 2 : i / 2 - 1, hi = (i & 1) ? (i - 1) / 2 : i / 2;
+  int n = 0;
+  for (int t = lo; t <= hi; ++t) {
+    if (per)
+      out[n++] = ((t % nc) + nc) % nc;
+    else if (t >= 0 && t < nc)
+      out[n++] = t;
   }
+  return n;
 }
 
-void build_level_structure(PMLevelData &L) {
+void build_level_structure(PMLevelData &L, int periodic) {
+  const bool px = periodic & PMH_PERIODIC_X, py = periodic & PMH_PERIODIC_Y,
+             pz = periodic & PMH_PERIODIC_Z;
   const int gx = L.gx(), gy = L.gy(), gz = L.gz();
   const int ng = gx * gy * gz;
+  // canonical grid node: the last node of a periodic direction is the first
+  auto canon = [&](int i, int j, int k) {
+    if (px && i == gx - 1) i = 0;
+    if (py && j == gy - 1) j = 0;
+    if (pz && k == gz - 1) k = 0;
+    return i + gx * (j + gy * k);
+  };
+  auto dirichlet = [&](int i, int j, int k) {
+    return (!px && (i == 0 || i == gx - 1)) || (!py && (j == 0 || j == gy - 1)) ||
+           (!pz && (k == 0 || k == gz - 1));
+  };
   L.n_cells = L.nx * L.ny * L.nz;
-  L.n_udof = ng;
   L.n_pdof = 4 * L.n_cells;
   L.grid2dof.assign(ng, -1);
-  L.dof2grid.assign(ng, -1);
   int next = 0;
-  for (int k = 1; k < gz - 1; ++k)
-    for (int j = 1; j < gy - 1; ++j)
-      for (int i = 1; i < gx - 1; ++i) L.grid2dof[i + gx * (j + gy * k)] = next++;
-  L.n_active = next;
+  for (int pass = 0; pass < 2; ++pass) {  // active nodes first, then Dirichlet
+    for (int k = 0; k < gz; ++k)
+      for (int j = 0; j < gy; ++j)
+        for (int i = 0; i < gx; ++i) {
+          const int g = i + gx * (j + gy * k);
+          if (canon(i, j, k) != g || dirichlet(i, j, k) != (pass == 1)) continue;
+          L.grid2dof[g] = next++;
+        }
+    if (pass == 0) L.n_active = next;
+  }
+  L.n_udof = next;
+  L.dof2grid.assign(next, -1);
   for (int k = 0; k < gz; ++k)
     for (int j = 0; j < gy; ++j)
       for (int i = 0; i < gx; ++i) {
-        int g = i + gx * (j + gy * k);
-        if (L.grid2dof[g] < 0) L.grid2dof[g] = next++;
+        const int g = i + gx * (j + gy * k), c = canon(i, j, k);
+        if (c == g) L.dof2grid[L.grid2dof[g]] = g;
+        else L.grid2dof[g] = L.grid2dof[c];
       }
-  for (int g = 0; g < ng; ++g) L.dof2grid[L.grid2dof[g]] = g;
 
   // cells
   L.cell_udofs.resize((size_t)L.n_cells * 27);
@@ -296,41 +358,39 @@ void build_level_structure(PMLevelData &L) {
         L.cell_colour[c] = (cx & 1) + 2 * (cy & 1) + 4 * (cz & 1);
       }
 
-  // A pattern
-  L.a_rowptr.assign(ng + 1, 0);
-  for (int r = 0; r < ng; ++r) {
-    int g = L.dof2grid[r];
-    if (r >= L.n_active) {
-      L.a_rowptr[r + 1] = 1;
-      continue;
-    }
-    int i = g % gx, j = (g / gx) % gy, k = g / (gx * gy);
-    int il, ih, jl, jh, kl, kh;
-    node_range(i, gx, il, ih);
-    node_range(j, gy, jl, jh);
-    node_range(k, gz, kl, kh);
-    L.a_rowptr[r + 1] = (ih - il + 1) * (jh - jl + 1) * (kh - kl + 1);
-  }
-  for (int r = 0; r < ng; ++r) L.a_rowptr[r + 1] += L.a_rowptr[r];
-  L.a_col.resize(L.a_rowptr[ng]);
+  // A pattern: active rows hold the nodes of all cells containing the node
+  const int nu = L.n_udof;
+  auto a_row = [&](int r, int *out) {
+    const int g = L.dof2grid[r];
+    const int i = g % gx, j = (g / gx) % gy, k = g / (gx * gy);
+    int li[5], lj[5], lk[5];
+    const int ni = node_list(i, gx, px, li), nj = node_list(j, gy, py, lj),
+              nk = node_list(k, gz, pz, lk);
+    int n = 0;
+    for (int c = 0; c < nk; ++c)
+      for (int b = 0; b < nj; ++b)
+        for (int a = 0; a < ni; ++a) out[n++] = L.grid2dof[li[a] + gx * (lj[b] + gy * lk[c])];
+    std::sort(out, out + n);
+    return (int)(std::unique(out, out + n) - out);
+  };
+  L.a_rowptr.assign(nu + 1, 0);
 #pragma omp parallel for schedule(static)
-  for (int r = 0; r < ng; ++r) {
+  for (int r = 0; r < nu; ++r) {
+    int buf[125];
+    L.a_rowptr[r + 1] = r >= L.n_active ? 1 : a_row(r, buf);
+  }
+  for (int r = 0; r < nu; ++r) L.a_rowptr[r + 1] += L.a_rowptr[r];
+  L.a_col.resize(L.a_rowptr[nu]);
+#pragma omp parallel for schedule(static)
+  for (int r = 0; r < nu; ++r) {
     int *out = L.a_col.data() + L.a_rowptr[r];
     if (r >= L.n_active) {
       out[0] = r;
       continue;
     }
-    int g = L.dof2grid[r];
-    int i = g % gx, j = (g / gx) % gy, k = g / (gx * gy);
-    int il, ih, jl, jh, kl, kh;
-    node_range(i, gx, il, ih);
-    node_range(j, gy, jl, jh);
-    node_range(k, gz, kl, kh);
-    int n = 0;
-    for (int kk = kl; kk <= kh; ++kk)
-      for (int jj = jl; jj <= jh; ++jj)
-        for (int ii = il; ii <= ih; ++ii) out[n++] = L.grid2dof[ii + gx * (jj + gy * kk)];
-    std::sort(out, out + n);
+    int buf[125];
+    const int n = a_row(r, buf);
+    std::memcpy(out, buf, sizeof(int) * n);
   }
   for (int b = 0; b < 9; ++b) L.a[b].assign(L.a_col.size(), 0.0);
 
@@ -348,35 +408,35 @@ void build_level_structure(PMLevelData &L) {
   for (int b = 0; b < 3; ++b) L.b[b].assign(L.b_col.size(), 0.0);
 
   // BT pattern: row r -> P dofs of all cells containing node r (sorted)
-  L.bt_rowptr.assign(ng + 1, 0);
-  for (int r = 0; r < ng; ++r) {
-    int g = L.dof2grid[r];
-    int i = g % gx, j = (g / gx) % gy, k = g / (gx * gy);
-    int il, ih, jl, jh, kl, kh;
-    cell_range(i, L.nx, il, ih);
-    cell_range(j, L.ny, jl, jh);
-    cell_range(k, L.nz, kl, kh);
-    L.bt_rowptr[r + 1] = 4 * (ih - il + 1) * (jh - jl + 1) * (kh - kl + 1);
-  }
-  for (int r = 0; r < ng; ++r) L.bt_rowptr[r + 1] += L.bt_rowptr[r];
-  L.bt_col.resize(L.bt_rowptr[ng]);
-#pragma omp parallel for schedule(static)
-  for (int r = 0; r < ng; ++r) {
-    int g = L.dof2grid[r];
-    int i = g % gx, j = (g / gx) % gy, k = g / (gx * gy);
-    int il, ih, jl, jh, kl, kh;
-    cell_range(i, L.nx, il, ih);
-    cell_range(j, L.ny, jl, jh);
-    cell_range(k, L.nz, kl, kh);
-    int *out = L.bt_col.data() + L.bt_rowptr[r];
+  auto bt_row = [&](int r, int *out) {
+    const int g = L.dof2grid[r];
+    const int i = g % gx, j = (g / gx) % gy, k = g / (gx * gy);
+    int li[2], lj[2], lk[2];
+    const int ni = cell_list(i, L.nx, px, li), nj = cell_list(j, L.ny, py, lj),
+              nk = cell_list(k, L.nz, pz, lk);
     int n = 0;
-    for (int kk = kl; kk <= kh; ++kk)
-      for (int jj = jl; jj <= jh; ++jj)
-        for (int ii = il; ii <= ih; ++ii) {
-          int c = ii + L.nx * (jj + L.ny * kk);
-          for (int m = 0; m < 4; ++m) out[n++] = 4 * c + m;
+    for (int c = 0; c < nk; ++c)
+      for (int b = 0; b < nj; ++b)
+        for (int a = 0; a < ni; ++a) {
+          const int cell = li[a] + L.nx * (lj[b] + L.ny * lk[c]);
+          for (int m = 0; m < 4; ++m) out[n++] = 4 * cell + m;
         }
     std::sort(out, out + n);
+    return (int)(std::unique(out, out + n) - out);
+  };
+  L.bt_rowptr.assign(nu + 1, 0);
+#pragma omp parallel for schedule(static)
+  for (int r = 0; r < nu; ++r) {
+    int buf[32];
+    L.bt_rowptr[r + 1] = bt_row(r, buf);
+  }
+  for (int r = 0; r < nu; ++r) L.bt_rowptr[r + 1] += L.bt_rowptr[r];
+  L.bt_col.resize(L.bt_rowptr[nu]);
+#pragma omp parallel for schedule(static)
+  for (int r = 0; r < nu; ++r) {
+    int buf[32];
+    const int n = bt_row(r, buf);
+    std::memcpy(L.bt_col.data() + L.bt_rowptr[r], buf, sizeof(int) * n);
   }
   for (int b = 0; b < 3; ++b) L.bt[b].assign(L.bt_col.size(), 0.0);
 }
@@ -519,6 +579,9 @@ void pmh_default_params(pmh_params *p) {
   p->example = PMH_EXAMPLE_RANDOM_OSEEN;
   p->n_modes = 8;
   p->nthreads = 0;
+  p->periodic = 0;
+  p->stretch_y = 0.0;
+  p->perturb = 0.05;
 }
 
 void pmh_q2_basis(double xi, double eta, double zeta, double *values, double *derivs) {
@@ -527,6 +590,13 @@ void pmh_q2_basis(double xi, double eta, double zeta, double *values, double *de
 
 pmh_problem *pmh_build(const pmh_params *prm) {
   if (!prm || prm->n_levels < 1 || prm->nx0 < 1 || prm->ny0 < 1 || prm->nz0 < 1) return nullptr;
+  // a periodic direction needs an even number of cells (>= 2): the parity
+  // colouring must separate the cells on both sides of the identified faces
+  if (((prm->periodic & PMH_PERIODIC_X) && (prm->nx0 < 2 || (prm->nx0 & 1))) ||
+      ((prm->periodic & PMH_PERIODIC_Y) && (prm->ny0 < 2 || (prm->ny0 & 1))) ||
+      ((prm->periodic & PMH_PERIODIC_Z) && (prm->nz0 < 2 || (prm->nz0 & 1))) ||
+      prm->stretch_y < 0.0)
+    return nullptr;
 #ifdef _OPENMP
   if (prm->nthreads > 0) omp_set_num_threads(prm->nthreads);
 #endif
@@ -557,9 +627,17 @@ pmh_problem *pmh_build(const pmh_params *prm) {
     L.ys.resize(L.ny + 1);
     L.zs.resize(L.nz + 1);
     for (int i = 0; i <= L.nx; ++i) L.xs[i] = prm->x0 + (prm->x1 - prm->x0) * i / L.nx;
-    for (int i = 0; i <= L.ny; ++i) L.ys[i] = prm->y0 + (prm->y1 - prm->y0) * i / L.ny;
+    for (int i = 0; i <= L.ny; ++i) {
+      if (prm->stretch_y > 0.0) {
+        const double eta = -1.0 + 2.0 * i / L.ny;
+        const double t = std::tanh(prm->stretch_y * eta) / std::tanh(prm->stretch_y);
+        L.ys[i] = prm->y0 + (prm->y1 - prm->y0) * 0.5 * (1.0 + t);
+      } else {
+        L.ys[i] = prm->y0 + (prm->y1 - prm->y0) * i / L.ny;
+      }
+    }
     for (int i = 0; i <= L.nz; ++i) L.zs[i] = prm->z0 + (prm->z1 - prm->z0) * i / L.nz;
-    build_level_structure(L);
+    build_level_structure(L, prm->periodic);
     L.cell_parent.assign(L.n_cells, -1);
     L.cell_child.assign(L.n_cells, -1);
     if (l > 0) {
@@ -589,9 +667,33 @@ pmh_problem *pmh_build(const pmh_params *prm) {
     P->bscale = bmax > 0 ? 1.0 / bmax : 1.0;
     P->bmax = 1.0;
   }
+  // channel: perturbation scaled to max |p| = perturb at the finest nodes
+  if (prm->example == PMH_EXAMPLE_CHANNEL) {
+    const PMLevelData &F = P->levels.back();
+    double pmax = 0.0;
+#pragma omp parallel for reduction(max : pmax) schedule(static)
+    for (int r = 0; r < F.n_udof; ++r) {
+      const int g = F.dof2grid[r];
+      const int i = g % F.gx(), j = (g / F.gx()) % F.gy(), k = g / (F.gx() * F.gy());
+      double p[3];
+      channel_perturbation(*P, F.node_x(i), F.node_y(j), F.node_z(k), p);
+      pmax = std::max(pmax, std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]));
+    }
+    P->bscale = pmax > 0 ? prm->perturb / pmax : 0.0;
+    double bmax = 0.0;
+#pragma omp parallel for reduction(max : bmax) schedule(static)
+    for (int r = 0; r < F.n_udof; ++r) {
+      const int g = F.dof2grid[r];
+      const int i = g % F.gx(), j = (g / F.gx()) % F.gy(), k = g / (F.gx() * F.gy());
+      double b[3];
+      convection(*P, F.node_x(i), F.node_y(j), F.node_z(k), b);
+      bmax = std::max(bmax, std::sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]));
+    }
+    P->bmax = bmax;
+  }
   for (int l = 0; l < prm->n_levels; ++l) assemble_level(*P, P->levels[l], l == prm->n_levels - 1);
 
-  if (prm->example != PMH_EXAMPLE_RANDOM_OSEEN) {
+  if (prm->example == PMH_EXAMPLE_QUADLIN_STOKES || prm->example == PMH_EXAMPLE_QUADLIN_OSEEN) {
     const PMLevelData &F = P->levels.back();
     P->has_exact = true;
     P->exact.assign((size_t)3 * F.n_udof + F.n_pdof, 0.0);

@@ -25,8 +25,13 @@ extern "C" {
 enum {
   PMH_EXAMPLE_RANDOM_OSEEN = 0,   /* seeded divergence-free Fourier convection + smooth forcing */
   PMH_EXAMPLE_QUADLIN_STOKES = 1, /* Examples/NSE_3D/AnsatzQuadLin.h, b = 0                     */
-  PMH_EXAMPLE_QUADLIN_OSEEN = 2   /* AnsatzQuadLin with b := exact u (Oseen linearisation)       */
+  PMH_EXAMPLE_QUADLIN_OSEEN = 2,  /* AnsatzQuadLin with b := exact u (Oseen linearisation)       */
+  PMH_EXAMPLE_CHANNEL = 3         /* channel: b = u0 = (1 - eta^2) e_x + seeded divergence-free
+                                     perturbation vanishing at the y walls, f = (2 nu (2/Ly)^2, 0, 0)
+                                     (holds the parabola in equilibrium), u = 0 on the y walls   */
 };
+
+enum { PMH_PERIODIC_X = 1, PMH_PERIODIC_Y = 2, PMH_PERIODIC_Z = 4 };
 
 typedef struct {
   int nx0, ny0, nz0;       /* cells per direction on the coarsest level          */
@@ -37,6 +42,11 @@ typedef struct {
   int example;             /* PMH_EXAMPLE_*                                        */
   int n_modes;             /* Fourier modes of b and f (8)                         */
   int nthreads;            /* OpenMP threads for assembly (0 = default)            */
+  int periodic;            /* PMH_PERIODIC_* bits: identified faces, no Dirichlet
+                              nodes there (at least 2 cells in such a direction)  */
+  double stretch_y;        /* > 0: y nodes at y0 + Ly (1 + tanh(s eta)/tanh(s)) / 2,
+                              eta uniform in [-1, 1] on every level; 0: uniform    */
+  double perturb;          /* channel: max |perturbation| at the finest nodes      */
 } pmh_params;
 
 typedef struct pmh_problem pmh_problem;

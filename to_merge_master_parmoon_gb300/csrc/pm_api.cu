@@ -91,6 +91,7 @@ struct LevelDev {
   double *asm_h = nullptr, *asm_conv = nullptr;
   double *asm_A = nullptr, *asm_M = nullptr;  // Oseen block and mass matrix (system assembly)
   bool asm_theta = false;  // asm_A / asm_M hold the last system assembly
+  int *coarse_nodes = nullptr;  // velocity DOF of this level at each node of level-1
 
   template <typename T>
   DevOp<T> op() const;
@@ -655,7 +656,7 @@ pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
         h->l_fallbacks++;
       }
       prev_res = resv;
-      if (j >= minit && (resv < resmin || resv < red * res0)) {
+      if (j >= minit && (resv < resmin || resv < red * (h->opt.red_initial ? r0 : res0))) {
         for (int k = 0; k <= i; ++k) y[k] = s[k];
         for (int r = i; r >= 0; --r) {
           y[r] /= hh(r, r);
@@ -976,6 +977,7 @@ void pm_default_options(pm_options *o) {
   o->residual_variant = 0;
   o->apply_variant = 0;
   o->upload_mode = 0;
+  o->red_initial = 0;
 }
 
 const char *pm_status_string(int s) {
@@ -1568,6 +1570,46 @@ pm_status pm_system_rhs_device(pm_handle *h, const double *d_old_rhs, const doub
   PM_LAUNCH(launch_system_rhs(asm_op(F), d_old_rhs, d_rhs, d_sol, c_old, c_new, c2, d_out,
                               h->stream));
   return sync(h, "system rhs");
+}
+
+// coarse DOF -> fine DOF: corner (fa, fb, fc) in {0, 2}^3 of the fine cell in
+// octant (ox, oy, oz) of its parent is the parent's local node
+// (ox + fa/2, oy + fb/2, oz + fc/2)
+static pm_status build_coarse_nodes(pm_handle *h, int level) {
+  LevelDev &F = h->L[level], &Cl = h->L[level - 1];
+  if (F.h_parent.empty() || F.h_child.empty())
+    return fail(h, PM_BADARG, "level without cell_parent / cell_child");
+  std::vector<int> map((size_t)Cl.nu, -1);
+  for (int f = 0; f < F.ncells; ++f) {
+    const int p = F.h_parent[f], o = F.h_child[f];
+    if (p < 0 || p >= Cl.ncells || o < 0 || o > 7) return fail(h, PM_BADARG, "bad cell_parent");
+    const int ox = o & 1, oy = (o >> 1) & 1, oz = (o >> 2) & 1;
+    for (int fc = 0; fc <= 2; fc += 2)
+      for (int fb = 0; fb <= 2; fb += 2)
+        for (int fa = 0; fa <= 2; fa += 2) {
+          const int cd = Cl.h_udofs[(size_t)p * NU_LOC + (ox + fa / 2) + 3 * (oy + fb / 2) +
+                                    9 * (oz + fc / 2)];
+          const int fd = F.h_udofs[(size_t)f * NU_LOC + fa + 3 * fb + 9 * fc];
+          if (cd < 0 || cd >= Cl.nu || fd < 0 || fd >= F.nu)
+            return fail(h, PM_BADARG, "cell DOF out of range");
+          if (map[cd] >= 0 && map[cd] != fd)
+            return fail(h, PM_BADARG, "coarse node with two fine DOFs: meshes not nested");
+          map[cd] = fd;
+        }
+  }
+  for (int v : map)
+    if (v < 0) return fail(h, PM_BADARG, "coarse node not covered by a child cell");
+  return upload(h, &F.coarse_nodes, map.data(), map.size());
+}
+
+pm_status pm_interpolate_coarse(pm_handle *h, int level, const double *d_fine, double *d_coarse) {
+  PM_CHECK_LEVEL(h, level);
+  if (level < 1 || !d_fine || !d_coarse) return PM_BADARG;
+  LevelDev &F = h->L[level];
+  if (!F.coarse_nodes) PM_TRY(build_coarse_nodes(h, level));
+  PM_LAUNCH(launch_interpolate_coarse(F.coarse_nodes, h->L[level - 1].nu, F.nu, d_fine, d_coarse,
+                                      h->stream));
+  return sync(h, "interpolate coarse");
 }
 
 pm_status pm_assemble_level(pm_handle *h, int level, const double *cell_h, const double *conv,

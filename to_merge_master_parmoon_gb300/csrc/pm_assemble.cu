@@ -285,6 +285,16 @@ __global__ void k_zero_pressure(double *p, int np) {
   if (k < np) p[k] = 0.0;
 }
 
+__global__ void k_interpolate_coarse(const int *__restrict__ map, int nc, int nf,
+                                     const double *__restrict__ fine,
+                                     double *__restrict__ coarse) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const int f = map[i];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) coarse[(size_t)c * nc + i] = fine[(size_t)c * nf + f];
+}
+
 inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 
 }  // namespace
@@ -336,6 +346,13 @@ int launch_assemble_level(const AsmOp &op, const DevCells &cells, const int *col
     ++n;
   }
   return n;
+}
+
+int launch_interpolate_coarse(const int *map, int nc, int nf, const double *fine, double *coarse,
+                              cudaStream_t s) {
+  if (nc <= 0) return 0;
+  k_interpolate_coarse<<<(nc + 255) / 256, 256, 0, s>>>(map, nc, nf, fine, coarse);
+  return ok() < 0 ? -1 : 1;
 }
 
 int launch_system_rhs(const AsmOp &op, const double *old_rhs, const double *rhs,

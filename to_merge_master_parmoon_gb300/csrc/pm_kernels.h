@@ -181,6 +181,9 @@ struct AsmOp {
 int launch_system_rhs(const AsmOp &op, const double *old_rhs, const double *rhs,
                       const double *sol, double c_old, double c_new, double c2, double *out,
                       cudaStream_t s);
+// coarse[c * nc + i] = fine[c * nf + map[i]] for the three velocity components
+int launch_interpolate_coarse(const int *map, int nc, int nf, const double *fine, double *coarse,
+                              cudaStream_t s);
 // reference tables into the current device's constant / global memory
 int assemble_tables_init();
 // Galerkin Oseen (and mass) blocks of one level (pm_assemble.cu): zero the values, then

@@ -16,6 +16,7 @@
 // whole colour in a separate launch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "pm_kernels.h"
@@ -960,6 +961,165 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense_lu(double *a, int N, in
   }
 }
 
+// Blocked right-looking LU with partial pivoting for larger coarse systems
+// (a coarsest level of several hundred to thousands of DOFs): per panel of
+// kLuNb columns, one CTA factors the panel (the same pivot rule as
+// k_dense_lu: first maximal |a|), one warp per other column applies the
+// panel's row interchanges and, right of the panel, the unit-lower
+// triangular solve with L11, and a tiled kernel updates the trailing matrix
+// A22 -= L21 U12 on all SMs.  The factors and ipiv have the same meaning as
+// k_dense_lu's (LAPACK dgetrf's sequential interchanges).
+constexpr int kLuNb = 32;
+
+__global__ void __launch_bounds__(kDenseThreads) k_lu_panel(double *a, int N, int k0, int *ipiv,
+                                                            int *status) {
+  __shared__ double bv[32];
+  __shared__ int bi[32];
+  __shared__ int piv_row;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = kDenseThreads / 32;
+  const int kend = min(k0 + kLuNb, N);
+  for (int k = k0; k < kend; ++k) {
+    double best = -1.0;
+    int bidx = k;
+    for (int i = k + tid; i < N; i += kDenseThreads) {
+      const double v = fabs(a[(size_t)k * N + i]);
+      if (v > best) {
+        best = v;
+        bidx = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(kFull, best, o);
+      const int oi = __shfl_xor_sync(kFull, bidx, o);
+      if (ob > best || (ob == best && oi < bidx)) {
+        best = ob;
+        bidx = oi;
+      }
+    }
+    if (lane == 0) {
+      bv[warp] = best;
+      bi[warp] = bidx;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      best = bv[lane];
+      bidx = bi[lane];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(kFull, best, o);
+        const int oi = __shfl_xor_sync(kFull, bidx, o);
+        if (ob > best || (ob == best && oi < bidx)) {
+          best = ob;
+          bidx = oi;
+        }
+      }
+      if (lane == 0) {
+        piv_row = bidx;
+        ipiv[k] = bidx;
+      }
+    }
+    __syncthreads();
+    const int p = piv_row;
+    if (p != k)
+      for (int j = k0 + tid; j < kend; j += kDenseThreads) {
+        const double t = a[(size_t)j * N + k];
+        a[(size_t)j * N + k] = a[(size_t)j * N + p];
+        a[(size_t)j * N + p] = t;
+      }
+    __syncthreads();
+    const double piv = a[(size_t)k * N + k];
+    if (piv == 0.0) {
+      if (tid == 0) atomicOr(status, 2);
+    } else {
+      const double rp = 1.0 / piv;
+      for (int i = k + 1 + tid; i < N; i += kDenseThreads) a[(size_t)k * N + i] *= rp;
+    }
+    __syncthreads();
+    for (int jj = k + 1 + warp; jj < kend; jj += nwarps) {
+      const double ukj = a[(size_t)jj * N + k];
+      if (ukj != 0.0)
+        for (int ii = k + 1 + lane; ii < N; ii += 32)
+          a[(size_t)jj * N + ii] -= a[(size_t)k * N + ii] * ukj;
+    }
+    __syncthreads();
+  }
+}
+
+// one warp per column outside the panel: the panel's interchanges, then
+// (right of the panel) U12 = L11^{-1} A12
+__global__ void k_lu_swap_trsm(double *a, int N, int k0, const int *ipiv) {
+  const int lane = threadIdx.x & 31;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int kend = min(k0 + kLuNb, N), m = kend - k0;
+  if (w >= N - m) return;  // whole warp
+  const int j = w < k0 ? (int)w : (int)w + m;
+  double *col = a + (size_t)j * N;
+  if (lane == 0)
+    for (int k = k0; k < kend; ++k) {
+      const int p = ipiv[k];
+      if (p != k) {
+        const double t = col[k];
+        col[k] = col[p];
+        col[p] = t;
+      }
+    }
+  __syncwarp();
+  if (j < k0) return;
+  double v = lane < m ? col[k0 + lane] : 0.0;
+  for (int k = 0; k < m; ++k) {
+    const double xk = __shfl_sync(kFull, v, k);
+    if (lane > k && lane < m) v -= a[(size_t)(k0 + k) * N + k0 + lane] * xk;
+  }
+  if (lane < m) col[k0 + lane] = v;
+}
+
+// A22 -= L21 U12: 64 x 64 tiles, 256 threads with 4 x 4 outputs each
+constexpr int kLuTile = 64;
+__global__ void __launch_bounds__(256) k_lu_gemm(double *a, int N, int k0) {
+  __shared__ double Ls[kLuNb][kLuTile + 1];  // [k][i]
+  __shared__ double Us[kLuNb][kLuTile + 1];  // [k][j]
+  const int kend = min(k0 + kLuNb, N), m = kend - k0;
+  const int i0 = kend + blockIdx.x * kLuTile, j0 = kend + blockIdx.y * kLuTile;
+  const int tid = threadIdx.x;
+  for (int t = tid; t < m * kLuTile; t += 256) {
+    const int k = t / kLuTile, i = t - kLuTile * k;
+    Ls[k][i] = (i0 + i < N) ? a[(size_t)(k0 + k) * N + i0 + i] : 0.0;
+  }
+  for (int t = tid; t < m * kLuTile; t += 256) {
+    const int jj = t / m, k = t - m * jj;
+    Us[k][jj] = (j0 + jj < N) ? a[(size_t)(j0 + jj) * N + k0 + k] : 0.0;
+  }
+  __syncthreads();
+  const int ti = tid & 15, tj = tid >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
+  for (int k = 0; k < m; ++k) {
+    double l[4], u[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) l[r] = Ls[k][ti + 16 * r];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) u[c] = Us[k][tj + 16 * c];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[r][c] += l[r] * u[c];
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int j = j0 + tj + 16 * c;
+    if (j >= N) continue;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int i = i0 + ti + 16 * r;
+      if (i < N) a[(size_t)j * N + i] -= acc[r][c];
+    }
+  }
+}
+
 constexpr int kDenseSolveThreads = 512;
 
 __global__ void __launch_bounds__(kDenseSolveThreads) k_dense_solve(const double *lu,
@@ -1138,8 +1298,28 @@ int launch_coarse_assemble(const DevOp<double> &op, double *dense, int project_p
 }
 
 int launch_dense_lu(double *a, int n, int *ipiv, int *status, cudaStream_t s) {
-  k_dense_lu<<<1, kDenseThreads, 0, s>>>(a, n, ipiv, status);
-  return ok() < 0 ? -1 : 1;
+  if (n <= 2 * kLuNb) {
+    k_dense_lu<<<1, kDenseThreads, 0, s>>>(a, n, ipiv, status);
+    return ok() < 0 ? -1 : 1;
+  }
+  int launches = 0;
+  for (int k0 = 0; k0 < n; k0 += kLuNb) {
+    const int m = std::min(kLuNb, n - k0), rest = n - k0 - m;
+    k_lu_panel<<<1, kDenseThreads, 0, s>>>(a, n, k0, ipiv, status);
+    ++launches;
+    if (n - m > 0) {
+      const long long threads = (long long)(n - m) * 32;
+      k_lu_swap_trsm<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a, n, k0, ipiv);
+      ++launches;
+    }
+    if (rest > 0) {
+      const unsigned t = (unsigned)((rest + kLuTile - 1) / kLuTile);
+      k_lu_gemm<<<dim3(t, t), 256, 0, s>>>(a, n, k0);
+      ++launches;
+    }
+    if (ok() < 0) return -1;
+  }
+  return launches;
 }
 
 int launch_dense_inverse(const double *lu, const int *ipiv, int n, double *inv, cudaStream_t s) {

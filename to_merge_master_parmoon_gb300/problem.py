@@ -13,7 +13,8 @@ import numpy as np
 
 from ._lib import PmhParams, PmLevelDesc, host_lib
 
-EXAMPLES = {"random": 0, "quadlin_stokes": 1, "quadlin_oseen": 2}
+EXAMPLES = {"random": 0, "quadlin_stokes": 1, "quadlin_oseen": 2, "channel": 3}
+PERIODIC = {"x": 1, "y": 2, "z": 4}
 
 
 class OseenProblem:
@@ -23,12 +24,18 @@ class OseenProblem:
     ``2**l`` times as many per direction.  ``example`` selects the seeded
     random Oseen problem (divergence-free Fourier convection, smooth forcing,
     u = 0 on the walls) or the known-answer polynomial solution of the
-    reference's Examples/NSE_3D/AnsatzQuadLin.h (Stokes, or Oseen with b := u).
+    reference's Examples/NSE_3D/AnsatzQuadLin.h (Stokes, or Oseen with b := u),
+    or the channel ("channel": b = u0 = parabola (1 - eta^2) e_x plus a seeded
+    divergence-free perturbation of size ``perturb`` vanishing at the y
+    walls, the body force that holds the parabola, u = 0 on the y walls).
+    ``periodic`` names identified directions ("xz"), ``stretch_y`` > 0 moves the
+    y nodes of every level to y0 + Ly (1 + tanh(s eta)/tanh(s))/2.
     """
 
     def __init__(self, n_levels: int = 4, nu: float = 1e-2, seed: int = 0,
                  example: str = "random", nx0: int = 2, ny0: int = 2, nz0: int = 2,
-                 box=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), n_modes: int = 8, nthreads: int = 0):
+                 box=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), n_modes: int = 8, nthreads: int = 0,
+                 periodic: str = "", stretch_y: float = 0.0, perturb: float = 0.05):
         lib = host_lib()
         p = PmhParams()
         lib.pmh_default_params(C.byref(p))
@@ -39,13 +46,17 @@ class OseenProblem:
         p.example = EXAMPLES[example]
         p.n_modes = n_modes
         p.nthreads = nthreads
+        p.periodic = sum(PERIODIC[c] for c in periodic)
+        p.stretch_y = stretch_y
+        p.perturb = perturb
         self._lib = lib
         self.params = p
         self.nu = nu
         self.example = example
         self._h = lib.pmh_build(C.byref(p))
         if not self._h:
-            raise ValueError("pmh_build rejected the parameters")
+            raise ValueError("pmh_build rejected the parameters (a periodic direction "
+                             "needs an even number >= 2 of coarsest cells)")
         self.n_levels = lib.pmh_n_levels(self._h)
         self._descs = (PmLevelDesc * self.n_levels)()
         for level in range(self.n_levels):

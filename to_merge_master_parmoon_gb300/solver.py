@@ -161,6 +161,13 @@ class PmSolver:
                                                    float(c2), C.c_void_p(d_out)),
                     "pm_system_rhs_device")
 
+    def interpolate_coarse(self, level, d_fine: int, d_coarse: int):
+        """pm_interpolate_coarse: velocity nodal values of `level` at the nodes
+        of level-1 (device addresses)."""
+        self._check(self._lib.pm_interpolate_coarse(self._h, level, C.c_void_p(d_fine),
+                                                    C.c_void_p(d_coarse)),
+                    "pm_interpolate_coarse")
+
     # ------------------------------------------------------------ level ops
     def coupled_defect(self, level, x, b, project=True):
         x, b = _f64(x), _f64(b)
