@@ -302,8 +302,10 @@ def channel_run(args, threads, net):
     on every level (pm_assemble_system_level_device), the refactorisation,
     the working right-hand side (pm_system_rhs_device) and the FGMRES solve
     from u.  NSTYPE-2 levels (the system keeps A11 = A22 = A33, A12..A32 = 0).
-    Variants: FP64, mixed, mixed + learned smoother; 2 untimed steps, then
-    args.channel_steps timed steps from the same initial state each."""
+    Variants: FP64, mixed, mixed + learned smoother, and mixed with the
+    divergence constraint scaled by dt (SCALE_DIVERGENCE_CONSTRAINT = 1); 2
+    untimed steps, then args.channel_steps timed steps from the same initial
+    state each."""
     import numpy as np
     import torch
     from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
@@ -325,8 +327,13 @@ def channel_run(args, threads, net):
     out = {"workload": "channel 64x64x32 (tanh 2.5 in y), periodic x/z, Q2/P1disc, nu=1/180, "
                        "CN dt=1e-3, one Oseen linearisation per step to 1e-8 reduction",
            "ndof": P.ndof(-1), "levels": L, "timed_steps": args.channel_steps}
-    for name, prec, learned in (("fp64", "fp64", False), ("mixed", "mixed", False),
-                                ("mixed_learned", "mixed", True)):
+    # B unscaled as with the reference's default SCALE_DIVERGENCE_CONSTRAINT = -1;
+    # the last variant sets it to 1 (B scaled by dt as well,
+    # src/System/SystemTNSE3D.C:1248-1264)
+    for name, prec, learned, b_scale in (("fp64", "fp64", False, 1.0),
+                                         ("mixed", "mixed", False, 1.0),
+                                         ("mixed_learned", "mixed", True, 1.0),
+                                         ("mixed_scaled_divergence", "mixed", False, tau)):
         kw = dict(precision=prec, restart=20, maxit=100, res_norm_min=1e-300, red_factor=1e-8,
                   red_initial=1)
         try:
@@ -347,7 +354,7 @@ def channel_run(args, threads, net):
                 conv[l - 1] = d_conv[l - 1]
             for l in range(L):
                 S.assemble_system_level_device(l, d_h[l].data_ptr(), conv[l].data_ptr(), P.nu,
-                                               1.0, tau * theta, 1.0, tau)
+                                               1.0, tau * theta, b_scale, tau)
             t1 = time.perf_counter()
             f_ms = S.refactor()
             t2 = time.perf_counter()
