@@ -173,6 +173,20 @@ typedef struct {
   /* optional cell colouring (no two cells of a colour share a DOF); NULL: the
    * library colours greedily, as TParFEMapper3D::colorCell does. */
   const int *cell_colour;
+  /* prolongation from the next coarser level (ignored on the coarsest):
+   * scalar CSR with fine rows and coarse columns, for the velocity (applied
+   * to each component) and the pressure; restriction is the transpose (as
+   * Prolongate / DefectRestriction are transposes in TNSE_MultiGrid).
+   * Required when n_ulocal != 27; NULL (nnz 0) for Q2 hexahedra builds them
+   * from the regular refinement (GetProlongationMatrix3D). */
+  int pu_nnz;
+  const int *pu_rowptr;  /* n_udof+1 */
+  const int *pu_col;
+  const double *pu_val;
+  int pp_nnz;
+  const int *pp_rowptr;  /* n_pdof+1 */
+  const int *pp_col;
+  const double *pp_val;
 } pm_level_desc;
 
 typedef struct {

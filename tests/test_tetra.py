@@ -1,0 +1,105 @@
+"""Tetrahedral P2+bubble/P1disc systems (ParMooN's C_B2_3D_T_A / D_P1_3D_T
+pair, 15 + 4 local DOFs, 49 x 49 Vanka blocks) on cubes split into 6 Kuhn
+tetrahedra.
+
+CPU: the builder's basis against the reference's own tables (golden fixture
+made from include/FE3D/BF_C_T_B2_3D.h and BF_D_T_P1_3D.h), the
+AnsatzQuadLin known answer (quadratic u, linear p lie in the discrete
+spaces) by a sparse direct solve, exactness of the handed-over prolongation
+on coarse-space functions, and the layout invariants (distinct cell DOFs, a
+valid colouring, sorted patterns)."""
+import ctypes as C
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spl
+
+GOLD = Path(__file__).parent / "golden" / "basis_tet_b2_p1.json"
+_cache = {}
+
+
+def tetra(n_levels=2, example="quadlin_oseen", nu=1.0, seed=0):
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    key = (n_levels, example, nu, seed)
+    if key not in _cache:
+        _cache[key] = OseenProblem(n_levels=n_levels, nu=nu, seed=seed, example=example,
+                                   element="tetra")
+    return _cache[key]
+
+
+def test_tet_basis_matches_reference_tables():
+    from to_merge_master_parmoon_gb300._lib import host_lib
+    g = json.loads(GOLD.read_text())
+    lib = host_lib()
+    v, d = (C.c_double * 15)(), (C.c_double * 45)()
+    pv, pd = (C.c_double * 4)(), (C.c_double * 12)()
+    for pt, ref in zip(g["points"], g["values"]):
+        lib.pmh_b2_basis(pt[0], pt[1], pt[2], v, d)
+        lib.pmh_p1t_basis(pt[0], pt[1], pt[2], pv, pd)
+        D, PD = np.array(d[:]).reshape(15, 3), np.array(pd[:]).reshape(4, 3)
+        np.testing.assert_allclose(v[:], ref["b2"], rtol=0, atol=1e-13)
+        for c, name in enumerate(("xi", "eta", "zeta")):
+            np.testing.assert_allclose(D[:, c], ref["b2_" + name], rtol=0, atol=1e-12)
+            np.testing.assert_allclose(PD[:, c], ref["p1_" + name], rtol=0, atol=1e-14)
+        np.testing.assert_allclose(pv[:], ref["p1"], rtol=0, atol=1e-14)
+
+
+def direct_solve(P, level, pin_value):
+    K = P.scipy_matrix(level).tolil()
+    b = P.rhs().copy()
+    r = 3 * P.desc(level).n_udof
+    K[r, :] = 0.0
+    K[r, r] = 1.0
+    b[r] = pin_value
+    return spl.splu(K.tocsc()).solve(b)
+
+
+@pytest.mark.parametrize("example,nu", [("quadlin_stokes", 1.0), ("quadlin_oseen", 1.0),
+                                        ("quadlin_oseen", 1e-2)])
+def test_tet_known_answer_direct(example, nu):
+    P = tetra(example=example, nu=nu)
+    ex = P.exact()
+    n3 = 3 * P.desc(1).n_udof
+    x = direct_solve(P, 1, ex[n3])
+    assert np.abs(x[:n3] - ex[:n3]).max() < 1e-9
+    assert np.abs(x[n3:] - ex[n3:]).max() < 1e-7
+
+
+def test_tet_prolongation_is_exact_on_coarse_functions():
+    P = tetra(n_levels=3)
+    for level in (1, 2):
+        a, c = P.arrays(level), P.desc(level - 1)
+        Pu = sp.csr_matrix((a["pu_val"], a["pu_col"], a["pu_rowptr"]),
+                           shape=(a["n_udof"], c.n_udof))
+        cf = P.convection_nodal(level - 1).reshape(3, -1)  # quadratic: in P2 on both levels
+        ff = P.convection_nodal(level).reshape(3, -1)
+        for k in range(3):
+            assert np.abs(Pu @ cf[k] - ff[k]).max() < 1e-12
+    # pressure: the P1disc coefficients of the linear exact pressure on level 1
+    # (finest level of the 2-level problem) map to those on level 2
+    a = P.arrays(2)
+    Pp = sp.csr_matrix((a["pp_val"], a["pp_col"], a["pp_rowptr"]),
+                       shape=(a["n_pdof"], P.desc(1).n_pdof))
+    e2, e3 = tetra(n_levels=2).exact(), P.exact()
+    p2, p3 = e2[3 * P.desc(1).n_udof:], e3[3 * P.desc(2).n_udof:]
+    assert np.abs(Pp @ p2 - p3).max() < 1e-12
+
+
+def test_tet_layout_invariants():
+    P = tetra(n_levels=2)
+    for level in range(P.n_levels):
+        a = P.arrays(level)
+        assert a["cell_udofs"].shape[1] == 15
+        assert all(len(set(c)) == 15 for c in a["cell_udofs"])
+        for colour in np.unique(a["cell_colour"]):
+            cells = a["cell_udofs"][a["cell_colour"] == colour]
+            assert len(np.unique(cells)) == cells.size  # no shared DOF in a colour
+        for r in range(a["n_active"]):
+            cols = a["a_col"][a["a_rowptr"][r]:a["a_rowptr"][r + 1]]
+            assert np.all(np.diff(cols) > 0)
+        # Dirichlet rows hold the diagonal only
+        for r in range(a["n_active"], a["n_udof"]):
+            assert list(a["a_col"][a["a_rowptr"][r]:a["a_rowptr"][r + 1]]) == [r]

@@ -26,6 +26,8 @@ class PmLevelDesc(C.Structure):
         ("n_cells", C.c_int), ("n_ulocal", C.c_int), ("n_plocal", C.c_int),
         ("cell_udofs", c_int_p), ("cell_pdofs", c_int_p),
         ("cell_parent", c_int_p), ("cell_child", c_int_p), ("cell_colour", c_int_p),
+        ("pu_nnz", C.c_int), ("pu_rowptr", c_int_p), ("pu_col", c_int_p), ("pu_val", c_double_p),
+        ("pp_nnz", C.c_int), ("pp_rowptr", c_int_p), ("pp_col", c_int_p), ("pp_val", c_double_p),
     ]
 
 
@@ -61,6 +63,7 @@ class PmhParams(C.Structure):
         ("z0", C.c_double), ("z1", C.c_double), ("nu", C.c_double), ("seed", C.c_uint64),
         ("example", C.c_int), ("n_modes", C.c_int), ("nthreads", C.c_int),
         ("periodic", C.c_int), ("stretch_y", C.c_double), ("perturb", C.c_double),
+        ("element", C.c_int),
     ]
 
 
@@ -141,6 +144,8 @@ HOST_SYMBOLS = {
     "pmh_rhs": (c_double_p, [C.c_void_p]),
     "pmh_exact": (c_double_p, [C.c_void_p]),
     "pmh_q2_basis": (None, [C.c_double, C.c_double, C.c_double, c_double_p, c_double_p]),
+    "pmh_b2_basis": (None, [C.c_double, C.c_double, C.c_double, c_double_p, c_double_p]),
+    "pmh_p1t_basis": (None, [C.c_double, C.c_double, C.c_double, c_double_p, c_double_p]),
     "pmh_max_convection": (C.c_double, [C.c_void_p]),
     "pmh_cell_sizes": (C.c_int, [C.c_void_p, C.c_int, c_double_p]),
     "pmh_convection_nodal": (C.c_int, [C.c_void_p, C.c_int, c_double_p]),

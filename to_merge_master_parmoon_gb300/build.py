@@ -32,9 +32,9 @@ GPU_CU = ["pm_api.cu", "pm_sparse.cu", "pm_vanka.cu", "pm_vanka_schur.cu", "pm_v
           "pm_learned.cu", "pm_mlp_tc.cu", "pm_assemble.cu",
           "pm_noalloc.cu"]
 GPU_CPP = ["pm_setup_host.cpp"]
-HOST_CPP = ["oseen_problem.cpp"]
+HOST_CPP = ["oseen_problem.cpp", "oseen_tet.cpp"]
 HEADERS = [INCLUDE / "pmgpu.h", CSRC / "pm_kernels.h", CSRC / "pm_setup_host.h",
-           CSRC / "oseen_problem.h", CSRC / "pm_learned.h"]
+           CSRC / "oseen_problem.h", CSRC / "oseen_internal.h", CSRC / "pm_learned.h"]
 
 
 def nvcc_path() -> str:

@@ -16,6 +16,7 @@
 //  * local forms: NSType4Galerkin3D (src/FE/NSE3D_FixPo.C:1919-2071) with
 //    4-point Gauss per direction (Gauss4Hexa, src/FE/FEDatabase3D.C:1015).
 #include "oseen_problem.h"
+#include "oseen_internal.h"
 
 #include <algorithm>
 #include <cmath>
@@ -47,11 +48,6 @@ struct SplitMix64 {
   }
 };
 
-struct Mode {
-  double k[3];
-  double a[3];
-  double phase;
-};
 
 // --------------------------------------------------------------- basis -----
 inline void lagrange2(double t, double *v, double *d) {
@@ -135,39 +131,9 @@ const RefTables &ref_tables() {
 }  // namespace
 
 // ------------------------------------------------------------ problem ------
-struct PMLevelData {
-  int nx, ny, nz;
-  int n_cells, n_udof, n_pdof, n_active;
-  std::vector<double> xs, ys, zs;     // cell boundaries
-  std::vector<int> grid2dof;          // Q2 node grid -> dof
-  std::vector<int> dof2grid;
-  std::vector<int> a_rowptr, a_col;
-  std::vector<double> a[9];
-  std::vector<int> b_rowptr, b_col;
-  std::vector<double> b[3];
-  std::vector<int> bt_rowptr, bt_col;
-  std::vector<double> bt[3];
-  std::vector<int> cell_udofs, cell_pdofs, cell_parent, cell_child, cell_colour;
-  int gx() const { return 2 * nx + 1; }
-  int gy() const { return 2 * ny + 1; }
-  int gz() const { return 2 * nz + 1; }
-  double node_x(int i) const { return (i & 1) ? 0.5 * (xs[i / 2] + xs[i / 2 + 1]) : xs[i / 2]; }
-  double node_y(int j) const { return (j & 1) ? 0.5 * (ys[j / 2] + ys[j / 2 + 1]) : ys[j / 2]; }
-  double node_z(int k) const { return (k & 1) ? 0.5 * (zs[k / 2] + zs[k / 2 + 1]) : zs[k / 2]; }
-};
+// PMLevelData and pmh_problem: oseen_internal.h
 
-struct pmh_problem {
-  pmh_params prm;
-  std::vector<PMLevelData> levels;
-  std::vector<double> rhs;
-  std::vector<double> exact;
-  bool has_exact = false;
-  std::vector<Mode> bmodes, fmodes;
-  double bscale = 1.0;
-  double bmax = 0.0;
-};
-
-namespace {
+namespace pmh_detail {
 
 // Exact solution of Examples/NSE_3D/AnsatzQuadLin.h:15-44.
 void quadlin_u(double x, double y, double z, double *u) {
@@ -192,7 +158,7 @@ void channel_perturbation(const pmh_problem &P, double x, double y, double z, do
   const double eta = (2.0 * y - q.y0 - q.y1) / Ly, e2 = 1.0 - eta * eta;
   const double w = e2 * e2, dw = -4.0 * eta * e2 * (2.0 / Ly);
   p[0] = p[1] = p[2] = 0.0;
-  for (const Mode &m : P.bmodes) {
+  for (const PmhMode &m : P.bmodes) {
     const double kx = 2.0 * M_PI * m.k[0] / Lx, ky = M_PI * m.k[1] / Ly,
                  kz = 2.0 * M_PI * m.k[2] / Lz;
     const double th = kx * (x - q.x0) + ky * (y - q.y0) + kz * (z - q.z0) + m.phase;
@@ -220,7 +186,7 @@ void convection(const pmh_problem &P, double x, double y, double z, double *b) {
     return;
   }
   // b = sum_m curl(a_m sin(2 pi k_m.x + phi_m)) = sum_m 2 pi cos(theta_m) (k_m x a_m)
-  for (const Mode &m : P.bmodes) {
+  for (const PmhMode &m : P.bmodes) {
     double th = 2.0 * M_PI * (m.k[0] * x + m.k[1] * y + m.k[2] * z) + m.phase;
     double c = 2.0 * M_PI * std::cos(th);
     b[0] += c * (m.k[1] * m.a[2] - m.k[2] * m.a[1]);
@@ -256,7 +222,7 @@ void forcing(const pmh_problem &P, double x, double y, double z, double *f) {
     return;
   }
   f[0] = f[1] = f[2] = 0.0;
-  for (const Mode &m : P.fmodes) {
+  for (const PmhMode &m : P.fmodes) {
     double s = std::sin(2.0 * M_PI * (m.k[0] * x + m.k[1] * y + m.k[2] * z) + m.phase);
     f[0] += m.a[0] * s;
     f[1] += m.a[1] * s;
@@ -272,6 +238,11 @@ bool boundary_value(const pmh_problem &P, double x, double y, double z, double *
   quadlin_u(x, y, z, u);
   return true;
 }
+
+}  // namespace pmh_detail
+
+namespace {
+using namespace pmh_detail;
 
 // per-dimension coupling lists of a Q2 node index i on a line of g = 2n + 1
 // grid nodes (the nodes of all cells that contain it); a periodic direction
@@ -582,10 +553,19 @@ void pmh_default_params(pmh_params *p) {
   p->periodic = 0;
   p->stretch_y = 0.0;
   p->perturb = 0.05;
+  p->element = PMH_ELEMENT_HEXA_Q2;
 }
 
 void pmh_q2_basis(double xi, double eta, double zeta, double *values, double *derivs) {
   q2_basis(xi, eta, zeta, values, derivs);
+}
+
+void pmh_b2_basis(double xi, double eta, double zeta, double *values, double *derivs) {
+  b2_basis(xi, eta, zeta, values, derivs);
+}
+
+void pmh_p1t_basis(double xi, double eta, double zeta, double *values, double *derivs) {
+  p1t_basis(xi, eta, zeta, values, derivs);
 }
 
 pmh_problem *pmh_build(const pmh_params *prm) {
@@ -597,6 +577,10 @@ pmh_problem *pmh_build(const pmh_params *prm) {
       ((prm->periodic & PMH_PERIODIC_Z) && (prm->nz0 < 2 || (prm->nz0 & 1))) ||
       prm->stretch_y < 0.0)
     return nullptr;
+  if (prm->element != PMH_ELEMENT_HEXA_Q2 &&
+      (prm->element != PMH_ELEMENT_TETRA_B2 || prm->periodic != 0 || prm->stretch_y != 0.0 ||
+       prm->example == PMH_EXAMPLE_CHANNEL))
+    return nullptr;
 #ifdef _OPENMP
   if (prm->nthreads > 0) omp_set_num_threads(prm->nthreads);
 #endif
@@ -604,14 +588,14 @@ pmh_problem *pmh_build(const pmh_params *prm) {
   P->prm = *prm;
   SplitMix64 rng(prm->seed);
   for (int m = 0; m < prm->n_modes; ++m) {
-    Mode md;
+    PmhMode md;
     for (int d = 0; d < 3; ++d) md.k[d] = 1.0 + std::floor(4.0 * rng.uniform());
     for (int d = 0; d < 3; ++d) md.a[d] = rng.normal();
     md.phase = 2.0 * M_PI * rng.uniform();
     P->bmodes.push_back(md);
   }
   for (int m = 0; m < prm->n_modes; ++m) {
-    Mode md;
+    PmhMode md;
     for (int d = 0; d < 3; ++d) md.k[d] = 1.0 + std::floor(4.0 * rng.uniform());
     for (int d = 0; d < 3; ++d) md.a[d] = rng.normal();
     md.phase = 2.0 * M_PI * rng.uniform();
@@ -637,7 +621,8 @@ pmh_problem *pmh_build(const pmh_params *prm) {
       }
     }
     for (int i = 0; i <= L.nz; ++i) L.zs[i] = prm->z0 + (prm->z1 - prm->z0) * i / L.nz;
-    build_level_structure(L, prm->periodic);
+    if (prm->element == PMH_ELEMENT_HEXA_Q2) build_level_structure(L, prm->periodic);
+    if (prm->element != PMH_ELEMENT_HEXA_Q2) continue;
     L.cell_parent.assign(L.n_cells, -1);
     L.cell_child.assign(L.n_cells, -1);
     if (l > 0) {
@@ -650,6 +635,52 @@ pmh_problem *pmh_build(const pmh_params *prm) {
             L.cell_child[c] = (cx & 1) + 2 * (cy & 1) + 4 * (cz & 1);
           }
     }
+  }
+  if (prm->element == PMH_ELEMENT_TETRA_B2) {
+    build_tet_levels(*P);
+    // normalise b: max |b| = 1 over the finest grid nodes (the P2 nodes)
+    if (prm->example == PMH_EXAMPLE_RANDOM_OSEEN) {
+      const PMLevelData &F = P->levels.back();
+      double bmax = 0.0;
+      P->bscale = 1.0;
+      const int gx = F.gx(), gy = F.gy(), gz = F.gz();
+#pragma omp parallel for reduction(max : bmax) schedule(static)
+      for (int g = 0; g < gx * gy * gz; ++g) {
+        const int i = g % gx, j = (g / gx) % gy, k = g / (gx * gy);
+        double b[3];
+        convection(*P, F.node_x(i), F.node_y(j), F.node_z(k), b);
+        bmax = std::max(bmax, std::sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]));
+      }
+      P->bscale = bmax > 0 ? 1.0 / bmax : 1.0;
+      P->bmax = 1.0;
+    }
+    for (int l = 0; l < prm->n_levels; ++l)
+      assemble_tet_level(*P, P->levels[l], l == prm->n_levels - 1);
+    if (prm->example == PMH_EXAMPLE_QUADLIN_STOKES || prm->example == PMH_EXAMPLE_QUADLIN_OSEEN) {
+      const PMLevelData &F = P->levels.back();
+      P->has_exact = true;
+      P->exact.assign((size_t)3 * F.n_udof + F.n_pdof, 0.0);
+      for (int r = 0; r < F.n_udof; ++r) {
+        double u[3];
+        quadlin_u(F.node_xyz[3 * r], F.node_xyz[3 * r + 1], F.node_xyz[3 * r + 2], u);
+        for (int d = 0; d < 3; ++d) P->exact[(size_t)d * F.n_udof + r] = u[d];
+      }
+      // P1disc coefficients: p at the 4 vertices = sum_m c_m psi_m(vertex)
+      for (int t = 0; t < F.n_cells; ++t) {
+        const double *x = &F.tet_xyz[(size_t)t * 12];
+        double pv[4];
+        for (int i = 0; i < 4; ++i) pv[i] = quadlin_p(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+        // psi at the reference vertices: (6, -1, -1, -1), (6, 1, 0, 0), (6, 0, 1, 0),
+        // (6, 0, 0, 1), so p_k - p_0 = c_k + s (k = 1..3) with s = c_1 + c_2 + c_3
+        double *c = &P->exact[(size_t)3 * F.n_udof + 4 * t];
+        const double s4 = (pv[1] + pv[2] + pv[3] - 3.0 * pv[0]) / 4.0;
+        c[1] = pv[1] - pv[0] - s4;
+        c[2] = pv[2] - pv[0] - s4;
+        c[3] = pv[3] - pv[0] - s4;
+        c[0] = (pv[1] - c[1]) / 6.0;
+      }
+    }
+    return P;
   }
   // normalise b: max over the finest level's Q2 nodes of |b| = 1
   if (prm->example == PMH_EXAMPLE_RANDOM_OSEEN) {
@@ -730,6 +761,7 @@ double pmh_max_convection(const pmh_problem *p) { return p ? p->bmax : 0.0; }
 int pmh_cell_sizes(const pmh_problem *p, int level, double *out) {
   if (!p || level < 0 || level >= (int)p->levels.size() || !out) return -1;
   const PMLevelData &L = p->levels[level];
+  if (L.nu_loc != 27) return -1;  // boxes only
   for (int c = 0; c < L.n_cells; ++c) {
     const int cx = c % L.nx, cy = (c / L.nx) % L.ny, cz = c / (L.nx * L.ny);
     out[3 * c] = L.xs[cx + 1] - L.xs[cx];
@@ -742,6 +774,14 @@ int pmh_cell_sizes(const pmh_problem *p, int level, double *out) {
 int pmh_convection_nodal(const pmh_problem *p, int level, double *out) {
   if (!p || level < 0 || level >= (int)p->levels.size() || !out) return -1;
   const PMLevelData &L = p->levels[level];
+  if (!L.node_xyz.empty()) {
+    for (int r = 0; r < L.n_udof; ++r) {
+      double b[3];
+      convection(*p, L.node_xyz[3 * r], L.node_xyz[3 * r + 1], L.node_xyz[3 * r + 2], b);
+      for (int d = 0; d < 3; ++d) out[(size_t)d * L.n_udof + r] = b[d];
+    }
+    return 0;
+  }
   const int gx = L.gx(), gy = L.gy();
   for (int r = 0; r < L.n_udof; ++r) {
     const int g = L.dof2grid[r];
@@ -761,7 +801,10 @@ int pmh_reassemble(pmh_problem *p) {
     for (auto &v : L.a) std::fill(v.begin(), v.end(), 0.0);
     for (auto &v : L.b) std::fill(v.begin(), v.end(), 0.0);
     for (auto &v : L.bt) std::fill(v.begin(), v.end(), 0.0);
-    assemble_level(*p, L, l == n - 1);
+    if (p->prm.element == PMH_ELEMENT_TETRA_B2)
+      assemble_tet_level(*p, L, l == n - 1);
+    else
+      assemble_level(*p, L, l == n - 1);
   }
   return 0;
 }
@@ -788,13 +831,23 @@ int pmh_level_desc(const pmh_problem *p, int level, pm_level_desc *o) {
   o->bt_col = L.bt_col.data();
   for (int b = 0; b < 3; ++b) o->bt[b] = L.bt[b].data();
   o->n_cells = L.n_cells;
-  o->n_ulocal = 27;
+  o->n_ulocal = L.nu_loc;
   o->n_plocal = 4;
   o->cell_udofs = L.cell_udofs.data();
   o->cell_pdofs = L.cell_pdofs.data();
   o->cell_parent = level > 0 ? L.cell_parent.data() : nullptr;
-  o->cell_child = level > 0 ? L.cell_child.data() : nullptr;
+  o->cell_child = level > 0 && L.nu_loc == 27 ? L.cell_child.data() : nullptr;
   o->cell_colour = L.cell_colour.data();
+  if (level > 0 && !L.pu_rowptr.empty()) {
+    o->pu_nnz = (int)L.pu_col.size();
+    o->pu_rowptr = L.pu_rowptr.data();
+    o->pu_col = L.pu_col.data();
+    o->pu_val = L.pu_val.data();
+    o->pp_nnz = (int)L.pp_col.size();
+    o->pp_rowptr = L.pp_rowptr.data();
+    o->pp_col = L.pp_col.data();
+    o->pp_val = L.pp_val.data();
+  }
   return 0;
 }
 

@@ -47,7 +47,15 @@ typedef struct {
   double stretch_y;        /* > 0: y nodes at y0 + Ly (1 + tanh(s eta)/tanh(s)) / 2,
                               eta uniform in [-1, 1] on every level; 0: uniform    */
   double perturb;          /* channel: max |perturbation| at the finest nodes      */
+  int element;             /* PMH_ELEMENT_*                                        */
 } pmh_params;
+
+enum {
+  PMH_ELEMENT_HEXA_Q2 = 0, /* hexahedra, Q2 / P1disc (27 + 4 local DOFs)                   */
+  PMH_ELEMENT_TETRA_B2 = 1 /* each cube split into 6 Kuhn tetrahedra, P2 + 4 face + 1 cell
+                              bubble / P1disc (15 + 4 local DOFs, C_B2_3D_T_A / D_P1_3D_T);
+                              no periodic directions, uniform grid                          */
+};
 
 typedef struct pmh_problem pmh_problem;
 
@@ -67,6 +75,12 @@ const double *pmh_exact(const pmh_problem *p);
 /* Q2 reference basis at (xi,eta,zeta): 27 values, and 81 derivatives
  * (d/dxi, d/deta, d/dzeta per function). */
 void pmh_q2_basis(double xi, double eta, double zeta, double *values, double *derivs);
+/* P2 + 4 face + 1 cell bubble basis on the reference tetrahedron
+ * (0,0,0), (1,0,0), (0,1,0), (0,0,1): 15 values and 45 derivatives (the
+ * local order of C_T_B2_3D_Funct, include/FE3D/BF_C_T_B2_3D.h); the P1disc
+ * basis there: 4 values, 12 derivatives. */
+void pmh_b2_basis(double xi, double eta, double zeta, double *values, double *derivs);
+void pmh_p1t_basis(double xi, double eta, double zeta, double *values, double *derivs);
 double pmh_max_convection(const pmh_problem *p);
 /* (hx, hy, hz) of every cell of a level (n_cells x 3); 0 or -1 */
 int pmh_cell_sizes(const pmh_problem *p, int level, double *out);

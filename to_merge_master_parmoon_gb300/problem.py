@@ -15,6 +15,7 @@ from ._lib import PmhParams, PmLevelDesc, host_lib
 
 EXAMPLES = {"random": 0, "quadlin_stokes": 1, "quadlin_oseen": 2, "channel": 3}
 PERIODIC = {"x": 1, "y": 2, "z": 4}
+ELEMENTS = {"hexa": 0, "tetra": 1}
 
 
 class OseenProblem:
@@ -30,12 +31,16 @@ class OseenProblem:
     walls, the body force that holds the parabola, u = 0 on the y walls).
     ``periodic`` names identified directions ("xz"), ``stretch_y`` > 0 moves the
     y nodes of every level to y0 + Ly (1 + tanh(s eta)/tanh(s))/2.
+    ``element="tetra"`` splits every cube into 6 Kuhn tetrahedra with P2 + face
+    and cell bubbles / P1disc (15 + 4 local DOFs) and hands the prolongation
+    over in the level descriptors (uniform grids, no periodic directions).
     """
 
     def __init__(self, n_levels: int = 4, nu: float = 1e-2, seed: int = 0,
                  example: str = "random", nx0: int = 2, ny0: int = 2, nz0: int = 2,
                  box=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), n_modes: int = 8, nthreads: int = 0,
-                 periodic: str = "", stretch_y: float = 0.0, perturb: float = 0.05):
+                 periodic: str = "", stretch_y: float = 0.0, perturb: float = 0.05,
+                 element: str = "hexa"):
         lib = host_lib()
         p = PmhParams()
         lib.pmh_default_params(C.byref(p))
@@ -49,10 +54,12 @@ class OseenProblem:
         p.periodic = sum(PERIODIC[c] for c in periodic)
         p.stretch_y = stretch_y
         p.perturb = perturb
+        p.element = ELEMENTS[element]
         self._lib = lib
         self.params = p
         self.nu = nu
         self.example = example
+        self.element = element
         self._h = lib.pmh_build(C.byref(p))
         if not self._h:
             raise ValueError("pmh_build rejected the parameters (a periodic direction "
@@ -160,13 +167,21 @@ class OseenProblem:
             "b": [dv(d.b[k], d.b_nnz) for k in range(3)],
             "bt_rowptr": iv(d.bt_rowptr, d.n_udof + 1), "bt_col": iv(d.bt_col, d.bt_nnz),
             "bt": [dv(d.bt[k], d.bt_nnz) for k in range(3)],
-            "cell_udofs": iv(d.cell_udofs, 27 * d.n_cells).reshape(d.n_cells, 27),
+            "cell_udofs": iv(d.cell_udofs, d.n_ulocal * d.n_cells).reshape(d.n_cells, d.n_ulocal),
             "cell_pdofs": iv(d.cell_pdofs, 4 * d.n_cells).reshape(d.n_cells, 4),
             "cell_colour": iv(d.cell_colour, d.n_cells),
         }
         if d.cell_parent:
             out["cell_parent"] = iv(d.cell_parent, d.n_cells)
+        if d.cell_child:
             out["cell_child"] = iv(d.cell_child, d.n_cells)
+        if d.pu_rowptr:
+            out["pu_rowptr"] = iv(d.pu_rowptr, d.n_udof + 1)
+            out["pu_col"] = iv(d.pu_col, d.pu_nnz)
+            out["pu_val"] = dv(d.pu_val, d.pu_nnz)
+            out["pp_rowptr"] = iv(d.pp_rowptr, d.n_pdof + 1)
+            out["pp_col"] = iv(d.pp_col, d.pp_nnz)
+            out["pp_val"] = dv(d.pp_val, d.pp_nnz)
         return out
 
     def scipy_matrix(self, level: int = -1):
