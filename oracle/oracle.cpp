@@ -15,13 +15,14 @@
 
 namespace {
 
-const int NU_LOC = 27;  // Q2 local DOFs
+const int NU_LOC = 27;  // Q2 local DOFs (hexahedral transfer tables)
 const int NP_LOC = 4;   // P1disc local DOFs
-const int NLOC = 3 * NU_LOC + NP_LOC;  // 85
+const int NLOC_MAX = 3 * NU_LOC + NP_LOC;  // 85: the largest local block
 
 struct OLevel {
   pm_level_desc d;
   int nu = 0, np = 0, ndof = 0;
+  int nl = 27, nloc = 85;  // velocity nodes per cell, local block size (27/85 or 15/49)
   std::vector<double> sol, rhs, aux0, aux1;
   // children[parent*8 + childnumber] = fine cell (stored on the fine level)
   std::vector<int> children;
@@ -319,7 +320,7 @@ void correct_defect(const oracle *o, const OLevel &L, double *v) {
 void local_system(const OLevel &L, int cell, const double *u, const double *rhs, double *System,
                   double *Rhs) {
   const pm_level_desc &d = L.d;
-  const int nu = L.nu, N = NLOC, active = d.n_active;
+  const int nu = L.nu, N = L.nloc, active = d.n_active, NU_LOC = L.nl;
   const double *u1 = u, *u2 = u + nu, *u3 = u + 2 * nu, *p = u + 3 * nu;
   const int *UDOFs = d.cell_udofs + (size_t)cell * NU_LOC;
   const int *PDOFs = d.cell_pdofs + (size_t)cell * NP_LOC;
@@ -394,7 +395,7 @@ void local_system(const OLevel &L, int cell, const double *u, const double *rhs,
 }
 
 void add_local(const OLevel &L, int cell, double *u, const double *sol, double damp) {
-  const int nu = L.nu;
+  const int nu = L.nu, NU_LOC = L.nl;
   const int *UDOFs = L.d.cell_udofs + (size_t)cell * NU_LOC;
   const int *PDOFs = L.d.cell_pdofs + (size_t)cell * NP_LOC;
   for (int j = 0; j < NU_LOC; ++j) {
@@ -407,6 +408,7 @@ void add_local(const OLevel &L, int cell, double *u, const double *sol, double d
 }
 
 void solve_local(oracle *o, OLevel &L, int cell, double *System, double *Rhs) {
+  const int NLOC = L.nloc;
   if (o->p.reuse_factors) {
     if (L.fac.empty()) {
       L.fac.assign(L.d.n_cells, {});
@@ -420,7 +422,7 @@ void solve_local(oracle *o, OLevel &L, int cell, double *System, double *Rhs) {
     lu_solve(L.fac[cell].data(), NLOC, L.piv[cell].data(), Rhs);
     return;
   }
-  int ipiv[NLOC];
+  int ipiv[NLOC_MAX];
   lu_factor(System, NLOC, ipiv);  // SolveLinearSystemLapack, src/FE/LinAlg.C:106-131
   lu_solve(System, NLOC, ipiv, Rhs);
 }
@@ -428,6 +430,7 @@ void solve_local(oracle *o, OLevel &L, int cell, double *System, double *Rhs) {
 // TNSE_MGLevel4::CellVanka (src/FE/NSE_MGLevel4.C:1653-2087): one sweep.
 void cell_vanka(oracle *o, OLevel &L, double *u, const double *rhs) {
   const double damp = o->p.smooth_damp;
+  const int NLOC = L.nloc;
   const int ncell = L.d.n_cells;
   set_dirichlet(L, u, rhs);
   std::vector<double> uold(u, u + L.ndof);
@@ -470,6 +473,22 @@ void cell_vanka(oracle *o, OLevel &L, double *u, const double *rhs) {
 // Prolongate (vector src/FE/MGComponents3D.C:468-708, scalar :184-467)
 void prolongate(const oracle *o, const OLevel &C, const OLevel &F, const double *coarse,
                 double *fine) {
+  if (F.d.pu_rowptr) {  // handed-over prolongation (non-hexahedral cells)
+    for (int comp = 0; comp < 3; ++comp)
+      for (int i = 0; i < F.nu; ++i) {
+        double s = 0.0;
+        for (int e = F.d.pu_rowptr[i]; e < F.d.pu_rowptr[i + 1]; ++e)
+          s += F.d.pu_val[e] * coarse[comp * C.nu + F.d.pu_col[e]];
+        fine[comp * F.nu + i] = s;
+      }
+    for (int i = 0; i < F.np; ++i) {
+      double s = 0.0;
+      for (int e = F.d.pp_rowptr[i]; e < F.d.pp_rowptr[i + 1]; ++e)
+        s += F.d.pp_val[e] * coarse[3 * C.nu + F.d.pp_col[e]];
+      fine[3 * F.nu + i] = s;
+    }
+    return;
+  }
   std::vector<double> aux(F.nu, 0.0);
   std::memset(fine, 0, sizeof(double) * F.ndof);
   const int ncc = C.d.n_cells;
@@ -520,8 +539,18 @@ void prolongate(const oracle *o, const OLevel &C, const OLevel &F, const double 
 // DefectRestriction (vector src/FE/MGComponents3D.C:996-1242, scalar :711-995)
 void defect_restriction(const oracle *o, const OLevel &C, const OLevel &F, double *coarse,
                         const double *fine_in) {
-  std::vector<double> fine(fine_in, fine_in + F.ndof);
   std::memset(coarse, 0, sizeof(double) * C.ndof);
+  if (F.d.pu_rowptr) {  // the transpose of the handed-over prolongation
+    for (int comp = 0; comp < 3; ++comp)
+      for (int i = 0; i < F.nu; ++i)
+        for (int e = F.d.pu_rowptr[i]; e < F.d.pu_rowptr[i + 1]; ++e)
+          coarse[comp * C.nu + F.d.pu_col[e]] += F.d.pu_val[e] * fine_in[comp * F.nu + i];
+    for (int i = 0; i < F.np; ++i)
+      for (int e = F.d.pp_rowptr[i]; e < F.d.pp_rowptr[i + 1]; ++e)
+        coarse[3 * C.nu + F.d.pp_col[e]] += F.d.pp_val[e] * fine_in[3 * F.nu + i];
+    return;
+  }
+  std::vector<double> fine(fine_in, fine_in + F.ndof);
   std::vector<double> aux(F.nu, 0.0), auxp(F.np, 0.0);
   for (int c = 0; c < F.d.n_cells; ++c) {
     for (int j = 0; j < NU_LOC; ++j) aux[F.d.cell_udofs[(size_t)c * NU_LOC + j]] += 1;
@@ -709,11 +738,13 @@ oracle *oracle_create(const pm_level_desc *levels, int n_levels, const oracle_pa
     L.nu = L.d.n_udof;
     L.np = L.d.n_pdof;
     L.ndof = 3 * L.nu + L.np;
+    L.nl = L.d.n_ulocal > 0 ? L.d.n_ulocal : NU_LOC;
+    L.nloc = 3 * L.nl + NP_LOC;
     L.sol.assign(L.ndof, 0.0);
     L.rhs.assign(L.ndof, 0.0);
     L.aux0.assign(L.ndof, 0.0);
     L.aux1.assign(L.ndof, 0.0);
-    if (l > 0) {
+    if (l > 0 && L.d.cell_child && !L.d.pu_rowptr) {
       L.children.assign((size_t)levels[l - 1].n_cells * 8, -1);
       for (int c = 0; c < L.d.n_cells; ++c)
         L.children[(size_t)L.d.cell_parent[c] * 8 + L.d.cell_child[c]] = c;
@@ -766,7 +797,7 @@ void oracle_lu_solve(double *a, double *b, int n) {
 int oracle_local_system(oracle *o, int level, int cell, const double *u, const double *rhs,
                         double *system, double *local_rhs) {
   local_system(o->L[level], cell, u, rhs, system, local_rhs);
-  return NLOC;
+  return o->L[level].nloc;
 }
 
 // TFgmresIte::Iterate, flexible branch (src/FE/FgmresIte.C:250-677)

@@ -63,7 +63,8 @@ int  oracle_fgmres(oracle *o, double *sol, const double *rhs, double *out);
 /* Dense LU with partial pivoting of an n x n column-major matrix and solve
  * (dgetrf + dgetrs semantics), exposed for the local-solve pin. */
 void oracle_lu_solve(double *a, double *b, int n);
-/* Local 85x85 Vanka system of one cell (column-major) and its local rhs. */
+/* Local Vanka system of one cell (column-major, 85x85 for Q2, 49x49 for
+ * P2+bubble tetrahedra) and its local rhs; returns the size. */
 int  oracle_local_system(oracle *o, int level, int cell, const double *u, const double *rhs,
                          double *system, double *local_rhs);
 

@@ -151,10 +151,11 @@ class Oracle:
 
     def local_system(self, level, cell, u, rhs):
         u, rhs = _f(u), _f(rhs)
-        S = np.zeros(85 * 85)
-        R = np.zeros(85)
+        n = 3 * self.problem.desc(level).n_ulocal + 4  # 85 (Q2) or 49 (P2+bubble)
+        S = np.zeros(n * n)
+        R = np.zeros(n)
         self._L.oracle_local_system(self._h, level, cell, _p(u), _p(rhs), _p(S), _p(R))
-        return S.reshape(85, 85).T.copy(), R  # row-major A[row, col]
+        return S.reshape(n, n).T.copy(), R  # row-major A[row, col]
 
 
 def lu_solve(a: np.ndarray, b: np.ndarray) -> np.ndarray:

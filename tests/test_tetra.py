@@ -103,3 +103,18 @@ def test_tet_layout_invariants():
         # Dirichlet rows hold the diagonal only
         for r in range(a["n_active"], a["n_udof"]):
             assert list(a["a_col"][a["a_rowptr"][r]:a["a_rowptr"][r + 1]]) == [r]
+
+
+@pytest.mark.parametrize("example,nu", [("quadlin_oseen", 1.0), ("random", 1e-2)])
+def test_oracle_fgmres_on_tetrahedra(example, nu):
+    """The oracle's FGMRES + V(2,2) with 49 x 49 cell Vanka (colour order) and
+    the handed-over transfers converges and agrees with a direct solve."""
+    from oracle.pyoracle import Oracle
+    P = tetra(n_levels=2, example=example, nu=nu)
+    b = P.rhs()
+    r0 = np.linalg.norm(Oracle(P).coupled_defect(1, np.zeros_like(b), b))
+    x, info = Oracle(P, restart=20, maxit=60, res_norm_min=1e-11 * r0).iterate(np.zeros_like(b), b)
+    assert info["true_res"] <= 1.05e-11 * r0 and info["iterations"] <= 30
+    n3 = 3 * P.desc(1).n_udof
+    xd = direct_solve(P, 1, x[n3])
+    assert np.linalg.norm(x - xd) <= 1e-8 * np.linalg.norm(xd)
