@@ -7,7 +7,11 @@ made from include/FE3D/BF_C_T_B2_3D.h and BF_D_T_P1_3D.h), the
 AnsatzQuadLin known answer (quadratic u, linear p lie in the discrete
 spaces) by a sparse direct solve, exactness of the handed-over prolongation
 on coarse-space functions, and the layout invariants (distinct cell DOFs, a
-valid colouring, sorted patterns)."""
+valid colouring, sorted patterns), and the oracle's FGMRES + GMG.
+GPU: defects, mat-vecs, transfers, coarse solve, Vanka sweeps and V-cycles
+against the oracle (FP64 1e-9, mixed 5e-4), FGMRES to 1e-10 with the
+solution within 1e-6 and, in FP64, the same iteration count; the known
+answer on the GPU; hexahedra-only features refuse tetrahedral levels."""
 import ctypes as C
 import json
 from pathlib import Path
@@ -118,3 +122,100 @@ def test_oracle_fgmres_on_tetrahedra(example, nu):
     n3 = 3 * P.desc(1).n_udof
     xd = direct_solve(P, 1, x[n3])
     assert np.linalg.norm(x - xd) <= 1e-8 * np.linalg.norm(xd)
+
+
+# ------------------------------------------------------------------ GPU ----
+# Every operator of the path through the C ABI on tetrahedral levels against
+# the oracle (same tolerances as the hexahedral parity tests), nine-block and
+# one-block descriptors, both precisions.
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def rnd(P, level, seed):
+    return np.random.default_rng(seed).standard_normal(P.ndof(level))
+
+
+def tet_solvers(one_block):
+    from oracle.pyoracle import Oracle
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P = tetra(n_levels=3, example="random", nu=1e-2)
+    descs = P.descs_one_block() if one_block else P.descs
+    return P, PmSolver(descs, precision="fp64"), PmSolver(descs, precision="mixed"), Oracle(P)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("one_block", [False, True])
+def test_tet_gpu_operators_match_oracle(one_block):
+    P, g64, g32, O = tet_solvers(one_block)
+    for level in range(3):
+        x, b = rnd(P, level, 1), rnd(P, level, 2)
+        assert rel(g64.coupled_defect(level, x, b, True), O.coupled_defect(level, x, b, True)) < 1e-12
+        assert rel(g64.matvec(level, x), O.matvec(level, x)) < 1e-12
+    for level in (1, 2):
+        xf, xc = rnd(P, level, 3), rnd(P, level - 1, 4)
+        assert rel(g64.restrict(level, xf), O.restrict(level, xf)) < 1e-13
+        assert rel(g64.prolongate(level, xc), O.prolongate(level, xc)) < 1e-13
+        u, f = 0.1 * rnd(P, level, 6), rnd(P, level, 7)
+        assert rel(g64.cell_vanka(level, u, f, 2), O.cell_vanka(level, u, f, 2)) < 1e-9
+        assert rel(g32.cell_vanka(level, u, f, 2), O.cell_vanka(level, u, f, 2)) < 5e-4
+    b0 = rnd(P, 0, 5)
+    assert rel(g64.solve_exact(b0), O.solve_exact(b0)) < 1e-10
+    v = rnd(P, 2, 8)
+    z = O.vcycle(v)
+    assert rel(g64.vcycle(v), z) < 1e-9
+    assert rel(g32.vcycle(v), z) < 5e-4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("apply_variant", [0, 2])
+def test_tet_gpu_fgmres_matches_oracle(precision, apply_variant):
+    from oracle.pyoracle import Oracle
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P = tetra(n_levels=3, example="random", nu=1e-2)
+    b = P.rhs()
+    x0 = np.zeros_like(b)
+    O = Oracle(P)
+    r0 = np.linalg.norm(O.coupled_defect(2, x0, b))
+    tol = 1e-10 * r0
+    xo, io = Oracle(P, restart=20, maxit=60, res_norm_min=tol).iterate(x0, b)
+    S = PmSolver(P.descs, precision=precision, restart=20, maxit=60, res_norm_min=tol,
+                 apply_variant=apply_variant)
+    xg, ig = S.iterate(x0, b)
+    n = P.desc(2).n_udof
+    pg, po = xg.copy(), xo.copy()
+    pg[3 * n::4] -= pg[3 * n::4].mean()
+    po[3 * n::4] -= po[3 * n::4].mean()
+    assert ig["true_res"] <= 1.05 * tol
+    assert rel(pg, po) < 1e-6
+    if precision == "fp64":
+        assert ig["iterations"] == io["iterations"]
+
+
+@pytest.mark.gpu
+def test_tet_known_answer_on_gpu():
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P = tetra(n_levels=3, example="quadlin_oseen", nu=1.0)
+    b, ex = P.rhs(), P.exact()
+    r0 = np.linalg.norm(PmSolver(P.descs).coupled_defect(2, np.zeros_like(b), b))
+    n3 = 3 * P.desc(2).n_udof
+    for precision in ("fp64", "mixed"):
+        S = PmSolver(P.descs, precision=precision, restart=20, maxit=60, res_norm_min=1e-12 * r0)
+        x, info = S.iterate(np.zeros_like(b), b)
+        assert np.abs(x[:n3] - ex[:n3]).max() < 1e-8
+        dp = x[n3:] - ex[n3:]
+        dp[0::4] -= dp[0::4].mean()
+        assert np.abs(dp).max() < 1e-6
+
+
+@pytest.mark.gpu
+def test_tet_hexahedral_only_features_refuse():
+    from to_merge_master_parmoon_gb300 import PmError, PmSolver
+    P = tetra(n_levels=2, example="random", nu=1e-2)
+    with pytest.raises(PmError):
+        PmSolver(P.descs, precision="mixed", vanka_inverse=1)
+    S = PmSolver(P.descs, precision="fp64")
+    with pytest.raises(PmError):
+        S.assemble_level(1, np.ones((P.desc(1).n_cells, 3)), np.zeros(3 * P.desc(1).n_udof), 1.0)

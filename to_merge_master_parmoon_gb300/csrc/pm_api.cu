@@ -65,6 +65,8 @@ struct LevelDev {
   int res_variant = 0;    // local-residual kernel of the sweep (0 row groups, 1 stream)
   int apply_variant = 0;  // LU apply: 0 two cells per warp, 1 bulk-staged (FP32), 2 one cell per warp
   std::vector<int> h_udofs, h_pdofs, h_parent, h_child, h_colour;
+  int nl = NU_LOC;                // velocity nodes per cell (27 Q2, 15 P2+bubble tetrahedra)
+  HostCsr h_pu, h_pp;             // handed-over prolongation from the next coarser level
   bool has_colour = false;
   int *a_rowptr = nullptr, *a_col = nullptr, *b_rowptr = nullptr, *b_col = nullptr;
   int *bt_rowptr = nullptr, *bt_col = nullptr;
@@ -95,7 +97,9 @@ struct LevelDev {
 
   template <typename T>
   DevOp<T> op() const;
-  DevCells cells() const { return DevCells{ncells, udofs, pdofs}; }
+  DevCells cells() const { return DevCells{ncells, udofs, pdofs, nl}; }
+  // the Schur block solve of one-block levels exists for Q2 hexahedra only
+  bool schur() const { return structured && nl == NU_LOC; }
 };
 template <>
 DevOp<double> LevelDev::op<double>() const {
@@ -327,11 +331,12 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
     PM_LAUNCH(launch_vanka_residual<T>(op, cells, Lv.colour_cells + b, n, u, rhs,
                                        static_cast<T *>(Lv.dbuf), Lv.res_variant, h->stream));
     if (e1) cudaEventRecord(e1, h->stream);
-    if (Lv.structured)
+    if (Lv.schur())
       PM_LAUNCH(launch_schur_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
                                       static_cast<const T *>(Lv.factors),
                                       static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
-    else if (sizeof(T) == sizeof(float) && !use_inverse(h) && Lv.apply_variant == 1)
+    else if (sizeof(T) == sizeof(float) && !use_inverse(h) && Lv.apply_variant == 1 &&
+             Lv.nl == NU_LOC)
       PM_LAUNCH(launch_vanka_apply_tma(cells, Lv.nu, Lv.colour_cells + b, n,
                                        static_cast<const float *>(Lv.factors), Lv.perm,
                                        reinterpret_cast<const float *>(Lv.dbuf), (float)damp,
@@ -710,7 +715,8 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
   const int rule_res = (sizeof(T) == sizeof(float) && !Lv.structured) ? 1 : 0;
   const int ro = h->opt.residual_variant;
   Lv.res_variant = ro == 0 ? rule_res : (ro == 2 ? 1 : 0);
-  const bool can_bulk = sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured;
+  const bool can_bulk =
+      sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured && Lv.nl == NU_LOC;
   const int ao = h->opt.apply_variant;
   const int rule_apply = sizeof(T) == sizeof(double) ? 0 : 2;
   Lv.apply_variant = ao == 0 ? rule_apply : (ao == 2 ? 2 : (can_bulk ? 1 : 0));
@@ -796,7 +802,7 @@ pm_status factor_all(pm_handle *h) {
   cudaEventRecord(e0, h->stream);
   for (size_t l = 1; l < h->L.size(); ++l) {
     LevelDev &Lv = h->L[l];
-    if (Lv.structured) {
+    if (Lv.schur()) {
       if (mixed(h))
         PM_LAUNCH(launch_schur_factor<float>(Lv.op<double>(), Lv.cells(),
                                              static_cast<float *>(Lv.factors), h->status_d, h->stream));
@@ -935,8 +941,13 @@ bool check_desc(pm_handle *h, const pm_level_desc *d) {
     return fail(h, PM_BADARG, "hanging nodes are not supported (hanging_bound != n_active)"), false;
   if (d->hanging_bound + d->n_dirichlet != d->n_udof)
     return fail(h, PM_BADARG, "n_dirichlet inconsistent with n_udof"), false;
-  if (d->n_ulocal != NU_LOC || d->n_plocal != NP_LOC)
-    return fail(h, PM_BADARG, "only Q2/P1disc hexahedra (27+4 local DOFs) are supported"), false;
+  if ((d->n_ulocal != NU_LOC && d->n_ulocal != NU_TET) || d->n_plocal != NP_LOC)
+    return fail(h, PM_BADARG,
+                "local DOFs: Q2/P1disc hexahedra (27+4) or P2+bubble/P1disc tetrahedra (15+4)"),
+           false;
+  if (d->pu_rowptr && (!d->pu_col || !d->pu_val || !d->pp_rowptr || !d->pp_col || !d->pp_val ||
+                       d->pu_rowptr[d->n_udof] != d->pu_nnz || d->pp_rowptr[d->n_pdof] != d->pp_nnz))
+    return fail(h, PM_BADARG, "incomplete prolongation arrays"), false;
   if (!d->a_rowptr || !d->a_col || !d->b_rowptr || !d->b_col || !d->bt_rowptr || !d->bt_col ||
       !d->cell_udofs || !d->cell_pdofs)
     return fail(h, PM_BADARG, "missing arrays"), false;
@@ -1063,7 +1074,18 @@ pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
   Lv.a_nnz = d->a_nnz;
   Lv.b_nnz = d->b_nnz;
   Lv.bt_nnz = d->bt_nnz;
-  Lv.h_udofs.assign(d->cell_udofs, d->cell_udofs + (size_t)Lv.ncells * NU_LOC);
+  Lv.nl = d->n_ulocal;
+  Lv.h_udofs.assign(d->cell_udofs, d->cell_udofs + (size_t)Lv.ncells * Lv.nl);
+  if (d->pu_rowptr) {
+    auto take = [](HostCsr &m, int rows, const int *rp, const int *c, const double *v, int nnz) {
+      m.rows = rows;
+      m.rowptr.assign(rp, rp + rows + 1);
+      m.col.assign(c, c + nnz);
+      m.val.assign(v, v + nnz);
+    };
+    take(Lv.h_pu, d->n_udof, d->pu_rowptr, d->pu_col, d->pu_val, d->pu_nnz);
+    take(Lv.h_pp, d->n_pdof, d->pp_rowptr, d->pp_col, d->pp_val, d->pp_nnz);
+  }
   Lv.h_pdofs.assign(d->cell_pdofs, d->cell_pdofs + (size_t)Lv.ncells * NP_LOC);
   if (d->cell_parent && d->cell_child) {
     Lv.h_parent.assign(d->cell_parent, d->cell_parent + Lv.ncells);
@@ -1103,40 +1125,58 @@ pm_status pm_setup(pm_handle *h) {
   if (h->L.empty()) return fail(h, PM_BADARG, "no levels");
   if (h->setup_done) return fail(h, PM_BADARG, "pm_setup called twice");
   const size_t es = mixed(h) ? sizeof(float) : sizeof(double);
+  for (const LevelDev &Lv : h->L)
+    if (Lv.nl != NU_LOC && use_inverse(h))
+      return fail(h, PM_BADARG, "vanka_inverse: Q2 hexahedral levels only");
   // colouring, transfers, buffers
   size_t maxcol = 0;
   for (size_t l = 0; l < h->L.size(); ++l) {
     LevelDev &Lv = h->L[l];
     std::string err;
-    if (!make_colouring(Lv.ncells, NU_LOC, NP_LOC, Lv.h_udofs.data(), Lv.h_pdofs.data(), Lv.nu,
+    if (!make_colouring(Lv.ncells, Lv.nl, NP_LOC, Lv.h_udofs.data(), Lv.h_pdofs.data(), Lv.nu,
                         Lv.np, Lv.has_colour ? Lv.h_colour.data() : nullptr, Lv.colouring, err))
       return fail(h, PM_BADARG, "level " + std::to_string(l) + ": " + err);
     PM_TRY(upload(h, &Lv.colour_cells, Lv.colouring.order.data(), Lv.colouring.order.size()));
     maxcol = std::max(maxcol, (size_t)Lv.colouring.max_size);
     if (l > 0) {
       LevelDev &K = h->L[l - 1];
-      if (Lv.h_parent.empty()) return fail(h, PM_BADARG, "fine level without cell_parent/cell_child");
       HostCsr Pu, Ru, Pp, Rp;
-      if (!build_transfers(K.ncells, K.h_udofs.data(), K.h_pdofs.data(), K.nu, K.np, Lv.ncells,
-                           Lv.h_udofs.data(), Lv.h_pdofs.data(), Lv.nu, Lv.np,
-                           Lv.h_parent.data(), Lv.h_child.data(), Pu, Ru, Pp, Rp, err))
-        return fail(h, PM_BADARG, "level " + std::to_string(l) + ": " + err);
+      if (!Lv.h_pu.rowptr.empty()) {  // handed over: restriction is the transpose
+        Pu = Lv.h_pu;
+        Pp = Lv.h_pp;
+        Pu.cols = K.nu;
+        Pp.cols = K.np;
+        for (int c : Pu.col)
+          if (c < 0 || c >= K.nu) return fail(h, PM_BADARG, "prolongation column out of range");
+        for (int c : Pp.col)
+          if (c < 0 || c >= K.np) return fail(h, PM_BADARG, "prolongation column out of range");
+        Ru = transpose(Pu);
+        Rp = transpose(Pp);
+      } else {
+        if (Lv.nl != NU_LOC || K.nl != NU_LOC)
+          return fail(h, PM_BADARG, "tetrahedral levels need the prolongation arrays");
+        if (Lv.h_parent.empty()) return fail(h, PM_BADARG, "fine level without cell_parent/cell_child");
+        if (!build_transfers(K.ncells, K.h_udofs.data(), K.h_pdofs.data(), K.nu, K.np, Lv.ncells,
+                             Lv.h_udofs.data(), Lv.h_pdofs.data(), Lv.nu, Lv.np,
+                             Lv.h_parent.data(), Lv.h_child.data(), Pu, Ru, Pp, Rp, err))
+          return fail(h, PM_BADARG, "level " + std::to_string(l) + ": " + err);
+      }
       PM_TRY(upload_csr(h, Lv.Pu, Pu));
       PM_TRY(upload_csr(h, Lv.Ru, Ru));
       PM_TRY(upload_csr(h, Lv.Pp, Pp));
       PM_TRY(upload_csr(h, Lv.Rp, Rp));
       // local factors (FP64 or FP32 storage) and permutations, or the
       // block-solve data of a one-block level
-      if (Lv.structured) {
+      if (Lv.schur()) {
         PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
                       (size_t)Lv.ncells * kSchurStride * es));
       } else {
         PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
-                      (size_t)Lv.ncells * kFacStride * es));
-        PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * NLOC));
+                      (size_t)Lv.ncells * elem_fac_stride(Lv.nl) * es));
+        PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * elem_nloc(Lv.nl)));
       }
       PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.dbuf),
-                    (size_t)Lv.colouring.max_size * kRStride * es));
+                    (size_t)Lv.colouring.max_size * elem_r_stride(Lv.nl) * es));
       if (std::fabs(1.0 - h->opt.alpha) > 1e-3)
         PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.uold), (size_t)Lv.ndof * es));
     }
@@ -1150,8 +1190,8 @@ pm_status pm_setup(pm_handle *h) {
                          (3.0 * sv + 4.0) * ((double)Lv.b_nnz + Lv.bt_nnz) + 4.0 * (Lv.np + 1) +
                          4.0 * (Lv.nu + 1);
       Lv.vanka_res_bytes = (mat + 2.0 * sv * Lv.ndof) / Lv.ncells;
-      const double per_cell =
-          Lv.structured ? (double)kSchurValues * sv : (double)NLOC * NLOC * sv + NLOC;
+      const double nloc = elem_nloc(Lv.nl);
+      const double per_cell = Lv.schur() ? (double)kSchurValues * sv : nloc * nloc * sv + nloc;
       Lv.vanka_apply_bytes = ((double)Lv.ncells * per_cell + 2.0 * sv * Lv.ndof) / Lv.ncells;
     }
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.sol), (size_t)Lv.ndof * es));
@@ -1472,6 +1512,7 @@ static pm_status assemble_impl(pm_handle *h, int level, const double *d_cell_h,
   if (!d_cell_h || !d_conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
   LevelDev &Lv = h->L[level];
   if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
+  if (Lv.nl != NU_LOC) return fail(h, PM_BADARG, "device assembly: Q2 hexahedral levels only");
   if (!h->asm_tables) {
     if (assemble_tables_init() < 0) return cuda_fail(h, "assembly tables");
     h->asm_tables = true;
@@ -1577,6 +1618,8 @@ pm_status pm_system_rhs_device(pm_handle *h, const double *d_old_rhs, const doub
 // (ox + fa/2, oy + fb/2, oz + fc/2)
 static pm_status build_coarse_nodes(pm_handle *h, int level) {
   LevelDev &F = h->L[level], &Cl = h->L[level - 1];
+  if (F.nl != NU_LOC || Cl.nl != NU_LOC)
+    return fail(h, PM_BADARG, "coarse-node interpolation: Q2 hexahedral levels only");
   if (F.h_parent.empty() || F.h_child.empty())
     return fail(h, PM_BADARG, "level without cell_parent / cell_child");
   std::vector<int> map((size_t)Cl.nu, -1);
@@ -1779,6 +1822,10 @@ pm_status pm_learned_attach(pm_handle *h, pm_mlp *m, double omega, double fallba
   if (!h) return PM_BADARG;
   if (!h->setup_done) return PM_NOT_SETUP;
   if (m && m->m.device != h->opt.device) return fail(h, PM_BADARG, "network on another device");
+  if (m)
+    for (const LevelDev &Lv : h->L)
+      if (Lv.nl != NU_LOC)
+        return fail(h, PM_BADARG, "learned smoother: Q2 hexahedral levels only (85-DOF cells)");
   drop_graphs(h);  // the captured V-cycles change
   if (!m) {
     h->mlp = nullptr;
@@ -1812,6 +1859,7 @@ pm_status pm_learned_harvest(pm_handle *h, const double *sol_exact, const double
   if (*n_pairs < 0 || *n_pairs + (long long)n_cycles * F.ncells > capacity)
     return fail(h, PM_BADARG, "harvest capacity exceeded");
   if (h->L.size() < 2) return fail(h, PM_BADARG, "harvest needs at least two levels");
+  if (F.nl != NU_LOC) return fail(h, PM_BADARG, "harvest: Q2 hexahedral levels only");
   PM_TRY(ensure_learned_buffers(h, F));
   const int N = F.ndof;
   double *u = h->xd, *b = h->bd, *ue = h->V, *e = h->V + N, *z = h->Z, *r = h->w;

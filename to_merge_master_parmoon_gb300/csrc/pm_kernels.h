@@ -16,6 +16,21 @@ constexpr int kRStride = 88;               // per-cell stride of the residual bu
 // per-cell stride (values) of the stored 85x85 factors: 7225 rounded up so
 // every cell's block starts on a 16-byte boundary in FP32 and FP64 (bulk copies)
 constexpr int kFacStride = 7228;
+constexpr int NU_TET = 15;  // P2 + face and cell bubbles on tetrahedra (local block 49)
+// local sizes of a cell with NU velocity nodes: block, factor and residual strides
+template <int NU>
+struct Elem {
+  static constexpr int nloc = 3 * NU + NP_LOC;
+  static constexpr int fac_stride = (nloc * nloc + 3) / 4 * 4;  // 7228 (85), 2404 (49)
+  static constexpr int r_stride = (nloc + 7) / 8 * 8;           // 88 (85), 56 (49)
+};
+inline int elem_nloc(int nl) { return 3 * nl + NP_LOC; }
+inline int elem_fac_stride(int nl) {
+  return nl == NU_TET ? Elem<NU_TET>::fac_stride : Elem<NU_LOC>::fac_stride;
+}
+inline int elem_r_stride(int nl) {
+  return nl == NU_TET ? Elem<NU_TET>::r_stride : Elem<NU_LOC>::r_stride;
+}
 
 // One level's operator in precision T (device pointers).  The nine velocity
 // blocks share the CSR pattern; off-diagonal blocks are zero on Dirichlet rows
@@ -45,8 +60,9 @@ struct DevCsr {
 // Local-block data of one level for the Vanka kernels.
 struct DevCells {
   int ncells;
-  const int *udofs;   // ncells x 27
+  const int *udofs;   // ncells x nl
   const int *pdofs;   // ncells x 4
+  int nl = NU_LOC;    // velocity nodes per cell: 27 (Q2 hexahedra) or 15 (P2+bubble tetrahedra)
 };
 
 // ---------------------------------------------------------------- sparse ---

@@ -45,11 +45,12 @@ __device__ __forceinline__ T ld_stream(const T *p) {
 // pivoting (first maximal |pivot|, dgetrf's choice).
 constexpr int kFactorThreads = 256;
 
-template <typename TC, typename TF>
+template <typename TC, typename TF, int NU>
 __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> op, DevCells cells,
                                                                  TF *__restrict__ factors,
                                                                  uint8_t *__restrict__ perm,
                                                                  int *status) {
+  constexpr int NU_LOC = NU, NLOC = Elem<NU>::nloc, kFacStride = Elem<NU>::fac_stride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TC *S = reinterpret_cast<TC *>(smem_raw);
   __shared__ int ud[NU_LOC], pd[NP_LOC];
@@ -545,10 +546,11 @@ __device__ __forceinline__ void row_group_sum(const int *__restrict__ col, const
   }
 }
 
-template <typename T, int VEC, bool ONE, int URA>
+template <typename T, int VEC, bool ONE, int URA, int NU>
 __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual_rows(
     DevOp<T> op, DevCells cells, const int *__restrict__ list, int ncol, const T *__restrict__ u,
     const T *__restrict__ rhs, T *__restrict__ rbuf) {
+  constexpr int NU_LOC = NU, kRStride = Elem<NU>::r_stride;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int slot = blockIdx.x * kResWarps + warp;
   if (slot >= ncol) return;  // whole warp; no block-wide barrier in this kernel
@@ -562,7 +564,7 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual_rows(
   for (int step = 0; step < (NU_LOC + 3) / 4; ++step) {
     const int k = step * 4 + sub;
     const bool valid = k < NU_LOC;
-    const int a = valid ? c_row_order[k] : 0;
+    const int a = valid ? (NU == 27 ? (int)c_row_order[k] : k) : 0;
     const int r = valid ? __ldg(ud + a) : 0;
     T s[3] = {T(0), T(0), T(0)};
     if (valid) {
@@ -595,9 +597,10 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual_rows(
   }
 }
 
-template <typename T>
+template <typename T, int NU = NU_LOC>
 __device__ __forceinline__ void scatter_local(int i, T v, const int *ud, const int *pd, int nu,
                                               T *u) {
+  constexpr int NU_LOC = NU;
   if (i < 3 * NU_LOC) {
     const int comp = i / NU_LOC, a = i - comp * NU_LOC;
     u[(size_t)comp * nu + ud[a]] += v;
@@ -639,19 +642,21 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply_inv(
   if (has2) scatter_local(lane + 64, damp * a2, ud, pd, nu, u);
 }
 
-template <typename T>
+template <typename T, int NU>
 __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
     DevCells cells, int nu, const int *__restrict__ list, int ncol, const T *__restrict__ F,
     const uint8_t *__restrict__ perm, const T *__restrict__ rbuf, T damp, T *__restrict__ u) {
+  constexpr int NU_LOC = NU, NLOC = Elem<NU>::nloc, kFacStride = Elem<NU>::fac_stride,
+                kRStride = Elem<NU>::r_stride;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int slot = blockIdx.x * kApplyWarps + warp;
   if (slot >= ncol) return;
   const int cell = list[slot];
-  const bool has2 = lane + 64 < NLOC;
+  const bool has1 = lane + 32 < NLOC, has2 = lane + 64 < NLOC;
   const uint8_t *pc = perm + (size_t)cell * NLOC;
   const T *R = rbuf + (size_t)slot * kRStride;
   T y0 = R[__ldg(pc + lane)];
-  T y1 = R[__ldg(pc + lane + 32)];
+  T y1 = has1 ? R[__ldg(pc + lane + 32)] : T(0);
   T y2 = has2 ? R[__ldg(pc + lane + 64)] : T(0);
   const T *Fc = F + (size_t)cell * kFacStride;
   // forward substitution with the unit lower factor, columns 0..83 in blocks
@@ -663,7 +668,7 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
       const int j = j0 + q;
       const T *col = Fc + (size_t)j * NLOC;
       b[q][0] = (lane > j) ? ld_stream(col + lane) : T(0);
-      b[q][1] = (lane + 32 > j) ? ld_stream(col + lane + 32) : T(0);
+      b[q][1] = (has1 && lane + 32 > j) ? ld_stream(col + lane + 32) : T(0);
       b[q][2] = (has2 && lane + 64 > j) ? ld_stream(col + lane + 64) : T(0);
     }
   };
@@ -691,7 +696,7 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
       const int j = jt - q;
       const T *col = Fc + (size_t)(j < 0 ? 0 : j) * NLOC;
       b[q][0] = (j >= 0 && lane <= j) ? ld_stream(col + lane) : T(0);
-      b[q][1] = (j >= 0 && lane + 32 <= j) ? ld_stream(col + lane + 32) : T(0);
+      b[q][1] = (j >= 0 && has1 && lane + 32 <= j) ? ld_stream(col + lane + 32) : T(0);
       b[q][2] = (j >= 0 && has2 && lane + 64 <= j) ? ld_stream(col + lane + 64) : T(0);
     }
   };
@@ -723,9 +728,9 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
   // u += damp * delta on the cell's DOFs (local order: u1 nodes, u2, u3, p)
   const int *ud = cells.udofs + (size_t)cell * NU_LOC;
   const int *pd = cells.pdofs + (size_t)cell * NP_LOC;
-  scatter_local(lane, damp * y0, ud, pd, nu, u);
-  scatter_local(lane + 32, damp * y1, ud, pd, nu, u);
-  if (has2) scatter_local(lane + 64, damp * y2, ud, pd, nu, u);
+  scatter_local<T, NU>(lane, damp * y0, ud, pd, nu, u);
+  if (has1) scatter_local<T, NU>(lane + 32, damp * y1, ud, pd, nu, u);
+  if (has2) scatter_local<T, NU>(lane + 64, damp * y2, ud, pd, nu, u);
 }
 
 // Two cells per warp: each half-warp owns one cell of the colour and each of
@@ -735,16 +740,17 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
 // four, the next block's entries loaded while the current one is used; the
 // row owning column j is held by half-lane j & 15 in slot j >> 4, so every
 // index below is a compile-time constant after unrolling.
-template <typename T>
-__device__ __forceinline__ void load_cols(T (&b)[4][6], const T *Fc, int hl, int j0, int dir,
+template <typename T, int NU, int SL>
+__device__ __forceinline__ void load_cols(T (&b)[4][SL], const T *Fc, int hl, int j0, int dir,
                                           bool lower) {
+  constexpr int NLOC = Elem<NU>::nloc;
 #pragma unroll
   for (int t = 0; t < 4; ++t) {
     const int j = j0 + dir * t;
     const bool jok = j >= 0 && j < NLOC;
     const T *col = Fc + (size_t)(jok ? j : 0) * NLOC;
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {
+    for (int q = 0; q < SL; ++q) {
       const int r = hl + 16 * q;
       const bool want = jok && r < NLOC && (lower ? r > j : r <= j);
       b[t][q] = want ? ld_stream(col + r) : T(0);
@@ -752,10 +758,14 @@ __device__ __forceinline__ void load_cols(T (&b)[4][6], const T *Fc, int hl, int
   }
 }
 
-template <typename T, int WARPS>
+template <typename T, int WARPS, int NU>
 __global__ void __launch_bounds__(WARPS * 32) k_vanka_apply2(
     DevCells cells, int nu, const int *__restrict__ list, int ncol, const T *__restrict__ F,
     const uint8_t *__restrict__ perm, const T *__restrict__ rbuf, T damp, T *__restrict__ u) {
+  constexpr int NU_LOC = NU, NLOC = Elem<NU>::nloc, kFacStride = Elem<NU>::fac_stride,
+                kRStride = Elem<NU>::r_stride;
+  constexpr int SL = (NLOC + 15) / 16;   // rows per half-lane: 6 (85), 4 (49)
+  constexpr int NB = (NLOC + 3) / 4;     // column blocks of the back substitution
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int pair = blockIdx.x * WARPS + warp;
   if (2 * pair >= ncol) return;  // whole warp
@@ -766,39 +776,39 @@ __global__ void __launch_bounds__(WARPS * 32) k_vanka_apply2(
   const int cell = list[cslot];
   const uint8_t *pc = perm + (size_t)cell * NLOC;
   const T *R = rbuf + (size_t)cslot * kRStride;
-  T y[6];
+  T y[SL];
 #pragma unroll
-  for (int q = 0; q < 6; ++q) {
+  for (int q = 0; q < SL; ++q) {
     const int r = hl + 16 * q;
     y[q] = r < NLOC ? R[__ldg(pc + r)] : T(0);
   }
   const T *Fc = F + (size_t)cell * kFacStride;
-  T cur[4][6], nxt[4][6];
+  T cur[4][SL], nxt[4][SL];
   // forward substitution with the unit lower factor, columns 0..83
-  load_cols(cur, Fc, hl, 0, 1, true);
+  load_cols<T, NU, SL>(cur, Fc, hl, 0, 1, true);
 #pragma unroll
-  for (int blk = 0; blk < (NLOC - 1) / 4; ++blk) {  // 21 blocks of 4 columns
+  for (int blk = 0; blk < (NLOC - 1) / 4; ++blk) {  // 21 (85) or 12 (49) blocks of 4 columns
     const int j0 = 4 * blk;
-    if (blk + 1 < (NLOC - 1) / 4) load_cols(nxt, Fc, hl, j0 + 4, 1, true);
+    if (blk + 1 < (NLOC - 1) / 4) load_cols<T, NU, SL>(nxt, Fc, hl, j0 + 4, 1, true);
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int j = j0 + t;
       const T yj = __shfl_sync(kFull, y[j >> 4], j & 15, 16);
 #pragma unroll
-      for (int q = 0; q < 6; ++q) y[q] -= cur[t][q] * yj;
+      for (int q = 0; q < SL; ++q) y[q] -= cur[t][q] * yj;
     }
 #pragma unroll
     for (int t = 0; t < 4; ++t)
 #pragma unroll
-      for (int q = 0; q < 6; ++q) cur[t][q] = nxt[t][q];
+      for (int q = 0; q < SL; ++q) cur[t][q] = nxt[t][q];
   }
-  // back substitution with U (diagonal stores 1/U_jj), columns 84..0 in
-  // blocks 87..84 (only 84 real), 83..80, ..., 3..0
-  load_cols(cur, Fc, hl, 87, -1, false);
+  // back substitution with U (diagonal stores 1/U_jj), columns NLOC-1..0 in
+  // blocks of 4 from 4 NB - 1 down (85: 87..84 with only 84 real, ..., 3..0)
+  load_cols<T, NU, SL>(cur, Fc, hl, 4 * NB - 1, -1, false);
 #pragma unroll
-  for (int blk = 21; blk >= 0; --blk) {
+  for (int blk = NB - 1; blk >= 0; --blk) {
     const int jt = 4 * blk + 3;
-    if (blk > 0) load_cols(nxt, Fc, hl, jt - 4, -1, false);
+    if (blk > 0) load_cols<T, NU, SL>(nxt, Fc, hl, jt - 4, -1, false);
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int j = jt - t;
@@ -807,22 +817,22 @@ __global__ void __launch_bounds__(WARPS * 32) k_vanka_apply2(
         if (hl == owner) y[qb] *= cur[t][qb];
         const T xj = __shfl_sync(kFull, y[qb], owner, 16);
 #pragma unroll
-        for (int q = 0; q < 6; ++q)
+        for (int q = 0; q < SL; ++q)
           if (hl + 16 * q < j) y[q] -= cur[t][q] * xj;
       }
     }
 #pragma unroll
     for (int t = 0; t < 4; ++t)
 #pragma unroll
-      for (int q = 0; q < 6; ++q) cur[t][q] = nxt[t][q];
+      for (int q = 0; q < SL; ++q) cur[t][q] = nxt[t][q];
   }
   if (live) {
     const int *ud = cells.udofs + (size_t)cell * NU_LOC;
     const int *pd = cells.pdofs + (size_t)cell * NP_LOC;
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {
+    for (int q = 0; q < SL; ++q) {
       const int r = hl + 16 * q;
-      if (r < NLOC) scatter_local(r, damp * y[q], ud, pd, nu, u);
+      if (r < NLOC) scatter_local<T, NU>(r, damp * y[q], ud, pd, nu, u);
     }
   }
 }
@@ -1219,14 +1229,24 @@ inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 
 }  // namespace
 
+template <typename TC, typename TF, int NU>
+int launch_factor_nu(const DevOp<double> &op, const DevCells &cells, TF *factors, uint8_t *perm,
+                     int *status, cudaStream_t s) {
+  constexpr int n = Elem<NU>::nloc;
+  const size_t sm = sizeof(TC) * n * n;
+  cudaFuncSetAttribute(k_vanka_factor<TC, TF, NU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sm);
+  k_vanka_factor<TC, TF, NU><<<cells.ncells, kFactorThreads, sm, s>>>(op, cells, factors, perm,
+                                                                     status);
+  return ok() < 0 ? -1 : 1;
+}
+
 template <typename TC, typename TF>
 int launch_factor_impl(const DevOp<double> &op, const DevCells &cells, TF *factors, uint8_t *perm,
                        int *status, cudaStream_t s) {
-  const size_t sm = sizeof(TC) * NLOC * NLOC;
-  cudaFuncSetAttribute(k_vanka_factor<TC, TF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sm);
-  k_vanka_factor<TC, TF><<<cells.ncells, kFactorThreads, sm, s>>>(op, cells, factors, perm, status);
-  return ok() < 0 ? -1 : 1;
+  if (cells.nl == NU_TET) return launch_factor_nu<TC, TF, NU_TET>(op, cells, factors, perm, status, s);
+  if (cells.nl != NU_LOC) return -1;
+  return launch_factor_nu<TC, TF, NU_LOC>(op, cells, factors, perm, status, s);
 }
 
 template <typename TF>
@@ -1236,6 +1256,7 @@ int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *fact
   const int n = factor_fp32 ? launch_factor_impl<float, TF>(op, cells, factors, perm, status, s)
                             : launch_factor_impl<double, TF>(op, cells, factors, perm, status, s);
   if (n < 0 || !inverse) return n;
+  if (cells.nl != NU_LOC) return -1;  // the stored inverse: hexahedral blocks only
   if constexpr (sizeof(TF) == sizeof(float)) {
     k_lu_inverse_f32<<<cells.ncells, kInvThreadsLU, 0, s>>>(factors, perm);
     return ok() < 0 ? -1 : n + 1;
@@ -1250,15 +1271,25 @@ int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *
   constexpr int VEC = sizeof(T) == 4 ? 4 : 2;
   constexpr int U = sizeof(T) == 4 ? 1 : 2;
   const int grid = (ncol + kResWarps - 1) / kResWarps;
+  if (cells.nl == NU_TET) {  // tetrahedra: the row-group kernel
+    if (op.structured)
+      k_vanka_residual_rows<T, VEC, true, 2, NU_TET><<<grid, kResWarps * 32, 0, s>>>(
+          op, cells, cell_list, ncol, u, rhs, rbuf);
+    else
+      k_vanka_residual_rows<T, VEC, false, 1, NU_TET><<<grid, kResWarps * 32, 0, s>>>(
+          op, cells, cell_list, ncol, u, rhs, rbuf);
+    return ok() < 0 ? -1 : 1;
+  }
+  if (cells.nl != NU_LOC) return -1;
   if (variant == 1) {
     k_vanka_residual<T, VEC, U><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list, ncol, u, rhs,
                                                                rbuf);
   } else if (op.structured) {
-    k_vanka_residual_rows<T, VEC, true, 2><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list,
-                                                                          ncol, u, rhs, rbuf);
+    k_vanka_residual_rows<T, VEC, true, 2, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
+        op, cells, cell_list, ncol, u, rhs, rbuf);
   } else {
-    k_vanka_residual_rows<T, VEC, false, 1><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list,
-                                                                           ncol, u, rhs, rbuf);
+    k_vanka_residual_rows<T, VEC, false, 1, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
+        op, cells, cell_list, ncol, u, rhs, rbuf);
   }
   return ok() < 0 ? -1 : 1;
 }
@@ -1269,17 +1300,28 @@ int launch_vanka_apply(const DevCells &cells, int nu, const int *cell_list, int 
                        T *u, bool pairs, cudaStream_t s) {
   if (ncol <= 0) return 0;
   const int grid = (ncol + kApplyWarps - 1) / kApplyWarps;
+  constexpr int W = sizeof(T) == 4 ? 8 : 4;  // FP64 holds twice the registers
+  const int g2 = (ncol + 2 * W - 1) / (2 * W);
+  if (cells.nl == NU_TET) {
+    if (inverse) return -1;  // the stored inverse: hexahedral blocks only
+    if (pairs)
+      k_vanka_apply2<T, W, NU_TET><<<g2, W * 32, 0, s>>>(cells, nu, cell_list, ncol, factors,
+                                                         perm, rbuf, damp, u);
+    else
+      k_vanka_apply<T, NU_TET><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol,
+                                                                factors, perm, rbuf, damp, u);
+    return ok() < 0 ? -1 : 1;
+  }
+  if (cells.nl != NU_LOC) return -1;
   if (inverse)
     k_vanka_apply_inv<T><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors,
                                                           rbuf, damp, u);
-  else if (pairs) {
-    constexpr int W = sizeof(T) == 4 ? 8 : 4;  // FP64 holds twice the registers
-    const int g2 = (ncol + 2 * W - 1) / (2 * W);
-    k_vanka_apply2<T, W><<<g2, W * 32, 0, s>>>(cells, nu, cell_list, ncol, factors, perm, rbuf,
-                                               damp, u);
-  } else
-    k_vanka_apply<T><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors, perm,
-                                                      rbuf, damp, u);
+  else if (pairs)
+    k_vanka_apply2<T, W, NU_LOC><<<g2, W * 32, 0, s>>>(cells, nu, cell_list, ncol, factors, perm,
+                                                       rbuf, damp, u);
+  else
+    k_vanka_apply<T, NU_LOC><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors,
+                                                              perm, rbuf, damp, u);
   return ok() < 0 ? -1 : 1;
 }
 
