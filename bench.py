@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--batch-systems", type=int, default=48)
     ap.add_argument("--no-assembly", action="store_true")
     ap.add_argument("--no-channel", action="store_true")
+    ap.add_argument("--only-factor", action="store_true",
+                    help="refactorisation of every level only (nine-block mixed levels, "
+                         "warm-up + steps passes): the case profiled for k_vanka_factor")
     ap.add_argument("--channel-steps", type=int, default=10,
                     help="timed Crank-Nicolson steps per variant of the channel run "
                          "(a bounded sample of its 200 steps)")
@@ -381,6 +384,18 @@ def channel_run(args, threads, net):
     return out
 
 
+def only_factor(args):
+    """pm_refactor of nine-block mixed levels, args.warmup + args.steps times;
+    prints the mean factorisation time (the library's CUDA events)."""
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed, nthreads=os.cpu_count() or 1)
+    S = PmSolver(P.descs, precision="mixed")
+    ms = [S.refactor() for _ in range(args.warmup + args.steps)][args.warmup:]
+    print(json.dumps({"only_factor": True, "levels": P.n_levels,
+                      "cells": sum(P.desc(l).n_cells for l in range(1, P.n_levels)),
+                      "factor_ms": sum(ms) / len(ms)}), flush=True)
+
+
 def only_assembly(args):
     """pm_assemble_level_device on every level of one-block FP64 levels,
     args.warmup + args.steps passes; prints the mean time of a pass."""
@@ -512,6 +527,9 @@ def main():
         return
     if args.only_assembly:
         only_assembly(args)
+        return
+    if args.only_factor:
+        only_factor(args)
         return
     rank, world, local = dist_env()
     import numpy as np
