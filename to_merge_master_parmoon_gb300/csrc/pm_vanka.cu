@@ -54,7 +54,9 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TC *S = reinterpret_cast<TC *>(smem_raw);
   __shared__ int ud[NU_LOC], pd[NP_LOC];
+  __shared__ int skey[NU_LOC], sloc[NU_LOC];  // the cell's DOFs sorted, with local indices
   __shared__ int piv_row;
+  __shared__ TC piv_rcp, piv_val, piv_d0;  // 1 / pivot, the pivot, the old diagonal
   __shared__ unsigned char pm[NLOC];
   __shared__ int singular;
   const int cell = blockIdx.x;
@@ -66,6 +68,23 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
   if (tid < NLOC) pm[tid] = (unsigned char)tid;
   if (tid == 0) singular = 0;
   __syncthreads();
+  if (tid < NU_LOC) {  // rank sort (the DOFs of a cell are distinct)
+    const int v = ud[tid];
+    int rank = 0;
+    for (int q = 0; q < NU_LOC; ++q) rank += ud[q] < v;
+    skey[rank] = v;
+    sloc[rank] = tid;
+  }
+  __syncthreads();
+  // local index of velocity DOF l in the cell, -1 if absent (binary search)
+  auto local_of = [&](int l) {
+    int lo = 0, hi = NU_LOC;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (skey[mid] < l) lo = mid + 1; else hi = mid;
+    }
+    return (lo < NU_LOC && skey[lo] == l) ? sloc[lo] : -1;
+  };
 
   // gather: velocity rows (9 blocks + BT), pressure rows (B)
   for (int a = warp; a < NU_LOC; a += nwarps) {
@@ -73,12 +92,7 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
     const bool dir = r >= op.nact;
     for (int j = op.a_rowptr[r] + lane; j < op.a_rowptr[r + 1]; j += 32) {
       const int l = op.a_col[j];
-      int m = -1;
-      for (int q = 0; q < NU_LOC; ++q)
-        if (ud[q] == l) {
-          m = q;
-          break;
-        }
+      const int m = local_of(l);
       if (m < 0) continue;
       const int c1 = m * NLOC, c2 = (m + NU_LOC) * NLOC, c3 = (m + 2 * NU_LOC) * NLOC;
       if (op.structured) {  // one block for the three components, no coupling
@@ -121,12 +135,7 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
     const int r = pd[k], row = 3 * NU_LOC + k;
     for (int j = op.b_rowptr[r] + lane; j < op.b_rowptr[r + 1]; j += 32) {
       const int l = op.b_col[j];
-      int m = -1;
-      for (int q = 0; q < NU_LOC; ++q)
-        if (ud[q] == l) {
-          m = q;
-          break;
-        }
+      const int m = local_of(l);
       if (m < 0) continue;
       S[m * NLOC + row] = (TC)op.b[0][j];
       S[(m + NU_LOC) * NLOC + row] = (TC)op.b[1][j];
@@ -135,55 +144,76 @@ __global__ void __launch_bounds__(kFactorThreads) k_vanka_factor(DevOp<double> o
   }
   __syncthreads();
 
-  for (int k = 0; k < NLOC; ++k) {
-    if (warp == 0) {
-      TC best = TC(-1);
-      int bi = k;
-      for (int i = k + lane; i < NLOC; i += 32) {
-        const TC v = fabs(S[k * NLOC + i]);
-        if (v > best) {
-          best = v;
-          bi = i;
-        }
+  // Right-looking LU, two barriers per step: (1) the interchange of rows k
+  // and p in every column with the scaling of column k (disjoint memory),
+  // (2) the rank-1 update, during which warp 0 -- the warp that updates
+  // column k+1 -- also finds the next pivot (look-ahead) from its own
+  // freshly updated entries.
+  // pivot of column k (rows k..): first maximal |a|, with its signed value
+  auto pivot_search = [&](int k) {
+    TC best = TC(-1), bv = TC(0);
+    int bi = k;
+    for (int i = k + lane; i < NLOC; i += 32) {
+      const TC v = S[k * NLOC + i];
+      if (fabs(v) > best) {
+        best = fabs(v);
+        bv = v;
+        bi = i;
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const TC ob = __shfl_xor_sync(kFull, best, o);
-        const int oi = __shfl_xor_sync(kFull, bi, o);
-        if (ob > best || (ob == best && oi < bi)) {
-          best = ob;
-          bi = oi;
-        }
-      }
-      if (lane == 0) piv_row = bi;
     }
-    __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const TC ob = __shfl_xor_sync(kFull, best, o);
+      const TC ov = __shfl_xor_sync(kFull, bv, o);
+      const int oi = __shfl_xor_sync(kFull, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      piv_row = bi;
+      piv_val = bv;
+      piv_d0 = S[k * NLOC + k];  // lane 0 holds row k (its own entry)
+      piv_rcp = bv != TC(0) ? TC(1) / bv : TC(0);
+      if (bv == TC(0)) singular = 1;
+    }
+  };
+  if (warp == 0) pivot_search(0);
+  __syncthreads();
+  for (int k = 0; k < NLOC; ++k) {
     const int p = piv_row;
-    if (p != k) {
+    const TC pv = piv_val, d0 = piv_d0, rp = piv_rcp;
+    if (p != k)
       for (int j = tid; j < NLOC; j += kFactorThreads) {
+        if (j == k) continue;
         const TC t = S[j * NLOC + k];
         S[j * NLOC + k] = S[j * NLOC + p];
         S[j * NLOC + p] = t;
       }
-      if (tid == 0) {
+    // column k after the interchange: pv on the diagonal, row p holds the
+    // old diagonal d0; below the diagonal scaled by 1 / pivot
+    const TC sc = rp != TC(0) ? rp : TC(1);
+    for (int i = k + 1 + tid; i < NLOC; i += kFactorThreads)
+      S[k * NLOC + i] = (i == p ? d0 : S[k * NLOC + i]) * sc;
+    if (tid == 0) {
+      S[k * NLOC + k] = pv;
+      if (p != k) {
         const unsigned char t = pm[k];
         pm[k] = pm[p];
         pm[p] = t;
       }
     }
     __syncthreads();
-    const TC piv = S[k * NLOC + k];
-    if (piv == TC(0)) {
-      if (tid == 0) singular = 1;
-    } else {
-      const TC rp = TC(1) / piv;
-      for (int i = k + 1 + tid; i < NLOC; i += kFactorThreads) S[k * NLOC + i] *= rp;
-    }
-    __syncthreads();
     for (int jj = k + 1 + warp; jj < NLOC; jj += nwarps) {
       const TC ukj = S[jj * NLOC + k];
       if (ukj != TC(0))
         for (int ii = k + 1 + lane; ii < NLOC; ii += 32) S[jj * NLOC + ii] -= S[k * NLOC + ii] * ukj;
+    }
+    if (warp == 0 && k + 1 < NLOC) {
+      __syncwarp();
+      pivot_search(k + 1);
     }
     __syncthreads();
   }
@@ -902,6 +932,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense_lu(double *a, int N, in
   __shared__ double bv[32];
   __shared__ int bi[32];
   __shared__ int piv_row;
+  __shared__ double piv_rcp;  // 1 / pivot, computed once per step
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = kDenseThreads / 32;
   for (int k = 0; k < N; ++k) {
     double best = -1.0;
@@ -942,6 +973,8 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense_lu(double *a, int N, in
       if (lane == 0) {
         piv_row = bidx;
         ipiv[k] = bidx;
+        const double pv = a[(size_t)k * N + bidx];  // the pivot before the interchange
+        piv_rcp = pv != 0.0 ? 1.0 / pv : 0.0;
       }
     }
     __syncthreads();
@@ -953,11 +986,10 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense_lu(double *a, int N, in
         a[(size_t)j * N + p] = t;
       }
     __syncthreads();
-    const double piv = a[(size_t)k * N + k];
-    if (piv == 0.0) {
+    const double rp = piv_rcp;
+    if (rp == 0.0) {
       if (tid == 0) atomicOr(status, 2);
     } else {
-      const double rp = 1.0 / piv;
       for (int i = k + 1 + tid; i < N; i += kDenseThreads) a[(size_t)k * N + i] *= rp;
     }
     __syncthreads();
@@ -986,6 +1018,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_lu_panel(double *a, int N, in
   __shared__ double bv[32];
   __shared__ int bi[32];
   __shared__ int piv_row;
+  __shared__ double piv_rcp;  // 1 / pivot, computed once per step
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = kDenseThreads / 32;
   const int kend = min(k0 + kLuNb, N);
   for (int k = k0; k < kend; ++k) {
@@ -1027,6 +1060,8 @@ __global__ void __launch_bounds__(kDenseThreads) k_lu_panel(double *a, int N, in
       if (lane == 0) {
         piv_row = bidx;
         ipiv[k] = bidx;
+        const double pv = a[(size_t)k * N + bidx];  // the pivot before the interchange
+        piv_rcp = pv != 0.0 ? 1.0 / pv : 0.0;
       }
     }
     __syncthreads();
@@ -1038,11 +1073,10 @@ __global__ void __launch_bounds__(kDenseThreads) k_lu_panel(double *a, int N, in
         a[(size_t)j * N + p] = t;
       }
     __syncthreads();
-    const double piv = a[(size_t)k * N + k];
-    if (piv == 0.0) {
+    const double rp = piv_rcp;
+    if (rp == 0.0) {
       if (tid == 0) atomicOr(status, 2);
     } else {
-      const double rp = 1.0 / piv;
       for (int i = k + 1 + tid; i < N; i += kDenseThreads) a[(size_t)k * N + i] *= rp;
     }
     __syncthreads();
