@@ -689,6 +689,17 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
   T y1 = has1 ? R[__ldg(pc + lane + 32)] : T(0);
   T y2 = has2 ? R[__ldg(pc + lane + 64)] : T(0);
   const T *Fc = F + (size_t)cell * kFacStride;
+  // L2 prefetch of the 4 columns from j0 (one 128-byte line per lane, inside
+  // this cell's factor block), kPfDist columns ahead of their use: the demand
+  // loads then hit L2
+  constexpr int kPfDist = 32;
+  const char *fend = reinterpret_cast<const char *>(Fc + (size_t)NLOC * NLOC);
+  auto prefetch4 = [&](int j0) {
+    if (j0 < 0 || j0 >= NLOC) return;
+    const char *a = reinterpret_cast<const char *>(Fc + (size_t)j0 * NLOC) + 128 * lane;
+    if (lane * 128 < 4 * NLOC * (int)sizeof(T) && a < fend)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+  };
   // forward substitution with the unit lower factor, columns 0..83 in blocks
   // of 4, the next block's column entries loaded while this one is used
   T cur[4][3], nxt[4][3];
@@ -703,7 +714,9 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
     }
   };
   load_l(cur, 0);
+  for (int j = 4; j < kPfDist; j += 4) prefetch4(j);
   for (int j0 = 0; j0 < NLOC - 1; j0 += 4) {
+    prefetch4(j0 + kPfDist);
     if (j0 + 4 < NLOC - 1) load_l(nxt, j0 + 4);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -732,6 +745,7 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
   };
   load_u(cur, NLOC - 1);
   for (int jt = NLOC - 1; jt >= 0; jt -= 4) {
+    prefetch4(jt - kPfDist - 3);
     if (jt - 4 >= 0) load_u(nxt, jt - 4);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
