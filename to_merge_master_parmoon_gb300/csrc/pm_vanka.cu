@@ -692,7 +692,7 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_vanka_apply(
   // L2 prefetch of the 4 columns from j0 (one 128-byte line per lane, inside
   // this cell's factor block), kPfDist columns ahead of their use: the demand
   // loads then hit L2
-  constexpr int kPfDist = 32;
+  constexpr int kPfDist = 16;
   const char *fend = reinterpret_cast<const char *>(Fc + (size_t)NLOC * NLOC);
   auto prefetch4 = [&](int j0) {
     if (j0 < 0 || j0 >= NLOC) return;
