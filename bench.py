@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--batch-systems", type=int, default=48)
     ap.add_argument("--no-assembly", action="store_true")
     ap.add_argument("--no-channel", action="store_true")
+    ap.add_argument("--only-mlp", type=int, default=0, metavar="ROWS",
+                    help="forward passes of the learned smoother's MLP on ROWS random "
+                         "feature rows only (warm-up + steps): the case profiled for "
+                         "k_mlp_layer_tc")
     ap.add_argument("--only-factor", action="store_true",
                     help="refactorisation of every level only (nine-block mixed levels, "
                          "warm-up + steps passes): the case profiled for k_vanka_factor")
@@ -384,6 +388,29 @@ def channel_run(args, threads, net):
     return out
 
 
+def only_mlp(args):
+    """MLP forward (397 -> 256 -> 256 -> 85, BF16 on tcgen05, FP32 accumulate)
+    on args.only_mlp rows of seeded random features; prints the mean time of
+    a pass and the flop rate (3.78e5 flop per row)."""
+    import torch
+    from to_merge_master_parmoon_gb300.learned import Mlp
+    m = args.only_mlp
+    net = Mlp(device=0, seed=0, max_batch=m)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    X = torch.randn(m, 397, device="cuda", generator=g)
+    ts = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        net.forward(X)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    t = sum(ts[args.warmup:]) / args.steps
+    flop = 2.0 * (397 * 256 + 256 * 256 + 256 * 85) * m
+    print(json.dumps({"only_mlp": True, "rows": m, "ms_per_pass": t * 1e3,
+                      "tflops": flop / t / 1e12}), flush=True)
+
+
 def only_factor(args):
     """pm_refactor of nine-block mixed levels, args.warmup + args.steps times;
     prints the mean factorisation time (the library's CUDA events)."""
@@ -531,6 +558,9 @@ def main():
     if args.only_factor:
         only_factor(args)
         return
+    if args.only_mlp > 0:
+        only_mlp(args)
+        return
     rank, world, local = dist_env()
     import numpy as np
     import torch
@@ -568,9 +598,13 @@ def main():
         except PmError:
             return PmSolver(descs, upload_mode=0, **kw)
 
-    solvers = {}
+    solvers, setup_s = {}, {}
     for name, prec in (("mixed_learned", "mixed"), ("mixed", "mixed"), ("fp64", "fp64")):
+        # set-up: upload, colouring, transfers, local factorisation, coarse LU
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         solvers[name] = make(P.descs, prec)
+        setup_s[name] = time.perf_counter() - t0
     solvers["mixed_learned"].attach_learned(net, omega=1.0, fallback_ratio=0.5)
     # the same system as NSTYPE-2 levels (one velocity block; the Galerkin
     # Oseen form has A12..A32 = 0 and A11 = A22 = A33), smoothed by the exact
@@ -621,6 +655,10 @@ def main():
             "factor_ms": fms, "solve_ms": info["solve_ms"], "iterations": iters[-1],
             "rel_res": info["true_res"] / info["res0"], "launches": S.kernel_launches - launches0,
             "clocks": clk.summary(),
+            # each FGMRES iteration applies one V-cycle
+            "vcycles_per_s": iters[-1] / (info["solve_ms"] * 1e-3),
+            "dof_iterations_per_s": n * iters[-1] / (info["solve_ms"] * 1e-3),
+            "setup_s": setup_s.get(prec),
         }
         if profile:
             results[prec]["profile"] = S.profile_read()
@@ -737,15 +775,21 @@ def main():
                                            "post-smoothing step on every level",
                    "l2": "inputs (11.7 GB of matrices) larger than L2", "parallelism": "replicas"},
         "fp64": {"value": results["fp64"]["ms"] * 1e-3, "iterations": results["fp64"]["iterations"],
+                 "vcycles_per_s": results["fp64"]["vcycles_per_s"],
+                 "dof_iterations_per_s": results["fp64"]["dof_iterations_per_s"],
+                 "setup_s": results["fp64"]["setup_s"],
                  "factor_ms": results["fp64"]["factor_ms"], "solve_ms": results["fp64"]["solve_ms"],
                  "rel_res": results["fp64"]["rel_res"],
                  "sweep_kernels": {k: {"ms_total": v["ms"], "launches": v["launches"],
                                        "achieved_gbs": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] else None}
                                    for k, v in results["fp64"].get("profile", {}).items()}},
         "mixed": {"value": results["mixed"]["ms"] * 1e-3,
-                  **{k: results["mixed"][k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res")}},
+                  **{k: results["mixed"][k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res",
+                                                      "vcycles_per_s", "dof_iterations_per_s",
+                                                      "setup_s")}},
         "mixed_learned": {**{k: results["mixed_learned"][k]
-                             for k in ("factor_ms", "solve_ms", "iterations", "rel_res", "wall_ms")},
+                             for k in ("factor_ms", "solve_ms", "iterations", "rel_res", "wall_ms",
+                                       "vcycles_per_s", "dof_iterations_per_s", "setup_s")},
                           "learned_status": results["mixed_learned"].get("learned"),
                           "training": learned_info},
         "speedup_vs_fp64": results["fp64"]["ms"] / results["mixed_learned"]["ms"],
