@@ -827,12 +827,27 @@ __global__ void __launch_bounds__(WARPS * 32) k_vanka_apply2(
     y[q] = r < NLOC ? R[__ldg(pc + r)] : T(0);
   }
   const T *Fc = F + (size_t)cell * kFacStride;
+  // L2 prefetch of the 4 columns from j0, 16 columns ahead of their use (two
+  // 128-byte lines per half-lane, inside this cell's factor block)
+  const char *fend = reinterpret_cast<const char *>(Fc + (size_t)NLOC * NLOC);
+  auto prefetch4 = [&](int j0) {
+    if (j0 < 0 || j0 >= NLOC) return;
+    const char *base = reinterpret_cast<const char *>(Fc + (size_t)j0 * NLOC);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int off = 128 * (hl + 16 * h);
+      if (off < 4 * NLOC * (int)sizeof(T) && base + off < fend)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + off));
+    }
+  };
   T cur[4][SL], nxt[4][SL];
   // forward substitution with the unit lower factor, columns 0..83
   load_cols<T, NU, SL>(cur, Fc, hl, 0, 1, true);
+  for (int jp = 4; jp < 16; jp += 4) prefetch4(jp);
 #pragma unroll
   for (int blk = 0; blk < (NLOC - 1) / 4; ++blk) {  // 21 (85) or 12 (49) blocks of 4 columns
     const int j0 = 4 * blk;
+    prefetch4(j0 + 16);
     if (blk + 1 < (NLOC - 1) / 4) load_cols<T, NU, SL>(nxt, Fc, hl, j0 + 4, 1, true);
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
@@ -852,6 +867,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_vanka_apply2(
 #pragma unroll
   for (int blk = NB - 1; blk >= 0; --blk) {
     const int jt = 4 * blk + 3;
+    prefetch4(jt - 19);
     if (blk > 0) load_cols<T, NU, SL>(nxt, Fc, hl, jt - 4, -1, false);
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
