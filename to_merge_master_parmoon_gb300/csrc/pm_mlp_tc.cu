@@ -3,15 +3,16 @@
 // K contiguous) and W [N x K] BF16 (weights, K contiguous), FP32 accumulation
 // in tensor memory.
 //
-// One CTA of four warps per 128-row tile of A (UMMA shape M = 128, N = the
-// layer width 256 or 96, K = 16 per instruction).  K is staged through shared
+// One CTA of eight warps (two warpgroups) per 128-row tile of A (UMMA shape
+// M = 128, N = the layer width 256 or 96, K = 16 per instruction).  K is staged through shared
 // memory in chunks of KC columns, in the K-major canonical layout without
 // swizzling: 8-row x 16-byte core matrices, LBO = 128 bytes between core
 // matrices along K, SBO = KC/8 * 128 bytes between 8-row groups.  Thread 0
 // issues the chunk's tcgen05.mma instructions and commits them to an
 // mbarrier, which every thread waits on (bounded) before the chunk buffers
 // are refilled.  The epilogue reads the accumulator with tcgen05.ld (warp w
-// owns TMEM lanes 32w..32w+31, i.e. tile rows 32w..32w+31), adds the bias,
+// owns TMEM lanes 32(w%4)..32(w%4)+31, i.e. tile rows 32(w%4)..+31; the two
+// warpgroups take alternate 32-column blocks), adds the bias,
 // applies GELU and writes FP32 and/or BF16 rows.  The TMEM columns (256 or
 // 128) are always released before the CTA exits; a barrier wait that gives
 // up sets PM_ERR_BULK_TIMEOUT in *err and skips the epilogue.
@@ -26,7 +27,7 @@ namespace pm {
 
 namespace {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;  // two warpgroups
 constexpr long long kTcMaxPolls = 1ll << 22;
 // dynamic shared memory per CTA: at most two CTAs per SM, so their TMEM
 // allocations (<= 256 columns each) always fit the SM's 512 columns
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
   bool ok = true;
   for (int c = 0; c < NCH; ++c) {
     // stage the chunk: A rows m0..m0+127 (zeros past M) and all N rows of W
+#pragma unroll 4
     for (int u = tid; u < 128 * KB; u += kTcThreads) {
       const int r = u / KB, kb = u - r * KB;
       const int gm = m0 + r;
@@ -141,6 +143,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
         v = __ldg(reinterpret_cast<const uint4 *>(a.A + (size_t)gm * a.lda + c * KC + kb * 8));
       *reinterpret_cast<uint4 *>(As + (r >> 3) * SBO + kb * 128 + (r & 7) * 16) = v;
     }
+#pragma unroll 4
     for (int u = tid; u < N * KB; u += kTcThreads) {
       const int r = u / KB, kb = u - r * KB;
       const uint4 v =
@@ -177,11 +180,12 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
   tc_fence_after();
 
   if (ok) {
-    const int row = m0 + warp * 32 + lane;
+    const int q = warp & 3, half = warp >> 2;  // TMEM lane quarter, column parity
+    const int row = m0 + q * 32 + lane;
 #pragma unroll 1
-    for (int cb = 0; cb < N; cb += 32) {
+    for (int cb = 32 * half; cb < N; cb += 64) {
       uint32_t v[32];
-      const uint32_t taddr = tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb;
+      const uint32_t taddr = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)cb;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
           "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
