@@ -736,7 +736,7 @@ def main():
             "kernel": "k_vanka_residual<float,4,1> (cell-local residuals over full CSR rows, "
                       "one colour; flattened entry stream)",
             "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "bytes_per_launch": per_launch,
-            "apply_kernel": {"name": "k_vanka_apply2<float,8> (stored FP32 LU, two cells per "
+            "apply_kernel": {"name": "k_vanka_apply<float> (stored FP32 LU, one cell per "
                                      "warp, columns prefetched in registers and L2; "
                                      "substitution + update)",
                              "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,

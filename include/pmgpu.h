@@ -107,8 +107,9 @@ typedef struct {
                              pm_setup and keep the faster                    */
   int apply_variant;      /* LU apply of nine-block levels, factor columns
                              loaded from HBM with register and L2 prefetch:
-                             0 (default) two cells per warp (half a warp per
-                             cell; measured faster in both precisions); 1 (FP32
+                             0 (default) per level: two cells per warp (half a
+                             warp per cell) in FP64, one cell per warp in
+                             FP32 (each measured faster there); 1 (FP32
                              only; FP64 levels use pairs) each cell's factors
                              staged in shared memory by bulk copies; 2 one
                              cell per warp; -1 time them per level at

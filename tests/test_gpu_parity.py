@@ -109,10 +109,10 @@ def test_kernel_variants(P, oracle, variant, precision):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_default_kernels(P, gpu64, gpu32, precision):
-    """The per-level defaults: stream residual in FP32, row groups in FP64,
-    two cells per warp in both (coarsest level: no cells)."""
+    """The per-level defaults: stream residual + one cell per warp in FP32,
+    row groups + two cells per warp in FP64 (coarsest level: no cells)."""
     S = gpu64 if precision == "fp64" else gpu32
-    want = 0 if precision == "fp64" else 1
+    want = 0 if precision == "fp64" else 1 + 2 * 2
     assert [S._lib.pm_level_variant(S._h, l) for l in range(1, 3)] == [want, want]
 
 

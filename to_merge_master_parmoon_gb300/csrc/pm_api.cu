@@ -711,15 +711,15 @@ template <typename T>
 pm_status tune_level(pm_handle *h, LevelDev &Lv) {
   // defaults (option 0): row groups except on FP32 nine-block levels, where
   // the flattened stream measured faster; LU apply with two cells per warp
-  // (with the L2 prefetch of the factor columns it measured faster in both
-  // precisions)
+  // in FP64 (the FP64 chain is the bound), one cell per warp in FP32 (each
+  // measured faster in the full solve, with the L2 prefetch of the columns)
   const int rule_res = (sizeof(T) == sizeof(float) && !Lv.structured) ? 1 : 0;
   const int ro = h->opt.residual_variant;
   Lv.res_variant = ro == 0 ? rule_res : (ro == 2 ? 1 : 0);
   const bool can_bulk =
       sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured && Lv.nl == NU_LOC;
   const int ao = h->opt.apply_variant;
-  const int rule_apply = 0;
+  const int rule_apply = sizeof(T) == sizeof(double) ? 0 : 2;
   Lv.apply_variant = ao == 0 ? rule_apply : (ao == 2 ? 2 : (can_bulk ? 1 : 0));
   const bool tune_res = h->opt.residual_variant < 0;
   const bool tune_apply = h->opt.apply_variant < 0 && !use_inverse(h) && !Lv.structured;
