@@ -134,9 +134,13 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
   bool ok = true;
   for (int c = 0; c < NCH; ++c) {
     // stage the chunk: A rows m0..m0+127 (zeros past M) and all N rows of W
+    // thread u -> row r = 8 * (u / (8 KB)) + u % 8, 16-byte column kb =
+    // (u / 8) % KB: eight consecutive threads fill one 128-byte core matrix
+    // (conflict-free shared stores; the second half of each 32-byte global
+    // sector is read from L1 by the next eight threads)
 #pragma unroll 4
     for (int u = tid; u < 128 * KB; u += kTcThreads) {
-      const int r = u / KB, kb = u - r * KB;
+      const int rl = u & 7, q = u >> 3, kb = q % KB, r = 8 * (q / KB) + rl;
       const int gm = m0 + r;
       uint4 v = make_uint4(0u, 0u, 0u, 0u);
       if (gm < a.M)
@@ -145,7 +149,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
     }
 #pragma unroll 4
     for (int u = tid; u < N * KB; u += kTcThreads) {
-      const int r = u / KB, kb = u - r * KB;
+      const int rl = u & 7, q = u >> 3, kb = q % KB, r = 8 * (q / KB) + rl;
       const uint4 v =
           __ldg(reinterpret_cast<const uint4 *>(a.W + (size_t)r * K + c * KC + kb * 8));
       *reinterpret_cast<uint4 *>(Bs + (r >> 3) * SBO + kb * 128 + (r & 7) * 16) = v;
