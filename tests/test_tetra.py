@@ -109,6 +109,23 @@ def test_tet_layout_invariants():
             assert list(a["a_col"][a["a_rowptr"][r]:a["a_rowptr"][r + 1]]) == [r]
 
 
+@pytest.mark.parametrize("element", ["hexa", "tetra"])
+def test_host_reassembly_reproduces_the_build(element):
+    """pmh_reassemble (the host timing of a re-assembly) rewrites every
+    level's values with the build's cell loop: bit-identical arrays."""
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    P = OseenProblem(n_levels=2, nu=1e-2, seed=5, element=element)
+    before = [{k: [v.copy() for v in P.arrays(l)[k]] for k in ("a", "b", "bt")}
+              for l in range(P.n_levels)]
+    rhs = P.rhs()
+    P.reassemble()
+    for l in range(P.n_levels):
+        a = P.arrays(l)
+        for k in ("a", "b", "bt"):
+            assert all(np.array_equal(x, y) for x, y in zip(before[l][k], a[k]))
+    assert np.array_equal(rhs, P.rhs())
+
+
 @pytest.mark.parametrize("example,nu", [("quadlin_oseen", 1.0), ("random", 1e-2)])
 def test_oracle_fgmres_on_tetrahedra(example, nu):
     """The oracle's FGMRES + V(2,2) with 49 x 49 cell Vanka (colour order) and
