@@ -82,6 +82,19 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, world: int) -> float:
+    """The largest x over the ranks of the process group (the replicas' step
+    time); a CUDA tensor with NCCL, a host tensor otherwise (gloo)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class Clocks:
     """nvidia-smi samples during the timed region."""
 
@@ -667,12 +680,7 @@ def main():
             results[prec]["learned"] = S.learned_status()
 
     # reduce: max over ranks
-    ms = results["mixed_learned"]["ms"]
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(results["mixed_learned"]["ms"], world)
 
     # end to end through the C ABI with host buffers: every step uploads the
     # level matrices (pm_update_matrices, which refactors) and solves from
