@@ -203,14 +203,40 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if (row < a.M) {
+        // 16-byte stores of the row's 32 values (row * ldo + cb is a multiple
+        // of 32 elements, so every store is aligned)
         const size_t o = (size_t)row * a.ldo + cb;
+        float x[32];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          float x = __uint_as_float(v[j]) + __ldg(a.bias + cb + j);
-          if (a.pre) a.pre[o + j] = x;
-          if (a.act == 1) x = gelu_tc(x);
-          if (a.Cf) a.Cf[o + j] = x;
-          if (a.Cb) a.Cb[o + j] = __float2bfloat16(x);
+        for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]) + __ldg(a.bias + cb + j);
+        if (a.pre) {
+#pragma unroll
+          for (int j = 0; j < 32; j += 4)
+            *reinterpret_cast<float4 *>(a.pre + o + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+        }
+        if (a.act == 1) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) x[j] = gelu_tc(x[j]);
+        }
+        if (a.Cf) {
+#pragma unroll
+          for (int j = 0; j < 32; j += 4)
+            *reinterpret_cast<float4 *>(a.Cf + o + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+        }
+        if (a.Cb) {
+#pragma unroll
+          for (int j = 0; j < 32; j += 8) {
+            uint4 w;
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(x[j], x[j + 1]);
+            __nv_bfloat162 h1 = __floats2bfloat162_rn(x[j + 2], x[j + 3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(x[j + 4], x[j + 5]);
+            __nv_bfloat162 h3 = __floats2bfloat162_rn(x[j + 6], x[j + 7]);
+            w.x = *reinterpret_cast<uint32_t *>(&h0);
+            w.y = *reinterpret_cast<uint32_t *>(&h1);
+            w.z = *reinterpret_cast<uint32_t *>(&h2);
+            w.w = *reinterpret_cast<uint32_t *>(&h3);
+            *reinterpret_cast<uint4 *>(a.Cb + o + j) = w;
+          }
         }
       }
     }
