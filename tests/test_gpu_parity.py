@@ -4,7 +4,7 @@ oracle on the same seeded inputs.
 Tolerances: FP64 kernels differ from the oracle only in summation order and
 FMA contraction (relative 1e-11 for sweeps, 1e-9 after factorisations);
 mixed precision (FP32 V-cycle) is compared at 5e-4 relative per operator and
-must reach the same FP64 solution to the spec bar (relative L2
+must reach the same FP64 solution to the required bar (relative L2
 difference <= 1e-6 after FGMRES to 1e-10)."""
 import numpy as np
 import pytest
