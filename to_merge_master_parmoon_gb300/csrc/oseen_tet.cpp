@@ -460,7 +460,10 @@ void build_prolongation(const PMLevelData &C, PMLevelData &F) {
     }
     F.cell_parent[t] = parent;
     F.cell_child[t] = parent >= 0 ? nchild[parent]++ : -1;
-    if (parent < 0) continue;
+    if (parent < 0) {  // cannot happen for nested Kuhn splits; keep the CSR consistent
+      for (int m = 0; m < 4; ++m) F.pp_rowptr[4 * t + m + 1] = 4;
+      continue;
+    }
     const int *cud = &C.cell_udofs[(size_t)parent * NT];
     const int *fud = &F.cell_udofs[(size_t)t * NT];
     for (int k = 0; k < NT; ++k) {
