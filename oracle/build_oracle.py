@@ -4,6 +4,11 @@
 * ``oracle/_ref/ref_basis_pin``  — the reference's own basis-function headers
   compiled where they lie under the reference tree (only when that tree is
   present; its output is committed as tests/golden/basis_q2_p1.json).
+* ``oracle/_ref/libref_harness.so`` — the reference's coupled-system kernels
+  (src/FE/MGComponents3D.C with the matrix classes of src/FE/Matrix.C,
+  SquareMatrix.C, Structure.C, SquareStructure.C and src/FE/Blas1.C) compiled
+  where they lie, driven by ref_harness.cpp (only when the tree is present;
+  its outputs are committed as tests/golden/ref_defect_*.npz).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 what this builds.
@@ -31,10 +36,11 @@ def build_oracle() -> Path:
     BUILD.mkdir(parents=True, exist_ok=True)
     out = BUILD / "liboracle.so"
     srcs = [HERE / "oracle.cpp"]
-    deps = srcs + [HERE / "oracle.h", ROOT / "include" / "pmgpu.h"]
+    deps = srcs + [HERE / "oracle.h", ROOT / "include" / "pmgpu.h", Path(__file__)]
     if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return out
-    _run(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-shared", f"-I{ROOT / 'include'}",
+    _run(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-shared",
+          f"-I{ROOT / 'include'}",
           f"-I{HERE}", *map(str, srcs), "-o", str(out)])
     return out
 
@@ -49,6 +55,47 @@ def build_ref_pin() -> Path | None:
     return out
 
 
+# reference translation units of the harness, compiled where they lie
+REF_HARNESS_TUS = ("MGComponents3D", "Matrix", "SquareMatrix", "Structure", "SquareStructure",
+                   "Blas1")
+REF_INCLUDE_DIRS = ("General", "FE", "Geometry", "FE3D", "FE2D", "FE1D", "System",
+                    "QuadFormulas", "Parallel", "AMG")
+
+
+def build_ref_harness() -> Path | None:
+    """Compile the reference's coupled defect / mat-vec code with
+    ref_harness.cpp into oracle/_ref/libref_harness.so.  The reference objects
+    are built with hidden symbols and function sections so that the link
+    (``--gc-sections``) keeps only what the harness reaches, and ``-z defs``
+    proves nothing it keeps is unresolved.  Returns None without the tree."""
+    src = REFERENCE / "src" / "FE"
+    if not all((src / f"{t}.C").exists() for t in REF_HARNESS_TUS):
+        return None
+    objdir = REF_OUT / "harness_obj"
+    objdir.mkdir(parents=True, exist_ok=True)
+    out = REF_OUT / "libref_harness.so"
+    mine = [HERE / "ref_harness.cpp", HERE / "ref_stubs" / "mkl_spblas.h",
+            HERE / "ref_stubs" / "mkl_types.h", Path(__file__)]
+    if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in mine):
+        return out
+    inc = ["-D__3D__", f"-I{HERE / 'ref_stubs'}"]
+    inc += [f"-I{REFERENCE / 'include' / d}" for d in REF_INCLUDE_DIRS]
+    flags = ["g++", "-O2", "-std=c++11", "-fPIC", "-fopenmp", "-w", "-ffp-contract=off",
+             "-ffunction-sections", "-fdata-sections", "-fvisibility=hidden"]
+    jobs = [(src / f"{t}.C", objdir / f"{t}.o") for t in REF_HARNESS_TUS]
+    jobs.append((HERE / "ref_harness.cpp", objdir / "ref_harness.o"))
+    procs = [(subprocess.Popen([*flags, *inc, "-c", str(s), "-o", str(o)], stdout=subprocess.PIPE,
+                               stderr=subprocess.STDOUT, text=True), s) for s, o in jobs]
+    for pr, s in procs:
+        log = pr.communicate()[0]
+        if pr.returncode != 0:
+            raise RuntimeError(f"reference harness: compiling {s} failed:\n{log}")
+    _run(["g++", "-shared", "-fopenmp", "-Wl,--gc-sections", "-Wl,-z,defs",
+          *[str(o) for _, o in jobs], "-o", str(out)])
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_ref_pin())
+    print(build_ref_harness())

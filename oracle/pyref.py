@@ -1,0 +1,113 @@
+"""ctypes front end of oracle/_ref/libref_harness.so: the reference's own
+Defect_NSE4 / MatVect_NSE4 / IntoL20Vector3D (src/FE/MGComponents3D.C:3210,
+:3030, :1756) run on one level of a problem built here.  TEST INFRASTRUCTURE
+ONLY — it exists where the reference tree does (see build_ref_harness).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .build_oracle import build_ref_harness
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+_dpp = C.POINTER(_dp)
+_LIB = None
+
+
+def ref_harness_lib():
+    """The loaded harness, or None when the reference tree is absent."""
+    global _LIB
+    if _LIB is None:
+        path = build_ref_harness()
+        if path is None:
+            return None
+        L = C.CDLL(str(path))
+        level = [C.c_int, C.c_int, C.c_int, _ip, _ip, _dpp, _ip, _ip, _dpp, _ip, _ip, _dpp]
+        L.ref_defect_nse4.argtypes = level + [_dp, _dp, _dp, C.c_int, C.c_int]
+        L.ref_defect_nse4.restype = None
+        L.ref_matvec_nse4.argtypes = level + [_dp, _dp, C.c_int]
+        L.ref_matvec_nse4.restype = None
+        L.ref_into_l20.argtypes = [_dp, C.c_int, C.c_int]
+        L.ref_into_l20.restype = None
+        _LIB = L
+    return _LIB
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(_ip)
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_dp)
+
+
+class RefLevel:
+    """One level (the dict of ``OseenProblem.arrays``) handed to the
+    reference's kernels."""
+
+    def __init__(self, arrays: dict, threads: int = 1):
+        L = ref_harness_lib()
+        if L is None:
+            raise RuntimeError("reference tree not present: the reference harness is not built")
+        self._L = L
+        self.threads = threads
+        self.n_u, self.n_p = int(arrays["n_udof"]), int(arrays["n_pdof"])
+        self.n_active = int(arrays["n_active"])
+        keep = []
+
+        def ip(a):
+            a, p = _i(a)
+            keep.append(a)
+            return p
+
+        def dpp(arrs):
+            ptrs = (_dp * len(arrs))()
+            for k, a in enumerate(arrs):
+                a, p = _d(a)
+                keep.append(a)
+                ptrs[k] = p
+            keep.append(ptrs)
+            return C.cast(ptrs, _dpp)
+
+        self._args = [self.n_u, self.n_active, self.n_p,
+                      ip(arrays["a_rowptr"]), ip(arrays["a_col"]), dpp(arrays["a"]),
+                      ip(arrays["b_rowptr"]), ip(arrays["b_col"]), dpp(arrays["b"]),
+                      ip(arrays["bt_rowptr"]), ip(arrays["bt_col"]), dpp(arrays["bt"])]
+        self._keep = keep
+
+    @property
+    def ndof(self) -> int:
+        return 3 * self.n_u + self.n_p
+
+    def defect(self, x, b, project: bool) -> np.ndarray:
+        """r = b - K x; the pressure part projected into L2_0 (P1disc) when
+        ``project``, as Defect_NSE4 does under INTERNAL_PROJECT_PRESSURE."""
+        x, xp = _d(x)
+        b, bp = _d(b)
+        assert x.size == self.ndof and b.size == self.ndof
+        r = np.empty(self.ndof)
+        self._L.ref_defect_nse4(*self._args, xp, bp, r.ctypes.data_as(_dp), int(project),
+                                self.threads)
+        return r
+
+    def matvec(self, x) -> np.ndarray:
+        x, xp = _d(x)
+        assert x.size == self.ndof
+        y = np.empty(self.ndof)
+        self._L.ref_matvec_nse4(*self._args, xp, y.ctypes.data_as(_dp), self.threads)
+        return y
+
+
+def ref_into_l20(v, order: int = -11) -> np.ndarray:
+    """IntoL20Vector3D on a copy of ``v``."""
+    L = ref_harness_lib()
+    if L is None:
+        raise RuntimeError("reference tree not present: the reference harness is not built")
+    v = np.array(v, dtype=np.float64, copy=True)
+    L.ref_into_l20(v.ctypes.data_as(_dp), v.size, order)
+    return v

@@ -1,0 +1,142 @@
+// ref_harness.cpp — drives the reference's own coupled-system kernels on a
+// level handed over as plain CSR arrays.  TEST INFRASTRUCTURE ONLY: it pins
+// the oracle's restatement (oracle.cpp: coupled_defect, coupled_matvec,
+// into_l20) against the reference code itself, and generates the golden
+// vectors tests/golden/ref_defect_*.npz (tests/golden/make_ref_defect_golden.py).
+//
+// The reference translation units are compiled where they lie in the
+// reference tree by oracle/build_oracle.py (build_ref_harness):
+//   src/FE/MGComponents3D.C  Defect_NSE4 (:3210), MatVect_NSE4 (:3030),
+//                            CoupledDefect (:3038), CoupledMatVect (:2872),
+//                            IntoL20Vector3D (:1756)
+//   src/FE/Matrix.C, SquareMatrix.C, Structure.C, SquareStructure.C
+//                            TMatrix / TSquareMatrix / TStructure /
+//                            TSquareStructure constructors and accessors
+// with -D__3D__ and the MKL declarations of oracle/ref_stubs/ (the MKL calls
+// in Matrix.C sit on paths this harness never takes).  The library links
+// with -z defs, so every symbol the kept code needs is resolved.
+//
+// Objects the reference owns:
+// * TStructure takes ownership of the row/column arrays it is given
+//   (src/FE/Structure.C:40-45, freed in ~TStructure at :90-96), so the
+//   harness hands it fresh new[] copies.
+// * TMatrix(TStructure*, double*) leaves its MKL members unset
+//   (src/FE/Matrix.C:55-59) and ~TMatrix frees them (:126-132).  So the
+//   matrices are never destroyed: a harness process builds one level, runs,
+//   and exits.
+// * The active bound of a TSquareStructure is the row count in the
+//   array constructor (src/FE/SquareStructure.C:28-32) and is a protected
+//   member.  So a derived class sets it to the number of non-Dirichlet rows,
+//   which the reference's own structure builder does for its velocity
+//   spaces.
+#include <cstring>
+#include <fstream>
+
+#include <Database.h>
+#include <LinAlg.h>
+#include <Matrix.h>
+#include <SquareMatrix.h>
+#include <SquareStructure.h>
+#include <Structure.h>
+
+// storage of the static parameter database the kernels read
+// (TDatabase::ParamDB->OMPNUMTHREADS, INTERNAL_PROJECT_PRESSURE,
+// INTERNAL_PRESSURE_SPACE) and of the log stream the reference's headers name
+static TParamDB g_param;
+TParamDB *TDatabase::ParamDB = &g_param;
+std::ofstream OutFile;
+
+namespace {
+
+struct ActiveStructure : public TSquareStructure {
+  ActiveStructure(int n, int n_active, int nnz, int *col, int *rowptr)
+      : TSquareStructure(n, nnz, col, rowptr) {
+    ActiveBound = n_active;
+  }
+};
+
+template <class T>
+T *copy_of(const T *src, long n) {
+  T *d = new T[n > 0 ? n : 1];
+  if (n > 0) std::memcpy(d, src, sizeof(T) * n);
+  return d;
+}
+
+struct Level {
+  TSquareMatrix *A[9];
+  TMatrix *B[6];  // B1, B2, B3 (pressure rows), B1T, B2T, B3T (velocity rows)
+};
+
+Level make_level(int n_u, int n_active, int n_p, const int *a_rowptr, const int *a_col,
+                 const double *const *a, const int *b_rowptr, const int *b_col,
+                 const double *const *b, const int *bt_rowptr, const int *bt_col,
+                 const double *const *bt) {
+  Level L;
+  const int a_nnz = a_rowptr[n_u], b_nnz = b_rowptr[n_p], bt_nnz = bt_rowptr[n_u];
+  TSquareStructure *sa = new ActiveStructure(n_u, n_active, a_nnz, copy_of(a_col, a_nnz),
+                                             copy_of(a_rowptr, n_u + 1L));
+  for (int k = 0; k < 9; ++k) {
+    L.A[k] = new TSquareMatrix(sa);
+    std::memcpy(L.A[k]->GetEntries(), a[k], sizeof(double) * a_nnz);
+  }
+  TStructure *sb = new TStructure(n_p, n_u, b_nnz, copy_of(b_col, b_nnz),
+                                  copy_of(b_rowptr, n_p + 1L));
+  TStructure *sbt = new TStructure(n_u, n_p, bt_nnz, copy_of(bt_col, bt_nnz),
+                                   copy_of(bt_rowptr, n_u + 1L));
+  for (int k = 0; k < 3; ++k) {
+    L.B[k] = new TMatrix(sb, copy_of(b[k], b_nnz));
+    L.B[3 + k] = new TMatrix(sbt, copy_of(bt[k], bt_nnz));
+  }
+  return L;
+}
+
+void set_params(int threads, int project) {
+  std::memset(&g_param, 0, sizeof(g_param));
+  g_param.OMPNUMTHREADS = threads > 0 ? threads : 1;
+  g_param.INTERNAL_PROJECT_PRESSURE = project;
+  g_param.INTERNAL_PRESSURE_SPACE = -11;  // P1disc on hexahedra
+}
+
+}  // namespace
+
+extern "C" {
+
+// r = b - K x through Defect_NSE4, with the reference's own pressure
+// projection when project != 0.  a[9], b[3], bt[3] are the value arrays of
+// the shared A pattern, the B pattern (pressure rows) and the BT pattern
+// (velocity rows); Dirichlet velocity rows are the last n_u - n_active.
+__attribute__((visibility("default"))) void ref_defect_nse4(
+    int n_u, int n_active, int n_p, const int *a_rowptr, const int *a_col,
+    const double *const *a, const int *b_rowptr, const int *b_col, const double *const *b,
+    const int *bt_rowptr, const int *bt_col, const double *const *bt, const double *x,
+    const double *rhs, double *r, int project, int threads) {
+  set_params(threads, project);
+  Level L = make_level(n_u, n_active, n_p, a_rowptr, a_col, a, b_rowptr, b_col, b, bt_rowptr,
+                       bt_col, bt);
+  const long n = 3L * n_u + n_p;
+  double *xx = copy_of(x, n), *bb = copy_of(rhs, n);
+  Defect_NSE4(L.A, L.B, xx, bb, r);
+  delete[] xx;
+  delete[] bb;
+}
+
+// y = K x through MatVect_NSE4
+__attribute__((visibility("default"))) void ref_matvec_nse4(
+    int n_u, int n_active, int n_p, const int *a_rowptr, const int *a_col,
+    const double *const *a, const int *b_rowptr, const int *b_col, const double *const *b,
+    const int *bt_rowptr, const int *bt_col, const double *const *bt, const double *x, double *y,
+    int threads) {
+  set_params(threads, 0);
+  Level L = make_level(n_u, n_active, n_p, a_rowptr, a_col, a, b_rowptr, b_col, b, bt_rowptr,
+                       bt_col, bt);
+  double *xx = copy_of(x, 3L * n_u + n_p);
+  MatVect_NSE4(L.A, L.B, xx, y);
+  delete[] xx;
+}
+
+// in-place IntoL20Vector3D(v, len, order)
+__attribute__((visibility("default"))) void ref_into_l20(double *v, int len, int order) {
+  IntoL20Vector3D(v, len, order);
+}
+
+}  // extern "C"

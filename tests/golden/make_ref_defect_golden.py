@@ -1,0 +1,64 @@
+"""Regenerate tests/golden/ref_defect_*.npz: the reference's own Defect_NSE4
+(with and without the P1disc pressure projection) and MatVect_NSE4
+(src/FE/MGComponents3D.C:3210, :3030) on levels built by the problem builder,
+run through oracle/ref_harness.cpp, which oracle/build_oracle.py compiles with
+the reference sources where they lie.  Needs the reference tree; the fixtures
+are committed so the tests do not.
+
+Inputs are exact binary fractions of the DOF index (``golden_inputs``), so
+every platform forms the same x and b without a random generator.
+"""
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+HERE = Path(__file__).resolve().parent
+
+# name -> (OseenProblem keyword arguments, level)
+CASES = {
+    "hexa": (dict(n_levels=2, nu=1e-2, seed=0), 1),
+    "channel": (dict(n_levels=2, nu=1e-2, seed=0, example="channel", periodic="xz",
+                     stretch_y=1.5, box=[0.0, 6.0, -1.0, 1.0, 0.0, 3.0]), 1),
+    "tetra": (dict(n_levels=2, nu=1.0, seed=0, example="quadlin_oseen", element="tetra"), 0),
+}
+
+
+def golden_inputs(n: int):
+    i = np.arange(n, dtype=np.int64)
+    x = ((i * 7919 + 13) % 2003 - 1001).astype(np.float64) / 512.0
+    b = ((i * 104729 + 7) % 1999 - 999).astype(np.float64) / 256.0
+    return x, b
+
+
+def build_problem(kwargs: dict):
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    kw = dict(kwargs)
+    if "box" in kw:
+        kw["box"] = tuple(kw["box"])
+    return OseenProblem(**kw)
+
+
+def main() -> None:
+    from oracle.pyref import RefLevel, ref_harness_lib
+    if ref_harness_lib() is None:
+        raise SystemExit("reference tree not found; cannot regenerate the defect golden files")
+    for name, (kwargs, level) in CASES.items():
+        P = build_problem(kwargs)
+        R = RefLevel(P.arrays(level), threads=1)
+        x, b = golden_inputs(R.ndof)
+        np.savez_compressed(
+            HERE / f"ref_defect_{name}.npz",
+            problem=json.dumps(kwargs), level=level, n_udof=R.n_u, n_pdof=R.n_p,
+            r_project=R.defect(x, b, True), r_plain=R.defect(x, b, False), y=R.matvec(x),
+            source=("reference src/FE/MGComponents3D.C Defect_NSE4 / MatVect_NSE4 "
+                    "run by oracle/ref_harness.cpp"))
+        print("wrote", name, "level", level, "ndof", R.ndof)
+
+
+if __name__ == "__main__":
+    main()

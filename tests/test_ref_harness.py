@@ -1,0 +1,114 @@
+"""The reference's own coupled-system kernels as the oracle's oracle.
+
+oracle/ref_harness.cpp runs the reference's Defect_NSE4 (with the P1disc
+projection IntoL20Vector3D) and MatVect_NSE4 (src/FE/MGComponents3D.C:3210,
+:3030, :1756), compiled from the reference sources where they lie, on levels
+built here.  With the reference tree present the oracle's restatement must
+equal it bit for bit (same operation order, no contraction).  Its outputs are
+committed as tests/golden/ref_defect_*.npz, so that without the tree (and on
+the GPU) the oracle and the CUDA defect/mat-vec are still checked against
+the reference's numbers:
+* the oracle: relative 1e-13 (builds on another platform may differ in the
+  last bits of the assembled matrices);
+* the FP64 CUDA kernels: relative 1e-12 (summation order and FMA contraction
+  differ).
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+
+GOLD = Path(__file__).parent / "golden"
+CASES = ("hexa", "channel", "tetra")
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def ref_lib_or_skip():
+    from oracle.pyref import ref_harness_lib
+    lib = ref_harness_lib()
+    if lib is None:
+        pytest.skip("reference tree not present (the committed fixtures cover this case)")
+    return lib
+
+
+def load_case(name):
+    from tests.golden.make_ref_defect_golden import build_problem, golden_inputs
+    g = np.load(GOLD / f"ref_defect_{name}.npz")
+    P = build_problem(json.loads(str(g["problem"])))
+    level = int(g["level"])
+    assert P.arrays(level)["n_udof"] == int(g["n_udof"])
+    assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
+    x, b = golden_inputs(P.ndof(level))
+    return P, level, x, b, g
+
+
+@pytest.mark.parametrize("kwargs", [
+    dict(n_levels=3, nu=1e-2, seed=0),
+    dict(n_levels=2, nu=1e-3, seed=5, example="channel", periodic="xz", stretch_y=2.0,
+         box=(0.0, 6.0, -1.0, 1.0, 0.0, 3.0)),
+    dict(n_levels=2, nu=1.0, seed=0, example="quadlin_oseen", element="tetra"),
+], ids=["hexa", "channel", "tetra"])
+def test_oracle_equals_reference_kernels_bitwise(kwargs):
+    ref_lib_or_skip()
+    from oracle.pyref import RefLevel
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    P = OseenProblem(**kwargs)
+    O = Oracle(P)
+    rng = np.random.default_rng(11)
+    for level in range(P.n_levels):
+        R = RefLevel(P.arrays(level), threads=2)
+        x, b = rng.standard_normal(R.ndof), rng.standard_normal(R.ndof)
+        for project in (False, True):
+            assert np.array_equal(R.defect(x, b, project), O.coupled_defect(level, x, b, project))
+        assert np.array_equal(R.matvec(x), O.matvec(level, x))
+
+
+def test_reference_l20_projection_removes_the_constant_mode_mean():
+    """IntoL20Vector3D(., ., -11) leaves every 4th entry (the P1disc
+    constant modes) with zero mean and the other entries untouched."""
+    ref_lib_or_skip()
+    from oracle.pyref import ref_into_l20
+    v = np.random.default_rng(4).standard_normal(4 * 37)
+    w = ref_into_l20(v)
+    assert abs(w[::4].sum()) < 1e-13
+    mask = np.arange(v.size) % 4 != 0
+    assert np.array_equal(w[mask], v[mask])
+    assert np.allclose(w[::4] - v[::4], -v[::4].mean())
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fixtures_reproduce_from_the_reference(name):
+    """The committed fixtures are what the reference computes here."""
+    ref_lib_or_skip()
+    from oracle.pyref import RefLevel
+    P, level, x, b, g = load_case(name)
+    R = RefLevel(P.arrays(level), threads=1)
+    assert np.array_equal(R.defect(x, b, True), g["r_project"])
+    assert np.array_equal(R.defect(x, b, False), g["r_plain"])
+    assert np.array_equal(R.matvec(x), g["y"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference_fixtures(name):
+    P, level, x, b, g = load_case(name)
+    O = Oracle(P)
+    assert rel(O.coupled_defect(level, x, b, True), g["r_project"]) < 1e-13
+    assert rel(O.coupled_defect(level, x, b, False), g["r_plain"]) < 1e-13
+    assert rel(O.matvec(level, x), g["y"]) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_defect_and_matvec_match_reference_fixtures(name):
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, x, b, g = load_case(name)
+    S = PmSolver(P.descs, precision="fp64")
+    assert rel(S.coupled_defect(level, x, b, True), g["r_project"]) < 1e-12
+    assert rel(S.coupled_defect(level, x, b, False), g["r_plain"]) < 1e-12
+    assert rel(S.matvec(level, x), g["y"]) < 1e-12
