@@ -5,7 +5,8 @@
   compiled where they lie under the reference tree (only when that tree is
   present; its output is committed as tests/golden/basis_q2_p1.json).
 * ``oracle/_ref/libref_harness.so`` — the reference's coupled-system kernels
-  (src/FE/MGComponents3D.C with the matrix classes of src/FE/Matrix.C,
+  and its flexible FGMRES (src/FE/MGComponents3D.C, src/FE/FgmresIte.C and
+  src/FE/ItMethod.C, with the matrix classes of src/FE/Matrix.C,
   SquareMatrix.C, Structure.C, SquareStructure.C and src/FE/Blas1.C) compiled
   where they lie, driven by ref_harness.cpp (only when the tree is present;
   its outputs are committed as tests/golden/ref_defect_*.npz).
@@ -56,8 +57,8 @@ def build_ref_pin() -> Path | None:
 
 
 # reference translation units of the harness, compiled where they lie
-REF_HARNESS_TUS = ("MGComponents3D", "Matrix", "SquareMatrix", "Structure", "SquareStructure",
-                   "Blas1")
+REF_HARNESS_TUS = ("MGComponents3D", "FgmresIte", "ItMethod", "Matrix", "SquareMatrix",
+                   "Structure", "SquareStructure", "Blas1")
 REF_INCLUDE_DIRS = ("General", "FE", "Geometry", "FE3D", "FE2D", "FE1D", "System",
                     "QuadFormulas", "Parallel", "AMG")
 
@@ -80,6 +81,10 @@ def build_ref_harness() -> Path | None:
         return out
     inc = ["-D__3D__", f"-I{HERE / 'ref_stubs'}"]
     inc += [f"-I{REFERENCE / 'include' / d}" for d in REF_INCLUDE_DIRS]
+    # include/FE/NSE_MGLevel.h (reached from FgmresIte.C) includes the CUDA
+    # runtime headers; declarations only, nothing of them is linked
+    cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
+    inc += ["-isystem", str(cuda_inc)]
     flags = ["g++", "-O2", "-std=c++11", "-fPIC", "-fopenmp", "-w", "-ffp-contract=off",
              "-ffunction-sections", "-fdata-sections", "-fvisibility=hidden"]
     jobs = [(src / f"{t}.C", objdir / f"{t}.o") for t in REF_HARNESS_TUS]

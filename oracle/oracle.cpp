@@ -287,6 +287,14 @@ double dot(const double *a, const double *b, int n) {
   return s;
 }
 
+// Ddot (src/FE/Blas1.C:14-31): one sequential sum, the order of the
+// reference's TFgmresIte::Dotprod without MPI (src/FE/FgmresIte.C:857-926)
+double ddot(const double *a, const double *b, int n) {
+  double s = 0;
+  for (int i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
 // TNSE_MGLevel4::Defect (src/FE/NSE_MGLevel4.C:465-539)
 void level_defect(const oracle *o, const OLevel &L, const double *u, const double *f, double *d,
                   double *res) {
@@ -701,6 +709,17 @@ void apply_rot(double *dx, double *dy, double cs, double sn) {
   *dx = t;
 }
 
+// UpdateGmresIterate's sum z_0 y_0 + ... + z_k y_k, formed in a zeroed vector
+// and then added to the iterate with Daxpy (src/FE/FgmresIte.C:229-247,
+// :464-477, :580-583): the same rounding as the reference
+void add_update(double *sol, const std::vector<std::vector<double>> &zv,
+                const std::vector<double> &y, int k, int N) {
+  std::vector<double> w(N, 0.0);
+  for (int j = 0; j <= k; ++j)
+    for (int t = 0; t < N; ++t) w[t] += zv[j][t] * y[j];
+  for (int t = 0; t < N; ++t) sol[t] += 1.0 * w[t];
+}
+
 }  // namespace
 
 extern "C" {
@@ -816,7 +835,7 @@ int oracle_fgmres(oracle *o, double *sol, const double *rhs, double *out) {
   std::vector<double> defect(N);
 
   defect_nse4(o, sol, rhs, v[0].data());
-  double res = std::sqrt(dot(v[0].data(), v[0].data(), N));
+  double res = std::sqrt(ddot(v[0].data(), v[0].data(), N));
   double res0 = res, beta = res;
   if (out) out[0] = res0;
   int maxite = maxit;
@@ -842,11 +861,11 @@ int oracle_fgmres(oracle *o, double *sol, const double *rhs, double *out) {
       vcycle(o, zv[i].data(), v[i].data());
       coupled_matvec(F, zv[i].data(), defect.data());
       for (int k = 0; k <= i; ++k) {
-        h(k, i) = dot(defect.data(), v[k].data(), N);
+        h(k, i) = ddot(defect.data(), v[k].data(), N);
         const double hk = h(k, i);
         for (int t = 0; t < N; ++t) defect[t] -= hk * v[k][t];
       }
-      h(i + 1, i) = std::sqrt(dot(defect.data(), defect.data(), N));
+      h(i + 1, i) = std::sqrt(ddot(defect.data(), defect.data(), N));
       v[i + 1] = defect;
       if (h(i + 1, i) != 0)
         for (int t = 0; t < N; ++t) v[i + 1][t] *= 1.0 / h(i + 1, i);
@@ -861,13 +880,12 @@ int oracle_fgmres(oracle *o, double *sol, const double *rhs, double *out) {
           y[r] /= h(r, r);
           for (int q = r - 1; q >= 0; --q) y[q] -= h(q, r) * y[r];
         }
-        for (int k = 0; k <= i; ++k)
-          for (int t = 0; t < N; ++t) sol[t] += zv[k][t] * y[k];
+        add_update(sol, zv, y, i, N);
         if (out) {
           out[1] = res;
           std::vector<double> r(N);
           defect_nse4(o, sol, rhs, r.data());
-          out[2] = std::sqrt(dot(r.data(), r.data(), N));
+          out[2] = std::sqrt(ddot(r.data(), r.data(), N));
         }
         return j;
       }
@@ -887,11 +905,10 @@ int oracle_fgmres(oracle *o, double *sol, const double *rhs, double *out) {
         y[r] /= h(r, r);
         for (int q = r - 1; q >= 0; --q) y[q] -= h(q, r) * y[r];
       }
-      for (int kk = 0; kk <= k; ++kk)
-        for (int t = 0; t < N; ++t) sol[t] += zv[kk][t] * y[kk];
+      add_update(sol, zv, y, k, N);
     }
     defect_nse4(o, sol, rhs, v[0].data());
-    res = std::sqrt(dot(v[0].data(), v[0].data(), N));
+    res = std::sqrt(ddot(v[0].data(), v[0].data(), N));
     res0 = res;
     beta = res;
   }
@@ -900,7 +917,7 @@ int oracle_fgmres(oracle *o, double *sol, const double *rhs, double *out) {
     out[1] = res;
     std::vector<double> r(N);
     defect_nse4(o, sol, rhs, r.data());
-    out[2] = std::sqrt(dot(r.data(), r.data(), N));
+    out[2] = std::sqrt(ddot(r.data(), r.data(), N));
   }
   return status_div ? -j : j;
 }

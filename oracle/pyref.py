@@ -1,6 +1,7 @@
 """ctypes front end of oracle/_ref/libref_harness.so: the reference's own
 Defect_NSE4 / MatVect_NSE4 / IntoL20Vector3D (src/FE/MGComponents3D.C:3210,
-:3030, :1756) run on one level of a problem built here.  TEST INFRASTRUCTURE
+:3030, :1756) and flexible FGMRES (TFgmresIte::Iterate, src/FE/FgmresIte.C:250)
+run on one level of a problem built here.  TEST INFRASTRUCTURE
 ONLY — it exists where the reference tree does (see build_ref_harness).
 """
 from __future__ import annotations
@@ -30,6 +31,10 @@ def ref_harness_lib():
         L.ref_defect_nse4.restype = None
         L.ref_matvec_nse4.argtypes = level + [_dp, _dp, C.c_int]
         L.ref_matvec_nse4.restype = None
+        L.ref_fgmres.argtypes = level + [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
+                                         C.c_double, C.c_double, C.c_int, C.c_void_p,
+                                         C.c_void_p, C.c_int]
+        L.ref_fgmres.restype = C.c_int
         L.ref_into_l20.argtypes = [_dp, C.c_int, C.c_int]
         L.ref_into_l20.restype = None
         _LIB = L
@@ -101,6 +106,24 @@ class RefLevel:
         y = np.empty(self.ndof)
         self._L.ref_matvec_nse4(*self._args, xp, y.ctypes.data_as(_dp), self.threads)
         return y
+
+    def fgmres_with_oracle_vcycle(self, oracle, sol, rhs) -> tuple[np.ndarray, int]:
+        """The reference's FGMRES on this level (which must be the oracle's
+        finest), preconditioned by the oracle's V-cycle (``oracle_vcycle``
+        called directly as the harness's C preconditioner), with the
+        oracle's restart / maxit / minit / red_factor / res_norm_min /
+        div_factor / project_pressure.  Returns (solution, iterations)."""
+        p = oracle.params
+        sol = np.array(sol, dtype=np.float64, copy=True)
+        rhs, rp = _d(rhs)
+        assert sol.size == self.ndof == rhs.size == oracle.ndof(-1)
+        fn = C.cast(oracle._L.oracle_vcycle, C.c_void_p)
+        it = self._L.ref_fgmres(*self._args, sol.ctypes.data_as(_dp), rp, p.restart, p.maxit,
+                                p.minit, p.red_factor, p.res_norm_min, p.div_factor,
+                                p.project_pressure, fn, C.c_void_p(oracle._h), self.threads)
+        if it < 0:
+            raise ValueError("ref_fgmres refused the parameters (div_factor < 1)")
+        return sol, it
 
 
 def ref_into_l20(v, order: int = -11) -> np.ndarray:

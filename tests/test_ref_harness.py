@@ -1,13 +1,18 @@
-"""The reference's own coupled-system kernels as the oracle's oracle.
+"""The reference's own coupled-system kernels and FGMRES as the oracle's oracle.
 
 oracle/ref_harness.cpp runs the reference's Defect_NSE4 (with the P1disc
-projection IntoL20Vector3D) and MatVect_NSE4 (src/FE/MGComponents3D.C:3210,
-:3030, :1756), compiled from the reference sources where they lie, on levels
-built here.  With the reference tree present the oracle's restatement must
-equal it bit for bit (same operation order, no contraction).  Its outputs are
-committed as tests/golden/ref_defect_*.npz, so that without the tree (and on
-the GPU) the oracle and the CUDA defect/mat-vec are still checked against
-the reference's numbers:
+projection IntoL20Vector3D), MatVect_NSE4 (src/FE/MGComponents3D.C:3210,
+:3030, :1756) and flexible FGMRES (TFgmresIte::Iterate, src/FE/FgmresIte.C:250),
+compiled from the reference sources where they lie, on levels built here.
+With the reference tree present the oracle's restatement must equal it bit
+for bit (same operation order, no contraction).  The reference's FGMRES is
+preconditioned by the oracle's V-cycle, so the FGMRES comparison pins the
+Krylov part (Arnoldi, Givens rotations, restarts, stopping rules, the
+solution update) while the V-cycle is pinned elsewhere.  The reference's
+defects and mat-vecs on one level of each mesh kind are committed as
+tests/golden/ref_defect_*.npz, so that without the tree (and on the GPU) the
+oracle and the CUDA defect/mat-vec are still checked against the
+reference's numbers:
 * the oracle: relative 1e-13 (builds on another platform may differ in the
   last bits of the assembled matrices);
 * the FP64 CUDA kernels: relative 1e-12 (summation order and FMA contraction
@@ -80,6 +85,65 @@ def test_reference_l20_projection_removes_the_constant_mode_mean():
     mask = np.arange(v.size) % 4 != 0
     assert np.array_equal(w[mask], v[mask])
     assert np.allclose(w[::4] - v[::4], -v[::4].mean())
+
+
+FGMRES_CASES = {
+    # converges within the first restart cycle, default parameters
+    "hexa": (dict(n_levels=3, nu=1e-2, seed=0), dict(), False),
+    # stops at maxit = 3 restart cycles
+    "hexa-maxit": (dict(n_levels=3, nu=1e-2, seed=0),
+                   dict(restart=3, maxit=9, red_factor=0.0, res_norm_min=1e-30), False),
+    # stopping by minit from a nonzero start, res_norm_min reached at once
+    "hexa-minit": (dict(n_levels=3, nu=1e-2, seed=1),
+                   dict(restart=4, maxit=30, minit=6, res_norm_min=1e3), True),
+    "channel": (dict(n_levels=2, nu=0.1, seed=0, example="channel", periodic="xz",
+                     stretch_y=1.5, box=(0.0, 6.0, -1.0, 1.0, 0.0, 3.0)),
+                dict(restart=10, maxit=60, red_factor=1e-8), False),
+    "tetra": (dict(n_levels=2, nu=1.0, seed=0, example="quadlin_oseen", element="tetra"),
+              dict(restart=8, maxit=40, red_factor=1e-9, res_norm_min=0.0), False),
+}
+
+
+def fgmres_pair(problem_kw, oracle_kw, nonzero_start):
+    from oracle.pyref import RefLevel
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    P = OseenProblem(**problem_kw)
+    O = Oracle(P, **oracle_kw)
+    R = RefLevel(P.arrays(P.n_levels - 1), threads=2)
+    rhs = P.rhs()
+    x0 = (np.random.default_rng(5).standard_normal(rhs.size) if nonzero_start
+          else np.zeros_like(rhs))
+    x_o, info = O.iterate(x0, rhs)
+    x_r, it = R.fgmres_with_oracle_vcycle(O, x0, rhs)
+    return P, O, rhs, x_o, info, x_r, it
+
+
+@pytest.mark.parametrize("case", list(FGMRES_CASES))
+def test_oracle_fgmres_equals_reference_fgmres_bitwise(case):
+    ref_lib_or_skip()
+    _, _, _, x_o, info, x_r, it = fgmres_pair(*FGMRES_CASES[case])
+    assert info["iterations"] == it
+    assert np.array_equal(x_o, x_r)
+
+
+def test_partial_last_cycle_is_the_documented_deviation():
+    """When maxit ends a restart cycle after i < restart steps, the reference
+    back-solves with restart-1 columns (src/FE/FgmresIte.C:580), i.e. with
+    Hessenberg columns left from the previous cycle; the oracle uses the i
+    columns of this cycle.  Up to the last whole cycle both agree bit for bit,
+    and the oracle's answer does not lose what that cycle gained."""
+    ref_lib_or_skip()
+    pk = dict(n_levels=2, nu=1e-3, seed=2)
+    ok = dict(restart=4, red_factor=1e-14, res_norm_min=0.0)
+    P, O8, rhs, x8, info8, x8r, it8 = fgmres_pair(pk, dict(ok, maxit=8), True)
+    assert it8 == info8["iterations"] == 8 and np.array_equal(x8, x8r)
+    _, O10, _, x10, info10, x10r, it10 = fgmres_pair(pk, dict(ok, maxit=10), True)
+    assert it10 == info10["iterations"] == 10
+    assert not np.array_equal(x10, x10r)
+    level = P.n_levels - 1
+    res8 = np.linalg.norm(O8.coupled_defect(level, x8, rhs))
+    res10 = np.linalg.norm(O10.coupled_defect(level, x10, rhs))
+    assert res10 <= res8 * (1 + 1e-12)
 
 
 @pytest.mark.parametrize("name", CASES)
