@@ -31,6 +31,8 @@ def ref_harness_lib():
         L.ref_defect_nse4.restype = None
         L.ref_matvec_nse4.argtypes = level + [_dp, _dp, C.c_int]
         L.ref_matvec_nse4.restype = None
+        L.ref_nse2.argtypes = level + [_dp, _dp, _dp, C.c_int, C.c_int]
+        L.ref_nse2.restype = None
         L.ref_fgmres.argtypes = level + [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
                                          C.c_double, C.c_double, C.c_int, C.c_void_p,
                                          C.c_void_p, C.c_int]
@@ -105,6 +107,24 @@ class RefLevel:
         assert x.size == self.ndof
         y = np.empty(self.ndof)
         self._L.ref_matvec_nse4(*self._args, xp, y.ctypes.data_as(_dp), self.threads)
+        return y
+
+    def defect_nse2(self, x, b, project: bool) -> np.ndarray:
+        """Defect_NSE2: the one-block (NSTYPE-2) defect with a[0] as the A
+        matrix of every velocity component."""
+        x, xp = _d(x)
+        b, bp = _d(b)
+        assert x.size == self.ndof and b.size == self.ndof
+        r = np.empty(self.ndof)
+        self._L.ref_nse2(*self._args, xp, bp, r.ctypes.data_as(_dp), int(project), self.threads)
+        return r
+
+    def matvec_nse2(self, x) -> np.ndarray:
+        """MatVect_NSE2 with a[0] as the one A matrix."""
+        x, xp = _d(x)
+        assert x.size == self.ndof
+        y = np.empty(self.ndof)
+        self._L.ref_nse2(*self._args, xp, None, y.ctypes.data_as(_dp), 0, self.threads)
         return y
 
     def fgmres_with_oracle_vcycle(self, oracle, sol, rhs) -> tuple[np.ndarray, int]:

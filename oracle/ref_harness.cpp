@@ -9,7 +9,9 @@
 // reference tree by oracle/build_oracle.py (build_ref_harness):
 //   src/FE/MGComponents3D.C  Defect_NSE4 (:3210), MatVect_NSE4 (:3030),
 //                            CoupledDefect (:3038), CoupledMatVect (:2872),
-//                            IntoL20Vector3D (:1756)
+//                            the NSTYPE-2 Defect_NSE2 (:2560), MatVect_NSE2
+//                            (:2439), CoupledDefect (:2446), CoupledMatVect
+//                            (:2329), and IntoL20Vector3D (:1756)
 //   src/FE/FgmresIte.C       TFgmresIte (constructor :75, flexible branch of
 //                            Iterate :250-677, Dotprod :857, the plane
 //                            rotations and UpdateGmresIterate :199-247)
@@ -90,15 +92,16 @@ struct Level {
   TMatrix *B[6];  // B1, B2, B3 (pressure rows), B1T, B2T, B3T (velocity rows)
 };
 
+// n_a = 9 (NSTYPE 4: A11..A33) or 1 (NSTYPE 2: one A for all components)
 Level make_level(int n_u, int n_active, int n_p, const int *a_rowptr, const int *a_col,
                  const double *const *a, const int *b_rowptr, const int *b_col,
                  const double *const *b, const int *bt_rowptr, const int *bt_col,
-                 const double *const *bt) {
-  Level L;
+                 const double *const *bt, int n_a = 9) {
+  Level L{};
   const int a_nnz = a_rowptr[n_u], b_nnz = b_rowptr[n_p], bt_nnz = bt_rowptr[n_u];
   TSquareStructure *sa = new ActiveStructure(n_u, n_active, a_nnz, copy_of(a_col, a_nnz),
                                              copy_of(a_rowptr, n_u + 1L));
-  for (int k = 0; k < 9; ++k) {
+  for (int k = 0; k < n_a; ++k) {
     L.A[k] = new TSquareMatrix(sa);
     std::memcpy(L.A[k]->GetEntries(), a[k], sizeof(double) * a_nnz);
   }
@@ -168,6 +171,29 @@ __attribute__((visibility("default"))) void ref_matvec_nse4(
                        bt_col, bt);
   double *xx = copy_of(x, 3L * n_u + n_p);
   MatVect_NSE4(L.A, L.B, xx, y);
+  delete[] xx;
+}
+
+// The NSTYPE-2 pair: r = b - K x through Defect_NSE2 (projection as above)
+// or y = K x through MatVect_NSE2 (when rhs is null), with a[0] the one A
+// matrix of all three velocity components.
+__attribute__((visibility("default"))) void ref_nse2(
+    int n_u, int n_active, int n_p, const int *a_rowptr, const int *a_col,
+    const double *const *a, const int *b_rowptr, const int *b_col, const double *const *b,
+    const int *bt_rowptr, const int *bt_col, const double *const *bt, const double *x,
+    const double *rhs, double *out, int project, int threads) {
+  set_params(threads, project);
+  Level L = make_level(n_u, n_active, n_p, a_rowptr, a_col, a, b_rowptr, b_col, b, bt_rowptr,
+                       bt_col, bt, 1);
+  const long n = 3L * n_u + n_p;
+  double *xx = copy_of(x, n);
+  if (rhs) {
+    double *bb = copy_of(rhs, n);
+    Defect_NSE2(L.A, L.B, xx, bb, out);
+    delete[] bb;
+  } else {
+    MatVect_NSE2(L.A, L.B, xx, out);
+  }
   delete[] xx;
 }
 

@@ -74,6 +74,32 @@ def test_oracle_equals_reference_kernels_bitwise(kwargs):
         assert np.array_equal(R.matvec(x), O.matvec(level, x))
 
 
+def test_one_block_levels_equal_the_reference_nstype2_kernels_bitwise():
+    """On a one-block problem (A12..A32 = 0 on active rows, A11 = A22 = A33)
+    the reference's NSTYPE-2 Defect_NSE2 / MatVect_NSE2 with the single A
+    equal the oracle's nine-block defect and mat-vec bit for bit, and they
+    reproduce the NSTYPE-4 golden vectors of the hexahedral case."""
+    ref_lib_or_skip()
+    from oracle.pyref import RefLevel
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    P = OseenProblem(n_levels=3, nu=1e-2, seed=0)
+    assert P.is_one_block()
+    O = Oracle(P)
+    rng = np.random.default_rng(12)
+    for level in range(P.n_levels):
+        R = RefLevel(P.arrays(level), threads=2)
+        x, b = rng.standard_normal(R.ndof), rng.standard_normal(R.ndof)
+        for project in (False, True):
+            assert np.array_equal(R.defect_nse2(x, b, project),
+                                  O.coupled_defect(level, x, b, project))
+        assert np.array_equal(R.matvec_nse2(x), O.matvec(level, x))
+    P, level, x, b, g = load_case("hexa")
+    assert P.is_one_block()
+    R = RefLevel(P.arrays(level), threads=1)
+    assert np.array_equal(R.defect_nse2(x, b, True), g["r_project"])
+    assert np.array_equal(R.matvec_nse2(x), g["y"])
+
+
 def test_reference_l20_projection_removes_the_constant_mode_mean():
     """IntoL20Vector3D(., ., -11) leaves every 4th entry (the P1disc
     constant modes) with zero mean and the other entries untouched."""
@@ -173,6 +199,19 @@ def test_gpu_defect_and_matvec_match_reference_fixtures(name):
     from to_merge_master_parmoon_gb300 import PmSolver
     P, level, x, b, g = load_case(name)
     S = PmSolver(P.descs, precision="fp64")
+    assert rel(S.coupled_defect(level, x, b, True), g["r_project"]) < 1e-12
+    assert rel(S.coupled_defect(level, x, b, False), g["r_plain"]) < 1e-12
+    assert rel(S.matvec(level, x), g["y"]) < 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_one_block_defect_and_matvec_match_reference_fixture():
+    """The NSTYPE-2 (one A array) CUDA path against the reference's numbers
+    for the hexahedral case, whose system is one-block."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, x, b, g = load_case("hexa")
+    assert P.is_one_block()
+    S = PmSolver(P.descs_one_block(), precision="fp64")
     assert rel(S.coupled_defect(level, x, b, True), g["r_project"]) < 1e-12
     assert rel(S.coupled_defect(level, x, b, False), g["r_plain"]) < 1e-12
     assert rel(S.matvec(level, x), g["y"]) < 1e-12
