@@ -18,6 +18,7 @@ reference's numbers:
 * the FP64 CUDA kernels: relative 1e-12 (summation order and FMA contraction
   differ).
 """
+import importlib.util
 import json
 from pathlib import Path
 
@@ -42,14 +43,24 @@ def ref_lib_or_skip():
     return lib
 
 
+def _golden_module():
+    """tests/golden/make_ref_defect_golden.py, loaded by path (its inputs and
+    problem constructor are shared with the generator)."""
+    spec = importlib.util.spec_from_file_location("make_ref_defect_golden",
+                                                  GOLD / "make_ref_defect_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def load_case(name):
-    from tests.golden.make_ref_defect_golden import build_problem, golden_inputs
+    gm = _golden_module()
     g = np.load(GOLD / f"ref_defect_{name}.npz")
-    P = build_problem(json.loads(str(g["problem"])))
+    P = gm.build_problem(json.loads(str(g["problem"])))
     level = int(g["level"])
     assert P.arrays(level)["n_udof"] == int(g["n_udof"])
     assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
-    x, b = golden_inputs(P.ndof(level))
+    x, b = gm.golden_inputs(P.ndof(level))
     return P, level, x, b, g
 
 
