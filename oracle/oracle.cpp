@@ -711,7 +711,7 @@ void apply_rot(double *dx, double *dy, double cs, double sn) {
 
 // UpdateGmresIterate's sum z_0 y_0 + ... + z_k y_k, formed in a zeroed vector
 // and then added to the iterate with Daxpy (src/FE/FgmresIte.C:229-247,
-// :464-477, :580-583): the same rounding as the reference
+// :480-490, :574-577): the same rounding as the reference
 void add_update(double *sol, const std::vector<std::vector<double>> &zv,
                 const std::vector<double> &y, int k, int N) {
   std::vector<double> w(N, 0.0);
@@ -897,7 +897,7 @@ int oracle_fgmres(oracle *o, double *sol, const double *rhs, double *out) {
     if (status_div) break;
     {
       // the reference always back-solves with restart-1 columns
-      // (src/FE/FgmresIte.C:580); when the loop ended early at maxit only
+      // (src/FE/FgmresIte.C:575); when the loop ended early at maxit only
       // the first i columns of H belong to this cycle, so use those.
       std::vector<double> y(s.begin(), s.end());
       const int k = i - 1;

@@ -36,7 +36,7 @@
 //   and its destructor frees the auxiliary arrays, so the FGMRES object and
 //   the preconditioner are not destroyed either.
 // * FGMRES calls exit(4711) when a residual exceeds div_factor times the
-//   residual at the start of its restart cycle (src/FE/FgmresIte.C:585-588).
+//   residual at the start of its restart cycle (src/FE/FgmresIte.C:564-566).
 //   The GMRES residual never grows within a cycle, so a div_factor >= 1
 //   keeps that branch closed.  ref_fgmres refuses a smaller one.
 // * The active bound of a TSquareStructure is the row count in the
@@ -117,7 +117,7 @@ Level make_level(int n_u, int n_active, int n_p, const int *a_rowptr, const int 
 }
 
 // A preconditioner given as a C function z = M^{-1} v (z starts at zero, as
-// FGMRES clears it before prec->Iterate, src/FE/FgmresIte.C:371-378).
+// FGMRES clears it before prec->Iterate, src/FE/FgmresIte.C:372-389).
 typedef void (*prec_fn)(void *ctx, double *z, const double *v);
 
 struct CallbackPrec : public TItMethod {

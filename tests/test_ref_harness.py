@@ -165,7 +165,7 @@ def test_oracle_fgmres_equals_reference_fgmres_bitwise(case):
 
 def test_partial_last_cycle_is_the_documented_deviation():
     """When maxit ends a restart cycle after i < restart steps, the reference
-    back-solves with restart-1 columns (src/FE/FgmresIte.C:580), i.e. with
+    back-solves with restart-1 columns (src/FE/FgmresIte.C:575), i.e. with
     Hessenberg columns left from the previous cycle; the oracle uses the i
     columns of this cycle.  Up to the last whole cycle both agree bit for bit,
     and the oracle's answer does not lose what that cycle gained."""
