@@ -26,16 +26,18 @@ def ref_harness_lib():
         if path is None:
             return None
         L = C.CDLL(str(path))
-        level = [C.c_int, C.c_int, C.c_int, _ip, _ip, _dpp, _ip, _ip, _dpp, _ip, _ip, _dpp]
-        L.ref_defect_nse4.argtypes = level + [_dp, _dp, _dp, C.c_int, C.c_int]
-        L.ref_defect_nse4.restype = None
-        L.ref_matvec_nse4.argtypes = level + [_dp, _dp, C.c_int]
-        L.ref_matvec_nse4.restype = None
-        L.ref_nse2.argtypes = level + [_dp, _dp, _dp, C.c_int, C.c_int]
-        L.ref_nse2.restype = None
-        L.ref_fgmres.argtypes = level + [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
-                                         C.c_double, C.c_double, C.c_int, C.c_void_p,
-                                         C.c_void_p, C.c_int]
+        L.ref_level_create.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _dpp, _ip, _ip, _dpp,
+                                       _ip, _ip, _dpp]
+        L.ref_level_create.restype = C.c_void_p
+        L.ref_level_destroy.argtypes = [C.c_void_p]
+        L.ref_level_destroy.restype = None
+        L.ref_defect.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int, C.c_int]
+        L.ref_defect.restype = None
+        L.ref_matvec.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int]
+        L.ref_matvec.restype = None
+        L.ref_fgmres.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
+                                 C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p,
+                                 C.c_int]
         L.ref_fgmres.restype = C.c_int
         L.ref_into_l20.argtypes = [_dp, C.c_int, C.c_int]
         L.ref_into_l20.restype = None
@@ -54,14 +56,15 @@ def _d(a):
 
 
 class RefLevel:
-    """One level (the dict of ``OseenProblem.arrays``) handed to the
-    reference's kernels."""
+    """One level (the dict of ``OseenProblem.arrays``) built as the
+    reference's matrix objects (copied once; freed with this object)."""
 
     def __init__(self, arrays: dict, threads: int = 1):
         L = ref_harness_lib()
         if L is None:
             raise RuntimeError("reference tree not present: the reference harness is not built")
         self._L = L
+        self._h = None
         self.threads = threads
         self.n_u, self.n_p = int(arrays["n_udof"]), int(arrays["n_pdof"])
         self.n_active = int(arrays["n_active"])
@@ -81,51 +84,54 @@ class RefLevel:
             keep.append(ptrs)
             return C.cast(ptrs, _dpp)
 
-        self._args = [self.n_u, self.n_active, self.n_p,
-                      ip(arrays["a_rowptr"]), ip(arrays["a_col"]), dpp(arrays["a"]),
-                      ip(arrays["b_rowptr"]), ip(arrays["b_col"]), dpp(arrays["b"]),
-                      ip(arrays["bt_rowptr"]), ip(arrays["bt_col"]), dpp(arrays["bt"])]
-        self._keep = keep
+        self._h = L.ref_level_create(
+            self.n_u, self.n_active, self.n_p,
+            ip(arrays["a_rowptr"]), ip(arrays["a_col"]), dpp(arrays["a"]),
+            ip(arrays["b_rowptr"]), ip(arrays["b_col"]), dpp(arrays["b"]),
+            ip(arrays["bt_rowptr"]), ip(arrays["bt_col"]), dpp(arrays["bt"]))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.ref_level_destroy(self._h)
+            self._h = None
 
     @property
     def ndof(self) -> int:
         return 3 * self.n_u + self.n_p
 
-    def defect(self, x, b, project: bool) -> np.ndarray:
-        """r = b - K x; the pressure part projected into L2_0 (P1disc) when
-        ``project``, as Defect_NSE4 does under INTERNAL_PROJECT_PRESSURE."""
+    def _defect(self, nstype, x, b, project):
         x, xp = _d(x)
         b, bp = _d(b)
         assert x.size == self.ndof and b.size == self.ndof
         r = np.empty(self.ndof)
-        self._L.ref_defect_nse4(*self._args, xp, bp, r.ctypes.data_as(_dp), int(project),
-                                self.threads)
+        self._L.ref_defect(self._h, nstype, xp, bp, r.ctypes.data_as(_dp), int(project),
+                           self.threads)
         return r
+
+    def _matvec(self, nstype, x):
+        x, xp = _d(x)
+        assert x.size == self.ndof
+        y = np.empty(self.ndof)
+        self._L.ref_matvec(self._h, nstype, xp, y.ctypes.data_as(_dp), self.threads)
+        return y
+
+    def defect(self, x, b, project: bool) -> np.ndarray:
+        """r = b - K x through Defect_NSE4; the pressure part projected into
+        L2_0 (P1disc) when ``project``, as under INTERNAL_PROJECT_PRESSURE."""
+        return self._defect(4, x, b, project)
 
     def matvec(self, x) -> np.ndarray:
-        x, xp = _d(x)
-        assert x.size == self.ndof
-        y = np.empty(self.ndof)
-        self._L.ref_matvec_nse4(*self._args, xp, y.ctypes.data_as(_dp), self.threads)
-        return y
+        """y = K x through MatVect_NSE4."""
+        return self._matvec(4, x)
 
     def defect_nse2(self, x, b, project: bool) -> np.ndarray:
-        """Defect_NSE2: the one-block (NSTYPE-2) defect with a[0] as the A
+        """Defect_NSE2: the one-block (NSTYPE-2) defect with A11 as the A
         matrix of every velocity component."""
-        x, xp = _d(x)
-        b, bp = _d(b)
-        assert x.size == self.ndof and b.size == self.ndof
-        r = np.empty(self.ndof)
-        self._L.ref_nse2(*self._args, xp, bp, r.ctypes.data_as(_dp), int(project), self.threads)
-        return r
+        return self._defect(2, x, b, project)
 
     def matvec_nse2(self, x) -> np.ndarray:
-        """MatVect_NSE2 with a[0] as the one A matrix."""
-        x, xp = _d(x)
-        assert x.size == self.ndof
-        y = np.empty(self.ndof)
-        self._L.ref_nse2(*self._args, xp, None, y.ctypes.data_as(_dp), 0, self.threads)
-        return y
+        """MatVect_NSE2 with A11 as the one A matrix."""
+        return self._matvec(2, x)
 
     def fgmres_with_oracle_vcycle(self, oracle, sol, rhs) -> tuple[np.ndarray, int]:
         """The reference's FGMRES on this level (which must be the oracle's
@@ -138,7 +144,7 @@ class RefLevel:
         rhs, rp = _d(rhs)
         assert sol.size == self.ndof == rhs.size == oracle.ndof(-1)
         fn = C.cast(oracle._L.oracle_vcycle, C.c_void_p)
-        it = self._L.ref_fgmres(*self._args, sol.ctypes.data_as(_dp), rp, p.restart, p.maxit,
+        it = self._L.ref_fgmres(self._h, sol.ctypes.data_as(_dp), rp, p.restart, p.maxit,
                                 p.minit, p.red_factor, p.res_norm_min, p.div_factor,
                                 p.project_pressure, fn, C.c_void_p(oracle._h), self.threads)
         if it < 0:
