@@ -4,12 +4,11 @@
 * ``oracle/_ref/ref_basis_pin``  — the reference's own basis-function headers
   compiled where they lie under the reference tree (only when that tree is
   present; its output is committed as tests/golden/basis_q2_p1.json).
-* ``oracle/_ref/libref_harness.so`` — the reference's coupled-system kernels
-  and its flexible FGMRES (src/FE/MGComponents3D.C, src/FE/FgmresIte.C and
-  src/FE/ItMethod.C, with the matrix classes of src/FE/Matrix.C,
-  SquareMatrix.C, Structure.C, SquareStructure.C and src/FE/Blas1.C) compiled
-  where they lie, driven by ref_harness.cpp (only when the tree is present;
-  its outputs are committed as tests/golden/ref_defect_*.npz).
+* ``oracle/_ref/libref_harness.so`` — the reference's coupled-system kernels,
+  its flexible FGMRES and its cell Vanka (the translation units of
+  REF_HARNESS_TUS below) compiled where they lie, driven by ref_harness.cpp
+  and ref_vanka.cpp (only when the tree is present; the defect outputs are
+  committed as tests/golden/ref_defect_*.npz).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 what this builds.
@@ -57,8 +56,11 @@ def build_ref_pin() -> Path | None:
 
 
 # reference translation units of the harness, compiled where they lie
-REF_HARNESS_TUS = ("MGComponents3D", "FgmresIte", "ItMethod", "Matrix", "SquareMatrix",
-                   "Structure", "SquareStructure", "Blas1")
+REF_HARNESS_TUS = ("FE/MGComponents3D", "FE/FgmresIte", "FE/ItMethod", "FE/Matrix",
+                   "FE/SquareMatrix", "FE/Structure", "FE/SquareStructure", "FE/Blas1",
+                   "FE/NSE_MGLevel4", "FE/NSE_MGLevel", "FE/LinAlg", "FE/FESpace",
+                   "FE/FESpace3D", "FE/FE3D", "FE/Structure3D", "FE/SquareStructure3D",
+                   "FE/SquareMatrix3D", "FE/Matrix3D", "Geometry/Collection")
 REF_INCLUDE_DIRS = ("General", "FE", "Geometry", "FE3D", "FE2D", "FE1D", "System",
                     "QuadFormulas", "Parallel", "AMG")
 
@@ -69,26 +71,29 @@ def build_ref_harness() -> Path | None:
     are built with hidden symbols and function sections so that the link
     (``--gc-sections``) keeps only what the harness reaches, and ``-z defs``
     proves nothing it keeps is unresolved.  Returns None without the tree."""
-    src = REFERENCE / "src" / "FE"
+    src = REFERENCE / "src"
     if not all((src / f"{t}.C").exists() for t in REF_HARNESS_TUS):
         return None
     objdir = REF_OUT / "harness_obj"
     objdir.mkdir(parents=True, exist_ok=True)
     out = REF_OUT / "libref_harness.so"
-    mine = [HERE / "ref_harness.cpp", HERE / "ref_stubs" / "mkl_spblas.h",
-            HERE / "ref_stubs" / "mkl_types.h", Path(__file__)]
+    mine = [HERE / "ref_harness.cpp", HERE / "ref_vanka.cpp", Path(__file__),
+            *sorted((HERE / "ref_stubs").glob("*.h"))]
     if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in mine):
         return out
-    inc = ["-D__3D__", f"-I{HERE / 'ref_stubs'}"]
+    # _SEQ: the reference's sequential build, whose cell Vanka the oracle restates
+    inc = ["-D__3D__", "-D_SEQ", f"-I{HERE / 'ref_stubs'}"]
     inc += [f"-I{REFERENCE / 'include' / d}" for d in REF_INCLUDE_DIRS]
-    # include/FE/NSE_MGLevel.h (reached from FgmresIte.C) includes the CUDA
-    # runtime headers; declarations only, nothing of them is linked
+    # include/FE/NSE_MGLevel.h (reached from FgmresIte.C and NSE_MGLevel4.C)
+    # includes the CUDA runtime headers; declarations only, nothing of them
+    # is linked
     cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
     inc += ["-isystem", str(cuda_inc)]
     flags = ["g++", "-O2", "-std=c++11", "-fPIC", "-fopenmp", "-w", "-ffp-contract=off",
              "-ffunction-sections", "-fdata-sections", "-fvisibility=hidden"]
-    jobs = [(src / f"{t}.C", objdir / f"{t}.o") for t in REF_HARNESS_TUS]
+    jobs = [(src / f"{t}.C", objdir / f"{Path(t).name}.o") for t in REF_HARNESS_TUS]
     jobs.append((HERE / "ref_harness.cpp", objdir / "ref_harness.o"))
+    jobs.append((HERE / "ref_vanka.cpp", objdir / "ref_vanka.o"))
     procs = [(subprocess.Popen([*flags, *inc, "-c", str(s), "-o", str(o)], stdout=subprocess.PIPE,
                                stderr=subprocess.STDOUT, text=True), s) for s, o in jobs]
     for pr, s in procs:

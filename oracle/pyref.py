@@ -1,7 +1,8 @@
 """ctypes front end of oracle/_ref/libref_harness.so: the reference's own
 Defect_NSE4 / MatVect_NSE4 / IntoL20Vector3D (src/FE/MGComponents3D.C:3210,
 :3030, :1756) and flexible FGMRES (TFgmresIte::Iterate, src/FE/FgmresIte.C:250)
-run on one level of a problem built here.  TEST INFRASTRUCTURE
+and cell Vanka (TNSE_MGLevel4::CellVanka, src/FE/NSE_MGLevel4.C:1653) run on
+one level of a problem built here.  TEST INFRASTRUCTURE
 ONLY — it exists where the reference tree does (see build_ref_harness).
 """
 from __future__ import annotations
@@ -41,6 +42,14 @@ def ref_harness_lib():
         L.ref_fgmres.restype = C.c_int
         L.ref_into_l20.argtypes = [_dp, C.c_int, C.c_int]
         L.ref_into_l20.restype = None
+        L.ref_vanka_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip,
+                                       _ip, _ip, _dpp, _ip, _ip, _dpp, _ip, _ip, _dpp,
+                                       C.c_double]
+        L.ref_vanka_create.restype = C.c_void_p
+        L.ref_vanka_destroy.argtypes = [C.c_void_p]
+        L.ref_vanka_destroy.restype = None
+        L.ref_vanka_sweeps.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double]
+        L.ref_vanka_sweeps.restype = None
         _LIB = L
     return _LIB
 
@@ -150,6 +159,61 @@ class RefLevel:
         if it < 0:
             raise ValueError("ref_fgmres refused the parameters (div_factor < 1)")
         return sol, it
+
+
+class RefVankaLevel:
+    """One level (the dict of ``OseenProblem.arrays``) as the reference's
+    TNSE_MGLevel4 in its sequential build, for its cell Vanka
+    (src/FE/NSE_MGLevel4.C:1653-2087, run by oracle/ref_vanka.cpp)."""
+
+    def __init__(self, arrays: dict, alpha: float = 1.0):
+        L = ref_harness_lib()
+        if L is None:
+            raise RuntimeError("reference tree not present: the reference harness is not built")
+        self._L = L
+        self._h = None
+        self.n_u, self.n_p = int(arrays["n_udof"]), int(arrays["n_pdof"])
+        udofs = np.ascontiguousarray(arrays["cell_udofs"], dtype=np.int32)
+        pdofs = np.ascontiguousarray(arrays["cell_pdofs"], dtype=np.int32)
+        n_cells, nu_loc = udofs.shape
+        keep = [udofs, pdofs]
+
+        def ip(a):
+            a, p = _i(a)
+            keep.append(a)
+            return p
+
+        def dpp(arrs):
+            ptrs = (_dp * len(arrs))()
+            for k, a in enumerate(arrs):
+                a, p = _d(a)
+                keep.append(a)
+                ptrs[k] = p
+            keep.append(ptrs)
+            return C.cast(ptrs, _dpp)
+
+        self._h = L.ref_vanka_create(
+            self.n_u, int(arrays["n_active"]), self.n_p, n_cells, nu_loc,
+            udofs.ctypes.data_as(_ip), pdofs.ctypes.data_as(_ip),
+            ip(arrays["a_rowptr"]), ip(arrays["a_col"]), dpp(arrays["a"]),
+            ip(arrays["b_rowptr"]), ip(arrays["b_col"]), dpp(arrays["b"]),
+            ip(arrays["bt_rowptr"]), ip(arrays["bt_col"]), dpp(arrays["bt"]), float(alpha))
+        if not self._h:
+            raise ValueError(f"unsupported local velocity size {nu_loc}")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.ref_vanka_destroy(self._h)
+            self._h = None
+
+    def cell_vanka(self, u, rhs, sweeps: int = 1, damp: float = 1.0) -> np.ndarray:
+        """``sweeps`` reference CellVanka sweeps from ``u`` (a copy is
+        returned) with damping ``damp``."""
+        u = np.array(u, dtype=np.float64, copy=True)
+        rhs, rp = _d(rhs)
+        assert u.size == rhs.size == 3 * self.n_u + self.n_p
+        self._L.ref_vanka_sweeps(self._h, u.ctypes.data_as(_dp), rp, sweeps, damp)
+        return u
 
 
 def ref_into_l20(v, order: int = -11) -> np.ndarray:

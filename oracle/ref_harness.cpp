@@ -3,7 +3,7 @@
 // INFRASTRUCTURE ONLY: it pins the oracle's restatement (oracle.cpp:
 // coupled_defect, coupled_matvec, into_l20, oracle_fgmres) against the
 // reference code itself, and generates the golden vectors
-// tests/golden/ref_defect_*.npz (tests/golden/make_ref_defect_golden.py).
+// tests/golden/ref_defect_*.npz (tests/golden/make_ref_golden.py).
 //
 // The reference translation units are compiled where they lie in the
 // reference tree by oracle/build_oracle.py (build_ref_harness):

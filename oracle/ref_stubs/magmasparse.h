@@ -1,0 +1,6 @@
+// Stand-in for magmasparse.h, which the reference's NSE_MGLevel4 sources include
+// without using anything from it on the harness's path.  TEST
+// INFRASTRUCTURE ONLY.
+#ifndef REF_STUB_MAGMASPARSE_H
+#define REF_STUB_MAGMASPARSE_H
+#endif

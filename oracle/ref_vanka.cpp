@@ -1,0 +1,359 @@
+// ref_vanka.cpp — runs the reference's own cell Vanka smoother on a level
+// handed over as plain arrays.  TEST INFRASTRUCTURE ONLY: it pins the
+// oracle's cell_vanka (sequential mode) against the reference code itself.
+// Linked into oracle/_ref/libref_harness.so with ref_harness.cpp by
+// oracle/build_oracle.py (build_ref_harness), with -D__3D__ -D_SEQ (the
+// reference's sequential build; the _SEQ cell loop is the one the oracle
+// restates).
+//
+// Reference code that runs here:
+//   src/FE/NSE_MGLevel4.C    TNSE_MGLevel4 constructor (:119-328) and the _SEQ
+//                            CellVanka (:1653-2087): local 85x85 (or 49x49)
+//                            systems from the global matrices, the direct
+//                            local solve, the damped update, the relaxation
+//                            and the Dirichlet values
+//   src/FE/NSE_MGLevel.C     TNSE_MGLevel constructor, SetHangingNodes
+//   src/FE/FESpace.C, FESpace3D.C, src/Geometry/Collection.C, src/FE/FE3D.C,
+//   SquareStructure3D.C, SquareMatrix3D.C, Matrix3D.C, Structure3D.C
+//                            the space, collection, element and matrix
+//                            objects the level reads through
+//   src/FE/LinAlg.C          SolveLinearSystemLapack (:106-131)
+//
+// What the harness supplies instead of the mesh and FE machinery:
+// * LevelSpace: a TFESpace3D whose DOF maps (GlobalNumbers, BeginIndex), DOF
+//   count, active / hanging / Dirichlet bounds and per-cell element ids
+//   (AllElements, which TFESpace3D::GetFE3D returns before it would look at
+//   a cell, src/FE/FESpace3D.C:412-422) are set from the level's arrays.
+//   There are no hanging nodes.  The collection's cell array holds null
+//   pointers: code on this path reads the array but no cell.
+// * TFEDatabase3D::FEs3D: storage for the element table, whose two used
+//   entries are registered (RegisterFE3D) as elements with 27 (or 15) and 4
+//   local DOFs (TFE3D::GetN_DOF is all the level asks of them).
+// * LevelStructure: a TStructure3D built from two spaces on different
+//   collections, for which its constructor returns at once
+//   (src/FE/Structure3D.C:43-46), then given the B / BT pattern and the
+//   level's spaces.
+// * dgetrf_ / dgetrs_ (called by SolveLinearSystemLapack): LAPACK's
+//   unblocked right-looking LU with partial pivoting (first maximal |a|,
+//   multipliers scaled by the reciprocal of the pivot) and the two
+//   triangular solves.  The arithmetic is the same as the oracle's
+//   lu_factor / lu_solve.  The reference links MKL, whose blocking rounds
+//   differently, so the rounding of LAPACK itself is not pinned here (the
+//   oracle's LU is checked against scipy's LAPACK instead).
+// * DirectSolver, which SolveExact calls, stops the process if reached (it
+//   is not).  The Magma_Solver of the level exists only in CUDA builds.
+// As in ref_harness.cpp, no reference destructor runs.  The level lives in
+// storage the harness owns, and the harness frees what it allocated.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include <Collection.h>
+#include <Database.h>
+#include <DirectSolver.h>
+#include <FE3D.h>
+#include <FEDatabase3D.h>
+#include <FESpace3D.h>
+#include <Matrix3D.h>
+#include <NSE_MGLevel4.h>  // includes Magma_Solver.h (no include guard)
+#include <SquareMatrix3D.h>
+#include <SquareStructure3D.h>
+#include <Structure3D.h>
+
+TFE3D *TFEDatabase3D::FEs3D[N_FEs3D] = {nullptr};
+
+void DirectSolver(TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *,
+                  TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *,
+                  TSquareMatrix3D *, TMatrix3D *, TMatrix3D *, TMatrix3D *, TMatrix3D *,
+                  TMatrix3D *, TMatrix3D *, double *, double *, int) {
+  std::fprintf(stderr, "ref_vanka: DirectSolver is not part of the harness\n");
+  std::abort();
+}
+
+extern "C" {
+void dgetrf_(int *m, int *n, double *a, int *lda, int *ipiv, int *info) {
+  const int N = *n, ld = *lda;
+  *info = 0;
+  if (*m != N) {
+    *info = -1;
+    return;
+  }
+  for (int k = 0; k < N; ++k) {
+    int p = k;
+    double amax = std::fabs(a[k + k * ld]);
+    for (int i = k + 1; i < N; ++i) {
+      const double v = std::fabs(a[i + k * ld]);
+      if (v > amax) {
+        amax = v;
+        p = i;
+      }
+    }
+    ipiv[k] = p + 1;
+    if (p != k)
+      for (int j = 0; j < N; ++j) {
+        const double t = a[k + j * ld];
+        a[k + j * ld] = a[p + j * ld];
+        a[p + j * ld] = t;
+      }
+    const double piv = a[k + k * ld];
+    if (piv != 0.0) {
+      const double r = 1.0 / piv;
+      for (int i = k + 1; i < N; ++i) a[i + k * ld] *= r;
+    } else if (*info == 0) {
+      *info = k + 1;
+    }
+    for (int j = k + 1; j < N; ++j) {
+      const double ukj = a[k + j * ld];
+      if (ukj == 0.0) continue;
+      for (int i = k + 1; i < N; ++i) a[i + j * ld] -= a[i + k * ld] * ukj;
+    }
+  }
+}
+
+void dgetrs_(char *trans, int *n, int *nrhs, double *a, int *lda, int *ipiv, double *b, int *ldb,
+             int *info) {
+  const int N = *n, ld = *lda;
+  *info = (*trans == 'n' || *trans == 'N') ? 0 : -1;
+  if (*info) return;
+  for (int r = 0; r < *nrhs; ++r) {
+    double *x = b + (size_t)r * *ldb;
+    for (int k = 0; k < N; ++k)
+      if (ipiv[k] - 1 != k) {
+        const double t = x[k];
+        x[k] = x[ipiv[k] - 1];
+        x[ipiv[k] - 1] = t;
+      }
+    for (int j = 0; j < N; ++j) {
+      const double xj = x[j];
+      if (xj != 0.0)
+        for (int i = j + 1; i < N; ++i) x[i] -= a[i + j * ld] * xj;
+    }
+    for (int j = N - 1; j >= 0; --j) {
+      x[j] /= a[j + j * ld];
+      const double xj = x[j];
+      if (xj != 0.0)
+        for (int i = 0; i < j; ++i) x[i] -= a[i + j * ld] * xj;
+    }
+  }
+}
+}  // extern "C"
+
+namespace {
+
+struct FixedElement : public TFE3D {
+  explicit FixedElement(int n_dof) : TFE3D() { N_DOF = n_dof; }
+};
+
+// element ids the level's spaces name (any two distinct ids serve)
+const FE3D kVelocityElement = C_Q2_3D_H_A;
+const FE3D kPressureElement = D_P1_3D_H_A;
+
+struct LevelSpace : public TFESpace3D {
+  LevelSpace(TCollection *coll, int n_dof, int active, int n_dirichlet, int *global, int *begin,
+             FE3D *all)
+      : TFESpace3D(coll, (char *)"harness", (char *)"harness") {
+    N_DegreesOfFreedom = n_dof;
+    GlobalNumbers = global;
+    BeginIndex = begin;
+    ActiveBound = active;
+    HangingBound = active;
+    DirichletBound = n_dof;
+    InnerBound = active;
+    N_Inner = active;
+    N_Dirichlet = n_dirichlet;
+    N_ActiveDegrees = active;
+    N_SlaveDegrees = 0;
+    AllElements = all;
+  }
+};
+
+struct LevelSquareStructure : public TSquareStructure3D {
+  LevelSquareStructure(int n, int active, int nnz, int *col, int *rowptr, TFESpace3D *space)
+      : TSquareStructure3D(n, nnz, col, rowptr) {
+    ActiveBound = active;
+    FESpace = space;
+  }
+};
+
+struct LevelStructure : public TStructure3D {
+  LevelStructure(TFESpace3D *other_a, TFESpace3D *other_b, TFESpace3D *test, TFESpace3D *ansatz,
+                 int rows, int cols, int nnz, int *col, int *rowptr)
+      : TStructure3D(other_a, other_b) {
+    N_Rows = rows;
+    N_Columns = cols;
+    N_Entries = nnz;
+    KCol = col;
+    RowPtr = rowptr;
+    HangingN_Entries = 0;
+    HangingKCol = nullptr;
+    HangingRowPtr = nullptr;
+    TestSpace3D = test;
+    AnsatzSpace3D = ansatz;
+    TestSpace2D = nullptr;
+    AnsatzSpace2D = nullptr;
+  }
+};
+
+struct Level : public TNSE_MGLevel4 {
+  using TNSE_MGLevel4::TNSE_MGLevel4;
+  // the auxiliary vectors of the constructor (src/FE/NSE_MGLevel4.C:274-278);
+  // its Magma_Solver is created only in CUDA builds (:305-307)
+  void release() {
+    delete[] Aux[0];
+    delete[] Aux;
+  }
+};
+
+template <class T>
+T *copy_of(const T *src, long n) {
+  T *d = new T[n > 0 ? n : 1];
+  if (n > 0) std::memcpy(d, src, sizeof(T) * n);
+  return d;
+}
+
+struct VankaLevel {
+  int n_u = 0, n_p = 0, n = 0;
+  TCollection *coll = nullptr, *other_a = nullptr, *other_b = nullptr;
+  int *u_global = nullptr, *u_begin = nullptr, *p_global = nullptr, *p_begin = nullptr;
+  FE3D *u_all = nullptr, *p_all = nullptr;
+  alignas(LevelSpace) unsigned char us_store[sizeof(LevelSpace)];
+  alignas(LevelSpace) unsigned char ps_store[sizeof(LevelSpace)];
+  alignas(LevelSpace) unsigned char oa_store[sizeof(LevelSpace)];
+  alignas(LevelSpace) unsigned char ob_store[sizeof(LevelSpace)];
+  LevelSpace *us = nullptr, *ps = nullptr, *oa = nullptr, *ob = nullptr;
+  LevelSquareStructure *sa = nullptr;
+  LevelStructure *sb = nullptr, *sbt = nullptr;
+  alignas(TSquareMatrix3D) unsigned char a_store[9][sizeof(TSquareMatrix3D)];
+  alignas(TMatrix3D) unsigned char b_store[6][sizeof(TMatrix3D)];
+  TSquareMatrix3D *A[9] = {};
+  TMatrix3D *B[6] = {};
+  double *f = nullptr, *u = nullptr, *aux = nullptr;
+  double al[2] = {1.0, 1.0};
+  alignas(Level) unsigned char level_store[sizeof(Level)];
+  Level *level = nullptr;
+};
+
+FixedElement *element_of(int n_dof) {
+  static FixedElement e27(27), e15(15), e4(4);
+  return n_dof == 27 ? &e27 : n_dof == 15 ? &e15 : &e4;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Build the level: n_cells cells of nu_loc (27 or 15) velocity and 4
+// pressure DOFs (cell_udofs, cell_pdofs), the CSR arrays as for
+// ref_level_create, and the relaxation alpha of the level (al[0] of the
+// TNSE_MGLevel4 constructor).  Returns null for an unsupported nu_loc.
+__attribute__((visibility("default"))) void *ref_vanka_create(
+    int n_u, int n_active, int n_p, int n_cells, int nu_loc, const int *cell_udofs,
+    const int *cell_pdofs, const int *a_rowptr, const int *a_col, const double *const *a,
+    const int *b_rowptr, const int *b_col, const double *const *b, const int *bt_rowptr,
+    const int *bt_col, const double *const *bt, double alpha) {
+  if (nu_loc != 27 && nu_loc != 15) return nullptr;
+  VankaLevel *V = new VankaLevel;
+  V->n_u = n_u;
+  V->n_p = n_p;
+  V->n = 3 * n_u + n_p;
+  TFEDatabase3D::RegisterFE3D(kVelocityElement, element_of(nu_loc));
+  TFEDatabase3D::RegisterFE3D(kPressureElement, element_of(4));
+  // a cell array of null pointers: GetCell reads the array, and nothing on
+  // this path reads a cell (~TCollection frees the array with delete[])
+  V->coll = new TCollection(n_cells, new TBaseCell *[n_cells > 0 ? n_cells : 1]());
+  V->other_a = new TCollection(0, nullptr);
+  V->other_b = new TCollection(0, nullptr);
+  V->u_global = copy_of(cell_udofs, (long)n_cells * nu_loc);
+  V->p_global = copy_of(cell_pdofs, 4L * n_cells);
+  V->u_begin = new int[n_cells + 1];
+  V->p_begin = new int[n_cells + 1];
+  V->u_all = new FE3D[n_cells > 0 ? n_cells : 1];
+  V->p_all = new FE3D[n_cells > 0 ? n_cells : 1];
+  for (int c = 0; c <= n_cells; ++c) {
+    V->u_begin[c] = nu_loc * c;
+    V->p_begin[c] = 4 * c;
+  }
+  for (int c = 0; c < n_cells; ++c) {
+    V->u_all[c] = kVelocityElement;
+    V->p_all[c] = kPressureElement;
+  }
+  V->us = new (V->us_store)
+      LevelSpace(V->coll, n_u, n_active, n_u - n_active, V->u_global, V->u_begin, V->u_all);
+  V->ps = new (V->ps_store) LevelSpace(V->coll, n_p, n_p, 0, V->p_global, V->p_begin, V->p_all);
+  V->oa = new (V->oa_store) LevelSpace(V->other_a, 0, 0, 0, nullptr, nullptr, nullptr);
+  V->ob = new (V->ob_store) LevelSpace(V->other_b, 0, 0, 0, nullptr, nullptr, nullptr);
+  const int a_nnz = a_rowptr[n_u], b_nnz = b_rowptr[n_p], bt_nnz = bt_rowptr[n_u];
+  V->sa = new LevelSquareStructure(n_u, n_active, a_nnz, copy_of(a_col, a_nnz),
+                                   copy_of(a_rowptr, n_u + 1L), V->us);
+  V->sb = new LevelStructure(V->oa, V->ob, V->ps, V->us, n_p, n_u, b_nnz, copy_of(b_col, b_nnz),
+                             copy_of(b_rowptr, n_p + 1L));
+  V->sbt = new LevelStructure(V->oa, V->ob, V->us, V->ps, n_u, n_p, bt_nnz,
+                              copy_of(bt_col, bt_nnz), copy_of(bt_rowptr, n_u + 1L));
+  for (int k = 0; k < 9; ++k) {
+    V->A[k] = new (V->a_store[k]) TSquareMatrix3D(V->sa);  // allocates its entries
+    std::memcpy(V->A[k]->GetEntries(), a[k], sizeof(double) * a_nnz);
+  }
+  for (int k = 0; k < 3; ++k) {
+    V->B[k] = new (V->b_store[k]) TMatrix3D(V->sb);
+    std::memcpy(V->B[k]->GetEntries(), b[k], sizeof(double) * b_nnz);
+    V->B[3 + k] = new (V->b_store[3 + k]) TMatrix3D(V->sbt);
+    std::memcpy(V->B[3 + k]->GetEntries(), bt[k], sizeof(double) * bt_nnz);
+  }
+  V->f = new double[V->n]();
+  V->u = new double[V->n]();
+  V->aux = new double[V->n]();
+  V->al[0] = alpha;
+  V->level = new (V->level_store)
+      Level(0, V->A[0], V->A[1], V->A[2], V->A[3], V->A[4], V->A[5], V->A[6], V->A[7], V->A[8],
+            V->B[0], V->B[1], V->B[2], V->B[3], V->B[4], V->B[5], V->f, V->u, 1, V->al, 0, 0,
+            V->coll, nullptr);
+  return V;
+}
+
+__attribute__((visibility("default"))) void ref_vanka_destroy(void *h) {
+  VankaLevel *V = static_cast<VankaLevel *>(h);
+  if (!V) return;
+  V->level->release();
+  for (int k = 0; k < 9; ++k) delete[] V->A[k]->GetEntries();
+  for (int k = 0; k < 6; ++k) delete[] V->B[k]->GetEntries();
+  delete V->sa;
+  delete V->sb;
+  delete V->sbt;
+  for (LevelSpace *s : {V->us, V->ps, V->oa, V->ob}) {
+    std::free(s->GetName());
+    std::free(s->GetDescription());
+  }
+  delete[] V->u_global;
+  delete[] V->p_global;
+  delete[] V->u_begin;
+  delete[] V->p_begin;
+  delete[] V->u_all;
+  delete[] V->p_all;
+  delete V->coll;
+  delete V->other_a;
+  delete V->other_b;
+  delete[] V->f;
+  delete[] V->u;
+  delete[] V->aux;
+  delete V;
+}
+
+// sweeps x TNSE_MGLevel4::CellVanka(u, rhs, aux, 0, NULL, 2, 1) with the
+// damping SC_SMOOTH_DAMP_FACTOR_COARSE_SADDLE = damp and direct local
+// solves (SC_LARGEST_DIRECT_SOLVE above the local size); u is updated.
+__attribute__((visibility("default"))) void ref_vanka_sweeps(void *h, double *u,
+                                                             const double *rhs, int sweeps,
+                                                             double damp) {
+  VankaLevel *V = static_cast<VankaLevel *>(h);
+  TParamDB *db = TDatabase::ParamDB;
+  db->SC_SMOOTH_DAMP_FACTOR_COARSE_SADDLE = damp;
+  db->SC_LARGEST_DIRECT_SOLVE = 1 << 20;
+  db->INTERNAL_LOCAL_DOF = -1;
+  double *r = copy_of(rhs, V->n);
+  for (int s = 0; s < sweeps; ++s) V->level->CellVanka(u, r, V->aux, 0, nullptr, 2, 1);
+  delete[] r;
+}
+
+}  // extern "C"

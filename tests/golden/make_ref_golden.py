@@ -1,9 +1,12 @@
-"""Regenerate tests/golden/ref_defect_*.npz: the reference's own Defect_NSE4
-(with and without the P1disc pressure projection) and MatVect_NSE4
-(src/FE/MGComponents3D.C:3210, :3030) on levels built by the problem builder,
-run through oracle/ref_harness.cpp, which oracle/build_oracle.py compiles with
-the reference sources where they lie.  Needs the reference tree; the fixtures
-are committed so the tests do not.
+"""Regenerate the reference's golden vectors on levels built by the problem
+builder, run through oracle/ref_harness.cpp and oracle/ref_vanka.cpp, which
+oracle/build_oracle.py compiles with the reference sources where they lie:
+* tests/golden/ref_defect_*.npz: Defect_NSE4 (with and without the P1disc
+  pressure projection) and MatVect_NSE4 (src/FE/MGComponents3D.C:3210, :3030);
+* tests/golden/ref_vanka_*.npz: one and two sweeps of the cell Vanka
+  TNSE_MGLevel4::CellVanka (src/FE/NSE_MGLevel4.C:1653-2087, sequential
+  build, damping 1, no relaxation) from u = x with right-hand side b.
+Needs the reference tree; the fixtures are committed so the tests do not.
 
 Inputs are exact binary fractions of the DOF index (``golden_inputs``), so
 every platform forms the same x and b without a random generator.
@@ -43,8 +46,18 @@ def build_problem(kwargs: dict):
     return OseenProblem(**kw)
 
 
+# name -> (OseenProblem keyword arguments, level) of the Vanka fixtures: a
+# level above the coarsest (which the library solves exactly) and small
+# enough that one colour per cell stays within the library's colour limit
+VANKA_CASES = {
+    "hexa": (CASES["hexa"][0], 1),
+    "tetra": (dict(n_levels=2, nu=1.0, seed=0, example="quadlin_oseen", element="tetra",
+                   nx0=1, ny0=1, nz0=1), 1),
+}
+
+
 def main() -> None:
-    from oracle.pyref import RefLevel, ref_harness_lib
+    from oracle.pyref import RefLevel, RefVankaLevel, ref_harness_lib
     if ref_harness_lib() is None:
         raise SystemExit("reference tree not found; cannot regenerate the defect golden files")
     for name, (kwargs, level) in CASES.items():
@@ -58,6 +71,17 @@ def main() -> None:
             source=("reference src/FE/MGComponents3D.C Defect_NSE4 / MatVect_NSE4 "
                     "run by oracle/ref_harness.cpp"))
         print("wrote", name, "level", level, "ndof", R.ndof)
+    for name, (kwargs, level) in VANKA_CASES.items():
+        P = build_problem(kwargs)
+        V = RefVankaLevel(P.arrays(level))
+        x, b = golden_inputs(P.ndof(level))
+        np.savez_compressed(
+            HERE / f"ref_vanka_{name}.npz",
+            problem=json.dumps(kwargs), level=level, n_cells=P.arrays(level)["n_cells"],
+            u_sweep1=V.cell_vanka(x, b, 1), u_sweep2=V.cell_vanka(x, b, 2),
+            source=("reference src/FE/NSE_MGLevel4.C TNSE_MGLevel4::CellVanka (_SEQ) "
+                    "run by oracle/ref_vanka.cpp"))
+        print("wrote vanka", name, "level", level, "ndof", P.ndof(level))
 
 
 if __name__ == "__main__":

@@ -1,4 +1,5 @@
-"""The reference's own coupled-system kernels and FGMRES as the oracle's oracle.
+"""The reference's own coupled-system kernels, FGMRES and cell Vanka as the
+oracle's oracle.
 
 oracle/ref_harness.cpp runs the reference's Defect_NSE4 (with the P1disc
 projection IntoL20Vector3D), MatVect_NSE4 (src/FE/MGComponents3D.C:3210,
@@ -8,7 +9,11 @@ With the reference tree present the oracle's restatement must equal it bit
 for bit (same operation order, no contraction).  The reference's FGMRES is
 preconditioned by the oracle's V-cycle, so the FGMRES comparison pins the
 Krylov part (Arnoldi, Givens rotations, restarts, stopping rules, the
-solution update) while the V-cycle is pinned elsewhere.  The reference's
+solution update) while the V-cycle is pinned elsewhere.  oracle/ref_vanka.cpp
+runs the reference's TNSE_MGLevel4::CellVanka (src/FE/NSE_MGLevel4.C:1653,
+sequential build) on the same levels.  The oracle's sequential Vanka equals
+it bit for bit, except for LAPACK's rounding: the harness's dgetrf_ /
+dgetrs_ do the oracle's LU arithmetic.  The reference's
 defects and mat-vecs on one level of each mesh kind are committed as
 tests/golden/ref_defect_*.npz, so that without the tree (and on the GPU) the
 oracle and the CUDA defect/mat-vec are still checked against the
@@ -17,7 +22,12 @@ reference's numbers:
   last bits of the assembled matrices);
 * the FP64 CUDA kernels: relative 1e-12 (summation order and FMA contraction
   differ).
+The reference's Vanka sweeps are committed as tests/golden/ref_vanka_*.npz.
+The GPU's colour-block sweep equals the sequential cell loop when every cell
+is its own colour, so the CUDA Vanka is checked against the reference's with
+such a colouring, at 1e-9 relative (FP64 LU rounding).
 """
+import ctypes as C
 import importlib.util
 import json
 from pathlib import Path
@@ -44,22 +54,25 @@ def ref_lib_or_skip():
 
 
 def _golden_module():
-    """tests/golden/make_ref_defect_golden.py, loaded by path (its inputs and
+    """tests/golden/make_ref_golden.py, loaded by path (its inputs and
     problem constructor are shared with the generator)."""
-    spec = importlib.util.spec_from_file_location("make_ref_defect_golden",
-                                                  GOLD / "make_ref_defect_golden.py")
+    spec = importlib.util.spec_from_file_location("make_ref_golden",
+                                                  GOLD / "make_ref_golden.py")
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
     return mod
 
 
-def load_case(name):
+def load_case(name, kind="defect"):
     gm = _golden_module()
-    g = np.load(GOLD / f"ref_defect_{name}.npz")
+    g = np.load(GOLD / f"ref_{kind}_{name}.npz")
     P = gm.build_problem(json.loads(str(g["problem"])))
     level = int(g["level"])
-    assert P.arrays(level)["n_udof"] == int(g["n_udof"])
-    assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
+    if kind == "defect":
+        assert P.arrays(level)["n_udof"] == int(g["n_udof"])
+        assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
+    else:
+        assert P.arrays(level)["n_cells"] == int(g["n_cells"])
     x, b = gm.golden_inputs(P.ndof(level))
     return P, level, x, b, g
 
@@ -183,6 +196,83 @@ def test_partial_last_cycle_is_the_documented_deviation():
     assert res10 <= res8 * (1 + 1e-12)
 
 
+VANKA_CASES = {
+    # (problem, sweeps, damping, relaxation alpha)
+    "hexa": (dict(n_levels=3, nu=1e-2, seed=0), 2, 0.8, 1.0),
+    "hexa-alpha": (dict(n_levels=2, nu=1e-3, seed=3), 3, 1.0, 0.7),
+    "channel": (dict(n_levels=2, nu=0.1, seed=0, example="channel", periodic="xz",
+                     stretch_y=1.5, box=(0.0, 6.0, -1.0, 1.0, 0.0, 3.0)), 2, 1.0, 1.0),
+    "tetra": (dict(n_levels=2, nu=1.0, seed=0, example="quadlin_oseen", element="tetra"),
+              2, 0.9, 1.0),
+}
+
+
+@pytest.mark.parametrize("case", list(VANKA_CASES))
+def test_oracle_vanka_equals_reference_cell_vanka_bitwise(case):
+    """Local systems (85x85 or 49x49) from the global matrices, Dirichlet
+    rows, the damped update and the relaxation, every level."""
+    ref_lib_or_skip()
+    from oracle.pyref import RefVankaLevel
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    pk, sweeps, damp, alpha = VANKA_CASES[case]
+    P = OseenProblem(**pk)
+    O = Oracle(P, vanka_mode="seq", smooth_damp=damp, alpha=alpha)
+    rng = np.random.default_rng(21)
+    for level in range(P.n_levels):
+        V = RefVankaLevel(P.arrays(level), alpha=alpha)
+        u, f = rng.standard_normal(P.ndof(level)), rng.standard_normal(P.ndof(level))
+        u_ref = V.cell_vanka(u, f, sweeps, damp)
+        assert np.array_equal(u_ref, O.cell_vanka(level, u, f, sweeps))
+        assert np.max(np.abs(u_ref - u)) > 1e-3  # the sweep did change u
+
+
+def per_cell_colours(P, level):
+    """The problem's descriptors with every cell of ``level`` its own colour
+    (the colour-block sweep then runs the cells one by one, in index order).
+    Returns the descriptors and the colour array they point at."""
+    from to_merge_master_parmoon_gb300._lib import PmLevelDesc
+    descs = (PmLevelDesc * P.n_levels)()
+    for l in range(P.n_levels):
+        C.pointer(descs[l])[0] = P.descs[l]
+    colours = np.arange(P.arrays(level)["n_cells"], dtype=np.int32)
+    descs[level].cell_colour = colours.ctypes.data_as(C.POINTER(C.c_int))
+    return descs, colours
+
+
+class _Levels:
+    """A problem's levels with substituted descriptors, as Oracle takes them."""
+
+    def __init__(self, P, descs):
+        self.descs, self.n_levels, self._P = descs, P.n_levels, P
+
+    def desc(self, level):
+        return self.descs[level % self.n_levels]
+
+
+@pytest.mark.parametrize("name", ["hexa", "tetra"])
+def test_vanka_fixtures_reproduce_from_the_reference(name):
+    ref_lib_or_skip()
+    from oracle.pyref import RefVankaLevel
+    P, level, x, b, g = load_case(name, "vanka")
+    V = RefVankaLevel(P.arrays(level))
+    assert np.array_equal(V.cell_vanka(x, b, 1), g["u_sweep1"])
+    assert np.array_equal(V.cell_vanka(x, b, 2), g["u_sweep2"])
+
+
+@pytest.mark.parametrize("name", ["hexa", "tetra"])
+def test_oracle_vanka_matches_reference_fixtures(name):
+    """Both oracle modes: the sequential loop, and the colour-block sweep
+    (the GPU's semantics) with one cell per colour."""
+    P, level, x, b, g = load_case(name, "vanka")
+    O = Oracle(P, vanka_mode="seq")
+    assert rel(O.cell_vanka(level, x, b, 1), g["u_sweep1"]) < 1e-13
+    assert rel(O.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-13
+    descs, colours = per_cell_colours(P, level)
+    Oc = Oracle(_Levels(P, descs), vanka_mode="colour")
+    assert rel(Oc.cell_vanka(level, x, b, 1), g["u_sweep1"]) < 1e-13
+    assert rel(Oc.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-13
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_fixtures_reproduce_from_the_reference(name):
     """The committed fixtures are what the reference computes here."""
@@ -226,3 +316,17 @@ def test_gpu_one_block_defect_and_matvec_match_reference_fixture():
     assert rel(S.coupled_defect(level, x, b, True), g["r_project"]) < 1e-12
     assert rel(S.coupled_defect(level, x, b, False), g["r_plain"]) < 1e-12
     assert rel(S.matvec(level, x), g["y"]) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hexa", "tetra"])
+def test_gpu_cell_vanka_matches_reference_fixtures(name):
+    """The FP64 CUDA Vanka (factor once, colour-block apply) with one cell per
+    colour against the reference's own CellVanka sweeps."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, x, b, g = load_case(name, "vanka")
+    descs, colours = per_cell_colours(P, level)
+    S = PmSolver(descs, precision="fp64")
+    assert rel(S.cell_vanka(level, x, b, 1), g["u_sweep1"]) < 1e-9
+    assert rel(S.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-9
+    del colours
