@@ -7,8 +7,12 @@
 * ``oracle/_ref/libref_harness.so`` — the reference's coupled-system kernels,
   its flexible FGMRES and its cell Vanka (the translation units of
   REF_HARNESS_TUS below) compiled where they lie, driven by ref_harness.cpp
-  and ref_vanka.cpp (only when the tree is present; the defect outputs are
-  committed as tests/golden/ref_defect_*.npz).
+  and ref_vanka.cpp (only when the tree is present; the defect and Vanka
+  outputs are committed as tests/golden/ref_defect_*.npz, ref_vanka_*.npz).
+* ``oracle/_ref/libref_transfer.so`` — the reference's grid transfers with
+  the FE and geometry databases they read (REF_TRANSFER_TUS), driven by
+  ref_transfer.cpp (only when the tree is present; its outputs are committed
+  as tests/golden/ref_transfer_*.npz).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 what this builds.
@@ -62,7 +66,7 @@ REF_HARNESS_TUS = ("FE/MGComponents3D", "FE/FgmresIte", "FE/ItMethod", "FE/Matri
                    "FE/FESpace3D", "FE/FE3D", "FE/Structure3D", "FE/SquareStructure3D",
                    "FE/SquareMatrix3D", "FE/Matrix3D", "Geometry/Collection")
 REF_INCLUDE_DIRS = ("General", "FE", "Geometry", "FE3D", "FE2D", "FE1D", "System",
-                    "QuadFormulas", "Parallel", "AMG")
+                    "QuadFormulas", "Parallel", "AMG", "Refinement")
 
 
 def build_ref_harness() -> Path | None:
@@ -77,31 +81,126 @@ def build_ref_harness() -> Path | None:
     objdir = REF_OUT / "harness_obj"
     objdir.mkdir(parents=True, exist_ok=True)
     out = REF_OUT / "libref_harness.so"
-    mine = [HERE / "ref_harness.cpp", HERE / "ref_vanka.cpp", Path(__file__),
-            *sorted((HERE / "ref_stubs").glob("*.h"))]
+    mine = [HERE / "ref_harness.cpp", HERE / "ref_vanka.cpp", *_ref_deps()]
     if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in mine):
         return out
-    # _SEQ: the reference's sequential build, whose cell Vanka the oracle restates
-    inc = ["-D__3D__", "-D_SEQ", f"-I{HERE / 'ref_stubs'}"]
+    jobs = [(src / f"{t}.C", objdir / f"{Path(t).name}.o") for t in REF_HARNESS_TUS]
+    jobs.append((HERE / "ref_harness.cpp", objdir / "ref_harness.o"))
+    jobs.append((HERE / "ref_vanka.cpp", objdir / "ref_vanka.o"))
+    _compile(jobs, _ref_flags())
+    _run(["g++", "-shared", "-fopenmp", "-Wl,--gc-sections", "-Wl,-z,defs",
+          *[str(o) for _, o in jobs], "-o", str(out)])
+    return out
+
+
+def _ref_deps():
+    """Files every reference-harness object depends on besides its source."""
+    return [HERE / "ref_level_space.h", Path(__file__), *sorted((HERE / "ref_stubs").glob("*.h"))]
+
+
+def _compile(jobs, cmd):
+    """Compile (source, object) pairs with ``cmd``, os.cpu_count() at a time,
+    skipping objects newer than their source and _ref_deps()."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    newest_dep = max(d.stat().st_mtime for d in _ref_deps())
+
+    def one(job):
+        src, obj = job
+        if obj.exists() and obj.stat().st_mtime >= max(src.stat().st_mtime, newest_dep):
+            return None
+        r = subprocess.run([*cmd, "-c", str(src), "-o", str(obj)], capture_output=True, text=True)
+        return None if r.returncode == 0 else f"compiling {src} failed:\n{r.stdout}{r.stderr}"
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
+        errors = [e for e in pool.map(one, jobs) if e]
+    if errors:
+        raise RuntimeError("reference harness: " + errors[0])
+
+
+def _ref_flags():
+    """The reference's 3D sequential build (-D_SEQ: its cell Vanka is the
+    sequential one the oracle restates), the stubs of oracle/ref_stubs/, and
+    the reference's own include directories."""
+    inc = ["-D__3D__", "-D_SEQ", f"-I{HERE / 'ref_stubs'}", f"-I{HERE}"]
     inc += [f"-I{REFERENCE / 'include' / d}" for d in REF_INCLUDE_DIRS]
     # include/FE/NSE_MGLevel.h (reached from FgmresIte.C and NSE_MGLevel4.C)
     # includes the CUDA runtime headers; declarations only, nothing of them
     # is linked
     cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
     inc += ["-isystem", str(cuda_inc)]
-    flags = ["g++", "-O2", "-std=c++11", "-fPIC", "-fopenmp", "-w", "-ffp-contract=off",
-             "-ffunction-sections", "-fdata-sections", "-fvisibility=hidden"]
-    jobs = [(src / f"{t}.C", objdir / f"{Path(t).name}.o") for t in REF_HARNESS_TUS]
-    jobs.append((HERE / "ref_harness.cpp", objdir / "ref_harness.o"))
-    jobs.append((HERE / "ref_vanka.cpp", objdir / "ref_vanka.o"))
-    procs = [(subprocess.Popen([*flags, *inc, "-c", str(s), "-o", str(o)], stdout=subprocess.PIPE,
-                               stderr=subprocess.STDOUT, text=True), s) for s, o in jobs]
-    for pr, s in procs:
-        log = pr.communicate()[0]
-        if pr.returncode != 0:
-            raise RuntimeError(f"reference harness: compiling {s} failed:\n{log}")
-    _run(["g++", "-shared", "-fopenmp", "-Wl,--gc-sections", "-Wl,-z,defs",
-          *[str(o) for _, o in jobs], "-o", str(out)])
+    return ["g++", "-O2", "-std=c++11", "-fPIC", "-fopenmp", "-w", "-ffp-contract=off",
+            "-ffunction-sections", "-fdata-sections", "-fvisibility=hidden", *inc]
+
+
+# The reference translation units of the transfer harness: what the link of
+# ref_transfer.cpp pulls from the reference's src/ (the TDatabase and
+# TFEDatabase3D constructors register every descriptor and element, so their
+# closure is wide).  Linked from a static archive, so that only needed
+# members enter and the 2D twins of some 3D helpers do not collide.
+REF_TRANSFER_TUS = {
+    "FE": ("AuxParam3D", "BaseFunct1D", "BaseFunct2D", "BaseFunct3D", "Blas1", "ConvDiff",
+          "Convolution", "FE1D", "FE2D", "FE2DMapper", "FE2DMapper1Reg", "FE3D", "FE3DMapper",
+          "FE3DMapper1Reg", "FEDatabase2D", "FEDatabase3D", "FEDesc1D", "FEDesc2D", "FEDesc3D",
+          "FEFunction3D", "FESpace", "FESpace3D", "HNDesc", "HangingNode", "HexaAffin",
+          "HexaIsoparametric", "HexaTrilinear", "LinAlg", "LineAffin", "MGComponents3D",
+          "NodalFunctional1D", "NodalFunctional2D", "NodalFunctional3D", "QuadAffin",
+          "QuadBilinear", "QuadIsoparametric", "RefTrans3D", "TNSE3D_FixPo", "TetraAffin",
+          "TetraIsoparametric", "TriaAffin", "TriaIsoparametric"),
+    "General": ("Database", "MainUtilities", "MooNMD_Io", "Utilities", "Vector"),
+    "Geometry": ("BaseCell", "BdPlane", "BoundComp", "BoundComp3D", "BoundEdge", "BoundFace", "Brick",
+          "Collection", "GridCell", "Hexahedron", "InterfaceJoint3D", "It_Between", "It_EQ",
+          "It_EQLevel", "It_Finest", "It_LE", "It_LELevel", "It_OCAF", "It_Search", "Joint",
+          "JointCollection", "JointEqN", "Line", "Mapper", "Parallelogram", "Quadrangle",
+          "Rectangle", "RefDesc", "Tetrahedron", "Triangle", "Vertex"),
+    "QuadFormulas": ("QuadFormula", "QuadFormula1D", "QuadFormula2D", "QuadFormula3D", "QuadFormulaHexa",
+          "QuadFormulaQuad", "QuadFormulaTetra", "QuadFormulaTria"),
+    "Refinement": ("RefHexaRegDesc", "RefLineDesc", "RefNoRef", "RefQuad1Conf0Desc", "RefQuad1Conf1Desc",
+          "RefQuad1Conf2Desc", "RefQuad1Conf3Desc", "RefQuad2Conf0Desc", "RefQuad2Conf1Desc",
+          "RefQuad2Conf2Desc", "RefQuad2Conf3Desc", "RefQuadBis0Desc", "RefQuadBis1Desc",
+          "RefQuadRegDesc", "RefQuadToTri0Desc", "RefQuadToTri1Desc", "RefTetraBis01Desc",
+          "RefTetraBis02Desc", "RefTetraBis03Desc", "RefTetraBis04Desc", "RefTetraBis05Desc",
+          "RefTetraBis0Desc", "RefTetraBis10Desc", "RefTetraBis12Desc", "RefTetraBis13Desc",
+          "RefTetraBis14Desc", "RefTetraBis15Desc", "RefTetraBis1Desc", "RefTetraBis20Desc",
+          "RefTetraBis21Desc", "RefTetraBis23Desc", "RefTetraBis24Desc", "RefTetraBis25Desc",
+          "RefTetraBis2Desc", "RefTetraBis30Desc", "RefTetraBis32Desc", "RefTetraBis34Desc",
+          "RefTetraBis35Desc", "RefTetraBis3Desc", "RefTetraBis40Desc", "RefTetraBis41Desc",
+          "RefTetraBis43Desc", "RefTetraBis45Desc", "RefTetraBis4Desc", "RefTetraBis51Desc",
+          "RefTetraBis52Desc", "RefTetraBis53Desc", "RefTetraBis54Desc", "RefTetraBis5Desc",
+          "RefTetraQuad0Desc", "RefTetraQuad1Desc", "RefTetraQuad2Desc", "RefTetraQuad3Desc",
+          "RefTetraReg0Desc", "RefTetraReg1Desc", "RefTetraReg2Desc", "RefTetraRegDesc",
+          "RefTriBis01Desc", "RefTriBis02Desc", "RefTriBis0Desc", "RefTriBis10Desc",
+          "RefTriBis12Desc", "RefTriBis1Desc", "RefTriBis20Desc", "RefTriBis21Desc",
+          "RefTriBis2Desc", "RefTriRegDesc", "Refinement"),
+}
+
+
+def build_ref_transfer() -> Path | None:
+    """Compile the reference's grid transfers (Prolongate, DefectRestriction,
+    GetProlongationMatrix3D) and the databases they read, with
+    ref_transfer.cpp, into oracle/_ref/libref_transfer.so.  Returns None
+    without the tree."""
+    srcs = [REFERENCE / "src" / d / f"{t}.C" for d, ts in REF_TRANSFER_TUS.items() for t in ts]
+    if not all(s.exists() for s in srcs):
+        return None
+    objdir = REF_OUT / "transfer_obj"
+    objdir.mkdir(parents=True, exist_ok=True)
+    out = REF_OUT / "libref_transfer.so"
+    mine = [HERE / "ref_transfer.cpp", *_ref_deps()]
+    if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in mine):
+        return out
+    jobs = [(s, objdir / f"{s.parent.name}_{s.stem}.o") for s in srcs]
+    _compile(jobs, _ref_flags())
+    own = objdir / "ref_transfer.o"
+    _compile([(HERE / "ref_transfer.cpp", own)], _ref_flags())
+    archive = objdir / "libref_transfer_tus.a"
+    if archive.exists():
+        archive.unlink()
+    _run(["ar", "rcs", str(archive), *[str(o) for _, o in jobs]])
+    # -Bsymbolic: the reference objects call this library's own operator new
+    # (zero-filling, see ref_transfer.cpp), whatever was loaded before it
+    _run(["g++", "-shared", "-fopenmp", "-Wl,--gc-sections", "-Wl,-z,defs", "-Wl,-Bsymbolic",
+          str(own), str(archive), "-o", str(out)])
     return out
 
 
@@ -109,3 +208,4 @@ if __name__ == "__main__":
     print(build_oracle())
     print(build_ref_pin())
     print(build_ref_harness())
+    print(build_ref_transfer())

@@ -2,7 +2,8 @@
 Defect_NSE4 / MatVect_NSE4 / IntoL20Vector3D (src/FE/MGComponents3D.C:3210,
 :3030, :1756) and flexible FGMRES (TFgmresIte::Iterate, src/FE/FgmresIte.C:250)
 and cell Vanka (TNSE_MGLevel4::CellVanka, src/FE/NSE_MGLevel4.C:1653) run on
-one level of a problem built here.  TEST INFRASTRUCTURE
+one level of a problem built here; and (oracle/_ref/libref_transfer.so) the
+grid transfers Prolongate / DefectRestriction between two levels.  TEST INFRASTRUCTURE
 ONLY — it exists where the reference tree does (see build_ref_harness).
 """
 from __future__ import annotations
@@ -11,7 +12,7 @@ import ctypes as C
 
 import numpy as np
 
-from .build_oracle import build_ref_harness
+from .build_oracle import build_ref_harness, build_ref_transfer
 
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
@@ -214,6 +215,73 @@ class RefVankaLevel:
         assert u.size == rhs.size == 3 * self.n_u + self.n_p
         self._L.ref_vanka_sweeps(self._h, u.ctypes.data_as(_dp), rp, sweeps, damp)
         return u
+
+
+_TLIB = None
+
+
+def ref_transfer_lib():
+    """The loaded transfer harness, or None when the reference tree is absent."""
+    global _TLIB
+    if _TLIB is None:
+        path = build_ref_transfer()
+        if path is None:
+            return None
+        L = C.CDLL(str(path))
+        L.ref_transfer_create.argtypes = [C.c_int] * 4 + [_ip, _ip] + [C.c_int] * 4 + [_ip] * 4
+        L.ref_transfer_create.restype = C.c_void_p
+        L.ref_transfer_destroy.argtypes = [C.c_void_p]
+        L.ref_transfer_destroy.restype = None
+        L.ref_transfer_prolongate.argtypes = [C.c_void_p, _dp, _dp]
+        L.ref_transfer_prolongate.restype = None
+        L.ref_transfer_restrict.argtypes = [C.c_void_p, _dp, _dp]
+        L.ref_transfer_restrict.restype = None
+        _TLIB = L
+    return _TLIB
+
+
+class RefTransfer:
+    """The reference's Prolongate / DefectRestriction between level ``level``
+    of a hexahedral Q2/P1disc problem and the next coarser one
+    (src/FE/MGComponents3D.C, run by oracle/ref_transfer.cpp)."""
+
+    def __init__(self, problem, level: int):
+        L = ref_transfer_lib()
+        if L is None:
+            raise RuntimeError("reference tree not present: the transfer harness is not built")
+        self._L = L
+        self._h = None
+        c, f = problem.arrays(level - 1), problem.arrays(level)
+        self.nc = 3 * c["n_udof"] + c["n_pdof"]
+        self.nf = 3 * f["n_udof"] + f["n_pdof"]
+        keep = [np.ascontiguousarray(a, dtype=np.int32) for a in
+                (c["cell_udofs"], c["cell_pdofs"], f["cell_udofs"], f["cell_pdofs"],
+                 f["cell_parent"], f["cell_child"])]
+        ptr = [a.ctypes.data_as(_ip) for a in keep]
+        self._h = L.ref_transfer_create(c["n_cells"], c["n_udof"], c["n_active"], c["n_pdof"],
+                                        ptr[0], ptr[1], f["n_cells"], f["n_udof"],
+                                        f["n_active"], f["n_pdof"], *ptr[2:])
+        if not self._h:
+            raise ValueError("the levels are not a regular refinement (8 children per cell)")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.ref_transfer_destroy(self._h)
+            self._h = None
+
+    def prolongate(self, coarse) -> np.ndarray:
+        coarse, cp = _d(coarse)
+        assert coarse.size == self.nc
+        fine = np.empty(self.nf)
+        self._L.ref_transfer_prolongate(self._h, cp, fine.ctypes.data_as(_dp))
+        return fine
+
+    def restrict(self, fine) -> np.ndarray:
+        fine, fp = _d(fine)
+        assert fine.size == self.nf
+        coarse = np.empty(self.nc)
+        self._L.ref_transfer_restrict(self._h, fp, coarse.ctypes.data_as(_dp))
+        return coarse
 
 
 def ref_into_l20(v, order: int = -11) -> np.ndarray:

@@ -1,0 +1,347 @@
+// ref_transfer.cpp — runs the reference's own grid transfers on two nested
+// hexahedral levels handed over as plain arrays.  TEST INFRASTRUCTURE ONLY:
+// it pins the oracle's prolongate / defect_restriction (and with them the
+// per-child Q2 and P1disc matrices) against the reference code itself.
+// Built by oracle/build_oracle.py (build_ref_transfer) into
+// oracle/_ref/libref_transfer.so, with -D__3D__ -D_SEQ, from the reference
+// sources where they lie.
+//
+// Reference code that runs here:
+//   src/General/Database.C, src/FE/FEDatabase3D.C
+//                            the TDatabase and TFEDatabase3D constructors
+//                            (shape and refinement descriptors, every
+//                            element, basis, nodal functional and reference
+//                            transformation registered as in a ParMooN run)
+//   src/FE/MGComponents3D.C  Prolongate (vector :468-708, scalar :184-467)
+//                            and DefectRestriction (vector :996-1242,
+//                            scalar :711-995)
+//   src/FE/FEDatabase3D.C    GetProlongationMatrix3D (:1630-1790): the
+//                            per-child matrices from the elements' nodal
+//                            functionals on the refined reference cell
+//   with the geometry, refinement and FE classes they call.
+//
+// What the harness supplies instead of a ParMooN mesh:
+// * cells: reference TGridCell objects without vertices.  A coarse cell
+//   carries the regular hexahedral refinement descriptor and its 8 children,
+//   a fine cell its parent.  Prolongate and DefectRestriction ask cells for
+//   nothing else, and ChangeBF returns at once for Q2 and P1disc (no
+//   BF2Change table, src/FE/BaseFunct3D.C:589-595).
+// * the children: the reference numbers the children of a regular
+//   refinement by its refinement descriptor, each child with its own vertex
+//   order.  A child's vertex 0 is a corner of the parent, and its local
+//   axes are a rotation or reflection of the parent's.  The level arrays
+//   number children by octant, every cell with axis-aligned local DOFs.
+//   The harness refines the reference element with the reference's own
+//   code, exactly as GetProlongationMatrix3D does
+//   (src/FE/FEDatabase3D.C:1721-1727).  From each child's vertices it
+//   takes the octant, which links every coarse cell's child slots.  It
+//   also takes the child's local frame and hands each fine cell over in it:
+//   - the 27 Q2 DOF numbers in the child's local node order;
+//   - the P1disc coefficients (basis 1, xi, eta, zeta; the child's local
+//     coordinates are a signed permutation of the axis-aligned ones)
+//     transformed by that signed permutation on the way in (defects) and
+//     on the way out (prolongated functions).
+//   The coarse cells have the reference element's own frame, which is the
+//   axis-aligned one.
+// * spaces: LevelSpace (ref_level_space.h) with C_Q2_3D_H_A velocity and
+//   D_P1_3D_H_A pressure elements in every cell.
+// * allocation: on this path the reference reads memory that it allocated
+//   and did not initialise (TGridCell::Refine of the cell from
+//   GenerateRefElement, as GetProlongationMatrix3D itself runs it).  A ParMooN
+//   run gets away with this because its heap is fresh, zero pages from the
+//   system.  In a process whose heap has been used before, it faults.  So
+//   inside this library operator new / new[] return zero-filled memory (the
+//   library links with -Bsymbolic, so the reference objects in it call
+//   these; no other library does).
+// No reference destructor runs; the harness frees what it allocated.
+#include <cmath>
+#include <cstdlib>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include <BaseCell.h>
+#include <BaseFunct3D.h>
+#include <Collection.h>
+#include <Database.h>
+#include <FE3D.h>
+#include <FEDatabase3D.h>
+#include <FESpace3D.h>
+#include <GridCell.h>
+#include <LinAlg.h>
+#include <MultiGrid3D.h>
+#include <RefDesc.h>
+#include <Vertex.h>
+
+#include "ref_level_space.h"
+
+void *operator new(std::size_t n) {
+  void *p = std::calloc(1, n ? n : 1);
+  if (!p) throw std::bad_alloc();
+  return p;
+}
+void *operator new[](std::size_t n) {
+  void *p = std::calloc(1, n ? n : 1);
+  if (!p) throw std::bad_alloc();
+  return p;
+}
+void operator delete(void *p) noexcept { std::free(p); }
+void operator delete[](void *p) noexcept { std::free(p); }
+
+namespace {
+
+struct HarnessCell : public TGridCell {
+  explicit HarnessCell(TRefDesc *rd) : TGridCell(rd, 0) {}
+  void set_children(TBaseCell **c) { Children = c; }
+  TBaseCell **children() { return Children; }
+  TVertex **vertices() { return Vertices; }
+};
+
+bool g_ready = false;
+int g_octant_of_child[8];
+// per reference child: axis-aligned local Q2 node of each of its local nodes,
+// and for its local coordinate i (xi, eta, zeta) the axis-aligned coordinate
+// g_paxis[j][i] and the sign g_psign[j][i] with xi_i = sign * x_axis
+int g_uperm[8][27];
+int g_paxis[8][3];
+double g_psign[8][3];
+
+// octant (bit 0: xi > 0, bit 1: eta > 0, bit 2: zeta > 0, relative to the
+// parent's centre) of each child of the regular hexahedral refinement
+bool init_databases() {
+  if (g_ready) return true;
+  new TDatabase();
+  new TFEDatabase3D();
+  TBaseFunct3D *bf = TFEDatabase3D::GetBaseFunct3D(BF_C_H_Q2_3D);
+  TBaseCell *ref = bf->GenerateRefElement();
+  double c[3] = {0, 0, 0};
+  for (int v = 0; v < 8; ++v) {
+    double x, y, z;
+    ref->GetVertex(v)->GetCoords(x, y, z);
+    c[0] += x / 8;
+    c[1] += y / 8;
+    c[2] += z / 8;
+  }
+  ref->SetRefDesc(TDatabase::RefDescDB[N_SHAPES + HexaReg]);
+  ref->Refine(0);
+  int seen = 0;
+  for (int j = 0; j < 8; ++j) {
+    TBaseCell *child = ref->GetChild(j);
+    double m[3] = {0, 0, 0};
+    for (int v = 0; v < 8; ++v) {
+      double x, y, z;
+      child->GetVertex(v)->GetCoords(x, y, z);
+      m[0] += x / 8;
+      m[1] += y / 8;
+      m[2] += z / 8;
+    }
+    const int o = (m[0] > c[0]) | ((m[1] > c[1]) << 1) | ((m[2] > c[2]) << 2);
+    g_octant_of_child[j] = o;
+    seen |= 1 << o;
+    // the child's frame: vertex 0 and the edges to vertices 1, 3, 4
+    double v[4][3];
+    const int vid[4] = {0, 1, 3, 4};
+    for (int t = 0; t < 4; ++t) child->GetVertex(vid[t])->GetCoords(v[t][0], v[t][1], v[t][2]);
+    double lo[3];  // the child's lower corner
+    for (int a = 0; a < 3; ++a) {
+      double mn = 1e300;
+      for (int vv = 0; vv < 8; ++vv) {
+        double x[3];
+        child->GetVertex(vv)->GetCoords(x[0], x[1], x[2]);
+        if (x[a] < mn) mn = x[a];
+      }
+      lo[a] = mn;
+    }
+    for (int i = 0; i < 3; ++i) {
+      double e[3];
+      for (int a = 0; a < 3; ++a) e[a] = v[i + 1][a] - v[0][a];
+      int ax = 0;
+      for (int a = 1; a < 3; ++a)
+        if (std::fabs(e[a]) > std::fabs(e[ax])) ax = a;
+      g_paxis[j][i] = ax;
+      g_psign[j][i] = e[ax] > 0 ? 1.0 : -1.0;
+    }
+    const double h = std::fabs(v[1][g_paxis[j][0]] - v[0][g_paxis[j][0]]);  // child edge
+    for (int cc = 0; cc < 3; ++cc)
+      for (int b = 0; b < 3; ++b)
+        for (int a = 0; a < 3; ++a) {
+          double pos[3];
+          for (int d = 0; d < 3; ++d)
+            pos[d] = v[0][d] + 0.5 * a * (v[1][d] - v[0][d]) + 0.5 * b * (v[2][d] - v[0][d]) +
+                     0.5 * cc * (v[3][d] - v[0][d]);
+          int q[3];
+          for (int d = 0; d < 3; ++d) q[d] = (int)std::lround(2.0 * (pos[d] - lo[d]) / h);
+          g_uperm[j][a + 3 * b + 9 * cc] = q[0] + 3 * q[1] + 9 * q[2];
+        }
+  }
+  ref->Derefine();
+  if (seen != 0xff) {
+    std::fprintf(stderr, "ref_transfer: the refined reference cell has no child per octant\n");
+    return false;
+  }
+  g_ready = true;
+  return true;
+}
+
+struct Side {
+  int n_cells = 0, n_u = 0, n_p = 0;
+  std::vector<HarnessCell *> cells;
+  TBaseCell **cell_array = nullptr;
+  TCollection *coll = nullptr;
+  int *ug = nullptr, *ub = nullptr, *pg = nullptr, *pb = nullptr;
+  FE3D *ua = nullptr, *pa = nullptr;
+  alignas(LevelSpace) unsigned char us_store[sizeof(LevelSpace)];
+  alignas(LevelSpace) unsigned char ps_store[sizeof(LevelSpace)];
+  LevelSpace *us = nullptr, *ps = nullptr;
+};
+
+void make_side(Side &S, int n_cells, int n_u, int n_active, int n_p, const int *udofs,
+               const int *pdofs, TRefDesc *rd) {
+  S.n_cells = n_cells;
+  S.n_u = n_u;
+  S.n_p = n_p;
+  S.cell_array = new TBaseCell *[n_cells > 0 ? n_cells : 1];
+  for (int c = 0; c < n_cells; ++c) {
+    S.cells.push_back(new HarnessCell(rd));
+    S.cell_array[c] = S.cells.back();
+  }
+  S.coll = new TCollection(n_cells, S.cell_array);
+  S.ug = new int[(size_t)27 * n_cells + 1];
+  S.pg = new int[(size_t)4 * n_cells + 1];
+  std::memcpy(S.ug, udofs, sizeof(int) * 27 * (size_t)n_cells);
+  std::memcpy(S.pg, pdofs, sizeof(int) * 4 * (size_t)n_cells);
+  S.ub = new int[n_cells + 1];
+  S.pb = new int[n_cells + 1];
+  S.ua = new FE3D[n_cells + 1];
+  S.pa = new FE3D[n_cells + 1];
+  for (int c = 0; c <= n_cells; ++c) {
+    S.ub[c] = 27 * c;
+    S.pb[c] = 4 * c;
+    S.ua[c] = C_Q2_3D_H_A;
+    S.pa[c] = D_P1_3D_H_A;
+  }
+  S.us = new (S.us_store) LevelSpace(S.coll, n_u, n_active, n_u - n_active, S.ug, S.ub, S.ua);
+  S.ps = new (S.ps_store) LevelSpace(S.coll, n_p, n_p, 0, S.pg, S.pb, S.pa);
+}
+
+void free_side(Side &S) {
+  for (HarnessCell *c : S.cells) {
+    delete[] c->children();
+    c->set_children(nullptr);
+    delete[] c->vertices();
+    ::operator delete(static_cast<void *>(c));  // storage only: no reference destructor
+  }
+  S.us->release_names();
+  S.ps->release_names();
+  delete S.coll;  // frees cell_array (delete[], src/Geometry/Collection.C:57-62)
+  delete[] S.ug;
+  delete[] S.pg;
+  delete[] S.ub;
+  delete[] S.pb;
+  delete[] S.ua;
+  delete[] S.pa;
+}
+
+struct Pair {
+  Side coarse, fine;
+  std::vector<int> ref_child;  // per fine cell: its reference child number
+};
+
+// pressure coefficients of every fine cell between the axis-aligned frame
+// and the cell's reference-child frame (to_child: xi_i coefficient =
+// sign_i * coefficient of axis(i); the inverse otherwise)
+void convert_pressure(const Pair &T, double *fp, bool to_child) {
+  const Side &F = T.fine;
+  for (int f = 0; f < F.n_cells; ++f) {
+    const int j = T.ref_child[f];
+    const int *dof = F.pg + 4 * (size_t)f;
+    double in[3], out[3];
+    for (int i = 0; i < 3; ++i) in[i] = fp[dof[1 + i]];
+    for (int i = 0; i < 3; ++i) {
+      if (to_child)
+        out[i] = g_psign[j][i] * in[g_paxis[j][i]];
+      else
+        out[g_paxis[j][i]] = g_psign[j][i] * in[i];
+    }
+    for (int i = 0; i < 3; ++i) fp[dof[1 + i]] = out[i];
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// Two nested Q2/P1disc hexahedral levels: per cell 27 velocity and 4
+// pressure DOFs; fine cell f is child number fine_child[f] (its octant:
+// bit 0 x, bit 1 y, bit 2 z) of coarse cell fine_parent[f].  Returns null
+// when a coarse cell has not exactly one child per octant.
+__attribute__((visibility("default"))) void *ref_transfer_create(
+    int nc_cells, int nc_u, int nc_active, int nc_p, const int *c_udofs, const int *c_pdofs,
+    int nf_cells, int nf_u, int nf_active, int nf_p, const int *f_udofs, const int *f_pdofs,
+    const int *fine_parent, const int *fine_child) {
+  if (!init_databases()) return nullptr;
+  std::vector<int> slot((size_t)8 * nc_cells, -1);
+  for (int f = 0; f < nf_cells; ++f) {
+    const int p = fine_parent[f], o = fine_child[f];
+    if (p < 0 || p >= nc_cells || o < 0 || o > 7 || slot[(size_t)8 * p + o] >= 0) return nullptr;
+    slot[(size_t)8 * p + o] = f;
+  }
+  for (int s : slot)
+    if (s < 0) return nullptr;
+  Pair *T = new Pair;
+  make_side(T->coarse, nc_cells, nc_u, nc_active, nc_p, c_udofs, c_pdofs,
+            TDatabase::RefDescDB[N_SHAPES + HexaReg]);
+  make_side(T->fine, nf_cells, nf_u, nf_active, nf_p, f_udofs, f_pdofs,
+            TDatabase::RefDescDB[Hexahedron]);
+  T->ref_child.assign(nf_cells, 0);
+  for (int c = 0; c < nc_cells; ++c) {
+    TBaseCell **ch = new TBaseCell *[8];
+    for (int j = 0; j < 8; ++j) {
+      const int f = slot[(size_t)8 * c + g_octant_of_child[j]];
+      ch[j] = T->fine.cells[f];
+      ch[j]->SetParent(T->coarse.cells[c]);
+      T->ref_child[f] = j;
+      for (int t = 0; t < 27; ++t)  // the fine cell's DOFs in the child's node order
+        T->fine.ug[(size_t)27 * f + t] = f_udofs[(size_t)27 * f + g_uperm[j][t]];
+    }
+    T->coarse.cells[c]->set_children(ch);
+  }
+  return T;
+}
+
+__attribute__((visibility("default"))) void ref_transfer_destroy(void *h) {
+  Pair *T = static_cast<Pair *>(h);
+  if (!T) return;
+  free_side(T->coarse);
+  free_side(T->fine);
+  delete T;
+}
+
+// fine = the reference's prolongation of coarse: Prolongate over the three
+// velocity components (N_Functions = 3) and the scalar Prolongate for the
+// pressure; vectors are [u1|u2|u3|p] of each level.
+__attribute__((visibility("default"))) void ref_transfer_prolongate(void *h, const double *coarse,
+                                                                    double *fine) {
+  Pair *T = static_cast<Pair *>(h);
+  const Side &C = T->coarse, &F = T->fine;
+  std::vector<double> cu(coarse, coarse + 3 * (size_t)C.n_u + C.n_p), aux(F.n_u + F.n_p + 1);
+  Prolongate(C.us, F.us, 3, cu.data(), fine, aux.data());
+  Prolongate(C.ps, F.ps, cu.data() + 3 * (size_t)C.n_u, fine + 3 * (size_t)F.n_u, aux.data());
+  convert_pressure(*T, fine + 3 * (size_t)F.n_u, false);
+}
+
+// coarse = the reference's defect restriction of fine (DefectRestriction
+// over the velocity components, then the scalar one for the pressure)
+__attribute__((visibility("default"))) void ref_transfer_restrict(void *h, const double *fine,
+                                                                  double *coarse) {
+  Pair *T = static_cast<Pair *>(h);
+  const Side &C = T->coarse, &F = T->fine;
+  std::vector<double> fu(fine, fine + 3 * (size_t)F.n_u + F.n_p), aux(F.n_u + F.n_p + 1);
+  convert_pressure(*T, fu.data() + 3 * (size_t)F.n_u, true);
+  DefectRestriction(C.us, F.us, 3, coarse, fu.data(), aux.data());
+  DefectRestriction(C.ps, F.ps, coarse + 3 * (size_t)C.n_u, fu.data() + 3 * (size_t)F.n_u,
+                    aux.data());
+}
+
+}  // extern "C"

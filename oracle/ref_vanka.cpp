@@ -20,11 +20,8 @@
 //   src/FE/LinAlg.C          SolveLinearSystemLapack (:106-131)
 //
 // What the harness supplies instead of the mesh and FE machinery:
-// * LevelSpace: a TFESpace3D whose DOF maps (GlobalNumbers, BeginIndex), DOF
-//   count, active / hanging / Dirichlet bounds and per-cell element ids
-//   (AllElements, which TFESpace3D::GetFE3D returns before it would look at
-//   a cell, src/FE/FESpace3D.C:412-422) are set from the level's arrays.
-//   There are no hanging nodes.  The collection's cell array holds null
+// * LevelSpace (ref_level_space.h): a TFESpace3D filled from the level's
+//   arrays.  The collection's cell array holds null
 //   pointers: code on this path reads the array but no cell.
 // * TFEDatabase3D::FEs3D: storage for the element table, whose two used
 //   entries are registered (RegisterFE3D) as elements with 27 (or 15) and 4
@@ -61,6 +58,8 @@
 #include <SquareMatrix3D.h>
 #include <SquareStructure3D.h>
 #include <Structure3D.h>
+
+#include "ref_level_space.h"
 
 TFE3D *TFEDatabase3D::FEs3D[N_FEs3D] = {nullptr};
 
@@ -149,25 +148,6 @@ struct FixedElement : public TFE3D {
 // element ids the level's spaces name (any two distinct ids serve)
 const FE3D kVelocityElement = C_Q2_3D_H_A;
 const FE3D kPressureElement = D_P1_3D_H_A;
-
-struct LevelSpace : public TFESpace3D {
-  LevelSpace(TCollection *coll, int n_dof, int active, int n_dirichlet, int *global, int *begin,
-             FE3D *all)
-      : TFESpace3D(coll, (char *)"harness", (char *)"harness") {
-    N_DegreesOfFreedom = n_dof;
-    GlobalNumbers = global;
-    BeginIndex = begin;
-    ActiveBound = active;
-    HangingBound = active;
-    DirichletBound = n_dof;
-    InnerBound = active;
-    N_Inner = active;
-    N_Dirichlet = n_dirichlet;
-    N_ActiveDegrees = active;
-    N_SlaveDegrees = 0;
-    AllElements = all;
-  }
-};
 
 struct LevelSquareStructure : public TSquareStructure3D {
   LevelSquareStructure(int n, int active, int nnz, int *col, int *rowptr, TFESpace3D *space)
@@ -321,10 +301,7 @@ __attribute__((visibility("default"))) void ref_vanka_destroy(void *h) {
   delete V->sa;
   delete V->sb;
   delete V->sbt;
-  for (LevelSpace *s : {V->us, V->ps, V->oa, V->ob}) {
-    std::free(s->GetName());
-    std::free(s->GetDescription());
-  }
+  for (LevelSpace *s : {V->us, V->ps, V->oa, V->ob}) s->release_names();
   delete[] V->u_global;
   delete[] V->p_global;
   delete[] V->u_begin;

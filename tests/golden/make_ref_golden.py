@@ -3,6 +3,9 @@ builder, run through oracle/ref_harness.cpp and oracle/ref_vanka.cpp, which
 oracle/build_oracle.py compiles with the reference sources where they lie:
 * tests/golden/ref_defect_*.npz: Defect_NSE4 (with and without the P1disc
   pressure projection) and MatVect_NSE4 (src/FE/MGComponents3D.C:3210, :3030);
+* tests/golden/ref_transfer_*.npz: Prolongate of x and DefectRestriction
+  of b between a level and the next coarser one (src/FE/MGComponents3D.C:468,
+  :996 and the scalar versions for the pressure);
 * tests/golden/ref_vanka_*.npz: one and two sweeps of the cell Vanka
   TNSE_MGLevel4::CellVanka (src/FE/NSE_MGLevel4.C:1653-2087, sequential
   build, damping 1, no relaxation) from u = x with right-hand side b.
@@ -56,8 +59,15 @@ VANKA_CASES = {
 }
 
 
+# name -> (OseenProblem keyword arguments, fine level) of the transfer fixtures
+TRANSFER_CASES = {
+    "hexa": (CASES["hexa"][0], 1),
+    "channel": (CASES["channel"][0], 1),
+}
+
+
 def main() -> None:
-    from oracle.pyref import RefLevel, RefVankaLevel, ref_harness_lib
+    from oracle.pyref import RefLevel, RefTransfer, RefVankaLevel, ref_harness_lib
     if ref_harness_lib() is None:
         raise SystemExit("reference tree not found; cannot regenerate the defect golden files")
     for name, (kwargs, level) in CASES.items():
@@ -82,6 +92,18 @@ def main() -> None:
             source=("reference src/FE/NSE_MGLevel4.C TNSE_MGLevel4::CellVanka (_SEQ) "
                     "run by oracle/ref_vanka.cpp"))
         print("wrote vanka", name, "level", level, "ndof", P.ndof(level))
+    for name, (kwargs, level) in TRANSFER_CASES.items():
+        P = build_problem(kwargs)
+        T = RefTransfer(P, level)
+        xc, _ = golden_inputs(P.ndof(level - 1))
+        _, bf = golden_inputs(P.ndof(level))
+        np.savez_compressed(
+            HERE / f"ref_transfer_{name}.npz",
+            problem=json.dumps(kwargs), level=level, prolongated=T.prolongate(xc),
+            restricted=T.restrict(bf),
+            source=("reference src/FE/MGComponents3D.C Prolongate / DefectRestriction "
+                    "run by oracle/ref_transfer.cpp"))
+        print("wrote transfer", name, "level", level)
 
 
 if __name__ == "__main__":

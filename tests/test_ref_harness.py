@@ -22,6 +22,11 @@ reference's numbers:
   last bits of the assembled matrices);
 * the FP64 CUDA kernels: relative 1e-12 (summation order and FMA contraction
   differ).
+oracle/ref_transfer.cpp runs the reference's Prolongate and DefectRestriction
+(src/FE/MGComponents3D.C), with the per-child matrices its FE database
+computes, between levels built here; they agree with the oracle's to
+summation order (1e-14), and their outputs are the fixtures
+tests/golden/ref_transfer_*.npz (oracle 1e-13, GPU 1e-12).
 The reference's Vanka sweeps are committed as tests/golden/ref_vanka_*.npz.
 The GPU's colour-block sweep equals the sequential cell loop when every cell
 is its own colour, so the CUDA Vanka is checked against the reference's with
@@ -71,8 +76,10 @@ def load_case(name, kind="defect"):
     if kind == "defect":
         assert P.arrays(level)["n_udof"] == int(g["n_udof"])
         assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
-    else:
+    elif kind == "vanka":
         assert P.arrays(level)["n_cells"] == int(g["n_cells"])
+    if kind == "transfer":  # x on the coarse level, b on the fine one
+        return P, level, gm.golden_inputs(P.ndof(level - 1))[0], gm.golden_inputs(P.ndof(level))[1], g
     x, b = gm.golden_inputs(P.ndof(level))
     return P, level, x, b, g
 
@@ -273,6 +280,56 @@ def test_oracle_vanka_matches_reference_fixtures(name):
     assert rel(Oc.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-13
 
 
+def ref_transfer_or_skip():
+    from oracle.pyref import ref_transfer_lib
+    if ref_transfer_lib() is None:
+        pytest.skip("reference tree not present (the committed fixtures cover this case)")
+
+
+TRANSFER_PROBLEMS = {
+    "hexa": dict(n_levels=3, nu=1e-2, seed=0),
+    "channel": dict(n_levels=2, nu=0.1, seed=0, example="channel", periodic="xz",
+                    stretch_y=1.5, box=(0.0, 6.0, -1.0, 1.0, 0.0, 3.0)),
+}
+
+
+@pytest.mark.parametrize("case", list(TRANSFER_PROBLEMS))
+def test_oracle_transfers_match_the_reference_transfers(case):
+    """Prolongate / DefectRestriction of the reference, with the per-child
+    Q2 and P1disc matrices its FE database computes from the elements' nodal
+    functionals, against the oracle's: equal up to summation order (the two
+    accumulate shared fine DOFs in different cell orders)."""
+    ref_transfer_or_skip()
+    from oracle.pyref import RefTransfer
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    P = OseenProblem(**TRANSFER_PROBLEMS[case])
+    O = Oracle(P)
+    rng = np.random.default_rng(31)
+    for level in range(1, P.n_levels):
+        T = RefTransfer(P, level)
+        xc, xf = rng.standard_normal(P.ndof(level - 1)), rng.standard_normal(P.ndof(level))
+        assert rel(T.prolongate(xc), O.prolongate(level, xc)) < 1e-14
+        assert rel(T.restrict(xf), O.restrict(level, xf)) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["hexa", "channel"])
+def test_transfer_fixtures_reproduce_from_the_reference(name):
+    ref_transfer_or_skip()
+    from oracle.pyref import RefTransfer
+    P, level, xc, bf, g = load_case(name, "transfer")
+    T = RefTransfer(P, level)
+    assert np.array_equal(T.prolongate(xc), g["prolongated"])
+    assert np.array_equal(T.restrict(bf), g["restricted"])
+
+
+@pytest.mark.parametrize("name", ["hexa", "channel"])
+def test_oracle_transfers_match_reference_fixtures(name):
+    P, level, xc, bf, g = load_case(name, "transfer")
+    O = Oracle(P)
+    assert rel(O.prolongate(level, xc), g["prolongated"]) < 1e-13
+    assert rel(O.restrict(level, bf), g["restricted"]) < 1e-13
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_fixtures_reproduce_from_the_reference(name):
     """The committed fixtures are what the reference computes here."""
@@ -330,3 +387,15 @@ def test_gpu_cell_vanka_matches_reference_fixtures(name):
     assert rel(S.cell_vanka(level, x, b, 1), g["u_sweep1"]) < 1e-9
     assert rel(S.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-9
     del colours
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hexa", "channel"])
+def test_gpu_transfers_match_reference_fixtures(name):
+    """The CUDA prolongation / restriction (host-built CSR of the per-child
+    matrices) against the reference's own Prolongate / DefectRestriction."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, xc, bf, g = load_case(name, "transfer")
+    S = PmSolver(P.descs, precision="fp64")
+    assert rel(S.prolongate(level, xc), g["prolongated"]) < 1e-12
+    assert rel(S.restrict(level, bf), g["restricted"]) < 1e-12
