@@ -51,6 +51,8 @@ def ref_harness_lib():
         L.ref_vanka_destroy.restype = None
         L.ref_vanka_sweeps.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double]
         L.ref_vanka_sweeps.restype = None
+        L.ref_vanka_solve_exact.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
+        L.ref_vanka_solve_exact.restype = None
         _LIB = L
     return _LIB
 
@@ -214,6 +216,16 @@ class RefVankaLevel:
         rhs, rp = _d(rhs)
         assert u.size == rhs.size == 3 * self.n_u + self.n_p
         self._L.ref_vanka_sweeps(self._h, u.ctypes.data_as(_dp), rp, sweeps, damp)
+        return u
+
+    def solve_exact(self, rhs, pin_pressure: bool = True) -> np.ndarray:
+        """TNSE_MGLevel4::SolveExact: the dense solve of the level's system,
+        the first pressure equation replaced by p_0 = 0 when
+        ``pin_pressure`` (INTERNAL_PROJECT_PRESSURE)."""
+        rhs, rp = _d(rhs)
+        assert rhs.size == 3 * self.n_u + self.n_p
+        u = np.zeros(rhs.size)
+        self._L.ref_vanka_solve_exact(self._h, u.ctypes.data_as(_dp), rp, int(pin_pressure))
         return u
 
 

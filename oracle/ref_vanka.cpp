@@ -7,11 +7,12 @@
 // restates).
 //
 // Reference code that runs here:
-//   src/FE/NSE_MGLevel4.C    TNSE_MGLevel4 constructor (:119-328) and the _SEQ
+//   src/FE/NSE_MGLevel4.C    TNSE_MGLevel4 constructor (:119-328), the _SEQ
 //                            CellVanka (:1653-2087): local 85x85 (or 49x49)
 //                            systems from the global matrices, the direct
 //                            local solve, the damped update, the relaxation
-//                            and the Dirichlet values
+//                            and the Dirichlet values; and SolveExact
+//                            (:5728-5847), the dense coarse solve
 //   src/FE/NSE_MGLevel.C     TNSE_MGLevel constructor, SetHangingNodes
 //   src/FE/FESpace.C, FESpace3D.C, src/Geometry/Collection.C, src/FE/FE3D.C,
 //   SquareStructure3D.C, SquareMatrix3D.C, Matrix3D.C, Structure3D.C
@@ -330,6 +331,21 @@ __attribute__((visibility("default"))) void ref_vanka_sweeps(void *h, double *u,
   db->INTERNAL_LOCAL_DOF = -1;
   double *r = copy_of(rhs, V->n);
   for (int s = 0; s < sweeps; ++s) V->level->CellVanka(u, r, V->aux, 0, nullptr, 2, 1);
+  delete[] r;
+}
+
+// TNSE_MGLevel4::SolveExact(u, rhs) (src/FE/NSE_MGLevel4.C:5728-5847): the
+// level's full system as a dense matrix, solved by SolveLinearSystemLapack;
+// u is overwritten.  With pin_pressure (INTERNAL_PROJECT_PRESSURE) the first
+// pressure equation becomes p_0 = 0 (:5822-5832), as in the solver's runs.
+__attribute__((visibility("default"))) void ref_vanka_solve_exact(void *h, double *u,
+                                                                  const double *rhs,
+                                                                  int pin_pressure) {
+  VankaLevel *V = static_cast<VankaLevel *>(h);
+  TDatabase::ParamDB->INTERNAL_PROJECT_PRESSURE = pin_pressure;
+  TDatabase::ParamDB->INTERNAL_PRESSURE_SPACE = -11;
+  double *r = copy_of(rhs, V->n);
+  V->level->SolveExact(u, r);
   delete[] r;
 }
 

@@ -6,6 +6,9 @@ oracle/build_oracle.py compiles with the reference sources where they lie:
 * tests/golden/ref_transfer_*.npz: Prolongate of x and DefectRestriction
   of b between a level and the next coarser one (src/FE/MGComponents3D.C:468,
   :996 and the scalar versions for the pressure);
+* tests/golden/ref_coarse_*.npz: the coarse solve TNSE_MGLevel4::SolveExact
+  (src/FE/NSE_MGLevel4.C:5728-5847, first pressure equation p_0 = 0) of b
+  on the coarsest level;
 * tests/golden/ref_vanka_*.npz: one and two sweeps of the cell Vanka
   TNSE_MGLevel4::CellVanka (src/FE/NSE_MGLevel4.C:1653-2087, sequential
   build, damping 1, no relaxation) from u = x with right-hand side b.
@@ -92,6 +95,16 @@ def main() -> None:
             source=("reference src/FE/NSE_MGLevel4.C TNSE_MGLevel4::CellVanka (_SEQ) "
                     "run by oracle/ref_vanka.cpp"))
         print("wrote vanka", name, "level", level, "ndof", P.ndof(level))
+    for name, (kwargs, _) in CASES.items():
+        P = build_problem(kwargs)
+        V = RefVankaLevel(P.arrays(0))
+        _, b = golden_inputs(P.ndof(0))
+        np.savez_compressed(
+            HERE / f"ref_coarse_{name}.npz", problem=json.dumps(kwargs), level=0,
+            n_cells=P.arrays(0)["n_cells"], solution=V.solve_exact(b),
+            source=("reference src/FE/NSE_MGLevel4.C TNSE_MGLevel4::SolveExact "
+                    "run by oracle/ref_vanka.cpp"))
+        print("wrote coarse", name, "ndof", P.ndof(0))
     for name, (kwargs, level) in TRANSFER_CASES.items():
         P = build_problem(kwargs)
         T = RefTransfer(P, level)

@@ -27,7 +27,9 @@ oracle/ref_transfer.cpp runs the reference's Prolongate and DefectRestriction
 computes, between levels built here; they agree with the oracle's to
 summation order (1e-14), and their outputs are the fixtures
 tests/golden/ref_transfer_*.npz (oracle 1e-13, GPU 1e-12).
-The reference's Vanka sweeps are committed as tests/golden/ref_vanka_*.npz.
+The reference's Vanka sweeps are committed as tests/golden/ref_vanka_*.npz,
+and its coarse solves (TNSE_MGLevel4::SolveExact, which the oracle equals bit
+for bit) as tests/golden/ref_coarse_*.npz (oracle 1e-12, GPU 1e-10).
 The GPU's colour-block sweep equals the sequential cell loop when every cell
 is its own colour, so the CUDA Vanka is checked against the reference's with
 such a colouring, at 1e-9 relative (FP64 LU rounding).
@@ -76,7 +78,7 @@ def load_case(name, kind="defect"):
     if kind == "defect":
         assert P.arrays(level)["n_udof"] == int(g["n_udof"])
         assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
-    elif kind == "vanka":
+    elif kind in ("vanka", "coarse"):
         assert P.arrays(level)["n_cells"] == int(g["n_cells"])
     if kind == "transfer":  # x on the coarse level, b on the fine one
         return P, level, gm.golden_inputs(P.ndof(level - 1))[0], gm.golden_inputs(P.ndof(level))[1], g
@@ -280,6 +282,29 @@ def test_oracle_vanka_matches_reference_fixtures(name):
     assert rel(Oc.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-13
 
 
+@pytest.mark.parametrize("case", ["hexa", "hexa-alpha", "channel", "tetra"])
+def test_oracle_coarse_solve_equals_reference_solve_exact_bitwise(case):
+    """The dense coarse matrix (Dirichlet rows, B / BT blocks, p_0 = 0) and
+    its solve, on the coarsest level."""
+    ref_lib_or_skip()
+    from oracle.pyref import RefVankaLevel
+    from to_merge_master_parmoon_gb300 import OseenProblem
+    P = OseenProblem(**VANKA_CASES[case][0])
+    O = Oracle(P)
+    b = np.random.default_rng(41).standard_normal(P.ndof(0))
+    assert np.array_equal(RefVankaLevel(P.arrays(0)).solve_exact(b), O.solve_exact(b))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_coarse_fixtures_reproduce_and_pin_the_oracle(name):
+    P, level, _, b, g = load_case(name, "coarse")
+    assert rel(Oracle(P).solve_exact(b), g["solution"]) < 1e-12
+    from oracle.pyref import ref_harness_lib
+    if ref_harness_lib() is not None:
+        from oracle.pyref import RefVankaLevel
+        assert np.array_equal(RefVankaLevel(P.arrays(level)).solve_exact(b), g["solution"])
+
+
 def ref_transfer_or_skip():
     from oracle.pyref import ref_transfer_lib
     if ref_transfer_lib() is None:
@@ -399,3 +424,14 @@ def test_gpu_transfers_match_reference_fixtures(name):
     S = PmSolver(P.descs, precision="fp64")
     assert rel(S.prolongate(level, xc), g["prolongated"]) < 1e-12
     assert rel(S.restrict(level, bf), g["restricted"]) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_coarse_solve_matches_reference_fixtures(name):
+    """The GPU coarse solve (pinned dense LU and its inverse) against the
+    reference's own SolveExact."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, _, b, g = load_case(name, "coarse")
+    S = PmSolver(P.descs, precision="fp64")
+    assert rel(S.solve_exact(b), g["solution"]) < 1e-10
