@@ -94,8 +94,15 @@ namespace {
 struct HarnessCell : public TGridCell {
   explicit HarnessCell(TRefDesc *rd) : TGridCell(rd, 0) {}
   void set_children(TBaseCell **c) { Children = c; }
-  TBaseCell **children() { return Children; }
-  TVertex **vertices() { return Vertices; }
+  // the arrays the TBaseCell and TGridCell constructors allocate
+  // (src/Geometry/BaseCell.C:16-45, src/Geometry/GridCell.C:22-30)
+  void release_arrays() {
+    delete[] Children;
+    Children = nullptr;
+    delete[] Vertices;
+    delete[] Joints;
+    delete[] Edges;
+  }
 };
 
 bool g_ready = false;
@@ -227,9 +234,7 @@ void make_side(Side &S, int n_cells, int n_u, int n_active, int n_p, const int *
 
 void free_side(Side &S) {
   for (HarnessCell *c : S.cells) {
-    delete[] c->children();
-    c->set_children(nullptr);
-    delete[] c->vertices();
+    c->release_arrays();
     ::operator delete(static_cast<void *>(c));  // storage only: no reference destructor
   }
   S.us->release_names();
