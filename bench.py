@@ -13,8 +13,17 @@ pm_solve.
 
 ``--impl reference`` times the CPU restatement of the reference solver
 (oracle/, FP64, every Vanka block refactored in every sweep as in
-src/FE/NSE_MGLevel4.C:1653-2087) on all host cores, on a bounded sample:
-one FGMRES iteration per step, scaled by the iteration count of the solve.
+src/FE/NSE_MGLevel4.C:1653-2087) on all host cores: one complete solve to
+1e-8 (its measured wall time is the value), then one FGMRES iteration per
+step as the bounded per-step sample.
+
+The same oracle solve at the full size is ``cpu_baseline`` of the default
+run, and its solution is the answer every GPU variant's ``error_vs_oracle``
+(relative L2 of velocity and of the L2_0-normalised pressure) is taken
+against.  ``cpu_runs_16cube`` adds the three CPU settings of the
+CPU-runnable case (16^3, rtol 1e-10): one thread with the reference's
+cell-by-cell Vanka, all cores with colour-parallel Vanka, and all cores
+with the local factors kept across sweeps.
 """
 from __future__ import annotations
 
@@ -170,20 +179,131 @@ def ncu_traffic(P):
     return per_cell * sum(cells) / (8 * len(cells))
 
 
-def cpu_baseline(P, iterations, levels, threads):
-    """Oracle (FP64, per-sweep refactorisation as the reference) on the host
-    cores: one FGMRES iteration at the full size, scaled by `iterations`."""
+def split_error(x, ref, nu):
+    """Relative L2 differences of the velocity [u1|u2|u3] and of the pressure
+    after the same L2_0 normalisation of both (the constant P1disc modes,
+    every 4th pressure entry, as IntoL20FEFunction3D)."""
+    import numpy as np
+    n3 = 3 * nu
+    xp, rp = x[n3:].copy(), ref[n3:].copy()
+    xp[0::4] -= xp[0::4].mean()
+    rp[0::4] -= rp[0::4].mean()
+    return {"u": float(np.linalg.norm(x[:n3] - ref[:n3]) / np.linalg.norm(ref[:n3])),
+            "p": float(np.linalg.norm(xp - rp) / np.linalg.norm(rp))}
+
+
+def oracle_solve(P, b, tol, threads, maxit=200, **params):
+    """The oracle's FGMRES(20) + V(2,2) from x0 = 0 to ||b - K x|| <= tol on
+    `threads` host threads; returns (solution, result, wall seconds)."""
     import numpy as np
     from oracle.pyoracle import Oracle
-    b = P.rhs()
-    O = Oracle(P, restart=20, maxit=1, res_norm_min=0.0, nthreads=threads)
+    O = Oracle(P, restart=20, maxit=maxit, res_norm_min=tol, nthreads=threads, **params)
     t = time.perf_counter()
-    O.iterate(np.zeros_like(b), b)
-    dt = time.perf_counter() - t
-    return dt
+    x, info = O.iterate(np.zeros_like(b), b)
+    return x, info, time.perf_counter() - t
+
+
+def pressure_projected_norm(P, b):
+    """||b - K 0|| with the pressure part projected (Defect_NSE4 of x0 = 0)."""
+    import numpy as np
+    bp = b.copy()
+    nu3 = 3 * P.desc(P.n_levels - 1).n_udof
+    bp[nu3::4] -= bp[nu3::4].mean()
+    return float(np.linalg.norm(bp))
+
+
+def cpu_runs_16cube(threads, device):
+    """The CPU-runnable case (16^3 cells, 4 levels, nu = 1e-2, seed 0,
+    FGMRES(20) + V(2,2), rtol 1e-10) in the three CPU settings: (1) one
+    thread, the reference's cell-by-cell Vanka (_SEQ,
+    src/FE/NSE_MGLevel4.C:1653-2087) refactoring every block in every sweep;
+    (2) all cores, colour-parallel Vanka (the _HYBRID colour loop,
+    :807-820), refactoring every sweep; (3) as (2) with the local factors
+    kept across sweeps (separates the algorithmic gain of factor reuse from
+    the GPU's).  Beside them the GPU FP64 and mixed solves of the same
+    system; every result with its error against setting (2)."""
+    import numpy as np
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    P = OseenProblem(n_levels=4, nu=1e-2, seed=0, nthreads=threads)
+    b = P.rhs()
+    tol = 1e-10 * pressure_projected_norm(P, b)
+    nu = P.desc(3).n_udof
+    runs = {}
+    x2, i2, t2 = oracle_solve(P, b, tol, threads)
+    for name, th, params in (("run1_one_thread_seq", 1, {"vanka_mode": "seq"}),
+                             ("run2_all_cores", threads, {}),
+                             ("run3_all_cores_factor_reuse", threads, {"reuse_factors": 1})):
+        if name == "run2_all_cores":
+            x, i, t = x2, i2, t2
+        else:
+            x, i, t = oracle_solve(P, b, tol, th, **params)
+        runs[name] = {"s": t, "threads": th, "iterations": i["iterations"],
+                      "rel_res": i["true_res"] / i["res0"], "error_vs_oracle": split_error(x, x2, nu)}
+    for prec in ("fp64", "mixed"):
+        S = PmSolver(P.descs, precision=prec, device=device, restart=20, maxit=200,
+                     res_norm_min=tol)
+        S.iterate(np.zeros_like(b), b)  # untimed: graph capture
+        f_ms = S.refactor()
+        t = time.perf_counter()
+        x, i = S.iterate(np.zeros_like(b), b)
+        t = time.perf_counter() - t
+        runs[f"gpu_{prec}"] = {"s": t + f_ms * 1e-3, "factor_ms": f_ms, "solve_ms": i["solve_ms"],
+                               "iterations": i["iterations"], "rel_res": i["true_res"] / i["res0"],
+                               "error_vs_oracle": split_error(x, x2, nu)}
+        S.close()
+    return {"workload": "steady 3D Oseen, Q2/P1disc, 16^3 cells, 4 levels from 2^3, nu=0.01, "
+                        "seed 0, FGMRES(20)+V(2,2), rtol 1e-10", "ndof": P.ndof(-1),
+            "timer": "wall clock (time.perf_counter) around the solve, set-up excluded; GPU "
+                     "rows: refactorisation + solve with host vectors", **runs}
+
+
+def solve_bytes(P, s, iterations, nblk=9, pre=2, post=2, restart=20):
+    """Algorithmic (unique) bytes of one FGMRES solve of `iterations`
+    iterations: per iteration one V(pre,post) cycle in value size `s` (8
+    FP64, 4 FP32), one FP64 mat-vec on the finest level and the modified
+    Gram-Schmidt vector traffic.  Per level with cells, matrix bytes
+    mat = nblk s nnzA + 4 nnzA + 4 (N_U+1) + (3 s + 4)(nnzB + nnzBT)
+    + 4 (N_P+1) + 4 (N_U+1); defect = mat + 3 s DOF; Vanka sweep = mat +
+    3 s DOF + cells (85^2 s + 85) (stored LU and pivots); transfers
+    s (2 DOF_f + 2 DOF_c); the coarse dense solve reads its inverse (FP64).
+    Arnoldi step k of a restart cycle: (k+1) x (2 + 3) x 8 DOF."""
+    L = P.n_levels
+    nbytes = 0.0
+
+    def mat(d, sv, nb):
+        return (nb * sv * d.a_nnz + 4.0 * d.a_nnz + 4.0 * (d.n_udof + 1)
+                + (3 * sv + 4.0) * (d.b_nnz + d.bt_nnz) + 4.0 * (d.n_pdof + 1)
+                + 4.0 * (d.n_udof + 1))
+
+    for l in range(1, L):
+        d = P.desc(l)
+        dof = 3 * d.n_udof + d.n_pdof
+        nloc = 3 * d.n_ulocal + d.n_plocal
+        m = mat(d, s, nblk)
+        sweep = m + 3 * s * dof + d.n_cells * (nloc * nloc * s + nloc)
+        dc = P.desc(l - 1)
+        dof_c = 3 * dc.n_udof + dc.n_pdof
+        nbytes += (pre + post) * sweep + (m + 3 * s * dof) + s * (2 * dof + 2 * dof_c)
+    d0 = P.desc(0)
+    n0 = 3 * d0.n_udof + d0.n_pdof
+    nbytes += 8.0 * n0 * n0
+    df = P.desc(L - 1)
+    dof_f = 3 * df.n_udof + df.n_pdof
+    per_it_fixed = nbytes + mat(df, 8, nblk) + 2 * 8.0 * dof_f
+    total = 0.0
+    for j in range(iterations):
+        k = j % restart
+        total += per_it_fixed + (k + 1) * 5 * 8.0 * dof_f
+    return total
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the reference's algorithm restated on
+    the CPU, FP64, every local block refactored in every sweep) on all host
+    threads, on rank 0 only.  One complete solve to 1e-8 is timed first; its
+    wall time is the value (time to tolerance).  Then warm-up + steps bounded
+    samples of one FGMRES iteration each (V(2,2) + mat-vec + MGS) give the
+    per-step time."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -193,8 +313,9 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed, nthreads=threads)
     b = P.rhs()
+    tol = RTOL * pressure_projected_norm(P, b)
+    _, info, t_full = oracle_solve(P, b, tol, threads)
     O = Oracle(P, restart=20, maxit=1, res_norm_min=0.0, nthreads=threads)
-    iters = FGMRES_ITERATIONS.get((args.levels, args.nu), 10)
     times = []
     for s in range(args.warmup + args.steps):
         t = time.perf_counter()
@@ -203,7 +324,7 @@ def run_reference(args):
         if s >= args.warmup:
             times.append(dt)
     per_it = sum(times) / len(times)
-    value = per_it * iters
+    value = t_full
     n = args.levels
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
@@ -213,9 +334,12 @@ def run_reference(args):
         "config": {"workload": f"steady 3D Oseen, Q2/P1disc, {2 ** n}^3 cells, {n} levels from 2^3, "
                                f"nu={args.nu}, FGMRES(20)+V(2,2) cell Vanka, rtol 1e-8",
                    "ndof": P.ndof(-1)},
+        "iterations": info["iterations"], "rel_res": info["true_res"] / info["res0"],
+        "per_iteration_s": per_it,
         "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
-                         "sample": f"one FGMRES iteration (V(2,2) + mat-vec + MGS) per step at "
-                                   f"the full size, x {iters} iterations to 1e-8"},
+                         "sample": f"one complete solve to 1e-8 at the full size, timed once "
+                                   f"({info['iterations']} FGMRES iterations); each step: one "
+                                   f"FGMRES iteration (V(2,2) + mat-vec + MGS)"},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -498,11 +622,6 @@ def train_network(device, args, log=None):
     return net, info
 
 
-# FGMRES iterations to 1e-8 of this workload (measured on the GPU FP64 path,
-# which runs the same algorithm as the reference; used to scale the CPU sample)
-FGMRES_ITERATIONS = {(6, 1e-2): 10, (5, 1e-2): 10, (4, 1e-2): 9}
-
-
 def batch_run(args, device, log=None):
     """Batched independent systems of uneven size: sizes drawn uniformly from
     {8^3, 16^3, 32^3} cubes, nu log-uniform in [1e-3, 1e-1], seeds 100+s;
@@ -591,11 +710,7 @@ def main():
     d_b = torch.from_numpy(b).cuda()
     d_x = torch.zeros(n, dtype=torch.float64, device="cuda")
 
-    # ||b - K 0|| with the pressure part projected (Defect_NSE4 of x0 = 0)
-    bp = b.copy()
-    nu3 = 3 * P.desc(args.levels - 1).n_udof
-    bp[nu3::4] -= bp[nu3::4].mean()
-    r0 = float(np.linalg.norm(bp))
+    r0 = pressure_projected_norm(P, b)
     # learned smoother: trained once (harvest on 32^3 problems, GPU training),
     # outside the timed region; cached by configuration in the build folder
     net, learned_info = train_network(local, args, log=lambda *a: print(*a, file=sys.stderr))
@@ -641,7 +756,7 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    results = {}
+    results, solutions = {}, {}
     for prec, S in solvers.items():
         for _ in range(args.warmup):
             step(S)
@@ -663,6 +778,7 @@ def main():
             barrier()
             wall = time.perf_counter() - t0
             torch.cuda.nvtx.range_pop()
+        solutions[prec] = d_x.cpu().numpy()
         results[prec] = {
             "ms": sum(t_dev) / len(t_dev), "wall_ms": wall * 1e3 / args.steps,
             "factor_ms": fms, "solve_ms": info["solve_ms"], "iterations": iters[-1],
@@ -728,6 +844,21 @@ def main():
 
     if rank != 0:
         return
+    cpu = cpu16 = None
+    errors = {}
+    if not args.no_cpu_baseline:
+        # the oracle's complete solve at the full size: the CPU baseline's
+        # time to tolerance and the answer every GPU variant is checked against
+        xo, io, t_or = oracle_solve(P, b, RTOL * r0, threads)
+        cpu = {"value": t_or, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"oracle FGMRES(20)+V(2,2) solve to 1e-8 at the full size, timed once "
+                         f"({io['iterations']} iterations, colour-parallel cell Vanka refactoring "
+                         f"every local block in every sweep)",
+               "iterations": io["iterations"], "rel_res": io["true_res"] / io["res0"]}
+        nu_f = P.desc(args.levels - 1).n_udof
+        errors = {k: split_error(x, xo, nu_f) for k, x in solutions.items()}
+        del xo
+        cpu16 = cpu_runs_16cube(threads, local)
     peak, peak_kind = measured_peaks()
     prof = results["mixed"].get("profile", {})
 
@@ -749,6 +880,15 @@ def main():
                                      "substitution + update)",
                              "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,
                              "avg_launch_ms": a_ms, "bytes_per_launch": a_bytes}}
+    def whole_solve(name, s_val):
+        r = results[name]
+        nb = solve_bytes(P, s_val, r["iterations"])
+        gbs = nb / (r["solve_ms"] * 1e-3) / 1e9
+        return {"algorithmic_gb": nb / 1e9, "achieved_gbs": gbs, "frac": gbs / peak,
+                "note": "unique bytes of the whole FGMRES solve (V-cycles, FP64 mat-vecs, "
+                        "Gram-Schmidt) / solve time; peak = measured HBM copy bandwidth"}
+
+    whole = {"fp64": whole_solve("fp64", 8), "mixed": whole_solve("mixed", 4)}
     one = None
     if one_block:
         one = {"note": "same system as NSTYPE-2 levels (a[0] only); exact block solve of the "
@@ -758,19 +898,13 @@ def main():
             r = results[name]
             one[name] = {"value": r["ms"] * 1e-3,
                          **{k: r[k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res")},
+                         "error_vs_oracle": errors.get(name),
                          "sweep_kernels": {
                              k: {"ms_total": v["ms"], "launches": v["launches"],
                                  "achieved_gbs": kernel_roof(v)[0],
                                  "frac": (kernel_roof(v)[0] / peak) if v["ms"] else None}
                              for k, v in r.get("profile", {}).items()}}
         one["e2e"] = e2e1
-    cpu = None
-    if not args.no_cpu_baseline:
-        per_it = cpu_baseline(P, results["fp64"]["iterations"], args.levels, threads)
-        its = results["fp64"]["iterations"]
-        cpu = {"value": per_it * its, "unit": "s", "cores": threads, "kind": "port",
-               "sample": f"oracle: one FGMRES iteration (V(2,2) with per-sweep refactorisation, "
-                         f"mat-vec, MGS) at the full size = {per_it:.2f} s, x {its} iterations"}
     nlev = args.levels
     line = {
         "metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -789,26 +923,31 @@ def main():
                  "setup_s": results["fp64"]["setup_s"],
                  "factor_ms": results["fp64"]["factor_ms"], "solve_ms": results["fp64"]["solve_ms"],
                  "rel_res": results["fp64"]["rel_res"],
+                 "error_vs_oracle": errors.get("fp64"),
                  "sweep_kernels": {k: {"ms_total": v["ms"], "launches": v["launches"],
                                        "achieved_gbs": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] else None}
                                    for k, v in results["fp64"].get("profile", {}).items()}},
         "mixed": {"value": results["mixed"]["ms"] * 1e-3,
                   **{k: results["mixed"][k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res",
                                                       "vcycles_per_s", "dof_iterations_per_s",
-                                                      "setup_s")}},
+                                                      "setup_s")},
+                  "error_vs_oracle": errors.get("mixed")},
         "mixed_learned": {**{k: results["mixed_learned"][k]
                              for k in ("factor_ms", "solve_ms", "iterations", "rel_res", "wall_ms",
                                        "vcycles_per_s", "dof_iterations_per_s", "setup_s")},
                           "learned_status": results["mixed_learned"].get("learned"),
+                          "error_vs_oracle": errors.get("mixed_learned"),
                           "training": learned_info},
         "speedup_vs_fp64": results["fp64"]["ms"] / results["mixed_learned"]["ms"],
         "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "roofline": roof,
+        "whole_solve_roofline": whole,
         "one_block": one,
         "batch": batch,
         "assembly": assembly,
         "channel": channel,
         "cpu_baseline": cpu,
+        "cpu_runs_16cube": cpu16,
         "e2e": e2e,
         "gpu_launches": results["mixed_learned"]["launches"],
         "clocks": {k: results["mixed_learned"]["clocks"][k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},

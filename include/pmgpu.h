@@ -376,8 +376,8 @@ pm_status pm_learned_status(pm_handle *h, int *enabled, int *fallbacks);
 
 /* Allocation-free L2_0 projection of a P1disc pressure vector on the device
  * (subtract the mean of the constant modes d_p[0], d_p[4], ...), for callers
- * that cannot allocate device memory where they need it: code inside CUDA
- * stream capture, solvers confined to an application-owned memory pool, MPI
+ * that cannot allocate device memory where they need it: solvers confined to
+ * an application-owned memory pool whose budget is fixed up front, and MPI
  * ranks whose GPU memory is partitioned before the time loop.  No counterpart
  * in the reference (there the projection is host code, IntoL20Vector3D); it
  * computes what pm_coupled_defect's projection computes, without a handle.

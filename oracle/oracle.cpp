@@ -418,10 +418,8 @@ void add_local(const OLevel &L, int cell, double *u, const double *sol, double d
 void solve_local(oracle *o, OLevel &L, int cell, double *System, double *Rhs) {
   const int NLOC = L.nloc;
   if (o->p.reuse_factors) {
-    if (L.fac.empty()) {
-      L.fac.assign(L.d.n_cells, {});
-      L.piv.assign(L.d.n_cells, {});
-    }
+    // the per-cell slots exist (cell_vanka sizes them before any parallel
+    // loop); each cell is factored by the one thread that owns it
     if (L.fac[cell].empty()) {
       L.fac[cell].assign(System, System + NLOC * NLOC);
       L.piv[cell].assign(NLOC, 0);
@@ -442,6 +440,10 @@ void cell_vanka(oracle *o, OLevel &L, double *u, const double *rhs) {
   const int ncell = L.d.n_cells;
   set_dirichlet(L, u, rhs);
   std::vector<double> uold(u, u + L.ndof);
+  if (o->p.reuse_factors && L.fac.size() != (size_t)ncell) {
+    L.fac.assign(ncell, {});
+    L.piv.assign(ncell, {});
+  }
   if (o->p.vanka_mode == ORACLE_VANKA_SEQ) {
     std::vector<double> System(NLOC * NLOC), Rhs(NLOC);
     for (int c = 0; c < ncell; ++c) {

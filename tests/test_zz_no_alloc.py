@@ -1,9 +1,9 @@
 """pm_l20_project_noalloc: the allocation-free L2_0 pressure projection.
 
 It exists for callers that cannot allocate device memory where they need the
-projection (inside CUDA stream capture, inside an application-owned memory
-pool, MPI ranks with pre-partitioned GPU memory); its reduction scratch is a
-file-scope device array.  Checked through the C ABI against the projection
+projection (solvers inside an application-owned memory pool, MPI ranks with
+pre-partitioned GPU memory); its reduction scratch is a file-scope device
+array.  Checked through the C ABI against the projection
 the existing entry point pm_coupled_defect applies, on two calls in a row,
 within the FP64 tolerance of the other defect tests (1e-12 relative).
 

@@ -1,11 +1,10 @@
 // pm_noalloc.cu — allocation-free variant of the L2_0 pressure projection.
 //
 // Some callers of this library cannot allocate device memory at the point
-// where they need the projection: code that runs inside CUDA stream capture
-// (cudaMalloc is not capturable and synchronises the device), solvers that
-// run inside an application-owned memory pool whose budget is fixed up front,
-// and MPI-parallel ParMooN ranks that partition each GPU's memory before the
-// time loop starts.  For them, pm_l20_project_noalloc keeps the scratch of its
+// where they need the projection: solvers that run inside an
+// application-owned memory pool whose budget is fixed up front, and
+// MPI-parallel ParMooN ranks that partition each GPU's memory before the
+// time loop starts (a cudaMalloc there would also synchronise the device).  For them, pm_l20_project_noalloc keeps the scratch of its
 // deterministic two-stage reduction (one partial sum per block, the mean and
 // a completion counter) in the file-scope device array below instead of in
 // memory owned by a pm_handle.
