@@ -257,16 +257,20 @@ def cpu_runs_16cube(threads, device):
                      "rows: refactorisation + solve with host vectors", **runs}
 
 
-def solve_bytes(P, s, iterations, nblk=9, pre=2, post=2, restart=20):
+def solve_bytes(P, s, iterations, decoupled=False, pre=2, post=2, restart=20):
     """Algorithmic (unique) bytes of one FGMRES solve of `iterations`
     iterations: per iteration one V(pre,post) cycle in value size `s` (8
     FP64, 4 FP32), one FP64 mat-vec on the finest level and the modified
     Gram-Schmidt vector traffic.  Per level with cells, matrix bytes
     mat = nblk s nnzA + 4 nnzA + 4 (N_U+1) + (3 s + 4)(nnzB + nnzBT)
-    + 4 (N_P+1) + 4 (N_U+1); defect = mat + 3 s DOF; Vanka sweep = mat +
-    3 s DOF + cells (85^2 s + 85) (stored LU and pivots); transfers
-    s (2 DOF_f + 2 DOF_c); the coarse dense solve reads its inverse (FP64).
-    Arnoldi step k of a restart cycle: (k+1) x (2 + 3) x 8 DOF."""
+    + 4 (N_P+1) + 4 (N_U+1) with nblk = 9 A arrays, or 3 on decoupled
+    levels (A11, A22, A33); defect = mat + 3 s DOF; Vanka sweep = mat +
+    3 s DOF + the stored local solve per cell: 85^2 s + 85 (LU and pivots)
+    or 2851 s (block elimination: three 27x27 inverses, B, A^-1 BT and the
+    4x4 Schur inverse); transfers s (2 DOF_f + 2 DOF_c); the coarse dense
+    solve reads its inverse (FP64).  Arnoldi step k of a restart cycle:
+    (k+1) x (2 + 3) x 8 DOF."""
+    nblk = 3 if decoupled else 9
     L = P.n_levels
     nbytes = 0.0
 
@@ -280,7 +284,8 @@ def solve_bytes(P, s, iterations, nblk=9, pre=2, post=2, restart=20):
         dof = 3 * d.n_udof + d.n_pdof
         nloc = 3 * d.n_ulocal + d.n_plocal
         m = mat(d, s, nblk)
-        sweep = m + 3 * s * dof + d.n_cells * (nloc * nloc * s + nloc)
+        local = 2851 * s if decoupled else nloc * nloc * s + nloc
+        sweep = m + 3 * s * dof + d.n_cells * local
         dc = P.desc(l - 1)
         dof_c = 3 * dc.n_udof + dc.n_pdof
         nbytes += (pre + post) * sweep + (m + 3 * s * dof) + s * (2 * dof + 2 * dof_c)
@@ -719,19 +724,25 @@ def main():
     # copies.  The arrays are not page-locked: on the GB300 machine copies from
     # cudaHostRegister'ed memory fell to 5-10 GB/s after sustained GPU load
     # while pageable memory kept 175-190 GB/s.
-    def make(descs, prec):
-        kw = dict(precision=prec, device=local, restart=20, maxit=200, res_norm_min=RTOL * r0)
+    def make(descs, prec, **extra):
+        kw = dict(precision=prec, device=local, restart=20, maxit=200, res_norm_min=RTOL * r0,
+                  **extra)
         try:
             return PmSolver(descs, upload_mode=1, **kw)
         except PmError:
             return PmSolver(descs, upload_mode=0, **kw)
 
     solvers, setup_s = {}, {}
-    for name, prec in (("mixed_learned", "mixed"), ("mixed", "mixed"), ("fp64", "fp64")):
+    # the Galerkin levels have A12..A32 = 0: by default they run decoupled
+    # (A11, A22, A33 only, block-elimination cell solve); the *_lu variants
+    # keep the reference's 85x85 LU and all nine blocks (decouple=0)
+    for name, prec, extra in (("mixed_learned", "mixed", {}), ("mixed", "mixed", {}),
+                              ("fp64", "fp64", {}), ("mixed_lu", "mixed", {"decouple": 0}),
+                              ("fp64_lu", "fp64", {"decouple": 0})):
         # set-up: upload, colouring, transfers, local factorisation, coarse LU
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        solvers[name] = make(P.descs, prec)
+        solvers[name] = make(P.descs, prec, **extra)
         setup_s[name] = time.perf_counter() - t0
     solvers["mixed_learned"].attach_learned(net, omega=1.0, fallback_ratio=0.5)
     # the same system as NSTYPE-2 levels (one velocity block; the Galerkin
@@ -880,15 +891,30 @@ def main():
                                      "substitution + update)",
                              "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,
                              "avg_launch_ms": a_ms, "bytes_per_launch": a_bytes}}
-    def whole_solve(name, s_val):
+    def whole_solve(name, s_val, decoupled=True):
         r = results[name]
-        nb = solve_bytes(P, s_val, r["iterations"])
+        nb = solve_bytes(P, s_val, r["iterations"], decoupled=decoupled)
         gbs = nb / (r["solve_ms"] * 1e-3) / 1e9
         return {"algorithmic_gb": nb / 1e9, "achieved_gbs": gbs, "frac": gbs / peak,
                 "note": "unique bytes of the whole FGMRES solve (V-cycles, FP64 mat-vecs, "
                         "Gram-Schmidt) / solve time; peak = measured HBM copy bandwidth"}
 
-    whole = {"fp64": whole_solve("fp64", 8), "mixed": whole_solve("mixed", 4)}
+    whole = {"fp64": whole_solve("fp64", 8), "mixed": whole_solve("mixed", 4),
+             "fp64_lu": whole_solve("fp64_lu", 8, False),
+             "mixed_lu": whole_solve("mixed_lu", 4, False)}
+    lu = {"note": "the same nine-block system with decouple=0: every cell solved by the "
+                  "85x85 LU of the reference's CellVanka and all nine A blocks read"}
+    for name in ("mixed_lu", "fp64_lu"):
+        r = results[name]
+        lu[name] = {"value": r["ms"] * 1e-3,
+                    **{k: r[k] for k in ("factor_ms", "solve_ms", "iterations", "rel_res",
+                                         "vcycles_per_s", "dof_iterations_per_s", "setup_s")},
+                    "error_vs_oracle": errors.get(name),
+                    "sweep_kernels": {
+                        k: {"ms_total": v["ms"], "launches": v["launches"],
+                            "achieved_gbs": kernel_roof(v)[0],
+                            "frac": (kernel_roof(v)[0] / peak) if v["ms"] else None}
+                        for k, v in r.get("profile", {}).items()}}
     one = None
     if one_block:
         one = {"note": "same system as NSTYPE-2 levels (a[0] only); exact block solve of the "
@@ -942,6 +968,7 @@ def main():
         "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "roofline": roof,
         "whole_solve_roofline": whole,
+        "nine_block_lu": lu,
         "one_block": one,
         "batch": batch,
         "assembly": assembly,

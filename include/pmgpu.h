@@ -128,6 +128,25 @@ typedef struct {
                              1: to the residual at the start of the solve, so
                              that "reduce by red_factor" holds across
                              restarts (e.g. one time step solved to 1e-8)  */
+  int decouple;           /* 1 (default): a nine-block level whose
+                             off-diagonal blocks A12..A32 are all zero
+                             (checked on the device after every upload or
+                             assembly) reads only A11, A22, A33 in its
+                             defects and sweeps, and its cells are solved by
+                             exact block elimination (three 27x27 inverses
+                             and the 4x4 pressure Schur complement) instead
+                             of the 85x85 LU -- the same local solution;
+                             0: the 85x85 LU and all nine blocks on every
+                             nine-block level, as the reference's CellVanka
+                             (src/FE/NSE_MGLevel4.C:1784-2031)              */
+  int wait_limit;         /* polls of the first bounded mbarrier wait of the
+                             bulk-copy apply before it gives up (0: the
+                             default 2^22; the wait that drains the copies
+                             in flight keeps the default); a wait that gives
+                             up makes the solve return PM_TIMEOUT           */
+  long long max_device_bytes; /* cap on the device memory the handle
+                             allocates (0: none); an allocation beyond it
+                             fails with PM_OOM, as a failed cudaMalloc does  */
 } pm_options;
 
 /* One multigrid level in the reference's data layout.  Levels are added
@@ -220,6 +239,10 @@ int       pm_n_levels(pm_handle *h);
 int       pm_level_ndof(pm_handle *h, int level);
 /* velocity blocks of a level: 9 (NSTYPE 4) or 1 (NSTYPE 2); -1 if no such level */
 int       pm_level_blocks(pm_handle *h, int level);
+/* 1 if a nine-block level runs decoupled (pm_options.decouple and its
+ * A12..A32 are zero: diagonal blocks only, block-elimination cell solve),
+ * 0 if not, -1 if no such level */
+int       pm_level_decoupled(pm_handle *h, int level);
 /* kernels a level runs: residual kernel (0 row groups, 1 stream) + 2 * apply
  * kernel (0 two cells per warp, 1 bulk-staged, 2 one cell per warp); -1 if
  * no such level */

@@ -1,0 +1,123 @@
+"""Nine-block levels whose off-diagonal velocity blocks vanish (the Galerkin
+Oseen form, src/FE/NSE3D_FixPo.C:1919-2071) run decoupled: their defects and
+sweeps read A11, A22, A33 only and each cell's 85x85 system is solved by
+exact block elimination (three 27x27 inverses and the 4x4 pressure Schur
+complement) instead of the LU of the reference's CellVanka
+(src/FE/NSE_MGLevel4.C:1784-2031).  The local solution is the same, so the
+sweeps match the oracle's LU sweeps to the FP64 tolerance of the other
+Vanka tests (1e-9), the mixed ones to 5e-4, and FGMRES reaches the same
+solution (1e-6 after L2_0 normalisation) in the same FP64 iteration count.
+
+A level whose A12..A32 hold nonzero entries keeps the 85x85 LU and all nine
+blocks; pm_update_matrices re-checks after every upload and switches.
+"""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+OFFDIAG = (1, 2, 3, 5, 6, 7)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def normalise_p(v, nu):
+    v = v.copy()
+    v[3 * nu::4] -= v[3 * nu::4].mean()
+    return v
+
+
+def couple(P, eps):
+    """Velocity coupling A12 = A21 = eps A11 on every level (active rows: the
+    off-diagonal blocks of Dirichlet rows are ignored), in place."""
+    for level in range(P.n_levels):
+        a = P.arrays(level)
+        a["a"][1][:] = eps * a["a"][0]
+        a["a"][3][:] = eps * a["a"][0]
+
+
+def uncouple(P):
+    for level in range(P.n_levels):
+        a = P.arrays(level)
+        for k in OFFDIAG:
+            a["a"][k][:] = 0.0
+
+
+def fgmres_parity(P, S, oracle_params=None):
+    b = P.rhs()
+    x0 = np.zeros_like(b)
+    L = P.n_levels
+    r0 = np.linalg.norm(Oracle(P).coupled_defect(L - 1, x0, b))
+    tol = 1e-10 * r0
+    xo, io = Oracle(P, restart=20, maxit=80, res_norm_min=tol).iterate(x0, b)
+    xg, ig = S.iterate(x0, b)
+    nu = P.desc(L - 1).n_udof
+    return rel(normalise_p(xg, nu), normalise_p(xo, nu)), ig, io, tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_galerkin_levels_run_decoupled(problems, precision):
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P = problems(3, 1e-2, 0)
+    S = PmSolver(P.descs, precision=precision, restart=20, maxit=80)
+    assert [S.level_decoupled(l) for l in range(3)] == [True, True, True]
+    S0 = PmSolver(P.descs, precision=precision, decouple=0)
+    assert [S0.level_decoupled(l) for l in range(3)] == [False, False, False]
+    O = Oracle(P)
+    rng = np.random.default_rng(3)
+    tol = 1e-9 if precision == "fp64" else 5e-4
+    for level in (1, 2):
+        u = 0.1 * rng.standard_normal(P.ndof(level))
+        f = rng.standard_normal(P.ndof(level))
+        want = O.cell_vanka(level, u, f, 2)
+        assert rel(S.cell_vanka(level, u, f, 2), want) < tol
+        assert rel(S0.cell_vanka(level, u, f, 2), want) < tol
+        x, b = rng.standard_normal(P.ndof(level)), rng.standard_normal(P.ndof(level))
+        assert rel(S.coupled_defect(level, x, b), O.coupled_defect(level, x, b)) < (
+            1e-12 if precision == "fp64" else 1e-12)
+    S0.close()
+    S.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_decoupled_fgmres_matches_oracle(problems, precision):
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P = problems(3, 1e-2, 0)
+    b = P.rhs()
+    r0 = np.linalg.norm(Oracle(P).coupled_defect(2, np.zeros_like(b), b))
+    S = PmSolver(P.descs, precision=precision, restart=20, maxit=80, res_norm_min=1e-10 * r0)
+    d, ig, io, tol = fgmres_parity(P, S)
+    assert ig["true_res"] <= 1.05 * tol and d < 1e-6
+    if precision == "fp64":
+        assert ig["iterations"] == io["iterations"]
+    S.close()
+
+
+def test_coupled_blocks_keep_the_lu_and_update_switches():
+    """Set up on Galerkin values (block solve on every level), then
+    pm_update_matrices with A12 = A21 = 0.05 A11 switches every level to the
+    85x85 LU and the nine blocks (its factor storage grows), and back with
+    the uncoupled values; each time FGMRES matches the oracle's."""
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    P = OseenProblem(n_levels=3, nu=1e-2, seed=5)
+    b = P.rhs()
+    r0 = np.linalg.norm(Oracle(P).coupled_defect(2, np.zeros_like(b), b))
+    S = PmSolver(P.descs, precision="fp64", restart=20, maxit=80, res_norm_min=1e-10 * r0)
+    assert all(S.level_decoupled(l) for l in range(3))
+    d, ig, io, tol = fgmres_parity(P, S)
+    assert d < 1e-6 and ig["iterations"] == io["iterations"]
+    couple(P, 0.05)
+    S.update_matrices(P.descs)
+    assert not any(S.level_decoupled(l) for l in range(3))
+    d, ig, io, tol = fgmres_parity(P, S)
+    assert d < 1e-6 and ig["iterations"] == io["iterations"]
+    uncouple(P)
+    S.update_matrices(P.descs)
+    assert all(S.level_decoupled(l) for l in range(3))
+    d, ig, io, tol = fgmres_parity(P, S)
+    assert d < 1e-6 and ig["iterations"] == io["iterations"]
+    S.close()

@@ -93,7 +93,9 @@ def test_kernel_variants(P, oracle, variant, precision):
     apply (1 bulk-staged or two cells per warp, 2 one cell per warp) and the
     tuner's per-level choice (-1) give the same sweeps as the oracle."""
     from to_merge_master_parmoon_gb300 import PmSolver
-    S = PmSolver(P.descs, precision=precision, residual_variant=variant, apply_variant=variant)
+    # decouple=0: every level keeps the 85x85 LU, whose apply kernels are tested
+    S = PmSolver(P.descs, precision=precision, residual_variant=variant, apply_variant=variant,
+                 decouple=0)
     chosen = [S._lib.pm_level_variant(S._h, l) for l in range(3)]
     assert all(0 <= v <= 5 for v in chosen)
     bulk = 2 if precision == "mixed" else 0  # the bulk-staged apply is FP32 only
@@ -120,7 +122,7 @@ def test_inverse_apply(P, oracle):
     """vanka_inverse=1: the FP32 inverse of every local block (computed from
     the FP32 LU factors by a separate kernel) applied as a GEMV."""
     from to_merge_master_parmoon_gb300 import PmSolver
-    S = PmSolver(P.descs, precision="mixed", vanka_inverse=1)
+    S = PmSolver(P.descs, precision="mixed", vanka_inverse=1, decouple=0)
     for level in (1, 2):
         u, f = 0.1 * rand(P, level, 6), rand(P, level, 7)
         assert rel(S.cell_vanka(level, u, f, 2), oracle.cell_vanka(level, u, f, 2)) < 5e-4

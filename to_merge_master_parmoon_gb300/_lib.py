@@ -42,6 +42,7 @@ class PmOptions(C.Structure):
         ("device", C.c_int), ("use_graphs", C.c_int), ("verbose", C.c_int),
         ("pin_host", C.c_int), ("vanka_inverse", C.c_int), ("residual_variant", C.c_int),
         ("apply_variant", C.c_int), ("upload_mode", C.c_int), ("red_initial", C.c_int),
+        ("decouple", C.c_int), ("wait_limit", C.c_int), ("max_device_bytes", C.c_longlong),
     ]
 
 
@@ -86,6 +87,7 @@ GPU_SYMBOLS = {
     "pm_n_levels": (C.c_int, [_P]),
     "pm_level_ndof": (C.c_int, [_P, C.c_int]),
     "pm_level_blocks": (C.c_int, [_P, C.c_int]),
+    "pm_level_decoupled": (C.c_int, [_P, C.c_int]),
     "pm_level_variant": (C.c_int, [_P, C.c_int]),
     "pm_coupled_defect": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, c_double_p, C.c_int]),
     "pm_defect": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, c_double_p, c_double_p]),

@@ -62,6 +62,7 @@ struct LevelDev {
   int nu = 0, np = 0, ndof = 0, nact = 0, hb = 0, ndir = 0, ncells = 0;
   int a_nnz = 0, b_nnz = 0, bt_nnz = 0;
   int structured = 0;  // velocity blocks: A12..A32 = 0 and A11 = A22 = A33 (exactly)
+  int diag = 0;        // nine-block level whose A12..A32 are all zero (block solve)
   int res_variant = 0;    // local-residual kernel of the sweep (0 row groups, 1 stream)
   int apply_variant = 0;  // LU apply: 0 two cells per warp, 1 bulk-staged (FP32), 2 one cell per warp
   std::vector<int> h_udofs, h_pdofs, h_parent, h_child, h_colour;
@@ -100,17 +101,22 @@ struct LevelDev {
   DevCells cells() const { return DevCells{ncells, udofs, pdofs, nl}; }
   // the Schur block solve of one-block levels exists for Q2 hexahedra only
   bool schur() const { return structured && nl == NU_LOC; }
+  // block elimination with three diagonal blocks (decoupled nine-block levels)
+  bool schur3() const { return diag && !structured && nl == NU_LOC; }
+  size_t fac_bytes = 0;  // allocated factor storage
 };
 template <>
 DevOp<double> LevelDev::op<double>() const {
   DevOp<double> o;
   o.nu = nu;
   o.structured = structured;
+  o.diag = diag;
   o.np = np;
   o.nact = nact;
   o.a_rowptr = a_rowptr;
   o.a_col = a_col;
   for (int k = 0; k < 9; ++k) o.a[k] = a64[k];
+  for (int k = 0; k < 3; ++k) o.ad[k] = a64[4 * k];
   o.b_rowptr = b_rowptr;
   o.b_col = b_col;
   o.bt_rowptr = bt_rowptr;
@@ -126,11 +132,13 @@ DevOp<float> LevelDev::op<float>() const {
   DevOp<float> o;
   o.nu = nu;
   o.structured = structured;
+  o.diag = diag;
   o.np = np;
   o.nact = nact;
   o.a_rowptr = a_rowptr;
   o.a_col = a_col;
   for (int k = 0; k < 9; ++k) o.a[k] = a32[k];
+  for (int k = 0; k < 3; ++k) o.ad[k] = a32[4 * k];
   o.b_rowptr = b_rowptr;
   o.b_col = b_col;
   o.bt_rowptr = bt_rowptr;
@@ -161,6 +169,7 @@ struct pm_handle {
   double *ydev = nullptr;
   int *status_d = nullptr;
   int *sweep_err = nullptr;  // device flags of bounded waits inside sweep kernels
+  int *diag_flags = nullptr; // per level: an off-diagonal velocity block is nonzero
   bool asm_tables = false;   // assembly reference tables on the device
   int num_sms = 0;
   // coarse direct solve
@@ -211,6 +220,13 @@ template <typename T>
 pm_status dalloc(pm_handle *h, T **p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
+  if (h->opt.max_device_bytes > 0 &&
+      h->bytes + (long long)(count * sizeof(T)) > h->opt.max_device_bytes) {
+    h->err = "device allocation of " + std::to_string(count * sizeof(T)) +
+             " bytes exceeds max_device_bytes (" + std::to_string(h->opt.max_device_bytes) +
+             ", " + std::to_string(h->bytes) + " held)";
+    return PM_OOM;
+  }
   void *q = nullptr;
   cudaError_t e = cudaMalloc(&q, count * sizeof(T));
   if (e != cudaSuccess) {
@@ -335,13 +351,17 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
       PM_LAUNCH(launch_schur_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
                                       static_cast<const T *>(Lv.factors),
                                       static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
+    else if (Lv.schur3())
+      PM_LAUNCH(launch_schur3_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
+                                       static_cast<const T *>(Lv.factors),
+                                       static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
     else if (sizeof(T) == sizeof(float) && !use_inverse(h) && Lv.apply_variant == 1 &&
              Lv.nl == NU_LOC)
       PM_LAUNCH(launch_vanka_apply_tma(cells, Lv.nu, Lv.colour_cells + b, n,
                                        static_cast<const float *>(Lv.factors), Lv.perm,
                                        reinterpret_cast<const float *>(Lv.dbuf), (float)damp,
                                        reinterpret_cast<float *>(u), h->sweep_err, h->num_sms,
-                                       h->stream));
+                                       h->opt.wait_limit, h->stream));
     else
       PM_LAUNCH(launch_vanka_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
                                       static_cast<const T *>(Lv.factors), Lv.perm, use_inverse(h),
@@ -704,6 +724,80 @@ pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
 }
 
 // ------------------------------------------------------------- setup ------
+// Factor storage for the level's local solve: the 85x85 (or 49x49) LU with
+// its permutation, or the block-elimination data (one-block levels, and
+// decoupled nine-block levels).  Grows the allocation when a level changes
+// to a solve that stores more (a decoupled level whose matrices gain
+// velocity coupling in pm_update_matrices).
+pm_status ensure_factors(pm_handle *h, LevelDev &Lv) {
+  if (Lv.ncells == 0) return PM_OK;
+  const size_t es = mixed(h) ? sizeof(float) : sizeof(double);
+  const size_t per_cell = Lv.schur() ? (size_t)kSchurStride
+                          : Lv.schur3() ? (size_t)Schur<3>::stride
+                                        : (size_t)elem_fac_stride(Lv.nl);
+  const size_t need = (size_t)Lv.ncells * per_cell * es;
+  if (need > Lv.fac_bytes) {
+    PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors), need));
+    Lv.fac_bytes = need;
+  }
+  if (!Lv.schur() && !Lv.schur3() && !Lv.perm)
+    PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * elem_nloc(Lv.nl)));
+  return PM_OK;
+}
+
+// Unique bytes of one sweep per cell (each stored element counted once):
+// residual kernel = matrix values (the A arrays the level reads: 9, 3 when
+// decoupled, 1 for one-block levels) + column indices + row pointers, u and
+// rhs read; apply kernel = factors (+ permutation), u read+write.
+void level_bytes(pm_handle *h, LevelDev &Lv) {
+  if (Lv.ncells <= 0) return;
+  const double sv = mixed(h) ? 4.0 : 8.0;
+  const double nblk = Lv.structured ? 1.0 : (Lv.diag ? 3.0 : 9.0);
+  const double mat = nblk * sv * Lv.a_nnz + 4.0 * Lv.a_nnz + 4.0 * (Lv.nu + 1) +
+                     (3.0 * sv + 4.0) * ((double)Lv.b_nnz + Lv.bt_nnz) + 4.0 * (Lv.np + 1) +
+                     4.0 * (Lv.nu + 1);
+  Lv.vanka_res_bytes = (mat + 2.0 * sv * Lv.ndof) / Lv.ncells;
+  const double nloc = elem_nloc(Lv.nl);
+  const double per_cell = Lv.schur()    ? (double)kSchurValues * sv
+                          : Lv.schur3() ? (double)Schur<3>::values * sv
+                                        : nloc * nloc * sv + nloc;
+  Lv.vanka_apply_bytes = ((double)Lv.ncells * per_cell + 2.0 * sv * Lv.ndof) / Lv.ncells;
+}
+
+// Decoupled nine-block levels: one device pass per level over the six
+// off-diagonal velocity blocks (after their Dirichlet rows were zeroed),
+// then one read-back.  *changed reports levels whose mode flipped; their
+// captured V-cycles are dropped (the kernels differ).
+pm_status detect_decoupled(pm_handle *h, bool *changed) {
+  const int n = (int)h->L.size();
+  if (changed) *changed = false;
+  if (!h->diag_flags) PM_TRY(dalloc(h, &h->diag_flags, (size_t)n));
+  if (cudaMemsetAsync(h->diag_flags, 0, sizeof(int) * n, h->stream) != cudaSuccess)
+    return cuda_fail(h, "block check reset");
+  for (int l = 0; l < n; ++l) {
+    LevelDev &Lv = h->L[l];
+    if (Lv.structured || !h->opt.decouple) continue;
+    PM_LAUNCH(launch_offdiag_nonzero(Lv.op<double>(), Lv.a_nnz, h->diag_flags + l, h->stream));
+  }
+  std::vector<int> f(n, 1);
+  if (cudaMemcpyAsync(f.data(), h->diag_flags, sizeof(int) * n, cudaMemcpyDeviceToHost,
+                      h->stream) != cudaSuccess)
+    return cuda_fail(h, "block check read");
+  PM_TRY(sync(h, "block check"));
+  bool any = false;
+  for (int l = 0; l < n; ++l) {
+    LevelDev &Lv = h->L[l];
+    const int d = (!Lv.structured && h->opt.decouple && f[l] == 0) ? 1 : 0;
+    if (d != Lv.diag) {
+      Lv.diag = d;
+      any = true;
+    }
+  }
+  if (any) drop_graphs(h);
+  if (changed) *changed = any;
+  return PM_OK;
+}
+
 // Kernel choice per level (pm_options.residual_variant / apply_variant = -1):
 // both variants timed with CUDA events on the level's largest colour (zeroed
 // vectors, 3 launches after one warm-up launch), the faster one kept.
@@ -716,13 +810,14 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
   const int rule_res = (sizeof(T) == sizeof(float) && !Lv.structured) ? 1 : 0;
   const int ro = h->opt.residual_variant;
   Lv.res_variant = ro == 0 ? rule_res : (ro == 2 ? 1 : 0);
-  const bool can_bulk =
-      sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured && Lv.nl == NU_LOC;
+  const bool can_bulk = sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured &&
+                        !Lv.schur3() && Lv.nl == NU_LOC;
   const int ao = h->opt.apply_variant;
   const int rule_apply = sizeof(T) == sizeof(double) ? 0 : 2;
   Lv.apply_variant = ao == 0 ? rule_apply : (ao == 2 ? 2 : (can_bulk ? 1 : 0));
   const bool tune_res = h->opt.residual_variant < 0;
-  const bool tune_apply = h->opt.apply_variant < 0 && !use_inverse(h) && !Lv.structured;
+  const bool tune_apply =
+      h->opt.apply_variant < 0 && !use_inverse(h) && !Lv.structured && !Lv.schur3();
   if ((!tune_res && !tune_apply) || Lv.ncells == 0) return PM_OK;
   int kb = 0, nb = 0;
   for (size_t k = 0; k + 1 < Lv.colouring.ptr.size(); ++k) {
@@ -774,7 +869,7 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
                                         reinterpret_cast<const float *>(F), Lv.perm,
                                         reinterpret_cast<const float *>(rb), 1.f,
                                         reinterpret_cast<float *>(u), h->sweep_err, h->num_sms,
-                                        h->stream);
+                                        h->opt.wait_limit, h->stream);
         }, t[1]);
       } else {
         st = time_it([&] {
@@ -794,6 +889,24 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
   return st;
 }
 
+// After new matrix values: re-check which levels run decoupled and, for
+// levels whose mode changed, the factor storage, byte counts and kernels.
+pm_status refresh_modes(pm_handle *h) {
+  bool changed = false;
+  PM_TRY(detect_decoupled(h, &changed));
+  if (!changed) return PM_OK;
+  for (size_t l = 1; l < h->L.size(); ++l) {
+    LevelDev &Lv = h->L[l];
+    PM_TRY(ensure_factors(h, Lv));
+    level_bytes(h, Lv);
+    if (mixed(h))
+      PM_TRY(tune_level<float>(h, Lv));
+    else
+      PM_TRY(tune_level<double>(h, Lv));
+  }
+  return PM_OK;
+}
+
 pm_status factor_all(pm_handle *h) {
   if (cudaMemsetAsync(h->status_d, 0, sizeof(int), h->stream) != cudaSuccess)
     return cuda_fail(h, "status reset");
@@ -811,6 +924,15 @@ pm_status factor_all(pm_handle *h) {
         PM_LAUNCH(launch_schur_factor<double>(Lv.op<double>(), Lv.cells(),
                                               static_cast<double *>(Lv.factors), h->status_d,
                                               h->stream));
+    } else if (Lv.schur3()) {
+      if (mixed(h))
+        PM_LAUNCH(launch_schur3_factor<float>(Lv.op<double>(), Lv.cells(),
+                                              static_cast<float *>(Lv.factors), h->status_d,
+                                              h->stream));
+      else
+        PM_LAUNCH(launch_schur3_factor<double>(Lv.op<double>(), Lv.cells(),
+                                               static_cast<double *>(Lv.factors), h->status_d,
+                                               h->stream));
     } else if (mixed(h))
       PM_LAUNCH(launch_vanka_factor<float>(Lv.op<double>(), Lv.cells(), static_cast<float *>(Lv.factors),
                                            Lv.perm, h->opt.factor_fp32 != 0, use_inverse(h),
@@ -990,6 +1112,9 @@ void pm_default_options(pm_options *o) {
   o->apply_variant = 0;
   o->upload_mode = 0;
   o->red_initial = 0;
+  o->decouple = 1;
+  o->wait_limit = 0;
+  o->max_device_bytes = 0;
 }
 
 const char *pm_status_string(int s) {
@@ -1129,6 +1254,8 @@ pm_status pm_setup(pm_handle *h) {
   for (const LevelDev &Lv : h->L)
     if (Lv.nl != NU_LOC && use_inverse(h))
       return fail(h, PM_BADARG, "vanka_inverse: Q2 hexahedral levels only");
+  // which nine-block levels run decoupled (reads the uploaded values)
+  PM_TRY(detect_decoupled(h, nullptr));
   // colouring, transfers, buffers
   size_t maxcol = 0;
   for (size_t l = 0; l < h->L.size(); ++l) {
@@ -1167,34 +1294,14 @@ pm_status pm_setup(pm_handle *h) {
       PM_TRY(upload_csr(h, Lv.Pp, Pp));
       PM_TRY(upload_csr(h, Lv.Rp, Rp));
       // local factors (FP64 or FP32 storage) and permutations, or the
-      // block-solve data of a one-block level
-      if (Lv.schur()) {
-        PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
-                      (size_t)Lv.ncells * kSchurStride * es));
-      } else {
-        PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.factors),
-                      (size_t)Lv.ncells * elem_fac_stride(Lv.nl) * es));
-        PM_TRY(dalloc(h, &Lv.perm, (size_t)Lv.ncells * elem_nloc(Lv.nl)));
-      }
+      // block-solve data of a level without velocity coupling
+      PM_TRY(ensure_factors(h, Lv));
       PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.dbuf),
                     (size_t)Lv.colouring.max_size * elem_r_stride(Lv.nl) * es));
       if (std::fabs(1.0 - h->opt.alpha) > 1e-3)
         PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.uold), (size_t)Lv.ndof * es));
     }
-    if (Lv.ncells > 0) {
-      // unique bytes of one sweep (each stored element counted once):
-      // residual kernel = matrix values + column indices + row pointers, u
-      // and rhs read; apply kernel = factors + permutation, u read+write
-      const double sv = (double)es;
-      const double nblk = Lv.structured ? 1.0 : 9.0;
-      const double mat = nblk * sv * Lv.a_nnz + 4.0 * Lv.a_nnz + 4.0 * (Lv.nu + 1) +
-                         (3.0 * sv + 4.0) * ((double)Lv.b_nnz + Lv.bt_nnz) + 4.0 * (Lv.np + 1) +
-                         4.0 * (Lv.nu + 1);
-      Lv.vanka_res_bytes = (mat + 2.0 * sv * Lv.ndof) / Lv.ncells;
-      const double nloc = elem_nloc(Lv.nl);
-      const double per_cell = Lv.schur() ? (double)kSchurValues * sv : nloc * nloc * sv + nloc;
-      Lv.vanka_apply_bytes = ((double)Lv.ncells * per_cell + 2.0 * sv * Lv.ndof) / Lv.ncells;
-    }
+    level_bytes(h, Lv);
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.sol), (size_t)Lv.ndof * es));
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.rhs), (size_t)Lv.ndof * es));
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.def), (size_t)Lv.ndof * es));
@@ -1252,6 +1359,7 @@ pm_status pm_update_matrices(pm_handle *h, const pm_level_desc *levels, int n) {
       return fail(h, PM_BADARG, "pattern changed");
     PM_TRY(upload_values(h, Lv, d, false));
   }
+  PM_TRY(refresh_modes(h));
   if (h->opt.verbose) {
     // host timing of the two phases (the sync separates them)
     PM_TRY(sync(h, "upload"));
@@ -1299,6 +1407,9 @@ int pm_level_variant(pm_handle *h, int l) {
 }
 int pm_level_blocks(pm_handle *h, int l) {
   return (h && l >= 0 && l < (int)h->L.size()) ? (h->L[l].structured ? 1 : 9) : -1;
+}
+int pm_level_decoupled(pm_handle *h, int l) {
+  return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].diag : -1;
 }
 
 #define PM_CHECK_LEVEL(h, level)                                           \
@@ -1532,10 +1643,25 @@ static pm_status assemble_impl(pm_handle *h, int level, const double *d_cell_h,
   PM_LAUNCH(launch_assemble_level(op, Lv.cells(), Lv.colour_cells, Lv.colouring.ptr.data(),
                                   (int)Lv.colouring.ptr.size() - 1, d_cell_h, d_conv, nu,
                                   h->stream));
+  if (!Lv.structured) {
+    // the assembled A12..A32 are zero by construction: no device check
+    const int d = h->opt.decouple ? 1 : 0;
+    if (d != Lv.diag) {
+      Lv.diag = d;
+      drop_graphs(h);
+      PM_TRY(ensure_factors(h, Lv));
+      level_bytes(h, Lv);
+      if (mixed(h))
+        PM_TRY(tune_level<float>(h, Lv));
+      else
+        PM_TRY(tune_level<double>(h, Lv));
+    }
+  }
   if (mixed(h)) {
     const int nblk = Lv.structured ? 1 : 9;
     for (int k = 0; k < nblk; ++k)
-      PM_LAUNCH((launch_convert<float, double>(Lv.a32[k], Lv.a64[k], Lv.a_nnz, h->stream)));
+      if (!Lv.diag || k % 4 == 0)  // a decoupled level reads A11, A22, A33 only
+        PM_LAUNCH((launch_convert<float, double>(Lv.a32[k], Lv.a64[k], Lv.a_nnz, h->stream)));
     for (int k = 0; k < 3; ++k) {
       PM_LAUNCH((launch_convert<float, double>(Lv.b32[k], Lv.b64[k], Lv.b_nnz, h->stream)));
       PM_LAUNCH((launch_convert<float, double>(Lv.bt32[k], Lv.bt64[k], Lv.bt_nnz, h->stream)));

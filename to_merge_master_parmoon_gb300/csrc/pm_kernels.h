@@ -41,8 +41,13 @@ struct DevOp {
   // 1: A12..A32 are zero and A11 = A22 = A33 (checked exactly at set-up);
   // only a[0] is read
   int structured;
+  // 1 (nine-block levels only): the off-diagonal blocks A12..A32 are all
+  // zero (checked on the device after every upload); the sweeps read only
+  // the diagonal blocks ad[0..2] = A11, A22, A33
+  int diag;
   const int *a_rowptr, *a_col;
   const T *a[9];
+  const T *ad[3];
   const int *b_rowptr, *b_col;
   const T *b[3];
   const int *bt_rowptr, *bt_col;
@@ -155,26 +160,48 @@ constexpr int PM_ERR_BULK_TIMEOUT = 1;
 // bulk copies (two cell buffers per warp, three warps per CTA, at most
 // num_sms CTAs walking the colour's cells with a stride).  Same arithmetic
 // as launch_vanka_apply.  _init sets the kernel's shared-memory limit (call
-// once before any launch, outside stream capture).
+// once before any launch, outside stream capture).  wait_limit: polls of
+// each wait for a cell's factors before the kernel gives up (0: default).
 int launch_vanka_apply_tma_init();
 int launch_vanka_apply_tma(const DevCells &cells, int nu, const int *cell_list, int ncol,
                            const float *factors, const uint8_t *perm, const float *rbuf, float damp,
-                           float *u, int *err, int num_sms, cudaStream_t s);
+                           float *u, int *err, int num_sms, long long wait_limit, cudaStream_t s);
 
-// Block (Schur-complement) local solve for structured operators: per cell
-// A^{-1} (27x27, column-major), D (4x3x27), W = A^{-1} G (4x3x27) and S^{-1}
-// (4x4, column-major), kSchurStride values of the storage precision.
-constexpr int kSchurOffD = NU_LOC * NU_LOC;                    // 729
-constexpr int kSchurOffW = kSchurOffD + NP_LOC * 3 * NU_LOC;   // 1053
-constexpr int kSchurOffS = kSchurOffW + NP_LOC * 3 * NU_LOC;   // 1377
-constexpr int kSchurValues = kSchurOffS + NP_LOC * NP_LOC;     // 1393
-constexpr int kSchurStride = 1396;                             // 16-byte multiple per cell
+// Block (Schur-complement) local solve of levels without velocity coupling,
+// NB = 1 (one-block operators: one A for the three components) or NB = 3
+// (nine-block levels whose A12..A32 are zero: A11, A22, A33).  Per cell:
+// the NB inverses A_b^{-1} (27x27, column-major, one after the other), D
+// (4x3x27), W = A^{-1} G (4x3x27) and S^{-1} (4x4, column-major), padded to
+// a 16-byte multiple of the storage precision.
+template <int NB>
+struct Schur {
+  static constexpr int offD = NB * NU_LOC * NU_LOC;           // 729 / 2187
+  static constexpr int offW = offD + NP_LOC * 3 * NU_LOC;     // 1053 / 2511
+  static constexpr int offS = offW + NP_LOC * 3 * NU_LOC;     // 1377 / 2835
+  static constexpr int values = offS + NP_LOC * NP_LOC;       // 1393 / 2851
+  static constexpr int stride = (values + 3) / 4 * 4;         // 1396 / 2852
+};
+constexpr int kSchurOffD = Schur<1>::offD;
+constexpr int kSchurOffW = Schur<1>::offW;
+constexpr int kSchurOffS = Schur<1>::offS;
+constexpr int kSchurValues = Schur<1>::values;
+constexpr int kSchurStride = Schur<1>::stride;
 template <typename TF>
 int launch_schur_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,
                         cudaStream_t s);
 template <typename T>
 int launch_schur_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                        const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s);
+// the same for NB = 3 (op.diag levels)
+template <typename TF>
+int launch_schur3_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,
+                         cudaStream_t s);
+template <typename T>
+int launch_schur3_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
+                        const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s);
+// flag[0] |= 1 if any entry of the off-diagonal velocity blocks
+// a[1], a[2], a[3], a[5], a[6], a[7] (n entries each) is nonzero
+int launch_offdiag_nonzero(const DevOp<double> &op, long long n, int *flag, cudaStream_t s);
 
 // --------------------------------------------------------------- assembly --
 // Writable view of a level's FP64 values for device assembly: NSTYPE 4 fills

@@ -74,8 +74,10 @@ struct VLd<double, 2> {
 };
 
 // s[0..2] += the row's products; NV = 9 (A blocks) and 1 (one-block A)
-// gather x0..x2; NV = 3 (BT) gathers x0 only
-template <typename T, int VEC, int NV, int UR>
+// gather x0..x2; NV = 3 (BT) gathers x0 only; NV = 3 with DIAG (the
+// diagonal blocks A11, A22, A33 of a level without velocity coupling)
+// multiplies value k with x_k into s[k]
+template <typename T, int VEC, int NV, int UR, bool DIAG = false>
 __device__ __forceinline__ void rows8_sum(const int *__restrict__ col, const T *const *vals, int rs,
                                           int re, int sl, const T *__restrict__ x0,
                                           const T *__restrict__ x1, const T *__restrict__ x2,
@@ -107,7 +109,11 @@ __device__ __forceinline__ void rows8_sum(const int *__restrict__ col, const T *
         const int e = e0 + m;
         if (e >= rs && e < re) {
           const int c = ci[q][m];
-          if constexpr (NV == 3) {
+          if constexpr (DIAG) {
+            s[0] += v[q][0][m] * __ldg(x0 + c);
+            s[1] += v[q][1][m] * __ldg(x1 + c);
+            s[2] += v[q][2][m] * __ldg(x2 + c);
+          } else if constexpr (NV == 3) {
             const T pc = __ldg(x0 + c);
             s[0] += v[q][0][m] * pc;
             s[1] += v[q][1][m] * pc;
@@ -129,7 +135,9 @@ __device__ __forceinline__ void rows8_sum(const int *__restrict__ col, const T *
   }
 }
 
-template <typename T, int VEC, bool ONE, int UR>
+// KIND 0: nine A blocks; 1: one A block for the three components; 2: the
+// three diagonal blocks only (A12..A32 zero on the level)
+template <typename T, int VEC, int KIND, int UR>
 __global__ void __launch_bounds__(kBlock) k_coupled_velocity8(DevOp<T> op, const T *__restrict__ x,
                                                               const T *__restrict__ b,
                                                               T *__restrict__ r, int defect,
@@ -144,8 +152,12 @@ __global__ void __launch_bounds__(kBlock) k_coupled_velocity8(DevOp<T> op, const
   const T *u1 = x, *u2 = x + nu, *u3 = x + 2 * nu, *p = x + 3 * nu;
   T s[3] = {T(0), T(0), T(0)};
   if (!skip) {
-    rows8_sum<T, VEC, ONE ? 1 : 9, UR>(op.a_col, op.a, op.a_rowptr[i], op.a_rowptr[i + 1], sl, u1,
-                                       u2, u3, s);
+    if constexpr (KIND == 2)
+      rows8_sum<T, VEC, 3, UR, true>(op.a_col, op.ad, op.a_rowptr[i], op.a_rowptr[i + 1], sl, u1,
+                                     u2, u3, s);
+    else
+      rows8_sum<T, VEC, KIND == 1 ? 1 : 9, UR>(op.a_col, op.a, op.a_rowptr[i], op.a_rowptr[i + 1],
+                                               sl, u1, u2, u3, s);
     if (i < op.nact)
       rows8_sum<T, VEC, 3, 1>(op.bt_col, op.bt, op.bt_rowptr[i], op.bt_rowptr[i + 1], sl, p, p,
                               p, s);
@@ -446,11 +458,14 @@ int launch_coupled(const DevOp<T> &op, const T *x, const T *b, T *r, bool defect
   constexpr int VEC = sizeof(T) == 4 ? 4 : 2;
   const unsigned gv = grid_for((long long)op.nu * 8);
   if (op.structured)
-    k_coupled_velocity8<T, VEC, true, 2><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
-                                                              zero_nonactive ? 1 : 0);
+    k_coupled_velocity8<T, VEC, 1, 2><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+                                                           zero_nonactive ? 1 : 0);
+  else if (op.diag)
+    k_coupled_velocity8<T, VEC, 2, 2><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+                                                           zero_nonactive ? 1 : 0);
   else
-    k_coupled_velocity8<T, VEC, false, 1><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
-                                                               zero_nonactive ? 1 : 0);
+    k_coupled_velocity8<T, VEC, 0, 1><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+                                                           zero_nonactive ? 1 : 0);
   if (ok() < 0) return -1;
   k_coupled_pressure<T, GP><<<grid_for((long long)op.np * GP), kBlock, 0, s>>>(op, x, b, r,
                                                                                defect ? 1 : 0);

@@ -385,6 +385,8 @@ __device__ __forceinline__ int seg_setup(const SegTab &t, int lane, bool valid, 
 // MODE 1: BT rows (3 values, gather p -> 3 outputs)
 // MODE 2: B rows (3 values, gather u1,u2,u3 -> 1 output)
 // MODE 3: A rows of a one-block operator (1 value, gather u1,u2,u3 -> 3 outputs)
+// MODE 4: A rows of a level without velocity coupling (the 3 diagonal
+//         blocks, value k times u_k into output k)
 template <typename T, int MODE, int VEC, int U>
 __device__ __forceinline__ void flat_rows(const SegTab &t, int nseg, int total,
                                           const int *__restrict__ col, const T *const *vals,
@@ -445,6 +447,10 @@ __device__ __forceinline__ void flat_rows(const SegTab &t, int nseg, int total,
               s[0] += a * __ldg(x0 + c);
               s[1 % NO] += a * __ldg(x1 + c);
               s[2 % NO] += a * __ldg(x2 + c);
+            } else if constexpr (MODE == 4) {
+              s[0] += v[q][0][m] * __ldg(x0 + c);
+              s[1 % NO] += v[q][1][m] * __ldg(x1 + c);
+              s[2 % NO] += v[q][2][m] * __ldg(x2 + c);
             } else {
               const T g0 = __ldg(x0 + c), g1 = __ldg(x1 + c), g2 = __ldg(x2 + c);
               if constexpr (MODE == 0) {
@@ -481,11 +487,14 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual(
   const bool vu = lane < NU_LOC, vp = lane < NP_LOC;
   const int my_r = vu ? cells.udofs[(size_t)cell * NU_LOC + lane] : 0;
   const int my_p = vp ? cells.pdofs[(size_t)cell * NP_LOC + lane] : 0;
-  // A rows: nine blocks, or the one block of a structured operator
+  // A rows: nine blocks, the one block of a structured operator, or the
+  // three diagonal blocks of a level without velocity coupling
   int total = seg_setup<VEC>(tab, lane, vu, vu ? op.a_rowptr[my_r] : 0,
                              vu ? op.a_rowptr[my_r + 1] : 0);
   if (op.structured)
     flat_rows<T, 3, VEC, U>(tab, NU_LOC, total, op.a_col, op.a, u1, u2, u3, acc, lane);
+  else if (op.diag)
+    flat_rows<T, 4, VEC, U>(tab, NU_LOC, total, op.a_col, op.ad, u1, u2, u3, acc, lane);
   else
     flat_rows<T, 0, VEC, U>(tab, NU_LOC, total, op.a_col, op.a, u1, u2, u3, acc, lane);
   // BT rows of active velocity DOFs
@@ -517,7 +526,10 @@ __constant__ unsigned char c_row_order[NU_LOC] = {0, 2, 6, 8, 18, 20, 24, 26, 1,
                                                   15, 17, 19, 21, 23, 25, 4, 10, 12, 14, 16, 22,
                                                   13};
 
-template <typename T, int VEC, int NV, int UR>
+// NV = 9 (nine A blocks), 1 (one A block), 3 with gather3 (a B row: one
+// output) or without (a BT row: gather p, three outputs); DIAG (NV = 3):
+// the diagonal blocks A11, A22, A33, value k times x_k into s[k]
+template <typename T, int VEC, int NV, int UR, bool DIAG = false>
 __device__ __forceinline__ void row_group_sum(const int *__restrict__ col, const T *const *vals,
                                               int rs, int re, int sl, const T *__restrict__ x0,
                                               const T *__restrict__ x1, const T *__restrict__ x2,
@@ -551,7 +563,11 @@ __device__ __forceinline__ void row_group_sum(const int *__restrict__ col, const
           const int c = ci[q][m];
           if (gather3) {
             const T g0 = __ldg(x0 + c), g1 = __ldg(x1 + c), g2 = __ldg(x2 + c);
-            if constexpr (NV == 1) {
+            if constexpr (DIAG) {
+              s[0] += v[q][0][m] * g0;
+              s[1] += v[q][1][m] * g1;
+              s[2] += v[q][2][m] * g2;
+            } else if constexpr (NV == 1) {
               s[0] += v[q][0][m] * g0;
               s[1] += v[q][0][m] * g1;
               s[2] += v[q][0][m] * g2;
@@ -576,7 +592,8 @@ __device__ __forceinline__ void row_group_sum(const int *__restrict__ col, const
   }
 }
 
-template <typename T, int VEC, bool ONE, int URA, int NU>
+// KIND 0: nine A blocks; 1: one A block; 2: the three diagonal blocks
+template <typename T, int VEC, int KIND, int URA, int NU>
 __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual_rows(
     DevOp<T> op, DevCells cells, const int *__restrict__ list, int ncol, const T *__restrict__ u,
     const T *__restrict__ rhs, T *__restrict__ rbuf) {
@@ -598,8 +615,12 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual_rows(
     const int r = valid ? __ldg(ud + a) : 0;
     T s[3] = {T(0), T(0), T(0)};
     if (valid) {
-      row_group_sum<T, VEC, ONE ? 1 : 9, URA>(op.a_col, op.a, op.a_rowptr[r], op.a_rowptr[r + 1],
-                                              sl, u1, u2, u3, true, s);
+      if constexpr (KIND == 2)
+        row_group_sum<T, VEC, 3, URA, true>(op.a_col, op.ad, op.a_rowptr[r], op.a_rowptr[r + 1],
+                                            sl, u1, u2, u3, true, s);
+      else
+        row_group_sum<T, VEC, KIND == 1 ? 1 : 9, URA>(op.a_col, op.a, op.a_rowptr[r],
+                                                      op.a_rowptr[r + 1], sl, u1, u2, u3, true, s);
       if (r < op.nact)
         row_group_sum<T, VEC, 3, 1>(op.bt_col, op.bt, op.bt_rowptr[r], op.bt_rowptr[r + 1], sl, p,
                                     p, p, false, s);
@@ -1337,10 +1358,13 @@ int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *
   const int grid = (ncol + kResWarps - 1) / kResWarps;
   if (cells.nl == NU_TET) {  // tetrahedra: the row-group kernel
     if (op.structured)
-      k_vanka_residual_rows<T, VEC, true, 2, NU_TET><<<grid, kResWarps * 32, 0, s>>>(
+      k_vanka_residual_rows<T, VEC, 1, 2, NU_TET><<<grid, kResWarps * 32, 0, s>>>(
+          op, cells, cell_list, ncol, u, rhs, rbuf);
+    else if (op.diag)
+      k_vanka_residual_rows<T, VEC, 2, 2, NU_TET><<<grid, kResWarps * 32, 0, s>>>(
           op, cells, cell_list, ncol, u, rhs, rbuf);
     else
-      k_vanka_residual_rows<T, VEC, false, 1, NU_TET><<<grid, kResWarps * 32, 0, s>>>(
+      k_vanka_residual_rows<T, VEC, 0, 1, NU_TET><<<grid, kResWarps * 32, 0, s>>>(
           op, cells, cell_list, ncol, u, rhs, rbuf);
     return ok() < 0 ? -1 : 1;
   }
@@ -1349,10 +1373,13 @@ int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *
     k_vanka_residual<T, VEC, U><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list, ncol, u, rhs,
                                                                rbuf);
   } else if (op.structured) {
-    k_vanka_residual_rows<T, VEC, true, 2, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
+    k_vanka_residual_rows<T, VEC, 1, 2, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
+        op, cells, cell_list, ncol, u, rhs, rbuf);
+  } else if (op.diag) {
+    k_vanka_residual_rows<T, VEC, 2, 2, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
         op, cells, cell_list, ncol, u, rhs, rbuf);
   } else {
-    k_vanka_residual_rows<T, VEC, false, 1, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
+    k_vanka_residual_rows<T, VEC, 0, 1, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
         op, cells, cell_list, ncol, u, rhs, rbuf);
   }
   return ok() < 0 ? -1 : 1;

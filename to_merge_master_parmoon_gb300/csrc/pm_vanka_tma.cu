@@ -11,9 +11,11 @@
 // with a 16-byte-aligned per-cell stride, kFacStride) under an mbarrier.
 // Three warps per CTA, one CTA per SM (173 KB of buffers).
 //
-// Every wait on an mbarrier is bounded: after kMaxPolls unsuccessful polls
+// Every wait on an mbarrier is bounded: after `limit` unsuccessful polls
+// (non-blocking mbarrier.test_wait; kMaxPolls by default, a few hundred ms)
 // the warp records PM_ERR_BULK_TIMEOUT in *err, stops issuing copies, waits
-// (again bounded) for the copies it still has in flight and returns.
+// for the copies it still has in flight (bounded by kMaxPolls, whatever the
+// limit of the first waits) and returns.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -57,11 +59,11 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
       : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(done)
       : "r"(smem_addr(bar)), "r"(parity)
@@ -69,12 +71,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait by the whole warp; true when the phase completed.  The result
-// is warp-uniform (every lane has observed the completion itself, so every
-// lane's later shared-memory reads are ordered after the copy).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (long long it = 0; it < kMaxPolls; ++it)
-    if (__all_sync(kFull, mbar_try_wait(bar, parity))) return true;
+// Bounded wait by the whole warp (at most `polls` non-blocking tests); true
+// when the phase completed.  The result is warp-uniform (every lane has
+// observed the completion itself, so every lane's later shared-memory reads
+// are ordered after the copy).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long polls) {
+  for (long long it = 0; it < polls; ++it)
+    if (__all_sync(kFull, mbar_test_wait(bar, parity))) return true;
   return false;
 }
 
@@ -125,7 +128,7 @@ __device__ __forceinline__ void substitute(const float *Fc, int lane, float &y0,
 __global__ void __launch_bounds__(kTmaWarps * 32, 1) k_vanka_apply_tma(
     DevCells cells, int nu, const int *__restrict__ list, int ncol, const float *__restrict__ F,
     const uint8_t *__restrict__ perm, const float *__restrict__ rbuf, float damp,
-    float *__restrict__ u, int *err) {
+    float *__restrict__ u, int *err, long long limit) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[kTmaWarps][2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -155,7 +158,7 @@ __global__ void __launch_bounds__(kTmaWarps * 32, 1) k_vanka_apply_tma(
       issued[b ^ 1] += 1;
     }
     if (!ok) break;
-    if (!mbar_wait(&bars[warp][b], done[b] & 1u)) {
+    if (!mbar_wait(&bars[warp][b], done[b] & 1u, limit)) {
       ok = false;
       break;
     }
@@ -179,7 +182,7 @@ __global__ void __launch_bounds__(kTmaWarps * 32, 1) k_vanka_apply_tma(
     // drain: wait (bounded) for the copies this warp still has in flight
     for (int b = 0; b < 2; ++b)
       while (done[b] < issued[b]) {
-        if (!mbar_wait(&bars[warp][b], done[b] & 1u)) break;
+        if (!mbar_wait(&bars[warp][b], done[b] & 1u, kMaxPolls)) break;
         done[b] += 1;
       }
   }
@@ -198,12 +201,13 @@ int launch_vanka_apply_tma_init() {
 
 int launch_vanka_apply_tma(const DevCells &cells, int nu, const int *cell_list, int ncol,
                            const float *factors, const uint8_t *perm, const float *rbuf, float damp,
-                           float *u, int *err, int num_sms, cudaStream_t s) {
+                           float *u, int *err, int num_sms, long long wait_limit, cudaStream_t s) {
   if (ncol <= 0) return 0;
   int grid = (ncol + kTmaWarps - 1) / kTmaWarps;
   if (grid > num_sms) grid = num_sms;
+  const long long limit = wait_limit > 0 ? wait_limit : kMaxPolls;
   k_vanka_apply_tma<<<grid, kTmaWarps * 32, kTmaSmem, s>>>(cells, nu, cell_list, ncol, factors,
-                                                           perm, rbuf, damp, u, err);
+                                                           perm, rbuf, damp, u, err, limit);
   return ok() < 0 ? -1 : 1;
 }
 

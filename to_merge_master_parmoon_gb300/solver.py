@@ -91,6 +91,11 @@ class PmSolver:
     def n_levels(self) -> int:
         return self._lib.pm_n_levels(self._h)
 
+    def level_decoupled(self, level: int) -> bool:
+        """True when a nine-block level runs decoupled (A12..A32 zero:
+        diagonal blocks only, block-elimination cell solve)."""
+        return self._lib.pm_level_decoupled(self._h, level) == 1
+
     def ndof(self, level: int = -1) -> int:
         return self._ndof[level]
 
