@@ -73,7 +73,14 @@ def parse():
                          "k_mlp_layer_tc")
     ap.add_argument("--only-factor", action="store_true",
                     help="refactorisation of every level only (nine-block mixed levels, "
-                         "warm-up + steps passes): the case profiled for k_vanka_factor")
+                         "warm-up + steps passes): the case profiled for the factor kernels")
+    ap.add_argument("--only-sweep", default="", choices=["", "mixed", "fp64"],
+                    help="cell-Vanka sweeps of the finest level only (pm_cell_vanka, warm-up "
+                         "+ steps sweeps) in the given precision: the case profiled for the "
+                         "local-residual and apply kernels")
+    ap.add_argument("--decouple", type=int, default=1,
+                    help="pm_options.decouple of the --only-sweep / --only-factor cases (0: the "
+                         "85x85 LU and all nine blocks on every level)")
     ap.add_argument("--channel-steps", type=int, default=10,
                     help="timed Crank-Nicolson steps per variant of the channel run "
                          "(a bounded sample of its 200 steps)")
@@ -159,24 +166,25 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes (read + write) per cell of one local-residual launch on a
+# decoupled FP32 level (k_vanka_residual_rows, three A blocks), from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of a 32^3 colour
+# launch of 4,096 cells:
+#   ncu --set full --clock-control none -k regex:k_vanka_residual -s 16 -c 1 \
+#       python bench.py --only-sweep mixed --levels 5 --warmup 1 --steps 2
+# None until measured.  Traffic grows with the cells a launch processes
+# (every cell reads its own 27 rows), so it scales to a launch of any size.
+RESIDUAL_DRAM_BYTES_PER_CELL = None
+
+
 def ncu_traffic(P):
-    """DRAM bytes per average residual launch: the per-cell traffic of one
-    32^3 colour launch from the committed ncu summary
-    (profiles/vanka_kernels_32cube_level.md), times the average number of
-    cells per residual launch of this workload (all smoothed cells / (8
-    colours x smoothed levels)); None without the summary."""
-    p = ROOT / "profiles" / "vanka_kernels_32cube_level.md"
-    if not p.exists():
-        return None
-    per_cell = None
-    for line in p.read_text().splitlines():
-        parts = line.split()
-        if len(parts) == 2 and parts[0] == "residual_dram_bytes_per_cell":
-            per_cell = float(parts[1])
-    if per_cell is None:
+    """DRAM bytes per average residual launch of this workload: the measured
+    per-cell traffic times the average cells per residual launch (all
+    smoothed cells / (8 colours x smoothed levels)); None when unmeasured."""
+    if RESIDUAL_DRAM_BYTES_PER_CELL is None:
         return None
     cells = [P.desc(l).n_cells for l in range(1, P.n_levels)]
-    return per_cell * sum(cells) / (8 * len(cells))
+    return RESIDUAL_DRAM_BYTES_PER_CELL * sum(cells) / (8 * len(cells))
 
 
 def split_error(x, ref, nu):
@@ -300,6 +308,31 @@ def solve_bytes(P, s, iterations, decoupled=False, pre=2, post=2, restart=20):
         k = j % restart
         total += per_it_fixed + (k + 1) * 5 * 8.0 * dof_f
     return total
+
+
+def residual_fma(P, nblk):
+    """FMA of the cell-local residual kernel for one sweep of every level with
+    cells: per cell, every entry of its 27 velocity rows' A rows (nblk FMA:
+    9 with nine blocks, 3 decoupled), of their BT rows on active rows (3) and
+    of its 4 pressure rows' B rows (3).  Returns {level: FMA per sweep}."""
+    import numpy as np
+    out = {}
+    for l in range(1, P.n_levels):
+        a = P.arrays(l)
+        la = np.diff(a["a_rowptr"]).astype(np.int64)
+        lbt = np.diff(a["bt_rowptr"]).astype(np.int64)
+        lbt[a["n_active"]:] = 0
+        lb = np.diff(a["b_rowptr"]).astype(np.int64)
+        ud, pd = a["cell_udofs"], a["cell_pdofs"]
+        out[l] = int(nblk * la[ud].sum() + 3 * lbt[ud].sum() + 3 * lb[pd].sum())
+    return out
+
+
+# FMA of one cell's block-elimination factorisation with three diagonal
+# blocks (k_schur_factor<3>): per component a Gauss-Jordan on [A_c | I | G_c]
+# (27 x 58: sum over k of 26 rows x (57 - k) columns) and its share of the
+# 4x4 Schur complement (16 x 27)
+SCHUR3_FMA_PER_CELL = 3 * (26 * sum(57 - k for k in range(27)) + 16 * 27)
 
 
 def run_reference(args):
@@ -558,11 +591,48 @@ def only_factor(args):
     prints the mean factorisation time (the library's CUDA events)."""
     from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
     P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed, nthreads=os.cpu_count() or 1)
-    S = PmSolver(P.descs, precision="mixed")
+    S = PmSolver(P.descs, precision="mixed", decouple=args.decouple)
     ms = [S.refactor() for _ in range(args.warmup + args.steps)][args.warmup:]
     print(json.dumps({"only_factor": True, "levels": P.n_levels,
                       "cells": sum(P.desc(l).n_cells for l in range(1, P.n_levels)),
                       "factor_ms": sum(ms) / len(ms)}), flush=True)
+
+
+def only_sweep(args):
+    """pm_cell_vanka on the finest level of a nine-block problem (args.levels
+    levels from 2^3, seed args.seed), one sweep per call, args.warmup +
+    args.steps calls in the precision args.only_sweep; prints the kernels a
+    sweep launches and the mean device time of the local-residual and apply
+    kernels per sweep (profiling events around every launch).  A sweep is 8
+    colours x (residual + apply) between two Dirichlet updates, so under a
+    profiler the residual launch of colour k of sweep s is number
+    8 s + k of its kernel."""
+    import numpy as np
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed, nthreads=os.cpu_count() or 1)
+    S = PmSolver(P.descs, precision=args.only_sweep, decouple=args.decouple)
+    L = P.n_levels
+    rng = np.random.default_rng(0)
+    u = 0.1 * rng.standard_normal(P.ndof(L - 1))
+    f = rng.standard_normal(P.ndof(L - 1))
+    for _ in range(args.warmup):
+        u = S.cell_vanka(L - 1, u, f, 1)
+    S.profile(True)
+    n0 = S.kernel_launches
+    for _ in range(args.steps):
+        u = S.cell_vanka(L - 1, u, f, 1)
+    launches = (S.kernel_launches - n0) // args.steps
+    prof = S.profile_read()
+    S.profile(False)
+    out = {"only_sweep": args.only_sweep, "levels": L, "decoupled": S.level_decoupled(L - 1),
+           "cells": P.desc(L - 1).n_cells, "kernel_launches_per_sweep": launches}
+    for k, v in prof.items():
+        out[k] = {"ms_per_sweep": v["ms"] / args.steps, "launches": v["launches"],
+                  "avg_launch_ms": v["ms"] / max(v["launches"], 1),
+                  "bytes_per_launch": v["bytes"] / max(v["launches"], 1),
+                  "achieved_gbs": v["bytes"] / (v["ms"] * 1e-3) / 1e9 if v["ms"] else None}
+    print(json.dumps(out), flush=True)
+    S.close()
 
 
 def only_assembly(args):
@@ -694,6 +764,9 @@ def main():
         return
     if args.only_factor:
         only_factor(args)
+        return
+    if args.only_sweep:
+        only_sweep(args)
         return
     if args.only_mlp > 0:
         only_mlp(args)
@@ -883,12 +956,13 @@ def main():
     a_ach, a_ms, a_bytes = kernel_roof(prof.get("apply"))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(P),
-            "kernel": "k_vanka_residual<float,4,1> (cell-local residuals over full CSR rows, "
-                      "one colour; flattened entry stream)",
+            "kernel": "k_vanka_residual_rows<float,4,2,2,27> (cell-local residuals over full "
+                      "CSR rows of one colour, 8 lanes per row; decoupled levels: A11, A22, A33, "
+                      "BT, B)",
             "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "bytes_per_launch": per_launch,
-            "apply_kernel": {"name": "k_vanka_apply<float> (stored FP32 LU, one cell per "
-                                     "warp, columns prefetched in registers and L2; "
-                                     "substitution + update)",
+            "apply_kernel": {"name": "k_schur_apply<float,3> (stored FP32 block elimination: "
+                                     "three 27x27 inverses, B, A^-1 BT, 4x4 Schur inverse; "
+                                     "one cell per warp, GEMVs + update)",
                              "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,
                              "avg_launch_ms": a_ms, "bytes_per_launch": a_bytes}}
     def whole_solve(name, s_val, decoupled=True):
@@ -899,6 +973,38 @@ def main():
                 "note": "unique bytes of the whole FGMRES solve (V-cycles, FP64 mat-vecs, "
                         "Gram-Schmidt) / solve time; peak = measured HBM copy bandwidth"}
 
+    # FP64 pipe: the measured FMA rate of this GPU (a kernel of the library)
+    # against the FP64 residual kernel and the factorisation
+    fp64_roof = None
+    import ctypes as C
+    from to_merge_master_parmoon_gb300._lib import gpu_lib
+    rate = C.c_double()
+    if gpu_lib().pm_measure_fp64_fma(local, C.byref(rate)) == 0 and rate.value > 0:
+        r64 = results["fp64"]
+        pr = r64.get("profile", {}).get("residual")
+        sweeps = r64["iterations"] * 4
+        fma = residual_fma(P, 3)
+        res = None
+        if pr and pr["ms"]:
+            t = pr["ms"] * 1e-3 / args.steps
+            fl = 2.0 * sum(fma.values()) * sweeps
+            by = pr["bytes"] / args.steps
+            res = {"flop_per_solve": fl, "achieved_tflops": fl / t / 1e12,
+                   "fp64_frac": fl / t / rate.value, "hbm_frac": by / t / 1e9 / peak,
+                   "flop_per_algorithmic_byte": fl / by,
+                   "balance_flop_per_byte": rate.value / (peak * 1e9)}
+            res["bound"] = "fp64" if res["fp64_frac"] > res["hbm_frac"] else "hbm"
+        cells = sum(P.desc(l).n_cells for l in range(1, P.n_levels))
+        fac_fl = 2.0 * SCHUR3_FMA_PER_CELL * cells
+        fp64_roof = {"fp64_rate_tflops": rate.value / 1e12,
+                     "how": "pm_measure_fp64_fma: 8 independent FMA chains per thread, 16 CTAs "
+                            "of 256 threads per SM, CUDA events, 2 flop per FMA",
+                     "fp64_residual": res,
+                     "factor": {"flop": fac_fl, "ms": r64["factor_ms"],
+                                "achieved_tflops": fac_fl / (r64["factor_ms"] * 1e-3) / 1e12,
+                                "fp64_frac": fac_fl / (r64["factor_ms"] * 1e-3) / rate.value,
+                                "note": "block elimination of every decoupled cell, Gauss-Jordan "
+                                        "FMA counted in full (zero multipliers are skipped)"}}
     whole = {"fp64": whole_solve("fp64", 8), "mixed": whole_solve("mixed", 4),
              "fp64_lu": whole_solve("fp64_lu", 8, False),
              "mixed_lu": whole_solve("mixed_lu", 4, False)}
@@ -968,6 +1074,7 @@ def main():
         "speedup_mixed_vs_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "roofline": roof,
         "whole_solve_roofline": whole,
+        "fp64_roofline": fp64_roof,
         "nine_block_lu": lu,
         "one_block": one,
         "batch": batch,

@@ -397,6 +397,14 @@ pm_status pm_learned_harvest(pm_handle *h, const double *sol_exact, const double
 /* learned step enabled now (1/0) and fallbacks since attach */
 pm_status pm_learned_status(pm_handle *h, int *enabled, int *fallbacks);
 
+/* Diagnostic (no counterpart in the reference): the FP64 FMA rate of GPU
+ * `device` in flop/s, measured by a kernel of this library (independent FMA
+ * chains on every SM, CUDA events, 2 flop per FMA).  It is the compute
+ * ceiling of the FP64 factorisations and of FP64 sweeps that do more FP64
+ * FMA per byte than the GPU's FP64:HBM balance.  Allocates and frees a
+ * small output buffer. */
+pm_status pm_measure_fp64_fma(int device, double *flops_per_s);
+
 /* Allocation-free L2_0 projection of a P1disc pressure vector on the device
  * (subtract the mean of the constant modes d_p[0], d_p[4], ...), for callers
  * that cannot allocate device memory where they need it: solvers confined to

@@ -109,13 +109,19 @@ def test_kernel_variants(P, oracle, variant, precision):
         assert rel(S.cell_vanka(level, u, f, 2), oracle.cell_vanka(level, u, f, 2)) < tol
 
 
+@pytest.mark.parametrize("decouple", [1, 0])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_default_kernels(P, gpu64, gpu32, precision):
-    """The per-level defaults: stream residual + one cell per warp in FP32,
-    row groups + two cells per warp in FP64 (coarsest level: no cells)."""
-    S = gpu64 if precision == "fp64" else gpu32
-    want = 0 if precision == "fp64" else 1 + 2 * 2
+def test_default_kernels(P, precision, decouple):
+    """The per-level defaults: row groups on decoupled levels (three A
+    blocks) in both precisions; with nine blocks, the flattened stream in
+    FP32 and row groups in FP64; LU apply (where the level keeps the LU) one
+    cell per warp in FP32, two cells per warp in FP64."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    S = PmSolver(P.descs, precision=precision, decouple=decouple)
+    res = 1 if (precision == "mixed" and not decouple) else 0
+    want = res + 2 * (2 if precision == "mixed" else 0)
     assert [S._lib.pm_level_variant(S._h, l) for l in range(1, 3)] == [want, want]
+    S.close()
 
 
 def test_inverse_apply(P, oracle):

@@ -803,11 +803,14 @@ pm_status detect_decoupled(pm_handle *h, bool *changed) {
 // vectors, 3 launches after one warm-up launch), the faster one kept.
 template <typename T>
 pm_status tune_level(pm_handle *h, LevelDev &Lv) {
-  // defaults (option 0): row groups except on FP32 nine-block levels, where
-  // the flattened stream measured faster; LU apply with two cells per warp
-  // in FP64 (the FP64 chain is the bound), one cell per warp in FP32 (each
-  // measured faster in the full solve, with the L2 prefetch of the columns)
-  const int rule_res = (sizeof(T) == sizeof(float) && !Lv.structured) ? 1 : 0;
+  // defaults (option 0): row groups except on FP32 nine-block levels that
+  // read all nine blocks, where the flattened stream measured faster (0.64
+  // against 0.91 ms per 64^3 colour launch); decoupled levels read three blocks and
+  // the row groups are faster there (259 against 272 ms mixed, 549 against
+  // 1087 ms FP64); LU apply with two cells per warp in FP64 (the FP64 chain
+  // is the bound), one cell per warp in FP32 (each measured faster in the
+  // full solve, with the L2 prefetch of the columns)
+  const int rule_res = (sizeof(T) == sizeof(float) && !Lv.structured && !Lv.diag) ? 1 : 0;
   const int ro = h->opt.residual_variant;
   Lv.res_variant = ro == 0 ? rule_res : (ro == 2 ? 1 : 0);
   const bool can_bulk = sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured &&
