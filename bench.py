@@ -177,6 +177,24 @@ def measured_peaks():
 RESIDUAL_DRAM_BYTES_PER_CELL = None
 
 
+# the FP32 sweep kernels by level mode (0 nine blocks + LU, 1 three diagonal
+# blocks, 2 one block A11 = A22 = A33)
+RESIDUAL_KERNEL = {
+    0: "k_vanka_residual<float,4,1> (cell-local residuals over full CSR rows of one colour, "
+       "flattened entry stream; nine A blocks, BT, B)",
+    1: "k_vanka_residual_rows<float,4,2,2,27> (cell-local residuals over full CSR rows of one "
+       "colour, 8 lanes per row; A11, A22, A33, BT, B)",
+    2: "k_vanka_residual_rows<float,4,1,2,27> (cell-local residuals over full CSR rows of one "
+       "colour, 8 lanes per row; one A block (A11 = A22 = A33), BT, B)"}
+APPLY_KERNEL = {
+    0: "k_vanka_apply<float,27> (stored FP32 LU, one cell per warp, columns prefetched in "
+       "registers and L2; substitution + update)",
+    1: "k_schur_apply<float,3> (stored FP32 block elimination: three 27x27 inverses, B, A^-1 BT, "
+       "4x4 Schur inverse; one cell per warp, GEMVs + update)",
+    2: "k_schur_apply<float,1> (stored FP32 block elimination: one 27x27 inverse, B, A^-1 BT, "
+       "4x4 Schur inverse; one cell per warp, GEMVs + update)"}
+
+
 def ncu_traffic(P):
     """DRAM bytes per average residual launch of this workload: the measured
     per-cell traffic times the average cells per residual launch (all
@@ -265,20 +283,21 @@ def cpu_runs_16cube(threads, device):
                      "rows: refactorisation + solve with host vectors", **runs}
 
 
-def solve_bytes(P, s, iterations, decoupled=False, pre=2, post=2, restart=20):
+def solve_bytes(P, s, iterations, mode=0, pre=2, post=2, restart=20):
     """Algorithmic (unique) bytes of one FGMRES solve of `iterations`
     iterations: per iteration one V(pre,post) cycle in value size `s` (8
     FP64, 4 FP32), one FP64 mat-vec on the finest level and the modified
     Gram-Schmidt vector traffic.  Per level with cells, matrix bytes
     mat = nblk s nnzA + 4 nnzA + 4 (N_U+1) + (3 s + 4)(nnzB + nnzBT)
-    + 4 (N_P+1) + 4 (N_U+1) with nblk = 9 A arrays, or 3 on decoupled
-    levels (A11, A22, A33); defect = mat + 3 s DOF; Vanka sweep = mat +
-    3 s DOF + the stored local solve per cell: 85^2 s + 85 (LU and pivots)
-    or 2851 s (block elimination: three 27x27 inverses, B, A^-1 BT and the
-    4x4 Schur inverse); transfers s (2 DOF_f + 2 DOF_c); the coarse dense
-    solve reads its inverse (FP64).  Arnoldi step k of a restart cycle:
-    (k+1) x (2 + 3) x 8 DOF."""
-    nblk = 3 if decoupled else 9
+    + 4 (N_P+1) + 4 (N_U+1) with nblk = 9 A arrays (mode 0), 3 on
+    decoupled levels with distinct diagonal blocks (mode 1) or 1 when
+    A11 = A22 = A33 (mode 2); defect = mat + 3 s DOF; Vanka sweep = mat +
+    3 s DOF + the stored local solve per cell: 85^2 s + 85 (LU and pivots),
+    2851 s (mode 1: three 27x27 inverses, B, A^-1 BT, the 4x4 Schur
+    inverse) or 1393 s (mode 2: one inverse); transfers s (2 DOF_f +
+    2 DOF_c); the coarse dense solve reads its inverse (FP64).  Arnoldi step
+    k of a restart cycle: (k+1) x (2 + 3) x 8 DOF."""
+    nblk = {0: 9, 1: 3, 2: 1}[mode]
     L = P.n_levels
     nbytes = 0.0
 
@@ -292,7 +311,7 @@ def solve_bytes(P, s, iterations, decoupled=False, pre=2, post=2, restart=20):
         dof = 3 * d.n_udof + d.n_pdof
         nloc = 3 * d.n_ulocal + d.n_plocal
         m = mat(d, s, nblk)
-        local = 2851 * s if decoupled else nloc * nloc * s + nloc
+        local = {0: nloc * nloc * s + nloc, 1: 2851 * s, 2: 1393 * s}[mode]
         sweep = m + 3 * s * dof + d.n_cells * local
         dc = P.desc(l - 1)
         dof_c = 3 * dc.n_udof + dc.n_pdof
@@ -328,11 +347,14 @@ def residual_fma(P, nblk):
     return out
 
 
-# FMA of one cell's block-elimination factorisation with three diagonal
-# blocks (k_schur_factor<3>): per component a Gauss-Jordan on [A_c | I | G_c]
-# (27 x 58: sum over k of 26 rows x (57 - k) columns) and its share of the
-# 4x4 Schur complement (16 x 27)
-SCHUR3_FMA_PER_CELL = 3 * (26 * sum(57 - k for k in range(27)) + 16 * 27)
+# FMA of one cell's block-elimination factorisation (k_schur_factor<NB>):
+# NB = 3 (distinct diagonal blocks): per component a Gauss-Jordan on
+# [A_c | I | G_c] (27 x 58: sum over k of 26 rows x (57 - k) columns) and its
+# share of the 4x4 Schur complement (16 x 27); NB = 1 (A11 = A22 = A33): one
+# Gauss-Jordan on [A | I | G1 G2 G3] (27 x 66) and the Schur complement
+# (16 x 27 x 3)
+SCHUR_FMA_PER_CELL = {1: 3 * (26 * sum(57 - k for k in range(27)) + 16 * 27),
+                      2: 26 * sum(65 - k for k in range(27)) + 16 * 27 * 3}
 
 
 def run_reference(args):
@@ -818,6 +840,9 @@ def main():
         solvers[name] = make(P.descs, prec, **extra)
         setup_s[name] = time.perf_counter() - t0
     solvers["mixed_learned"].attach_learned(net, omega=1.0, fallback_ratio=0.5)
+    # how the finest level runs per variant: 0 nine blocks + 85x85 LU, 1
+    # three diagonal blocks, 2 one block (A11 = A22 = A33)
+    modes = {k: S.level_decoupled(args.levels - 1) for k, S in solvers.items()}
     # the same system as NSTYPE-2 levels (one velocity block; the Galerkin
     # Oseen form has A12..A32 = 0 and A11 = A22 = A33), smoothed by the exact
     # block solve of the cell systems: reported beside the headline
@@ -956,18 +981,14 @@ def main():
     a_ach, a_ms, a_bytes = kernel_roof(prof.get("apply"))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(P),
-            "kernel": "k_vanka_residual_rows<float,4,2,2,27> (cell-local residuals over full "
-                      "CSR rows of one colour, 8 lanes per row; decoupled levels: A11, A22, A33, "
-                      "BT, B)",
+            "kernel": RESIDUAL_KERNEL[modes["mixed"]],
             "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "bytes_per_launch": per_launch,
-            "apply_kernel": {"name": "k_schur_apply<float,3> (stored FP32 block elimination: "
-                                     "three 27x27 inverses, B, A^-1 BT, 4x4 Schur inverse; "
-                                     "one cell per warp, GEMVs + update)",
+            "apply_kernel": {"name": APPLY_KERNEL[modes["mixed"]],
                              "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,
                              "avg_launch_ms": a_ms, "bytes_per_launch": a_bytes}}
-    def whole_solve(name, s_val, decoupled=True):
+    def whole_solve(name, s_val):
         r = results[name]
-        nb = solve_bytes(P, s_val, r["iterations"], decoupled=decoupled)
+        nb = solve_bytes(P, s_val, r["iterations"], mode=modes[name])
         gbs = nb / (r["solve_ms"] * 1e-3) / 1e9
         return {"algorithmic_gb": nb / 1e9, "achieved_gbs": gbs, "frac": gbs / peak,
                 "note": "unique bytes of the whole FGMRES solve (V-cycles, FP64 mat-vecs, "
@@ -995,7 +1016,7 @@ def main():
                    "balance_flop_per_byte": rate.value / (peak * 1e9)}
             res["bound"] = "fp64" if res["fp64_frac"] > res["hbm_frac"] else "hbm"
         cells = sum(P.desc(l).n_cells for l in range(1, P.n_levels))
-        fac_fl = 2.0 * SCHUR3_FMA_PER_CELL * cells
+        fac_fl = 2.0 * SCHUR_FMA_PER_CELL.get(modes["fp64"], 0) * cells
         fp64_roof = {"fp64_rate_tflops": rate.value / 1e12,
                      "how": "pm_measure_fp64_fma: 8 independent FMA chains per thread, 16 CTAs "
                             "of 256 threads per SM, CUDA events, 2 flop per FMA",
@@ -1006,8 +1027,7 @@ def main():
                                 "note": "block elimination of every decoupled cell, Gauss-Jordan "
                                         "FMA counted in full (zero multipliers are skipped)"}}
     whole = {"fp64": whole_solve("fp64", 8), "mixed": whole_solve("mixed", 4),
-             "fp64_lu": whole_solve("fp64_lu", 8, False),
-             "mixed_lu": whole_solve("mixed_lu", 4, False)}
+             "fp64_lu": whole_solve("fp64_lu", 8), "mixed_lu": whole_solve("mixed_lu", 4)}
     lu = {"note": "the same nine-block system with decouple=0: every cell solved by the "
                   "85x85 LU of the reference's CellVanka and all nine A blocks read"}
     for name in ("mixed_lu", "fp64_lu"):

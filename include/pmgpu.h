@@ -132,10 +132,11 @@ typedef struct {
                              off-diagonal blocks A12..A32 are all zero
                              (checked on the device after every upload or
                              assembly) reads only A11, A22, A33 in its
-                             defects and sweeps, and its cells are solved by
-                             exact block elimination (three 27x27 inverses
-                             and the 4x4 pressure Schur complement) instead
-                             of the 85x85 LU -- the same local solution;
+                             defects and sweeps -- only A11 when the three
+                             are identical -- and its cells are solved by
+                             exact block elimination (the 27x27 inverses and
+                             the 4x4 pressure Schur complement) instead of
+                             the 85x85 LU: the same local solution;
                              0: the 85x85 LU and all nine blocks on every
                              nine-block level, as the reference's CellVanka
                              (src/FE/NSE_MGLevel4.C:1784-2031)              */
@@ -239,9 +240,12 @@ int       pm_n_levels(pm_handle *h);
 int       pm_level_ndof(pm_handle *h, int level);
 /* velocity blocks of a level: 9 (NSTYPE 4) or 1 (NSTYPE 2); -1 if no such level */
 int       pm_level_blocks(pm_handle *h, int level);
-/* 1 if a nine-block level runs decoupled (pm_options.decouple and its
- * A12..A32 are zero: diagonal blocks only, block-elimination cell solve),
- * 0 if not, -1 if no such level */
+/* How a nine-block level runs (pm_options.decouple, decided on the device
+ * after every upload or assembly): 0 all nine blocks and the 85x85 LU; 1
+ * A12..A32 are zero: A11, A22, A33 read, cells solved by block elimination
+ * with three 27x27 inverses; 2 also A11 = A22 = A33: one block read, one
+ * inverse per cell (the one-block operator's kernels).  0 for one-block
+ * descriptors, -1 if no such level. */
 int       pm_level_decoupled(pm_handle *h, int level);
 /* kernels a level runs: residual kernel (0 row groups, 1 stream) + 2 * apply
  * kernel (0 two cells per warp, 1 bulk-staged, 2 one cell per warp); -1 if

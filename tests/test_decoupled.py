@@ -1,15 +1,18 @@
-"""Nine-block levels whose off-diagonal velocity blocks vanish (the Galerkin
-Oseen form, src/FE/NSE3D_FixPo.C:1919-2071) run decoupled: their defects and
-sweeps read A11, A22, A33 only and each cell's 85x85 system is solved by
-exact block elimination (three 27x27 inverses and the 4x4 pressure Schur
-complement) instead of the LU of the reference's CellVanka
-(src/FE/NSE_MGLevel4.C:1784-2031).  The local solution is the same, so the
-sweeps match the oracle's LU sweeps to the FP64 tolerance of the other
-Vanka tests (1e-9), the mixed ones to 5e-4, and FGMRES reaches the same
-solution (1e-6 after L2_0 normalisation) in the same FP64 iteration count.
+"""Nine-block levels whose off-diagonal velocity blocks vanish run decoupled:
+their defects and sweeps read the diagonal blocks only and each cell's 85x85
+system is solved by exact block elimination (27x27 inverses and the 4x4
+pressure Schur complement) instead of the LU of the reference's CellVanka
+(src/FE/NSE_MGLevel4.C:1784-2031).  Mode 1: A11, A22, A33 differ (three
+arrays, three inverses); mode 2: A11 = A22 = A33, as in the Galerkin Oseen
+form (src/FE/NSE3D_FixPo.C:1919-2071): one array, one inverse.  The local
+solution is the same, so the sweeps match the oracle's LU sweeps to the FP64
+tolerance of the other Vanka tests (1e-9), the mixed ones to 5e-4, and
+FGMRES reaches the same solution (1e-6 after L2_0 normalisation) in the same
+FP64 iteration count.
 
 A level whose A12..A32 hold nonzero entries keeps the 85x85 LU and all nine
-blocks; pm_update_matrices re-checks after every upload and switches.
+blocks (mode 0); pm_update_matrices re-checks after every upload and
+switches.
 """
 import numpy as np
 import pytest
@@ -47,6 +50,14 @@ def uncouple(P):
             a["a"][k][:] = 0.0
 
 
+def distinct_diagonal(P):
+    """A22 = 1.5 A11, A33 = 0.75 A11 (still uncoupled), in place."""
+    for level in range(P.n_levels):
+        a = P.arrays(level)
+        a["a"][4][:] = 1.5 * a["a"][0]
+        a["a"][8][:] = 0.75 * a["a"][0]
+
+
 def fgmres_parity(P, S, oracle_params=None):
     b = P.rhs()
     x0 = np.zeros_like(b)
@@ -64,9 +75,9 @@ def test_galerkin_levels_run_decoupled(problems, precision):
     from to_merge_master_parmoon_gb300 import PmSolver
     P = problems(3, 1e-2, 0)
     S = PmSolver(P.descs, precision=precision, restart=20, maxit=80)
-    assert [S.level_decoupled(l) for l in range(3)] == [True, True, True]
+    assert [S.level_decoupled(l) for l in range(3)] == [2, 2, 2]
     S0 = PmSolver(P.descs, precision=precision, decouple=0)
-    assert [S0.level_decoupled(l) for l in range(3)] == [False, False, False]
+    assert [S0.level_decoupled(l) for l in range(3)] == [0, 0, 0]
     O = Oracle(P)
     rng = np.random.default_rng(3)
     tol = 1e-9 if precision == "fp64" else 5e-4
@@ -97,27 +108,55 @@ def test_decoupled_fgmres_matches_oracle(problems, precision):
     S.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_distinct_diagonal_blocks(precision):
+    """Uncoupled levels with A11, A22, A33 all different run in mode 1 (three
+    arrays, three inverses per cell) and match the oracle's LU sweeps and
+    FGMRES."""
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    P = OseenProblem(n_levels=3, nu=1e-2, seed=4)
+    distinct_diagonal(P)
+    b = P.rhs()
+    r0 = np.linalg.norm(Oracle(P).coupled_defect(2, np.zeros_like(b), b))
+    S = PmSolver(P.descs, precision=precision, restart=20, maxit=80, res_norm_min=1e-10 * r0)
+    assert [S.level_decoupled(l) for l in range(3)] == [1, 1, 1]
+    O = Oracle(P)
+    rng = np.random.default_rng(8)
+    tol = 1e-9 if precision == "fp64" else 5e-4
+    for level in (1, 2):
+        u = 0.1 * rng.standard_normal(P.ndof(level))
+        f = rng.standard_normal(P.ndof(level))
+        assert rel(S.cell_vanka(level, u, f, 2), O.cell_vanka(level, u, f, 2)) < tol
+    d, ig, io, tol = fgmres_parity(P, S)
+    assert ig["true_res"] <= 1.05 * tol and d < 1e-6
+    if precision == "fp64":
+        assert ig["iterations"] == io["iterations"]
+    S.close()
+
+
 def test_coupled_blocks_keep_the_lu_and_update_switches():
-    """Set up on Galerkin values (block solve on every level), then
+    """Set up on Galerkin values (mode 2 on every level), then
     pm_update_matrices with A12 = A21 = 0.05 A11 switches every level to the
-    85x85 LU and the nine blocks (its factor storage grows), and back with
-    the uncoupled values; each time FGMRES matches the oracle's."""
+    85x85 LU and the nine blocks (mode 0: its factor storage grows), then
+    uncoupled with distinct diagonal blocks to mode 1; each time FGMRES
+    matches the oracle's."""
     from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
     P = OseenProblem(n_levels=3, nu=1e-2, seed=5)
     b = P.rhs()
     r0 = np.linalg.norm(Oracle(P).coupled_defect(2, np.zeros_like(b), b))
     S = PmSolver(P.descs, precision="fp64", restart=20, maxit=80, res_norm_min=1e-10 * r0)
-    assert all(S.level_decoupled(l) for l in range(3))
+    assert [S.level_decoupled(l) for l in range(3)] == [2, 2, 2]
     d, ig, io, tol = fgmres_parity(P, S)
     assert d < 1e-6 and ig["iterations"] == io["iterations"]
     couple(P, 0.05)
     S.update_matrices(P.descs)
-    assert not any(S.level_decoupled(l) for l in range(3))
+    assert [S.level_decoupled(l) for l in range(3)] == [0, 0, 0]
     d, ig, io, tol = fgmres_parity(P, S)
     assert d < 1e-6 and ig["iterations"] == io["iterations"]
     uncouple(P)
+    distinct_diagonal(P)
     S.update_matrices(P.descs)
-    assert all(S.level_decoupled(l) for l in range(3))
+    assert [S.level_decoupled(l) for l in range(3)] == [1, 1, 1]
     d, ig, io, tol = fgmres_parity(P, S)
     assert d < 1e-6 and ig["iterations"] == io["iterations"]
     S.close()

@@ -61,8 +61,11 @@ DevCsr<float> CsrStore::view<float>() const {
 struct LevelDev {
   int nu = 0, np = 0, ndof = 0, nact = 0, hb = 0, ndir = 0, ncells = 0;
   int a_nnz = 0, b_nnz = 0, bt_nnz = 0;
-  int structured = 0;  // velocity blocks: A12..A32 = 0 and A11 = A22 = A33 (exactly)
-  int diag = 0;        // nine-block level whose A12..A32 are all zero (block solve)
+  int structured = 0;  // one-block descriptor (NSTYPE 2: a[0] only)
+  // decoupled nine-block level (A12..A32 all zero): 1 with distinct diagonal
+  // blocks (three A arrays read, block solve with three inverses), 2 with
+  // A11 = A22 = A33 (one array read, the one-block operator's solve)
+  int diag = 0;
   int res_variant = 0;    // local-residual kernel of the sweep (0 row groups, 1 stream)
   int apply_variant = 0;  // LU apply: 0 two cells per warp, 1 bulk-staged (FP32), 2 one cell per warp
   std::vector<int> h_udofs, h_pdofs, h_parent, h_child, h_colour;
@@ -99,18 +102,21 @@ struct LevelDev {
   template <typename T>
   DevOp<T> op() const;
   DevCells cells() const { return DevCells{ncells, udofs, pdofs, nl}; }
+  // one A block for the three components: a one-block descriptor, or a
+  // decoupled nine-block level with A11 = A22 = A33
+  bool one_block() const { return structured || diag == 2; }
   // the Schur block solve of one-block levels exists for Q2 hexahedra only
-  bool schur() const { return structured && nl == NU_LOC; }
+  bool schur() const { return one_block() && nl == NU_LOC; }
   // block elimination with three diagonal blocks (decoupled nine-block levels)
-  bool schur3() const { return diag && !structured && nl == NU_LOC; }
+  bool schur3() const { return diag == 1 && nl == NU_LOC; }
   size_t fac_bytes = 0;  // allocated factor storage
 };
 template <>
 DevOp<double> LevelDev::op<double>() const {
   DevOp<double> o;
   o.nu = nu;
-  o.structured = structured;
-  o.diag = diag;
+  o.structured = structured || diag == 2;
+  o.diag = diag == 1;
   o.np = np;
   o.nact = nact;
   o.a_rowptr = a_rowptr;
@@ -131,8 +137,8 @@ template <>
 DevOp<float> LevelDev::op<float>() const {
   DevOp<float> o;
   o.nu = nu;
-  o.structured = structured;
-  o.diag = diag;
+  o.structured = structured || diag == 2;
+  o.diag = diag == 1;
   o.np = np;
   o.nact = nact;
   o.a_rowptr = a_rowptr;
@@ -752,7 +758,7 @@ pm_status ensure_factors(pm_handle *h, LevelDev &Lv) {
 void level_bytes(pm_handle *h, LevelDev &Lv) {
   if (Lv.ncells <= 0) return;
   const double sv = mixed(h) ? 4.0 : 8.0;
-  const double nblk = Lv.structured ? 1.0 : (Lv.diag ? 3.0 : 9.0);
+  const double nblk = Lv.one_block() ? 1.0 : (Lv.diag == 1 ? 3.0 : 9.0);
   const double mat = nblk * sv * Lv.a_nnz + 4.0 * Lv.a_nnz + 4.0 * (Lv.nu + 1) +
                      (3.0 * sv + 4.0) * ((double)Lv.b_nnz + Lv.bt_nnz) + 4.0 * (Lv.np + 1) +
                      4.0 * (Lv.nu + 1);
@@ -764,20 +770,25 @@ void level_bytes(pm_handle *h, LevelDev &Lv) {
   Lv.vanka_apply_bytes = ((double)Lv.ncells * per_cell + 2.0 * sv * Lv.ndof) / Lv.ncells;
 }
 
-// Decoupled nine-block levels: one device pass per level over the six
-// off-diagonal velocity blocks (after their Dirichlet rows were zeroed),
-// then one read-back.  *changed reports levels whose mode flipped; their
-// captured V-cycles are dropped (the kernels differ).
-pm_status detect_decoupled(pm_handle *h, bool *changed) {
+// Decoupled nine-block levels: one device pass per level over the nine
+// velocity blocks (after the Dirichlet rows' off-diagonal entries were
+// zeroed), then one read-back: A12..A32 all zero -> diag 1, and A11 = A22 =
+// A33 as well -> diag 2.  Levels `only` (all when -1).  *changed reports
+// levels whose mode flipped; the captured V-cycles are then dropped (the
+// kernels differ).
+pm_status detect_decoupled(pm_handle *h, bool *changed, int only = -1) {
   const int n = (int)h->L.size();
   if (changed) *changed = false;
   if (!h->diag_flags) PM_TRY(dalloc(h, &h->diag_flags, (size_t)n));
   if (cudaMemsetAsync(h->diag_flags, 0, sizeof(int) * n, h->stream) != cudaSuccess)
     return cuda_fail(h, "block check reset");
+  auto checked = [&](int l) {
+    return (only < 0 || l == only) && !h->L[l].structured && h->opt.decouple;
+  };
   for (int l = 0; l < n; ++l) {
+    if (!checked(l)) continue;
     LevelDev &Lv = h->L[l];
-    if (Lv.structured || !h->opt.decouple) continue;
-    PM_LAUNCH(launch_offdiag_nonzero(Lv.op<double>(), Lv.a_nnz, h->diag_flags + l, h->stream));
+    PM_LAUNCH(launch_block_structure(Lv.op<double>(), Lv.a_nnz, h->diag_flags + l, h->stream));
   }
   std::vector<int> f(n, 1);
   if (cudaMemcpyAsync(f.data(), h->diag_flags, sizeof(int) * n, cudaMemcpyDeviceToHost,
@@ -786,8 +797,9 @@ pm_status detect_decoupled(pm_handle *h, bool *changed) {
   PM_TRY(sync(h, "block check"));
   bool any = false;
   for (int l = 0; l < n; ++l) {
+    if (only >= 0 && l != only) continue;
     LevelDev &Lv = h->L[l];
-    const int d = (!Lv.structured && h->opt.decouple && f[l] == 0) ? 1 : 0;
+    const int d = !checked(l) ? 0 : ((f[l] & 1) ? 0 : ((f[l] & 2) ? 1 : 2));
     if (d != Lv.diag) {
       Lv.diag = d;
       any = true;
@@ -814,13 +826,13 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
   const int ro = h->opt.residual_variant;
   Lv.res_variant = ro == 0 ? rule_res : (ro == 2 ? 1 : 0);
   const bool can_bulk = sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured &&
-                        !Lv.schur3() && Lv.nl == NU_LOC;
+                        Lv.diag == 0 && Lv.nl == NU_LOC;
   const int ao = h->opt.apply_variant;
   const int rule_apply = sizeof(T) == sizeof(double) ? 0 : 2;
   Lv.apply_variant = ao == 0 ? rule_apply : (ao == 2 ? 2 : (can_bulk ? 1 : 0));
   const bool tune_res = h->opt.residual_variant < 0;
   const bool tune_apply =
-      h->opt.apply_variant < 0 && !use_inverse(h) && !Lv.structured && !Lv.schur3();
+      h->opt.apply_variant < 0 && !use_inverse(h) && !Lv.structured && Lv.diag == 0;
   if ((!tune_res && !tune_apply) || Lv.ncells == 0) return PM_OK;
   int kb = 0, nb = 0;
   for (size_t k = 0; k + 1 < Lv.colouring.ptr.size(); ++k) {
@@ -894,11 +906,12 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
 
 // After new matrix values: re-check which levels run decoupled and, for
 // levels whose mode changed, the factor storage, byte counts and kernels.
-pm_status refresh_modes(pm_handle *h) {
+pm_status refresh_modes(pm_handle *h, int only = -1) {
   bool changed = false;
-  PM_TRY(detect_decoupled(h, &changed));
+  PM_TRY(detect_decoupled(h, &changed, only));
   if (!changed) return PM_OK;
   for (size_t l = 1; l < h->L.size(); ++l) {
+    if (only >= 0 && (int)l != only) continue;
     LevelDev &Lv = h->L[l];
     PM_TRY(ensure_factors(h, Lv));
     level_bytes(h, Lv);
@@ -1646,20 +1659,9 @@ static pm_status assemble_impl(pm_handle *h, int level, const double *d_cell_h,
   PM_LAUNCH(launch_assemble_level(op, Lv.cells(), Lv.colour_cells, Lv.colouring.ptr.data(),
                                   (int)Lv.colouring.ptr.size() - 1, d_cell_h, d_conv, nu,
                                   h->stream));
-  if (!Lv.structured) {
-    // the assembled A12..A32 are zero by construction: no device check
-    const int d = h->opt.decouple ? 1 : 0;
-    if (d != Lv.diag) {
-      Lv.diag = d;
-      drop_graphs(h);
-      PM_TRY(ensure_factors(h, Lv));
-      level_bytes(h, Lv);
-      if (mixed(h))
-        PM_TRY(tune_level<float>(h, Lv));
-      else
-        PM_TRY(tune_level<double>(h, Lv));
-    }
-  }
+  // the level's block structure (the assembly zeroes A12..A32 and writes
+  // the same values into A11, A22, A33)
+  PM_TRY(refresh_modes(h, level));
   if (mixed(h)) {
     const int nblk = Lv.structured ? 1 : 9;
     for (int k = 0; k < nblk; ++k)

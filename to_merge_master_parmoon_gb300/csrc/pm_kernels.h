@@ -42,8 +42,9 @@ struct DevOp {
   // only a[0] is read
   int structured;
   // 1 (nine-block levels only): the off-diagonal blocks A12..A32 are all
-  // zero (checked on the device after every upload); the sweeps read only
-  // the diagonal blocks ad[0..2] = A11, A22, A33
+  // zero and the diagonal blocks differ (checked on the device after every
+  // upload); the sweeps read only ad[0..2] = A11, A22, A33.  (A nine-block
+  // level whose diagonal blocks are also identical runs with structured = 1.)
   int diag;
   const int *a_rowptr, *a_col;
   const T *a[9];
@@ -199,9 +200,10 @@ int launch_schur3_factor(const DevOp<double> &op, const DevCells &cells, TF *fac
 template <typename T>
 int launch_schur3_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                         const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s);
-// flag[0] |= 1 if any entry of the off-diagonal velocity blocks
-// a[1], a[2], a[3], a[5], a[6], a[7] (n entries each) is nonzero
-int launch_offdiag_nonzero(const DevOp<double> &op, long long n, int *flag, cudaStream_t s);
+// Block structure of a nine-block level (n entries per block): flag[0] |= 1
+// if any entry of the off-diagonal blocks a[1], a[2], a[3], a[5], a[6], a[7]
+// is nonzero, |= 2 if the diagonal blocks a[0], a[4], a[8] differ anywhere
+int launch_block_structure(const DevOp<double> &op, long long n, int *flag, cudaStream_t s);
 
 // --------------------------------------------------------------- assembly --
 // Writable view of a level's FP64 values for device assembly: NSTYPE 4 fills

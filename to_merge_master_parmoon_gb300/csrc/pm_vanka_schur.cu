@@ -347,16 +347,21 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_schur_apply(
   }
 }
 
-// flag |= 1 when an off-diagonal velocity block holds a nonzero entry
-__global__ void __launch_bounds__(256) k_offdiag_nonzero(DevOp<double> op, long long n,
+// flag |= 1 when an off-diagonal velocity block holds a nonzero entry,
+// |= 2 when the diagonal blocks differ somewhere (A22 != A11 or A33 != A11,
+// compared as values; a NaN counts as different)
+__global__ void __launch_bounds__(256) k_block_structure(DevOp<double> op, long long n,
                                                          int *flag) {
-  bool nz = false;
+  bool nz = false, differ = false;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     nz |= op.a[1][i] != 0.0 || op.a[2][i] != 0.0 || op.a[3][i] != 0.0 || op.a[5][i] != 0.0 ||
           op.a[6][i] != 0.0 || op.a[7][i] != 0.0;
+    const double d = op.a[0][i];
+    differ |= !(op.a[4][i] == d) || !(op.a[8][i] == d);
   }
-  if (__any_sync(kFull, nz) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+  const int bits = (__any_sync(kFull, nz) ? 1 : 0) | (__any_sync(kFull, differ) ? 2 : 0);
+  if (bits && (threadIdx.x & 31) == 0) atomicOr(flag, bits);
 }
 
 inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
@@ -409,11 +414,11 @@ int launch_schur3_apply(const DevCells &cells, int nu, const int *cell_list, int
   return apply_impl<T, 3>(cells, nu, cell_list, ncol, factors, rbuf, damp, u, s);
 }
 
-int launch_offdiag_nonzero(const DevOp<double> &op, long long n, int *flag, cudaStream_t s) {
+int launch_block_structure(const DevOp<double> &op, long long n, int *flag, cudaStream_t s) {
   if (n <= 0) return 0;
   long long g = (n + 255) / 256;
   if (g > 4 * 152) g = 4 * 152;
-  k_offdiag_nonzero<<<(unsigned)g, 256, 0, s>>>(op, n, flag);
+  k_block_structure<<<(unsigned)g, 256, 0, s>>>(op, n, flag);
   return ok() < 0 ? -1 : 1;
 }
 

@@ -91,10 +91,11 @@ class PmSolver:
     def n_levels(self) -> int:
         return self._lib.pm_n_levels(self._h)
 
-    def level_decoupled(self, level: int) -> bool:
-        """True when a nine-block level runs decoupled (A12..A32 zero:
-        diagonal blocks only, block-elimination cell solve)."""
-        return self._lib.pm_level_decoupled(self._h, level) == 1
+    def level_decoupled(self, level: int) -> int:
+        """How a nine-block level runs: 0 nine blocks and the 85x85 LU; 1
+        A12..A32 zero (three diagonal blocks, block elimination); 2 also
+        A11 = A22 = A33 (one block read, one inverse per cell)."""
+        return self._lib.pm_level_decoupled(self._h, level)
 
     def ndof(self, level: int = -1) -> int:
         return self._ndof[level]
