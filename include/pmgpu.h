@@ -236,6 +236,12 @@ pm_status pm_setup(pm_handle *h);
 /* Replace the matrix values of every level (same patterns) and refactor. */
 pm_status pm_update_matrices(pm_handle *h, const pm_level_desc *levels, int n_levels);
 pm_status pm_destroy(pm_handle *h);
+/* FGMRES stopping parameters of the next solves (TItMethod::SetMaxit,
+ * SetMinit, SetRedFactor, SetResNormMin, SetDivFactor, SetRestart,
+ * include/FE/ItMethod.h:118-171); restart at most the value the handle was
+ * set up with (PM_BADARG otherwise). */
+pm_status pm_set_tolerances(pm_handle *h, int restart, int maxit, int minit, double red_factor,
+                            double res_norm_min, double div_factor);
 int       pm_n_levels(pm_handle *h);
 int       pm_level_ndof(pm_handle *h, int level);
 /* velocity blocks of a level: 9 (NSTYPE 4) or 1 (NSTYPE 2); -1 if no such level */

@@ -13,6 +13,10 @@
   the FE and geometry databases they read (REF_TRANSFER_TUS), driven by
   ref_transfer.cpp (only when the tree is present; its outputs are committed
   as tests/golden/ref_transfer_*.npz).
+* ``oracle/_ref/libref_facade.so`` — include/pmgpu_parmoon.h (the solver as a
+  ParMooN TItMethod) compiled against the reference's headers and matrix
+  classes in ref_facade.cpp, linked with libpmgpu.so (only when the tree is
+  present).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 what this builds.
@@ -90,6 +94,39 @@ def build_ref_harness() -> Path | None:
     _compile(jobs, _ref_flags())
     _run(["g++", "-shared", "-fopenmp", "-Wl,--gc-sections", "-Wl,-z,defs",
           *[str(o) for _, o in jobs], "-o", str(out)])
+    return out
+
+
+# reference translation units of the facade check: the TItMethod base and
+# the matrix and structure classes the adapter reads
+REF_FACADE_TUS = ("FE/ItMethod", "FE/Matrix", "FE/SquareMatrix", "FE/Structure",
+                  "FE/SquareStructure", "FE/Blas1")
+
+
+def build_ref_facade() -> Path | None:
+    """Compile include/pmgpu_parmoon.h (the library as a ParMooN TItMethod)
+    against the reference's own headers in ref_facade.cpp, with the
+    reference's matrix classes, into oracle/_ref/libref_facade.so, linked
+    with the package's libpmgpu.so.  Returns None without the tree or
+    without libpmgpu.so."""
+    src = REFERENCE / "src"
+    gpu = ROOT / "to_merge_master_parmoon_gb300" / "_build" / "libpmgpu.so"
+    if not gpu.exists() or not all((src / f"{t}.C").exists() for t in REF_FACADE_TUS):
+        return None
+    objdir = REF_OUT / "facade_obj"
+    objdir.mkdir(parents=True, exist_ok=True)
+    out = REF_OUT / "libref_facade.so"
+    mine = [HERE / "ref_facade.cpp", ROOT / "include" / "pmgpu_parmoon.h",
+            ROOT / "include" / "pmgpu_facade.h", ROOT / "include" / "pmgpu.h", gpu, *_ref_deps()]
+    if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in mine):
+        return out
+    jobs = [(src / f"{t}.C", objdir / f"{Path(t).name}.o") for t in REF_FACADE_TUS]
+    jobs.append((HERE / "ref_facade.cpp", objdir / "ref_facade.o"))
+    flags = _ref_flags() + [f"-I{ROOT / 'include'}"]
+    _compile(jobs, [f if f != "-std=c++11" else "-std=c++17" for f in flags])
+    _run(["g++", "-shared", "-fopenmp", "-Wl,--gc-sections", "-Wl,-z,defs",
+          *[str(o) for _, o in jobs], f"-L{gpu.parent}", "-lpmgpu",
+          f"-Wl,-rpath,{gpu.parent}", "-o", str(out)])
     return out
 
 
@@ -209,3 +246,4 @@ if __name__ == "__main__":
     print(build_ref_pin())
     print(build_ref_harness())
     print(build_ref_transfer())
+    print(build_ref_facade())

@@ -88,6 +88,8 @@ GPU_SYMBOLS = {
     "pm_level_ndof": (C.c_int, [_P, C.c_int]),
     "pm_level_blocks": (C.c_int, [_P, C.c_int]),
     "pm_level_decoupled": (C.c_int, [_P, C.c_int]),
+    "pm_set_tolerances": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                    C.c_double]),
     "pm_measure_fp64_fma": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "pm_level_variant": (C.c_int, [_P, C.c_int]),
     "pm_coupled_defect": (C.c_int, [_P, C.c_int, c_double_p, c_double_p, c_double_p, C.c_int]),

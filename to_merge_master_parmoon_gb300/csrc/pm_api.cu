@@ -1413,6 +1413,23 @@ pm_status pm_destroy(pm_handle *h) {
   return PM_OK;
 }
 
+pm_status pm_set_tolerances(pm_handle *h, int restart, int maxit, int minit, double red_factor,
+                            double res_norm_min, double div_factor) {
+  if (!h) return PM_BADARG;
+  if (maxit < 0 || minit < 0 || restart <= 0 || !(red_factor >= 0.0) || !(res_norm_min >= 0.0) ||
+      !(div_factor > 0.0))
+    return fail(h, PM_BADARG, "pm_set_tolerances: invalid value");
+  if (h->setup_done && std::min(restart, maxit) > h->restart)
+    return fail(h, PM_BADARG, "pm_set_tolerances: restart larger than the set-up allocation");
+  h->opt.restart = restart;
+  h->opt.maxit = maxit;
+  h->opt.minit = minit;
+  h->opt.red_factor = red_factor;
+  h->opt.res_norm_min = res_norm_min;
+  h->opt.div_factor = div_factor;
+  return PM_OK;
+}
+
 int pm_n_levels(pm_handle *h) { return h ? (int)h->L.size() : 0; }
 int pm_level_ndof(pm_handle *h, int l) {
   return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].ndof : -1;
