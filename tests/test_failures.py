@@ -107,7 +107,7 @@ def test_bulk_copy_wait_limit_gives_pm_timeout(problems):
     from to_merge_master_parmoon_gb300 import PmError, PmSolver
     P = problems(3, 1e-2, 0)
     S = PmSolver(P.descs, precision="mixed", decouple=0, apply_variant=1, wait_limit=1)
-    assert S._lib.pm_level_variant(S._h, 2) // 2 == 1  # the bulk-copy apply
+    assert S._lib.pm_level_variant(S._h, 2) // 3 == 1  # the bulk-copy apply
     rng = np.random.default_rng(1)
     u, f = 0.1 * rng.standard_normal(P.ndof(2)), rng.standard_normal(P.ndof(2))
     with pytest.raises(PmError) as e:
@@ -115,3 +115,21 @@ def test_bulk_copy_wait_limit_gives_pm_timeout(problems):
     assert e.value.status == PM_TIMEOUT
     S.close()
     assert clean_solve_ok(P, precision="mixed", decouple=0, apply_variant=1)
+
+
+def test_update_with_a_changed_pattern_is_refused():
+    """pm_update_matrices takes new values for the set-up's patterns only:
+    a column index moved within the same nnz is refused (PM_BADARG), the
+    original pattern is accepted again."""
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmError, PmSolver
+    P = OseenProblem(n_levels=3, nu=1e-2, seed=0)
+    S = PmSolver(P.descs)
+    col = P.arrays(2)["a_col"]
+    old = int(col[61])
+    col[61] = col[62]  # a sampled position: same nnz, different pattern
+    with pytest.raises(PmError) as e:
+        S.update_matrices(P.descs)
+    assert e.value.status == 6
+    col[61] = old
+    S.update_matrices(P.descs)
+    S.close()
