@@ -78,12 +78,19 @@ def parse():
                     help="cell-Vanka sweeps of the finest level only (pm_cell_vanka, warm-up "
                          "+ steps sweeps) in the given precision: the case profiled for the "
                          "local-residual and apply kernels")
+    ap.add_argument("--residual-variant", type=int, default=0,
+                    help="pm_options.residual_variant of the --only-sweep case")
     ap.add_argument("--decouple", type=int, default=1,
                     help="pm_options.decouple of the --only-sweep / --only-factor cases (0: the "
                          "85x85 LU and all nine blocks on every level)")
     ap.add_argument("--channel-steps", type=int, default=10,
                     help="timed Crank-Nicolson steps per variant of the channel run "
                          "(a bounded sample of its 200 steps)")
+    ap.add_argument("--channel-variants", default="fp64,mixed,mixed_learned,mixed_scaled_divergence",
+                    help="comma-separated channel variants to run")
+    ap.add_argument("--only-channel", action="store_true",
+                    help="the time-dependent channel run only (the learned variant is skipped): "
+                         "e.g. all 200 steps of one variant")
     ap.add_argument("--only-assembly", action="store_true",
                     help="device assembly of every level only (one-block FP64 levels, "
                          "warm-up + steps passes): the case profiled for k_assemble_cells")
@@ -182,13 +189,23 @@ RESIDUAL_DRAM_BYTES_PER_CELL = None
 
 # the FP32 sweep kernels by level mode (0 nine blocks + LU, 1 three diagonal
 # blocks, 2 one block A11 = A22 = A33)
-RESIDUAL_KERNEL = {
-    0: "k_vanka_residual<float,4,1> (cell-local residuals over full CSR rows of one colour, "
-       "flattened entry stream; nine A blocks, BT, B)",
-    1: "k_vanka_residual_rows<float,4,2,2,27> (cell-local residuals over full CSR rows of one "
-       "colour, 8 lanes per row; A11, A22, A33, BT, B)",
-    2: "k_vanka_residual_rows<float,4,1,2,27> (cell-local residuals over full CSR rows of one "
-       "colour, 8 lanes per row; one A block (A11 = A22 = A33), BT, B)"}
+def residual_kernel_name(mode, variant):
+    """The FP32 local-residual kernel a level runs: level mode (0 nine blocks
+    + LU, 1 three diagonal blocks, 2 one block A11 = A22 = A33) and residual
+    kernel (0 row groups, 1 flattened stream, 2 cell store)."""
+    blocks = {0: "nine A blocks", 1: "A11, A22, A33", 2: "one A block (A11 = A22 = A33)"}[mode]
+    if variant == 2:
+        return (f"k_vanka_residual_cells<float,{1 if mode == 2 else 3}> (cell-local residuals "
+                f"from the per-cell row store of one colour, vector loads, segmented warp sums; "
+                f"{blocks}, BT, B)")
+    if variant == 1:
+        return ("k_vanka_residual<float,4,1> (cell-local residuals over full CSR rows of one "
+                f"colour, flattened entry stream; {blocks}, BT, B)")
+    kind = {0: 0, 1: 2, 2: 1}[mode]
+    return (f"k_vanka_residual_rows<float,4,{kind},{1 if kind == 0 else 2},27> (cell-local "
+            f"residuals over full CSR rows of one colour, 8 lanes per row; {blocks}, BT, B)")
+
+
 APPLY_KERNEL = {
     0: "k_vanka_apply<float,27> (stored FP32 LU, one cell per warp, columns prefetched in "
        "registers and L2; substitution + update)",
@@ -537,10 +554,13 @@ def channel_run(args, threads, net):
     # B unscaled as with the reference's default SCALE_DIVERGENCE_CONSTRAINT = -1;
     # the last variant sets it to 1 (B scaled by dt as well,
     # src/System/SystemTNSE3D.C:1248-1264)
+    wanted = set(args.channel_variants.split(","))
     for name, prec, learned, b_scale in (("fp64", "fp64", False, 1.0),
                                          ("mixed", "mixed", False, 1.0),
                                          ("mixed_learned", "mixed", True, 1.0),
                                          ("mixed_scaled_divergence", "mixed", False, tau)):
+        if name not in wanted or (learned and net is None):
+            continue
         kw = dict(precision=prec, restart=20, maxit=100, res_norm_min=1e-300, red_factor=1e-8,
                   red_initial=1)
         try:
@@ -579,7 +599,9 @@ def channel_run(args, threads, net):
         out[name] = {k: mean(k) for k in ("step_ms", "assembly_ms", "factor_ms", "solve_ms",
                                            "iterations")}
         out[name]["max_reduction"] = max(r["reduction"] for r in rows)
+        out[name]["s_timed_steps"] = sum(r["step_ms"] for r in rows) / 1e3
         out[name]["s_per_200_steps"] = mean("step_ms") * 200 / 1e3
+        out[name]["s_per_200_steps_measured"] = len(rows) >= 200
         if learned:
             out[name]["learned_status"] = S.learned_status()
         umax = float(d_u[:n3].abs().max())
@@ -635,7 +657,8 @@ def only_sweep(args):
     import numpy as np
     from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
     P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed, nthreads=os.cpu_count() or 1)
-    S = PmSolver(P.descs, precision=args.only_sweep, decouple=args.decouple)
+    S = PmSolver(P.descs, precision=args.only_sweep, decouple=args.decouple,
+                 residual_variant=args.residual_variant)
     L = P.n_levels
     rng = np.random.default_rng(0)
     u = 0.1 * rng.standard_normal(P.ndof(L - 1))
@@ -650,6 +673,7 @@ def only_sweep(args):
     prof = S.profile_read()
     S.profile(False)
     out = {"only_sweep": args.only_sweep, "levels": L, "decoupled": S.level_decoupled(L - 1),
+           "residual_kernel": S._lib.pm_level_variant(S._h, L - 1) % 3,
            "cells": P.desc(L - 1).n_cells, "kernel_launches_per_sweep": launches}
     for k, v in prof.items():
         out[k] = {"ms_per_sweep": v["ms"] / args.steps, "launches": v["launches"],
@@ -854,6 +878,12 @@ def main():
     if args.only_sweep:
         only_sweep(args)
         return
+    if args.only_channel:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"only_channel": channel_run(args, os.cpu_count() or 1, None)}),
+              flush=True)
+        return
     if args.only_mlp > 0:
         only_mlp(args)
         return
@@ -907,6 +937,8 @@ def main():
     # how the finest level runs per variant: 0 nine blocks + 85x85 LU, 1
     # three diagonal blocks, 2 one block (A11 = A22 = A33)
     modes = {k: S.level_decoupled(args.levels - 1) for k, S in solvers.items()}
+    res_variants = {k: S._lib.pm_level_variant(S._h, args.levels - 1) % 3
+                    for k, S in solvers.items()}
     # the same system as NSTYPE-2 levels (one velocity block; the Galerkin
     # Oseen form has A12..A32 = 0 and A11 = A22 = A33), smoothed by the exact
     # block solve of the cell systems: reported beside the headline
@@ -967,6 +999,9 @@ def main():
             S.profile(False)
         if prec == "mixed_learned":
             results[prec]["learned"] = S.learned_status()
+        # variants the later legs do not use give their device memory back
+        if prec in ("fp64", "fp64_lu", "mixed_lu", "fp64_one_block"):
+            S.close()
 
     # reduce: max over ranks
     ms = max_over_ranks(results["mixed_learned"]["ms"], world)
@@ -1049,7 +1084,7 @@ def main():
     a_ach, a_ms, a_bytes = kernel_roof(prof.get("apply"))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(P),
-            "kernel": RESIDUAL_KERNEL[modes["mixed"]],
+            "kernel": residual_kernel_name(modes["mixed"], res_variants["mixed"]),
             "peak_kind": peak_kind, "avg_launch_ms": avg_ms, "bytes_per_launch": per_launch,
             "apply_kernel": {"name": APPLY_KERNEL[modes["mixed"]],
                              "achieved": a_ach, "frac": (a_ach / peak) if a_ach else None,

@@ -112,13 +112,13 @@ def test_kernel_variants(P, oracle, variant, precision):
 @pytest.mark.parametrize("decouple", [1, 0])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_default_kernels(P, precision, decouple):
-    """The per-level defaults: the cell store on decoupled levels in both
-    precisions; with nine blocks, the flattened stream in FP32 and row
-    groups in FP64; LU apply (where the level keeps the LU) one cell per
-    warp in FP32, two cells per warp in FP64."""
+    """The per-level defaults: in FP32 the cell store on decoupled levels
+    and the flattened stream with nine blocks; row groups in FP64; LU apply
+    (where the level keeps the LU) one cell per warp in FP32, two cells per
+    warp in FP64."""
     from to_merge_master_parmoon_gb300 import PmSolver
     S = PmSolver(P.descs, precision=precision, decouple=decouple)
-    res = 2 if decouple else (1 if precision == "mixed" else 0)
+    res = (2 if decouple else 1) if precision == "mixed" else 0
     want = res + 3 * (2 if precision == "mixed" else 0)
     assert [S._lib.pm_level_variant(S._h, l) for l in range(1, 3)] == [want, want]
     S.close()

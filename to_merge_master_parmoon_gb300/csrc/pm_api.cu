@@ -906,8 +906,10 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
   // full solve, with the L2 prefetch of the columns)
   // kernel index: 0 row groups, 1 flattened stream, 2 cell store (levels
   // without velocity coupling: Q2 hexahedra, decoupled or one-block)
-  const int rule_res = Lv.store_ok() ? 2
-                       : (sizeof(T) == sizeof(float) && !Lv.structured && !Lv.diag) ? 1 : 0;
+  // (the cell store in FP32 only: in FP64 its per-step segmented sums add
+  // FP64 work to a kernel the FP64 pipe already bounds)
+  const bool f32 = sizeof(T) == sizeof(float);
+  const int rule_res = (f32 && Lv.store_ok()) ? 2 : (f32 && !Lv.structured && !Lv.diag) ? 1 : 0;
   const int ro = h->opt.residual_variant;
   Lv.res_variant = ro == 0 ? rule_res
                    : ro == 1 ? 0
@@ -1303,9 +1305,11 @@ pm_status pm_create(pm_handle **out, const pm_options *opt) {
   if (o.precision != PM_PREC_FP64 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.factor_fp32 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.pre_smooth < 0 || o.post_smooth < 0 || o.restart <= 0 || o.maxit <= 0) return PM_BADARG;
-  if (o.residual_variant < -1 || o.residual_variant > 2) return PM_BADARG;
+  if (o.residual_variant < -1 || o.residual_variant > 3) return PM_BADARG;
   if (o.apply_variant < -1 || o.apply_variant > 2) return PM_BADARG;
   if (o.upload_mode < 0 || o.upload_mode > 1) return PM_BADARG;
+  if (o.decouple < 0 || o.decouple > 1 || o.wait_limit < 0 || o.max_device_bytes < 0)
+    return PM_BADARG;
   if (pm_device_count() <= 0) return PM_NO_DEVICE;
   if (cudaSetDevice(o.device) != cudaSuccess) {
     cudaGetLastError();

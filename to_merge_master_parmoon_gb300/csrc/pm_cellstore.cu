@@ -82,19 +82,21 @@ __device__ __forceinline__ void seg_add(int seg, T (&v)[NO], T *acc, int stride,
 
 // One warp per cell.  KIND 0: A groups (NVA values, gather u1, u2, u3, three
 // outputs); 1: BT groups (three values, gather p, three outputs); 2: B
-// groups (three values, gather u1, u2, u3, one output).
+// groups (three values, gather u1, u2, u3, one output).  Software-pipelined:
+// the loads of the next 32 x UR groups are issued before the gathers, the
+// products and the segmented sums of the current ones, so one memory round
+// trip overlaps the other work of a step.
 template <typename T, int KIND, int NVA, int UR>
-__device__ __forceinline__ void stream_groups(const int *__restrict__ col,
-                                              const unsigned char *__restrict__ rid,
-                                              const T *const *vals, long long g0, int ng,
-                                              const T *__restrict__ x0, const T *__restrict__ x1,
-                                              const T *__restrict__ x2, T *acc, int lane) {
-  constexpr int VEC = Vec<T>::n;
-  constexpr int NV = KIND == 0 ? NVA : 3;
-  constexpr int NO = KIND == 2 ? 1 : 3;
-  for (int b = 0; b < ng; b += 32 * UR) {
-    int c[UR][VEC], seg[UR];
-    T v[UR][NV][VEC];
+struct Groups {
+  static constexpr int VEC = Vec<T>::n;
+  static constexpr int NV = KIND == 0 ? NVA : 3;
+  int c[UR][VEC], seg[UR];
+  T v[UR][NV][VEC];
+
+  __device__ __forceinline__ void load(const int *__restrict__ col,
+                                       const unsigned char *__restrict__ rid,
+                                       const T *const *vals, long long g0, int ng, int b,
+                                       int lane) {
 #pragma unroll
     for (int q = 0; q < UR; ++q) {
       const int g = b + q * 32 + lane;
@@ -107,38 +109,56 @@ __device__ __forceinline__ void stream_groups(const int *__restrict__ col,
         for (int k = 0; k < NV; ++k) Vec<T>::ld(vals[k] + e, v[q][k]);
       }
     }
+  }
+};
+
+template <typename T, int KIND, int NVA, int UR>
+__device__ __forceinline__ void stream_groups(const int *__restrict__ col,
+                                              const unsigned char *__restrict__ rid,
+                                              const T *const *vals, long long g0, int ng,
+                                              const T *__restrict__ x0, const T *__restrict__ x1,
+                                              const T *__restrict__ x2, T *acc, int lane) {
+  constexpr int VEC = Vec<T>::n;
+  constexpr int NV = KIND == 0 ? NVA : 3;
+  constexpr int NO = KIND == 2 ? 1 : 3;
+  if (ng <= 0) return;
+  Groups<T, KIND, NVA, UR> cur, nxt;
+  nxt.load(col, rid, vals, g0, ng, 0, lane);
+  for (int b = 0; b < ng; b += 32 * UR) {
+    cur = nxt;
+    if (b + 32 * UR < ng) nxt.load(col, rid, vals, g0, ng, b + 32 * UR, lane);
 #pragma unroll
     for (int q = 0; q < UR; ++q) {
       T s[NO];
 #pragma unroll
       for (int k = 0; k < NO; ++k) s[k] = T(0);
-      if (seg[q] >= 0) {
+      if (cur.seg[q] >= 0) {
 #pragma unroll
         for (int m = 0; m < VEC; ++m) {
-          const int cc = c[q][m];
+          const int cc = cur.c[q][m];
           if constexpr (KIND == 0) {
             if constexpr (NVA == 1) {
-              const T a = v[q][0][m];
+              const T a = cur.v[q][0][m];
               s[0] += a * __ldg(x0 + cc);
               s[1 % NO] += a * __ldg(x1 + cc);
               s[2 % NO] += a * __ldg(x2 + cc);
             } else {
-              s[0] += v[q][0][m] * __ldg(x0 + cc);
-              s[1 % NO] += v[q][1 % NV][m] * __ldg(x1 + cc);
-              s[2 % NO] += v[q][2 % NV][m] * __ldg(x2 + cc);
+              s[0] += cur.v[q][0][m] * __ldg(x0 + cc);
+              s[1 % NO] += cur.v[q][1 % NV][m] * __ldg(x1 + cc);
+              s[2 % NO] += cur.v[q][2 % NV][m] * __ldg(x2 + cc);
             }
           } else if constexpr (KIND == 1) {
             const T pc = __ldg(x0 + cc);
-            s[0] += v[q][0][m] * pc;
-            s[1 % NO] += v[q][1][m] * pc;
-            s[2 % NO] += v[q][2][m] * pc;
+            s[0] += cur.v[q][0][m] * pc;
+            s[1 % NO] += cur.v[q][1][m] * pc;
+            s[2 % NO] += cur.v[q][2][m] * pc;
           } else {
-            s[0] += v[q][0][m] * __ldg(x0 + cc) + v[q][1][m] * __ldg(x1 + cc) +
-                    v[q][2][m] * __ldg(x2 + cc);
+            s[0] += cur.v[q][0][m] * __ldg(x0 + cc) + cur.v[q][1][m] * __ldg(x1 + cc) +
+                    cur.v[q][2][m] * __ldg(x2 + cc);
           }
         }
       }
-      seg_add<T, NO>(seg[q], s, acc, NU_LOC, lane);
+      seg_add<T, NO>(cur.seg[q], s, acc, NU_LOC, lane);
     }
   }
 }
@@ -159,8 +179,7 @@ __global__ void __launch_bounds__(kCsWarps * 32) k_vanka_residual_cells(
   const T *u1 = u, *u2 = u + nu, *u3 = u + 2 * (size_t)nu, *p = u + 3 * (size_t)nu;
   const int nA = cs.cnt[3 * s], nBT = cs.cnt[3 * s + 1], nB = cs.cnt[3 * s + 2];
   const long long gA = cs.offA[s], gP = cs.offP[s];
-  constexpr int UR = sizeof(T) == 4 ? 2 : 2;
-  stream_groups<T, 0, NVA, UR>(cs.colA, cs.ridA, cs.a, gA, nA, u1, u2, u3, acc, lane);
+  stream_groups<T, 0, NVA, 2>(cs.colA, cs.ridA, cs.a, gA, nA, u1, u2, u3, acc, lane);
   stream_groups<T, 1, NVA, 1>(cs.colP, cs.ridP, cs.p, gP, nBT, p, p, p, acc, lane);
   stream_groups<T, 2, NVA, 1>(cs.colP, cs.ridP, cs.p, gP + nBT, nB, u1, u2, u3,
                               acc + 3 * NU_LOC, lane);

@@ -175,10 +175,16 @@ __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double
       __syncwarp();
       for (int c = k + 1 + lane; c < GW; c += 32) M[k * MS + c] *= rp;
       __syncwarp();
+      // row updates; a zero entry of the pivot row changes nothing, and
+      // most of the identity block's entries still are zero at step k, so
+      // they are skipped (the branch is the same for every lane)
       if (lane < NU_LOC && lane != k) {
         const double f = my[k];
         if (f != 0.0)
-          for (int c = k + 1; c < GW; ++c) my[c] -= f * M[k * MS + c];
+          for (int c = k + 1; c < GW; ++c) {
+            const double pk = M[k * MS + c];
+            if (pk != 0.0) my[c] -= f * pk;
+          }
       }
       __syncwarp();
     }
@@ -290,17 +296,33 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_schur_apply(
   const T r0 = vr ? R[lane] : T(0), r1 = vr ? R[NU_LOC + lane] : T(0),
           r2 = vr ? R[2 * NU_LOC + lane] : T(0);
   const T *F = factors + (size_t)cell * L::stride;
+  // every load of the cell's block is issued before the arithmetic needs
+  // it (one memory round trip per cell where the registers allow: all of
+  // A^{-1}, D and W for one block; D and W up front for three blocks)
+  T Dv[NP_LOC][3], Wv[NP_LOC][3];
+#pragma unroll
+  for (int k = 0; k < NP_LOC; ++k)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      Dv[k][c] = vr ? __ldcs(F + L::offD + (k * 3 + c) * NU_LOC + lane) : T(0);
+      Wv[k][c] = vr ? __ldcs(F + L::offW + (k * 3 + c) * NU_LOC + lane) : T(0);
+    }
   // y_c = A_c^{-1} r_c
   T y0 = 0, y1 = 0, y2 = 0;
+  if constexpr (NB == 1) {
+    T a[NU_LOC];
+#pragma unroll
+    for (int j = 0; j < NU_LOC; ++j) a[j] = vr ? __ldcs(F + j * NU_LOC + lane) : T(0);
+#pragma unroll
+    for (int j = 0; j < NU_LOC; ++j) {
+      y0 += a[j] * __shfl_sync(kFull, r0, j);
+      y1 += a[j] * __shfl_sync(kFull, r1, j);
+      y2 += a[j] * __shfl_sync(kFull, r2, j);
+    }
+  } else {
 #pragma unroll 9
-  for (int j = 0; j < NU_LOC; ++j) {
-    const T *Fj = F + j * NU_LOC + lane;
-    if constexpr (NB == 1) {
-      const T a = vr ? __ldcs(Fj) : T(0);
-      y0 += a * __shfl_sync(kFull, r0, j);
-      y1 += a * __shfl_sync(kFull, r1, j);
-      y2 += a * __shfl_sync(kFull, r2, j);
-    } else {
+    for (int j = 0; j < NU_LOC; ++j) {
+      const T *Fj = F + j * NU_LOC + lane;
       const T a0 = vr ? __ldcs(Fj) : T(0), a1 = vr ? __ldcs(Fj + B1) : T(0),
               a2 = vr ? __ldcs(Fj + 2 * B1) : T(0);
       y0 += a0 * __shfl_sync(kFull, r0, j);
@@ -311,14 +333,8 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_schur_apply(
   // t = r_p - sum_c D_c y_c
   T t[NP_LOC];
 #pragma unroll
-  for (int k = 0; k < NP_LOC; ++k) {
-    const T *Dk = F + L::offD + k * 3 * NU_LOC;
-    T part = T(0);
-    if (vr)
-      part = __ldcs(Dk + lane) * y0 + __ldcs(Dk + NU_LOC + lane) * y1 +
-             __ldcs(Dk + 2 * NU_LOC + lane) * y2;
-    t[k] = R[3 * NU_LOC + k] - warp_sum(part);
-  }
+  for (int k = 0; k < NP_LOC; ++k)
+    t[k] = R[3 * NU_LOC + k] - warp_sum(Dv[k][0] * y0 + Dv[k][1] * y1 + Dv[k][2] * y2);
   // p = S^{-1} t (column-major S^{-1}, loaded by every lane)
   T p[NP_LOC];
 #pragma unroll
@@ -331,10 +347,9 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_schur_apply(
   if (vr) {
 #pragma unroll
     for (int k = 0; k < NP_LOC; ++k) {
-      const T *Wk = F + L::offW + k * 3 * NU_LOC;
-      y0 -= __ldcs(Wk + lane) * p[k];
-      y1 -= __ldcs(Wk + NU_LOC + lane) * p[k];
-      y2 -= __ldcs(Wk + 2 * NU_LOC + lane) * p[k];
+      y0 -= Wv[k][0] * p[k];
+      y1 -= Wv[k][1] * p[k];
+      y2 -= Wv[k][2] * p[k];
     }
     const int d = cells.udofs[(size_t)cell * NU_LOC + lane];
     u[d] += damp * y0;
