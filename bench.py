@@ -192,12 +192,8 @@ RESIDUAL_DRAM_BYTES_PER_CELL = None
 def residual_kernel_name(mode, variant):
     """The FP32 local-residual kernel a level runs: level mode (0 nine blocks
     + LU, 1 three diagonal blocks, 2 one block A11 = A22 = A33) and residual
-    kernel (0 row groups, 1 flattened stream, 2 cell store)."""
+    kernel (0 row groups, 1 flattened stream)."""
     blocks = {0: "nine A blocks", 1: "A11, A22, A33", 2: "one A block (A11 = A22 = A33)"}[mode]
-    if variant == 2:
-        return (f"k_vanka_residual_cells<float,{1 if mode == 2 else 3}> (cell-local residuals "
-                f"from the per-cell row store of one colour, vector loads, segmented warp sums; "
-                f"{blocks}, BT, B)")
     if variant == 1:
         return ("k_vanka_residual<float,4,1> (cell-local residuals over full CSR rows of one "
                 f"colour, flattened entry stream; {blocks}, BT, B)")
@@ -673,7 +669,7 @@ def only_sweep(args):
     prof = S.profile_read()
     S.profile(False)
     out = {"only_sweep": args.only_sweep, "levels": L, "decoupled": S.level_decoupled(L - 1),
-           "residual_kernel": S._lib.pm_level_variant(S._h, L - 1) % 3,
+           "residual_kernel": S._lib.pm_level_variant(S._h, L - 1) % 2,
            "cells": P.desc(L - 1).n_cells, "kernel_launches_per_sweep": launches}
     for k, v in prof.items():
         out[k] = {"ms_per_sweep": v["ms"] / args.steps, "launches": v["launches"],
@@ -937,7 +933,7 @@ def main():
     # how the finest level runs per variant: 0 nine blocks + 85x85 LU, 1
     # three diagonal blocks, 2 one block (A11 = A22 = A33)
     modes = {k: S.level_decoupled(args.levels - 1) for k, S in solvers.items()}
-    res_variants = {k: S._lib.pm_level_variant(S._h, args.levels - 1) % 3
+    res_variants = {k: S._lib.pm_level_variant(S._h, args.levels - 1) % 2
                     for k, S in solvers.items()}
     # the same system as NSTYPE-2 levels (one velocity block; the Galerkin
     # Oseen form has A12..A32 = 0 and A11 = A22 = A33), smoothed by the exact

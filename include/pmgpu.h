@@ -99,17 +99,13 @@ typedef struct {
                              sweep applies it as a GEMV; 0 (default) keeps
                              the FP32 LU factors and substitution            */
   int residual_variant;   /* local-residual kernel of the Vanka sweep:
-                             0 (default) per level: the cell store on Q2
-                             levels without velocity coupling (each cell's
-                             rows copied contiguously in colour order at
-                             every refactorisation, streamed with vector
-                             loads), else row groups (8 lanes per CSR row),
-                             except the flattened entry stream with
-                             segmented sums on FP32 nine-block levels (faster
-                             there); 1 row groups everywhere; 2 the stream
-                             everywhere; 3 the cell store where a level
-                             allows it (else the default); -1 time them on
-                             every level at pm_setup and keep the fastest   */
+                             0 (default) per level: row groups (8 lanes per
+                             CSR row), except the flattened entry stream with
+                             segmented sums on FP32 levels that read all
+                             nine A blocks (faster there); 1 row groups
+                             everywhere; 2 the stream everywhere; -1 time
+                             both on every level at pm_setup and keep the
+                             faster                                          */
   int apply_variant;      /* LU apply of nine-block levels, factor columns
                              loaded from HBM with register and L2 prefetch:
                              0 (default) per level: two cells per warp (half a
@@ -119,8 +115,8 @@ typedef struct {
                              staged in shared memory by bulk copies; 2 one
                              cell per warp; -1 time them per level at
                              pm_setup.  pm_level_variant reports residual
-                             kernel (0 rows, 1 stream, 2 cell store) + 3 *
-                             apply kernel (0 pairs, 1 bulk, 2 single)        */
+                             kernel (0 rows, 1 stream) + 2 * apply kernel
+                             (0 pairs, 1 bulk, 2 single)                     */
   int upload_mode;        /* how pm_add_level / pm_update_matrices move matrix
                              values: 0 (default) copy-engine copies
                              (cudaMemcpyAsync) then device conversions; 1 the
@@ -261,10 +257,10 @@ int       pm_level_blocks(pm_handle *h, int level);
  * inverse per cell (the one-block operator's kernels).  0 for one-block
  * descriptors, -1 if no such level. */
 int       pm_level_decoupled(pm_handle *h, int level);
-/* kernels a level runs: residual kernel (0 row groups, 1 stream, 2 cell
- * store) + 3 * LU apply kernel (0 two cells per warp, 1 bulk-staged, 2 one
- * cell per warp; levels without velocity coupling apply their block
- * elimination instead); -1 if no such level */
+/* kernels a level runs: residual kernel (0 row groups, 1 stream) + 2 * LU
+ * apply kernel (0 two cells per warp, 1 bulk-staged, 2 one cell per warp;
+ * levels without velocity coupling apply their block elimination instead);
+ * -1 if no such level */
 int       pm_level_variant(pm_handle *h, int level);
 
 /* Level operators (FP64 on host vectors of length ndof(level)). */

@@ -162,21 +162,21 @@ def test_coupled_blocks_keep_the_lu_and_update_switches():
     S.close()
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, -1])
+@pytest.mark.parametrize("variant", [1, 2, -1])
 @pytest.mark.parametrize("mode", [2, 1])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_residual_kernels_on_decoupled_levels(precision, mode, variant):
     """Every local-residual kernel on decoupled levels (1 row groups, 2
-    flattened stream, 3 the cell store, -1 the tuner's choice) gives the
-    oracle's sweeps; mode 2 reads one A block, mode 1 three."""
+    flattened stream, -1 the tuner's choice) gives the oracle's sweeps;
+    mode 2 reads one A block, mode 1 three."""
     from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
     P = OseenProblem(n_levels=3, nu=1e-2, seed=6)
     if mode == 1:
         distinct_diagonal(P)
     S = PmSolver(P.descs, precision=precision, residual_variant=variant)
     assert [S.level_decoupled(l) for l in range(3)] == [mode] * 3
-    res = [S._lib.pm_level_variant(S._h, l) % 3 for l in (1, 2)]
-    if variant in (1, 2, 3):
+    res = [S._lib.pm_level_variant(S._h, l) % 2 for l in (1, 2)]
+    if variant in (1, 2):
         assert res == [variant - 1] * 2
     O = Oracle(P)
     rng = np.random.default_rng(9)

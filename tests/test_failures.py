@@ -107,7 +107,7 @@ def test_bulk_copy_wait_limit_gives_pm_timeout(problems):
     from to_merge_master_parmoon_gb300 import PmError, PmSolver
     P = problems(3, 1e-2, 0)
     S = PmSolver(P.descs, precision="mixed", decouple=0, apply_variant=1, wait_limit=1)
-    assert S._lib.pm_level_variant(S._h, 2) // 3 == 1  # the bulk-copy apply
+    assert S._lib.pm_level_variant(S._h, 2) // 2 == 1  # the bulk-copy apply
     rng = np.random.default_rng(1)
     u, f = 0.1 * rng.standard_normal(P.ndof(2)), rng.standard_normal(P.ndof(2))
     with pytest.raises(PmError) as e:

@@ -97,12 +97,12 @@ def test_kernel_variants(P, oracle, variant, precision):
     S = PmSolver(P.descs, precision=precision, residual_variant=variant, apply_variant=variant,
                  decouple=0)
     chosen = [S._lib.pm_level_variant(S._h, l) for l in range(3)]
-    assert all(0 <= v <= 8 for v in chosen)
-    bulk = 3 if precision == "mixed" else 0  # the bulk-staged apply is FP32 only
+    assert all(0 <= v <= 5 for v in chosen)
+    bulk = 2 if precision == "mixed" else 0  # the bulk-staged apply is FP32 only
     if variant == 1:
         assert chosen[1:] == [bulk, bulk]  # row groups, bulk-staged (FP32) or two cells per warp
     if variant == 2:
-        assert chosen[1:] == [7, 7]  # flattened stream, one cell per warp
+        assert chosen[1:] == [5, 5]  # flattened stream, one cell per warp
     tol = 1e-9 if precision == "fp64" else 5e-4
     for level in (1, 2):
         u, f = 0.1 * rand(P, level, 6), rand(P, level, 7)
@@ -112,14 +112,14 @@ def test_kernel_variants(P, oracle, variant, precision):
 @pytest.mark.parametrize("decouple", [1, 0])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_default_kernels(P, precision, decouple):
-    """The per-level defaults: in FP32 the cell store on decoupled levels
-    and the flattened stream with nine blocks; row groups in FP64; LU apply
-    (where the level keeps the LU) one cell per warp in FP32, two cells per
-    warp in FP64."""
+    """The per-level defaults: row groups on decoupled levels in both
+    precisions; with nine blocks, the flattened stream in FP32 and row
+    groups in FP64; LU apply (where the level keeps the LU) one cell per
+    warp in FP32, two cells per warp in FP64."""
     from to_merge_master_parmoon_gb300 import PmSolver
     S = PmSolver(P.descs, precision=precision, decouple=decouple)
-    res = (2 if decouple else 1) if precision == "mixed" else 0
-    want = res + 3 * (2 if precision == "mixed" else 0)
+    res = 1 if (precision == "mixed" and not decouple) else 0
+    want = res + 2 * (2 if precision == "mixed" else 0)
     assert [S._lib.pm_level_variant(S._h, l) for l in range(1, 3)] == [want, want]
     S.close()
 

@@ -30,7 +30,7 @@ GXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", f"-I{INCLUDE}", f"-I{CSRC
 
 GPU_CU = ["pm_api.cu", "pm_sparse.cu", "pm_vanka.cu", "pm_vanka_schur.cu", "pm_vanka_tma.cu",
           "pm_learned.cu", "pm_mlp_tc.cu", "pm_assemble.cu",
-          "pm_noalloc.cu", "pm_diag.cu", "pm_cellstore.cu"]
+          "pm_noalloc.cu", "pm_diag.cu"]
 GPU_CPP = ["pm_setup_host.cpp"]
 HOST_CPP = ["oseen_problem.cpp", "oseen_tet.cpp"]
 HEADERS = [INCLUDE / "pmgpu.h", CSRC / "pm_kernels.h", CSRC / "pm_setup_host.h",

@@ -111,35 +111,6 @@ struct LevelDev {
   bool schur3() const { return diag == 1 && nl == NU_LOC; }
   size_t fac_bytes = 0;  // allocated factor storage
   uint64_t pattern_key = 0;  // fingerprint of the CSR patterns (pattern_fingerprint)
-  // row pointers on the host (layout of the cell store)
-  std::vector<int> h_a_rowptr, h_b_rowptr, h_bt_rowptr;
-  // cell store of the local residual (decoupled Q2 levels, residual kernel 2)
-  long long *cs_offA = nullptr, *cs_offP = nullptr;
-  int *cs_cnt = nullptr, *cs_colA = nullptr, *cs_colP = nullptr;
-  unsigned char *cs_ridA = nullptr, *cs_ridP = nullptr;
-  void *cs_a[3] = {}, *cs_p[3] = {};
-  long long cs_groupsA = 0, cs_groupsP = 0;
-  int cs_nva = 0;             // A value arrays allocated (1 or 3)
-  bool cs_pattern = false;    // columns and row ids written
-  // a level that can run the cell-store residual
-  bool store_ok() const { return nl == NU_LOC && ncells > 0 && (one_block() || diag == 1); }
-  template <typename T>
-  CellStore<T> cell_store() const {
-    CellStore<T> c;
-    c.nva = one_block() ? 1 : 3;
-    c.offA = cs_offA;
-    c.offP = cs_offP;
-    c.cnt = cs_cnt;
-    c.ridA = cs_ridA;
-    c.ridP = cs_ridP;
-    c.colA = cs_colA;
-    c.colP = cs_colP;
-    for (int k = 0; k < 3; ++k) {
-      c.a[k] = static_cast<const T *>(cs_a[k]);
-      c.p[k] = static_cast<const T *>(cs_p[k]);
-    }
-    return c;
-  }
 };
 template <>
 DevOp<double> LevelDev::op<double>() const {
@@ -380,13 +351,8 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
       h->evused += 3;
       cudaEventRecord(e0, h->stream);
     }
-    if (Lv.res_variant == 2)
-      PM_LAUNCH(launch_vanka_residual_cells<T>(Lv.cell_store<T>(), cells, Lv.nu, b,
-                                               Lv.colour_cells + b, n, u, rhs,
-                                               static_cast<T *>(Lv.dbuf), h->stream));
-    else
-      PM_LAUNCH(launch_vanka_residual<T>(op, cells, Lv.colour_cells + b, n, u, rhs,
-                                         static_cast<T *>(Lv.dbuf), Lv.res_variant, h->stream));
+    PM_LAUNCH(launch_vanka_residual<T>(op, cells, Lv.colour_cells + b, n, u, rhs,
+                                       static_cast<T *>(Lv.dbuf), Lv.res_variant, h->stream));
     if (e1) cudaEventRecord(e1, h->stream);
     if (Lv.schur())
       PM_LAUNCH(launch_schur_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
@@ -786,53 +752,6 @@ pm_status ensure_factors(pm_handle *h, LevelDev &Lv) {
   return PM_OK;
 }
 
-// The cell store of a level that runs the cell-store residual: layout and
-// pattern once (from the host row pointers and the colour order), value
-// arrays as the level's mode needs (A: 1 or 3), values from the FP64 CSR
-// on every call (pm_setup, and every refactorisation, since the values may
-// have changed).
-pm_status fill_cell_store(pm_handle *h, LevelDev &Lv) {
-  if (Lv.res_variant != 2 || !Lv.store_ok()) return PM_OK;
-  const bool f32 = mixed(h);
-  const size_t es = f32 ? sizeof(float) : sizeof(double);
-  const int vec = f32 ? cell_store_vec<float>() : cell_store_vec<double>();
-  if (!Lv.cs_offA) {
-    const int n = Lv.ncells;
-    std::vector<long long> offA(n + 1), offP(n + 1);
-    std::vector<int> cnt(3 * (size_t)n);
-    cell_store_layout(n, Lv.colouring.order.data(), Lv.h_udofs.data(), Lv.h_pdofs.data(), Lv.nact,
-                      Lv.h_a_rowptr.data(), Lv.h_b_rowptr.data(), Lv.h_bt_rowptr.data(), vec,
-                      offA.data(), offP.data(), cnt.data());
-    Lv.cs_groupsA = offA[n];
-    Lv.cs_groupsP = offP[n];
-    PM_TRY(upload(h, &Lv.cs_offA, offA.data(), offA.size()));
-    PM_TRY(upload(h, &Lv.cs_offP, offP.data(), offP.size()));
-    PM_TRY(upload(h, &Lv.cs_cnt, cnt.data(), cnt.size()));
-    PM_TRY(dalloc(h, &Lv.cs_ridA, (size_t)Lv.cs_groupsA));
-    PM_TRY(dalloc(h, &Lv.cs_ridP, (size_t)Lv.cs_groupsP));
-    PM_TRY(dalloc(h, &Lv.cs_colA, (size_t)Lv.cs_groupsA * vec));
-    PM_TRY(dalloc(h, &Lv.cs_colP, (size_t)Lv.cs_groupsP * vec));
-    for (int k = 0; k < 3; ++k)
-      PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.cs_p[k]),
-                    (size_t)Lv.cs_groupsP * vec * es));
-  }
-  const int nva = Lv.one_block() ? 1 : 3;
-  for (int k = Lv.cs_nva; k < nva; ++k)
-    PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.cs_a[k]),
-                  (size_t)Lv.cs_groupsA * vec * es));
-  Lv.cs_nva = std::max(Lv.cs_nva, nva);
-  if (f32)
-    PM_LAUNCH(launch_cell_store_fill<float>(Lv.cell_store<float>(), Lv.op<double>(), Lv.cells(),
-                                            Lv.colour_cells, Lv.ncells, !Lv.cs_pattern,
-                                            h->stream));
-  else
-    PM_LAUNCH(launch_cell_store_fill<double>(Lv.cell_store<double>(), Lv.op<double>(), Lv.cells(),
-                                             Lv.colour_cells, Lv.ncells, !Lv.cs_pattern,
-                                             h->stream));
-  Lv.cs_pattern = true;
-  return PM_OK;
-}
-
 // Unique bytes of one sweep per cell (each stored element counted once):
 // residual kernel = matrix values (the A arrays the level reads: 9, 3 when
 // decoupled, 1 for one-block levels) + column indices + row pointers, u and
@@ -904,17 +823,10 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
   // 1087 ms FP64); LU apply with two cells per warp in FP64 (the FP64 chain
   // is the bound), one cell per warp in FP32 (each measured faster in the
   // full solve, with the L2 prefetch of the columns)
-  // kernel index: 0 row groups, 1 flattened stream, 2 cell store (levels
-  // without velocity coupling: Q2 hexahedra, decoupled or one-block)
-  // (the cell store in FP32 only: in FP64 its per-step segmented sums add
-  // FP64 work to a kernel the FP64 pipe already bounds)
-  const bool f32 = sizeof(T) == sizeof(float);
-  const int rule_res = (f32 && Lv.store_ok()) ? 2 : (f32 && !Lv.structured && !Lv.diag) ? 1 : 0;
+  // kernel index: 0 row groups, 1 flattened stream
+  const int rule_res = (sizeof(T) == sizeof(float) && !Lv.structured && !Lv.diag) ? 1 : 0;
   const int ro = h->opt.residual_variant;
-  Lv.res_variant = ro == 0 ? rule_res
-                   : ro == 1 ? 0
-                   : ro == 2 ? 1
-                   : (ro == 3 && Lv.store_ok()) ? 2 : rule_res;
+  Lv.res_variant = ro == 0 ? rule_res : (ro == 2 ? 1 : 0);
   const bool can_bulk = sizeof(T) == sizeof(float) && !use_inverse(h) && !Lv.structured &&
                         Lv.diag == 0 && Lv.nl == NU_LOC;
   const int ao = h->opt.apply_variant;
@@ -954,27 +866,13 @@ pm_status tune_level(pm_handle *h, LevelDev &Lv) {
   };
   pm_status st = PM_OK;
   if (tune_res) {
-    float t[3] = {0.f, 0.f, 1e30f};
+    float t[2] = {0.f, 0.f};
     for (int v = 0; v < 2 && st == PM_OK; ++v)
       st = time_it([&] {
         return launch_vanka_residual<T>(op, Lv.cells(), list, nb, u,
                                         static_cast<const T *>(Lv.rhs), rb, v, h->stream);
       }, t[v]);
-    if (Lv.store_ok() && st == PM_OK) {
-      Lv.res_variant = 2;
-      st = fill_cell_store(h, Lv);
-      const int slot0 = Lv.colouring.ptr[kb];
-      if (st == PM_OK)
-        st = time_it([&] {
-          return launch_vanka_residual_cells<T>(Lv.cell_store<T>(), Lv.cells(), Lv.nu, slot0,
-                                                list, nb, u, static_cast<const T *>(Lv.rhs), rb,
-                                                h->stream);
-        }, t[2]);
-    }
-    int best = 0;
-    for (int v = 1; v < 3; ++v)
-      if (t[v] < t[best]) best = v;
-    Lv.res_variant = best;  // kernel index: 0 row groups, 1 stream, 2 cell store
+    Lv.res_variant = t[1] < t[0] ? 1 : 0;  // kernel index: 0 row groups, 1 stream
   }
   if (tune_apply && st == PM_OK) {
     // kernel index: 0 two cells per warp, 1 bulk-staged (FP32 only), 2 one cell per warp
@@ -1023,7 +921,6 @@ pm_status refresh_modes(pm_handle *h, int only = -1) {
       PM_TRY(tune_level<float>(h, Lv));
     else
       PM_TRY(tune_level<double>(h, Lv));
-    PM_TRY(fill_cell_store(h, Lv));
   }
   return PM_OK;
 }
@@ -1062,8 +959,6 @@ pm_status factor_all(pm_handle *h) {
       PM_LAUNCH(launch_vanka_factor<double>(Lv.op<double>(), Lv.cells(), static_cast<double *>(Lv.factors),
                                             Lv.perm, false, false, h->status_d, h->stream));
   }
-  // the cell stores hold copies of the level matrices: refresh their values
-  for (size_t l = 1; l < h->L.size(); ++l) PM_TRY(fill_cell_store(h, h->L[l]));
   LevelDev &C = h->L[0];
   PM_LAUNCH(launch_coarse_assemble(C.op<double>(), h->coarse_lu, h->opt.project_pressure, h->stream));
   PM_LAUNCH(launch_dense_lu(h->coarse_lu, h->coarse_n, h->coarse_ipiv, h->status_d, h->stream));
@@ -1305,7 +1200,7 @@ pm_status pm_create(pm_handle **out, const pm_options *opt) {
   if (o.precision != PM_PREC_FP64 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.factor_fp32 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.pre_smooth < 0 || o.post_smooth < 0 || o.restart <= 0 || o.maxit <= 0) return PM_BADARG;
-  if (o.residual_variant < -1 || o.residual_variant > 3) return PM_BADARG;
+  if (o.residual_variant < -1 || o.residual_variant > 2) return PM_BADARG;
   if (o.apply_variant < -1 || o.apply_variant > 2) return PM_BADARG;
   if (o.upload_mode < 0 || o.upload_mode > 1) return PM_BADARG;
   if (o.decouple < 0 || o.decouple > 1 || o.wait_limit < 0 || o.max_device_bytes < 0)
@@ -1370,9 +1265,6 @@ pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
     Lv.h_child.assign(d->cell_child, d->cell_child + Lv.ncells);
   }
   Lv.pattern_key = pattern_fingerprint(d);
-  Lv.h_a_rowptr.assign(d->a_rowptr, d->a_rowptr + Lv.nu + 1);
-  Lv.h_b_rowptr.assign(d->b_rowptr, d->b_rowptr + Lv.np + 1);
-  Lv.h_bt_rowptr.assign(d->bt_rowptr, d->bt_rowptr + Lv.nu + 1);
   Lv.has_colour = d->cell_colour != nullptr;
   if (Lv.has_colour) Lv.h_colour.assign(d->cell_colour, d->cell_colour + Lv.ncells);
   PM_TRY(upload(h, &Lv.a_rowptr, d->a_rowptr, (size_t)Lv.nu + 1));
@@ -1497,9 +1389,7 @@ pm_status pm_setup(pm_handle *h) {
       PM_TRY(tune_level<float>(h, h->L[l]));
     else
       PM_TRY(tune_level<double>(h, h->L[l]));
-    PM_TRY(fill_cell_store(h, h->L[l]));
   }
-  PM_TRY(sync(h, "cell stores"));
   h->setup_done = true;
   return PM_OK;
 }
@@ -1578,7 +1468,7 @@ int pm_level_ndof(pm_handle *h, int l) {
   return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].ndof : -1;
 }
 int pm_level_variant(pm_handle *h, int l) {
-  return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].res_variant + 3 * h->L[l].apply_variant
+  return (h && l >= 0 && l < (int)h->L.size()) ? h->L[l].res_variant + 2 * h->L[l].apply_variant
                                                 : -1;
 }
 int pm_level_blocks(pm_handle *h, int l) {

@@ -238,48 +238,6 @@ int launch_assemble_level(const AsmOp &op, const DevCells &cells, const int *col
                           const int *colour_ptr, int ncolours, const double *cell_h,
                           const double *conv, double nu, cudaStream_t s);
 
-// ------------------------------------------------------------- cell store --
-// Per-cell copies of the matrix rows a Vanka cell reads, in the colour order
-// of the sweep (slot s = position in the level's colour_cells), for levels
-// without velocity coupling: per cell its 27 A rows, then the BT rows of its
-// active velocity DOFs and its 4 B rows, each row padded with zeros to a
-// whole number of groups of VEC entries (4 in FP32, 2 in FP64; padding
-// columns repeat the row's last column).  A rows go to the "A" arrays (nva
-// values per entry: 1 when A11 = A22 = A33, else A11, A22, A33), BT and B
-// rows to the "P" arrays (three values per entry).  Every group carries its
-// local row (0..26 for A and BT, 0..3 for B).  Offsets count groups.
-template <typename T>
-struct CellStore {
-  int nva;
-  const long long *offA, *offP;       // nslots + 1 each
-  const int *cnt;                     // 3 per slot: A, BT and B groups
-  const unsigned char *ridA, *ridP;   // per group
-  const int *colA, *colP;             // per entry
-  const T *a[3];                      // A values (a[1], a[2] only when nva == 3)
-  const T *p[3];                      // BT / B values of the three components
-};
-template <typename T>
-constexpr int cell_store_vec() {
-  return sizeof(T) == 4 ? 4 : 2;
-}
-// Host-side layout of a level's store: offsets and group counts per slot
-// from the CSR row pointers, the cell maps and the colour order.
-void cell_store_layout(int nslots, const int *order, const int *udofs, const int *pdofs, int nact,
-                       const int *a_rowptr, const int *b_rowptr, const int *bt_rowptr, int vec,
-                       long long *offA, long long *offP, int *cnt);
-// Fill the store's values (and, with write_pattern, its columns and row
-// ids) from the level's FP64 CSR values, converted to T.
-template <typename T>
-int launch_cell_store_fill(const CellStore<T> &cs, const DevOp<double> &op, const DevCells &cells,
-                           const int *order, int nslots, bool write_pattern, cudaStream_t s);
-// Local residuals r = f - K u of the ncol cells of one colour (store slots
-// slot0 .. slot0 + ncol - 1, cells cell_list[0 .. ncol - 1]) from the store;
-// same output as launch_vanka_residual.
-template <typename T>
-int launch_vanka_residual_cells(const CellStore<T> &cs, const DevCells &cells, int nu, int slot0,
-                                const int *cell_list, int ncol, const T *u, const T *rhs, T *rbuf,
-                                cudaStream_t s);
-
 // ----------------------------------------------------------------- coarse --
 // Dense column-major N x N coarse saddle matrix of SolveExact
 // (src/FE/NSE_MGLevel4.C:5728-5830) from the FP64 CSR.
