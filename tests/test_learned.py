@@ -167,3 +167,26 @@ def test_learned_solve_matches_plain_solution_and_falls_back(problems, trained):
     S.attach_learned(None)
     S.close()
     plain.close()
+
+
+def test_manufactured_harvest_matches_exact_solution_harvest(problems):
+    """Pairs from a manufactured solution (b := K u*) equal the pairs of the
+    exact-solution harvest when u* is that harvest's solution: the targets
+    are the same errors, known without solving the system."""
+    import torch
+    from to_merge_master_parmoon_gb300 import PmSolver
+    from to_merge_master_parmoon_gb300.learned import harvest_manufactured, harvest_pairs
+    P = problems(3, 1e-2, 7)
+    b = P.rhs()
+    nu3 = 3 * P.desc(2).n_udof
+    bp = b.copy()
+    bp[nu3::4] -= bp[nu3::4].mean()
+    S = PmSolver(P.descs, precision="fp64", restart=30, maxit=300,
+                 res_norm_min=1e-11 * np.linalg.norm(bp))
+    xs, _ = S.iterate(np.zeros_like(b), b)
+    S.close()
+    X1, T1 = harvest_pairs([P], n_cycles=3)
+    X2, T2 = harvest_manufactured([P], n_cycles=3, solutions=[xs])
+    assert X1.shape == X2.shape and T1.shape == T2.shape
+    assert float(torch.linalg.norm(X1 - X2) / torch.linalg.norm(X1)) < 1e-3
+    assert float(torch.linalg.norm(T1 - T2) / torch.linalg.norm(T1)) < 1e-3

@@ -607,23 +607,49 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual_rows(
   const T *u1 = u, *u2 = u + nu, *u3 = u + 2 * nu, *p = u + 3 * nu;
   const int *ud = cells.udofs + (size_t)cell * NU_LOC;
   T *R = rbuf + (size_t)slot * kRStride;
-  // velocity rows: A (one or nine blocks) and, on active rows, BT
+  // The cell's rows, their row-pointer ranges and right-hand sides, loaded
+  // once, all in parallel, by the lane that owns each (lane a: velocity DOF
+  // a; lane q < 4 also pressure DOF q) and handed to the 8-lane groups by
+  // shuffles, so that a row step waits only for its values and gathers.
+  const bool own_u = lane < NU_LOC, own_p = lane < NP_LOC;
+  const int my_r = own_u ? __ldg(ud + lane) : 0;
+  const int my_q = own_p ? __ldg(cells.pdofs + (size_t)cell * NP_LOC + lane) : 0;
+  int my_ars = 0, my_are = 0, my_trs = 0, my_tre = 0, my_brs = 0, my_bre = 0;
+  T my_f0 = T(0), my_f1 = T(0), my_f2 = T(0), my_fp = T(0);
+  if (own_u) {
+    my_ars = __ldg(op.a_rowptr + my_r);
+    my_are = __ldg(op.a_rowptr + my_r + 1);
+    if (my_r < op.nact) {
+      my_trs = __ldg(op.bt_rowptr + my_r);
+      my_tre = __ldg(op.bt_rowptr + my_r + 1);
+    }
+    my_f0 = rhs[my_r];
+    my_f1 = rhs[(size_t)nu + my_r];
+    my_f2 = rhs[(size_t)2 * nu + my_r];
+  }
+  if (own_p) {
+    my_brs = __ldg(op.b_rowptr + my_q);
+    my_bre = __ldg(op.b_rowptr + my_q + 1);
+    my_fp = rhs[(size_t)3 * nu + my_q];
+  }
+  // velocity rows: A (one, three or nine blocks) and, on active rows, BT
   for (int step = 0; step < (NU_LOC + 3) / 4; ++step) {
     const int k = step * 4 + sub;
     const bool valid = k < NU_LOC;
     const int a = valid ? (NU == 27 ? (int)c_row_order[k] : k) : 0;
-    const int r = valid ? __ldg(ud + a) : 0;
+    const int ars = __shfl_sync(kFull, my_ars, a), are = __shfl_sync(kFull, my_are, a);
+    const int trs = __shfl_sync(kFull, my_trs, a), tre = __shfl_sync(kFull, my_tre, a);
+    const T f0 = __shfl_sync(kFull, my_f0, a), f1 = __shfl_sync(kFull, my_f1, a),
+            f2 = __shfl_sync(kFull, my_f2, a);
     T s[3] = {T(0), T(0), T(0)};
     if (valid) {
       if constexpr (KIND == 2)
-        row_group_sum<T, VEC, 3, URA, true>(op.a_col, op.ad, op.a_rowptr[r], op.a_rowptr[r + 1],
-                                            sl, u1, u2, u3, true, s);
+        row_group_sum<T, VEC, 3, URA, true>(op.a_col, op.ad, ars, are, sl, u1, u2, u3, true, s);
       else
-        row_group_sum<T, VEC, KIND == 1 ? 1 : 9, URA>(op.a_col, op.a, op.a_rowptr[r],
-                                                      op.a_rowptr[r + 1], sl, u1, u2, u3, true, s);
-      if (r < op.nact)
-        row_group_sum<T, VEC, 3, 1>(op.bt_col, op.bt, op.bt_rowptr[r], op.bt_rowptr[r + 1], sl, p,
-                                    p, p, false, s);
+        row_group_sum<T, VEC, KIND == 1 ? 1 : 9, URA>(op.a_col, op.a, ars, are, sl, u1, u2, u3,
+                                                      true, s);
+      if (tre > trs)  // active rows only (Dirichlet rows carry no BT)
+        row_group_sum<T, VEC, 3, 1>(op.bt_col, op.bt, trs, tre, sl, p, p, p, false, s);
     }
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) {
@@ -631,20 +657,20 @@ __global__ void __launch_bounds__(kResWarps * 32) k_vanka_residual_rows(
       for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(kFull, s[c], o);
     }
     if (valid && sl == 0) {
-      R[a] = rhs[r] - s[0];
-      R[NU_LOC + a] = rhs[(size_t)nu + r] - s[1];
-      R[2 * NU_LOC + a] = rhs[(size_t)2 * nu + r] - s[2];
+      R[a] = f0 - s[0];
+      R[NU_LOC + a] = f1 - s[1];
+      R[2 * NU_LOC + a] = f2 - s[2];
     }
   }
   // pressure rows (B): group `sub` owns the cell's pressure DOF `sub`
   {
-    const int r = cells.pdofs[(size_t)cell * NP_LOC + sub];
+    const int brs = __shfl_sync(kFull, my_brs, sub), bre = __shfl_sync(kFull, my_bre, sub);
+    const T fp = __shfl_sync(kFull, my_fp, sub);
     T s[3] = {T(0), T(0), T(0)};
-    row_group_sum<T, VEC, 3, 1>(op.b_col, op.b, op.b_rowptr[r], op.b_rowptr[r + 1], sl, u1, u2, u3,
-                                true, s);
+    row_group_sum<T, VEC, 3, 1>(op.b_col, op.b, brs, bre, sl, u1, u2, u3, true, s);
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) s[0] += __shfl_xor_sync(kFull, s[0], o);
-    if (sl == 0) R[3 * NU_LOC + sub] = rhs[(size_t)3 * nu + r] - s[0];
+    if (sl == 0) R[3 * NU_LOC + sub] = fp - s[0];
   }
 }
 
@@ -1373,7 +1399,9 @@ int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *
     k_vanka_residual<T, VEC, U><<<grid, kResWarps * 32, 0, s>>>(op, cells, cell_list, ncol, u, rhs,
                                                                rbuf);
   } else if (op.structured) {
-    k_vanka_residual_rows<T, VEC, 1, 2, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
+    // one A value per entry: in FP32 four vector groups per lane in flight,
+    // so that a vertex row (125 entries) needs one load round trip
+    k_vanka_residual_rows<T, VEC, 1, (sizeof(T) == 4 ? 4 : 2), NU_LOC><<<grid, kResWarps * 32, 0, s>>>(
         op, cells, cell_list, ncol, u, rhs, rbuf);
   } else if (op.diag) {
     k_vanka_residual_rows<T, VEC, 2, 2, NU_LOC><<<grid, kResWarps * 32, 0, s>>>(

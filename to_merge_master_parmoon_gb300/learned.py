@@ -136,6 +136,48 @@ def harvest_pairs(problems, n_cycles: int = 8, device: int = 0, precision: str =
     return X[keep].contiguous(), T[keep].contiguous()
 
 
+def harvest_manufactured(problems, n_cycles: int = 8, device: int = 0, noise: float = 0.1,
+                         seed: int = 0, max_target_rms: float = 1e4, solutions=None, log=None):
+    """(features, scaled error) pairs with a manufactured solution on each
+    problem's finest level: u* = a smooth divergence-free field (the nodal
+    convection field of a problem with another seed) plus `noise` times
+    seeded white noise on every DOF (or solutions[k] when given), right-hand
+    side b := K u* (the library's FP64 mat-vec), so the error u* - u of the
+    plain iterates is known without an exact solve, also where the plain
+    solver does not converge (strongly convective nu).  Same filters and
+    output as harvest_pairs."""
+    import torch
+    from .problem import OseenProblem
+    total = sum(P.desc(P.n_levels - 1).n_cells * n_cycles for P in problems)
+    X = torch.empty((total, N_IN), dtype=torch.float32, device=f"cuda:{device}")
+    T = torch.empty((total, N_OUT), dtype=torch.float32, device=f"cuda:{device}")
+    n = 0
+    rng = np.random.default_rng(seed)
+    for k, P in enumerate(problems):
+        L = P.n_levels
+        S = PmSolver(P.descs, precision="fp64", device=device)
+        nu3 = 3 * P.desc(L - 1).n_udof
+        if solutions is not None:
+            us = np.ascontiguousarray(solutions[k], dtype=np.float64)
+        else:
+            Q = OseenProblem(n_levels=L, nu=P.nu, seed=5000 + k)
+            us = np.zeros(P.ndof(-1))
+            us[:nu3] = Q.convection_nodal(L - 1)
+            us += noise * rng.standard_normal(us.size)
+        b = S.matvec(L - 1, us)
+        n0 = n
+        _torch_done(X)
+        n = S.harvest(us, b, n_cycles, X.data_ptr(), T.data_ptr(), total, n)
+        S.close()
+        if log:
+            log(f"manufactured harvest nu={P.nu:.2e}: {n - n0} rows")
+    X, T = X[:n], T[:n]
+    keep = torch.isfinite(X).all(1) & torch.isfinite(T).all(1)
+    keep &= T.pow(2).mean(1).sqrt() <= max_target_rms
+    keep &= X.abs().amax(1) < 0.999 * FEATURE_CLAMP
+    return X[keep].contiguous(), T[keep].contiguous()
+
+
 def train(mlp: Mlp, X, T, epochs: int = 20, batch: int = 4096, lr: float = 1e-3,
           weight_decay: float = 1e-2, seed: int = 0, log=None):
     """AdamW mini-batch training on device tensors; returns per-epoch mean loss."""
