@@ -1709,9 +1709,21 @@ static pm_status assemble_impl(pm_handle *h, int level, const double *d_cell_h,
   PM_LAUNCH(launch_assemble_level(op, Lv.cells(), Lv.colour_cells, Lv.colouring.ptr.data(),
                                   (int)Lv.colouring.ptr.size() - 1, d_cell_h, d_conv, nu,
                                   h->stream));
-  // the level's block structure (the assembly zeroes A12..A32 and writes
-  // the same values into A11, A22, A33)
-  PM_TRY(refresh_modes(h, level));
+  // the assembly zeroes A12..A32 and writes the same values into A11, A22
+  // and A33 (k_assemble_cells): mode 2 by construction, no device check
+  if (!Lv.structured) {
+    const int d = h->opt.decouple ? 2 : 0;
+    if (d != Lv.diag) {
+      Lv.diag = d;
+      drop_graphs(h);
+      PM_TRY(ensure_factors(h, Lv));
+      level_bytes(h, Lv);
+      if (mixed(h))
+        PM_TRY(tune_level<float>(h, Lv));
+      else
+        PM_TRY(tune_level<double>(h, Lv));
+    }
+  }
   if (mixed(h)) {
     const int nblk = Lv.structured ? 1 : 9;
     for (int k = 0; k < nblk; ++k)

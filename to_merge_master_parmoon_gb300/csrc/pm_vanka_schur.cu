@@ -175,16 +175,10 @@ __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double
       __syncwarp();
       for (int c = k + 1 + lane; c < GW; c += 32) M[k * MS + c] *= rp;
       __syncwarp();
-      // row updates; a zero entry of the pivot row changes nothing, and
-      // most of the identity block's entries still are zero at step k, so
-      // they are skipped (the branch is the same for every lane)
       if (lane < NU_LOC && lane != k) {
         const double f = my[k];
         if (f != 0.0)
-          for (int c = k + 1; c < GW; ++c) {
-            const double pk = M[k * MS + c];
-            if (pk != 0.0) my[c] -= f * pk;
-          }
+          for (int c = k + 1; c < GW; ++c) my[c] -= f * M[k * MS + c];
       }
       __syncwarp();
     }
