@@ -176,15 +176,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-# DRAM bytes (read + write) per cell of one local-residual launch on a
-# decoupled FP32 level (k_vanka_residual_rows, three A blocks), from one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum) of a 32^3 colour
-# launch of 4,096 cells:
-#   ncu --set full --clock-control none -k regex:k_vanka_residual -s 16 -c 1 \
+# DRAM bytes (read + write) per cell of one local-residual launch of the
+# headline kernel (k_vanka_residual_rows<float,4,1,4,27>: FP32, one A block)
+# from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum =
+# 134.74 + 3.09 MB) of a 32^3 colour launch of 4,096 cells:
+#   ncu --set full --clock-control none -k regex:'k_vanka_residual|k_schur_apply' -s 32 -c 2 \
 #       python bench.py --only-sweep mixed --levels 5 --warmup 1 --steps 2
-# None until measured.  Traffic grows with the cells a launch processes
-# (every cell reads its own 27 rows), so it scales to a launch of any size.
-RESIDUAL_DRAM_BYTES_PER_CELL = None
+# Traffic grows with the cells a launch processes (every cell reads its own
+# 27 rows), so it scales to a launch of any size.
+RESIDUAL_DRAM_BYTES_PER_CELL = 33651
 
 
 # the FP32 sweep kernels by level mode (0 nine blocks + LU, 1 three diagonal
