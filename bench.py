@@ -177,14 +177,14 @@ def measured_peaks():
 
 
 # DRAM bytes (read + write) per cell of one local-residual launch of the
-# headline kernel (k_vanka_residual_rows<float,4,1,4,27>: FP32, one A block)
-# from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum =
-# 134.74 + 3.09 MB) of a 32^3 colour launch of 4,096 cells:
+# headline kernel (k_vanka_residual_rows<float,1,1,8,27,true,true>: FP32, one
+# A block, interleaved velocity) from one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum = 136.83 + 2.90 MB) of a 32^3 colour launch of 4,096 cells:
 #   ncu --set full --clock-control none -k regex:'k_vanka_residual|k_schur_apply' -s 32 -c 2 \
 #       python bench.py --only-sweep mixed --levels 5 --warmup 1 --steps 2
 # Traffic grows with the cells a launch processes (every cell reads its own
 # 27 rows), so it scales to a launch of any size.
-RESIDUAL_DRAM_BYTES_PER_CELL = 33651
+RESIDUAL_DRAM_BYTES_PER_CELL = 34114
 
 
 # the FP32 sweep kernels by level mode (0 nine blocks + LU, 1 three diagonal
@@ -197,8 +197,13 @@ def residual_kernel_name(mode, variant):
     if variant == 1:
         return ("k_vanka_residual<float,4,1> (cell-local residuals over full CSR rows of one "
                 f"colour, flattened entry stream; {blocks}, BT, B)")
-    kind = {0: 0, 1: 2, 2: 1}[mode]
-    return (f"k_vanka_residual_rows<float,4,{kind},{1 if kind == 0 else 2},27> (cell-local "
+    if mode == 2:
+        return ("k_vanka_residual_rows<float,1,1,8,27,true,true> (cell-local residuals over full "
+                "CSR rows of one colour, 8 lanes per row, A and BT rows of a step loaded "
+                f"together, velocity gathered from its interleaved copy; {blocks}, BT, B)")
+    kind = {0: 0, 1: 2}[mode]
+    vec, ur = {0: (4, 1), 2: (1, 8)}[kind]
+    return (f"k_vanka_residual_rows<float,{vec},{kind},{ur},27> (cell-local "
             f"residuals over full CSR rows of one colour, 8 lanes per row; {blocks}, BT, B)")
 
 
@@ -207,8 +212,9 @@ APPLY_KERNEL = {
        "registers and L2; substitution + update)",
     1: "k_schur_apply<float,3> (stored FP32 block elimination: three 27x27 inverses, B, A^-1 BT, "
        "4x4 Schur inverse; one cell per warp, GEMVs + update)",
-    2: "k_schur_apply<float,1> (stored FP32 block elimination: one 27x27 inverse, B, A^-1 BT, "
-       "4x4 Schur inverse; one cell per warp, GEMVs + update)"}
+    2: "k_schur_apply<float,1,true> (stored FP32 block elimination: one 27x27 inverse, B, "
+       "A^-1 BT, 4x4 Schur inverse; one cell per warp, GEMVs + update of the interleaved "
+       "velocity)"}
 
 
 def ncu_traffic(P):

@@ -83,6 +83,9 @@ struct LevelDev {
   uint8_t *perm = nullptr;
   CsrStore Pu, Ru, Pp, Rp;
   void *sol = nullptr, *rhs = nullptr, *def = nullptr, *uold = nullptr, *dbuf = nullptr;
+  // interleaved FP32 velocity (16 bytes per node) that the one-block sweep
+  // gathers from and updates; mixed precision, hexahedral smoothed levels
+  float4 *ux = nullptr;
   double *x64 = nullptr, *y64 = nullptr, *z64 = nullptr;
   // unique bytes of one Vanka sweep per cell, split by kernel (see pm_setup)
   double vanka_res_bytes = 0.0, vanka_apply_bytes = 0.0;
@@ -340,6 +343,14 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
   const DevOp<T> op = Lv.op<T>();
   const DevCells cells = Lv.cells();
   const int ncol = (int)Lv.colouring.ptr.size() - 1;
+  // FP32 one-block levels: the sweep gathers the velocity from its
+  // interleaved copy (one 16-byte load per matrix entry instead of three
+  // 4-byte loads, the residual being bound by the L1 wavefronts of its
+  // gathers) and the apply updates that copy; packed before the colours,
+  // unpacked after them
+  const bool aos = sizeof(T) == sizeof(float) && Lv.ux && Lv.schur() && Lv.res_variant == 0;
+  float *uf = reinterpret_cast<float *>(u);
+  if (aos) PM_LAUNCH(launch_pack_velocity(uf, Lv.ux, Lv.nu, h->stream));
   for (int k = 0; k < ncol; ++k) {
     const int b = Lv.colouring.ptr[k], n = Lv.colouring.ptr[k + 1] - b;
     if (n == 0) continue;
@@ -351,10 +362,20 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
       h->evused += 3;
       cudaEventRecord(e0, h->stream);
     }
-    PM_LAUNCH(launch_vanka_residual<T>(op, cells, Lv.colour_cells + b, n, u, rhs,
-                                       static_cast<T *>(Lv.dbuf), Lv.res_variant, h->stream));
+    if (aos)
+      PM_LAUNCH(launch_vanka_residual_aos(Lv.op<float>(), cells, Lv.colour_cells + b, n, uf,
+                                          Lv.ux, reinterpret_cast<const float *>(rhs),
+                                          static_cast<float *>(Lv.dbuf), h->stream));
+    else
+      PM_LAUNCH(launch_vanka_residual<T>(op, cells, Lv.colour_cells + b, n, u, rhs,
+                                         static_cast<T *>(Lv.dbuf), Lv.res_variant, h->stream));
     if (e1) cudaEventRecord(e1, h->stream);
-    if (Lv.schur())
+    if (aos)
+      PM_LAUNCH(launch_schur_apply_aos(cells, Lv.nu, Lv.colour_cells + b, n,
+                                       static_cast<const float *>(Lv.factors),
+                                       static_cast<const float *>(Lv.dbuf), (float)damp, uf,
+                                       Lv.ux, h->stream));
+    else if (Lv.schur())
       PM_LAUNCH(launch_schur_apply<T>(cells, Lv.nu, Lv.colour_cells + b, n,
                                       static_cast<const T *>(Lv.factors),
                                       static_cast<const T *>(Lv.dbuf), damp, u, h->stream));
@@ -383,6 +404,7 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
       h->prof_bytes.push_back(Lv.vanka_apply_bytes * n);
     }
   }
+  if (aos) PM_LAUNCH(launch_unpack_velocity(Lv.ux, uf, Lv.nu, h->stream));
   if (relax) PM_LAUNCH(launch_relax<T>(u, static_cast<const T *>(Lv.uold), (T)h->opt.alpha, Lv.ndof, h->stream));
   PM_LAUNCH(launch_dirichlet<T>(u, rhs, Lv.nu, Lv.hb, Lv.ndir, h->stream));
   return PM_OK;
@@ -1348,6 +1370,7 @@ pm_status pm_setup(pm_handle *h) {
                     (size_t)Lv.colouring.max_size * elem_r_stride(Lv.nl) * es));
       if (std::fabs(1.0 - h->opt.alpha) > 1e-3)
         PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.uold), (size_t)Lv.ndof * es));
+      if (mixed(h) && Lv.nl == NU_LOC) PM_TRY(dalloc(h, &Lv.ux, (size_t)Lv.nu));
     }
     level_bytes(h, Lv);
     PM_TRY(dalloc(h, reinterpret_cast<unsigned char **>(&Lv.sol), (size_t)Lv.ndof * es));

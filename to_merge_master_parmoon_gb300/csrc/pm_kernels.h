@@ -118,6 +118,9 @@ int launch_zero_nonactive(T *v, int nu, int nact, cudaStream_t s);
 // u = uold + alpha (u - uold)
 template <typename T>
 int launch_relax(T *u, const T *uold, T alpha, int n, cudaStream_t s);
+// FP32 velocity u[c*nu + d] (c = 0..2) <-> its interleaved copy ux[d] (pad 0)
+int launch_pack_velocity(const float *u, float4 *ux, int nu, cudaStream_t s);
+int launch_unpack_velocity(const float4 *ux, float *u, int nu, cudaStream_t s);
 // zero off-diagonal velocity blocks on rows >= nact
 int launch_zero_dirichlet_offdiag(double *const a[9], const int *rowptr, int nu, int nact,
                                   cudaStream_t s);
@@ -147,6 +150,12 @@ int launch_vanka_factor(const DevOp<double> &op, const DevCells &cells, TF *fact
 template <typename T>
 int launch_vanka_residual(const DevOp<T> &op, const DevCells &cells, const int *cell_list, int ncol,
                           const T *u, const T *rhs, T *rbuf, int variant, cudaStream_t s);
+// The same (row groups) on an FP32 one-block hexahedral level with the
+// velocity read from its interleaved copy ux (node d: ux[d].x/y/z) and the
+// pressure from u; -1 for any other level.
+int launch_vanka_residual_aos(const DevOp<float> &op, const DevCells &cells, const int *cell_list,
+                              int ncol, const float *u, const float4 *ux, const float *rhs,
+                              float *rbuf, cudaStream_t s);
 // Local solve with the stored factors and u[dofs] += damp * delta, for the
 // same cells (run after launch_vanka_residual of the whole colour).  pairs:
 // two cells per warp (half-warp per cell) instead of one.
@@ -193,6 +202,10 @@ int launch_schur_factor(const DevOp<double> &op, const DevCells &cells, TF *fact
 template <typename T>
 int launch_schur_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                        const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s);
+// FP32 one-block apply updating the interleaved velocity ux and the pressure in u
+int launch_schur_apply_aos(const DevCells &cells, int nu, const int *cell_list, int ncol,
+                           const float *factors, const float *rbuf, float damp, float *u,
+                           float4 *ux, cudaStream_t s);
 // the same for NB = 3 (op.diag levels)
 template <typename TF>
 int launch_schur3_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,

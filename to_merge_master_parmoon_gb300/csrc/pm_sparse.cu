@@ -61,6 +61,11 @@ struct VLd<float, 4> {
     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
   }
 };
+template <typename T>
+struct VLd<T, 1> {
+  static __device__ __forceinline__ void val(const T *p, T (&o)[1]) { o[0] = __ldcs(p); }
+  static __device__ __forceinline__ void idx(const int *p, int (&o)[1]) { o[0] = __ldg(p); }
+};
 template <>
 struct VLd<double, 2> {
   static __device__ __forceinline__ void val(const double *p, double (&o)[2]) {
@@ -142,6 +147,8 @@ __global__ void __launch_bounds__(kBlock) k_coupled_velocity8(DevOp<T> op, const
                                                               const T *__restrict__ b,
                                                               T *__restrict__ r, int defect,
                                                               int zero_nonactive) {
+  // BT rows (at most 32 entries on hexahedra): one load round trip
+  constexpr int URB = (16 / (int)sizeof(T)) / VEC > 1 ? (16 / (int)sizeof(T)) / VEC : 1;
   // no early return before the group shuffles: every lane of the warp joins
   const int sl = threadIdx.x & 7;
   const long long row = ((long long)blockIdx.x * kBlock + threadIdx.x) >> 3;
@@ -159,8 +166,8 @@ __global__ void __launch_bounds__(kBlock) k_coupled_velocity8(DevOp<T> op, const
       rows8_sum<T, VEC, KIND == 1 ? 1 : 9, UR>(op.a_col, op.a, op.a_rowptr[i], op.a_rowptr[i + 1],
                                                sl, u1, u2, u3, s);
     if (i < op.nact)
-      rows8_sum<T, VEC, 3, 1>(op.bt_col, op.bt, op.bt_rowptr[i], op.bt_rowptr[i + 1], sl, p, p,
-                              p, s);
+      rows8_sum<T, VEC, 3, URB>(op.bt_col, op.bt, op.bt_rowptr[i], op.bt_rowptr[i + 1], sl, p, p,
+                                p, s);
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c) s[c] = group_sum<8>(s[c]);
@@ -385,6 +392,21 @@ __global__ void k_relax(T *u, const T *uold, T alpha, int n) {
     u[i] = uold[i] + alpha * (u[i] - uold[i]);
 }
 
+// the FP32 velocity between its three component arrays and the interleaved
+// copy the one-block sweep gathers from (16 bytes per node, pad 0)
+__global__ void k_pack_velocity(const float *__restrict__ u, float4 *__restrict__ ux, int nu) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += gridDim.x * blockDim.x)
+    ux[i] = make_float4(u[i], u[(size_t)nu + i], u[(size_t)2 * nu + i], 0.f);
+}
+__global__ void k_unpack_velocity(const float4 *__restrict__ ux, float *__restrict__ u, int nu) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += gridDim.x * blockDim.x) {
+    const float4 v = ux[i];
+    u[i] = v.x;
+    u[(size_t)nu + i] = v.y;
+    u[(size_t)2 * nu + i] = v.z;
+  }
+}
+
 struct Ptr9 {
   double *p[9];
 };
@@ -457,15 +479,26 @@ int launch_coupled(const DevOp<T> &op, const T *x, const T *b, T *r, bool defect
   constexpr int GP = 16;
   constexpr int VEC = sizeof(T) == 4 ? 4 : 2;
   const unsigned gv = grid_for((long long)op.nu * 8);
-  if (op.structured)
-    k_coupled_velocity8<T, VEC, 1, 2><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+  if (op.structured) {
+    // FP32: scalar entries, the 8 lanes of a row gathering consecutive
+    // columns (fewer cache lines per gather instruction than vectors of 4)
+    if constexpr (sizeof(T) == 4)
+      k_coupled_velocity8<T, 1, 1, 8><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
                                                            zero_nonactive ? 1 : 0);
-  else if (op.diag)
-    k_coupled_velocity8<T, VEC, 2, 2><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+    else
+      k_coupled_velocity8<T, VEC, 1, 2><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+                                                             zero_nonactive ? 1 : 0);
+  } else if (op.diag) {
+    if constexpr (sizeof(T) == 4)
+      k_coupled_velocity8<T, 1, 2, 8><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
                                                            zero_nonactive ? 1 : 0);
-  else
+    else
+      k_coupled_velocity8<T, VEC, 2, 2><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
+                                                             zero_nonactive ? 1 : 0);
+  } else {
     k_coupled_velocity8<T, VEC, 0, 1><<<gv, kBlock, 0, s>>>(op, x, b, r, defect ? 1 : 0,
                                                            zero_nonactive ? 1 : 0);
+  }
   if (ok() < 0) return -1;
   k_coupled_pressure<T, GP><<<grid_for((long long)op.np * GP), kBlock, 0, s>>>(op, x, b, r,
                                                                                defect ? 1 : 0);
@@ -552,6 +585,16 @@ int launch_zero_nonactive(T *v, int nu, int nact, cudaStream_t s) {
 template <typename T>
 int launch_relax(T *u, const T *uold, T alpha, int n, cudaStream_t s) {
   k_relax<T><<<stride_grid(n), kBlock, 0, s>>>(u, uold, alpha, n);
+  return ok() < 0 ? -1 : 1;
+}
+int launch_pack_velocity(const float *u, float4 *ux, int nu, cudaStream_t s) {
+  if (nu <= 0) return 0;
+  k_pack_velocity<<<stride_grid(nu), kBlock, 0, s>>>(u, ux, nu);
+  return ok() < 0 ? -1 : 1;
+}
+int launch_unpack_velocity(const float4 *ux, float *u, int nu, cudaStream_t s) {
+  if (nu <= 0) return 0;
+  k_unpack_velocity<<<stride_grid(nu), kBlock, 0, s>>>(ux, u, nu);
   return ok() < 0 ? -1 : 1;
 }
 int launch_zero_dirichlet_offdiag(double *const a[9], const int *rowptr, int nu, int nact,

@@ -275,10 +275,14 @@ __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double
   if (lane == 0 && singular) atomicOr(status, 1);
 }
 
-template <typename T, int NB>
+// AOS (FP32): the velocity update goes to the interleaved copy ux (node d
+// at ux[d]: three components and a pad; one 16-byte read-modify-write per
+// node), the pressure update to u
+template <typename T, int NB, bool AOS = false>
 __global__ void __launch_bounds__(kApplyWarps * 32) k_schur_apply(
     DevCells cells, int nu, const int *__restrict__ list, int ncol, const T *__restrict__ factors,
-    const T *__restrict__ rbuf, T damp, T *__restrict__ u) {
+    const T *__restrict__ rbuf, T damp, T *__restrict__ u, float4 *__restrict__ ux) {
+  static_assert(!AOS || sizeof(T) == sizeof(float), "interleaved velocity: FP32 only");
   using L = Schur<NB>;
   constexpr int B1 = NB == 1 ? 0 : NU_LOC * NU_LOC;  // offset of A_2^{-1} (A_3^{-1}: 2 B1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -346,9 +350,17 @@ __global__ void __launch_bounds__(kApplyWarps * 32) k_schur_apply(
       y2 -= Wv[k][2] * p[k];
     }
     const int d = cells.udofs[(size_t)cell * NU_LOC + lane];
-    u[d] += damp * y0;
-    u[(size_t)nu + d] += damp * y1;
-    u[(size_t)2 * nu + d] += damp * y2;
+    if constexpr (AOS) {
+      float4 v = ux[d];
+      v.x += damp * y0;
+      v.y += damp * y1;
+      v.z += damp * y2;
+      ux[d] = v;
+    } else {
+      u[d] += damp * y0;
+      u[(size_t)nu + d] += damp * y1;
+      u[(size_t)2 * nu + d] += damp * y2;
+    }
   }
   if (lane < NP_LOC) {
     const T pl = lane == 0 ? p[0] : (lane == 1 ? p[1] : (lane == 2 ? p[2] : p[3]));
@@ -391,7 +403,7 @@ int apply_impl(const DevCells &cells, int nu, const int *cell_list, int ncol, co
   if (ncol <= 0) return 0;
   const int grid = (ncol + kApplyWarps - 1) / kApplyWarps;
   k_schur_apply<T, NB><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol, factors,
-                                                        rbuf, damp, u);
+                                                        rbuf, damp, u, nullptr);
   return ok() < 0 ? -1 : 1;
 }
 
@@ -421,6 +433,17 @@ template <typename T>
 int launch_schur3_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                         const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s) {
   return apply_impl<T, 3>(cells, nu, cell_list, ncol, factors, rbuf, damp, u, s);
+}
+
+int launch_schur_apply_aos(const DevCells &cells, int nu, const int *cell_list, int ncol,
+                           const float *factors, const float *rbuf, float damp, float *u,
+                           float4 *ux, cudaStream_t s) {
+  if (ncol <= 0) return 0;
+  if (cells.nl != NU_LOC || ux == nullptr) return -1;
+  const int grid = (ncol + kApplyWarps - 1) / kApplyWarps;
+  k_schur_apply<float, 1, true><<<grid, kApplyWarps * 32, 0, s>>>(cells, nu, cell_list, ncol,
+                                                                 factors, rbuf, damp, u, ux);
+  return ok() < 0 ? -1 : 1;
 }
 
 int launch_block_structure(const DevOp<double> &op, long long n, int *flag, cudaStream_t s) {
