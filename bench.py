@@ -91,6 +91,9 @@ def parse():
     ap.add_argument("--only-channel", action="store_true",
                     help="the time-dependent channel run only (the learned variant is skipped): "
                          "e.g. all 200 steps of one variant")
+    ap.add_argument("--only-batch", action="store_true",
+                    help="the batch of independent systems only (concurrent handles, one "
+                         "after another, and fused groups)")
     ap.add_argument("--only-assembly", action="store_true",
                     help="device assembly of every level only (one-block FP64 levels, "
                          "warm-up + steps passes): the case profiled for k_assemble_cells")
@@ -852,18 +855,86 @@ def batch_run(args, device, log=None):
     if log:
         log(f"batch: {len(solvers)} systems, {conv} converged, batch {t_batch:.3f} s, "
             f"one after another {t_seq:.3f} s")
+    xs_batch = solve_batch(solvers, zeros, rhss, allow=(0, 1, 2, 3))[0]
+    for S in solvers:
+        S.close()
+    solvers = []
+    fused = fused_batch_run(probs, rhss, xs_batch, infos, device, log)
     tet = [P.element == "tetra" for P in probs]
-    out = {"systems": len(solvers), "tetrahedral_systems": sum(tet),
+    out = {"systems": len(probs), "tetrahedral_systems": sum(tet),
            "converged_to_1e-8": conv, "total_dof": dofs,
            "tetrahedral_dof": sum(P.ndof(-1) for P, t in zip(probs, tet) if t),
            "cells": sorted({P.desc(P.n_levels - 1).n_cells for P in probs}),
            "iterations": [i["iterations"] for i in infos],
            "iterations_tetrahedral": [i["iterations"] for i, t in zip(infos, tet) if t],
            "batch_s": t_batch, "sequential_s": t_seq, "speedup": t_seq / t_batch,
-           "build_s": build_s}
-    for S in solvers:
-        S.close()
+           "build_s": build_s, "fused": fused}
     return out
+
+
+def fused_batch_run(probs, rhss, xs_ref, infos_ref, device, log=None):
+    """The same systems as fused groups: systems of one mesh (same element
+    and size) stacked into one PmFusedSolver each, every kernel one launch
+    over the group; the groups run concurrently (one host thread and stream
+    each).  Timed after one untimed pass; per system the iterations and the
+    relative L2 difference to the pm_solve_batch solution (L2_0-normalised
+    pressure)."""
+    import numpy as np
+    from to_merge_master_parmoon_gb300 import PmFusedSolver, solve_fused_groups
+    keys = sorted({(P.element, P.n_levels) for P in probs})
+    members = {k: [i for i, P in enumerate(probs) if (P.element, P.n_levels) == k] for k in keys}
+    t0 = time.perf_counter()
+    groups = []
+    for k in keys:
+        idx = members[k]
+        # each system to 1e-8 of its own initial residual (x0 = 0: the same
+        # test as res_norm_min = 1e-8 ||b|| of the single-system solves)
+        groups.append(PmFusedSolver([probs[i].descs for i in idx], precision="mixed",
+                                    device=device, restart=20, maxit=100, res_norm_min=0.0,
+                                    red_factor=RTOL, red_initial=1))
+    setup_s = time.perf_counter() - t0
+    zs = [[np.zeros_like(rhss[i]) for i in members[k]] for k in keys]
+    bs = [[rhss[i] for i in members[k]] for k in keys]
+    solve_fused_groups(groups, zs, bs, allow=(0, 1, 2, 3))  # untimed pass
+    t = time.perf_counter()
+    xs, infos = solve_fused_groups(groups, zs, bs, allow=(0, 1, 2, 3))
+    t_fused = time.perf_counter() - t
+    per_group = []
+    diffs = [0.0] * len(probs)
+    its = [0] * len(probs)
+    for g, k in enumerate(keys):
+        t = time.perf_counter()
+        groups[g].solve(zs[g], bs[g], allow=(0, 1, 2, 3))
+        t_alone = time.perf_counter() - t
+        for q, i in enumerate(members[k]):
+            P = probs[i]
+            nu3 = 3 * P.desc(P.n_levels - 1).n_udof
+            a, r = xs[g][q].copy(), xs_ref[i].copy()
+            a[nu3::4] -= a[nu3::4].mean()
+            r[nu3::4] -= r[nu3::4].mean()
+            diffs[i] = float(np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-300))
+            its[i] = infos[g][q]["iterations"]
+        per_group.append({"element": k[0], "cells": probs[members[k][0]].desc(k[1] - 1).n_cells,
+                          "systems": len(members[k]), "solve_s": t_alone,
+                          "max_iterations": max(infos[g][q]["iterations"]
+                                                for q in range(len(members[k]))),
+                          "kernel_launches": groups[g].kernel_launches,
+                          # kernels the tuner chose per smoothed level of the
+                          # stacked hierarchy (pm_level_variant: residual
+                          # kernel + 2 * apply kernel)
+                          "level_variants": [groups[g]._lib.pm_level_variant(groups[g]._h, lv)
+                                             for lv in range(1, k[1])]})
+    conv = sum(1 for grp in infos for i in grp if i["status"] == 0)
+    if log:
+        log(f"fused batch: {len(keys)} groups, {conv} converged, {t_fused:.3f} s "
+            f"(groups concurrently), set-up {setup_s:.2f} s")
+    for G in groups:
+        G.close()
+    return {"groups": per_group, "fused_s": t_fused, "setup_s": setup_s,
+            "converged_to_1e-8": conv, "iterations": its,
+            "max_rel_diff_vs_batch_converged": max(
+                (d for d, i in zip(diffs, infos_ref) if i["status"] == 0), default=None),
+            "rel_diff_vs_batch": diffs}
 
 
 def main():
@@ -873,6 +944,12 @@ def main():
         return
     if args.only_assembly:
         only_assembly(args)
+        return
+    if args.only_batch:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"only_batch": batch_run(args, 0, log=lambda *a: print(*a, file=sys.stderr))}),
+              flush=True)
         return
     if args.only_factor:
         only_factor(args)

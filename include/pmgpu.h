@@ -343,6 +343,32 @@ pm_status pm_interpolate_coarse(pm_handle *h, int level, const double *d_fine, d
  * status in index order, PM_OK if none. */
 pm_status pm_solve_batch(pm_handle *const *hs, int n, double *const *sols,
                          const double *const *rhss, pm_result *results, int nthreads);
+/* Fused batch: n_sys independent systems on one mesh (equal sizes on every
+ * level; values, convection and viscosity may differ) stacked into one
+ * block-diagonal hierarchy, so that every kernel of the V-cycle and of
+ * FGMRES covers all of them in one launch.  The reference batches the cells
+ * of one colour of one system per launch (CellVanka_GPU,
+ * src/FE/NSE_CellVanka.cu:2181-2365; magma_dgesv_batched,
+ * src/FE/Magma_Solver.C:38); here one launch covers that colour in all
+ * systems.  Call pm_add_level_batch once per level (coarsest first) with the
+ * n_sys descriptors of that level, instead of pm_add_level, then pm_setup.
+ * Each system keeps its own L^2_0 projection, coarse inverse, Arnoldi
+ * process, Givens rotations and stopping test (TFgmresIte::Iterate,
+ * src/FE/FgmresIte.C:250-677, per system): results agree with pm_solve of
+ * each system alone to rounding (the sums run in another order).  Systems
+ * that stop early leave the sweeps.  Entry points of one system
+ * (pm_solve, pm_solve_device, pm_solve_exact, pm_update_matrices, the
+ * assembly and time-step entry points, the learned smoother) return
+ * PM_BADARG on such a handle; the level operators and pm_vcycle act on
+ * stacked vectors. */
+pm_status pm_add_level_batch(pm_handle *h, const pm_level_desc *descs, int n_sys);
+/* sols[s] / rhss[s]: host vectors of system s in its own layout
+ * [u1|u2|u3|p]; results[s] per system (may be NULL).  Returns the first
+ * non-PM_OK per-system status in index order, PM_OK if none. */
+pm_status pm_solve_fused(pm_handle *h, double *const *sols, const double *const *rhss,
+                         pm_result *results);
+/* systems stacked in the handle (1 for a handle built by pm_add_level) */
+int pm_n_systems(pm_handle *h);
 /* Re-run the local-block and coarse factorisations on the device (timed into
  * out->setup_ms); used to time factor+solve with inputs resident in HBM. */
 pm_status pm_refactor(pm_handle *h, double *ms);

@@ -116,6 +116,10 @@ GPU_SYMBOLS = {
     "pm_interpolate_coarse": (C.c_int, [_P, C.c_int, C.c_void_p, C.c_void_p]),
     "pm_solve_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(c_double_p),
                                  C.POINTER(c_double_p), C.POINTER(PmResult), C.c_int]),
+    "pm_add_level_batch": (C.c_int, [_P, C.POINTER(PmLevelDesc), C.c_int]),
+    "pm_solve_fused": (C.c_int, [_P, C.POINTER(c_double_p), C.POINTER(c_double_p),
+                                 C.POINTER(PmResult)]),
+    "pm_n_systems": (C.c_int, [_P]),
     "pm_refactor": (C.c_int, [_P, c_double_p]),
     "pm_kernel_launches": (C.c_longlong, [_P]),
     "pm_device_bytes": (C.c_longlong, [_P]),

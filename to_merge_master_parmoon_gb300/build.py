@@ -29,6 +29,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
 GXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 GPU_CU = ["pm_api.cu", "pm_sparse.cu", "pm_vanka.cu", "pm_vanka_schur.cu", "pm_vanka_tma.cu",
+          "pm_batch.cu",
           "pm_learned.cu", "pm_mlp_tc.cu", "pm_assemble.cu",
           "pm_noalloc.cu", "pm_diag.cu"]
 GPU_CPP = ["pm_setup_host.cpp"]

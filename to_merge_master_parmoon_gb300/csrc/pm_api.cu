@@ -114,6 +114,12 @@ struct LevelDev {
   bool schur3() const { return diag == 1 && nl == NU_LOC; }
   size_t fac_bytes = 0;  // allocated factor storage
   uint64_t pattern_key = 0;  // fingerprint of the CSR patterns (pattern_fingerprint)
+  // stacked level of G systems (pm_add_level_batch): per-system layout and
+  // cells; the colour lists of all systems, kept while a solve sweeps only
+  // the systems still iterating
+  SegLayout seg;
+  int ncells_sys = 0;
+  std::vector<int> colour_full_ptr, colour_full_order;
 };
 template <>
 DevOp<double> LevelDev::op<double>() const {
@@ -210,6 +216,16 @@ struct pm_handle {
   int *d_on = nullptr;
   int l_on_host = 0;
   int l_fallbacks = 0;
+  // stacked systems (pm_add_level_batch / pm_solve_fused): system count,
+  // per-system flags (1 = still iterating), per-system scale factors, the
+  // native-layout staging vector, the coarse maps (stacked index -> s * nc +
+  // native index, and back) and whether the sweeps currently skip systems
+  int nsys = 1;
+  bool adding_stacked = false;
+  int *d_act = nullptr;
+  double *d_coef = nullptr, *stage = nullptr;
+  int *coarse_pos = nullptr, *coarse_sup = nullptr;
+  bool colours_restricted = false;
 };
 
 namespace {
@@ -296,6 +312,13 @@ pm_status upload(pm_handle *h, T **dst, const T *src, size_t count) {
     h->launches += _n;                                       \
   } while (0)
 
+// entry points of one system: not for a handle of stacked systems
+#define PM_SINGLE(h)                                                              \
+  do {                                                                            \
+    if ((h) && (h)->nsys > 1)                                                     \
+      return fail((h), PM_BADARG, "not available on a handle of stacked systems"); \
+  } while (0)
+
 bool mixed(const pm_handle *h) { return h->opt.precision == PM_PREC_MIXED; }
 // mixed mode stores each local block's FP32 inverse unless told otherwise
 bool use_inverse(const pm_handle *h) { return mixed(h) && h->opt.vanka_inverse != 0; }
@@ -319,7 +342,10 @@ pm_status sync(pm_handle *h, const char *what) {
 template <typename T>
 pm_status l20(pm_handle *h, T *p, int np) {
   if (!h->opt.project_pressure) return PM_OK;
-  PM_LAUNCH(launch_l20_project<T>(p, np, h->partials, h->counter, h->stream));
+  if (h->nsys > 1)  // stacked systems: each system's pressure block separately
+    PM_LAUNCH(launch_l20_seg<T>(p, np / h->nsys, h->nsys, h->stream));
+  else
+    PM_LAUNCH(launch_l20_project<T>(p, np, h->partials, h->counter, h->stream));
   return PM_OK;
 }
 
@@ -413,6 +439,12 @@ pm_status vanka_sweep(pm_handle *h, LevelDev &Lv, T *u, const T *rhs) {
 template <typename T>
 pm_status coarse_solve(pm_handle *h, LevelDev &Lv, const T *rhs, T *u) {
   // SolveExact with the inverse of the (pinned) coarse matrix, FP64 arithmetic
+  if (h->nsys > 1) {  // one inverse per stacked system, pinned at its first pressure DOF
+    const int pin = h->opt.project_pressure ? 3 * Lv.seg.nu : -1;
+    PM_LAUNCH((launch_dense_gemv_seg<T, T>(h->coarse_inv, h->coarse_n, h->nsys, h->coarse_sup,
+                                           rhs, u, pin, h->stream)));
+    return PM_OK;
+  }
   const int pin = h->opt.project_pressure ? 3 * Lv.nu : -1;
   PM_LAUNCH((launch_dense_gemv<T, T>(h->coarse_inv, h->coarse_n, rhs, u, pin, h->stream)));
   return PM_OK;
@@ -752,6 +784,243 @@ pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
   return PM_MAXIT;
 }
 
+// ---------------------------------------------------- stacked systems ----
+// While a fused solve runs, the Vanka sweeps of systems that have finished
+// are dropped from the colour lists (their vectors are zero from then on),
+// and the V-cycle graphs are captured again for the shorter lists.
+pm_status restrict_colours(pm_handle *h, const std::vector<int> &act) {
+  for (size_t l = 1; l < h->L.size(); ++l) {
+    LevelDev &Lv = h->L[l];
+    if (Lv.colour_full_ptr.empty()) {
+      Lv.colour_full_ptr = Lv.colouring.ptr;
+      Lv.colour_full_order = Lv.colouring.order;
+    }
+    const int ncol = (int)Lv.colour_full_ptr.size() - 1;
+    std::vector<int> ptr((size_t)ncol + 1, 0);
+    Lv.colouring.order.clear();
+    for (int k = 0; k < ncol; ++k) {
+      for (int q = Lv.colour_full_ptr[k]; q < Lv.colour_full_ptr[k + 1]; ++q) {
+        const int c = Lv.colour_full_order[(size_t)q];
+        if (act[(size_t)(c / Lv.ncells_sys)]) Lv.colouring.order.push_back(c);
+      }
+      ptr[(size_t)k + 1] = (int)Lv.colouring.order.size();
+    }
+    Lv.colouring.ptr = ptr;
+    if (!Lv.colouring.order.empty() &&
+        cudaMemcpyAsync(Lv.colour_cells, Lv.colouring.order.data(),
+                        sizeof(int) * Lv.colouring.order.size(), cudaMemcpyHostToDevice,
+                        h->stream) != cudaSuccess)
+      return cuda_fail(h, "colour lists");
+  }
+  drop_graphs(h);
+  h->colours_restricted = true;
+  return sync(h, "colour lists");
+}
+
+pm_status restore_colours(pm_handle *h) {
+  if (!h->colours_restricted) return PM_OK;
+  for (size_t l = 1; l < h->L.size(); ++l) {
+    LevelDev &Lv = h->L[l];
+    Lv.colouring.ptr = Lv.colour_full_ptr;
+    Lv.colouring.order = Lv.colour_full_order;
+    if (cudaMemcpyAsync(Lv.colour_cells, Lv.colouring.order.data(),
+                        sizeof(int) * Lv.colouring.order.size(), cudaMemcpyHostToDevice,
+                        h->stream) != cudaSuccess)
+      return cuda_fail(h, "colour lists");
+  }
+  drop_graphs(h);
+  h->colours_restricted = false;
+  return sync(h, "colour lists");
+}
+
+// TFgmresIte::Iterate (src/FE/FgmresIte.C:250-677) for G stacked systems in
+// lockstep: one Arnoldi process, Hessenberg matrix, Givens sequence and
+// stopping test per system, every device step (V-cycle, mat-vec, Gram-
+// Schmidt, updates) one launch over all systems.  A system leaves when it
+// meets its stopping test (its update is applied then), diverges or hits a
+// non-finite value; its vectors are zeroed and its sweeps dropped.  Returns
+// per-system results in res[0..G-1].
+pm_status fgmres_seg(pm_handle *h, double *x, const double *b, pm_result *res) {
+  LevelDev &F = h->L.back();
+  const int N = F.ndof, G = h->nsys;
+  const SegLayout &SL = F.seg;
+  int restart = h->opt.restart;
+  const int maxit = h->opt.maxit, minit = h->opt.minit;
+  if (restart > maxit) restart = maxit;
+  if (restart <= 0) restart = 10;
+  if (restart > h->restart) return fail(h, PM_BADARG, "restart larger than allocated");
+  const double red = h->opt.red_factor, resmin = h->opt.res_norm_min, divf = h->opt.div_factor;
+  const size_t R1 = (size_t)restart + 1;
+  std::vector<double> sv(R1 * G), cs(R1 * G), sn(R1 * G), y(R1), yall(R1 * G);
+  std::vector<double> H(R1 * restart * G, 0.0), col((R1 + 1) * G);
+  auto hh = [&](int s, int r, int c) -> double & {
+    return H[((size_t)s * R1 + r) * restart + c];
+  };
+  double *V = h->V, *Z = h->Z, *w = h->w;
+  auto v = [&](int k) { return V + (size_t)k * N; };
+  auto z = [&](int k) { return Z + (size_t)k * N; };
+  std::vector<int> act((size_t)G, 1);
+  std::vector<double> r0((size_t)G), res0((size_t)G), beta((size_t)G), resv((size_t)G);
+  std::vector<double> coef((size_t)G);
+  for (int s = 0; s < G; ++s) {
+    std::memset(&res[s], 0, sizeof(pm_result));
+    res[s].status = PM_OK;
+  }
+  auto upload_act = [&]() -> pm_status {
+    if (cudaMemcpyAsync(h->d_act, act.data(), sizeof(int) * G, cudaMemcpyHostToDevice,
+                        h->stream) != cudaSuccess)
+      return cuda_fail(h, "flag upload");
+    return PM_OK;
+  };
+  auto upload_coef = [&]() -> pm_status {
+    if (cudaMemcpyAsync(h->d_coef, coef.data(), sizeof(double) * G, cudaMemcpyHostToDevice,
+                        h->stream) != cudaSuccess)
+      return cuda_fail(h, "scale upload");
+    return PM_OK;
+  };
+  // systems that leave: flags, zeroed Arnoldi vector k, fewer sweeps
+  auto retire = [&](int k, const std::vector<int> &was) -> pm_status {
+    if (was == act) return PM_OK;
+    PM_TRY(upload_act());
+    for (int s = 0; s < G; ++s) coef[(size_t)s] = act[(size_t)s] ? 1.0 : 0.0;
+    PM_TRY(upload_coef());
+    PM_LAUNCH(launch_seg_scale(v(k), SL, h->d_coef, h->stream));
+    bool any = false;
+    for (int s = 0; s < G; ++s) any |= act[(size_t)s] != 0;
+    return any ? restrict_colours(h, act) : PM_OK;
+  };
+  auto any_active = [&]() {
+    for (int s = 0; s < G; ++s)
+      if (act[(size_t)s]) return true;
+    return false;
+  };
+  auto back_subst = [&](int s, int n) {  // y = H(0:n,0:n)^{-1} s(0:n) of system s
+    for (int k = 0; k < n; ++k) y[(size_t)k] = sv[(size_t)k * G + s];
+    for (int r = n - 1; r >= 0; --r) {
+      y[(size_t)r] /= hh(s, r, r);
+      for (int q = r - 1; q >= 0; --q) y[(size_t)q] -= hh(s, q, r) * y[(size_t)r];
+    }
+    for (int k = 0; k < n; ++k) yall[(size_t)k * G + s] = y[(size_t)k];
+  };
+  auto apply_updates = [&](int n) -> pm_status {  // x += Z yall (n columns)
+    if (n <= 0) return PM_OK;
+    if (cudaMemcpyAsync(h->ydev, yall.data(), sizeof(double) * (size_t)n * G,
+                        cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+      return cuda_fail(h, "y upload");
+    PM_LAUNCH(launch_seg_multi_axpy(x, Z, (size_t)N, h->ydev, n, SL, h->stream));
+    return PM_OK;
+  };
+
+  PM_TRY(upload_act());
+  PM_TRY(defect_nse4(h, x, b, v(0)));
+  PM_LAUNCH(launch_seg_dot(v(0), nullptr, SL, nullptr, h->partials, h->hcol, 1, true, h->stream));
+  PM_TRY(read_scalars(h, r0.data(), h->hcol, G));
+  std::vector<int> was = act;
+  for (int s = 0; s < G; ++s) {
+    res[s].res0 = res[s].res = r0[(size_t)s];
+    res0[(size_t)s] = beta[(size_t)s] = resv[(size_t)s] = r0[(size_t)s];
+    if (!std::isfinite(r0[(size_t)s])) {
+      res[s].status = PM_NAN;
+      act[(size_t)s] = 0;
+    } else if (r0[(size_t)s] <= resmin) {  // nothing to do (SC_MINIT is not applied here)
+      act[(size_t)s] = 0;
+    }
+  }
+  PM_TRY(retire(0, was));
+  int j = 1;
+  while (any_active() && j <= maxit) {
+    for (int s = 0; s < G; ++s)
+      coef[(size_t)s] = act[(size_t)s] ? 1.0 / beta[(size_t)s] : 0.0;
+    PM_TRY(upload_coef());
+    PM_LAUNCH(launch_seg_scale(v(0), SL, h->d_coef, h->stream));
+    std::fill(sv.begin(), sv.end(), 0.0);
+    for (int s = 0; s < G; ++s) sv[(size_t)s] = beta[(size_t)s];
+    int i;
+    for (i = 0; i < restart && j <= maxit; i++, j++) {
+      PM_TRY(precondition(h, z(i), v(i)));
+      for (int s = 0; s < G; ++s) res[s].vcycles += act[(size_t)s];
+      PM_LAUNCH(launch_coupled<double>(F.op<double>(), z(i), nullptr, w, false, false, h->stream));
+      // modified Gram-Schmidt per system, each step fused with the next dot
+      PM_LAUNCH(launch_seg_mgs(w, nullptr, nullptr, v(0), SL, h->d_act, h->partials, h->hcol,
+                               h->stream));
+      for (int k = 1; k <= i; ++k)
+        PM_LAUNCH(launch_seg_mgs(w, v(k - 1), h->hcol + (size_t)(k - 1) * G, v(k), SL, h->d_act,
+                                 h->partials, h->hcol + (size_t)k * G, h->stream));
+      PM_LAUNCH(launch_seg_mgs(w, v(i), h->hcol + (size_t)i * G, nullptr, SL, h->d_act,
+                               h->partials, h->hcol + (size_t)(i + 1) * G, h->stream));
+      PM_LAUNCH(launch_seg_scale_copy(v(i + 1), w, h->hcol + (size_t)(i + 1) * G, SL, h->d_act,
+                                      h->stream));
+      PM_TRY(read_scalars(h, col.data(), h->hcol, (i + 2) * G));
+      was = act;
+      bool finishing = false;
+      std::fill(yall.begin(), yall.end(), 0.0);
+      for (int s = 0; s < G; ++s) {
+        if (!act[(size_t)s]) continue;
+        bool bad = false;
+        for (int k = 0; k <= i + 1; ++k) {
+          hh(s, k, i) = col[(size_t)k * G + s];
+          if (!std::isfinite(hh(s, k, i))) bad = true;
+        }
+        if (bad) {
+          res[s].status = PM_NAN;
+          res[s].iterations = j;
+          res[s].res = NAN;
+          act[(size_t)s] = 0;
+          continue;
+        }
+        double *cs_s = &cs[(size_t)s * R1], *sn_s = &sn[(size_t)s * R1];
+        for (int k = 0; k < i; ++k) apply_rot(&hh(s, k, i), &hh(s, k + 1, i), cs_s[k], sn_s[k]);
+        gen_rot(hh(s, i, i), hh(s, i + 1, i), &cs_s[i], &sn_s[i]);
+        apply_rot(&hh(s, i, i), &hh(s, i + 1, i), cs_s[i], sn_s[i]);
+        apply_rot(&sv[(size_t)i * G + s], &sv[(size_t)(i + 1) * G + s], cs_s[i], sn_s[i]);
+        const double rv = std::fabs(sv[(size_t)(i + 1) * G + s]);
+        resv[(size_t)s] = rv;
+        res[s].res = rv;
+        res[s].iterations = j;
+        if (j >= minit &&
+            (rv < resmin || rv < red * (h->opt.red_initial ? r0[(size_t)s] : res0[(size_t)s]))) {
+          back_subst(s, i + 1);
+          finishing = true;
+          act[(size_t)s] = 0;
+        } else if (rv > divf * res0[(size_t)s]) {
+          res[s].status = PM_DIVERGED;
+          act[(size_t)s] = 0;
+        }
+      }
+      if (finishing) PM_TRY(apply_updates(i + 1));
+      PM_TRY(retire(i + 1, was));
+      if (!any_active()) break;
+    }
+    if (!any_active()) break;
+    // restart (src/FE/FgmresIte.C:574-590) of the systems still iterating
+    std::fill(yall.begin(), yall.end(), 0.0);
+    for (int s = 0; s < G; ++s)
+      if (act[(size_t)s]) back_subst(s, i);
+    PM_TRY(apply_updates(i));
+    PM_TRY(defect_nse4(h, x, b, v(0)));
+    PM_LAUNCH(launch_seg_dot(v(0), nullptr, SL, h->d_act, h->partials, h->hcol, 1, true,
+                             h->stream));
+    PM_TRY(read_scalars(h, col.data(), h->hcol, G));
+    was = act;
+    for (int s = 0; s < G; ++s) {
+      if (!act[(size_t)s]) continue;
+      res0[(size_t)s] = beta[(size_t)s] = resv[(size_t)s] = col[(size_t)s];
+      res[s].res = col[(size_t)s];
+      if (!std::isfinite(col[(size_t)s])) {
+        res[s].status = PM_NAN;
+        act[(size_t)s] = 0;
+      }
+    }
+    PM_TRY(retire(0, was));
+  }
+  for (int s = 0; s < G; ++s)
+    if (act[(size_t)s]) {
+      res[s].status = PM_MAXIT;
+      res[s].iterations = std::min(j, maxit);
+    }
+  return restore_colours(h);
+}
+
 // ------------------------------------------------------------- setup ------
 // Factor storage for the level's local solve: the 85x85 (or 49x49) LU with
 // its permutation, or the block-elimination data (one-block levels, and
@@ -982,9 +1251,23 @@ pm_status factor_all(pm_handle *h) {
                                             Lv.perm, false, false, h->status_d, h->stream));
   }
   LevelDev &C = h->L[0];
-  PM_LAUNCH(launch_coarse_assemble(C.op<double>(), h->coarse_lu, h->opt.project_pressure, h->stream));
-  PM_LAUNCH(launch_dense_lu(h->coarse_lu, h->coarse_n, h->coarse_ipiv, h->status_d, h->stream));
-  PM_LAUNCH(launch_dense_inverse(h->coarse_lu, h->coarse_ipiv, h->coarse_n, h->coarse_inv, h->stream));
+  if (h->nsys > 1) {  // one dense block per stacked system
+    const size_t nc = (size_t)h->coarse_n;
+    PM_LAUNCH(launch_coarse_assemble_seg(C.op<double>(), h->coarse_pos, h->coarse_n, h->nsys,
+                                         h->coarse_lu, h->opt.project_pressure, h->stream));
+    for (int s = 0; s < h->nsys; ++s) {
+      PM_LAUNCH(launch_dense_lu(h->coarse_lu + s * nc * nc, h->coarse_n, h->coarse_ipiv + s * nc,
+                                h->status_d, h->stream));
+      PM_LAUNCH(launch_dense_inverse(h->coarse_lu + s * nc * nc, h->coarse_ipiv + s * nc,
+                                     h->coarse_n, h->coarse_inv + s * nc * nc, h->stream));
+    }
+  } else {
+    PM_LAUNCH(launch_coarse_assemble(C.op<double>(), h->coarse_lu, h->opt.project_pressure,
+                                     h->stream));
+    PM_LAUNCH(launch_dense_lu(h->coarse_lu, h->coarse_n, h->coarse_ipiv, h->status_d, h->stream));
+    PM_LAUNCH(launch_dense_inverse(h->coarse_lu, h->coarse_ipiv, h->coarse_n, h->coarse_inv,
+                                   h->stream));
+  }
   cudaEventRecord(e1, h->stream);
   int st = 0;
   if (cudaMemcpyAsync(&st, h->status_d, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
@@ -1255,6 +1538,8 @@ pm_status pm_create(pm_handle **out, const pm_options *opt) {
 pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
   if (!h) return PM_BADARG;
   if (h->setup_done) return fail(h, PM_BADARG, "levels must be added before pm_setup");
+  if (h->nsys > 1 && !h->adding_stacked)
+    return fail(h, PM_BADARG, "a handle of stacked systems takes levels from pm_add_level_batch");
   if (!check_desc(h, d)) return PM_BADARG;
   if (cudaSetDevice(h->opt.device) != cudaSuccess) return cuda_fail(h, "set device");
   h->L.emplace_back();
@@ -1295,7 +1580,7 @@ pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
   PM_TRY(upload_padded(h, &Lv.b_col, d->b_col, (size_t)Lv.b_nnz));
   PM_TRY(upload(h, &Lv.bt_rowptr, d->bt_rowptr, (size_t)Lv.nu + 1));
   PM_TRY(upload_padded(h, &Lv.bt_col, d->bt_col, (size_t)Lv.bt_nnz));
-  if (h->opt.pin_host) {
+  if (h->opt.pin_host && !h->adding_stacked) {  // stacked arrays are temporary
     auto pin = [h](const void *p, size_t bytes) {
       if (!p || bytes < (1u << 20)) return;
       if (cudaHostRegister(const_cast<void *>(p), bytes, cudaHostRegisterPortable) == cudaSuccess) {
@@ -1313,7 +1598,47 @@ pm_status pm_add_level(pm_handle *h, const pm_level_desc *d) {
   PM_TRY(upload_values(h, Lv, d, true));
   PM_TRY(upload(h, &Lv.udofs, Lv.h_udofs.data(), Lv.h_udofs.size()));
   PM_TRY(upload(h, &Lv.pdofs, Lv.h_pdofs.data(), Lv.h_pdofs.size()));
+  Lv.seg.G = 1;
+  Lv.seg.nu = Lv.nu;
+  Lv.seg.na = Lv.nact;
+  Lv.seg.np = Lv.np;
+  Lv.ncells_sys = Lv.ncells;
   return sync(h, "add level");
+}
+
+pm_status pm_add_level_batch(pm_handle *h, const pm_level_desc *descs, int n_sys) {
+  if (!h || !descs || n_sys < 1) return PM_BADARG;
+  if (h->setup_done) return fail(h, PM_BADARG, "levels must be added before pm_setup");
+  if (h->L.empty())
+    h->nsys = n_sys;
+  else if (h->nsys != n_sys)
+    return fail(h, PM_BADARG, "every level of a stacked handle needs the same system count");
+  if (n_sys == 1) return pm_add_level(h, descs);
+  for (int s = 0; s < n_sys; ++s)
+    if (!check_desc(h, &descs[s])) return PM_BADARG;
+  StackSizes coarse;
+  if (!h->L.empty()) {
+    const LevelDev &K = h->L.back();
+    coarse.nu = K.seg.nu;
+    coarse.na = K.seg.na;
+    coarse.np = K.seg.np;
+    coarse.ncells = K.ncells_sys;
+  }
+  StackedLevel st;
+  pm_level_desc sd;
+  std::string err;
+  if (!stack_levels(descs, n_sys, coarse, st, sd, err)) return fail(h, PM_BADARG, err);
+  h->adding_stacked = true;
+  const pm_status r = pm_add_level(h, &sd);
+  h->adding_stacked = false;
+  if (r != PM_OK) return r;
+  LevelDev &Lv = h->L.back();
+  Lv.seg.G = n_sys;
+  Lv.seg.nu = descs[0].n_udof;
+  Lv.seg.na = descs[0].n_active;
+  Lv.seg.np = descs[0].n_pdof;
+  Lv.ncells_sys = descs[0].n_cells;
+  return PM_OK;
 }
 
 pm_status pm_setup(pm_handle *h) {
@@ -1381,7 +1706,8 @@ pm_status pm_setup(pm_handle *h) {
     PM_TRY(dalloc(h, &Lv.z64, (size_t)Lv.ndof));
   }
   (void)maxcol;
-  PM_TRY(dalloc(h, &h->partials, 8 * 152 + 64));
+  PM_TRY(dalloc(h, &h->partials,
+                std::max<size_t>(8 * 152 + 64, (size_t)seg_partials_size(h->L.back().seg))));
   PM_TRY(dalloc(h, &h->counter, 4));
   if (cudaMemsetAsync(h->counter, 0, 4 * sizeof(unsigned int), h->stream) != cudaSuccess)
     return cuda_fail(h, "counter reset");
@@ -1391,13 +1717,30 @@ pm_status pm_setup(pm_handle *h) {
     return cuda_fail(h, "flag reset");
   if (mixed(h) && launch_vanka_apply_tma_init() < 0) return cuda_fail(h, "bulk-copy apply set-up");
   h->restart = std::max(1, std::min(h->opt.restart, h->opt.maxit));
-  PM_TRY(dalloc(h, &h->hcol, (size_t)h->restart + 4));
-  PM_TRY(dalloc(h, &h->ydev, (size_t)h->restart + 4));
+  PM_TRY(dalloc(h, &h->hcol, ((size_t)h->restart + 4) * h->nsys));
+  PM_TRY(dalloc(h, &h->ydev, ((size_t)h->restart + 4) * h->nsys));
   LevelDev &C = h->L[0];
-  h->coarse_n = C.ndof;
-  PM_TRY(dalloc(h, &h->coarse_lu, (size_t)C.ndof * C.ndof));
-  PM_TRY(dalloc(h, &h->coarse_inv, (size_t)C.ndof * C.ndof));
+  // the coarse direct solve: one dense system, or one per stacked system
+  h->coarse_n = C.ndof / h->nsys;
+  const size_t ncoarse = (size_t)h->coarse_n * h->coarse_n * h->nsys;
+  PM_TRY(dalloc(h, &h->coarse_lu, ncoarse));
+  PM_TRY(dalloc(h, &h->coarse_inv, ncoarse));
   PM_TRY(dalloc(h, &h->coarse_ipiv, (size_t)C.ndof));
+  if (h->nsys > 1) {
+    std::vector<int> pos((size_t)C.ndof), sup((size_t)C.ndof);
+    const int nc = h->coarse_n;
+    for (int s = 0; s < h->nsys; ++s)
+      for (int l = 0; l < nc; ++l) {
+        const int q = (int)C.seg.stacked(s, l);
+        pos[(size_t)q] = s * nc + l;
+        sup[(size_t)s * nc + l] = q;
+      }
+    PM_TRY(upload(h, &h->coarse_pos, pos.data(), pos.size()));
+    PM_TRY(upload(h, &h->coarse_sup, sup.data(), sup.size()));
+    PM_TRY(dalloc(h, &h->d_act, (size_t)h->nsys));
+    PM_TRY(dalloc(h, &h->d_coef, (size_t)h->nsys));
+    PM_TRY(dalloc(h, &h->stage, (size_t)h->L.back().ndof));
+  }
   PM_TRY(dalloc(h, &h->coarse_b, (size_t)C.ndof));
   PM_TRY(dalloc(h, &h->coarse_x, (size_t)C.ndof));
   const size_t N = h->L.back().ndof;
@@ -1419,6 +1762,7 @@ pm_status pm_setup(pm_handle *h) {
 
 pm_status pm_update_matrices(pm_handle *h, const pm_level_desc *levels, int n) {
   if (!h || !levels) return PM_BADARG;
+  PM_SINGLE(h);
   if (!h->setup_done) return PM_NOT_SETUP;
   h->t_update0 = now_s();
   if (n != (int)h->L.size()) return fail(h, PM_BADARG, "level count mismatch");
@@ -1617,6 +1961,7 @@ pm_status pm_prolongate(pm_handle *h, int level, const double *coarse, double *f
 
 pm_status pm_solve_exact(pm_handle *h, const double *rhs, double *u) {
   PM_CHECK_LEVEL(h, 0);
+  PM_SINGLE(h);
   LevelDev &C = h->L[0];
   PM_TRY(h2d(h, C.x64, rhs, C.ndof));
   PM_LAUNCH(launch_dense_solve(h->coarse_lu, h->coarse_ipiv, h->coarse_n, C.x64, C.z64,
@@ -1634,6 +1979,7 @@ pm_status pm_vcycle(pm_handle *h, double *z, const double *v) {
 
 pm_status pm_solve_device(pm_handle *h, double *d_sol, const double *d_rhs, pm_result *out) {
   PM_CHECK_LEVEL(h, 0);
+  PM_SINGLE(h);
   pm_result r;
   std::memset(&r, 0, sizeof(r));
   cudaEvent_t e0, e1;
@@ -1675,6 +2021,67 @@ pm_status pm_solve(pm_handle *h, double *sol, const double *rhs, pm_result *out)
   return st != PM_OK ? st : s2;
 }
 
+pm_status pm_solve_fused(pm_handle *h, double *const *sols, const double *const *rhss,
+                         pm_result *results) {
+  PM_CHECK_LEVEL(h, 0);
+  if (!sols || !rhss) return PM_BADARG;
+  for (int s = 0; s < h->nsys; ++s)
+    if (!sols[s] || !rhss[s]) return PM_BADARG;
+  if (h->nsys == 1) return pm_solve(h, sols[0], rhss[0], results);
+  LevelDev &F = h->L.back();
+  const SegLayout &SL = F.seg;
+  const int G = h->nsys;
+  const size_t nd = (size_t)SL.ndof_sys();
+  // initial guesses and right-hand sides into the stacked layout
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int s = 0; s < G; ++s)
+      if (cudaMemcpyAsync(h->stage + (size_t)s * nd, pass == 0 ? sols[s] : rhss[s],
+                          sizeof(double) * nd, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+        return cuda_fail(h, "vector upload");
+    PM_LAUNCH(launch_seg_permute(pass == 0 ? h->xd : h->bd, h->stage, SL, true, h->stream));
+  }
+  std::vector<pm_result> r((size_t)G);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, h->stream);
+  pm_status st = fgmres_seg(h, h->xd, h->bd, r.data());
+  cudaEventRecord(e1, h->stream);
+  if (st == PM_OK) {  // true residual of every returned iterate (FP64)
+    std::vector<double> tr((size_t)G);
+    st = defect_nse4(h, h->xd, h->bd, h->w);
+    if (st == PM_OK) {
+      const int n = launch_seg_dot(h->w, nullptr, SL, nullptr, h->partials, h->hcol, 1, true,
+                                   h->stream);
+      st = n < 0 ? cuda_fail(h, "true residual") : read_scalars(h, tr.data(), h->hcol, G);
+      h->launches += n > 0 ? n : 0;
+    }
+    for (int s = 0; s < G && st == PM_OK; ++s) r[(size_t)s].true_res = tr[(size_t)s];
+  }
+  cudaStreamSynchronize(h->stream);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != PM_OK) return st;
+  PM_LAUNCH(launch_seg_permute(h->xd, h->stage, SL, false, h->stream));
+  for (int s = 0; s < G; ++s)
+    if (cudaMemcpyAsync(sols[s], h->stage + (size_t)s * nd, sizeof(double) * nd,
+                        cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+      return cuda_fail(h, "vector download");
+  PM_TRY(sync(h, "fused solve"));
+  pm_status first = PM_OK;
+  for (int s = 0; s < G; ++s) {
+    r[(size_t)s].solve_ms = ms;
+    r[(size_t)s].setup_ms = h->last_factor_ms;
+    if (results) results[s] = r[(size_t)s];
+    if (first == PM_OK && r[(size_t)s].status != PM_OK) first = (pm_status)r[(size_t)s].status;
+  }
+  return first;
+}
+
+int pm_n_systems(pm_handle *h) { return h ? h->nsys : 0; }
+
 static AsmOp asm_op(LevelDev &Lv) {
   AsmOp op{};
   op.nu = Lv.nu;
@@ -1710,6 +2117,7 @@ static pm_status assemble_impl(pm_handle *h, int level, const double *d_cell_h,
                                const double *d_conv, double nu, double c_mass, double c_a,
                                double b_scale, double bt_scale, bool sys) {
   PM_CHECK_LEVEL(h, level);
+  PM_SINGLE(h);
   if (!d_cell_h || !d_conv) return fail(h, PM_BADARG, "missing cell sizes or convection");
   LevelDev &Lv = h->L[level];
   if (Lv.ncells <= 0) return fail(h, PM_BADARG, "level without cells");
@@ -1801,6 +2209,7 @@ pm_status pm_assemble_system_level(pm_handle *h, int level, const double *cell_h
 pm_status pm_system_rhs(pm_handle *h, const double *old_rhs, const double *rhs, const double *sol,
                         double c_old, double c_new, double c2, double *out) {
   PM_CHECK_LEVEL(h, 0);
+  PM_SINGLE(h);
   if (!old_rhs || !rhs || !sol || !out) return PM_BADARG;
   LevelDev &F = h->L.back();
   if (!F.asm_theta)
@@ -1819,6 +2228,7 @@ pm_status pm_system_rhs_device(pm_handle *h, const double *d_old_rhs, const doub
                                const double *d_sol, double c_old, double c_new, double c2,
                                double *d_out) {
   PM_CHECK_LEVEL(h, 0);
+  PM_SINGLE(h);
   if (!d_old_rhs || !d_rhs || !d_sol || !d_out) return PM_BADARG;
   if (d_out == d_old_rhs || d_out == d_rhs || d_out == d_sol)
     return fail(h, PM_BADARG, "out aliases an input");
@@ -1864,6 +2274,7 @@ static pm_status build_coarse_nodes(pm_handle *h, int level) {
 
 pm_status pm_interpolate_coarse(pm_handle *h, int level, const double *d_fine, double *d_coarse) {
   PM_CHECK_LEVEL(h, level);
+  PM_SINGLE(h);
   if (level < 1 || !d_fine || !d_coarse) return PM_BADARG;
   LevelDev &F = h->L[level];
   if (!F.coarse_nodes) PM_TRY(build_coarse_nodes(h, level));
@@ -2037,6 +2448,7 @@ pm_status pm_mlp_adamw_step(pm_mlp *m, float lr, float beta1, float beta2, float
 
 pm_status pm_learned_attach(pm_handle *h, pm_mlp *m, double omega, double fallback_ratio) {
   if (!h) return PM_BADARG;
+  PM_SINGLE(h);
   if (!h->setup_done) return PM_NOT_SETUP;
   if (m && m->m.device != h->opt.device) return fail(h, PM_BADARG, "network on another device");
   if (m)
@@ -2071,6 +2483,7 @@ pm_status pm_learned_harvest(pm_handle *h, const double *sol_exact, const double
                              int n_cycles, float *d_X, float *d_T, long long capacity,
                              long long *n_pairs) {
   PM_CHECK_LEVEL(h, 0);
+  PM_SINGLE(h);
   if (!sol_exact || !rhs || !d_X || !d_T || !n_pairs || n_cycles <= 0) return PM_BADARG;
   LevelDev &F = h->L.back();
   if (*n_pairs < 0 || *n_pairs + (long long)n_cycles * F.ncells > capacity)

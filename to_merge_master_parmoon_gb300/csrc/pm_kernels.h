@@ -267,6 +267,80 @@ int launch_dense_inverse(const double *lu, const int *ipiv, int n, double *inv, 
 template <typename TB, typename TX>
 int launch_dense_gemv(const double *inv, int n, const TB *b, TX *x, int pin_row, cudaStream_t s);
 
+// ------------------------------------------------------- stacked systems ---
+// G systems of one mesh stacked into one level (pm_batch.cu): velocity
+// component c holds the G systems' na active DOFs (system s at c*G*nu +
+// s*na), then their nu - na Dirichlet DOFs (at c*G*nu + G*na + s*(nu-na));
+// the pressure block holds the systems' np DOFs one after the other (at
+// 3*G*nu + s*np).  nu, na, np are per system.  Seven ranges per system:
+// r = 2c (active part of component c), 2c+1 (its Dirichlet part), 6 (pressure).
+struct SegLayout {
+  int G = 1, nu = 0, na = 0, np = 0;
+  __host__ __device__ int ndof_sys() const { return 3 * nu + np; }
+  __host__ __device__ void range(int s, int r, long long &start, int &len) const {
+    const long long NU = (long long)G * nu;
+    if (r < 6) {
+      const int c = r >> 1;
+      if ((r & 1) == 0) {
+        start = c * NU + (long long)s * na;
+        len = na;
+      } else {
+        start = c * NU + (long long)G * na + (long long)s * (nu - na);
+        len = nu - na;
+      }
+    } else {
+      start = 3 * NU + (long long)s * np;
+      len = np;
+    }
+  }
+  // first native index ([u1 | u2 | u3 | p] of one system) of range r
+  __host__ __device__ int native_start(int r) const {
+    return r < 6 ? (r >> 1) * nu + ((r & 1) ? na : 0) : 3 * nu;
+  }
+  // stacked index of native index l of system s
+  __host__ __device__ long long stacked(int s, int l) const {
+    long long start;
+    int len;
+    int r = 6;
+    if (l < 3 * nu) r = 2 * (l / nu) + ((l % nu) >= na ? 1 : 0);
+    range(s, r, start, len);
+    return start + (l - native_start(r));
+  }
+};
+// partial-sum slots the segment reductions need
+int seg_partials_size(const SegLayout &L);
+// out[s*ostride] = <a, b> over system s (b == null: <a, a>; sqrt with norm);
+// systems with act[s] == 0 give 0 (act may be null: all active)
+int launch_seg_dot(const double *a, const double *b, const SegLayout &L, const int *act,
+                   double *partials, double *out, int ostride, bool norm, cudaStream_t s);
+// per system: w -= ha[s] * va (va != null), out[s] = <w, vd> (vd != null) or ||w||
+int launch_seg_mgs(double *w, const double *va, const double *ha, const double *vd,
+                   const SegLayout &L, const int *act, double *partials, double *out,
+                   cudaStream_t s);
+// v[system s] *= coef[s] (coef on the device)
+int launch_seg_scale(double *v, const SegLayout &L, const double *coef, cudaStream_t s);
+// v = w / h[s] where system s is active and h[s] != 0, else v = 0
+int launch_seg_scale_copy(double *v, const double *w, const double *h, const SegLayout &L,
+                          const int *act, cudaStream_t s);
+// x[system s] += sum_{k<nk} y[k*G + s] * Z[k*ld + :]
+int launch_seg_multi_axpy(double *x, const double *Z, size_t ld, const double *y, int nk,
+                          const SegLayout &L, cudaStream_t s);
+// stacked vector <-> G native vectors one after the other
+int launch_seg_permute(double *stacked, double *native, const SegLayout &L, bool to_stacked,
+                       cudaStream_t s);
+// L^2_0 projection of each of nsys consecutive pressure blocks of np_sys
+template <typename T>
+int launch_l20_seg(T *p, int np_sys, int nsys, cudaStream_t s);
+// one dense nc x nc coarse block per system (column-major, one after the
+// other) from a stacked coarse level; pos[i] = s*nc + native index of
+// stacked DOF i; each system's first pressure row pinned when projecting
+int launch_coarse_assemble_seg(const DevOp<double> &op, const int *pos, int nc, int nsys,
+                               double *blocks, int project_pressure, cudaStream_t s);
+// x = A_s^{-1} b per system through sup[s*nc + l] = stacked index of native l
+template <typename TB, typename TX>
+int launch_dense_gemv_seg(const double *inv, int nc, int nsys, const int *sup, const TB *b, TX *x,
+                          int pin, cudaStream_t s);
+
 }  // namespace pm
 
 #endif

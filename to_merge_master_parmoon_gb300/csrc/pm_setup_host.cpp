@@ -4,6 +4,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <string>
+#include <utility>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -289,6 +292,198 @@ bool make_colouring(int ncells, int nulocal, int nplocal, const int *udofs, cons
         sp[d] = k;
       }
     }
+  return true;
+}
+
+}  // namespace pm
+
+namespace pm {
+
+namespace {
+
+// stacked index of velocity DOF i of system s (n_active-first per component)
+inline int vmap(int G, int nu, int na, int s, int i) {
+  return i < na ? s * na + i : G * na + s * (nu - na) + (i - na);
+}
+
+// CSR rows in stacked order (rows_of(s, i) for stacked row R), columns mapped
+void stack_csr(int G, int rows_sys, const std::vector<std::pair<int, int>> &order,
+               const pm_level_desc *d, const int *pm_level_desc::*rp, const int *pm_level_desc::*cp,
+               int nnz_sys, const std::function<int(int, int)> &colmap, std::vector<int> &rowptr,
+               std::vector<int> &col, std::vector<long long> &src) {
+  (void)rows_sys;
+  rowptr.assign(order.size() + 1, 0);
+  col.clear();
+  col.reserve((size_t)G * nnz_sys);
+  src.clear();
+  src.reserve((size_t)G * nnz_sys);
+  for (size_t R = 0; R < order.size(); ++R) {
+    const int s = order[R].first, i = order[R].second;
+    const int *rowp = d[s].*rp;
+    const int *colp = d[s].*cp;
+    for (int j = rowp[i]; j < rowp[i + 1]; ++j) {
+      col.push_back(colmap(s, colp[j]));
+      src.push_back((long long)s * nnz_sys + j);
+    }
+    rowptr[R + 1] = (int)col.size();
+  }
+}
+
+void gather_vals(int G, const std::vector<long long> &src, const double *const *per_sys,
+                 int nnz_sys, std::vector<double> &out) {
+  (void)G;
+  out.resize(src.size());
+  for (size_t k = 0; k < src.size(); ++k) {
+    const long long q = src[k];
+    out[k] = per_sys[q / nnz_sys][q % nnz_sys];
+  }
+}
+
+}  // namespace
+
+bool stack_levels(const pm_level_desc *d, int G, const StackSizes &coarse, StackedLevel &st,
+                  pm_level_desc &out, std::string &err) {
+  const pm_level_desc &d0 = d[0];
+  for (int s = 1; s < G; ++s) {
+    const pm_level_desc &e = d[s];
+    if (e.n_udof != d0.n_udof || e.n_pdof != d0.n_pdof || e.n_active != d0.n_active ||
+        e.n_dirichlet != d0.n_dirichlet || e.hanging_bound != d0.hanging_bound ||
+        e.a_nnz != d0.a_nnz || e.b_nnz != d0.b_nnz || e.bt_nnz != d0.bt_nnz ||
+        e.n_cells != d0.n_cells || e.n_ulocal != d0.n_ulocal || e.n_plocal != d0.n_plocal ||
+        e.pu_nnz != d0.pu_nnz || e.pp_nnz != d0.pp_nnz) {
+      err = "stacked systems must have equal sizes on every level (system " +
+            std::to_string(s) + " differs)";
+      return false;
+    }
+    for (int k = 0; k < 9; ++k)
+      if ((e.a[k] != nullptr) != (d0.a[k] != nullptr)) {
+        err = "stacked systems must give the same A blocks";
+        return false;
+      }
+    if ((e.cell_colour != nullptr) != (d0.cell_colour != nullptr) ||
+        (e.cell_parent != nullptr) != (d0.cell_parent != nullptr) ||
+        (e.pu_rowptr != nullptr) != (d0.pu_rowptr != nullptr)) {
+      err = "stacked systems must give the same optional arrays";
+      return false;
+    }
+  }
+  const int nu = d0.n_udof, na = d0.n_active, np = d0.n_pdof, nc = d0.n_cells;
+  const int nl = d0.n_ulocal, npl = d0.n_plocal;
+  if ((long long)G * (3LL * nu + np) > 2000000000LL || (long long)G * d0.a_nnz > 2000000000LL) {
+    err = "stacked level too large for 32-bit indices";
+    return false;
+  }
+  // stacked velocity rows: the G systems' active rows, then their Dirichlet rows
+  std::vector<std::pair<int, int>> vrows;
+  vrows.reserve((size_t)G * nu);
+  for (int s = 0; s < G; ++s)
+    for (int i = 0; i < na; ++i) vrows.emplace_back(s, i);
+  for (int s = 0; s < G; ++s)
+    for (int i = na; i < nu; ++i) vrows.emplace_back(s, i);
+  std::vector<std::pair<int, int>> prows;
+  prows.reserve((size_t)G * np);
+  for (int s = 0; s < G; ++s)
+    for (int i = 0; i < np; ++i) prows.emplace_back(s, i);
+  auto vcol = [&](int s, int c) { return vmap(G, nu, na, s, c); };
+  auto pcol = [&](int s, int c) { return s * np + c; };
+  std::vector<long long> src;
+  std::vector<const double *> per((size_t)G);
+  stack_csr(G, nu, vrows, d, &pm_level_desc::a_rowptr, &pm_level_desc::a_col, d0.a_nnz, vcol,
+            st.a_rowptr, st.a_col, src);
+  for (int k = 0; k < 9; ++k) {
+    st.a[k].clear();
+    if (!d0.a[k]) continue;
+    for (int s = 0; s < G; ++s) per[(size_t)s] = d[s].a[k];
+    gather_vals(G, src, per.data(), d0.a_nnz, st.a[k]);
+  }
+  stack_csr(G, np, prows, d, &pm_level_desc::b_rowptr, &pm_level_desc::b_col, d0.b_nnz, vcol,
+            st.b_rowptr, st.b_col, src);
+  for (int k = 0; k < 3; ++k) {
+    for (int s = 0; s < G; ++s) per[(size_t)s] = d[s].b[k];
+    gather_vals(G, src, per.data(), d0.b_nnz, st.b[k]);
+  }
+  stack_csr(G, nu, vrows, d, &pm_level_desc::bt_rowptr, &pm_level_desc::bt_col, d0.bt_nnz, pcol,
+            st.bt_rowptr, st.bt_col, src);
+  for (int k = 0; k < 3; ++k) {
+    for (int s = 0; s < G; ++s) per[(size_t)s] = d[s].bt[k];
+    gather_vals(G, src, per.data(), d0.bt_nnz, st.bt[k]);
+  }
+  // cells, system after system
+  st.udofs.resize((size_t)G * nc * nl);
+  st.pdofs.resize((size_t)G * nc * npl);
+  for (int s = 0; s < G; ++s) {
+    for (size_t k = 0; k < (size_t)nc * nl; ++k)
+      st.udofs[(size_t)s * nc * nl + k] = vcol(s, d[s].cell_udofs[k]);
+    for (size_t k = 0; k < (size_t)nc * npl; ++k)
+      st.pdofs[(size_t)s * nc * npl + k] = pcol(s, d[s].cell_pdofs[k]);
+  }
+  st.parent.clear();
+  st.child.clear();
+  if (d0.cell_parent && d0.cell_child) {
+    st.parent.resize((size_t)G * nc);
+    st.child.resize((size_t)G * nc);
+    for (int s = 0; s < G; ++s)
+      for (int k = 0; k < nc; ++k) {
+        st.parent[(size_t)s * nc + k] = s * coarse.ncells + d[s].cell_parent[k];
+        st.child[(size_t)s * nc + k] = d[s].cell_child[k];
+      }
+  }
+  st.colour.clear();
+  if (d0.cell_colour) {
+    st.colour.resize((size_t)G * nc);
+    for (int s = 0; s < G; ++s)
+      std::memcpy(st.colour.data() + (size_t)s * nc, d[s].cell_colour, sizeof(int) * nc);
+  }
+  if (d0.pu_rowptr) {
+    auto cvcol = [&](int s, int c) { return vmap(G, coarse.nu, coarse.na, s, c); };
+    auto cpcol = [&](int s, int c) { return s * coarse.np + c; };
+    stack_csr(G, nu, vrows, d, &pm_level_desc::pu_rowptr, &pm_level_desc::pu_col, d0.pu_nnz,
+              cvcol, st.pu_rowptr, st.pu_col, src);
+    for (int s = 0; s < G; ++s) per[(size_t)s] = d[s].pu_val;
+    gather_vals(G, src, per.data(), d0.pu_nnz, st.pu_val);
+    stack_csr(G, np, prows, d, &pm_level_desc::pp_rowptr, &pm_level_desc::pp_col, d0.pp_nnz,
+              cpcol, st.pp_rowptr, st.pp_col, src);
+    for (int s = 0; s < G; ++s) per[(size_t)s] = d[s].pp_val;
+    gather_vals(G, src, per.data(), d0.pp_nnz, st.pp_val);
+  }
+  std::memset(&out, 0, sizeof(out));
+  out.n_udof = G * nu;
+  out.n_pdof = G * np;
+  out.n_active = G * na;
+  out.hanging_bound = G * na;
+  out.n_dirichlet = G * (nu - na);
+  out.a_nnz = (int)st.a_col.size();
+  out.a_rowptr = st.a_rowptr.data();
+  out.a_col = st.a_col.data();
+  for (int k = 0; k < 9; ++k) out.a[k] = st.a[k].empty() ? nullptr : st.a[k].data();
+  out.b_nnz = (int)st.b_col.size();
+  out.b_rowptr = st.b_rowptr.data();
+  out.b_col = st.b_col.data();
+  out.bt_nnz = (int)st.bt_col.size();
+  out.bt_rowptr = st.bt_rowptr.data();
+  out.bt_col = st.bt_col.data();
+  for (int k = 0; k < 3; ++k) {
+    out.b[k] = st.b[k].data();
+    out.bt[k] = st.bt[k].data();
+  }
+  out.n_cells = G * nc;
+  out.n_ulocal = nl;
+  out.n_plocal = npl;
+  out.cell_udofs = st.udofs.data();
+  out.cell_pdofs = st.pdofs.data();
+  out.cell_parent = st.parent.empty() ? nullptr : st.parent.data();
+  out.cell_child = st.child.empty() ? nullptr : st.child.data();
+  out.cell_colour = st.colour.empty() ? nullptr : st.colour.data();
+  if (d0.pu_rowptr) {
+    out.pu_nnz = (int)st.pu_col.size();
+    out.pu_rowptr = st.pu_rowptr.data();
+    out.pu_col = st.pu_col.data();
+    out.pu_val = st.pu_val.data();
+    out.pp_nnz = (int)st.pp_col.size();
+    out.pp_rowptr = st.pp_rowptr.data();
+    out.pp_col = st.pp_col.data();
+    out.pp_val = st.pp_val.data();
+  }
   return true;
 }
 

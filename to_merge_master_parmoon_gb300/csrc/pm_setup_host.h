@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include "pmgpu.h"
+
 namespace pm {
 
 struct HostCsr {
@@ -47,6 +49,25 @@ HostCsr transpose(const HostCsr &a);
 void build_neighbours(int ncells, const int *udofs, int nu, std::vector<int> &nbr);
 // 1 / (number of cells containing each velocity node)
 void node_inverse_multiplicity(int ncells, const int *udofs, int nu, std::vector<float> &inv);
+
+// G level descriptors of one mesh (equal sizes, nnz and local DOF counts;
+// values and patterns may differ) stacked into one block-diagonal level:
+// velocity DOF i of system s goes to s*na + i if i < na (na = n_active),
+// else to G*na + s*(nu - na) + (i - na), pressure DOF j to s*np + j, cell k
+// to s*ncells + k.  `coarse` gives the per-system sizes of the next coarser
+// stacked level (for parent cells and prolongation columns; ignored for the
+// coarsest).  The arrays live in `st`; `out` points into them.
+struct StackSizes {
+  int nu = 0, na = 0, np = 0, ncells = 0;
+};
+struct StackedLevel {
+  std::vector<int> a_rowptr, a_col, b_rowptr, b_col, bt_rowptr, bt_col;
+  std::vector<int> udofs, pdofs, parent, child, colour;
+  std::vector<int> pu_rowptr, pu_col, pp_rowptr, pp_col;
+  std::vector<double> a[9], b[3], bt[3], pu_val, pp_val;
+};
+bool stack_levels(const pm_level_desc *d, int G, const StackSizes &coarse, StackedLevel &st,
+                  pm_level_desc &out, std::string &err);
 
 }  // namespace pm
 

@@ -15,7 +15,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import PM_STATUS, PmOptions, PmResult, gpu_lib
+from ._lib import PM_STATUS, PmLevelDesc, PmOptions, PmResult, gpu_lib
 
 OPTION_NAMES = [f for f, _ in PmOptions._fields_]
 
@@ -295,3 +295,68 @@ def solve_batch(solvers, sols, rhss, nthreads=0, allow=(0,)):
         raise PmError(st, "pm_solve_batch")
     return sols, [R[i].as_dict() for i in range(n)]
 
+
+
+class PmFusedSolver(PmSolver):
+    """Independent systems on one mesh stacked into one block-diagonal
+    hierarchy (pm_add_level_batch): every V-cycle and FGMRES kernel covers all
+    of them in one launch, while each system keeps its own Arnoldi process,
+    Givens rotations, coarse inverse, L2_0 projection and stopping test.
+    ``systems[s][l]`` is the level-l descriptor of system s (equal sizes
+    across systems on every level)."""
+
+    def __init__(self, systems, **options):
+        super().__init__(None, **options)
+        G = len(systems)
+        L = len(systems[0])
+        if any(len(d) != L for d in systems):
+            raise ValueError("every stacked system needs the same number of levels")
+        for lev in range(L):
+            arr = (PmLevelDesc * G)(*[systems[s][lev] for s in range(G)])
+            self._check(self._lib.pm_add_level_batch(self._h, arr, G), "pm_add_level_batch")
+            d = systems[0][lev]
+            self._ndof.append(G * (3 * d.n_udof + d.n_pdof))
+        self.setup()
+        self.n_systems = G
+        self.ndof_sys = 3 * systems[0][-1].n_udof + systems[0][-1].n_pdof
+
+    def solve(self, sols, rhss, allow=(0,)):
+        """pm_solve_fused on host vectors (one per system, own layout);
+        returns (solutions, list of per-system result dicts)."""
+        G = self.n_systems
+        sols = [_f64(x).copy() for x in sols]
+        rhss = [_f64(b) for b in rhss]
+        X = (C.POINTER(C.c_double) * G)(*[_dp(x) for x in sols])
+        B = (C.POINTER(C.c_double) * G)(*[_dp(b) for b in rhss])
+        R = (PmResult * G)()
+        st = self._lib.pm_solve_fused(self._h, X, B, R)
+        if st not in allow:
+            self._check(st, "pm_solve_fused")
+        out = [R[i].as_dict() for i in range(G)]
+        for o in out:
+            o["status_name"] = PM_STATUS.get(o["status"], str(o["status"]))
+        return sols, out
+
+
+def solve_fused_groups(groups, sols, rhss, allow=(0,)):
+    """Several PmFusedSolver groups at once, one host thread per group (the
+    groups' streams overlap on the GPU).  sols[g] / rhss[g]: lists of the
+    group's vectors.  Returns (solutions, results) nested like the input."""
+    import threading
+    out = [None] * len(groups)
+    err = []
+
+    def run(g):
+        try:
+            out[g] = groups[g].solve(sols[g], rhss[g], allow=allow)
+        except Exception as e:  # reported after the join
+            err.append(e)
+
+    threads = [threading.Thread(target=run, args=(g,)) for g in range(len(groups))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if err:
+        raise err[0]
+    return [o[0] for o in out], [o[1] for o in out]
