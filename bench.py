@@ -714,41 +714,13 @@ def only_assembly(args):
 
 
 def train_network(device, args, log=None):
-    """The learned smoother's network: (residual, error) pairs harvested from
-    plain FP64 solves of 32^3 problems with nu log-uniform in [1e-3, 1e-1]
-    (seeds 1000+k), AdamW lr 1e-3, 20 epochs, all on the GPU.  Cached in the
+    """The learned smoother's network (learned.STANDARD_CONFIG: pairs
+    harvested from plain FP64 solves of 32^3 problems with nu log-uniform in
+    [1e-3, 1e-1], AdamW lr 1e-3, 20 epochs, all on the GPU), cached in the
     package's build folder keyed by the training configuration."""
-    import hashlib
-
-    import numpy as np
-    from to_merge_master_parmoon_gb300 import OseenProblem
-    from to_merge_master_parmoon_gb300.learned import Mlp, harvest_pairs, relative_loss, train
-    cfg = dict(levels=5, problems=args.train_problems, cycles=8, epochs=20, batch=4096, lr=1e-3,
-               seed=0, nu_range=(1e-3, 1e-1), features="neighbourhood-max-rms")
-    key = hashlib.sha1(json.dumps(cfg, sort_keys=True).encode()).hexdigest()[:12]
-    cache = ROOT / "to_merge_master_parmoon_gb300" / "_build" / f"mlp_{key}.npy"
-    net = Mlp(device=device, seed=cfg["seed"], max_batch=cfg["batch"])
-    info = {"config": cfg, "cached": cache.exists()}
-    if cache.exists():
-        net.set_params(np.load(cache))
-        return net, info
-    rng = np.random.default_rng(cfg["seed"])
-    lo, hi = np.log10(cfg["nu_range"][0]), np.log10(cfg["nu_range"][1])
-    t = time.perf_counter()
-    probs = [OseenProblem(n_levels=cfg["levels"], nu=float(10 ** rng.uniform(lo, hi)), seed=1000 + k)
-             for k in range(cfg["problems"])]
-    X, T = harvest_pairs(probs, n_cycles=cfg["cycles"], device=device, log=log)
-    info["harvest_s"] = time.perf_counter() - t
-    info["pairs"] = int(X.shape[0])
-    t = time.perf_counter()
-    hist = train(net, X, T, epochs=cfg["epochs"], batch=cfg["batch"], lr=cfg["lr"], seed=cfg["seed"])
-    info["train_s"] = time.perf_counter() - t
-    info["loss_first_last"] = [hist[0], hist[-1]]
-    info["relative_loss"] = relative_loss(net, X, T)
-    cache.parent.mkdir(parents=True, exist_ok=True)
-    np.save(cache, net.params())
-    del X, T
-    return net, info
+    from to_merge_master_parmoon_gb300.learned import standard_network
+    return standard_network(device, problems=args.train_problems,
+                            cache_dir=ROOT / "to_merge_master_parmoon_gb300" / "_build", log=log)
 
 
 def nu_study(args, device, net, threads, log=None):

@@ -149,6 +149,10 @@ typedef struct {
   long long max_device_bytes; /* cap on the device memory the handle
                              allocates (0: none); an allocation beyond it
                              fails with PM_OOM, as a failed cudaMalloc does  */
+  int learned_levels;     /* levels that run the learned post-smoothing step,
+                             counted from the finest: 1 (default) the finest
+                             level only, k > 1 the k finest, 0 every
+                             smoothed level                                */
 } pm_options;
 
 /* One multigrid level in the reference's data layout.  Levels are added
@@ -395,9 +399,11 @@ pm_status pm_profile_read(pm_handle *h, int kernel, double *ms_total, long long 
  * FP32 accumulation on the tensor cores) maps a cell's scaled local residual
  * plus 26 neighbour residual summaries (12 each) to a correction of the
  * cell's 85 DOFs.  Attached to a handle, it runs as one extra post-smoothing
- * step on every level; FGMRES switches it off for the rest of a solve when
- * the residual reduction of an iteration is worse than fallback_ratio, so
- * plain cell Vanka is the fallback.
+ * step on the pm_options.learned_levels finest levels (default: the finest
+ * only; 0: every smoothed level); FGMRES
+ * switches it off for the rest of a solve when the residual reduction of an
+ * iteration is worse than fallback_ratio and computes that iteration again
+ * with the plain V-cycle, so plain cell Vanka is the fallback.
  * Feature vector of cell c (divided by s_c = rms of its 85 local residual
  * entries): [local residual in local DOF order (u1 nodes, u2, u3, p modes)] then,
  * for each neighbour slot n = 0..25 (offsets (dx,dy,dz) in {-1,0,1}^3 \ 0,

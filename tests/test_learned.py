@@ -113,31 +113,39 @@ def test_harvest_and_training_reduce_loss(trained):
     assert after < before, (before, after)
 
 
-def test_learned_gain_over_plain(problems, trained):
-    """What the trained network gains: FGMRES iterations and the mean
-    residual reduction per iteration with and without the learned step
-    (printed; the learned solve must still reach the tolerance)."""
-    from to_merge_master_parmoon_gb300 import PmSolver
-    m = trained[0]
-    P = problems(3, 2e-2, 31)
+def test_learned_step_saves_an_iteration():
+    """What the trained network gains: the benchmark's network (pairs from 8
+    harvested 32^3 problems, 20 epochs, trained here on the GPU) on the 32^3
+    Oseen problem of the benchmark's family (nu = 1e-2, seed 1) solved to
+    1e-8 by FGMRES(20) with mixed-precision V(2,2) cycles: plain cell Vanka
+    takes 10 iterations; with the learned post-smoothing step on the finest
+    level the solve takes fewer, stays on (no fallback) and reaches the same
+    solution to 1e-6."""
+    from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
+    from to_merge_master_parmoon_gb300.learned import standard_network
+    net, info = standard_network(device=0)
+    P = OseenProblem(n_levels=5, nu=1e-2, seed=1)
     b = P.rhs()
-    nu3 = 3 * P.desc(2).n_udof
+    nu3 = 3 * P.desc(4).n_udof
     bp = b.copy()
     bp[nu3::4] -= bp[nu3::4].mean()
     r0 = np.linalg.norm(bp)
     out = {}
-    for name, net in (("plain", None), ("learned", m)):
-        S = PmSolver(P.descs, precision="mixed", restart=20, maxit=80, res_norm_min=1e-10 * r0)
-        if net is not None:
-            S.attach_learned(net, omega=1.0, fallback_ratio=0.5)
-        x, info = S.iterate(np.zeros_like(b), b)
-        out[name] = (info["iterations"], (info["true_res"] / r0) ** (1.0 / info["iterations"]))
-        assert info["true_res"] <= 1.05e-10 * r0
+    for name, m in (("plain", None), ("learned", net)):
+        S = PmSolver(P.descs, precision="mixed", restart=20, maxit=80, res_norm_min=1e-8 * r0)
+        if m is not None:
+            S.attach_learned(m, omega=1.0, fallback_ratio=0.5)
+        x, it = S.iterate(np.zeros_like(b), b)
+        assert it["true_res"] <= 1.05e-8 * r0
+        x[nu3::4] -= x[nu3::4].mean()
+        out[name] = (it["iterations"], x, S.learned_status() if m is not None else None)
         S.close()
-    print(f"learned-smoother gain on 8^3, nu=2e-2: iterations {out['plain'][0]} -> "
-          f"{out['learned'][0]}, mean reduction/iteration {out['plain'][1]:.3f} -> "
-          f"{out['learned'][1]:.3f}")
-    assert out["learned"][0] <= out["plain"][0] + 2
+    net.close()
+    print(f"learned step on 32^3, nu=1e-2: iterations {out['plain'][0]} -> "
+          f"{out['learned'][0]} (training relative loss {info['relative_loss']:.2f})")
+    assert out["learned"][2] == {"enabled": 1, "fallbacks": 0}
+    assert out["learned"][0] < out["plain"][0]
+    assert rel(out["learned"][1], out["plain"][1]) < 1e-6
 
 
 def test_learned_solve_matches_plain_solution_and_falls_back(problems, trained):

@@ -43,6 +43,7 @@ class PmOptions(C.Structure):
         ("pin_host", C.c_int), ("vanka_inverse", C.c_int), ("residual_variant", C.c_int),
         ("apply_variant", C.c_int), ("upload_mode", C.c_int), ("red_initial", C.c_int),
         ("decouple", C.c_int), ("wait_limit", C.c_int), ("max_device_bytes", C.c_longlong),
+        ("learned_levels", C.c_int),
     ]
 
 

@@ -540,7 +540,9 @@ pm_status cycle(pm_handle *h, int i) {
   PM_LAUNCH(launch_axpy<T>(u, (T)h->opt.beta, d, C.ndof, h->stream));
   PM_LAUNCH(launch_dirichlet<T>(u, (const T *)nullptr, C.nu, C.hb, C.ndir, h->stream));
   for (int s = 0; s < h->opt.post_smooth; ++s) PM_TRY(vanka_sweep<T>(h, C, u, f));
-  if (h->l_active) PM_TRY(learned_step<T>(h, C, u, f));
+  if (h->l_active &&
+      (h->opt.learned_levels <= 0 || i >= (int)h->L.size() - h->opt.learned_levels))
+    PM_TRY(learned_step<T>(h, C, u, f));
   return PM_OK;
 }
 
@@ -712,34 +714,43 @@ pm_status fgmres(pm_handle *h, double *x, const double *b, pm_result *res) {
     s[0] = beta;
     int i;
     for (i = 0; i < restart && j <= maxite; i++, j++) {
-      PM_TRY(precondition(h, z(i), v(i)));
-      res->vcycles++;
-      PM_LAUNCH(launch_coupled<double>(F.op<double>(), z(i), nullptr, w, false, false, h->stream));
-      // modified Gram-Schmidt, each step fused with the next dot product
-      PM_LAUNCH(launch_mgs_step(w, nullptr, nullptr, v(0), N, h->partials, h->counter, h->hcol,
-                                h->stream));
-      for (int k = 1; k <= i; ++k)
-        PM_LAUNCH(launch_mgs_step(w, v(k - 1), h->hcol + (k - 1), v(k), N, h->partials,
-                                  h->counter, h->hcol + k, h->stream));
-      PM_LAUNCH(launch_mgs_step(w, v(i), h->hcol + i, nullptr, N, h->partials, h->counter,
-                                h->hcol + i + 1, h->stream));
-      PM_LAUNCH(launch_scale_copy(v(i + 1), w, h->hcol + i + 1, N, h->stream));
-      PM_TRY(read_scalars(h, col.data(), h->hcol, i + 2));
-      for (int k = 0; k <= i + 1; ++k) hh(k, i) = col[k];
-      for (int k = 0; k <= i + 1; ++k)
-        if (!std::isfinite(col[k])) {
-          res->iterations = j;
-          res->res = col[k];
-          return fail(h, PM_NAN, "non-finite Arnoldi coefficient");
-        }
-      for (int k = 0; k < i; ++k) apply_rot(&hh(k, i), &hh(k + 1, i), cs[k], sn[k]);
-      gen_rot(hh(i, i), hh(i + 1, i), &cs[i], &sn[i]);
-      apply_rot(&hh(i, i), &hh(i + 1, i), cs[i], sn[i]);
-      apply_rot(&s[i], &s[i + 1], cs[i], sn[i]);
-      resv = std::fabs(s[i + 1]);
-      if (h->mlp && h->l_on_host && prev_res > 0.0 && resv > h->l_fallback * prev_res) {
+      for (int attempt = 0;; ++attempt) {
+        PM_TRY(precondition(h, z(i), v(i)));
+        res->vcycles++;
+        PM_LAUNCH(launch_coupled<double>(F.op<double>(), z(i), nullptr, w, false, false,
+                                         h->stream));
+        // modified Gram-Schmidt, each step fused with the next dot product
+        PM_LAUNCH(launch_mgs_step(w, nullptr, nullptr, v(0), N, h->partials, h->counter, h->hcol,
+                                  h->stream));
+        for (int k = 1; k <= i; ++k)
+          PM_LAUNCH(launch_mgs_step(w, v(k - 1), h->hcol + (k - 1), v(k), N, h->partials,
+                                    h->counter, h->hcol + k, h->stream));
+        PM_LAUNCH(launch_mgs_step(w, v(i), h->hcol + i, nullptr, N, h->partials, h->counter,
+                                  h->hcol + i + 1, h->stream));
+        PM_LAUNCH(launch_scale_copy(v(i + 1), w, h->hcol + i + 1, N, h->stream));
+        PM_TRY(read_scalars(h, col.data(), h->hcol, i + 2));
+        for (int k = 0; k <= i + 1; ++k) hh(k, i) = col[k];
+        for (int k = 0; k <= i + 1; ++k)
+          if (!std::isfinite(col[k])) {
+            res->iterations = j;
+            res->res = col[k];
+            return fail(h, PM_NAN, "non-finite Arnoldi coefficient");
+          }
+        const double s_i = s[i], s_i1 = s[i + 1];
+        for (int k = 0; k < i; ++k) apply_rot(&hh(k, i), &hh(k + 1, i), cs[k], sn[k]);
+        gen_rot(hh(i, i), hh(i + 1, i), &cs[i], &sn[i]);
+        apply_rot(&hh(i, i), &hh(i + 1, i), cs[i], sn[i]);
+        apply_rot(&s[i], &s[i + 1], cs[i], sn[i]);
+        resv = std::fabs(s[i + 1]);
+        if (!(h->mlp && h->l_on_host && prev_res > 0.0 && resv > h->l_fallback * prev_res))
+          break;
+        // the learned step failed the reduction test: off for the rest of the
+        // solve, and this column is computed again with the plain V-cycle, so
+        // that the rejected direction never enters the Krylov basis
         PM_TRY(set_learned_flag(h, 0));
         h->l_fallbacks++;
+        s[i] = s_i;
+        s[i + 1] = s_i1;
       }
       prev_res = resv;
       if (j >= minit && (resv < resmin || resv < red * (h->opt.red_initial ? r0 : res0))) {
@@ -1465,6 +1476,7 @@ void pm_default_options(pm_options *o) {
   o->decouple = 1;
   o->wait_limit = 0;
   o->max_device_bytes = 0;
+  o->learned_levels = 1;
 }
 
 const char *pm_status_string(int s) {
@@ -1508,7 +1520,8 @@ pm_status pm_create(pm_handle **out, const pm_options *opt) {
   if (o.residual_variant < -1 || o.residual_variant > 2) return PM_BADARG;
   if (o.apply_variant < -1 || o.apply_variant > 2) return PM_BADARG;
   if (o.upload_mode < 0 || o.upload_mode > 1) return PM_BADARG;
-  if (o.decouple < 0 || o.decouple > 1 || o.wait_limit < 0 || o.max_device_bytes < 0)
+  if (o.decouple < 0 || o.decouple > 1 || o.wait_limit < 0 || o.max_device_bytes < 0 ||
+      o.learned_levels < 0)
     return PM_BADARG;
   if (pm_device_count() <= 0) return PM_NO_DEVICE;
   if (cudaSetDevice(o.device) != cudaSuccess) {

@@ -4,18 +4,19 @@
 // in tensor memory.
 //
 // One CTA of eight warps (two warpgroups) per 128-row tile of A (UMMA shape
-// M = 128, N = the layer width 256 or 96, K = 16 per instruction).  K is staged through shared
-// memory in chunks of KC columns, in the K-major canonical layout without
-// swizzling: 8-row x 16-byte core matrices, LBO = 128 bytes between core
-// matrices along K, SBO = KC/8 * 128 bytes between 8-row groups.  Thread 0
-// issues the chunk's tcgen05.mma instructions and commits them to an
-// mbarrier, which every thread waits on (bounded) before the chunk buffers
-// are refilled.  The epilogue reads the accumulator with tcgen05.ld (warp w
-// owns TMEM lanes 32(w%4)..32(w%4)+31, i.e. tile rows 32(w%4)..+31; the two
-// warpgroups take alternate 32-column blocks), adds the bias,
-// applies GELU and writes FP32 and/or BF16 rows.  The TMEM columns (256 or
-// 128) are always released before the CTA exits; a barrier wait that gives
-// up sets PM_ERR_BULK_TIMEOUT in *err and skips the epilogue.
+// M = 128, N = the layer width 256 or 96, K = 16 per instruction).  K is
+// streamed in chunks of KC columns by TMA (cp.async.bulk.tensor) through a
+// ring of up to three shared-memory stages in the K-major canonical layout
+// without swizzling (8-row x 16-byte core matrices); thread 0 issues the
+// loads, thread 32 the tcgen05.mma instructions of each chunk as soon as its
+// bytes have landed, and the MMAs' commit frees the stage for the next loads,
+// so loads and MMAs overlap.  The epilogue reads the accumulator with
+// tcgen05.ld (warp w owns TMEM lanes 32(w%4)..32(w%4)+31, i.e. tile rows
+// 32(w%4)..+31; the two warpgroups take alternate 32-column blocks), adds the
+// bias, applies GELU and writes FP32 and/or BF16 rows.  The TMEM columns (256
+// or 128) are always released before the CTA exits; a barrier wait that
+// gives up sets PM_ERR_BULK_TIMEOUT in *err and skips the epilogue.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -29,9 +30,6 @@ namespace {
 
 constexpr int kTcThreads = 256;  // two warpgroups
 constexpr long long kTcMaxPolls = 1ll << 22;
-// dynamic shared memory per CTA: at most two CTAs per SM, so their TMEM
-// allocations (<= 256 columns each) always fit the SM's 512 columns
-constexpr int kTcSmem = 100 * 1024;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -84,7 +82,7 @@ __device__ __forceinline__ void tc_fence_after() {
 }
 
 struct TcArgs {
-  int M, lda, ldo;
+  int M, ldo;
   const __nv_bfloat16 *A, *W;
   const float *bias;
   int act;               // 0 identity, 1 GELU
@@ -95,26 +93,80 @@ struct TcArgs {
   int *err;
 };
 
+// one elected thread: 2-D tile (8 K-elements x `rows` rows) of a BF16 tensor
+// map into shared memory, completing on `bar` (transaction bytes)
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// Pipeline depth and chunking of a layer: K in chunks of KC columns (80 for
+// K = 400, 64 for K = 256), up to three chunks in flight.
 template <int N, int K>
-__global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
-  constexpr int KC = (K % 80 == 0) ? 80 : 64;  // K chunk (multiple of 16)
+struct TcPlan {
+  static constexpr int KC = (K % 80 == 0) ? 80 : 64;
+  static constexpr int NCH = K / KC;
+  static constexpr int S = NCH < 3 ? NCH : 3;
+  static constexpr int A_STAGE = 128 * KC * 2;  // bytes of the A tile of a chunk
+  static constexpr int W_STAGE = N * KC * 2;    // bytes of the W rows of a chunk
+  static constexpr int STAGE = A_STAGE + W_STAGE;
+  static constexpr int SMEM = S * STAGE;
   static_assert(K % KC == 0 && KC % 16 == 0, "K chunking");
   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "UMMA N for M = 128");
-  constexpr int NCH = K / KC;
-  constexpr int KB = KC / 8;                 // 16-byte units per row of a chunk
-  constexpr uint32_t SBO = KB * 128;         // bytes between 8-row groups
-  constexpr int A_BYTES = 128 * KC * 2;
+  static_assert(SMEM <= 200 * 1024, "stages fit in shared memory");
+};
+
+// Thread 0 streams the chunks with TMA (cp.async.bulk.tensor) into an
+// S-stage ring: per chunk KC/8 boxes of 8 K-elements x 128 rows of A and KC/8
+// boxes of 8 x N rows of W, each box one column of 8-row x 16-byte core
+// matrices, i.e. the K-major canonical layout without swizzling with LBO =
+// rows * 16 bytes (next 8 K-elements) and SBO = 128 bytes (next 8 rows).
+// Thread 32 waits for a chunk's bytes, issues its KC/16 tcgen05.mma and
+// commits them to the stage's `empty` barrier, which frees the stage for the
+// next TMA loads; the last commit goes to `done`.  Loads of later chunks so
+// overlap the MMAs of earlier ones.  Every wait is bounded; a wait that gives
+// up sets PM_ERR_BULK_TIMEOUT, the MMA thread still commits what it issued
+// to `done`, everyone waits (bounded) for that and for every load in
+// flight, and the TMEM columns are released before the CTA exits.
+template <int N, int K>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_mlp_layer_tc(const __grid_constant__ CUtensorMap mapA,
+                   const __grid_constant__ CUtensorMap mapW, TcArgs a) {
+  using PL = TcPlan<N, K>;
+  constexpr int KC = PL::KC, NCH = PL::NCH, S = PL::S;
   constexpr int NCOLS = N <= 128 ? 128 : 256;
-  static_assert(A_BYTES + N * KC * 2 <= kTcSmem, "chunk buffers fit");
   constexpr uint32_t IDESC = idesc_bf16(128, N);
+  constexpr uint32_t LBO_A = 128 * 16, LBO_W = N * 16, SBO = 128;
 
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t full[S], empty[S], done;
   __shared__ uint32_t tmem_slot;
+  __shared__ int failed, issued, consumed;
   if (a.on && *a.on == 0) return;  // uniform over the grid
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * 128;
-  unsigned char *As = smem, *Bs = smem + A_BYTES;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -122,47 +174,52 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
                  "r"(NCOLS)
                  : "memory");
   }
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
+  if (tid == 32) {
+    for (int st = 0; st < S; ++st) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], 1);
+    }
+    mbar_init(&done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    failed = 0;
+    issued = 0;
+    consumed = 0;
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = tmem_slot;
 
-  bool ok = true;
-  for (int c = 0; c < NCH; ++c) {
-    // stage the chunk: A rows m0..m0+127 (zeros past M) and all N rows of W
-    // thread u -> row r = 8 * (u / (8 KB)) + u % 8, 16-byte column kb =
-    // (u / 8) % KB: eight consecutive threads fill one 128-byte core matrix
-    // (conflict-free shared stores; the second half of each 32-byte global
-    // sector is read from L1 by the next eight threads)
-#pragma unroll 4
-    for (int u = tid; u < 128 * KB; u += kTcThreads) {
-      const int rl = u & 7, q = u >> 3, kb = q % KB, r = 8 * (q / KB) + rl;
-      const int gm = m0 + r;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (gm < a.M)
-        v = __ldg(reinterpret_cast<const uint4 *>(a.A + (size_t)gm * a.lda + c * KC + kb * 8));
-      *reinterpret_cast<uint4 *>(As + (r >> 3) * SBO + kb * 128 + (r & 7) * 16) = v;
+  if (tid == 0) {
+    // producer (lane 0 of warp 0; its other lanes wait at the __syncwarp
+    // below): chunk c into stage c % S once the MMAs of chunk c - S are done
+    int c = 0;
+    for (; c < NCH; ++c) {
+      const int st = c % S;
+      if (c >= S && !tc_wait(&empty[st], (uint32_t)((c / S - 1) & 1))) break;
+      if (*(volatile int *)&failed) break;
+      unsigned char *As = smem + st * PL::STAGE, *Ws = As + PL::A_STAGE;
+      mbar_expect_tx(&full[st], (uint32_t)PL::STAGE);
+#pragma unroll
+      for (int j = 0; j < KC / 8; ++j) {
+        tma_load_2d(As + j * (128 * 16), &mapA, c * KC + 8 * j, m0, &full[st]);
+        tma_load_2d(Ws + j * (N * 16), &mapW, c * KC + 8 * j, 0, &full[st]);
+      }
     }
-#pragma unroll 4
-    for (int u = tid; u < N * KB; u += kTcThreads) {
-      const int rl = u & 7, q = u >> 3, kb = q % KB, r = 8 * (q / KB) + rl;
-      const uint4 v =
-          __ldg(reinterpret_cast<const uint4 *>(a.W + (size_t)r * K + c * KC + kb * 8));
-      *reinterpret_cast<uint4 *>(Bs + (r >> 3) * SBO + kb * 128 + (r & 7) * 16) = v;
-    }
-    // make the generic-proxy stores visible to the tensor cores' async proxy
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
+    if (c < NCH) atomicOr(&failed, 1);
+    issued = c;
+  } else if (tid == 32) {
+    // MMA issuer
+    int c = 0;
+    for (; c < NCH; ++c) {
+      const int st = c % S;
+      if (!tc_wait(&full[st], (uint32_t)((c / S) & 1))) break;
       tc_fence_after();
+      const uint32_t as = smem_u32(smem + st * PL::STAGE), ws = as + PL::A_STAGE;
 #pragma unroll
       for (int kk = 0; kk < KC / 16; ++kk) {
-        const uint64_t ad = smem_desc(smem_u32(As) + kk * 256, 128, SBO);
-        const uint64_t bd = smem_desc(smem_u32(Bs) + kk * 256, 128, SBO);
+        const uint64_t ad = smem_desc(as + kk * 2 * LBO_A, LBO_A, SBO);
+        const uint64_t bd = smem_desc(ws + kk * 2 * LBO_W, LBO_W, SBO);
         const uint32_t accumulate = (c > 0 || kk > 0) ? 1u : 0u;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -171,16 +228,17 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
             "l"(ad), "l"(bd), "r"(IDESC), "r"(accumulate)
             : "memory");
       }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(&bar))
-          : "memory");
+      tc_commit(&empty[st]);
     }
-    // the chunk's MMAs are done before its buffers are refilled
-    const bool waited = tc_wait(&bar, (uint32_t)(c & 1));
-    ok = __syncthreads_and(waited) != 0;
-    if (!ok) break;
+    if (c < NCH) atomicOr(&failed, 1);
+    consumed = c;
+    tc_commit(&done);  // arrives once every MMA issued above has completed
   }
+  if (warp < 2) __syncwarp();
+  // all threads: the accumulator is complete (or the pipeline gave up)
+  const bool fin = tc_wait(&done, 0u);
+  __syncthreads();
+  const bool ok = fin && failed == 0;
   tc_fence_after();
 
   if (ok) {
@@ -240,12 +298,10 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
         }
       }
     }
-  } else {
-    // give the MMAs still in flight a last (bounded) chance before the
-    // columns are released
-    if (tid == 0) atomicOr(a.err, PM_ERR_BULK_TIMEOUT);
-    tc_wait(&bar, 0u);
-    tc_wait(&bar, 1u);
+  } else if (tid == 0) {
+    atomicOr(a.err, PM_ERR_BULK_TIMEOUT);
+    // loads issued but never consumed: let them land (bounded) before exit
+    for (int c = consumed; c < issued; ++c) tc_wait(&full[c % S], (uint32_t)((c / S) & 1));
   }
   tc_fence_before();
   __syncthreads();
@@ -258,17 +314,61 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_layer_tc(TcArgs a) {
 
 inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 
+// cuTensorMapEncodeTiled from the driver (no link against libcuda)
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                 const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                 const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled encode_fn() {
+  static EncodeTiled fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  }
+  return fn;
+}
+
+// 2-D BF16 map of a row-major [rows x cols] matrix (cols contiguous, row
+// pitch ld elements) read in boxes of 8 columns x box_rows rows; rows past
+// the end read as zeros
+bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int cols, int rows, int ld,
+              int box_rows) {
+  EncodeTiled f = encode_fn();
+  if (!f) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(__nv_bfloat16)};
+  const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1u, 1u};
+  return f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(base), dims,
+           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int N, int K>
-int launch_layer(const TcArgs &a, cudaStream_t s) {
+int set_smem_limit() {
+  return cudaFuncSetAttribute(k_mlp_layer_tc<N, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              TcPlan<N, K>::SMEM) == cudaSuccess
+             ? 0
+             : -1;
+}
+
+template <int N, int K>
+int launch_layer(const TcArgs &a, int lda, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(k_mlp_layer_tc<N, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kTcSmem) != cudaSuccess)
-      return -1;
+    if (set_smem_limit<N, K>() < 0) return -1;
     attr = true;
   }
+  CUtensorMap ma, mw;
+  if (!make_map(&ma, a.A, K, a.M, lda, 128) || !make_map(&mw, a.W, K, N, K, N)) return -1;
   const int grid = (a.M + 127) / 128;
-  k_mlp_layer_tc<N, K><<<grid, kTcThreads, kTcSmem, s>>>(a);
+  k_mlp_layer_tc<N, K><<<grid, kTcThreads, TcPlan<N, K>::SMEM, s>>>(ma, mw, a);
   return ok() < 0 ? -1 : 1;
 }
 
@@ -276,12 +376,10 @@ int launch_layer(const TcArgs &a, cudaStream_t s) {
 
 int mlp_tc_init() {
   int r = 0;
-  r |= cudaFuncSetAttribute(k_mlp_layer_tc<kMlpHidden, kMlpInPad>,
-                            cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-  r |= cudaFuncSetAttribute(k_mlp_layer_tc<kMlpHidden, kMlpHidden>,
-                            cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-  r |= cudaFuncSetAttribute(k_mlp_layer_tc<kMlpOutPad, kMlpHidden>,
-                            cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  r |= set_smem_limit<kMlpHidden, kMlpInPad>();
+  r |= set_smem_limit<kMlpHidden, kMlpHidden>();
+  r |= set_smem_limit<kMlpOutPad, kMlpHidden>();
+  if (!encode_fn()) r = -1;
   return r == 0 ? 0 : -1;
 }
 
@@ -302,17 +400,14 @@ int mlp_layer_tc(int layer, const __nv_bfloat16 *A, int M, const __nv_bfloat16 *
   a.err = err;
   switch (layer) {
     case 1:
-      a.lda = kMlpInPad;
       a.ldo = kMlpHidden;
-      return launch_layer<kMlpHidden, kMlpInPad>(a, s);
+      return launch_layer<kMlpHidden, kMlpInPad>(a, kMlpInPad, s);
     case 2:
-      a.lda = kMlpHidden;
       a.ldo = kMlpHidden;
-      return launch_layer<kMlpHidden, kMlpHidden>(a, s);
+      return launch_layer<kMlpHidden, kMlpHidden>(a, kMlpHidden, s);
     case 3:
-      a.lda = kMlpHidden;
       a.ldo = kMlpOutPad;
-      return launch_layer<kMlpOutPad, kMlpHidden>(a, s);
+      return launch_layer<kMlpOutPad, kMlpHidden>(a, kMlpHidden, s);
     default:
       return -1;
   }

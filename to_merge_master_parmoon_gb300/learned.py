@@ -216,3 +216,50 @@ def relative_loss(mlp: Mlp, X, T, batch: int = 8192) -> float:
         num += float(((y - tb) ** 2).sum())
         den += float((tb ** 2).sum())
     return num / max(den, 1e-300)
+
+
+# the benchmark's training configuration: pairs harvested from plain FP64
+# solves of 32^3 problems (5 levels) with nu log-uniform in [1e-3, 1e-1]
+# (seeds 1000+k), 8 cycles each, AdamW lr 1e-3, 20 epochs of batches of 4096
+STANDARD_CONFIG = dict(levels=5, problems=8, cycles=8, epochs=20, batch=4096, lr=1e-3, seed=0,
+                       nu_range=(1e-3, 1e-1), features="neighbourhood-max-rms")
+
+
+def standard_network(device: int = 0, problems: int | None = None, cache_dir=None, log=None):
+    """The network of STANDARD_CONFIG (``problems`` overrides the number of
+    harvested problems), trained on the GPU; with ``cache_dir`` the weights
+    are kept there keyed by the configuration.  Returns (Mlp, info dict)."""
+    import hashlib
+    import json
+    from pathlib import Path
+
+    from .problem import OseenProblem
+    cfg = dict(STANDARD_CONFIG)
+    if problems is not None:
+        cfg["problems"] = problems
+    key = hashlib.sha1(json.dumps(cfg, sort_keys=True).encode()).hexdigest()[:12]
+    cache = Path(cache_dir) / f"mlp_{key}.npy" if cache_dir is not None else None
+    net = Mlp(device=device, seed=cfg["seed"], max_batch=cfg["batch"])
+    info = {"config": cfg, "cached": bool(cache is not None and cache.exists())}
+    if info["cached"]:
+        net.set_params(np.load(cache))
+        return net, info
+    rng = np.random.default_rng(cfg["seed"])
+    lo, hi = np.log10(cfg["nu_range"][0]), np.log10(cfg["nu_range"][1])
+    t = time.perf_counter()
+    probs = [OseenProblem(n_levels=cfg["levels"], nu=float(10 ** rng.uniform(lo, hi)),
+                          seed=1000 + k) for k in range(cfg["problems"])]
+    X, T = harvest_pairs(probs, n_cycles=cfg["cycles"], device=device, log=log)
+    info["harvest_s"] = time.perf_counter() - t
+    info["pairs"] = int(X.shape[0])
+    t = time.perf_counter()
+    hist = train(net, X, T, epochs=cfg["epochs"], batch=cfg["batch"], lr=cfg["lr"],
+                 seed=cfg["seed"])
+    info["train_s"] = time.perf_counter() - t
+    info["loss_first_last"] = [hist[0], hist[-1]]
+    info["relative_loss"] = relative_loss(net, X, T)
+    if cache is not None:
+        cache.parent.mkdir(parents=True, exist_ok=True)
+        np.save(cache, net.params())
+    del X, T
+    return net, info
