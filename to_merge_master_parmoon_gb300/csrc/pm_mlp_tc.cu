@@ -3,23 +3,22 @@
 // K contiguous) and W [N x K] BF16 (weights, K contiguous), FP32 accumulation
 // in tensor memory.
 //
-// One CTA of eight warps (two warpgroups) per 128-row tile of A (UMMA shape
-// M = 128, N = the layer width 256 or 96, K = 16 per instruction).  K is
-// streamed in chunks of KC columns by TMA (cp.async.bulk.tensor) through a
-// ring of up to three shared-memory stages in the K-major canonical layout
-// without swizzling (8-row x 16-byte core matrices); thread 0 issues the
-// loads, thread 32 the tcgen05.mma instructions of each chunk as soon as its
-// bytes have landed, and the MMAs' commit frees the stage for the next loads,
-// so loads and MMAs overlap.  The epilogue reads the accumulator with
-// tcgen05.ld (warp w owns TMEM lanes 32(w%4)..32(w%4)+31, i.e. tile rows
-// 32(w%4)..+31; the two warpgroups take alternate 32-column blocks), adds the
-// bias, applies GELU and writes FP32 and/or BF16 rows.  The TMEM columns (256
-// or 128) are always released before the CTA exits; a barrier wait that
-// gives up sets PM_ERR_BULK_TIMEOUT in *err and skips the epilogue.
+// Persistent CTAs (one per SM for the 256-wide layers) walk the 128-row
+// tiles of A (UMMA shape M = 128, N = the layer width 256 or 96, K = 16 per
+// instruction) with warp specialisation: one thread streams the K chunks by
+// TMA (cp.async.bulk.tensor) through a three-stage shared-memory ring in the
+// K-major canonical layout without swizzling, one thread issues the
+// tcgen05.mma of each chunk as soon as its bytes have landed, into one of two
+// TMEM accumulators, and eight warps drain the other accumulator (tcgen05.ld,
+// bias, GELU, FP32 and/or BF16 rows), so loads, MMAs and the epilogue of
+// consecutive tiles overlap.  The TMEM columns are always released before
+// the CTA exits; a barrier wait that gives up sets PM_ERR_BULK_TIMEOUT in
+// *err and stops the pipeline.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "pm_learned.h"
@@ -28,7 +27,6 @@ namespace pm {
 
 namespace {
 
-constexpr int kTcThreads = 256;  // two warpgroups
 constexpr long long kTcMaxPolls = 1ll << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -39,12 +37,14 @@ __device__ __forceinline__ float gelu_tc(float x) {
   return 0.5f * x * (1.f + erff(x * 0.70710678118654752f));
 }
 
-// shared-memory matrix descriptor: K-major, no swizzle (sm_100 layout:
-// start >> 4 in bits 0-13, LBO >> 4 in 16-29, SBO >> 4 in 32-45, version 1 in
-// bits 46-47, swizzle mode 0 in bits 61-63)
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+// shared-memory matrix descriptor of a K-major operand in the 128-byte
+// swizzled layout that TMA writes with CU_TENSOR_MAP_SWIZZLE_128B: rows of
+// 64 BF16 (128 bytes), 8-row atoms of 1024 bytes (SBO), LBO unused (1),
+// version 1, layout type 2 (128-byte swizzle); the K = 16 slices of an atom
+// start 32 bytes apart
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | (1ull << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         (1ull << 46) | (2ull << 61);
 }
 
 // instruction descriptor of kind::f16: D F32, A and B BF16, both K-major
@@ -122,66 +122,86 @@ __device__ __forceinline__ void tc_commit(uint64_t *bar) {
       : "memory");
 }
 
-// Pipeline depth and chunking of a layer: K in chunks of KC columns (80 for
-// K = 400, 64 for K = 256), up to three chunks in flight.
+// Pipeline depth and chunking of a layer: K in chunks of 64 columns (one
+// 128-byte swizzle atom per row; the last chunk of K = 400 reads columns
+// 400..447 as zeros), up to three chunks in flight; two accumulators of
+// NCOLS TMEM columns (512 for N = 256: one CTA per SM; 256 for N = 96).
 template <int N, int K>
 struct TcPlan {
-  static constexpr int KC = (K % 80 == 0) ? 80 : 64;
-  static constexpr int NCH = K / KC;
-  static constexpr int S = NCH < 3 ? NCH : 3;
+  static constexpr int KC = 64;
+  static constexpr int NCH = (K + KC - 1) / KC;
+  static constexpr int S = 3;
   static constexpr int A_STAGE = 128 * KC * 2;  // bytes of the A tile of a chunk
   static constexpr int W_STAGE = N * KC * 2;    // bytes of the W rows of a chunk
   static constexpr int STAGE = A_STAGE + W_STAGE;
   static constexpr int SMEM = S * STAGE;
-  static_assert(K % KC == 0 && KC % 16 == 0, "K chunking");
+  static constexpr int NCOLS = N <= 128 ? 128 : 256;
+  static constexpr int CTAS_PER_SM = 512 / (2 * NCOLS);
+  static_assert(KC % 16 == 0 && STAGE % 1024 == 0, "K chunking, 1024-byte atoms");
   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "UMMA N for M = 128");
   static_assert(SMEM <= 200 * 1024, "stages fit in shared memory");
 };
 
-// Thread 0 streams the chunks with TMA (cp.async.bulk.tensor) into an
-// S-stage ring: per chunk KC/8 boxes of 8 K-elements x 128 rows of A and KC/8
-// boxes of 8 x N rows of W, each box one column of 8-row x 16-byte core
-// matrices, i.e. the K-major canonical layout without swizzling with LBO =
-// rows * 16 bytes (next 8 K-elements) and SBO = 128 bytes (next 8 rows).
-// Thread 32 waits for a chunk's bytes, issues its KC/16 tcgen05.mma and
-// commits them to the stage's `empty` barrier, which frees the stage for the
-// next TMA loads; the last commit goes to `done`.  Loads of later chunks so
-// overlap the MMAs of earlier ones.  Every wait is bounded; a wait that gives
-// up sets PM_ERR_BULK_TIMEOUT, the MMA thread still commits what it issued
-// to `done`, everyone waits (bounded) for that and for every load in
-// flight, and the TMEM columns are released before the CTA exits.
+constexpr int kTcWarps = 10;  // producer, MMA issuer, eight epilogue warps
+constexpr int kEpiWarps = 8;
+
+// Persistent, warp-specialised layer: each CTA walks the 128-row tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ...
+// * warp 0, lane 0 streams every tile's K chunks with TMA
+//   (cp.async.bulk.tensor) into an S-stage ring: per chunk one box of 64
+//   K-elements x 128 rows of A and one of 64 x N rows of W, written by TMA in
+//   the 128-byte swizzled K-major layout (8-row atoms of 1024 bytes) that
+//   the MMA descriptors name;
+// * warp 1, lane 0 issues a chunk's KC/16 tcgen05.mma once its bytes have
+//   landed, into accumulator (tile & 1), commits them to the stage's `empty`
+//   barrier (freeing it for the producer) and, after a tile's last chunk, to
+//   the accumulator's `tfull` barrier;
+// * warps 2..9 drain an accumulator with tcgen05.ld (warp w reads TMEM lanes
+//   32(w%4)..+31 = tile rows, the two groups of four alternate 32-column
+//   blocks), add the bias, apply GELU, store FP32 and/or BF16 rows and
+//   release the accumulator (`tempty`), while the MMAs of the next tile run
+//   into the other one.
+// Every wait is bounded.  A wait that gives up sets PM_ERR_BULK_TIMEOUT and
+// a shared flag that stops the other roles; the MMA thread still commits its
+// MMAs to `done`, which all threads wait for (bounded), the producer waits
+// for its loads in flight, and the TMEM columns are released before exit.
 template <int N, int K>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcWarps * 32, 1)
     k_mlp_layer_tc(const __grid_constant__ CUtensorMap mapA,
                    const __grid_constant__ CUtensorMap mapW, TcArgs a) {
   using PL = TcPlan<N, K>;
-  constexpr int KC = PL::KC, NCH = PL::NCH, S = PL::S;
-  constexpr int NCOLS = N <= 128 ? 128 : 256;
+  constexpr int KC = PL::KC, NCH = PL::NCH, S = PL::S, NCOLS = PL::NCOLS;
   constexpr uint32_t IDESC = idesc_bf16(128, N);
-  constexpr uint32_t LBO_A = 128 * 16, LBO_W = N * 16, SBO = 128;
 
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t full[S], empty[S], done;
+  __shared__ __align__(8) uint64_t full[S], empty[S], tfull[2], tempty[2], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int failed, issued, consumed;
   if (a.on && *a.on == 0) return;  // uniform over the grid
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * 128;
+  const int ntiles = (a.M + 127) / 128;
+  const int mine = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_slot)),
-                 "r"(NCOLS)
+                 "r"(2 * NCOLS)
                  : "memory");
   }
-  if (tid == 32) {
+  if (tid == 0) {
     for (int st = 0; st < S; ++st) {
       mbar_init(&full[st], 1);
       mbar_init(&empty[st], 1);
     }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], kEpiWarps);
+    }
     mbar_init(&done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    failed = 0;
+    // the swizzled stages need 1024-byte alignment: otherwise nothing is
+    // loaded and the layer reports the error flag
+    failed = (smem_u32(smem) & 1023u) != 0 ? 1 : 0;
     issued = 0;
     consumed = 0;
   }
@@ -189,124 +209,162 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = tmem_slot;
+  volatile int *vfailed = &failed;
 
-  if (tid == 0) {
-    // producer (lane 0 of warp 0; its other lanes wait at the __syncwarp
-    // below): chunk c into stage c % S once the MMAs of chunk c - S are done
-    int c = 0;
-    for (; c < NCH; ++c) {
-      const int st = c % S;
-      if (c >= S && !tc_wait(&empty[st], (uint32_t)((c / S - 1) & 1))) break;
-      if (*(volatile int *)&failed) break;
-      unsigned char *As = smem + st * PL::STAGE, *Ws = As + PL::A_STAGE;
-      mbar_expect_tx(&full[st], (uint32_t)PL::STAGE);
-#pragma unroll
-      for (int j = 0; j < KC / 8; ++j) {
-        tma_load_2d(As + j * (128 * 16), &mapA, c * KC + 8 * j, m0, &full[st]);
-        tma_load_2d(Ws + j * (N * 16), &mapW, c * KC + 8 * j, 0, &full[st]);
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: global chunk g = it * NCH + c into stage g % S once the
+      // MMAs of chunk g - S are done
+      int g = 0;
+      for (int it = 0; it < mine && !*vfailed; ++it) {
+        const int m0 = (blockIdx.x + it * gridDim.x) * 128;
+        for (int c = 0; c < NCH; ++c, ++g) {
+          const int st = g % S;
+          if ((g >= S && !tc_wait(&empty[st], (uint32_t)((g / S - 1) & 1))) || *vfailed) {
+            atomicOr(&failed, 1);
+            break;
+          }
+          unsigned char *As = smem + st * PL::STAGE, *Ws = As + PL::A_STAGE;
+          mbar_expect_tx(&full[st], (uint32_t)PL::STAGE);
+          tma_load_2d(As, &mapA, c * KC, m0, &full[st]);
+          tma_load_2d(Ws, &mapW, c * KC, 0, &full[st]);
+        }
       }
+      issued = g;
     }
-    if (c < NCH) atomicOr(&failed, 1);
-    issued = c;
-  } else if (tid == 32) {
-    // MMA issuer
-    int c = 0;
-    for (; c < NCH; ++c) {
-      const int st = c % S;
-      if (!tc_wait(&full[st], (uint32_t)((c / S) & 1))) break;
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int g = 0;
+      for (int it = 0; it < mine && !*vfailed; ++it) {
+        const int b = it & 1;
+        if (it >= 2 && !tc_wait(&tempty[b], (uint32_t)((it / 2 - 1) & 1))) {
+          atomicOr(&failed, 1);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc = tbase + (uint32_t)(b * NCOLS);
+        bool ok = true;
+        for (int c = 0; c < NCH; ++c, ++g) {
+          const int st = g % S;
+          if (!tc_wait(&full[st], (uint32_t)((g / S) & 1)) || *vfailed) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t as = smem_u32(smem + st * PL::STAGE), ws = as + PL::A_STAGE;
+#pragma unroll
+          for (int kk = 0; kk < KC / 16; ++kk) {
+            const uint64_t ad = smem_desc_sw128(as + kk * 32);
+            const uint64_t bd = smem_desc_sw128(ws + kk * 32);
+            const uint32_t accumulate = (c > 0 || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "setp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(acc),
+                "l"(ad), "l"(bd), "r"(IDESC), "r"(accumulate)
+                : "memory");
+          }
+          tc_commit(&empty[st]);
+        }
+        if (!ok) {
+          atomicOr(&failed, 1);
+          break;
+        }
+        tc_commit(&tfull[b]);
+      }
+      consumed = g;
+      tc_commit(&done);  // arrives once every MMA issued above has completed
+    }
+    __syncwarp();
+  } else {
+    // epilogue warps
+    const int q = warp & 3, half = (warp - 2) >> 2;  // TMEM lane quarter, column parity
+    for (int it = 0; it < mine; ++it) {
+      const int b = it & 1;
+      if (*vfailed || !tc_wait(&tfull[b], (uint32_t)((it / 2) & 1))) {
+        atomicOr(&failed, 1);
+        break;
+      }
       tc_fence_after();
-      const uint32_t as = smem_u32(smem + st * PL::STAGE), ws = as + PL::A_STAGE;
-#pragma unroll
-      for (int kk = 0; kk < KC / 16; ++kk) {
-        const uint64_t ad = smem_desc(as + kk * 2 * LBO_A, LBO_A, SBO);
-        const uint64_t bd = smem_desc(ws + kk * 2 * LBO_W, LBO_W, SBO);
-        const uint32_t accumulate = (c > 0 || kk > 0) ? 1u : 0u;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "setp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tbase),
-            "l"(ad), "l"(bd), "r"(IDESC), "r"(accumulate)
-            : "memory");
-      }
-      tc_commit(&empty[st]);
-    }
-    if (c < NCH) atomicOr(&failed, 1);
-    consumed = c;
-    tc_commit(&done);  // arrives once every MMA issued above has completed
-  }
-  if (warp < 2) __syncwarp();
-  // all threads: the accumulator is complete (or the pipeline gave up)
-  const bool fin = tc_wait(&done, 0u);
-  __syncthreads();
-  const bool ok = fin && failed == 0;
-  tc_fence_after();
-
-  if (ok) {
-    const int q = warp & 3, half = warp >> 2;  // TMEM lane quarter, column parity
-    const int row = m0 + q * 32 + lane;
+      const int row = (blockIdx.x + it * gridDim.x) * 128 + q * 32 + lane;
 #pragma unroll 1
-    for (int cb = 32 * half; cb < N; cb += 64) {
-      uint32_t v[32];
-      const uint32_t taddr = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)cb;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-            "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-            "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
-            "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-            "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-            "=r"(v[30]), "=r"(v[31])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < a.M) {
-        // 16-byte stores of the row's 32 values (row * ldo + cb is a multiple
-        // of 32 elements, so every store is aligned)
-        const size_t o = (size_t)row * a.ldo + cb;
-        float x[32];
+      for (int cb = 32 * half; cb < N; cb += 64) {
+        uint32_t v[32];
+        const uint32_t taddr = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * NCOLS + cb);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+              "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+              "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
+              "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+              "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+              "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row < a.M) {
+          // 16-byte stores of the row's 32 values (row * ldo + cb is a
+          // multiple of 32 elements, so every store is aligned)
+          const size_t o = (size_t)row * a.ldo + cb;
+          float x[32];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]) + __ldg(a.bias + cb + j);
-        if (a.pre) {
+          for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]) + __ldg(a.bias + cb + j);
+          if (a.pre) {
 #pragma unroll
-          for (int j = 0; j < 32; j += 4)
-            *reinterpret_cast<float4 *>(a.pre + o + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
-        }
-        if (a.act == 1) {
+            for (int j = 0; j < 32; j += 4)
+              *reinterpret_cast<float4 *>(a.pre + o + j) =
+                  make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+          }
+          if (a.act == 1) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) x[j] = gelu_tc(x[j]);
-        }
-        if (a.Cf) {
+            for (int j = 0; j < 32; ++j) x[j] = gelu_tc(x[j]);
+          }
+          if (a.Cf) {
 #pragma unroll
-          for (int j = 0; j < 32; j += 4)
-            *reinterpret_cast<float4 *>(a.Cf + o + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
-        }
-        if (a.Cb) {
+            for (int j = 0; j < 32; j += 4)
+              *reinterpret_cast<float4 *>(a.Cf + o + j) =
+                  make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+          }
+          if (a.Cb) {
 #pragma unroll
-          for (int j = 0; j < 32; j += 8) {
-            uint4 w;
-            __nv_bfloat162 h0 = __floats2bfloat162_rn(x[j], x[j + 1]);
-            __nv_bfloat162 h1 = __floats2bfloat162_rn(x[j + 2], x[j + 3]);
-            __nv_bfloat162 h2 = __floats2bfloat162_rn(x[j + 4], x[j + 5]);
-            __nv_bfloat162 h3 = __floats2bfloat162_rn(x[j + 6], x[j + 7]);
-            w.x = *reinterpret_cast<uint32_t *>(&h0);
-            w.y = *reinterpret_cast<uint32_t *>(&h1);
-            w.z = *reinterpret_cast<uint32_t *>(&h2);
-            w.w = *reinterpret_cast<uint32_t *>(&h3);
-            *reinterpret_cast<uint4 *>(a.Cb + o + j) = w;
+            for (int j = 0; j < 32; j += 8) {
+              uint4 w;
+              __nv_bfloat162 h0 = __floats2bfloat162_rn(x[j], x[j + 1]);
+              __nv_bfloat162 h1 = __floats2bfloat162_rn(x[j + 2], x[j + 3]);
+              __nv_bfloat162 h2 = __floats2bfloat162_rn(x[j + 4], x[j + 5]);
+              __nv_bfloat162 h3 = __floats2bfloat162_rn(x[j + 6], x[j + 7]);
+              w.x = *reinterpret_cast<uint32_t *>(&h0);
+              w.y = *reinterpret_cast<uint32_t *>(&h1);
+              w.z = *reinterpret_cast<uint32_t *>(&h2);
+              w.w = *reinterpret_cast<uint32_t *>(&h3);
+              *reinterpret_cast<uint4 *>(a.Cb + o + j) = w;
+            }
           }
         }
       }
+      // this warp is done reading accumulator b
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b]))
+                     : "memory");
     }
-  } else if (tid == 0) {
+  }
+  // every MMA issued has completed (or the wait gave up)
+  const bool fin = tc_wait(&done, 0u);
+  __syncthreads();
+  if (tid == 0 && (failed || !fin)) {
     atomicOr(a.err, PM_ERR_BULK_TIMEOUT);
     // loads issued but never consumed: let them land (bounded) before exit
-    for (int c = consumed; c < issued; ++c) tc_wait(&full[c % S], (uint32_t)((c / S) & 1));
+    for (int g = consumed; g < issued; ++g) tc_wait(&full[g % S], (uint32_t)((g / S) & 1));
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(NCOLS)
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
+                 "r"(2 * NCOLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -335,18 +393,19 @@ EncodeTiled encode_fn() {
 }
 
 // 2-D BF16 map of a row-major [rows x cols] matrix (cols contiguous, row
-// pitch ld elements) read in boxes of 8 columns x box_rows rows; rows past
-// the end read as zeros
+// pitch ld elements) read in boxes of 64 columns x box_rows rows, written to
+// shared memory with the 128-byte swizzle; columns and rows past the end
+// read as zeros
 bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int cols, int rows, int ld,
               int box_rows) {
   EncodeTiled f = encode_fn();
   if (!f) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(__nv_bfloat16)};
-  const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
+  const cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1u, 1u};
   return f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(base), dims,
-           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -367,8 +426,13 @@ int launch_layer(const TcArgs &a, int lda, cudaStream_t s) {
   }
   CUtensorMap ma, mw;
   if (!make_map(&ma, a.A, K, a.M, lda, 128) || !make_map(&mw, a.W, K, N, K, N)) return -1;
-  const int grid = (a.M + 127) / 128;
-  k_mlp_layer_tc<N, K><<<grid, kTcThreads, TcPlan<N, K>::SMEM, s>>>(ma, mw, a);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return -1;
+  const int tiles = (a.M + 127) / 128;
+  const int grid = std::min(tiles, sms * TcPlan<N, K>::CTAS_PER_SM);
+  k_mlp_layer_tc<N, K><<<grid, kTcWarps * 32, TcPlan<N, K>::SMEM, s>>>(ma, mw, a);
   return ok() < 0 ? -1 : 1;
 }
 
