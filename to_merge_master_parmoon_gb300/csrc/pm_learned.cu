@@ -177,11 +177,37 @@ __global__ void k_init_params(float *P, unsigned long long seed) {
 }
 
 __global__ void k_params_to_bf16(const float *P, __nv_bfloat16 *W1, __nv_bfloat16 *W2,
-                                 __nv_bfloat16 *W3) {
+                                 __nv_bfloat16 *W3, __nv_bfloat16 *W2t, __nv_bfloat16 *W3t) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < kOffB1) W1[i] = __float2bfloat16(P[kOffW1 + i]);
-  if (i < (long long)kMlpHidden * kMlpHidden) W2[i] = __float2bfloat16(P[kOffW2 + i]);
-  if (i < (long long)kMlpOutPad * kMlpHidden) W3[i] = __float2bfloat16(P[kOffW3 + i]);
+  if (i < (long long)kMlpHidden * kMlpHidden) {
+    const __nv_bfloat16 w = __float2bfloat16(P[kOffW2 + i]);
+    W2[i] = w;
+    // W2t[c][r] = W2[r][c]
+    W2t[(i % kMlpHidden) * kMlpHidden + i / kMlpHidden] = w;
+  }
+  if (i < (long long)kMlpOutPad * kMlpHidden) {
+    const __nv_bfloat16 w = __float2bfloat16(P[kOffW3 + i]);
+    W3[i] = w;
+    W3t[(i % kMlpHidden) * kMlpOutPad + i / kMlpHidden] = w;
+  }
+}
+
+// out[c * ldo + r] = in[r * ldi + c] for a rows x cols BF16 matrix (32 x 32
+// tiles through shared memory)
+__global__ void k_transpose_bf16(const __nv_bfloat16 *in, int rows, int cols, int ldi,
+                                 __nv_bfloat16 *out, int ldo) {
+  __shared__ __nv_bfloat16 t[32][33];
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) t[k][threadIdx.x] = in[(size_t)r * ldi + c];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int c = c0 + k, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[(size_t)c * ldo + r] = t[threadIdx.x][k];
+  }
 }
 
 __global__ void k_pad_input(const float *X, int M, __nv_bfloat16 *Xb) {
@@ -494,7 +520,15 @@ cudaError_t mlp_create(Mlp &m, int device, unsigned long long seed, int max_batc
   A((void **)&m.W1, sizeof(__nv_bfloat16) * (size_t)kMlpHidden * kMlpInPad);
   A((void **)&m.W2, sizeof(__nv_bfloat16) * (size_t)kMlpHidden * kMlpHidden);
   A((void **)&m.W3, sizeof(__nv_bfloat16) * (size_t)kMlpOutPad * kMlpHidden);
+  A((void **)&m.W2t, sizeof(__nv_bfloat16) * (size_t)kMlpHidden * kMlpHidden);
+  A((void **)&m.W3t, sizeof(__nv_bfloat16) * (size_t)kMlpHidden * kMlpOutPad);
   const size_t B = (size_t)max_batch;
+  m.ldt = (max_batch + 63) / 64 * 64;
+  const size_t LT = (size_t)m.ldt;
+  A((void **)&m.Tx, sizeof(__nv_bfloat16) * LT * kMlpInPad);
+  A((void **)&m.Th, sizeof(__nv_bfloat16) * LT * kMlpHidden);
+  A((void **)&m.Ta, sizeof(__nv_bfloat16) * LT * kMlpHidden);
+  A((void **)&m.Ty, sizeof(__nv_bfloat16) * LT * kMlpOutPad);
   A((void **)&m.X, sizeof(__nv_bfloat16) * B * kMlpInPad);
   A((void **)&m.H1, sizeof(__nv_bfloat16) * B * kMlpHidden);
   A((void **)&m.H2, sizeof(__nv_bfloat16) * B * kMlpHidden);
@@ -524,8 +558,9 @@ cudaError_t mlp_create(Mlp &m, int device, unsigned long long seed, int max_batc
 void mlp_destroy(Mlp &m) {
   cudaSetDevice(m.device);
   if (m.stream) cudaStreamSynchronize(m.stream);
-  void *ptrs[] = {m.P,  m.G,    m.Mo,   m.Vo,   m.W1,   m.W2, m.W3, m.X, m.H1, m.H2,
-                  m.dYb, m.dA2b, m.dA1b, m.pre1, m.pre2, m.Y,  m.dY, m.dH, m.loss, m.err};
+  void *ptrs[] = {m.P,   m.G,    m.Mo,   m.Vo,   m.W1,   m.W2,   m.W3,  m.W2t, m.W3t,
+                  m.Tx,  m.Th,   m.Ta,   m.Ty,   m.X,    m.H1,   m.H2,  m.dYb, m.dA2b,
+                  m.dA1b, m.pre1, m.pre2, m.Y,   m.dY,   m.dH,   m.loss, m.err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (m.stream) cudaStreamDestroy(m.stream);
@@ -533,7 +568,7 @@ void mlp_destroy(Mlp &m) {
 }
 
 int mlp_sync_bf16(const Mlp &m, cudaStream_t s) {
-  k_params_to_bf16<<<blocks_for(kOffB1), 256, 0, s>>>(m.P, m.W1, m.W2, m.W3);
+  k_params_to_bf16<<<blocks_for(kOffB1), 256, 0, s>>>(m.P, m.W1, m.W2, m.W3, m.W2t, m.W3t);
   return ok() < 0 ? -1 : 1;
 }
 
@@ -621,40 +656,92 @@ int mlp_loss_grad(Mlp &m, const float *X, const float *T, int M, cudaStream_t s)
   }
   k_mse_grad<<<blocks_for((long long)M * kMlpOutPad), 256, 0, s>>>(m.Y, T, M, m.dY, m.dYb, m.loss);
   n++;
-  // layer 3: dW3 = dY^T H2, db3, dH2 = dY W3
-  g = GemmArgs{kMlpOutPad, kMlpHidden, M, m.dYb, 1, kMlpOutPad, m.H2, kMlpHidden, 1, 1.f,
-               nullptr, 0, nullptr, m.G + kOffW3, nullptr, kMlpHidden};
-  if ((r = gemm(g, s)) < 0) return -1;
-  n += r;
-  k_colsum<<<1, 128, 0, s>>>(m.dY, M, kMlpOutPad, m.G + kOffB3);
-  n++;
-  g = GemmArgs{M, kMlpHidden, kMlpOutPad, m.dYb, kMlpOutPad, 1, m.W3, kMlpHidden, 1, 1.f,
-               nullptr, 0, nullptr, m.dH, nullptr, kMlpHidden};
-  if ((r = gemm(g, s)) < 0) return -1;
-  n += r;
-  const long long nh = (long long)M * kMlpHidden;
-  // layer 2 (dA2 in pre2's buffer)
-  k_gelu_back<<<blocks_for(nh), 256, 0, s>>>(m.dH, m.pre2, nh, m.pre2, m.dA2b);
-  n++;
-  g = GemmArgs{kMlpHidden, kMlpHidden, M, m.dA2b, 1, kMlpHidden, m.H1, kMlpHidden, 1, 1.f,
-               nullptr, 0, nullptr, m.G + kOffW2, nullptr, kMlpHidden};
-  if ((r = gemm(g, s)) < 0) return -1;
-  n += r;
-  k_colsum<<<2, 128, 0, s>>>(m.pre2, M, kMlpHidden, m.G + kOffB2);
-  n++;
-  g = GemmArgs{M, kMlpHidden, kMlpHidden, m.dA2b, kMlpHidden, 1, m.W2, kMlpHidden, 1, 1.f,
-               nullptr, 0, nullptr, m.dH, nullptr, kMlpHidden};
-  if ((r = gemm(g, s)) < 0) return -1;
-  n += r;
-  // layer 1 (dA1 in pre1's buffer)
-  k_gelu_back<<<blocks_for(nh), 256, 0, s>>>(m.dH, m.pre1, nh, m.pre1, m.dA1b);
-  n++;
-  g = GemmArgs{kMlpHidden, kMlpInPad, M, m.dA1b, 1, kMlpHidden, m.X, kMlpInPad, 1, 1.f,
-               nullptr, 0, nullptr, m.G + kOffW1, nullptr, kMlpInPad};
-  if ((r = gemm(g, s)) < 0) return -1;
-  n += r;
-  k_colsum<<<2, 128, 0, s>>>(m.pre1, M, kMlpHidden, m.G + kOffB1);
-  n++;
+  if (m.tc) {
+    // the six backward GEMMs on tcgen05: weight gradients as (batch-major
+    // operands transposed to K-major) products over the batch, data
+    // gradients against the transposed weights
+    const int lt = m.ldt;
+    auto tr = [&](const __nv_bfloat16 *in, int cols, __nv_bfloat16 *out) {
+      k_transpose_bf16<<<dim3((cols + 31) / 32, (M + 31) / 32), dim3(32, 8), 0, s>>>(in, M, cols,
+                                                                                    cols, out, lt);
+      n++;
+    };
+    const long long nh = (long long)M * kMlpHidden;
+    // layer 3: dW3 = dY^T H2, db3, dH2 = dY W3
+    tr(m.dYb, kMlpOutPad, m.Ty);
+    tr(m.H2, kMlpHidden, m.Th);
+    if ((r = mlp_gemm_tc(m.Ty, lt, kMlpOutPad, m.Th, lt, kMlpHidden, M, m.G + kOffW3, kMlpHidden,
+                         m.err, s)) < 0)
+      return -1;
+    n += r;
+    k_colsum<<<1, 128, 0, s>>>(m.dY, M, kMlpOutPad, m.G + kOffB3);
+    n++;
+    if ((r = mlp_gemm_tc(m.dYb, kMlpOutPad, M, m.W3t, kMlpOutPad, kMlpHidden, kMlpOutPad, m.dH,
+                         kMlpHidden, m.err, s)) < 0)
+      return -1;
+    n += r;
+    // layer 2 (dA2 in pre2's buffer)
+    k_gelu_back<<<blocks_for(nh), 256, 0, s>>>(m.dH, m.pre2, nh, m.pre2, m.dA2b);
+    n++;
+    tr(m.dA2b, kMlpHidden, m.Ta);
+    tr(m.H1, kMlpHidden, m.Th);
+    if ((r = mlp_gemm_tc(m.Ta, lt, kMlpHidden, m.Th, lt, kMlpHidden, M, m.G + kOffW2, kMlpHidden,
+                         m.err, s)) < 0)
+      return -1;
+    n += r;
+    k_colsum<<<2, 128, 0, s>>>(m.pre2, M, kMlpHidden, m.G + kOffB2);
+    n++;
+    if ((r = mlp_gemm_tc(m.dA2b, kMlpHidden, M, m.W2t, kMlpHidden, kMlpHidden, kMlpHidden, m.dH,
+                         kMlpHidden, m.err, s)) < 0)
+      return -1;
+    n += r;
+    // layer 1 (dA1 in pre1's buffer)
+    k_gelu_back<<<blocks_for(nh), 256, 0, s>>>(m.dH, m.pre1, nh, m.pre1, m.dA1b);
+    n++;
+    tr(m.dA1b, kMlpHidden, m.Ta);
+    tr(m.X, kMlpInPad, m.Tx);
+    if ((r = mlp_gemm_tc(m.Ta, lt, kMlpHidden, m.Tx, lt, kMlpInPad, M, m.G + kOffW1, kMlpInPad,
+                         m.err, s)) < 0)
+      return -1;
+    n += r;
+    k_colsum<<<2, 128, 0, s>>>(m.pre1, M, kMlpHidden, m.G + kOffB1);
+    n++;
+  } else {
+    // layer 3: dW3 = dY^T H2, db3, dH2 = dY W3
+    g = GemmArgs{kMlpOutPad, kMlpHidden, M, m.dYb, 1, kMlpOutPad, m.H2, kMlpHidden, 1, 1.f,
+                 nullptr, 0, nullptr, m.G + kOffW3, nullptr, kMlpHidden};
+    if ((r = gemm(g, s)) < 0) return -1;
+    n += r;
+    k_colsum<<<1, 128, 0, s>>>(m.dY, M, kMlpOutPad, m.G + kOffB3);
+    n++;
+    g = GemmArgs{M, kMlpHidden, kMlpOutPad, m.dYb, kMlpOutPad, 1, m.W3, kMlpHidden, 1, 1.f,
+                 nullptr, 0, nullptr, m.dH, nullptr, kMlpHidden};
+    if ((r = gemm(g, s)) < 0) return -1;
+    n += r;
+    const long long nh = (long long)M * kMlpHidden;
+    // layer 2 (dA2 in pre2's buffer)
+    k_gelu_back<<<blocks_for(nh), 256, 0, s>>>(m.dH, m.pre2, nh, m.pre2, m.dA2b);
+    n++;
+    g = GemmArgs{kMlpHidden, kMlpHidden, M, m.dA2b, 1, kMlpHidden, m.H1, kMlpHidden, 1, 1.f,
+                 nullptr, 0, nullptr, m.G + kOffW2, nullptr, kMlpHidden};
+    if ((r = gemm(g, s)) < 0) return -1;
+    n += r;
+    k_colsum<<<2, 128, 0, s>>>(m.pre2, M, kMlpHidden, m.G + kOffB2);
+    n++;
+    g = GemmArgs{M, kMlpHidden, kMlpHidden, m.dA2b, kMlpHidden, 1, m.W2, kMlpHidden, 1, 1.f,
+                 nullptr, 0, nullptr, m.dH, nullptr, kMlpHidden};
+    if ((r = gemm(g, s)) < 0) return -1;
+    n += r;
+    // layer 1 (dA1 in pre1's buffer)
+    k_gelu_back<<<blocks_for(nh), 256, 0, s>>>(m.dH, m.pre1, nh, m.pre1, m.dA1b);
+    n++;
+    g = GemmArgs{kMlpHidden, kMlpInPad, M, m.dA1b, 1, kMlpHidden, m.X, kMlpInPad, 1, 1.f,
+                 nullptr, 0, nullptr, m.G + kOffW1, nullptr, kMlpInPad};
+    if ((r = gemm(g, s)) < 0) return -1;
+    n += r;
+    k_colsum<<<2, 128, 0, s>>>(m.pre1, M, kMlpHidden, m.G + kOffB1);
+    n++;
+  }
   k_mask_grads<<<blocks_for(kNumParams), 256, 0, s>>>(m.G);
   n++;
   return ok() < 0 ? -1 : n;

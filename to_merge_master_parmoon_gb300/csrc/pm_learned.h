@@ -38,6 +38,10 @@ struct Mlp {
   long long step = 0;
   float *P = nullptr, *G = nullptr, *Mo = nullptr, *Vo = nullptr;  // params, grads, Adam moments
   __nv_bfloat16 *W1 = nullptr, *W2 = nullptr, *W3 = nullptr;      // BF16 copies
+  __nv_bfloat16 *W2t = nullptr, *W3t = nullptr;  // BF16 transposes (gradient GEMMs)
+  // transposed training operands [rows x ldt] (K = batch rows contiguous)
+  __nv_bfloat16 *Tx = nullptr, *Th = nullptr, *Ta = nullptr, *Ty = nullptr;
+  int ldt = 0;
   // training workspace (max_batch rows)
   __nv_bfloat16 *X = nullptr, *H1 = nullptr, *H2 = nullptr, *dYb = nullptr, *dA2b = nullptr,
                 *dA1b = nullptr;
@@ -56,6 +60,11 @@ int mlp_layer_tc(int layer, const __nv_bfloat16 *A, int M, const __nv_bfloat16 *
                  const int *on, int *err, cudaStream_t s);
 // sets the layers' shared-memory limits (once, outside stream capture)
 int mlp_tc_init();
+// C[rows x n] = A B^T on the tcgen05 path (FP32 out, row pitch ldc) for A
+// [rows x k] (pitch lda) and B [n x k] (pitch ldb), both BF16 with k
+// contiguous; n in {96, 256, 400}; pitches in elements, multiples of 8
+int mlp_gemm_tc(const __nv_bfloat16 *A, int lda, int rows, const __nv_bfloat16 *B, int ldb,
+                int n, int k, float *C, int ldc, int *err, cudaStream_t s);
 
 // allocate / free (returns cudaError_t)
 cudaError_t mlp_create(Mlp &m, int device, unsigned long long seed, int max_batch);

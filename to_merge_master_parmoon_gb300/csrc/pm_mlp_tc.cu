@@ -83,8 +83,10 @@ __device__ __forceinline__ void tc_fence_after() {
 
 struct TcArgs {
   int M, ldo;
+  int nch;               // K chunks of 64 columns (columns past K read as zeros)
+  int n_off;             // first row of W and first output column of this launch
   const __nv_bfloat16 *A, *W;
-  const float *bias;
+  const float *bias;     // per output column, or null
   int act;               // 0 identity, 1 GELU
   float *pre;            // pre-activation out (FP32) or null
   float *Cf;             // FP32 out or null
@@ -126,10 +128,9 @@ __device__ __forceinline__ void tc_commit(uint64_t *bar) {
 // 128-byte swizzle atom per row; the last chunk of K = 400 reads columns
 // 400..447 as zeros), up to three chunks in flight; two accumulators of
 // NCOLS TMEM columns (512 for N = 256: one CTA per SM; 256 for N = 96).
-template <int N, int K>
+template <int N>
 struct TcPlan {
   static constexpr int KC = 64;
-  static constexpr int NCH = (K + KC - 1) / KC;
   static constexpr int S = 3;
   static constexpr int A_STAGE = 128 * KC * 2;  // bytes of the A tile of a chunk
   static constexpr int W_STAGE = N * KC * 2;    // bytes of the W rows of a chunk
@@ -139,6 +140,7 @@ struct TcPlan {
   static constexpr int CTAS_PER_SM = 512 / (2 * NCOLS);
   static_assert(KC % 16 == 0 && STAGE % 1024 == 0, "K chunking, 1024-byte atoms");
   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "UMMA N for M = 128");
+  static_assert(N % 8 == 0, "16-byte stores of BF16 output rows");
   static_assert(SMEM <= 200 * 1024, "stages fit in shared memory");
 };
 
@@ -165,12 +167,13 @@ constexpr int kEpiWarps = 8;
 // a shared flag that stops the other roles; the MMA thread still commits its
 // MMAs to `done`, which all threads wait for (bounded), the producer waits
 // for its loads in flight, and the TMEM columns are released before exit.
-template <int N, int K>
+template <int N>
 __global__ void __launch_bounds__(kTcWarps * 32, 1)
     k_mlp_layer_tc(const __grid_constant__ CUtensorMap mapA,
                    const __grid_constant__ CUtensorMap mapW, TcArgs a) {
-  using PL = TcPlan<N, K>;
-  constexpr int KC = PL::KC, NCH = PL::NCH, S = PL::S, NCOLS = PL::NCOLS;
+  using PL = TcPlan<N>;
+  constexpr int KC = PL::KC, S = PL::S, NCOLS = PL::NCOLS;
+  const int NCH = a.nch;
   constexpr uint32_t IDESC = idesc_bf16(128, N);
 
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(kTcWarps * 32, 1)
           unsigned char *As = smem + st * PL::STAGE, *Ws = As + PL::A_STAGE;
           mbar_expect_tx(&full[st], (uint32_t)PL::STAGE);
           tma_load_2d(As, &mapA, c * KC, m0, &full[st]);
-          tma_load_2d(Ws, &mapW, c * KC, 0, &full[st]);
+          tma_load_2d(Ws, &mapW, c * KC, a.n_off, &full[st]);
         }
       }
       issued = g;
@@ -307,15 +310,24 @@ __global__ void __launch_bounds__(kTcWarps * 32, 1)
         if (row < a.M) {
           // 16-byte stores of the row's 32 values (row * ldo + cb is a
           // multiple of 32 elements, so every store is aligned)
-          const size_t o = (size_t)row * a.ldo + cb;
+          const size_t o = (size_t)row * a.ldo + a.n_off + cb;
           float x[32];
+          if (a.bias) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]) + __ldg(a.bias + cb + j);
+            for (int j = 0; j < 32; ++j)
+              x[j] = __uint_as_float(v[j]) + __ldg(a.bias + a.n_off + cb + j);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]);
+          }
+          // columns of the last block past N (N = 144: half a block) are not stored
+          const int nv = N - cb < 32 ? N - cb : 32;
           if (a.pre) {
 #pragma unroll
             for (int j = 0; j < 32; j += 4)
-              *reinterpret_cast<float4 *>(a.pre + o + j) =
-                  make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+              if (j < nv)
+                *reinterpret_cast<float4 *>(a.pre + o + j) =
+                    make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
           }
           if (a.act == 1) {
 #pragma unroll
@@ -324,12 +336,14 @@ __global__ void __launch_bounds__(kTcWarps * 32, 1)
           if (a.Cf) {
 #pragma unroll
             for (int j = 0; j < 32; j += 4)
-              *reinterpret_cast<float4 *>(a.Cf + o + j) =
-                  make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+              if (j < nv)
+                *reinterpret_cast<float4 *>(a.Cf + o + j) =
+                    make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
           }
           if (a.Cb) {
 #pragma unroll
             for (int j = 0; j < 32; j += 8) {
+              if (j >= nv) break;
               uint4 w;
               __nv_bfloat162 h0 = __floats2bfloat162_rn(x[j], x[j + 1]);
               __nv_bfloat162 h1 = __floats2bfloat162_rn(x[j + 2], x[j + 3]);
@@ -409,30 +423,36 @@ bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int cols, int rows, int
            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int N, int K>
+template <int N>
 int set_smem_limit() {
-  return cudaFuncSetAttribute(k_mlp_layer_tc<N, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              TcPlan<N, K>::SMEM) == cudaSuccess
+  return cudaFuncSetAttribute(k_mlp_layer_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              TcPlan<N>::SMEM) == cudaSuccess
              ? 0
              : -1;
 }
 
-template <int N, int K>
-int launch_layer(const TcArgs &a, int lda, cudaStream_t s) {
+// C[rows x N] (columns n_off.. of the output) = act(A W^T + bias) with A
+// [rows x K] (row pitch lda) and W [>= n_off + N rows x K] (row pitch ldw)
+template <int N>
+int launch_n(TcArgs a, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *W, int ldw, int K,
+             int w_rows, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    if (set_smem_limit<N, K>() < 0) return -1;
+    if (set_smem_limit<N>() < 0) return -1;
     attr = true;
   }
   CUtensorMap ma, mw;
-  if (!make_map(&ma, a.A, K, a.M, lda, 128) || !make_map(&mw, a.W, K, N, K, N)) return -1;
+  if (!make_map(&ma, A, K, a.M, lda, 128) || !make_map(&mw, W, K, w_rows, ldw, N)) return -1;
+  a.A = A;
+  a.W = W;
+  a.nch = (K + TcPlan<N>::KC - 1) / TcPlan<N>::KC;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return -1;
   const int tiles = (a.M + 127) / 128;
-  const int grid = std::min(tiles, sms * TcPlan<N, K>::CTAS_PER_SM);
-  k_mlp_layer_tc<N, K><<<grid, kTcWarps * 32, TcPlan<N, K>::SMEM, s>>>(ma, mw, a);
+  const int grid = std::min(tiles, sms * TcPlan<N>::CTAS_PER_SM);
+  k_mlp_layer_tc<N><<<grid, kTcWarps * 32, TcPlan<N>::SMEM, s>>>(ma, mw, a);
   return ok() < 0 ? -1 : 1;
 }
 
@@ -440,9 +460,9 @@ int launch_layer(const TcArgs &a, int lda, cudaStream_t s) {
 
 int mlp_tc_init() {
   int r = 0;
-  r |= set_smem_limit<kMlpHidden, kMlpInPad>();
-  r |= set_smem_limit<kMlpHidden, kMlpHidden>();
-  r |= set_smem_limit<kMlpOutPad, kMlpHidden>();
+  r |= set_smem_limit<kMlpHidden>();
+  r |= set_smem_limit<kMlpOutPad>();
+  r |= set_smem_limit<kMlpInPad - kMlpHidden>();
   if (!encode_fn()) r = -1;
   return r == 0 ? 0 : -1;
 }
@@ -453,8 +473,6 @@ int mlp_layer_tc(int layer, const __nv_bfloat16 *A, int M, const __nv_bfloat16 *
   if (M <= 0) return 0;
   TcArgs a{};
   a.M = M;
-  a.A = A;
-  a.W = W;
   a.bias = bias;
   a.act = act;
   a.pre = pre;
@@ -465,16 +483,44 @@ int mlp_layer_tc(int layer, const __nv_bfloat16 *A, int M, const __nv_bfloat16 *
   switch (layer) {
     case 1:
       a.ldo = kMlpHidden;
-      return launch_layer<kMlpHidden, kMlpInPad>(a, kMlpInPad, s);
+      return launch_n<kMlpHidden>(a, A, kMlpInPad, W, kMlpInPad, kMlpInPad, kMlpHidden, s);
     case 2:
       a.ldo = kMlpHidden;
-      return launch_layer<kMlpHidden, kMlpHidden>(a, kMlpHidden, s);
+      return launch_n<kMlpHidden>(a, A, kMlpHidden, W, kMlpHidden, kMlpHidden, kMlpHidden, s);
     case 3:
       a.ldo = kMlpOutPad;
-      return launch_layer<kMlpOutPad, kMlpHidden>(a, kMlpHidden, s);
+      return launch_n<kMlpOutPad>(a, A, kMlpHidden, W, kMlpHidden, kMlpHidden, kMlpOutPad, s);
     default:
       return -1;
   }
+}
+
+int mlp_gemm_tc(const __nv_bfloat16 *A, int lda, int rows, const __nv_bfloat16 *B, int ldb,
+                int n, int k, float *C, int ldc, int *err, cudaStream_t s) {
+  if (rows <= 0) return 0;
+  TcArgs a{};
+  a.M = rows;
+  a.ldo = ldc;
+  a.Cf = C;
+  a.err = err;
+  int launches = 0, r;
+  // output columns in tiles of at most 256 (the widths this library needs:
+  // 96, 256 and 400 = 256 + 144)
+  for (int n0 = 0; n0 < n; n0 += kMlpHidden) {
+    const int w = std::min(kMlpHidden, n - n0);
+    a.n_off = n0;
+    if (w == kMlpHidden)
+      r = launch_n<kMlpHidden>(a, A, lda, B, ldb, k, n, s);
+    else if (w == kMlpOutPad)
+      r = launch_n<kMlpOutPad>(a, A, lda, B, ldb, k, n, s);
+    else if (w == kMlpInPad - kMlpHidden)
+      r = launch_n<kMlpInPad - kMlpHidden>(a, A, lda, B, ldb, k, n, s);
+    else
+      return -1;
+    if (r < 0) return -1;
+    launches += r;
+  }
+  return launches;
 }
 
 }  // namespace pm
