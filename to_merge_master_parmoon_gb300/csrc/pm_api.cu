@@ -2060,6 +2060,9 @@ pm_status pm_solve_fused(pm_handle *h, double *const *sols, const double *const 
   cudaEventRecord(e0, h->stream);
   pm_status st = fgmres_seg(h, h->xd, h->bd, r.data());
   cudaEventRecord(e1, h->stream);
+  // every system sweeps again in the next solve, also after an error
+  const pm_status rs = restore_colours(h);
+  if (st == PM_OK) st = rs;
   if (st == PM_OK) {  // true residual of every returned iterate (FP64)
     std::vector<double> tr((size_t)G);
     st = defect_nse4(h, h->xd, h->bd, h->w);
