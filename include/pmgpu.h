@@ -420,8 +420,8 @@ pm_status pm_mlp_get_params(pm_mlp *m, float *host, long long n);
 pm_status pm_mlp_set_params(pm_mlp *m, const float *host, long long n);
 /* d_X [M x 397] FP32 (device) -> d_Y [M x 85] FP32 (device), BF16 compute */
 pm_status pm_mlp_forward(pm_mlp *m, const float *d_X, int M, float *d_Y);
-/* Forward layers of the network on the tcgen05 tensor cores (1, default) or
- * on the warp-level mma.sync path (0); training gradients use mma.sync. */
+/* The network's GEMMs (forward layers and the training gradients) on the
+ * tcgen05 tensor cores (1, default) or on the warp-level mma.sync path (0). */
 pm_status pm_mlp_set_tensor_path(pm_mlp *m, int tcgen05);
 /* MSE loss of the batch and its gradient (kept in the object; copied to
  * host_grad when non-NULL, length pm_mlp_num_params()) */

@@ -45,10 +45,11 @@ def test_forward_and_gradients_match_oracle(mlp):
 
 @pytest.mark.parametrize("M", [96, 300, 512])
 def test_tcgen05_and_mma_sync_paths_agree(mlp, M):
-    """The forward layers on tcgen05 (TMEM accumulators, the default) and on
-    mma.sync give the same outputs, loss and gradients (FP32 accumulation of
-    the same BF16 products in another order; tile edges at M not a multiple
-    of 128), and both match the oracle."""
+    """The network's GEMMs on tcgen05 (TMEM accumulators, the default: the
+    forward layers and the six backward products) and on mma.sync give the
+    same outputs, loss and gradients (FP32 accumulation of the same BF16
+    products in another order; tile edges at M not a multiple of 128 and
+    batch sizes not a multiple of 64), and both match the oracle."""
     import torch
     rng = np.random.default_rng(M)
     X = rng.standard_normal((M, mo.N_IN)).astype(np.float32)

@@ -63,7 +63,8 @@ class Mlp:
             raise PmError(st, "pm_mlp_set_params")
 
     def set_tensor_path(self, tcgen05: bool):
-        """Forward layers on tcgen05 (True, the default) or mma.sync (False)."""
+        """The GEMMs (forward and training) on tcgen05 (True, the default) or
+        mma.sync (False)."""
         st = self._lib.pm_mlp_set_tensor_path(self._h, int(tcgen05))
         if st != 0:
             raise PmError(st, "pm_mlp_set_tensor_path")
