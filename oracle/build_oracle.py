@@ -10,9 +10,11 @@
   and ref_vanka.cpp (only when the tree is present; the defect and Vanka
   outputs are committed as tests/golden/ref_defect_*.npz, ref_vanka_*.npz).
 * ``oracle/_ref/libref_transfer.so`` — the reference's grid transfers with
-  the FE and geometry databases they read (REF_TRANSFER_TUS), driven by
-  ref_transfer.cpp (only when the tree is present; its outputs are committed
-  as tests/golden/ref_transfer_*.npz).
+  the FE and geometry databases they read, and its multigrid cycle driver
+  (TMultiGridIte, TNSE_MultiGrid) over two TNSE_MGLevel4 levels
+  (REF_TRANSFER_TUS), driven by ref_transfer.cpp (only when the tree is
+  present; its outputs are committed as tests/golden/ref_transfer_*.npz and
+  tests/golden/ref_cycle_*.npz).
 * ``oracle/_ref/libref_facade.so`` — include/pmgpu_parmoon.h (the solver as a
   ParMooN TItMethod) compiled against the reference's headers and matrix
   classes in ref_facade.cpp, linked with libpmgpu.so (only when the tree is
@@ -132,7 +134,8 @@ def build_ref_facade() -> Path | None:
 
 def _ref_deps():
     """Files every reference-harness object depends on besides its source."""
-    return [HERE / "ref_level_space.h", Path(__file__), *sorted((HERE / "ref_stubs").glob("*.h"))]
+    return [HERE / "ref_level_space.h", HERE / "ref_lapack.h", Path(__file__),
+            *sorted((HERE / "ref_stubs").glob("*.h"))]
 
 
 def _compile(jobs, cmd):
@@ -183,7 +186,13 @@ REF_TRANSFER_TUS = {
           "HexaIsoparametric", "HexaTrilinear", "LinAlg", "LineAffin", "MGComponents3D",
           "NodalFunctional1D", "NodalFunctional2D", "NodalFunctional3D", "QuadAffin",
           "QuadBilinear", "QuadIsoparametric", "RefTrans3D", "TNSE3D_FixPo", "TetraAffin",
-          "TetraIsoparametric", "TriaAffin", "TriaIsoparametric"),
+          "TetraIsoparametric", "TriaAffin", "TriaIsoparametric",
+          # the cycle driver and what it runs: TMultiGridIte, TNSE_MultiGrid,
+          # the TNSE_MGLevel4 levels and their matrix classes
+          "ItMethod", "MultiGridIte", "FgmresIte", "NSE_MultiGrid", "NSE_MGLevel",
+          "NSE_MGLevel4", "NSE_MGLevel5",
+          "Matrix", "SquareMatrix", "Structure", "SquareStructure", "Matrix3D",
+          "SquareMatrix3D", "Structure3D", "SquareStructure3D"),
     "General": ("Database", "MainUtilities", "MooNMD_Io", "Utilities", "Vector"),
     "Geometry": ("BaseCell", "BdPlane", "BoundComp", "BoundComp3D", "BoundEdge", "BoundFace", "Brick",
           "Collection", "GridCell", "Hexahedron", "InterfaceJoint3D", "It_Between", "It_EQ",

@@ -3,8 +3,10 @@ Defect_NSE4 / MatVect_NSE4 / IntoL20Vector3D (src/FE/MGComponents3D.C:3210,
 :3030, :1756) and flexible FGMRES (TFgmresIte::Iterate, src/FE/FgmresIte.C:250)
 and cell Vanka (TNSE_MGLevel4::CellVanka, src/FE/NSE_MGLevel4.C:1653) run on
 one level of a problem built here; and (oracle/_ref/libref_transfer.so) the
-grid transfers Prolongate / DefectRestriction between two levels.  TEST INFRASTRUCTURE
-ONLY — it exists where the reference tree does (see build_ref_harness).
+grid transfers Prolongate / DefectRestriction between two levels and the
+multigrid cycle driver (TMultiGridIte::Iterate, TNSE_MultiGrid::Cycle) over
+them.  TEST INFRASTRUCTURE ONLY — it exists where the reference tree does (see
+build_ref_harness, build_ref_transfer).
 """
 from __future__ import annotations
 
@@ -248,6 +250,15 @@ def ref_transfer_lib():
         L.ref_transfer_prolongate.restype = None
         L.ref_transfer_restrict.argtypes = [C.c_void_p, _dp, _dp]
         L.ref_transfer_restrict.restype = None
+        _ipp = C.POINTER(_ip)
+        L.ref_cycle_create.argtypes = ([C.c_int] * 4 + [_ip, _ip] + [C.c_int] * 4 + [_ip] * 4
+                                       + [C.c_int, _ipp, _ipp, _dpp, _ipp, _ipp, _dpp, _ipp,
+                                          _ipp, _dpp, C.c_double, C.c_double])
+        L.ref_cycle_create.restype = C.c_void_p
+        L.ref_cycle_destroy.argtypes = [C.c_void_p]
+        L.ref_cycle_destroy.restype = None
+        L.ref_cycle_vcycle.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_double]
+        L.ref_cycle_vcycle.restype = None
         _TLIB = L
     return _TLIB
 
@@ -294,6 +305,65 @@ class RefTransfer:
         coarse = np.empty(self.nc)
         self._L.ref_transfer_restrict(self._h, fp, coarse.ctypes.data_as(_dp))
         return coarse
+
+
+class RefCycle:
+    """The reference's multigrid preconditioner call, TMultiGridIte::Iterate
+    (src/FE/MultiGridIte.C:76-132) with TNSE_MultiGrid::Cycle
+    (src/FE/NSE_MultiGrid.C:434-1779), over the two finest levels of a
+    hexahedral Q2/P1disc problem (run by oracle/ref_transfer.cpp).  A problem
+    of two levels gives the whole V-cycle: cell Vanka on the fine level, the
+    exact solve on the coarse one."""
+
+    def __init__(self, problem, alpha: float = 1.0, beta: float = 1.0):
+        L = ref_transfer_lib()
+        if L is None:
+            raise RuntimeError("reference tree not present: the transfer harness is not built")
+        self._L = L
+        self._h = None
+        top = problem.n_levels - 1
+        c, f = problem.arrays(top - 1), problem.arrays(top)
+        self.nf = 3 * f["n_udof"] + f["n_pdof"]
+        ints = [np.ascontiguousarray(a, dtype=np.int32) for a in
+                (c["cell_udofs"], c["cell_pdofs"], f["cell_udofs"], f["cell_pdofs"],
+                 f["cell_parent"], f["cell_child"])]
+        keep = list(ints)
+
+        def iarr(*arrs):
+            v = [np.ascontiguousarray(a, dtype=np.int32) for a in arrs]
+            keep.extend(v)
+            return (_ip * len(v))(*[a.ctypes.data_as(_ip) for a in v])
+
+        def darr(arrs):
+            v = [np.ascontiguousarray(a, dtype=np.float64) for a in arrs]
+            keep.extend(v)
+            return (_dp * len(v))(*[a.ctypes.data_as(_dp) for a in v])
+
+        n_blocks = len(c["a"])
+        ptr = [a.ctypes.data_as(_ip) for a in ints]
+        self._keep = keep
+        self._h = L.ref_cycle_create(
+            c["n_cells"], c["n_udof"], c["n_active"], c["n_pdof"], ptr[0], ptr[1], f["n_cells"],
+            f["n_udof"], f["n_active"], f["n_pdof"], *ptr[2:], n_blocks,
+            iarr(c["a_rowptr"], f["a_rowptr"]), iarr(c["a_col"], f["a_col"]),
+            darr(list(c["a"]) + list(f["a"])), iarr(c["b_rowptr"], f["b_rowptr"]),
+            iarr(c["b_col"], f["b_col"]), darr(list(c["b"]) + list(f["b"])),
+            iarr(c["bt_rowptr"], f["bt_rowptr"]), iarr(c["bt_col"], f["bt_col"]),
+            darr(list(c["bt"]) + list(f["bt"])), alpha, beta)
+        if not self._h:
+            raise ValueError("the levels are not a regular refinement (8 children per cell)")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.ref_cycle_destroy(self._h)
+            self._h = None
+
+    def vcycle(self, v, pre: int = 2, post: int = 2, damp: float = 1.0) -> np.ndarray:
+        v, vp = _d(v)
+        assert v.size == self.nf
+        z = np.zeros(self.nf)
+        self._L.ref_cycle_vcycle(self._h, vp, z.ctypes.data_as(_dp), pre, post, damp)
+        return z
 
 
 def ref_into_l20(v, order: int = -11) -> np.ndarray:

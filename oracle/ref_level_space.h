@@ -1,6 +1,6 @@
-// ref_level_space.h — a TFESpace3D filled from a level's arrays, shared by
-// the reference harnesses (ref_vanka.cpp, ref_transfer.cpp).  TEST
-// INFRASTRUCTURE ONLY.
+// ref_level_space.h — a TFESpace3D filled from a level's arrays, and the
+// structures of a level's matrices over it, shared by the reference
+// harnesses (ref_vanka.cpp, ref_transfer.cpp).  TEST INFRASTRUCTURE ONLY.
 //
 // The space's DOF maps (GlobalNumbers, BeginIndex), DOF count, active /
 // hanging / Dirichlet bounds and per-cell element ids (AllElements, which
@@ -15,6 +15,8 @@
 
 #include <Collection.h>
 #include <FESpace3D.h>
+#include <SquareStructure3D.h>
+#include <Structure3D.h>
 
 struct LevelSpace : public TFESpace3D {
   LevelSpace(TCollection *coll, int n_dof, int active, int n_dirichlet, int *global, int *begin,
@@ -36,6 +38,38 @@ struct LevelSpace : public TFESpace3D {
   void release_names() {
     std::free(Name);
     std::free(Description);
+  }
+};
+
+// The structures of a level's matrices over LevelSpace objects: A's square
+// structure with its active bound and space, and the B / BT structure (a
+// TStructure3D built from two spaces on different collections, for which its
+// constructor returns at once, src/FE/Structure3D.C:43-46, then given the
+// pattern and the level's spaces).
+struct LevelSquareStructure : public TSquareStructure3D {
+  LevelSquareStructure(int n, int active, int nnz, int *col, int *rowptr, TFESpace3D *space)
+      : TSquareStructure3D(n, nnz, col, rowptr) {
+    ActiveBound = active;
+    FESpace = space;
+  }
+};
+
+struct LevelStructure : public TStructure3D {
+  LevelStructure(TFESpace3D *other_a, TFESpace3D *other_b, TFESpace3D *test, TFESpace3D *ansatz,
+                 int rows, int cols, int nnz, int *col, int *rowptr)
+      : TStructure3D(other_a, other_b) {
+    N_Rows = rows;
+    N_Columns = cols;
+    N_Entries = nnz;
+    KCol = col;
+    RowPtr = rowptr;
+    HangingN_Entries = 0;
+    HangingKCol = nullptr;
+    HangingRowPtr = nullptr;
+    TestSpace3D = test;
+    AnsatzSpace3D = ansatz;
+    TestSpace2D = nullptr;
+    AnsatzSpace2D = nullptr;
   }
 };
 

@@ -1,7 +1,8 @@
-// ref_transfer.cpp — runs the reference's own grid transfers on two nested
-// hexahedral levels handed over as plain arrays.  TEST INFRASTRUCTURE ONLY:
-// it pins the oracle's prolongate / defect_restriction (and with them the
-// per-child Q2 and P1disc matrices) against the reference code itself.
+// ref_transfer.cpp — runs the reference's own grid transfers, and its
+// multigrid cycle driver, on two nested hexahedral levels handed over as
+// plain arrays.  TEST INFRASTRUCTURE ONLY: it pins the oracle's prolongate /
+// defect_restriction (and with them the per-child Q2 and P1disc matrices)
+// and its V-cycle against the reference code itself.
 // Built by oracle/build_oracle.py (build_ref_transfer) into
 // oracle/_ref/libref_transfer.so, with -D__3D__ -D_SEQ, from the reference
 // sources where they lie.
@@ -54,26 +55,47 @@
 //   library links with -Bsymbolic, so the reference objects in it call
 //   these; no other library does).
 // No reference destructor runs; the harness frees what it allocated.
+//
+// The same two levels also run the reference's multigrid cycle
+// (ref_cycle_*): TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132), the
+// preconditioner call, with TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:
+// 434-1779) over two TNSE_MGLevel4 levels (src/FE/NSE_MGLevel4.C) built on
+// the levels' spaces and matrices: cell Vanka pre- and post-smoothing (the
+// _SEQ cell loop), the level defects, DefectRestriction, SolveExact on the
+// coarse level, Prolongate, CorrectNodes and Update.  The fine cells keep
+// the child frames described above, so the fine level's B rows and BT
+// columns of every cell's linear pressure modes are transformed by that
+// cell's signed permutation, and so are the pressure parts of the vectors
+// on the way in and out; velocity DOFs keep their global numbers.
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <algorithm>
+#include <utility>
 #include <vector>
 
 #include <BaseCell.h>
 #include <BaseFunct3D.h>
 #include <Collection.h>
 #include <Database.h>
+#include <DirectSolver.h>
 #include <FE3D.h>
 #include <FEDatabase3D.h>
 #include <FESpace3D.h>
 #include <GridCell.h>
 #include <LinAlg.h>
+#include <Matrix3D.h>
 #include <MultiGrid3D.h>
+#include <MultiGridIte.h>
+#include <NSE_MGLevel4.h>  // includes Magma_Solver.h (no include guard)
+#include <NSE_MultiGrid.h>
 #include <RefDesc.h>
+#include <SquareMatrix3D.h>
 #include <Vertex.h>
 
+#include "ref_lapack.h"
 #include "ref_level_space.h"
 
 void *operator new(std::size_t n) {
@@ -347,6 +369,260 @@ __attribute__((visibility("default"))) void ref_transfer_restrict(void *h, const
   DefectRestriction(C.us, F.us, 3, coarse, fu.data(), aux.data());
   DefectRestriction(C.ps, F.ps, coarse + 3 * (size_t)C.n_u, fu.data() + 3 * (size_t)F.n_u,
                     aux.data());
+}
+
+
+// ================================================================ cycle ====
+}  // extern "C"
+
+void DirectSolver(TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *,
+                  TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *,
+                  TSquareMatrix3D *, TMatrix3D *, TMatrix3D *, TMatrix3D *, TMatrix3D *,
+                  TMatrix3D *, TMatrix3D *, double *, double *, int) {
+  std::fprintf(stderr, "ref_cycle: DirectSolver is not part of the harness\n");
+  std::abort();
+}
+
+namespace {
+
+struct CycleLevel : public TNSE_MGLevel4 {
+  using TNSE_MGLevel4::TNSE_MGLevel4;
+  // the auxiliary vectors of the constructor (src/FE/NSE_MGLevel4.C:274-278)
+  void release() {
+    delete[] Aux[0];
+    delete[] Aux;
+  }
+};
+
+// One level's matrices, vectors and TNSE_MGLevel4 over a Side's spaces
+struct MGLevelStore {
+  alignas(LevelSpace) unsigned char oa_store[sizeof(LevelSpace)];
+  alignas(LevelSpace) unsigned char ob_store[sizeof(LevelSpace)];
+  LevelSpace *oa = nullptr, *ob = nullptr;
+  TCollection *other_a = nullptr, *other_b = nullptr;
+  LevelSquareStructure *sa = nullptr;
+  LevelStructure *sb = nullptr, *sbt = nullptr;
+  alignas(TSquareMatrix3D) unsigned char a_store[9][sizeof(TSquareMatrix3D)];
+  alignas(TMatrix3D) unsigned char b_store[6][sizeof(TMatrix3D)];
+  TSquareMatrix3D *A[9] = {};
+  TMatrix3D *B[6] = {};
+  double *f = nullptr, *u = nullptr;
+  double al[2] = {1.0, 1.0};
+  alignas(CycleLevel) unsigned char level_store[sizeof(CycleLevel)];
+  CycleLevel *level = nullptr;
+};
+
+int *copy_ints(const int *src, long n) {
+  int *d = new int[n > 0 ? n : 1];
+  if (n > 0) std::memcpy(d, src, sizeof(int) * n);
+  return d;
+}
+
+// B (pressure rows) and BT (pressure columns) of level S with the linear
+// pressure modes of every cell c taken in frame `frame[c]` (a reference child
+// number, or -1 for the axis-aligned frame): row / column of mode i is
+// sign_i times the one of axis mode axis(i)
+void frame_pressure(const Side &S, const int *frame, int n_u, const int *b_rowptr,
+                    const int *b_col, const double *const *b, const int *bt_rowptr,
+                    const int *bt_col, const double *const *bt, std::vector<int> &brp,
+                    std::vector<int> &bc, std::vector<double> (&bv)[3], std::vector<int> &btc,
+                    std::vector<double> (&btv)[3]) {
+  const int n_p = S.n_p;
+  // per pressure DOF: the source row and its sign (B); per source column its
+  // new column and sign (BT)
+  std::vector<int> src(n_p), dst(n_p);
+  std::vector<double> sg(n_p, 1.0), dsg(n_p, 1.0);
+  for (int q = 0; q < n_p; ++q) src[q] = dst[q] = q;
+  for (int c = 0; c < S.n_cells; ++c) {
+    const int j = frame[c];
+    if (j < 0) continue;
+    const int *dof = S.pg + 4 * (size_t)c;
+    for (int i = 0; i < 3; ++i) {
+      src[dof[1 + i]] = dof[1 + g_paxis[j][i]];
+      sg[dof[1 + i]] = g_psign[j][i];
+      dst[dof[1 + g_paxis[j][i]]] = dof[1 + i];
+      dsg[dof[1 + g_paxis[j][i]]] = g_psign[j][i];
+    }
+  }
+  brp.assign(n_p + 1, 0);
+  bc.clear();
+  for (int k = 0; k < 3; ++k) bv[k].clear();
+  for (int q = 0; q < n_p; ++q) {
+    const int r = src[q];
+    for (int e = b_rowptr[r]; e < b_rowptr[r + 1]; ++e) {
+      bc.push_back(b_col[e]);
+      for (int k = 0; k < 3; ++k) bv[k].push_back(sg[q] * b[k][e]);
+    }
+    brp[q + 1] = (int)bc.size();
+  }
+  btc.assign(bt_col, bt_col + bt_rowptr[n_u]);
+  for (int k = 0; k < 3; ++k) btv[k].assign(bt[k], bt[k] + bt_rowptr[n_u]);
+  for (int i = 0; i < n_u; ++i) {
+    const int e0 = bt_rowptr[i], e1 = bt_rowptr[i + 1];
+    std::vector<std::pair<int, int>> order;  // (new column, entry)
+    for (int e = e0; e < e1; ++e) order.emplace_back(dst[bt_col[e]], e);
+    std::sort(order.begin(), order.end());
+    for (int t = 0; t < e1 - e0; ++t) {
+      const int e = order[(size_t)t].second;
+      btc[(size_t)e0 + t] = order[(size_t)t].first;
+      for (int k = 0; k < 3; ++k) btv[k][(size_t)e0 + t] = dsg[bt_col[e]] * bt[k][e];
+    }
+  }
+}
+
+void make_mg_level(MGLevelStore &M, Side &S, int level, int n_active, int n_blocks,
+                   const int *a_rowptr, const int *a_col, const double *const *a,
+                   const std::vector<int> &brp, const std::vector<int> &bc,
+                   const std::vector<double> (&bv)[3], const int *bt_rowptr,
+                   const std::vector<int> &btc, const std::vector<double> (&btv)[3],
+                   double alpha, double beta) {
+  const int n_u = S.n_u, n_p = S.n_p, n = 3 * n_u + n_p;
+  M.other_a = new TCollection(0, nullptr);
+  M.other_b = new TCollection(0, nullptr);
+  M.oa = new (M.oa_store) LevelSpace(M.other_a, 0, 0, 0, nullptr, nullptr, nullptr);
+  M.ob = new (M.ob_store) LevelSpace(M.other_b, 0, 0, 0, nullptr, nullptr, nullptr);
+  const int a_nnz = a_rowptr[n_u], b_nnz = brp[n_p], bt_nnz = bt_rowptr[n_u];
+  M.sa = new LevelSquareStructure(n_u, n_active, a_nnz, copy_ints(a_col, a_nnz),
+                                  copy_ints(a_rowptr, n_u + 1L), S.us);
+  M.sb = new LevelStructure(M.oa, M.ob, S.ps, S.us, n_p, n_u, b_nnz,
+                            copy_ints(bc.data(), b_nnz), copy_ints(brp.data(), n_p + 1L));
+  M.sbt = new LevelStructure(M.oa, M.ob, S.us, S.ps, n_u, n_p, bt_nnz,
+                             copy_ints(btc.data(), bt_nnz), copy_ints(bt_rowptr, n_u + 1L));
+  for (int k = 0; k < 9; ++k) {
+    M.A[k] = new (M.a_store[k]) TSquareMatrix3D(M.sa);  // allocates its entries
+    // one-block levels: A11 = A22 = A33 = a[0], A12..A32 = 0
+    const double *src = n_blocks == 9 ? a[k] : (k % 4 == 0 ? a[0] : nullptr);
+    if (src)
+      std::memcpy(M.A[k]->GetEntries(), src, sizeof(double) * a_nnz);
+    else
+      std::memset(M.A[k]->GetEntries(), 0, sizeof(double) * a_nnz);
+  }
+  for (int k = 0; k < 3; ++k) {
+    M.B[k] = new (M.b_store[k]) TMatrix3D(M.sb);
+    std::memcpy(M.B[k]->GetEntries(), bv[k].data(), sizeof(double) * b_nnz);
+    M.B[3 + k] = new (M.b_store[3 + k]) TMatrix3D(M.sbt);
+    std::memcpy(M.B[3 + k]->GetEntries(), btv[k].data(), sizeof(double) * bt_nnz);
+  }
+  M.f = new double[n]();
+  M.u = new double[n]();
+  M.al[0] = alpha;  // CellVanka's relaxation
+  M.al[1] = beta;   // the coarse-grid correction's damping (TNSE_MGLevel::Update)
+  // four auxiliary vectors, as TSystemNSE3D creates its levels; velocity
+  // space 2 (Q2) and pressure space -11 (P1disc: the L2_0 projections of
+  // CorrectNodes, CorrectDefect and Defect act on the constant modes)
+  M.level = new (M.level_store)
+      CycleLevel(level, M.A[0], M.A[1], M.A[2], M.A[3], M.A[4], M.A[5], M.A[6], M.A[7], M.A[8],
+                 M.B[0], M.B[1], M.B[2], M.B[3], M.B[4], M.B[5], M.f, M.u, 4, M.al, 2, -11,
+                 S.coll, nullptr);
+}
+
+void free_mg_level(MGLevelStore &M) {
+  M.level->release();
+  for (int k = 0; k < 9; ++k) delete[] M.A[k]->GetEntries();
+  for (int k = 0; k < 6; ++k) delete[] M.B[k]->GetEntries();
+  // the structures' destructors free their column and row-pointer copies
+  delete M.sa;
+  delete M.sb;
+  delete M.sbt;
+  M.oa->release_names();
+  M.ob->release_names();
+  delete M.other_a;
+  delete M.other_b;
+  delete[] M.f;
+  delete[] M.u;
+}
+
+struct Cycle2 {
+  Pair *T = nullptr;
+  MGLevelStore lev[2];
+  TNSE_MultiGrid *mg = nullptr;
+  alignas(TMultiGridIte) unsigned char ite_store[sizeof(TMultiGridIte)];
+  TMultiGridIte *ite = nullptr;
+};
+
+}  // namespace
+
+extern "C" {
+
+// The two levels of ref_transfer_create with their matrices (A: nine blocks
+// a[0..8], or a[0] alone for a one-block level; B: n_p x n_u, BT: n_u x n_p,
+// three blocks each) as the solver's level descriptors hold them, the level
+// relaxation alpha and the coarse-grid correction damping beta (al[0] and
+// al[1] of TNSE_MGLevel4, SC_GMG_DAMP_FACTOR_SADDLE).  Returns null when the
+// levels are not a regular refinement.
+__attribute__((visibility("default"))) void *ref_cycle_create(
+    int nc_cells, int nc_u, int nc_active, int nc_p, const int *c_udofs, const int *c_pdofs,
+    int nf_cells, int nf_u, int nf_active, int nf_p, const int *f_udofs, const int *f_pdofs,
+    const int *fine_parent, const int *fine_child, int n_blocks, const int *const *a_rowptr,
+    const int *const *a_col, const double *const *a, const int *const *b_rowptr,
+    const int *const *b_col, const double *const *b, const int *const *bt_rowptr,
+    const int *const *bt_col, const double *const *bt, double alpha, double beta) {
+  void *tp = ref_transfer_create(nc_cells, nc_u, nc_active, nc_p, c_udofs, c_pdofs, nf_cells,
+                                 nf_u, nf_active, nf_p, f_udofs, f_pdofs, fine_parent, fine_child);
+  if (!tp) return nullptr;
+  Cycle2 *Y = new Cycle2;
+  Y->T = static_cast<Pair *>(tp);
+  Side *side[2] = {&Y->T->coarse, &Y->T->fine};
+  const int active[2] = {nc_active, nf_active};
+  std::vector<int> axis_frame(nc_cells, -1);
+  for (int l = 0; l < 2; ++l) {
+    Side &S = *side[l];
+    std::vector<int> brp, bc, btc;
+    std::vector<double> bv[3], btv[3];
+    frame_pressure(S, l == 0 ? axis_frame.data() : Y->T->ref_child.data(), S.n_u, b_rowptr[l],
+                   b_col[l], b + 3 * l, bt_rowptr[l], bt_col[l], bt + 3 * l, brp, bc, bv, btc,
+                   btv);
+    make_mg_level(Y->lev[l], S, l, active[l], n_blocks, a_rowptr[l], a_col[l], a + 9 * l, brp,
+                  bc, bv, bt_rowptr[l], btc, btv, alpha, beta);
+  }
+  Y->mg = new TNSE_MultiGrid(1, 0, nullptr);
+  for (int l = 0; l < 2; ++l) Y->mg->AddLevel(Y->lev[l].level);
+  const int n_fine = 3 * nf_u + nf_p;
+  Y->ite = new (Y->ite_store) TMultiGridIte(nullptr, nullptr, nullptr, 0, n_fine, Y->mg, 1);
+  return Y;
+}
+
+__attribute__((visibility("default"))) void ref_cycle_destroy(void *h) {
+  Cycle2 *Y = static_cast<Cycle2 *>(h);
+  if (!Y) return;
+  // TItMethod's constructor allocates no vector for n_aux = 0
+  for (int l = 0; l < 2; ++l) free_mg_level(Y->lev[l]);
+  ::operator delete(static_cast<void *>(Y->mg));  // storage only: no reference destructor
+  ref_transfer_destroy(Y->T);
+  delete Y;
+}
+
+// z = one V(pre, post) cycle from zero on v (fine level, [u1|u2|u3|p] with
+// the pressure in the axis-aligned frame): TMultiGridIte::Iterate with cell
+// Vanka (SC_SMOOTHER_SADDLE 2, damping `damp`, direct local solves), the
+// coarse level solved exactly (SC_COARSE_SMOOTHER_SADDLE 17, first pressure
+// equation pinned), no step-length control.
+__attribute__((visibility("default"))) void ref_cycle_vcycle(void *h, const double *v, double *z,
+                                                             int pre, int post, double damp) {
+  Cycle2 *Y = static_cast<Cycle2 *>(h);
+  TParamDB *db = TDatabase::ParamDB;
+  db->SC_SMOOTHER_SADDLE = 2;
+  db->SC_COARSE_SMOOTHER_SADDLE = 17;
+  db->SC_PRE_SMOOTH_SADDLE = pre;
+  db->SC_POST_SMOOTH_SADDLE = post;
+  db->SC_SMOOTH_DAMP_FACTOR_SADDLE = damp;
+  db->SC_SMOOTH_DAMP_FACTOR_COARSE_SADDLE = damp;
+  db->SC_SMOOTH_DAMP_FACTOR_FINE_SADDLE = damp;
+  db->SC_MG_CYCLE_SADDLE = 1;
+  db->SC_STEP_LENGTH_CONTROL_ALL_SADDLE = 0;
+  db->SC_STEP_LENGTH_CONTROL_FINE_SADDLE = 0;
+  db->SC_LARGEST_DIRECT_SOLVE = 1 << 20;
+  db->INTERNAL_LOCAL_DOF = -1;
+  db->INTERNAL_PROJECT_PRESSURE = 1;
+  db->INTERNAL_PRESSURE_SPACE = -11;
+  db->SC_VERBOSE = 0;
+  db->MG_DEBUG = 0;
+  const Side &F = Y->T->fine;
+  const int n = 3 * F.n_u + F.n_p;
+  std::vector<double> rhs(v, v + n);
+  convert_pressure(*Y->T, rhs.data() + 3 * (size_t)F.n_u, true);
+  Y->ite->Iterate(nullptr, nullptr, z, rhs.data());
+  convert_pressure(*Y->T, z + 3 * (size_t)F.n_u, false);
 }
 
 }  // extern "C"

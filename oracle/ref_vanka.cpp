@@ -72,73 +72,7 @@ void DirectSolver(TSquareMatrix3D *, TSquareMatrix3D *, TSquareMatrix3D *, TSqua
   std::abort();
 }
 
-extern "C" {
-void dgetrf_(int *m, int *n, double *a, int *lda, int *ipiv, int *info) {
-  const int N = *n, ld = *lda;
-  *info = 0;
-  if (*m != N) {
-    *info = -1;
-    return;
-  }
-  for (int k = 0; k < N; ++k) {
-    int p = k;
-    double amax = std::fabs(a[k + k * ld]);
-    for (int i = k + 1; i < N; ++i) {
-      const double v = std::fabs(a[i + k * ld]);
-      if (v > amax) {
-        amax = v;
-        p = i;
-      }
-    }
-    ipiv[k] = p + 1;
-    if (p != k)
-      for (int j = 0; j < N; ++j) {
-        const double t = a[k + j * ld];
-        a[k + j * ld] = a[p + j * ld];
-        a[p + j * ld] = t;
-      }
-    const double piv = a[k + k * ld];
-    if (piv != 0.0) {
-      const double r = 1.0 / piv;
-      for (int i = k + 1; i < N; ++i) a[i + k * ld] *= r;
-    } else if (*info == 0) {
-      *info = k + 1;
-    }
-    for (int j = k + 1; j < N; ++j) {
-      const double ukj = a[k + j * ld];
-      if (ukj == 0.0) continue;
-      for (int i = k + 1; i < N; ++i) a[i + j * ld] -= a[i + k * ld] * ukj;
-    }
-  }
-}
-
-void dgetrs_(char *trans, int *n, int *nrhs, double *a, int *lda, int *ipiv, double *b, int *ldb,
-             int *info) {
-  const int N = *n, ld = *lda;
-  *info = (*trans == 'n' || *trans == 'N') ? 0 : -1;
-  if (*info) return;
-  for (int r = 0; r < *nrhs; ++r) {
-    double *x = b + (size_t)r * *ldb;
-    for (int k = 0; k < N; ++k)
-      if (ipiv[k] - 1 != k) {
-        const double t = x[k];
-        x[k] = x[ipiv[k] - 1];
-        x[ipiv[k] - 1] = t;
-      }
-    for (int j = 0; j < N; ++j) {
-      const double xj = x[j];
-      if (xj != 0.0)
-        for (int i = j + 1; i < N; ++i) x[i] -= a[i + j * ld] * xj;
-    }
-    for (int j = N - 1; j >= 0; --j) {
-      x[j] /= a[j + j * ld];
-      const double xj = x[j];
-      if (xj != 0.0)
-        for (int i = 0; i < j; ++i) x[i] -= a[i + j * ld] * xj;
-    }
-  }
-}
-}  // extern "C"
+#include "ref_lapack.h"
 
 namespace {
 
@@ -149,33 +83,6 @@ struct FixedElement : public TFE3D {
 // element ids the level's spaces name (any two distinct ids serve)
 const FE3D kVelocityElement = C_Q2_3D_H_A;
 const FE3D kPressureElement = D_P1_3D_H_A;
-
-struct LevelSquareStructure : public TSquareStructure3D {
-  LevelSquareStructure(int n, int active, int nnz, int *col, int *rowptr, TFESpace3D *space)
-      : TSquareStructure3D(n, nnz, col, rowptr) {
-    ActiveBound = active;
-    FESpace = space;
-  }
-};
-
-struct LevelStructure : public TStructure3D {
-  LevelStructure(TFESpace3D *other_a, TFESpace3D *other_b, TFESpace3D *test, TFESpace3D *ansatz,
-                 int rows, int cols, int nnz, int *col, int *rowptr)
-      : TStructure3D(other_a, other_b) {
-    N_Rows = rows;
-    N_Columns = cols;
-    N_Entries = nnz;
-    KCol = col;
-    RowPtr = rowptr;
-    HangingN_Entries = 0;
-    HangingKCol = nullptr;
-    HangingRowPtr = nullptr;
-    TestSpace3D = test;
-    AnsatzSpace3D = ansatz;
-    TestSpace2D = nullptr;
-    AnsatzSpace2D = nullptr;
-  }
-};
 
 struct Level : public TNSE_MGLevel4 {
   using TNSE_MGLevel4::TNSE_MGLevel4;

@@ -11,8 +11,14 @@ oracle/build_oracle.py compiles with the reference sources where they lie:
   on the coarsest level;
 * tests/golden/ref_vanka_*.npz: one and two sweeps of the cell Vanka
   TNSE_MGLevel4::CellVanka (src/FE/NSE_MGLevel4.C:1653-2087, sequential
-  build, damping 1, no relaxation) from u = x with right-hand side b.
+  build, damping 1, no relaxation) from u = x with right-hand side b;
+* tests/golden/ref_cycle_*.npz: one V(2,2) cycle from zero on b, the
+  preconditioner call TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132)
+  with TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779) over two
+  TNSE_MGLevel4 levels: cell Vanka on the fine level (sequential build),
+  SolveExact on the coarse one, the reference's transfers between them.
 Needs the reference tree; the fixtures are committed so the tests do not.
+``python make_ref_golden.py cycle`` writes the cycle fixtures only.
 
 Inputs are exact binary fractions of the DOF index (``golden_inputs``), so
 every platform forms the same x and b without a random generator.
@@ -69,10 +75,35 @@ TRANSFER_CASES = {
 }
 
 
+# name -> OseenProblem keyword arguments of the cycle fixtures (two levels:
+# the V-cycle of the fine level over the exactly solved coarse one)
+CYCLE_CASES = {
+    "hexa": CASES["hexa"][0],
+    "channel": CASES["channel"][0],
+}
+
+
+def write_cycle_fixtures() -> None:
+    from oracle.pyref import RefCycle
+    for name, kwargs in CYCLE_CASES.items():
+        P = build_problem(kwargs)
+        _, b = golden_inputs(P.ndof(-1))
+        np.savez_compressed(
+            HERE / f"ref_cycle_{name}.npz", problem=json.dumps(kwargs), level=P.n_levels - 1,
+            vcycle=RefCycle(P).vcycle(b, pre=2, post=2, damp=1.0),
+            source=("reference src/FE/MultiGridIte.C TMultiGridIte::Iterate with "
+                    "src/FE/NSE_MultiGrid.C TNSE_MultiGrid::Cycle (V(2,2), cell Vanka _SEQ, "
+                    "SolveExact) run by oracle/ref_transfer.cpp"))
+        print("wrote cycle", name, "ndof", P.ndof(-1))
+
+
 def main() -> None:
     from oracle.pyref import RefLevel, RefTransfer, RefVankaLevel, ref_harness_lib
     if ref_harness_lib() is None:
         raise SystemExit("reference tree not found; cannot regenerate the defect golden files")
+    if sys.argv[1:] == ["cycle"]:
+        write_cycle_fixtures()
+        return
     for name, (kwargs, level) in CASES.items():
         P = build_problem(kwargs)
         R = RefLevel(P.arrays(level), threads=1)
@@ -117,6 +148,7 @@ def main() -> None:
             source=("reference src/FE/MGComponents3D.C Prolongate / DefectRestriction "
                     "run by oracle/ref_transfer.cpp"))
         print("wrote transfer", name, "level", level)
+    write_cycle_fixtures()
 
 
 if __name__ == "__main__":

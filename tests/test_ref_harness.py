@@ -33,6 +33,11 @@ for bit) as tests/golden/ref_coarse_*.npz (oracle 1e-12, GPU 1e-10).
 The GPU's colour-block sweep equals the sequential cell loop when every cell
 is its own colour, so the CUDA Vanka is checked against the reference's with
 such a colouring, at 1e-9 relative (FP64 LU rounding).
+The same transfer harness runs the reference's cycle driver,
+TMultiGridIte::Iterate with TNSE_MultiGrid::Cycle, over two levels; the
+oracle's V-cycle agrees with it to 1e-13 (the fine cells' local DOF orders
+differ), and its output is committed as tests/golden/ref_cycle_*.npz (oracle
+1e-13, the FP64 CUDA V-cycle with one cell per colour 1e-9).
 """
 import ctypes as C
 import importlib.util
@@ -80,6 +85,8 @@ def load_case(name, kind="defect"):
         assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
     elif kind in ("vanka", "coarse"):
         assert P.arrays(level)["n_cells"] == int(g["n_cells"])
+    elif kind == "cycle":
+        assert level == P.n_levels - 1
     if kind == "transfer":  # x on the coarse level, b on the fine one
         return P, level, gm.golden_inputs(P.ndof(level - 1))[0], gm.golden_inputs(P.ndof(level))[1], g
     x, b = gm.golden_inputs(P.ndof(level))
@@ -435,3 +442,65 @@ def test_gpu_coarse_solve_matches_reference_fixtures(name):
     P, level, _, b, g = load_case(name, "coarse")
     S = PmSolver(P.descs, precision="fp64")
     assert rel(S.solve_exact(b), g["solution"]) < 1e-10
+
+
+# --------------------------------------------------------------- cycle ----
+# oracle/ref_transfer.cpp also runs the reference's multigrid preconditioner
+# call, TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132) with
+# TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779), over two
+# TNSE_MGLevel4 levels built on the transfer harness's cells and spaces:
+# sequential cell Vanka on the fine level, SolveExact on the coarse one, the
+# reference's DefectRestriction / Prolongate, CorrectDefect, CorrectNodes and
+# Update between them.  The fine cells are in the reference's child frames
+# (their local DOF orders differ from the oracle's), so the local solves
+# round differently: the oracle's V-cycle is checked to 1e-13.
+
+CYCLE_PARAMS = [(2, 2, 1.0, 1.0, 1.0), (1, 3, 0.8, 1.0, 1.0), (2, 2, 1.0, 0.9, 0.7)]
+
+
+@pytest.mark.parametrize("name", ["hexa", "channel"])
+@pytest.mark.parametrize("pre,post,damp,alpha,beta", CYCLE_PARAMS)
+def test_oracle_vcycle_matches_the_reference_cycle_driver(name, pre, post, damp, alpha, beta):
+    """Smoothing counts, Vanka damping, the level relaxation alpha and the
+    coarse-grid-correction damping beta (SC_GMG_DAMP_FACTOR_SADDLE)."""
+    from oracle.pyref import ref_transfer_lib
+    if ref_transfer_lib() is None:
+        pytest.skip("reference tree not present (the committed fixtures cover this case)")
+    from oracle.pyref import RefCycle
+    gm = _golden_module()
+    P = gm.build_problem(gm.CYCLE_CASES[name])
+    _, b = gm.golden_inputs(P.ndof(-1))
+    z_ref = RefCycle(P, alpha=alpha, beta=beta).vcycle(b, pre=pre, post=post, damp=damp)
+    O = Oracle(P, vanka_mode="seq", pre_smooth=pre, post_smooth=post, smooth_damp=damp,
+               alpha=alpha, beta=beta)
+    assert rel(O.vcycle(b), z_ref) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["hexa", "channel"])
+def test_cycle_fixtures_reproduce_from_the_reference(name):
+    from oracle.pyref import ref_transfer_lib
+    if ref_transfer_lib() is None:
+        pytest.skip("reference tree not present (the committed fixtures cover this case)")
+    from oracle.pyref import RefCycle
+    P, level, _, b, g = load_case(name, "cycle")
+    assert np.array_equal(RefCycle(P).vcycle(b, pre=2, post=2, damp=1.0), g["vcycle"])
+
+
+@pytest.mark.parametrize("name", ["hexa", "channel"])
+def test_oracle_vcycle_matches_reference_cycle_fixtures(name):
+    P, level, _, b, g = load_case(name, "cycle")
+    assert rel(Oracle(P, vanka_mode="seq").vcycle(b), g["vcycle"]) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hexa", "channel"])
+def test_gpu_vcycle_matches_reference_cycle_fixtures(name):
+    """The FP64 CUDA V-cycle (graph-captured, cell Vanka with one cell per
+    colour on the fine level: the sequential order, block-elimination local
+    solves) against the reference's own cycle driver."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, _, b, g = load_case(name, "cycle")
+    descs, colours = per_cell_colours(P, level)
+    S = PmSolver(descs, precision="fp64")
+    assert rel(S.vcycle(b), g["vcycle"]) < 1e-9
+    del colours
