@@ -11,10 +11,11 @@
   outputs are committed as tests/golden/ref_defect_*.npz, ref_vanka_*.npz).
 * ``oracle/_ref/libref_transfer.so`` — the reference's grid transfers with
   the FE and geometry databases they read, and its multigrid cycle driver
-  (TMultiGridIte, TNSE_MultiGrid) over two TNSE_MGLevel4 levels
+  (TMultiGridIte, TNSE_MultiGrid) over one TNSE_MGLevel4 per level
   (REF_TRANSFER_TUS), driven by ref_transfer.cpp (only when the tree is
   present; its outputs are committed as tests/golden/ref_transfer_*.npz and
-  tests/golden/ref_cycle_*.npz).
+  tests/golden/ref_cycle_*.npz, and with libref_harness.so's FGMRES as
+  tests/golden/ref_solve_*.npz).
 * ``oracle/_ref/libref_facade.so`` — include/pmgpu_parmoon.h (the solver as a
   ParMooN TItMethod) compiled against the reference's headers and matrix
   classes in ref_facade.cpp, linked with libpmgpu.so (only when the tree is

@@ -5,7 +5,8 @@ and cell Vanka (TNSE_MGLevel4::CellVanka, src/FE/NSE_MGLevel4.C:1653) run on
 one level of a problem built here; and (oracle/_ref/libref_transfer.so) the
 grid transfers Prolongate / DefectRestriction between two levels and the
 multigrid cycle driver (TMultiGridIte::Iterate, TNSE_MultiGrid::Cycle) over
-them.  TEST INFRASTRUCTURE ONLY — it exists where the reference tree does (see
+all levels of a problem, which the harnessed FGMRES can take as its
+preconditioner (the whole reference solver).  TEST INFRASTRUCTURE ONLY — it exists where the reference tree does (see
 build_ref_harness, build_ref_transfer).
 """
 from __future__ import annotations
@@ -153,14 +154,28 @@ class RefLevel:
         called directly as the harness's C preconditioner), with the
         oracle's restart / maxit / minit / red_factor / res_norm_min /
         div_factor / project_pressure.  Returns (solution, iterations)."""
-        p = oracle.params
+        assert self.ndof == oracle.ndof(-1)
+        fn = C.cast(oracle._L.oracle_vcycle, C.c_void_p)
+        return self.fgmres(fn, C.c_void_p(oracle._h), oracle.params, sol, rhs)
+
+    def fgmres_with_reference_cycle(self, cycle, params, sol, rhs) -> tuple[np.ndarray, int]:
+        """The whole reference solver: its FGMRES on this level (the
+        cycle's finest) preconditioned by its own cycle driver (``cycle``, a
+        RefCycle), with the smoothing and FGMRES parameters of ``params``
+        (an oracle's OracleParams).  Returns (solution, iterations)."""
+        assert self.ndof == cycle.nf
+        fn, ctx = cycle.preconditioner(params.pre_smooth, params.post_smooth, params.smooth_damp)
+        return self.fgmres(fn, ctx, params, sol, rhs)
+
+    def fgmres(self, fn, ctx, p, sol, rhs) -> tuple[np.ndarray, int]:
+        """ref_fgmres with the C preconditioner ``fn(ctx, z, v)`` and the
+        FGMRES parameters of ``p`` (an OracleParams)."""
         sol = np.array(sol, dtype=np.float64, copy=True)
         rhs, rp = _d(rhs)
-        assert sol.size == self.ndof == rhs.size == oracle.ndof(-1)
-        fn = C.cast(oracle._L.oracle_vcycle, C.c_void_p)
+        assert sol.size == self.ndof == rhs.size
         it = self._L.ref_fgmres(self._h, sol.ctypes.data_as(_dp), rp, p.restart, p.maxit,
                                 p.minit, p.red_factor, p.res_norm_min, p.div_factor,
-                                p.project_pressure, fn, C.c_void_p(oracle._h), self.threads)
+                                p.project_pressure, fn, ctx, self.threads)
         if it < 0:
             raise ValueError("ref_fgmres refused the parameters (div_factor < 1)")
         return sol, it
@@ -251,7 +266,7 @@ def ref_transfer_lib():
         L.ref_transfer_restrict.argtypes = [C.c_void_p, _dp, _dp]
         L.ref_transfer_restrict.restype = None
         _ipp = C.POINTER(_ip)
-        L.ref_cycle_create.argtypes = ([C.c_int] * 4 + [_ip, _ip] + [C.c_int] * 4 + [_ip] * 4
+        L.ref_cycle_create.argtypes = ([C.c_int] + [_ip] * 4 + [_ipp] * 4
                                        + [C.c_int, _ipp, _ipp, _dpp, _ipp, _ipp, _dpp, _ipp,
                                           _ipp, _dpp, C.c_double, C.c_double])
         L.ref_cycle_create.restype = C.c_void_p
@@ -259,6 +274,8 @@ def ref_transfer_lib():
         L.ref_cycle_destroy.restype = None
         L.ref_cycle_vcycle.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_double]
         L.ref_cycle_vcycle.restype = None
+        L.ref_cycle_configure.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
+        L.ref_cycle_configure.restype = None
         _TLIB = L
     return _TLIB
 
@@ -310,10 +327,9 @@ class RefTransfer:
 class RefCycle:
     """The reference's multigrid preconditioner call, TMultiGridIte::Iterate
     (src/FE/MultiGridIte.C:76-132) with TNSE_MultiGrid::Cycle
-    (src/FE/NSE_MultiGrid.C:434-1779), over the two finest levels of a
-    hexahedral Q2/P1disc problem (run by oracle/ref_transfer.cpp).  A problem
-    of two levels gives the whole V-cycle: cell Vanka on the fine level, the
-    exact solve on the coarse one."""
+    (src/FE/NSE_MultiGrid.C:434-1779), over every level of a hexahedral
+    Q2/P1disc problem (run by oracle/ref_transfer.cpp): cell Vanka on each
+    level above the coarsest, the exact solve on the coarsest one."""
 
     def __init__(self, problem, alpha: float = 1.0, beta: float = 1.0):
         L = ref_transfer_lib()
@@ -321,35 +337,45 @@ class RefCycle:
             raise RuntimeError("reference tree not present: the transfer harness is not built")
         self._L = L
         self._h = None
-        top = problem.n_levels - 1
-        c, f = problem.arrays(top - 1), problem.arrays(top)
-        self.nf = 3 * f["n_udof"] + f["n_pdof"]
-        ints = [np.ascontiguousarray(a, dtype=np.int32) for a in
-                (c["cell_udofs"], c["cell_pdofs"], f["cell_udofs"], f["cell_pdofs"],
-                 f["cell_parent"], f["cell_child"])]
-        keep = list(ints)
+        lv = [problem.arrays(l) for l in range(problem.n_levels)]
+        top = lv[-1]
+        self.nf = 3 * top["n_udof"] + top["n_pdof"]
+        keep = []
 
-        def iarr(*arrs):
-            v = [np.ascontiguousarray(a, dtype=np.int32) for a in arrs]
-            keep.extend(v)
-            return (_ip * len(v))(*[a.ctypes.data_as(_ip) for a in v])
+        def ints(vals):
+            v = np.ascontiguousarray(vals, dtype=np.int32)
+            keep.append(v)
+            return v.ctypes.data_as(_ip)
+
+        def iarr(arrs):  # one int array per entry; None -> null
+            v = [None if a is None else np.ascontiguousarray(a, dtype=np.int32) for a in arrs]
+            keep.extend(x for x in v if x is not None)
+            return (_ip * len(v))(*[_ip() if x is None else x.ctypes.data_as(_ip) for x in v])
 
         def darr(arrs):
             v = [np.ascontiguousarray(a, dtype=np.float64) for a in arrs]
             keep.extend(v)
             return (_dp * len(v))(*[a.ctypes.data_as(_dp) for a in v])
 
-        n_blocks = len(c["a"])
-        ptr = [a.ctypes.data_as(_ip) for a in ints]
+        n_blocks = len(lv[0]["a"])
+        assert all(len(d["a"]) == n_blocks for d in lv)
+
+        def cat(key):
+            return [m for d in lv for m in d[key]]
+
         self._keep = keep
         self._h = L.ref_cycle_create(
-            c["n_cells"], c["n_udof"], c["n_active"], c["n_pdof"], ptr[0], ptr[1], f["n_cells"],
-            f["n_udof"], f["n_active"], f["n_pdof"], *ptr[2:], n_blocks,
-            iarr(c["a_rowptr"], f["a_rowptr"]), iarr(c["a_col"], f["a_col"]),
-            darr(list(c["a"]) + list(f["a"])), iarr(c["b_rowptr"], f["b_rowptr"]),
-            iarr(c["b_col"], f["b_col"]), darr(list(c["b"]) + list(f["b"])),
-            iarr(c["bt_rowptr"], f["bt_rowptr"]), iarr(c["bt_col"], f["bt_col"]),
-            darr(list(c["bt"]) + list(f["bt"])), alpha, beta)
+            len(lv), ints([d["n_cells"] for d in lv]), ints([d["n_udof"] for d in lv]),
+            ints([d["n_active"] for d in lv]), ints([d["n_pdof"] for d in lv]),
+            iarr([d["cell_udofs"] for d in lv]), iarr([d["cell_pdofs"] for d in lv]),
+            iarr([None] + [d["cell_parent"] for d in lv[1:]]),
+            iarr([None] + [d["cell_child"] for d in lv[1:]]), n_blocks,
+            iarr([d["a_rowptr"] for d in lv]), iarr([d["a_col"] for d in lv]),
+            darr(cat("a") if n_blocks == 9 else
+                 [m for d in lv for m in list(d["a"]) + [d["a"][0]] * 8]),
+            iarr([d["b_rowptr"] for d in lv]), iarr([d["b_col"] for d in lv]), darr(cat("b")),
+            iarr([d["bt_rowptr"] for d in lv]), iarr([d["bt_col"] for d in lv]), darr(cat("bt")),
+            alpha, beta)
         if not self._h:
             raise ValueError("the levels are not a regular refinement (8 children per cell)")
 
@@ -364,6 +390,12 @@ class RefCycle:
         z = np.zeros(self.nf)
         self._L.ref_cycle_vcycle(self._h, vp, z.ctypes.data_as(_dp), pre, post, damp)
         return z
+
+    def preconditioner(self, pre: int = 2, post: int = 2, damp: float = 1.0):
+        """(C function pointer, context) of this cycle as the preconditioner
+        callback of RefLevel.fgmres, with the given smoothing."""
+        self._L.ref_cycle_configure(self._h, pre, post, damp)
+        return C.cast(self._L.ref_cycle_precond, C.c_void_p), C.c_void_p(self._h)
 
 
 def ref_into_l20(v, order: int = -11) -> np.ndarray:

@@ -1,6 +1,6 @@
 // ref_transfer.cpp — runs the reference's own grid transfers, and its
-// multigrid cycle driver, on two nested hexahedral levels handed over as
-// plain arrays.  TEST INFRASTRUCTURE ONLY: it pins the oracle's prolongate /
+// multigrid cycle driver, on nested hexahedral levels handed over as plain
+// arrays.  TEST INFRASTRUCTURE ONLY: it pins the oracle's prolongate /
 // defect_restriction (and with them the per-child Q2 and P1disc matrices)
 // and its V-cycle against the reference code itself.
 // Built by oracle/build_oracle.py (build_ref_transfer) into
@@ -56,17 +56,25 @@
 //   these; no other library does).
 // No reference destructor runs; the harness frees what it allocated.
 //
-// The same two levels also run the reference's multigrid cycle
-// (ref_cycle_*): TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132), the
-// preconditioner call, with TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:
-// 434-1779) over two TNSE_MGLevel4 levels (src/FE/NSE_MGLevel4.C) built on
-// the levels' spaces and matrices: cell Vanka pre- and post-smoothing (the
-// _SEQ cell loop), the level defects, DefectRestriction, SolveExact on the
-// coarse level, Prolongate, CorrectNodes and Update.  The fine cells keep
-// the child frames described above, so the fine level's B rows and BT
-// columns of every cell's linear pressure modes are transformed by that
-// cell's signed permutation, and so are the pressure parts of the vectors
-// on the way in and out; velocity DOFs keep their global numbers.
+// Over more than two levels every cell's frame composes its parent's with
+// the reference child's: a child of a cell whose frame is not the
+// axis-aligned one is found by its octant in the parent's frame, and its
+// local axes are the reference child's axes taken in the parent's frame.
+// The node orders this gives are checked against the ones read from the
+// refined reference cell's vertices.
+//
+// The same levels also run the reference's multigrid cycle (ref_cycle_*):
+// TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132), the preconditioner
+// call, with TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779) over
+// one TNSE_MGLevel4 level (src/FE/NSE_MGLevel4.C) per level, built on the
+// levels' spaces and matrices: cell Vanka pre- and post-smoothing (the _SEQ
+// cell loop) on every level above the coarsest, the level defects,
+// DefectRestriction, SolveExact on the coarsest level, Prolongate,
+// CorrectDefect, CorrectNodes and Update.  The cells keep the frames
+// described above, so every level's B rows and BT columns of each cell's
+// linear pressure modes are transformed by that cell's signed permutation,
+// and so are the pressure parts of the finest level's vectors on the way in
+// and out; velocity DOFs keep their global numbers.
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
@@ -135,6 +143,25 @@ int g_octant_of_child[8];
 int g_uperm[8][27];
 int g_paxis[8][3];
 double g_psign[8][3];
+
+// A cell's local frame: its local coordinate i (xi, eta, zeta) is
+// sign[i] times the axis-aligned coordinate axis[i].  The coarsest cells
+// have the identity; a child's frame composes its parent's with the
+// reference child's (g_paxis, g_psign).
+struct Frame {
+  int axis[3] = {0, 1, 2};
+  double sign[3] = {1.0, 1.0, 1.0};
+};
+
+// the axis-aligned Q2 node of local node t = a + 3b + 9c of a cell in frame
+// F: node (a, b, c) lies a, b, c half-edges from the cell's vertex 0 along
+// its local axes, and vertex 0 is at the low end of axis[i] where sign[i] > 0
+int aligned_node(const Frame &F, int t) {
+  const int n[3] = {t % 3, (t / 3) % 3, t / 9};
+  int q[3];
+  for (int i = 0; i < 3; ++i) q[F.axis[i]] = F.sign[i] > 0 ? n[i] : 2 - n[i];
+  return q[0] + 3 * q[1] + 9 * q[2];
+}
 
 // octant (bit 0: xi > 0, bit 1: eta > 0, bit 2: zeta > 0, relative to the
 // parent's centre) of each child of the regular hexahedral refinement
@@ -209,6 +236,20 @@ bool init_databases() {
     std::fprintf(stderr, "ref_transfer: the refined reference cell has no child per octant\n");
     return false;
   }
+  // the node orders taken from the children's vertices are the ones their
+  // frames give (what composing frames over several levels relies on)
+  for (int j = 0; j < 8; ++j) {
+    Frame F;
+    for (int i = 0; i < 3; ++i) {
+      F.axis[i] = g_paxis[j][i];
+      F.sign[i] = g_psign[j][i];
+    }
+    for (int t = 0; t < 27; ++t)
+      if (aligned_node(F, t) != g_uperm[j][t]) {
+        std::fprintf(stderr, "ref_transfer: child %d's node order is not its frame's\n", j);
+        return false;
+      }
+  }
   g_ready = true;
   return true;
 }
@@ -270,26 +311,91 @@ void free_side(Side &S) {
   delete[] S.pa;
 }
 
-struct Pair {
-  Side coarse, fine;
-  std::vector<int> ref_child;  // per fine cell: its reference child number
+// Nested levels, level 0 the coarsest: every cell of level l > 0 is a child
+// of a cell of level l - 1 and is handed to the reference in its frame.
+struct Hier {
+  std::vector<Side *> sides;
+  std::vector<std::vector<Frame>> frames;  // per level and cell
 };
 
-// pressure coefficients of every fine cell between the axis-aligned frame
-// and the cell's reference-child frame (to_child: xi_i coefficient =
-// sign_i * coefficient of axis(i); the inverse otherwise)
-void convert_pressure(const Pair &T, double *fp, bool to_child) {
-  const Side &F = T.fine;
-  for (int f = 0; f < F.n_cells; ++f) {
-    const int j = T.ref_child[f];
-    const int *dof = F.pg + 4 * (size_t)f;
+// The levels as plain arrays (per level: cells, DOFs, active velocity DOFs,
+// pressure DOFs, 27 + 4 DOFs per cell in the axis-aligned local order; for
+// l > 0 each cell's parent on level l - 1 and its octant there, bit 0 x,
+// bit 1 y, bit 2 z).  Null when a parent has not exactly one child per
+// octant.
+Hier *build_hier(int L, const int *n_cells, const int *n_u, const int *n_active, const int *n_p,
+                 const int *const *udofs, const int *const *pdofs, const int *const *parent,
+                 const int *const *child) {
+  if (L < 2 || !init_databases()) return nullptr;
+  std::vector<std::vector<int>> slot(L);
+  for (int l = 1; l < L; ++l) {
+    slot[l].assign((size_t)8 * n_cells[l - 1], -1);
+    for (int f = 0; f < n_cells[l]; ++f) {
+      const int p = parent[l][f], o = child[l][f];
+      if (p < 0 || p >= n_cells[l - 1] || o < 0 || o > 7 || slot[l][(size_t)8 * p + o] >= 0)
+        return nullptr;
+      slot[l][(size_t)8 * p + o] = f;
+    }
+    for (int sl : slot[l])
+      if (sl < 0) return nullptr;
+  }
+  Hier *H = new Hier;
+  H->frames.resize(L);
+  for (int l = 0; l < L; ++l) {
+    H->sides.push_back(new Side);
+    make_side(*H->sides.back(), n_cells[l], n_u[l], n_active[l], n_p[l], udofs[l], pdofs[l],
+              TDatabase::RefDescDB[l + 1 < L ? N_SHAPES + HexaReg : Hexahedron]);
+    H->frames[l].assign(n_cells[l], Frame());
+  }
+  for (int l = 1; l < L; ++l) {
+    Side &C = *H->sides[l - 1], &F = *H->sides[l];
+    for (int c = 0; c < C.n_cells; ++c) {
+      const Frame &P = H->frames[l - 1][c];
+      TBaseCell **ch = new TBaseCell *[8];
+      for (int j = 0; j < 8; ++j) {
+        // child j's octant in the parent's frame, then axis-aligned
+        const int lo = g_octant_of_child[j];
+        int o = 0;
+        for (int i = 0; i < 3; ++i) o |= (((lo >> i) & 1) ^ (P.sign[i] < 0 ? 1 : 0)) << P.axis[i];
+        const int f = slot[l][(size_t)8 * c + o];
+        ch[j] = F.cells[f];
+        ch[j]->SetParent(C.cells[c]);
+        Frame &Fr = H->frames[l][f];
+        for (int i = 0; i < 3; ++i) {
+          Fr.axis[i] = P.axis[g_paxis[j][i]];
+          Fr.sign[i] = P.sign[g_paxis[j][i]] * g_psign[j][i];
+        }
+        for (int t = 0; t < 27; ++t)  // the fine cell's DOFs in its frame's node order
+          F.ug[(size_t)27 * f + t] = udofs[l][(size_t)27 * f + aligned_node(Fr, t)];
+      }
+      C.cells[c]->set_children(ch);
+    }
+  }
+  return H;
+}
+
+void free_hier(Hier *H) {
+  for (Side *S : H->sides) {
+    free_side(*S);
+    delete S;
+  }
+  delete H;
+}
+
+// pressure coefficients of every cell of level S between the axis-aligned
+// frame and the cell's frame (to_child: xi_i coefficient = sign_i *
+// coefficient of axis(i); the inverse otherwise)
+void convert_pressure(const Side &S, const std::vector<Frame> &fr, double *fp, bool to_child) {
+  for (int f = 0; f < S.n_cells; ++f) {
+    const Frame &F = fr[f];
+    const int *dof = S.pg + 4 * (size_t)f;
     double in[3], out[3];
     for (int i = 0; i < 3; ++i) in[i] = fp[dof[1 + i]];
     for (int i = 0; i < 3; ++i) {
       if (to_child)
-        out[i] = g_psign[j][i] * in[g_paxis[j][i]];
+        out[i] = F.sign[i] * in[F.axis[i]];
       else
-        out[g_paxis[j][i]] = g_psign[j][i] * in[i];
+        out[F.axis[i]] = F.sign[i] * in[i];
     }
     for (int i = 0; i < 3; ++i) fp[dof[1 + i]] = out[i];
   }
@@ -307,42 +413,15 @@ __attribute__((visibility("default"))) void *ref_transfer_create(
     int nc_cells, int nc_u, int nc_active, int nc_p, const int *c_udofs, const int *c_pdofs,
     int nf_cells, int nf_u, int nf_active, int nf_p, const int *f_udofs, const int *f_pdofs,
     const int *fine_parent, const int *fine_child) {
-  if (!init_databases()) return nullptr;
-  std::vector<int> slot((size_t)8 * nc_cells, -1);
-  for (int f = 0; f < nf_cells; ++f) {
-    const int p = fine_parent[f], o = fine_child[f];
-    if (p < 0 || p >= nc_cells || o < 0 || o > 7 || slot[(size_t)8 * p + o] >= 0) return nullptr;
-    slot[(size_t)8 * p + o] = f;
-  }
-  for (int s : slot)
-    if (s < 0) return nullptr;
-  Pair *T = new Pair;
-  make_side(T->coarse, nc_cells, nc_u, nc_active, nc_p, c_udofs, c_pdofs,
-            TDatabase::RefDescDB[N_SHAPES + HexaReg]);
-  make_side(T->fine, nf_cells, nf_u, nf_active, nf_p, f_udofs, f_pdofs,
-            TDatabase::RefDescDB[Hexahedron]);
-  T->ref_child.assign(nf_cells, 0);
-  for (int c = 0; c < nc_cells; ++c) {
-    TBaseCell **ch = new TBaseCell *[8];
-    for (int j = 0; j < 8; ++j) {
-      const int f = slot[(size_t)8 * c + g_octant_of_child[j]];
-      ch[j] = T->fine.cells[f];
-      ch[j]->SetParent(T->coarse.cells[c]);
-      T->ref_child[f] = j;
-      for (int t = 0; t < 27; ++t)  // the fine cell's DOFs in the child's node order
-        T->fine.ug[(size_t)27 * f + t] = f_udofs[(size_t)27 * f + g_uperm[j][t]];
-    }
-    T->coarse.cells[c]->set_children(ch);
-  }
-  return T;
+  const int n_cells[2] = {nc_cells, nf_cells}, n_u[2] = {nc_u, nf_u},
+            n_active[2] = {nc_active, nf_active}, n_p[2] = {nc_p, nf_p};
+  const int *udofs[2] = {c_udofs, f_udofs}, *pdofs[2] = {c_pdofs, f_pdofs};
+  const int *parent[2] = {nullptr, fine_parent}, *child[2] = {nullptr, fine_child};
+  return build_hier(2, n_cells, n_u, n_active, n_p, udofs, pdofs, parent, child);
 }
 
 __attribute__((visibility("default"))) void ref_transfer_destroy(void *h) {
-  Pair *T = static_cast<Pair *>(h);
-  if (!T) return;
-  free_side(T->coarse);
-  free_side(T->fine);
-  delete T;
+  if (h) free_hier(static_cast<Hier *>(h));
 }
 
 // fine = the reference's prolongation of coarse: Prolongate over the three
@@ -350,22 +429,22 @@ __attribute__((visibility("default"))) void ref_transfer_destroy(void *h) {
 // pressure; vectors are [u1|u2|u3|p] of each level.
 __attribute__((visibility("default"))) void ref_transfer_prolongate(void *h, const double *coarse,
                                                                     double *fine) {
-  Pair *T = static_cast<Pair *>(h);
-  const Side &C = T->coarse, &F = T->fine;
+  Hier *H = static_cast<Hier *>(h);
+  const Side &C = *H->sides[0], &F = *H->sides[1];
   std::vector<double> cu(coarse, coarse + 3 * (size_t)C.n_u + C.n_p), aux(F.n_u + F.n_p + 1);
   Prolongate(C.us, F.us, 3, cu.data(), fine, aux.data());
   Prolongate(C.ps, F.ps, cu.data() + 3 * (size_t)C.n_u, fine + 3 * (size_t)F.n_u, aux.data());
-  convert_pressure(*T, fine + 3 * (size_t)F.n_u, false);
+  convert_pressure(F, H->frames[1], fine + 3 * (size_t)F.n_u, false);
 }
 
 // coarse = the reference's defect restriction of fine (DefectRestriction
 // over the velocity components, then the scalar one for the pressure)
 __attribute__((visibility("default"))) void ref_transfer_restrict(void *h, const double *fine,
                                                                   double *coarse) {
-  Pair *T = static_cast<Pair *>(h);
-  const Side &C = T->coarse, &F = T->fine;
+  Hier *H = static_cast<Hier *>(h);
+  const Side &C = *H->sides[0], &F = *H->sides[1];
   std::vector<double> fu(fine, fine + 3 * (size_t)F.n_u + F.n_p), aux(F.n_u + F.n_p + 1);
-  convert_pressure(*T, fu.data() + 3 * (size_t)F.n_u, true);
+  convert_pressure(F, H->frames[1], fu.data() + 3 * (size_t)F.n_u, true);
   DefectRestriction(C.us, F.us, 3, coarse, fu.data(), aux.data());
   DefectRestriction(C.ps, F.ps, coarse + 3 * (size_t)C.n_u, fu.data() + 3 * (size_t)F.n_u,
                     aux.data());
@@ -419,10 +498,9 @@ int *copy_ints(const int *src, long n) {
 }
 
 // B (pressure rows) and BT (pressure columns) of level S with the linear
-// pressure modes of every cell c taken in frame `frame[c]` (a reference child
-// number, or -1 for the axis-aligned frame): row / column of mode i is
-// sign_i times the one of axis mode axis(i)
-void frame_pressure(const Side &S, const int *frame, int n_u, const int *b_rowptr,
+// pressure modes of every cell c taken in its frame fr[c]: row / column of
+// mode i is sign_i times the one of axis mode axis(i)
+void frame_pressure(const Side &S, const std::vector<Frame> &fr, int n_u, const int *b_rowptr,
                     const int *b_col, const double *const *b, const int *bt_rowptr,
                     const int *bt_col, const double *const *bt, std::vector<int> &brp,
                     std::vector<int> &bc, std::vector<double> (&bv)[3], std::vector<int> &btc,
@@ -434,14 +512,13 @@ void frame_pressure(const Side &S, const int *frame, int n_u, const int *b_rowpt
   std::vector<double> sg(n_p, 1.0), dsg(n_p, 1.0);
   for (int q = 0; q < n_p; ++q) src[q] = dst[q] = q;
   for (int c = 0; c < S.n_cells; ++c) {
-    const int j = frame[c];
-    if (j < 0) continue;
+    const Frame &F = fr[c];
     const int *dof = S.pg + 4 * (size_t)c;
     for (int i = 0; i < 3; ++i) {
-      src[dof[1 + i]] = dof[1 + g_paxis[j][i]];
-      sg[dof[1 + i]] = g_psign[j][i];
-      dst[dof[1 + g_paxis[j][i]]] = dof[1 + i];
-      dsg[dof[1 + g_paxis[j][i]]] = g_psign[j][i];
+      src[dof[1 + i]] = dof[1 + F.axis[i]];
+      sg[dof[1 + i]] = F.sign[i];
+      dst[dof[1 + F.axis[i]]] = dof[1 + i];
+      dsg[dof[1 + F.axis[i]]] = F.sign[i];
     }
   }
   brp.assign(n_p + 1, 0);
@@ -532,9 +609,11 @@ void free_mg_level(MGLevelStore &M) {
   delete[] M.u;
 }
 
-struct Cycle2 {
-  Pair *T = nullptr;
-  MGLevelStore lev[2];
+struct CycleChain {
+  int pre = 2, post = 2;
+  double damp = 1.0;
+  Hier *H = nullptr;
+  std::vector<MGLevelStore *> lev;
   TNSE_MultiGrid *mg = nullptr;
   alignas(TMultiGridIte) unsigned char ite_store[sizeof(TMultiGridIte)];
   TMultiGridIte *ite = nullptr;
@@ -544,62 +623,63 @@ struct Cycle2 {
 
 extern "C" {
 
-// The two levels of ref_transfer_create with their matrices (A: nine blocks
-// a[0..8], or a[0] alone for a one-block level; B: n_p x n_u, BT: n_u x n_p,
-// three blocks each) as the solver's level descriptors hold them, the level
-// relaxation alpha and the coarse-grid correction damping beta (al[0] and
-// al[1] of TNSE_MGLevel4, SC_GMG_DAMP_FACTOR_SADDLE).  Returns null when the
-// levels are not a regular refinement.
+// Nested levels as in build_hier (n_levels >= 2, level 0 the coarsest) with
+// their matrices (per level, A: nine blocks a[9l..9l+8], or a[9l] alone for
+// one-block levels; B: n_p x n_u, BT: n_u x n_p, three blocks each at 3l) as
+// the solver's level descriptors hold them, the level relaxation alpha and
+// the coarse-grid correction damping beta (al[0] and al[1] of every
+// TNSE_MGLevel4, SC_GMG_DAMP_FACTOR_SADDLE).  Returns null when the levels
+// are not a regular refinement.
 __attribute__((visibility("default"))) void *ref_cycle_create(
-    int nc_cells, int nc_u, int nc_active, int nc_p, const int *c_udofs, const int *c_pdofs,
-    int nf_cells, int nf_u, int nf_active, int nf_p, const int *f_udofs, const int *f_pdofs,
-    const int *fine_parent, const int *fine_child, int n_blocks, const int *const *a_rowptr,
-    const int *const *a_col, const double *const *a, const int *const *b_rowptr,
-    const int *const *b_col, const double *const *b, const int *const *bt_rowptr,
-    const int *const *bt_col, const double *const *bt, double alpha, double beta) {
-  void *tp = ref_transfer_create(nc_cells, nc_u, nc_active, nc_p, c_udofs, c_pdofs, nf_cells,
-                                 nf_u, nf_active, nf_p, f_udofs, f_pdofs, fine_parent, fine_child);
-  if (!tp) return nullptr;
-  Cycle2 *Y = new Cycle2;
-  Y->T = static_cast<Pair *>(tp);
-  Side *side[2] = {&Y->T->coarse, &Y->T->fine};
-  const int active[2] = {nc_active, nf_active};
-  std::vector<int> axis_frame(nc_cells, -1);
-  for (int l = 0; l < 2; ++l) {
-    Side &S = *side[l];
+    int n_levels, const int *n_cells, const int *n_u, const int *n_active, const int *n_p,
+    const int *const *udofs, const int *const *pdofs, const int *const *parent,
+    const int *const *child, int n_blocks, const int *const *a_rowptr, const int *const *a_col,
+    const double *const *a, const int *const *b_rowptr, const int *const *b_col,
+    const double *const *b, const int *const *bt_rowptr, const int *const *bt_col,
+    const double *const *bt, double alpha, double beta) {
+  Hier *H = build_hier(n_levels, n_cells, n_u, n_active, n_p, udofs, pdofs, parent, child);
+  if (!H) return nullptr;
+  CycleChain *Y = new CycleChain;
+  Y->H = H;
+  Y->mg = new TNSE_MultiGrid(1, 0, nullptr);
+  for (int l = 0; l < n_levels; ++l) {
+    Side &S = *H->sides[l];
     std::vector<int> brp, bc, btc;
     std::vector<double> bv[3], btv[3];
-    frame_pressure(S, l == 0 ? axis_frame.data() : Y->T->ref_child.data(), S.n_u, b_rowptr[l],
-                   b_col[l], b + 3 * l, bt_rowptr[l], bt_col[l], bt + 3 * l, brp, bc, bv, btc,
-                   btv);
-    make_mg_level(Y->lev[l], S, l, active[l], n_blocks, a_rowptr[l], a_col[l], a + 9 * l, brp,
-                  bc, bv, bt_rowptr[l], btc, btv, alpha, beta);
+    frame_pressure(S, H->frames[l], S.n_u, b_rowptr[l], b_col[l], b + 3 * l, bt_rowptr[l],
+                   bt_col[l], bt + 3 * l, brp, bc, bv, btc, btv);
+    Y->lev.push_back(new MGLevelStore);
+    make_mg_level(*Y->lev.back(), S, l, n_active[l], n_blocks, a_rowptr[l], a_col[l], a + 9 * l,
+                  brp, bc, bv, bt_rowptr[l], btc, btv, alpha, beta);
+    Y->mg->AddLevel(Y->lev.back()->level);
   }
-  Y->mg = new TNSE_MultiGrid(1, 0, nullptr);
-  for (int l = 0; l < 2; ++l) Y->mg->AddLevel(Y->lev[l].level);
-  const int n_fine = 3 * nf_u + nf_p;
+  const int top = n_levels - 1, n_fine = 3 * n_u[top] + n_p[top];
   Y->ite = new (Y->ite_store) TMultiGridIte(nullptr, nullptr, nullptr, 0, n_fine, Y->mg, 1);
   return Y;
 }
 
 __attribute__((visibility("default"))) void ref_cycle_destroy(void *h) {
-  Cycle2 *Y = static_cast<Cycle2 *>(h);
+  CycleChain *Y = static_cast<CycleChain *>(h);
   if (!Y) return;
   // TItMethod's constructor allocates no vector for n_aux = 0
-  for (int l = 0; l < 2; ++l) free_mg_level(Y->lev[l]);
+  for (MGLevelStore *M : Y->lev) {
+    free_mg_level(*M);
+    delete M;
+  }
   ::operator delete(static_cast<void *>(Y->mg));  // storage only: no reference destructor
-  ref_transfer_destroy(Y->T);
+  free_hier(Y->H);
   delete Y;
 }
 
-// z = one V(pre, post) cycle from zero on v (fine level, [u1|u2|u3|p] with
+// z = one V(pre, post) cycle from zero on v (finest level, [u1|u2|u3|p] with
 // the pressure in the axis-aligned frame): TMultiGridIte::Iterate with cell
-// Vanka (SC_SMOOTHER_SADDLE 2, damping `damp`, direct local solves), the
-// coarse level solved exactly (SC_COARSE_SMOOTHER_SADDLE 17, first pressure
-// equation pinned), no step-length control.
+// Vanka on every level above the coarsest (SC_SMOOTHER_SADDLE 2, damping
+// `damp`, direct local solves), the coarsest level solved exactly
+// (SC_COARSE_SMOOTHER_SADDLE 17, first pressure equation pinned), no
+// step-length control.
 __attribute__((visibility("default"))) void ref_cycle_vcycle(void *h, const double *v, double *z,
                                                              int pre, int post, double damp) {
-  Cycle2 *Y = static_cast<Cycle2 *>(h);
+  CycleChain *Y = static_cast<CycleChain *>(h);
   TParamDB *db = TDatabase::ParamDB;
   db->SC_SMOOTHER_SADDLE = 2;
   db->SC_COARSE_SMOOTHER_SADDLE = 17;
@@ -617,12 +697,30 @@ __attribute__((visibility("default"))) void ref_cycle_vcycle(void *h, const doub
   db->INTERNAL_PRESSURE_SPACE = -11;
   db->SC_VERBOSE = 0;
   db->MG_DEBUG = 0;
-  const Side &F = Y->T->fine;
+  const int top = (int)Y->H->sides.size() - 1;
+  const Side &F = *Y->H->sides[top];
   const int n = 3 * F.n_u + F.n_p;
   std::vector<double> rhs(v, v + n);
-  convert_pressure(*Y->T, rhs.data() + 3 * (size_t)F.n_u, true);
+  convert_pressure(F, Y->H->frames[top], rhs.data() + 3 * (size_t)F.n_u, true);
   Y->ite->Iterate(nullptr, nullptr, z, rhs.data());
-  convert_pressure(*Y->T, z + 3 * (size_t)F.n_u, false);
+  convert_pressure(F, Y->H->frames[top], z + 3 * (size_t)F.n_u, false);
+}
+
+// The smoothing counts and damping of ref_cycle_precond (V(2,2) with
+// damping 1 until set).
+__attribute__((visibility("default"))) void ref_cycle_configure(void *h, int pre, int post,
+                                                                double damp) {
+  CycleChain *Y = static_cast<CycleChain *>(h);
+  Y->pre = pre;
+  Y->post = post;
+  Y->damp = damp;
+}
+
+// The cycle as a preconditioner callback z = M(v), the signature ref_fgmres
+// of oracle/ref_harness.cpp takes.
+__attribute__((visibility("default"))) void ref_cycle_precond(void *h, double *z, const double *v) {
+  CycleChain *Y = static_cast<CycleChain *>(h);
+  ref_cycle_vcycle(h, v, z, Y->pre, Y->post, Y->damp);
 }
 
 }  // extern "C"

@@ -14,11 +14,17 @@ oracle/build_oracle.py compiles with the reference sources where they lie:
   build, damping 1, no relaxation) from u = x with right-hand side b;
 * tests/golden/ref_cycle_*.npz: one V(2,2) cycle from zero on b, the
   preconditioner call TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132)
-  with TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779) over two
-  TNSE_MGLevel4 levels: cell Vanka on the fine level (sequential build),
-  SolveExact on the coarse one, the reference's transfers between them.
+  with TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779) over two or
+  three TNSE_MGLevel4 levels: cell Vanka on the levels above the coarsest
+  (sequential build), SolveExact on the coarsest, the reference's transfers
+  between them;
+* tests/golden/ref_solve_*.npz: the whole reference solver, its flexible
+  FGMRES (TFgmresIte::Iterate, src/FE/FgmresIte.C:250-677) preconditioned by
+  that cycle driver, from zero on the problem's right-hand side (stored with
+  the solution and the iteration count).
 Needs the reference tree; the fixtures are committed so the tests do not.
-``python make_ref_golden.py cycle`` writes the cycle fixtures only.
+``python make_ref_golden.py cycle`` writes the cycle fixtures only,
+``python make_ref_golden.py solve`` the whole-solver ones.
 
 Inputs are exact binary fractions of the DOF index (``golden_inputs``), so
 every platform forms the same x and b without a random generator.
@@ -75,11 +81,15 @@ TRANSFER_CASES = {
 }
 
 
-# name -> OseenProblem keyword arguments of the cycle fixtures (two levels:
-# the V-cycle of the fine level over the exactly solved coarse one)
+# name -> OseenProblem keyword arguments of the cycle fixtures: two levels
+# (the V-cycle of the fine level over the exactly solved coarse one) and
+# three (cell Vanka on the middle level too, its cells and the finest ones in
+# composed child frames)
 CYCLE_CASES = {
     "hexa": CASES["hexa"][0],
     "channel": CASES["channel"][0],
+    "hexa3": dict(CASES["hexa"][0], n_levels=3),
+    "channel3": dict(CASES["channel"][0], n_levels=3),
 }
 
 
@@ -97,12 +107,43 @@ def write_cycle_fixtures() -> None:
         print("wrote cycle", name, "ndof", P.ndof(-1))
 
 
+# name -> (OseenProblem keyword arguments, FGMRES parameters) of the fixtures
+# of the whole reference solver: its FGMRES over its own cycle driver on
+# every level of the problem, from zero on the problem's right-hand side
+SOLVE_CASES = {
+    "hexa3": (dict(CASES["hexa"][0], n_levels=3),
+              dict(restart=20, maxit=100, red_factor=1e-10, res_norm_min=1e-30)),
+}
+
+
+def write_solve_fixtures() -> None:
+    from oracle.pyoracle import Oracle
+    from oracle.pyref import RefCycle, RefLevel
+    for name, (kwargs, fgmres) in SOLVE_CASES.items():
+        P = build_problem(kwargs)
+        b = P.rhs()
+        params = Oracle(P, vanka_mode="seq", **fgmres).params
+        x, it = RefLevel(P.arrays(P.n_levels - 1), threads=1).fgmres_with_reference_cycle(
+            RefCycle(P), params, np.zeros_like(b), b)
+        np.savez_compressed(
+            HERE / f"ref_solve_{name}.npz", problem=json.dumps(kwargs), level=P.n_levels - 1,
+            fgmres=json.dumps(fgmres), rhs=b, solution=x, iterations=it,
+            source=("reference src/FE/FgmresIte.C TFgmresIte::Iterate (run by "
+                    "oracle/ref_harness.cpp) preconditioned by src/FE/MultiGridIte.C "
+                    "TMultiGridIte::Iterate with src/FE/NSE_MultiGrid.C TNSE_MultiGrid::Cycle "
+                    "(V(2,2), cell Vanka _SEQ, SolveExact; run by oracle/ref_transfer.cpp)"))
+        print("wrote solve", name, "iterations", it, "ndof", b.size)
+
+
 def main() -> None:
     from oracle.pyref import RefLevel, RefTransfer, RefVankaLevel, ref_harness_lib
     if ref_harness_lib() is None:
         raise SystemExit("reference tree not found; cannot regenerate the defect golden files")
     if sys.argv[1:] == ["cycle"]:
         write_cycle_fixtures()
+        return
+    if sys.argv[1:] == ["solve"]:
+        write_solve_fixtures()
         return
     for name, (kwargs, level) in CASES.items():
         P = build_problem(kwargs)

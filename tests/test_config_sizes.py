@@ -4,7 +4,10 @@ nu = 1e-2, seed 0), FGMRES(20) + one V(2,2) cell-Vanka cycle, relative
 residual 1e-10.
 
 The oracle's FGMRES (src/FE/FgmresIte.C:250-677 over the cycle of
-src/FE/NSE_MultiGrid.C:434-1779) is the reference answer.  Bars, as the
+src/FE/NSE_MultiGrid.C:434-1779) is the reference answer; where the
+reference tree is present, the reference's own solver (its FGMRES over its
+own cycle driver, compiled where they lie) is run on the same problem and
+the oracle checked against it.  Bars, as the
 path's correctness target states them: the GPU solution reaches 1e-10
 relative residual, its velocity and its pressure each differ from the
 oracle's by at most 1e-6 relative L2 (pressures compared after the same
@@ -54,6 +57,37 @@ def test_oracle_factor_reuse_is_exact(config0):
     assert i["iterations"] == io["iterations"]
     assert np.array_equal(x, xo)
     assert io["true_res"] <= RTOL * r0
+
+
+def test_oracle_equals_the_whole_reference_solver(config0):
+    """The reference's own solver on this problem, compiled where it lies
+    (single thread, sequential build): its flexible FGMRES
+    (TFgmresIte::Iterate, src/FE/FgmresIte.C:250-677, run by
+    oracle/ref_harness.cpp) preconditioned by its own cycle driver
+    (TMultiGridIte::Iterate with TNSE_MultiGrid::Cycle over four
+    TNSE_MGLevel4 levels, run by oracle/ref_transfer.cpp).  The oracle with
+    the sequential cell loop takes the same iterations and agrees to
+    rounding; the colour-ordered oracle the GPU is compared with is within
+    the solve tolerance of it."""
+    from oracle.pyref import ref_harness_lib, ref_transfer_lib
+    if ref_harness_lib() is None or ref_transfer_lib() is None:
+        pytest.skip("reference tree not present: the harnesses are not built")
+    from oracle.pyref import RefCycle, RefLevel
+    P, b, r0, xo, io = config0
+    x0 = np.zeros_like(b)
+    O = Oracle(P, restart=20, maxit=100, res_norm_min=RTOL * r0, vanka_mode="seq",
+               reuse_factors=1)
+    xs, i_s = O.iterate(x0, b)
+    xr, it = RefLevel(P.arrays(LEVELS - 1), threads=1).fgmres_with_reference_cycle(
+        RefCycle(P), O.params, x0, b)
+    nu = P.desc(LEVELS - 1).n_udof
+    eu, ep = split_error(xo, xr, nu)
+    print(f"config 0 reference solver: {it} iterations (oracle sequential "
+          f"{i_s['iterations']}, colour-ordered {io['iterations']}); colour-ordered oracle vs "
+          f"reference u {eu:.2e} p {ep:.2e}")
+    assert it == i_s["iterations"]
+    assert np.linalg.norm(xs - xr) <= 1e-13 * np.linalg.norm(xr)
+    assert eu <= 1e-7 and ep <= 1e-7
 
 
 @pytest.mark.gpu

@@ -34,10 +34,11 @@ The GPU's colour-block sweep equals the sequential cell loop when every cell
 is its own colour, so the CUDA Vanka is checked against the reference's with
 such a colouring, at 1e-9 relative (FP64 LU rounding).
 The same transfer harness runs the reference's cycle driver,
-TMultiGridIte::Iterate with TNSE_MultiGrid::Cycle, over two levels; the
-oracle's V-cycle agrees with it to 1e-13 (the fine cells' local DOF orders
-differ), and its output is committed as tests/golden/ref_cycle_*.npz (oracle
-1e-13, the FP64 CUDA V-cycle with one cell per colour 1e-9).
+TMultiGridIte::Iterate with TNSE_MultiGrid::Cycle, over two, three and four
+levels; the oracle's V-cycle agrees with it to 1e-13 (the refined cells'
+local DOF orders differ), and its output is committed as
+tests/golden/ref_cycle_*.npz for two and three levels (oracle 1e-13, the
+FP64 CUDA V-cycle with one cell per colour 1e-9).
 """
 import ctypes as C
 import importlib.util
@@ -242,16 +243,19 @@ def test_oracle_vanka_equals_reference_cell_vanka_bitwise(case):
         assert np.max(np.abs(u_ref - u)) > 1e-3  # the sweep did change u
 
 
-def per_cell_colours(P, level):
-    """The problem's descriptors with every cell of ``level`` its own colour
-    (the colour-block sweep then runs the cells one by one, in index order).
-    Returns the descriptors and the colour array they point at."""
+def per_cell_colours(P, levels):
+    """The problem's descriptors with every cell of each level in ``levels``
+    (one level or several) its own colour (the colour-block sweep then runs
+    the cells one by one, in index order).  Returns the descriptors and the
+    colour arrays they point at."""
     from to_merge_master_parmoon_gb300._lib import PmLevelDesc
     descs = (PmLevelDesc * P.n_levels)()
     for l in range(P.n_levels):
         C.pointer(descs[l])[0] = P.descs[l]
-    colours = np.arange(P.arrays(level)["n_cells"], dtype=np.int32)
-    descs[level].cell_colour = colours.ctypes.data_as(C.POINTER(C.c_int))
+    colours = []
+    for level in ([levels] if isinstance(levels, int) else levels):
+        colours.append(np.arange(P.arrays(level)["n_cells"], dtype=np.int32))
+        descs[level].cell_colour = colours[-1].ctypes.data_as(C.POINTER(C.c_int))
     return descs, colours
 
 
@@ -447,26 +451,34 @@ def test_gpu_coarse_solve_matches_reference_fixtures(name):
 # --------------------------------------------------------------- cycle ----
 # oracle/ref_transfer.cpp also runs the reference's multigrid preconditioner
 # call, TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132) with
-# TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779), over two
-# TNSE_MGLevel4 levels built on the transfer harness's cells and spaces:
-# sequential cell Vanka on the fine level, SolveExact on the coarse one, the
-# reference's DefectRestriction / Prolongate, CorrectDefect, CorrectNodes and
-# Update between them.  The fine cells are in the reference's child frames
+# TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779), over one
+# TNSE_MGLevel4 level per level of the problem, built on the transfer
+# harness's cells and spaces: sequential cell Vanka on every level above the
+# coarsest, SolveExact on the coarsest, the reference's DefectRestriction /
+# Prolongate, CorrectDefect, CorrectNodes and Update between them.  The cells
+# below the coarsest level are in the reference's (composed) child frames
 # (their local DOF orders differ from the oracle's), so the local solves
 # round differently: the oracle's V-cycle is checked to 1e-13.
 
 CYCLE_PARAMS = [(2, 2, 1.0, 1.0, 1.0), (1, 3, 0.8, 1.0, 1.0), (2, 2, 1.0, 0.9, 0.7)]
+CYCLE_NAMES = ["hexa", "channel", "hexa3", "channel3"]
 
 
-@pytest.mark.parametrize("name", ["hexa", "channel"])
-@pytest.mark.parametrize("pre,post,damp,alpha,beta", CYCLE_PARAMS)
-def test_oracle_vcycle_matches_the_reference_cycle_driver(name, pre, post, damp, alpha, beta):
-    """Smoothing counts, Vanka damping, the level relaxation alpha and the
-    coarse-grid-correction damping beta (SC_GMG_DAMP_FACTOR_SADDLE)."""
+def _ref_cycle_or_skip():
     from oracle.pyref import ref_transfer_lib
     if ref_transfer_lib() is None:
         pytest.skip("reference tree not present (the committed fixtures cover this case)")
     from oracle.pyref import RefCycle
+    return RefCycle
+
+
+@pytest.mark.parametrize("name", CYCLE_NAMES)
+@pytest.mark.parametrize("pre,post,damp,alpha,beta", CYCLE_PARAMS)
+def test_oracle_vcycle_matches_the_reference_cycle_driver(name, pre, post, damp, alpha, beta):
+    """Smoothing counts, Vanka damping, the level relaxation alpha and the
+    coarse-grid-correction damping beta (SC_GMG_DAMP_FACTOR_SADDLE), over two
+    and three levels."""
+    RefCycle = _ref_cycle_or_skip()
     gm = _golden_module()
     P = gm.build_problem(gm.CYCLE_CASES[name])
     _, b = gm.golden_inputs(P.ndof(-1))
@@ -476,31 +488,136 @@ def test_oracle_vcycle_matches_the_reference_cycle_driver(name, pre, post, damp,
     assert rel(O.vcycle(b), z_ref) < 1e-13
 
 
-@pytest.mark.parametrize("name", ["hexa", "channel"])
+def test_oracle_vcycle_matches_the_reference_cycle_driver_on_four_levels():
+    """Two middle levels: the coarsest level's grandchildren and their
+    children in frames composed over three refinements (16^3 cells)."""
+    RefCycle = _ref_cycle_or_skip()
+    gm = _golden_module()
+    P = gm.build_problem(dict(gm.CASES["hexa"][0], n_levels=4))
+    _, b = gm.golden_inputs(P.ndof(-1))
+    z_ref = RefCycle(P).vcycle(b, pre=2, post=2, damp=1.0)
+    assert rel(Oracle(P, vanka_mode="seq").vcycle(b), z_ref) < 1e-13
+
+
+@pytest.mark.parametrize("name", CYCLE_NAMES)
 def test_cycle_fixtures_reproduce_from_the_reference(name):
-    from oracle.pyref import ref_transfer_lib
-    if ref_transfer_lib() is None:
-        pytest.skip("reference tree not present (the committed fixtures cover this case)")
-    from oracle.pyref import RefCycle
+    RefCycle = _ref_cycle_or_skip()
     P, level, _, b, g = load_case(name, "cycle")
     assert np.array_equal(RefCycle(P).vcycle(b, pre=2, post=2, damp=1.0), g["vcycle"])
 
 
-@pytest.mark.parametrize("name", ["hexa", "channel"])
+@pytest.mark.parametrize("name", CYCLE_NAMES)
 def test_oracle_vcycle_matches_reference_cycle_fixtures(name):
     P, level, _, b, g = load_case(name, "cycle")
     assert rel(Oracle(P, vanka_mode="seq").vcycle(b), g["vcycle"]) < 1e-13
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["hexa", "channel"])
+@pytest.mark.parametrize("name", CYCLE_NAMES)
 def test_gpu_vcycle_matches_reference_cycle_fixtures(name):
     """The FP64 CUDA V-cycle (graph-captured, cell Vanka with one cell per
-    colour on the fine level: the sequential order, block-elimination local
-    solves) against the reference's own cycle driver."""
+    colour on every smoothed level: the sequential order, block-elimination
+    local solves) against the reference's own cycle driver."""
     from to_merge_master_parmoon_gb300 import PmSolver
     P, level, _, b, g = load_case(name, "cycle")
-    descs, colours = per_cell_colours(P, level)
+    descs, colours = per_cell_colours(P, list(range(1, P.n_levels)))
     S = PmSolver(descs, precision="fp64")
     assert rel(S.vcycle(b), g["vcycle"]) < 1e-9
     del colours
+
+
+# -------------------------------------------------------- whole solver ----
+# The reference's flexible FGMRES (oracle/ref_harness.cpp) with the
+# reference's own cycle driver (oracle/ref_transfer.cpp) as its
+# preconditioner is the whole reference solver of the path, every line of it
+# the reference's.  The oracle's FGMRES with the sequential cell loop takes
+# the same iterations and agrees to rounding.  (The iteration count is only
+# as stable as the stopping test: where a problem's solution is exactly
+# representable and the residual reaches rounding level, the restart-relative
+# reduction is decided by rounding noise, so such cases are not used here.)
+
+def _solver_cases(gm):
+    return {
+        "hexa3": gm.SOLVE_CASES["hexa3"],
+        "channel3": (dict(gm.CASES["channel"][0], n_levels=3, nu=0.1),
+                     dict(restart=10, maxit=60, red_factor=1e-8, res_norm_min=1e-30)),
+    }
+
+
+def _whole_reference_solve(P, params, b):
+    from oracle.pyref import RefCycle, RefLevel
+    return RefLevel(P.arrays(P.n_levels - 1), threads=1).fgmres_with_reference_cycle(
+        RefCycle(P), params, np.zeros_like(b), b)
+
+
+@pytest.mark.parametrize("name", ["hexa3", "channel3"])
+def test_oracle_fgmres_equals_the_whole_reference_solver(name):
+    _ref_cycle_or_skip()
+    ref_lib_or_skip()
+    gm = _golden_module()
+    kwargs, fgmres = _solver_cases(gm)[name]
+    P = gm.build_problem(kwargs)
+    b = P.rhs()
+    O = Oracle(P, vanka_mode="seq", **fgmres)
+    x_o, info = O.iterate(np.zeros_like(b), b)
+    x_r, it = _whole_reference_solve(P, O.params, b)
+    assert info["iterations"] == it
+    assert rel(x_o, x_r) < 1e-13
+
+
+def _load_solve(name):
+    gm = _golden_module()
+    g = np.load(GOLD / f"ref_solve_{name}.npz")
+    P = gm.build_problem(json.loads(str(g["problem"])))
+    assert int(g["level"]) == P.n_levels - 1
+    return P, json.loads(str(g["fgmres"])), g
+
+
+def test_solve_fixtures_reproduce_from_the_reference():
+    _ref_cycle_or_skip()
+    ref_lib_or_skip()
+    P, fgmres, g = _load_solve("hexa3")
+    assert np.array_equal(P.rhs(), g["rhs"])
+    x, it = _whole_reference_solve(P, Oracle(P, vanka_mode="seq", **fgmres).params, g["rhs"])
+    assert it == int(g["iterations"])
+    assert np.array_equal(x, g["solution"])
+
+
+def test_oracle_fgmres_matches_reference_solve_fixtures():
+    P, fgmres, g = _load_solve("hexa3")
+    x, info = Oracle(P, vanka_mode="seq", **fgmres).iterate(np.zeros_like(g["rhs"]), g["rhs"])
+    assert info["iterations"] == int(g["iterations"])
+    assert rel(x, g["solution"]) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gpu_fgmres_matches_reference_solve_fixtures(precision):
+    """The GPU solver against the whole reference solver's solution: FP64
+    with one cell per colour on every smoothed level (the sequential order)
+    takes the reference's iterations and agrees to 1e-9; mixed precision with
+    the library's own colouring reaches the same tolerance and is within
+    1e-6 of it (pressures after L2_0 normalisation)."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, fgmres, g = _load_solve("hexa3")
+    b, xr = g["rhs"], g["solution"]
+    if precision == "fp64":
+        descs, colours = per_cell_colours(P, list(range(1, P.n_levels)))
+    else:
+        descs, colours = P.descs, None
+    S = PmSolver(descs, precision=precision, **fgmres)
+    x, info = S.iterate(np.zeros_like(b), b)
+    S.close()
+    del colours
+    assert info["status"] == 0
+    if precision == "fp64":
+        assert info["iterations"] == int(g["iterations"])
+        assert rel(x, xr) < 1e-9
+    else:
+        assert info["true_res"] <= 1.05 * fgmres["red_factor"] * info["res0"]
+        n3 = 3 * P.desc(P.n_levels - 1).n_udof
+        assert rel(x[:n3], xr[:n3]) < 1e-6
+        xp, rp = x[n3:].copy(), xr[n3:].copy()
+        xp[0::4] -= xp[0::4].mean()
+        rp[0::4] -= rp[0::4].mean()
+        assert rel(xp, rp) < 1e-6
