@@ -1219,8 +1219,8 @@ def main():
         "data": "synthetic (seeded divergence-free Fourier convection, smooth forcing)",
         "config": {"workload": f"steady 3D Oseen, Q2/P1disc, {2 ** nlev}^3 cells, {nlev} levels "
                                f"from 2^3, nu={args.nu}, FGMRES(20)+V(2,2) cell Vanka, rtol 1e-8",
-                   "ndof": n, "precision": "mixed: FP32 V-cycle + FP32-stored FP64-computed "
-                                           "local block elimination, FP64 FGMRES/coarse; "
+                   "ndof": n, "precision": "mixed: FP32 V-cycle + FP32 local block "
+                                           "elimination, FP64 FGMRES/coarse; "
                                            "learned: BF16 MLP (tcgen05) post-smoothing step "
                                            "on the finest level",
                    "l2": "inputs (11.7 GB of matrices) larger than L2", "parallelism": "replicas"},

@@ -61,13 +61,16 @@ typedef enum {
 } pm_status;
 
 /* Precision of the V-cycle.  FGMRES, Arnoldi, Givens and the coarse direct
- * solve are FP64 in both modes; the local LU factorisations are computed in
- * FP64 (factor_fp32 = 0) and stored in the V-cycle precision. */
+ * solve are FP64 in both modes; the local factorisations are stored in the
+ * V-cycle precision.  FP64 mode computes them in FP64.  Mixed mode computes
+ * the block elimination of decoupled cells in FP32 and the 85x85 LU of
+ * coupled cells in FP64 (factor_fp32 = -1, the default); factor_fp32 = 0
+ * computes both in FP64, factor_fp32 = 1 both in FP32. */
 enum { PM_PREC_FP64 = 0, PM_PREC_MIXED = 1 };
 
 typedef struct {
   int precision;          /* PM_PREC_FP64 | PM_PREC_MIXED                          */
-  int factor_fp32;        /* 1: compute local LU in FP32 (mixed only); default 0   */
+  int factor_fp32;        /* -1 (default) | 0 | 1: see above; 1 mixed only         */
   /* multigrid (TDatabase::ParamDB names) */
   int pre_smooth;         /* SC_PRE_SMOOTH_SADDLE   (default 2)                    */
   int post_smooth;        /* SC_POST_SMOOTH_SADDLE  (default 2)                    */

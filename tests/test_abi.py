@@ -46,6 +46,9 @@ def test_options_defaults_mirror_reference_database():
     assert o.smooth_damp == 1.0 and o.beta == 1.0 and o.alpha == 1.0
     assert o.red_factor == 0.0 and o.res_norm_min == 1e-10 and o.div_factor == 1e10
     assert o.project_pressure == 1
+    # not a database entry: mixed precision eliminates decoupled cells in
+    # FP32 and factors coupled ones (85x85 LU) in FP64
+    assert o.factor_fp32 == -1
 
 
 def test_no_device_is_reported_not_faked(monkeypatch):

@@ -1236,26 +1236,30 @@ pm_status factor_all(pm_handle *h) {
   cudaEventRecord(e0, h->stream);
   for (size_t l = 1; l < h->L.size(); ++l) {
     LevelDev &Lv = h->L[l];
+    // block elimination in FP32 unless factor_fp32 = 0 (mixed only); the
+    // 85x85 LU in FP32 only with factor_fp32 = 1
+    const bool f32 = mixed(h) && h->opt.factor_fp32 != 0;
     if (Lv.schur()) {
       if (mixed(h))
         PM_LAUNCH(launch_schur_factor<float>(Lv.op<double>(), Lv.cells(),
-                                             static_cast<float *>(Lv.factors), h->status_d, h->stream));
+                                             static_cast<float *>(Lv.factors), h->status_d, f32,
+                                             h->stream));
       else
         PM_LAUNCH(launch_schur_factor<double>(Lv.op<double>(), Lv.cells(),
                                               static_cast<double *>(Lv.factors), h->status_d,
-                                              h->stream));
+                                              false, h->stream));
     } else if (Lv.schur3()) {
       if (mixed(h))
         PM_LAUNCH(launch_schur3_factor<float>(Lv.op<double>(), Lv.cells(),
-                                              static_cast<float *>(Lv.factors), h->status_d,
+                                              static_cast<float *>(Lv.factors), h->status_d, f32,
                                               h->stream));
       else
         PM_LAUNCH(launch_schur3_factor<double>(Lv.op<double>(), Lv.cells(),
                                                static_cast<double *>(Lv.factors), h->status_d,
-                                               h->stream));
+                                               false, h->stream));
     } else if (mixed(h))
       PM_LAUNCH(launch_vanka_factor<float>(Lv.op<double>(), Lv.cells(), static_cast<float *>(Lv.factors),
-                                           Lv.perm, h->opt.factor_fp32 != 0, use_inverse(h),
+                                           Lv.perm, h->opt.factor_fp32 > 0, use_inverse(h),
                                            h->status_d, h->stream));
     else
       PM_LAUNCH(launch_vanka_factor<double>(Lv.op<double>(), Lv.cells(), static_cast<double *>(Lv.factors),
@@ -1451,7 +1455,7 @@ extern "C" {
 void pm_default_options(pm_options *o) {
   std::memset(o, 0, sizeof(*o));
   o->precision = PM_PREC_FP64;
-  o->factor_fp32 = 0;
+  o->factor_fp32 = -1;
   o->pre_smooth = 2;
   o->post_smooth = 2;
   o->smooth_damp = 1.0;
@@ -1515,7 +1519,8 @@ pm_status pm_create(pm_handle **out, const pm_options *opt) {
   else
     pm_default_options(&o);
   if (o.precision != PM_PREC_FP64 && o.precision != PM_PREC_MIXED) return PM_BADARG;
-  if (o.factor_fp32 && o.precision != PM_PREC_MIXED) return PM_BADARG;
+  if (o.factor_fp32 < -1 || o.factor_fp32 > 1) return PM_BADARG;
+  if (o.factor_fp32 > 0 && o.precision != PM_PREC_MIXED) return PM_BADARG;
   if (o.pre_smooth < 0 || o.post_smooth < 0 || o.restart <= 0 || o.maxit <= 0) return PM_BADARG;
   if (o.residual_variant < -1 || o.residual_variant > 2) return PM_BADARG;
   if (o.apply_variant < -1 || o.apply_variant > 2) return PM_BADARG;

@@ -196,9 +196,10 @@ constexpr int kSchurOffW = Schur<1>::offW;
 constexpr int kSchurOffS = Schur<1>::offS;
 constexpr int kSchurValues = Schur<1>::values;
 constexpr int kSchurStride = Schur<1>::stride;
+// fp32: eliminate in FP32 (TF = float only; option factor_fp32), else FP64
 template <typename TF>
 int launch_schur_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,
-                        cudaStream_t s);
+                        bool fp32, cudaStream_t s);
 template <typename T>
 int launch_schur_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                        const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s);
@@ -209,7 +210,7 @@ int launch_schur_apply_aos(const DevCells &cells, int nu, const int *cell_list, 
 // the same for NB = 3 (op.diag levels)
 template <typename TF>
 int launch_schur3_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,
-                         cudaStream_t s);
+                         bool fp32, cudaStream_t s);
 template <typename T>
 int launch_schur3_apply(const DevCells &cells, int nu, const int *cell_list, int ncol,
                         const T *factors, const T *rbuf, T damp, T *u, cudaStream_t s);

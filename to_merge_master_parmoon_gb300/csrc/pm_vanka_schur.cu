@@ -29,10 +29,12 @@
 // reference's CellVanka (src/FE/NSE_MGLevel4.C:1784-2031) solves the 85x85
 // system by LU; the block solution is the same solution of the same system.
 //
-//  k_schur_factor<NB>: one warp per cell, FP64 Gauss-Jordan with partial
-//    pivoting (first maximal |pivot|) on [A_b | I | G] in shared memory,
-//    lane i owning row i, once (NB = 1, all three G) or per component
-//    (NB = 3); then S, and S^{-1} by every lane.
+//  k_schur_factor<TF,TC,NB>: one warp per cell, Gauss-Jordan with partial
+//    pivoting (first maximal |pivot|) on [A_b | I | G] in shared memory in
+//    the compute type TC (FP64, or FP32 with option factor_fp32), lane i
+//    owning row i, once (NB = 1, all three G) or per component (NB = 3);
+//    then S and S^{-1} in FP64 by every lane (16 dot products and a 4x4
+//    inverse).  Stored in TF.
 //  k_schur_apply<NB>: one warp per cell, lane i < 27 owning velocity row i
 //    of the three components; every load of the stored block is independent
 //    of the previous arithmetic (three GEMVs and two small reductions).
@@ -75,26 +77,31 @@ __device__ __forceinline__ int find_local(const int *ids, int n, int g) {
   return -1;
 }
 
-template <int NB>
+template <int NB, typename TC>
 struct FactorSmem {
-  double M[NU_LOC * Tab<NB>::ms];   // [A_b | I | G], row-major
+  TC M[NU_LOC * Tab<NB>::ms];       // [A_b | I | G], row-major
   double D[NP_LOC * 3 * NU_LOC];    // D[(k*3+c)*27 + i] = Bc(pdof_k, udof_i)
   int ud[NU_LOC], pd[NP_LOC];
 };
 
-template <typename TF, int NB>
+template <typename T>
+__device__ __forceinline__ T abs_of(T v) {
+  return v < T(0) ? -v : v;
+}
+
+template <typename TF, typename TC, int NB>
 __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double> op,
                                                                     DevCells cells,
                                                                     TF *__restrict__ factors,
                                                                     int *status) {
   using L = Schur<NB>;
   constexpr int MS = Tab<NB>::ms, GW = Tab<NB>::gw, GOFF = Tab<NB>::goff;
-  __shared__ FactorSmem<NB> sm_all[kFactorWarps];
+  __shared__ FactorSmem<NB, TC> sm_all[kFactorWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cell = blockIdx.x * kFactorWarps + warp;
   if (cell >= cells.ncells) return;  // whole warp; no block-wide barrier below
-  FactorSmem<NB> &sm = sm_all[warp];
-  double *M = sm.M;
+  FactorSmem<NB, TC> &sm = sm_all[warp];
+  TC *M = sm.M;
   for (int t = lane; t < NP_LOC * 3 * NU_LOC; t += 32) sm.D[t] = 0.0;
   if (lane < NU_LOC) sm.ud[lane] = cells.udofs[(size_t)cell * NU_LOC + lane];
   if (lane < NP_LOC) sm.pd[lane] = cells.pdofs[(size_t)cell * NP_LOC + lane];
@@ -115,20 +122,20 @@ __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double
   double S[NP_LOC * NP_LOC];
 #pragma unroll
   for (int t = 0; t < NP_LOC * NP_LOC; ++t) S[t] = 0.0;
-  double *my = M + (lane < NU_LOC ? lane : 0) * MS;
+  TC *my = M + (lane < NU_LOC ? lane : 0) * MS;
   for (int b = 0; b < NB; ++b) {
     // gather A_b and G from the velocity rows (NSE_MGLevel2.C:470-540;
     // NSE_MGLevel4.C:1823-1918 with A12..A32 = 0)
     const double *Ab = op.a[NB == 1 ? 0 : 4 * b];
     __syncwarp();
-    for (int t = lane; t < NU_LOC * MS; t += 32) M[t] = 0.0;
+    for (int t = lane; t < NU_LOC * MS; t += 32) M[t] = TC(0);
     __syncwarp();
-    if (lane < NU_LOC) M[lane * MS + NU_LOC + lane] = 1.0;
+    if (lane < NU_LOC) M[lane * MS + NU_LOC + lane] = TC(1);
     for (int a = 0; a < NU_LOC; ++a) {
       const int r = sm.ud[a];
       for (int j = op.a_rowptr[r] + lane; j < op.a_rowptr[r + 1]; j += 32) {
         const int m = find_local(sm.ud, NU_LOC, op.a_col[j]);
-        if (m >= 0) M[a * MS + m] = Ab[j];
+        if (m >= 0) M[a * MS + m] = (TC)Ab[j];
       }
       if (r < op.nact) {
         for (int j = op.bt_rowptr[r] + lane; j < op.bt_rowptr[r + 1]; j += 32) {
@@ -136,9 +143,9 @@ __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double
           if (q >= 0) {
             if constexpr (NB == 1) {
 #pragma unroll
-              for (int c = 0; c < 3; ++c) M[a * MS + GOFF + c * NP_LOC + q] = op.bt[c][j];
+              for (int c = 0; c < 3; ++c) M[a * MS + GOFF + c * NP_LOC + q] = (TC)op.bt[c][j];
             } else {
-              M[a * MS + GOFF + q] = op.bt[b][j];
+              M[a * MS + GOFF + q] = (TC)op.bt[b][j];
             }
           }
         }
@@ -148,11 +155,11 @@ __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double
 
     // Gauss-Jordan: [A_b | I | G] -> [I | A_b^{-1} | A_b^{-1} G]
     for (int k = 0; k < NU_LOC; ++k) {
-      double best = (lane >= k && lane < NU_LOC) ? fabs(my[k]) : -1.0;
+      TC best = (lane >= k && lane < NU_LOC) ? abs_of(my[k]) : TC(-1);
       int bi = lane;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(kFull, best, o);
+        const TC ob = __shfl_xor_sync(kFull, best, o);
         const int oi = __shfl_xor_sync(kFull, bi, o);
         if (ob > best || (ob == best && oi < bi)) {
           best = ob;
@@ -163,21 +170,21 @@ __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double
       if (bi < k || bi >= NU_LOC) bi = k;   // and always a row of the block
       if (bi != k) {
         for (int c = lane; c < GW; c += 32) {
-          const double t = M[k * MS + c];
+          const TC t = M[k * MS + c];
           M[k * MS + c] = M[bi * MS + c];
           M[bi * MS + c] = t;
         }
       }
       __syncwarp();
-      const double piv = M[k * MS + k];
-      if (piv == 0.0) singular = true;
-      const double rp = piv != 0.0 ? 1.0 / piv : 0.0;
+      const TC piv = M[k * MS + k];
+      if (piv == TC(0)) singular = true;
+      const TC rp = piv != TC(0) ? TC(1) / piv : TC(0);
       __syncwarp();
       for (int c = k + 1 + lane; c < GW; c += 32) M[k * MS + c] *= rp;
       __syncwarp();
       if (lane < NU_LOC && lane != k) {
-        const double f = my[k];
-        if (f != 0.0)
+        const TC f = my[k];
+        if (f != TC(0))
           for (int c = k + 1; c < GW; ++c) my[c] -= f * M[k * MS + c];
       }
       __syncwarp();
@@ -194,9 +201,9 @@ __global__ void __launch_bounds__(kFactorWarps * 32) k_schur_factor(DevOp<double
           if constexpr (NB == 1) {
 #pragma unroll
             for (int c = 0; c < 3; ++c)
-              part += sm.D[(k * 3 + c) * NU_LOC + lane] * my[GOFF + c * NP_LOC + m];
+              part += sm.D[(k * 3 + c) * NU_LOC + lane] * (double)my[GOFF + c * NP_LOC + m];
           } else {
-            part = sm.D[(k * 3 + b) * NU_LOC + lane] * my[GOFF + m];
+            part = sm.D[(k * 3 + b) * NU_LOC + lane] * (double)my[GOFF + m];
           }
         }
         S[k * NP_LOC + m] -= warp_sum(part);
@@ -389,11 +396,20 @@ inline int ok() { return cudaPeekAtLastError() == cudaSuccess ? 1 : -1; }
 
 template <typename TF, int NB>
 int factor_impl(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,
-                cudaStream_t s) {
+                bool fp32, cudaStream_t s) {
   if (cells.ncells <= 0) return 0;
   if (cells.nl != NU_LOC) return -1;  // Q2 hexahedra only
   const int grid = (cells.ncells + kFactorWarps - 1) / kFactorWarps;
-  k_schur_factor<TF, NB><<<grid, kFactorWarps * 32, 0, s>>>(op, cells, factors, status);
+  if constexpr (sizeof(TF) == sizeof(float)) {
+    if (fp32) {
+      k_schur_factor<TF, float, NB><<<grid, kFactorWarps * 32, 0, s>>>(op, cells, factors,
+                                                                       status);
+      return ok() < 0 ? -1 : 1;
+    }
+  } else {
+    if (fp32) return -1;  // FP32 elimination only for FP32 factors
+  }
+  k_schur_factor<TF, double, NB><<<grid, kFactorWarps * 32, 0, s>>>(op, cells, factors, status);
   return ok() < 0 ? -1 : 1;
 }
 
@@ -411,16 +427,16 @@ int apply_impl(const DevCells &cells, int nu, const int *cell_list, int ncol, co
 
 template <typename TF>
 int launch_schur_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,
-                        cudaStream_t s) {
+                        bool fp32, cudaStream_t s) {
   if (!op.structured) return -1;
-  return factor_impl<TF, 1>(op, cells, factors, status, s);
+  return factor_impl<TF, 1>(op, cells, factors, status, fp32, s);
 }
 
 template <typename TF>
 int launch_schur3_factor(const DevOp<double> &op, const DevCells &cells, TF *factors, int *status,
-                         cudaStream_t s) {
+                         bool fp32, cudaStream_t s) {
   if (op.structured || !op.diag) return -1;
-  return factor_impl<TF, 3>(op, cells, factors, status, s);
+  return factor_impl<TF, 3>(op, cells, factors, status, fp32, s);
 }
 
 template <typename T>
@@ -455,9 +471,9 @@ int launch_block_structure(const DevOp<double> &op, long long n, int *flag, cuda
 }
 
 #define PM_SINST(T)                                                                              \
-  template int launch_schur_factor<T>(const DevOp<double> &, const DevCells &, T *, int *,        \
+  template int launch_schur_factor<T>(const DevOp<double> &, const DevCells &, T *, int *, bool,  \
                                       cudaStream_t);                                              \
-  template int launch_schur3_factor<T>(const DevOp<double> &, const DevCells &, T *, int *,       \
+  template int launch_schur3_factor<T>(const DevOp<double> &, const DevCells &, T *, int *, bool, \
                                        cudaStream_t);                                             \
   template int launch_schur_apply<T>(const DevCells &, int, const int *, int, const T *,          \
                                      const T *, T, T *, cudaStream_t);                            \
