@@ -80,6 +80,9 @@ def parse():
                          "local-residual and apply kernels")
     ap.add_argument("--residual-variant", type=int, default=0,
                     help="pm_options.residual_variant of the --only-sweep case")
+    ap.add_argument("--factor-fp32", type=int, default=-1, choices=[-1, 0, 1],
+                    help="pm_options.factor_fp32 of the --only-factor case (-1: FP32 block "
+                         "elimination, FP64 85x85 LU; 0: both FP64; 1: both FP32)")
     ap.add_argument("--decouple", type=int, default=1,
                     help="pm_options.decouple of the --only-sweep / --only-factor cases (0: the "
                          "85x85 LU and all nine blocks on every level)")
@@ -643,9 +646,11 @@ def only_factor(args):
     prints the mean factorisation time (the library's CUDA events)."""
     from to_merge_master_parmoon_gb300 import OseenProblem, PmSolver
     P = OseenProblem(n_levels=args.levels, nu=args.nu, seed=args.seed, nthreads=os.cpu_count() or 1)
-    S = PmSolver(P.descs, precision="mixed", decouple=args.decouple)
+    S = PmSolver(P.descs, precision="mixed", decouple=args.decouple,
+                 factor_fp32=args.factor_fp32)
     ms = [S.refactor() for _ in range(args.warmup + args.steps)][args.warmup:]
     print(json.dumps({"only_factor": True, "levels": P.n_levels,
+                      "factor_fp32": args.factor_fp32,
                       "cells": sum(P.desc(l).n_cells for l in range(1, P.n_levels)),
                       "factor_ms": sum(ms) / len(ms)}), flush=True)
 
