@@ -9,6 +9,9 @@
   REF_HARNESS_TUS below) compiled where they lie, driven by ref_harness.cpp
   and ref_vanka.cpp (only when the tree is present; the defect and Vanka
   outputs are committed as tests/golden/ref_defect_*.npz, ref_vanka_*.npz).
+* ``oracle/_ref/libref_hybrid.so`` — the same with the reference's
+  colour-parallel build of its cell Vanka (-D_HYBRID; only when the tree is
+  present; its sweeps are committed as tests/golden/ref_vanka_colour_*.npz).
 * ``oracle/_ref/libref_transfer.so`` — the reference's grid transfers with
   the FE and geometry databases they read, and its multigrid cycle driver
   (TMultiGridIte, TNSE_MultiGrid) over one TNSE_MGLevel4 per level
@@ -100,6 +103,35 @@ def build_ref_harness() -> Path | None:
     return out
 
 
+def build_ref_hybrid() -> Path | None:
+    """The same translation units and harness as build_ref_harness, with the
+    reference's colour-parallel build (-D_HYBRID instead of -D_SEQ: the
+    OpenMP colour loop of TNSE_MGLevel4::CellVanka), into
+    oracle/_ref/libref_hybrid.so.  ref_hybrid_mapper.h is force-included and
+    stands for the constructor's TParFEMapper3D (parMapper_P).  Returns None
+    without the tree."""
+    src = REFERENCE / "src"
+    if not all((src / f"{t}.C").exists() for t in REF_HARNESS_TUS):
+        return None
+    objdir = REF_OUT / "hybrid_obj"
+    objdir.mkdir(parents=True, exist_ok=True)
+    out = REF_OUT / "libref_hybrid.so"
+    mine = [HERE / "ref_harness.cpp", HERE / "ref_vanka.cpp", HERE / "ref_hybrid_mapper.h",
+            *_ref_deps()]
+    if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in mine):
+        return out
+    jobs = [(src / f"{t}.C", objdir / f"{Path(t).name}.o") for t in REF_HARNESS_TUS]
+    jobs.append((HERE / "ref_harness.cpp", objdir / "ref_harness.o"))
+    jobs.append((HERE / "ref_vanka.cpp", objdir / "ref_vanka.o"))
+    flags = [f for f in _ref_flags() if f != "-D_SEQ"]
+    flags += ["-D_HYBRID", "-include", str(HERE / "ref_hybrid_mapper.h"),
+              "-DparMapper_P=ref_hybrid_mapper()"]
+    _compile(jobs, flags, extra_deps=[HERE / "ref_hybrid_mapper.h"])
+    _run(["g++", "-shared", "-fopenmp", "-Wl,--gc-sections", "-Wl,-z,defs",
+          *[str(o) for _, o in jobs], "-o", str(out)])
+    return out
+
+
 # reference translation units of the facade check: the TItMethod base and
 # the matrix and structure classes the adapter reads
 REF_FACADE_TUS = ("FE/ItMethod", "FE/Matrix", "FE/SquareMatrix", "FE/Structure",
@@ -139,12 +171,12 @@ def _ref_deps():
             *sorted((HERE / "ref_stubs").glob("*.h"))]
 
 
-def _compile(jobs, cmd):
+def _compile(jobs, cmd, extra_deps=()):
     """Compile (source, object) pairs with ``cmd``, os.cpu_count() at a time,
-    skipping objects newer than their source and _ref_deps()."""
+    skipping objects newer than their source, _ref_deps() and extra_deps."""
     from concurrent.futures import ThreadPoolExecutor
 
-    newest_dep = max(d.stat().st_mtime for d in _ref_deps())
+    newest_dep = max(d.stat().st_mtime for d in [*_ref_deps(), *extra_deps])
 
     def one(job):
         src, obj = job
@@ -255,5 +287,6 @@ if __name__ == "__main__":
     print(build_oracle())
     print(build_ref_pin())
     print(build_ref_harness())
+    print(build_ref_hybrid())
     print(build_ref_transfer())
     print(build_ref_facade())

@@ -453,8 +453,9 @@ void cell_vanka(oracle *o, OLevel &L, double *u, const double *rhs) {
     }
   } else {
     // colour-block: residuals of one colour from the state before the
-    // colour, batched solves, then the (disjoint) updates
-    // (CellVanka_GPU, src/FE/NSE_CellVanka.cu:2181-2365)
+    // colour, batched solves, then the (disjoint) updates (the OpenMP colour
+    // loop of the colour-parallel CellVanka, src/FE/NSE_MGLevel4.C:603-1651,
+    // and CellVanka_GPU, src/FE/NSE_CellVanka.cu:2181-2365)
     const int ncol = (int)L.colour_ptr.size() - 1;
     std::vector<double> sols;
     for (int col = 0; col < ncol; ++col) {

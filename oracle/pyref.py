@@ -15,7 +15,7 @@ import ctypes as C
 
 import numpy as np
 
-from .build_oracle import build_ref_harness, build_ref_transfer
+from .build_oracle import build_ref_harness, build_ref_hybrid, build_ref_transfer
 
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
@@ -30,34 +30,56 @@ def ref_harness_lib():
         path = build_ref_harness()
         if path is None:
             return None
-        L = C.CDLL(str(path))
-        L.ref_level_create.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _dpp, _ip, _ip, _dpp,
-                                       _ip, _ip, _dpp]
-        L.ref_level_create.restype = C.c_void_p
-        L.ref_level_destroy.argtypes = [C.c_void_p]
-        L.ref_level_destroy.restype = None
-        L.ref_defect.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int, C.c_int]
-        L.ref_defect.restype = None
-        L.ref_matvec.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int]
-        L.ref_matvec.restype = None
-        L.ref_fgmres.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
-                                 C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p,
-                                 C.c_int]
-        L.ref_fgmres.restype = C.c_int
-        L.ref_into_l20.argtypes = [_dp, C.c_int, C.c_int]
-        L.ref_into_l20.restype = None
-        L.ref_vanka_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip,
-                                       _ip, _ip, _dpp, _ip, _ip, _dpp, _ip, _ip, _dpp,
-                                       C.c_double]
-        L.ref_vanka_create.restype = C.c_void_p
-        L.ref_vanka_destroy.argtypes = [C.c_void_p]
-        L.ref_vanka_destroy.restype = None
-        L.ref_vanka_sweeps.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double]
-        L.ref_vanka_sweeps.restype = None
-        L.ref_vanka_solve_exact.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
-        L.ref_vanka_solve_exact.restype = None
-        _LIB = L
+        _LIB = _declare(C.CDLL(str(path)))
     return _LIB
+
+
+_HLIB = None
+
+
+def ref_hybrid_lib():
+    """The harness in the reference's colour-parallel build (its OpenMP
+    colour loop of CellVanka), or None when the reference tree is absent."""
+    global _HLIB
+    if _HLIB is None:
+        path = build_ref_hybrid()
+        if path is None:
+            return None
+        L = _declare(C.CDLL(str(path)))
+        L.ref_vanka_set_colours.argtypes = [C.c_void_p, C.c_int, _ip, _ip, C.c_int, C.c_int]
+        L.ref_vanka_set_colours.restype = C.c_int
+        _HLIB = L
+    return _HLIB
+
+
+def _declare(L):
+    """ctypes signatures of the harness entry points (both builds)."""
+    L.ref_level_create.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _dpp, _ip, _ip, _dpp,
+                                   _ip, _ip, _dpp]
+    L.ref_level_create.restype = C.c_void_p
+    L.ref_level_destroy.argtypes = [C.c_void_p]
+    L.ref_level_destroy.restype = None
+    L.ref_defect.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int, C.c_int]
+    L.ref_defect.restype = None
+    L.ref_matvec.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int]
+    L.ref_matvec.restype = None
+    L.ref_fgmres.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double,
+                             C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p,
+                             C.c_int]
+    L.ref_fgmres.restype = C.c_int
+    L.ref_into_l20.argtypes = [_dp, C.c_int, C.c_int]
+    L.ref_into_l20.restype = None
+    L.ref_vanka_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip,
+                                   _ip, _ip, _dpp, _ip, _ip, _dpp, _ip, _ip, _dpp,
+                                   C.c_double]
+    L.ref_vanka_create.restype = C.c_void_p
+    L.ref_vanka_destroy.argtypes = [C.c_void_p]
+    L.ref_vanka_destroy.restype = None
+    L.ref_vanka_sweeps.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double]
+    L.ref_vanka_sweeps.restype = None
+    L.ref_vanka_solve_exact.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
+    L.ref_vanka_solve_exact.restype = None
+    return L
 
 
 def _i(a):
@@ -183,11 +205,15 @@ class RefLevel:
 
 class RefVankaLevel:
     """One level (the dict of ``OseenProblem.arrays``) as the reference's
-    TNSE_MGLevel4 in its sequential build, for its cell Vanka
-    (src/FE/NSE_MGLevel4.C:1653-2087, run by oracle/ref_vanka.cpp)."""
+    TNSE_MGLevel4, for its cell Vanka (run by oracle/ref_vanka.cpp): the
+    sequential build's cell loop (src/FE/NSE_MGLevel4.C:1653-2087), or, with
+    ``colours`` (one colour per cell, no two cells of a colour sharing a
+    DOF), the colour-parallel build's OpenMP colour loop (:603-1651) over
+    those colours in increasing order, cells of a colour in index order, on
+    ``threads`` threads."""
 
-    def __init__(self, arrays: dict, alpha: float = 1.0):
-        L = ref_harness_lib()
+    def __init__(self, arrays: dict, alpha: float = 1.0, colours=None, threads: int = 4):
+        L = ref_harness_lib() if colours is None else ref_hybrid_lib()
         if L is None:
             raise RuntimeError("reference tree not present: the reference harness is not built")
         self._L = L
@@ -220,6 +246,17 @@ class RefVankaLevel:
             ip(arrays["bt_rowptr"]), ip(arrays["bt_col"]), dpp(arrays["bt"]), float(alpha))
         if not self._h:
             raise ValueError(f"unsupported local velocity size {nu_loc}")
+        if colours is not None:
+            col = np.asarray(colours, dtype=np.int64)
+            assert col.shape == (n_cells,) and col.min() >= 0
+            order = np.argsort(col, kind="stable").astype(np.int32)
+            counts = np.bincount(col)
+            used = counts[counts > 0]
+            ptr = np.concatenate([[0], np.cumsum(used)]).astype(np.int32)
+            keep += [order, ptr]
+            if L.ref_vanka_set_colours(self._h, len(used), ptr.ctypes.data_as(_ip),
+                                       order.ctypes.data_as(_ip), n_cells, threads) != 0:
+                raise ValueError("inconsistent colouring")
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -1,10 +1,19 @@
 // ref_vanka.cpp — runs the reference's own cell Vanka smoother on a level
 // handed over as plain arrays.  TEST INFRASTRUCTURE ONLY: it pins the
-// oracle's cell_vanka (sequential mode) against the reference code itself.
+// oracle's cell_vanka against the reference code itself.
 // Linked into oracle/_ref/libref_harness.so with ref_harness.cpp by
 // oracle/build_oracle.py (build_ref_harness), with -D__3D__ -D_SEQ (the
-// reference's sequential build; the _SEQ cell loop is the one the oracle
-// restates).
+// reference's sequential build; the _SEQ cell loop is the one the oracle's
+// sequential mode restates), and a second time into
+// oracle/_ref/libref_hybrid.so (build_ref_hybrid) with -D_HYBRID instead:
+// the reference's colour-parallel CellVanka (src/FE/NSE_MGLevel4.C:603-1651),
+// which per colour assembles every cell's local system and right-hand side
+// from the current iterate in an OpenMP loop, then solves them and adds the
+// damped corrections (cells of one colour share no DOF), colour after
+// colour: the ordering of the oracle's colour mode and of the GPU sweeps.
+// Its colouring (ptrCellColors / CellReorder, normally from the MPI build's
+// TParFEMapper3D) is set by ref_vanka_set_colours; ref_hybrid_mapper.h says
+// how the constructor is compiled without that mapper.
 //
 // Reference code that runs here:
 //   src/FE/NSE_MGLevel4.C    TNSE_MGLevel4 constructor (:119-328), the _SEQ
@@ -92,6 +101,16 @@ struct Level : public TNSE_MGLevel4 {
     delete[] Aux[0];
     delete[] Aux;
   }
+#ifdef _HYBRID
+  // the colouring the colour-parallel CellVanka walks (the members the
+  // constructor takes from TParFEMapper3D, src/FE/NSE_MGLevel4.C:315-324)
+  void set_colours(int n_colours, int *colour_ptr, int *cell_order, int max_cells) {
+    N_CIntCell = n_colours;
+    ptrCellColors = colour_ptr;
+    CellReorder = cell_order;
+    maxCellsPerColor = max_cells;
+  }
+#endif
 };
 
 template <class T>
@@ -121,6 +140,8 @@ struct VankaLevel {
   double al[2] = {1.0, 1.0};
   alignas(Level) unsigned char level_store[sizeof(Level)];
   Level *level = nullptr;
+  int *colour_ptr = nullptr, *cell_order = nullptr;  // colour-parallel build only
+  int threads = 1;
 };
 
 FixedElement *element_of(int n_dof) {
@@ -129,6 +150,13 @@ FixedElement *element_of(int n_dof) {
 }
 
 }  // namespace
+
+#ifdef _HYBRID
+RefHybridMapper *ref_hybrid_mapper() {
+  static RefHybridMapper none;
+  return &none;
+}
+#endif
 
 extern "C" {
 
@@ -222,8 +250,38 @@ __attribute__((visibility("default"))) void ref_vanka_destroy(void *h) {
   delete[] V->f;
   delete[] V->u;
   delete[] V->aux;
+  delete[] V->colour_ptr;
+  delete[] V->cell_order;
   delete V;
 }
+
+#ifdef _HYBRID
+// The colouring of the colour-parallel CellVanka: colour k holds the cells
+// cell_order[colour_ptr[k] .. colour_ptr[k+1]-1] (no two sharing a DOF),
+// solved by `threads` OpenMP threads (OMPNUMTHREADS; the result does not
+// depend on it).  Returns 0, or -1 for an inconsistent colouring.
+__attribute__((visibility("default"))) int ref_vanka_set_colours(void *h, int n_colours,
+                                                                 const int *colour_ptr,
+                                                                 const int *cell_order,
+                                                                 int n_cells, int threads) {
+  VankaLevel *V = static_cast<VankaLevel *>(h);
+  if (n_colours <= 0 || colour_ptr[0] != 0 || colour_ptr[n_colours] != n_cells || threads <= 0)
+    return -1;
+  int max_cells = 0;
+  for (int k = 0; k < n_colours; ++k) {
+    const int m = colour_ptr[k + 1] - colour_ptr[k];
+    if (m <= 0) return -1;
+    if (m > max_cells) max_cells = m;
+  }
+  delete[] V->colour_ptr;
+  delete[] V->cell_order;
+  V->colour_ptr = copy_of(colour_ptr, n_colours + 1L);
+  V->cell_order = copy_of(cell_order, (long)n_cells);
+  V->threads = threads;
+  V->level->set_colours(n_colours, V->colour_ptr, V->cell_order, max_cells);
+  return 0;
+}
+#endif
 
 // sweeps x TNSE_MGLevel4::CellVanka(u, rhs, aux, 0, NULL, 2, 1) with the
 // damping SC_SMOOTH_DAMP_FACTOR_COARSE_SADDLE = damp and direct local
@@ -236,6 +294,10 @@ __attribute__((visibility("default"))) void ref_vanka_sweeps(void *h, double *u,
   db->SC_SMOOTH_DAMP_FACTOR_COARSE_SADDLE = damp;
   db->SC_LARGEST_DIRECT_SOLVE = 1 << 20;
   db->INTERNAL_LOCAL_DOF = -1;
+#ifdef _HYBRID
+  if (!V->colour_ptr) return;  // no colouring set: nothing to sweep
+  db->OMPNUMTHREADS = V->threads;
+#endif
   double *r = copy_of(rhs, V->n);
   for (int s = 0; s < sweeps; ++s) V->level->CellVanka(u, r, V->aux, 0, nullptr, 2, 1);
   delete[] r;

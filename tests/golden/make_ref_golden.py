@@ -12,6 +12,10 @@ oracle/build_oracle.py compiles with the reference sources where they lie:
 * tests/golden/ref_vanka_*.npz: one and two sweeps of the cell Vanka
   TNSE_MGLevel4::CellVanka (src/FE/NSE_MGLevel4.C:1653-2087, sequential
   build, damping 1, no relaxation) from u = x with right-hand side b;
+* tests/golden/ref_vanka_colour_*.npz: the same sweeps by the reference's
+  colour-parallel build (-D_HYBRID: CellVanka's OpenMP colour loop,
+  src/FE/NSE_MGLevel4.C:603-1651) over the level's own colouring, and two
+  sweeps with damping 0.8 and relaxation 0.7;
 * tests/golden/ref_cycle_*.npz: one V(2,2) cycle from zero on b, the
   preconditioner call TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132)
   with TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779) over two or
@@ -24,7 +28,8 @@ oracle/build_oracle.py compiles with the reference sources where they lie:
   the solution and the iteration count).
 Needs the reference tree; the fixtures are committed so the tests do not.
 ``python make_ref_golden.py cycle`` writes the cycle fixtures only,
-``python make_ref_golden.py solve`` the whole-solver ones.
+``python make_ref_golden.py solve`` the whole-solver ones,
+``python make_ref_golden.py colour`` the colour-parallel Vanka ones.
 
 Inputs are exact binary fractions of the DOF index (``golden_inputs``), so
 every platform forms the same x and b without a random generator.
@@ -72,6 +77,38 @@ VANKA_CASES = {
     "tetra": (dict(n_levels=2, nu=1.0, seed=0, example="quadlin_oseen", element="tetra",
                    nx0=1, ny0=1, nz0=1), 1),
 }
+
+
+# name -> (OseenProblem keyword arguments, level) of the colour-parallel Vanka
+# fixtures: the reference's OpenMP colour loop over the level's own colouring
+# (cell_colour of the problem), which is also what the library sweeps by
+COLOUR_VANKA_CASES = {
+    "hexa": (dict(CASES["hexa"][0], n_levels=3), 2),
+    "channel": (CASES["channel"][0], 1),
+    "tetra": VANKA_CASES["tetra"],
+}
+# (damping, relaxation alpha) of the second pair of colour-parallel sweeps
+COLOUR_VANKA_DAMPED = (0.8, 0.7)
+
+
+def write_colour_vanka_fixtures() -> None:
+    from oracle.pyref import RefVankaLevel
+    damp, alpha = COLOUR_VANKA_DAMPED
+    for name, (kwargs, level) in COLOUR_VANKA_CASES.items():
+        P = build_problem(kwargs)
+        a = P.arrays(level)
+        x, b = golden_inputs(P.ndof(level))
+        V = RefVankaLevel(a, colours=a["cell_colour"])
+        W = RefVankaLevel(a, alpha=alpha, colours=a["cell_colour"])
+        np.savez_compressed(
+            HERE / f"ref_vanka_colour_{name}.npz",
+            problem=json.dumps(kwargs), level=level, n_cells=a["n_cells"],
+            colours=np.asarray(a["cell_colour"], dtype=np.int32),
+            u_sweep1=V.cell_vanka(x, b, 1), u_sweep2=V.cell_vanka(x, b, 2),
+            u_damped2=W.cell_vanka(x, b, 2, damp), damp=damp, alpha=alpha,
+            source=("reference src/FE/NSE_MGLevel4.C TNSE_MGLevel4::CellVanka (_HYBRID: "
+                    "the OpenMP colour loop) run by oracle/ref_vanka.cpp"))
+        print("wrote colour vanka", name, "level", level, "ndof", P.ndof(level))
 
 
 # name -> (OseenProblem keyword arguments, fine level) of the transfer fixtures
@@ -144,6 +181,9 @@ def main() -> None:
         return
     if sys.argv[1:] == ["solve"]:
         write_solve_fixtures()
+        return
+    if sys.argv[1:] == ["colour"]:
+        write_colour_vanka_fixtures()
         return
     for name, (kwargs, level) in CASES.items():
         P = build_problem(kwargs)

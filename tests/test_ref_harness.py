@@ -84,7 +84,7 @@ def load_case(name, kind="defect"):
     if kind == "defect":
         assert P.arrays(level)["n_udof"] == int(g["n_udof"])
         assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
-    elif kind in ("vanka", "coarse"):
+    elif kind in ("vanka", "coarse", "vanka_colour"):
         assert P.arrays(level)["n_cells"] == int(g["n_cells"])
     elif kind == "cycle":
         assert level == P.n_levels - 1
@@ -621,3 +621,81 @@ def test_gpu_fgmres_matches_reference_solve_fixtures(precision):
         xp[0::4] -= xp[0::4].mean()
         rp[0::4] -= rp[0::4].mean()
         assert rel(xp, rp) < 1e-6
+
+
+# ----------------------------------------------------- colour-parallel ----
+# oracle/_ref/libref_hybrid.so is the reference's colour-parallel build
+# (-D_HYBRID): CellVanka's OpenMP colour loop (src/FE/NSE_MGLevel4.C:603-1651)
+# assembles every cell's local system and right-hand side of one colour from
+# the current iterate, solves them and adds the damped corrections, colour
+# after colour.  That is the colour-block ordering of the oracle's colour mode
+# and of the GPU sweeps, so all three are compared over the same colouring
+# (the level's cell_colour), not only with one cell per colour.
+
+def _hybrid_or_skip():
+    from oracle.pyref import ref_hybrid_lib
+    if ref_hybrid_lib() is None:
+        pytest.skip("reference tree not present (the committed fixtures cover this case)")
+    from oracle.pyref import RefVankaLevel
+    return RefVankaLevel
+
+
+@pytest.mark.parametrize("name", ["hexa", "channel", "tetra"])
+@pytest.mark.parametrize("damp,alpha", [(1.0, 1.0), (0.8, 0.7)])
+def test_oracle_colour_vanka_equals_reference_colour_parallel_bitwise(name, damp, alpha):
+    RefVankaLevel = _hybrid_or_skip()
+    gm = _golden_module()
+    kwargs, level = gm.COLOUR_VANKA_CASES[name]
+    P = gm.build_problem(kwargs)
+    a = P.arrays(level)
+    x, b = gm.golden_inputs(P.ndof(level))
+    for threads in (1, 4):
+        V = RefVankaLevel(a, alpha=alpha, colours=a["cell_colour"], threads=threads)
+        want = V.cell_vanka(x, b, 2, damp)
+        got = Oracle(P, vanka_mode="colour", smooth_damp=damp, alpha=alpha).cell_vanka(
+            level, x, b, 2)
+        assert np.array_equal(got, want)
+    # the ordering matters: the sequential cell loop gives another iterate
+    seq = RefVankaLevel(a, alpha=alpha).cell_vanka(x, b, 2, damp)
+    assert rel(seq, want) > 1e-3
+
+
+@pytest.mark.parametrize("name", ["hexa", "channel", "tetra"])
+def test_colour_vanka_fixtures_reproduce_from_the_reference(name):
+    RefVankaLevel = _hybrid_or_skip()
+    P, level, x, b, g = load_case(name, "vanka_colour")
+    a = P.arrays(level)
+    assert np.array_equal(np.asarray(a["cell_colour"], dtype=np.int32), g["colours"])
+    V = RefVankaLevel(a, colours=g["colours"])
+    assert np.array_equal(V.cell_vanka(x, b, 1), g["u_sweep1"])
+    assert np.array_equal(V.cell_vanka(x, b, 2), g["u_sweep2"])
+    W = RefVankaLevel(a, alpha=float(g["alpha"]), colours=g["colours"])
+    assert np.array_equal(W.cell_vanka(x, b, 2, float(g["damp"])), g["u_damped2"])
+
+
+@pytest.mark.parametrize("name", ["hexa", "channel", "tetra"])
+def test_oracle_colour_vanka_matches_reference_fixtures(name):
+    P, level, x, b, g = load_case(name, "vanka_colour")
+    O = Oracle(P, vanka_mode="colour")
+    assert rel(O.cell_vanka(level, x, b, 1), g["u_sweep1"]) < 1e-13
+    assert rel(O.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-13
+    W = Oracle(P, vanka_mode="colour", smooth_damp=float(g["damp"]), alpha=float(g["alpha"]))
+    assert rel(W.cell_vanka(level, x, b, 2), g["u_damped2"]) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hexa", "channel", "tetra"])
+def test_gpu_vanka_matches_reference_colour_parallel_fixtures(name):
+    """The FP64 CUDA colour-block sweeps over the level's colouring (the
+    library's default local solves) against the reference's colour-parallel
+    CellVanka, undamped and with damping 0.8 / relaxation 0.7."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, x, b, g = load_case(name, "vanka_colour")
+    S = PmSolver(P.descs, precision="fp64")
+    assert rel(S.cell_vanka(level, x, b, 1), g["u_sweep1"]) < 1e-9
+    assert rel(S.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-9
+    S.close()
+    W = PmSolver(P.descs, precision="fp64", smooth_damp=float(g["damp"]),
+                 alpha=float(g["alpha"]))
+    assert rel(W.cell_vanka(level, x, b, 2), g["u_damped2"]) < 1e-9
+    W.close()
