@@ -19,6 +19,10 @@
   present; its outputs are committed as tests/golden/ref_transfer_*.npz and
   tests/golden/ref_cycle_*.npz, and with libref_harness.so's FGMRES as
   tests/golden/ref_solve_*.npz).
+* ``oracle/_ref/libref_transfer_hybrid.so`` — the same in the reference's
+  colour-parallel build (-D_HYBRID), whose levels smooth with the OpenMP
+  colour loop of CellVanka (only when the tree is present; committed as
+  tests/golden/ref_cycle_colour_*.npz and ref_solve_colour_*.npz).
 * ``oracle/_ref/libref_facade.so`` — include/pmgpu_parmoon.h (the solver as a
   ParMooN TItMethod) compiled against the reference's headers and matrix
   classes in ref_facade.cpp, linked with libpmgpu.so (only when the tree is
@@ -123,10 +127,7 @@ def build_ref_hybrid() -> Path | None:
     jobs = [(src / f"{t}.C", objdir / f"{Path(t).name}.o") for t in REF_HARNESS_TUS]
     jobs.append((HERE / "ref_harness.cpp", objdir / "ref_harness.o"))
     jobs.append((HERE / "ref_vanka.cpp", objdir / "ref_vanka.o"))
-    flags = [f for f in _ref_flags() if f != "-D_SEQ"]
-    flags += ["-D_HYBRID", "-include", str(HERE / "ref_hybrid_mapper.h"),
-              "-DparMapper_P=ref_hybrid_mapper()"]
-    _compile(jobs, flags, extra_deps=[HERE / "ref_hybrid_mapper.h"])
+    _compile(jobs, _hybrid_flags(), extra_deps=[HERE / "ref_hybrid_mapper.h"])
     _run(["g++", "-shared", "-fopenmp", "-Wl,--gc-sections", "-Wl,-z,defs",
           *[str(o) for _, o in jobs], "-o", str(out)])
     return out
@@ -254,24 +255,37 @@ REF_TRANSFER_TUS = {
 }
 
 
-def build_ref_transfer() -> Path | None:
+def _hybrid_flags():
+    """_ref_flags() for the reference's colour-parallel build: -D_HYBRID
+    instead of -D_SEQ, with ref_hybrid_mapper.h standing for the
+    constructor's TParFEMapper3D."""
+    return [f for f in _ref_flags() if f != "-D_SEQ"] + [
+        "-D_HYBRID", "-include", str(HERE / "ref_hybrid_mapper.h"),
+        "-DparMapper_P=ref_hybrid_mapper()"]
+
+
+def build_ref_transfer(hybrid: bool = False) -> Path | None:
     """Compile the reference's grid transfers (Prolongate, DefectRestriction,
-    GetProlongationMatrix3D) and the databases they read, with
-    ref_transfer.cpp, into oracle/_ref/libref_transfer.so.  Returns None
-    without the tree."""
+    GetProlongationMatrix3D) and the databases they read, and its cycle
+    driver, with ref_transfer.cpp, into oracle/_ref/libref_transfer.so, or
+    with ``hybrid`` in the reference's colour-parallel build into
+    oracle/_ref/libref_transfer_hybrid.so.  Returns None without the tree."""
     srcs = [REFERENCE / "src" / d / f"{t}.C" for d, ts in REF_TRANSFER_TUS.items() for t in ts]
     if not all(s.exists() for s in srcs):
         return None
-    objdir = REF_OUT / "transfer_obj"
+    tag = "transfer_hybrid" if hybrid else "transfer"
+    objdir = REF_OUT / f"{tag}_obj"
     objdir.mkdir(parents=True, exist_ok=True)
-    out = REF_OUT / "libref_transfer.so"
-    mine = [HERE / "ref_transfer.cpp", *_ref_deps()]
+    out = REF_OUT / f"libref_{tag}.so"
+    extra = [HERE / "ref_hybrid_mapper.h"] if hybrid else []
+    mine = [HERE / "ref_transfer.cpp", *extra, *_ref_deps()]
     if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in mine):
         return out
+    flags = _hybrid_flags() if hybrid else _ref_flags()
     jobs = [(s, objdir / f"{s.parent.name}_{s.stem}.o") for s in srcs]
-    _compile(jobs, _ref_flags())
+    _compile(jobs, flags, extra_deps=extra)
     own = objdir / "ref_transfer.o"
-    _compile([(HERE / "ref_transfer.cpp", own)], _ref_flags())
+    _compile([(HERE / "ref_transfer.cpp", own)], flags, extra_deps=extra)
     archive = objdir / "libref_transfer_tus.a"
     if archive.exists():
         archive.unlink()
@@ -289,4 +303,5 @@ if __name__ == "__main__":
     print(build_ref_harness())
     print(build_ref_hybrid())
     print(build_ref_transfer())
+    print(build_ref_transfer(hybrid=True))
     print(build_ref_facade())

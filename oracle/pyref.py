@@ -247,14 +247,9 @@ class RefVankaLevel:
         if not self._h:
             raise ValueError(f"unsupported local velocity size {nu_loc}")
         if colours is not None:
-            col = np.asarray(colours, dtype=np.int64)
-            assert col.shape == (n_cells,) and col.min() >= 0
-            order = np.argsort(col, kind="stable").astype(np.int32)
-            counts = np.bincount(col)
-            used = counts[counts > 0]
-            ptr = np.concatenate([[0], np.cumsum(used)]).astype(np.int32)
-            keep += [order, ptr]
-            if L.ref_vanka_set_colours(self._h, len(used), ptr.ctypes.data_as(_ip),
+            assert len(colours) == n_cells
+            ptr, order = colour_lists(colours)
+            if L.ref_vanka_set_colours(self._h, len(ptr) - 1, ptr.ctypes.data_as(_ip),
                                        order.ctypes.data_as(_ip), n_cells, threads) != 0:
                 raise ValueError("inconsistent colouring")
 
@@ -283,14 +278,14 @@ class RefVankaLevel:
         return u
 
 
-_TLIB = None
+_TLIB = {}
 
 
-def ref_transfer_lib():
-    """The loaded transfer harness, or None when the reference tree is absent."""
-    global _TLIB
-    if _TLIB is None:
-        path = build_ref_transfer()
+def ref_transfer_lib(hybrid: bool = False):
+    """The loaded transfer harness (with ``hybrid``: its colour-parallel
+    build), or None when the reference tree is absent."""
+    if hybrid not in _TLIB:
+        path = build_ref_transfer(hybrid=hybrid)
         if path is None:
             return None
         L = C.CDLL(str(path))
@@ -313,8 +308,23 @@ def ref_transfer_lib():
         L.ref_cycle_vcycle.restype = None
         L.ref_cycle_configure.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
         L.ref_cycle_configure.restype = None
-        _TLIB = L
-    return _TLIB
+        if hybrid:
+            L.ref_cycle_set_colours.argtypes = [C.c_void_p, C.c_int, C.c_int, _ip, _ip, C.c_int,
+                                                C.c_int]
+            L.ref_cycle_set_colours.restype = C.c_int
+        _TLIB[hybrid] = L
+    return _TLIB[hybrid]
+
+
+def colour_lists(colours):
+    """(colour_ptr, cell_order) of a per-cell colour array: the colours in
+    increasing order, each with its cells in index order."""
+    col = np.asarray(colours, dtype=np.int64)
+    assert col.ndim == 1 and col.size and col.min() >= 0
+    order = np.argsort(col, kind="stable").astype(np.int32)
+    counts = np.bincount(col)
+    ptr = np.concatenate([[0], np.cumsum(counts[counts > 0])]).astype(np.int32)
+    return ptr, order
 
 
 class RefTransfer:
@@ -366,10 +376,14 @@ class RefCycle:
     (src/FE/MultiGridIte.C:76-132) with TNSE_MultiGrid::Cycle
     (src/FE/NSE_MultiGrid.C:434-1779), over every level of a hexahedral
     Q2/P1disc problem (run by oracle/ref_transfer.cpp): cell Vanka on each
-    level above the coarsest, the exact solve on the coarsest one."""
+    level above the coarsest, the exact solve on the coarsest one.  The
+    sequential build's cell loop, or with ``colours`` the colour-parallel
+    build's OpenMP colour loop over every smoothed level's own colouring
+    (its cell_colour), on ``threads`` threads."""
 
-    def __init__(self, problem, alpha: float = 1.0, beta: float = 1.0):
-        L = ref_transfer_lib()
+    def __init__(self, problem, alpha: float = 1.0, beta: float = 1.0, colours: bool = False,
+                 threads: int = 4):
+        L = ref_transfer_lib(hybrid=colours)
         if L is None:
             raise RuntimeError("reference tree not present: the transfer harness is not built")
         self._L = L
@@ -415,6 +429,13 @@ class RefCycle:
             alpha, beta)
         if not self._h:
             raise ValueError("the levels are not a regular refinement (8 children per cell)")
+        if colours:
+            for l in range(1, len(lv)):
+                ptr, order = colour_lists(lv[l]["cell_colour"])
+                if L.ref_cycle_set_colours(self._h, l, len(ptr) - 1, ptr.ctypes.data_as(_ip),
+                                           order.ctypes.data_as(_ip), lv[l]["n_cells"],
+                                           threads) != 0:
+                    raise ValueError(f"inconsistent colouring on level {l}")
 
     def __del__(self):
         if getattr(self, "_h", None):

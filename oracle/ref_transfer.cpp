@@ -63,6 +63,13 @@
 // The node orders this gives are checked against the ones read from the
 // refined reference cell's vertices.
 //
+// Compiled a second time with -D_HYBRID instead of -D_SEQ
+// (libref_transfer_hybrid.so), the levels smooth with the reference's
+// colour-parallel CellVanka (src/FE/NSE_MGLevel4.C:603-1651, the OpenMP
+// colour loop) over colourings set by ref_cycle_set_colours;
+// ref_hybrid_mapper.h says how the constructor is compiled without the MPI
+// build's TParFEMapper3D.
+//
 // The same levels also run the reference's multigrid cycle (ref_cycle_*):
 // TMultiGridIte::Iterate (src/FE/MultiGridIte.C:76-132), the preconditioner
 // call, with TNSE_MultiGrid::Cycle (src/FE/NSE_MultiGrid.C:434-1779) over
@@ -471,7 +478,26 @@ struct CycleLevel : public TNSE_MGLevel4 {
     delete[] Aux[0];
     delete[] Aux;
   }
+#ifdef _HYBRID
+  // the colouring of the colour-parallel CellVanka (the members the
+  // constructor takes from TParFEMapper3D, src/FE/NSE_MGLevel4.C:315-324)
+  void set_colours(int n_colours, int *colour_ptr, int *cell_order, int max_cells) {
+    N_CIntCell = n_colours;
+    ptrCellColors = colour_ptr;
+    CellReorder = cell_order;
+    maxCellsPerColor = max_cells;
+  }
+#endif
 };
+
+#ifdef _HYBRID
+}  // namespace
+RefHybridMapper *ref_hybrid_mapper() {
+  static RefHybridMapper none;
+  return &none;
+}
+namespace {
+#endif
 
 // One level's matrices, vectors and TNSE_MGLevel4 over a Side's spaces
 struct MGLevelStore {
@@ -489,6 +515,7 @@ struct MGLevelStore {
   double al[2] = {1.0, 1.0};
   alignas(CycleLevel) unsigned char level_store[sizeof(CycleLevel)];
   CycleLevel *level = nullptr;
+  int *colour_ptr = nullptr, *cell_order = nullptr;  // colour-parallel build only
 };
 
 int *copy_ints(const int *src, long n) {
@@ -607,10 +634,12 @@ void free_mg_level(MGLevelStore &M) {
   delete M.other_b;
   delete[] M.f;
   delete[] M.u;
+  delete[] M.colour_ptr;
+  delete[] M.cell_order;
 }
 
 struct CycleChain {
-  int pre = 2, post = 2;
+  int pre = 2, post = 2, threads = 1;
   double damp = 1.0;
   Hier *H = nullptr;
   std::vector<MGLevelStore *> lev;
@@ -697,6 +726,9 @@ __attribute__((visibility("default"))) void ref_cycle_vcycle(void *h, const doub
   db->INTERNAL_PRESSURE_SPACE = -11;
   db->SC_VERBOSE = 0;
   db->MG_DEBUG = 0;
+#ifdef _HYBRID
+  db->OMPNUMTHREADS = Y->threads;
+#endif
   const int top = (int)Y->H->sides.size() - 1;
   const Side &F = *Y->H->sides[top];
   const int n = 3 * F.n_u + F.n_p;
@@ -705,6 +737,38 @@ __attribute__((visibility("default"))) void ref_cycle_vcycle(void *h, const doub
   Y->ite->Iterate(nullptr, nullptr, z, rhs.data());
   convert_pressure(F, Y->H->frames[top], z + 3 * (size_t)F.n_u, false);
 }
+
+#ifdef _HYBRID
+// The colour-parallel build: the colouring of level `level` (colour k holds
+// the cells cell_order[colour_ptr[k] .. colour_ptr[k+1]-1], no two sharing a
+// DOF) and the OpenMP threads of the colour loops (OMPNUMTHREADS; the result
+// does not depend on it).  Every smoothed level needs one before a cycle.
+// Returns 0, or -1 for an inconsistent colouring.
+__attribute__((visibility("default"))) int ref_cycle_set_colours(void *h, int level,
+                                                                 int n_colours,
+                                                                 const int *colour_ptr,
+                                                                 const int *cell_order,
+                                                                 int n_cells, int threads) {
+  CycleChain *Y = static_cast<CycleChain *>(h);
+  if (level < 0 || level >= (int)Y->lev.size() || n_cells != Y->H->sides[level]->n_cells ||
+      n_colours <= 0 || colour_ptr[0] != 0 || colour_ptr[n_colours] != n_cells || threads <= 0)
+    return -1;
+  int max_cells = 0;
+  for (int k = 0; k < n_colours; ++k) {
+    const int m = colour_ptr[k + 1] - colour_ptr[k];
+    if (m <= 0) return -1;
+    max_cells = std::max(max_cells, m);
+  }
+  MGLevelStore &M = *Y->lev[level];
+  delete[] M.colour_ptr;
+  delete[] M.cell_order;
+  M.colour_ptr = copy_ints(colour_ptr, n_colours + 1L);
+  M.cell_order = copy_ints(cell_order, n_cells);
+  M.level->set_colours(n_colours, M.colour_ptr, M.cell_order, max_cells);
+  Y->threads = threads;
+  return 0;
+}
+#endif
 
 // The smoothing counts and damping of ref_cycle_precond (V(2,2) with
 // damping 1 until set).

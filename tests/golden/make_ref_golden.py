@@ -22,6 +22,9 @@ oracle/build_oracle.py compiles with the reference sources where they lie:
   three TNSE_MGLevel4 levels: cell Vanka on the levels above the coarsest
   (sequential build), SolveExact on the coarsest, the reference's transfers
   between them;
+* tests/golden/ref_cycle_colour_*.npz, ref_solve_colour_*.npz: the same
+  cycle and whole solver in the reference's colour-parallel build (every
+  smoothed level swept by the OpenMP colour loop over its own colouring);
 * tests/golden/ref_solve_*.npz: the whole reference solver, its flexible
   FGMRES (TFgmresIte::Iterate, src/FE/FgmresIte.C:250-677) preconditioned by
   that cycle driver, from zero on the problem's right-hand side (stored with
@@ -29,7 +32,8 @@ oracle/build_oracle.py compiles with the reference sources where they lie:
 Needs the reference tree; the fixtures are committed so the tests do not.
 ``python make_ref_golden.py cycle`` writes the cycle fixtures only,
 ``python make_ref_golden.py solve`` the whole-solver ones,
-``python make_ref_golden.py colour`` the colour-parallel Vanka ones.
+``python make_ref_golden.py colour`` the colour-parallel Vanka, cycle and
+solver ones.
 
 Inputs are exact binary fractions of the DOF index (``golden_inputs``), so
 every platform forms the same x and b without a random generator.
@@ -172,6 +176,45 @@ def write_solve_fixtures() -> None:
         print("wrote solve", name, "iterations", it, "ndof", b.size)
 
 
+# the cycle and whole-solver fixtures of the reference's colour-parallel
+# build: every smoothed level swept by CellVanka's OpenMP colour loop over the
+# level's own colouring (its cell_colour)
+COLOUR_CYCLE_CASES = ("hexa3", "channel3")
+COLOUR_SOLVE_CASES = ("hexa3",)
+
+
+def write_colour_cycle_fixtures() -> None:
+    from oracle.pyoracle import Oracle
+    from oracle.pyref import RefCycle, RefLevel
+    for name in COLOUR_CYCLE_CASES:
+        kwargs = CYCLE_CASES[name]
+        P = build_problem(kwargs)
+        _, b = golden_inputs(P.ndof(-1))
+        np.savez_compressed(
+            HERE / f"ref_cycle_colour_{name}.npz", problem=json.dumps(kwargs),
+            level=P.n_levels - 1, vcycle=RefCycle(P, colours=True).vcycle(b, pre=2, post=2,
+                                                                          damp=1.0),
+            source=("reference src/FE/MultiGridIte.C TMultiGridIte::Iterate with "
+                    "src/FE/NSE_MultiGrid.C TNSE_MultiGrid::Cycle (V(2,2), cell Vanka _HYBRID "
+                    "colour loop over the levels' cell_colour, SolveExact) run by "
+                    "oracle/ref_transfer.cpp"))
+        print("wrote colour cycle", name, "ndof", P.ndof(-1))
+    for name in COLOUR_SOLVE_CASES:
+        kwargs, fgmres = SOLVE_CASES[name]
+        P = build_problem(kwargs)
+        b = P.rhs()
+        params = Oracle(P, vanka_mode="colour", **fgmres).params
+        x, it = RefLevel(P.arrays(P.n_levels - 1), threads=1).fgmres_with_reference_cycle(
+            RefCycle(P, colours=True), params, np.zeros_like(b), b)
+        np.savez_compressed(
+            HERE / f"ref_solve_colour_{name}.npz", problem=json.dumps(kwargs),
+            level=P.n_levels - 1, fgmres=json.dumps(fgmres), solution=x, iterations=it,
+            source=("reference src/FE/FgmresIte.C TFgmresIte::Iterate (run by "
+                    "oracle/ref_harness.cpp) preconditioned by the colour-parallel cycle of "
+                    "ref_cycle_colour_*; right-hand side: that of ref_solve_" + name + ".npz"))
+        print("wrote colour solve", name, "iterations", it)
+
+
 def main() -> None:
     from oracle.pyref import RefLevel, RefTransfer, RefVankaLevel, ref_harness_lib
     if ref_harness_lib() is None:
@@ -184,6 +227,7 @@ def main() -> None:
         return
     if sys.argv[1:] == ["colour"]:
         write_colour_vanka_fixtures()
+        write_colour_cycle_fixtures()
         return
     for name, (kwargs, level) in CASES.items():
         P = build_problem(kwargs)

@@ -86,7 +86,7 @@ def load_case(name, kind="defect"):
         assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
     elif kind in ("vanka", "coarse", "vanka_colour"):
         assert P.arrays(level)["n_cells"] == int(g["n_cells"])
-    elif kind == "cycle":
+    elif kind in ("cycle", "cycle_colour"):
         assert level == P.n_levels - 1
     if kind == "transfer":  # x on the coarse level, b on the fine one
         return P, level, gm.golden_inputs(P.ndof(level - 1))[0], gm.golden_inputs(P.ndof(level))[1], g
@@ -699,3 +699,109 @@ def test_gpu_vanka_matches_reference_colour_parallel_fixtures(name):
                  alpha=float(g["alpha"]))
     assert rel(W.cell_vanka(level, x, b, 2), g["u_damped2"]) < 1e-9
     W.close()
+
+
+# The cycle driver and the whole solver in the colour-parallel build: every
+# smoothed level swept by the OpenMP colour loop over its own colouring, the
+# ordering of the GPU's default V-cycle.  The oracle's colour mode agrees to
+# rounding (the refined cells' local DOF orders differ, as in the sequential
+# cycle tests).
+
+@pytest.mark.parametrize("name", ["hexa", "channel", "hexa3", "channel3"])
+@pytest.mark.parametrize("pre,post,damp,alpha,beta", [(2, 2, 1.0, 1.0, 1.0),
+                                                      (1, 3, 0.8, 0.9, 0.7)])
+def test_oracle_colour_vcycle_matches_the_reference_colour_parallel_cycle(
+        name, pre, post, damp, alpha, beta):
+    _hybrid_or_skip()
+    RefCycle = _ref_cycle_or_skip()
+    gm = _golden_module()
+    P = gm.build_problem(gm.CYCLE_CASES[name])
+    _, b = gm.golden_inputs(P.ndof(-1))
+    z_ref = RefCycle(P, alpha=alpha, beta=beta, colours=True).vcycle(b, pre, post, damp)
+    O = Oracle(P, vanka_mode="colour", pre_smooth=pre, post_smooth=post, smooth_damp=damp,
+               alpha=alpha, beta=beta)
+    assert rel(O.vcycle(b), z_ref) < 1e-13
+
+
+def test_oracle_fgmres_equals_the_whole_colour_parallel_reference_solver():
+    _hybrid_or_skip()
+    RefCycle = _ref_cycle_or_skip()
+    ref_lib_or_skip()
+    from oracle.pyref import RefLevel
+    gm = _golden_module()
+    kwargs, fgmres = gm.SOLVE_CASES["hexa3"]
+    P = gm.build_problem(kwargs)
+    b = P.rhs()
+    O = Oracle(P, vanka_mode="colour", **fgmres)
+    x_o, info = O.iterate(np.zeros_like(b), b)
+    x_r, it = RefLevel(P.arrays(P.n_levels - 1), threads=1).fgmres_with_reference_cycle(
+        RefCycle(P, colours=True), O.params, np.zeros_like(b), b)
+    assert info["iterations"] == it
+    assert rel(x_o, x_r) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["hexa3", "channel3"])
+def test_colour_cycle_fixtures_reproduce_from_the_reference(name):
+    _hybrid_or_skip()
+    RefCycle = _ref_cycle_or_skip()
+    P, level, _, b, g = load_case(name, "cycle_colour")
+    assert np.array_equal(RefCycle(P, colours=True).vcycle(b, pre=2, post=2, damp=1.0),
+                          g["vcycle"])
+
+
+@pytest.mark.parametrize("name", ["hexa3", "channel3"])
+def test_oracle_colour_vcycle_matches_reference_colour_cycle_fixtures(name):
+    P, level, _, b, g = load_case(name, "cycle_colour")
+    assert rel(Oracle(P, vanka_mode="colour").vcycle(b), g["vcycle"]) < 1e-13
+
+
+def _load_colour_solve():
+    P, fgmres, g = _load_solve("hexa3")
+    c = np.load(GOLD / "ref_solve_colour_hexa3.npz")
+    assert json.loads(str(c["problem"])) == json.loads(str(g["problem"]))
+    return P, fgmres, g["rhs"], c
+
+
+def test_oracle_colour_fgmres_matches_reference_colour_solve_fixture():
+    P, fgmres, b, c = _load_colour_solve()
+    x, info = Oracle(P, vanka_mode="colour", **fgmres).iterate(np.zeros_like(b), b)
+    assert info["iterations"] == int(c["iterations"])
+    assert rel(x, c["solution"]) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hexa3", "channel3"])
+def test_gpu_vcycle_matches_reference_colour_cycle_fixtures(name):
+    """The library's default FP64 V-cycle (graph-captured, colour-block
+    sweeps over the levels' colourings) against the reference's
+    colour-parallel cycle driver."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, _, b, g = load_case(name, "cycle_colour")
+    S = PmSolver(P.descs, precision="fp64")
+    assert rel(S.vcycle(b), g["vcycle"]) < 1e-9
+    S.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gpu_fgmres_matches_reference_colour_solve_fixture(precision):
+    """The library's default solve against the whole colour-parallel
+    reference solver: FP64 takes its iterations and agrees to 1e-9, mixed
+    precision is within 1e-6 (pressures after L2_0 normalisation)."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, fgmres, b, c = _load_colour_solve()
+    xr = c["solution"]
+    S = PmSolver(P.descs, precision=precision, **fgmres)
+    x, info = S.iterate(np.zeros_like(b), b)
+    S.close()
+    assert info["status"] == 0
+    if precision == "fp64":
+        assert info["iterations"] == int(c["iterations"])
+        assert rel(x, xr) < 1e-9
+    else:
+        n3 = 3 * P.desc(P.n_levels - 1).n_udof
+        assert rel(x[:n3], xr[:n3]) < 1e-6
+        xp, rp = x[n3:].copy(), xr[n3:].copy()
+        xp[0::4] -= xp[0::4].mean()
+        rp[0::4] -= rp[0::4].mean()
+        assert rel(xp, rp) < 1e-6
