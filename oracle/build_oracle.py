@@ -76,7 +76,8 @@ def build_ref_pin() -> Path | None:
 # reference translation units of the harness, compiled where they lie
 REF_HARNESS_TUS = ("FE/MGComponents3D", "FE/FgmresIte", "FE/ItMethod", "FE/Matrix",
                    "FE/SquareMatrix", "FE/Structure", "FE/SquareStructure", "FE/Blas1",
-                   "FE/NSE_MGLevel4", "FE/NSE_MGLevel", "FE/LinAlg", "FE/FESpace",
+                   "FE/NSE_MGLevel4", "FE/NSE_MGLevel2", "FE/NSE_MGLevel", "FE/LinAlg",
+                   "FE/FESpace",
                    "FE/FESpace3D", "FE/FE3D", "FE/Structure3D", "FE/SquareStructure3D",
                    "FE/SquareMatrix3D", "FE/Matrix3D", "Geometry/Collection")
 REF_INCLUDE_DIRS = ("General", "FE", "Geometry", "FE3D", "FE2D", "FE1D", "System",

@@ -73,6 +73,8 @@ def _declare(L):
                                    _ip, _ip, _dpp, _ip, _ip, _dpp, _ip, _ip, _dpp,
                                    C.c_double]
     L.ref_vanka_create.restype = C.c_void_p
+    L.ref_vanka2_create.argtypes = L.ref_vanka_create.argtypes
+    L.ref_vanka2_create.restype = C.c_void_p
     L.ref_vanka_destroy.argtypes = [C.c_void_p]
     L.ref_vanka_destroy.restype = None
     L.ref_vanka_sweeps.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double]
@@ -210,9 +212,13 @@ class RefVankaLevel:
     ``colours`` (one colour per cell, no two cells of a colour sharing a
     DOF), the colour-parallel build's OpenMP colour loop (:603-1651) over
     those colours in increasing order, cells of a colour in index order, on
-    ``threads`` threads."""
+    ``threads`` threads.  With ``one_block`` the level is an NSTYPE-2
+    TNSE_MGLevel2 (src/FE/NSE_MGLevel2.C) built on a[0] alone, its CellVanka
+    :336-700 (no colour-parallel variant)."""
 
-    def __init__(self, arrays: dict, alpha: float = 1.0, colours=None, threads: int = 4):
+    def __init__(self, arrays: dict, alpha: float = 1.0, colours=None, threads: int = 4,
+                 one_block: bool = False):
+        assert not (one_block and colours is not None)
         L = ref_harness_lib() if colours is None else ref_hybrid_lib()
         if L is None:
             raise RuntimeError("reference tree not present: the reference harness is not built")
@@ -238,10 +244,12 @@ class RefVankaLevel:
             keep.append(ptrs)
             return C.cast(ptrs, _dpp)
 
-        self._h = L.ref_vanka_create(
+        create = L.ref_vanka2_create if one_block else L.ref_vanka_create
+        self._h = create(
             self.n_u, int(arrays["n_active"]), self.n_p, n_cells, nu_loc,
             udofs.ctypes.data_as(_ip), pdofs.ctypes.data_as(_ip),
-            ip(arrays["a_rowptr"]), ip(arrays["a_col"]), dpp(arrays["a"]),
+            ip(arrays["a_rowptr"]), ip(arrays["a_col"]),
+            dpp(arrays["a"][:1] if one_block else arrays["a"]),
             ip(arrays["b_rowptr"]), ip(arrays["b_col"]), dpp(arrays["b"]),
             ip(arrays["bt_rowptr"]), ip(arrays["bt_col"]), dpp(arrays["bt"]), float(alpha))
         if not self._h:

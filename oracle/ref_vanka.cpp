@@ -64,6 +64,7 @@
 #include <FEDatabase3D.h>
 #include <FESpace3D.h>
 #include <Matrix3D.h>
+#include <NSE_MGLevel2.h>
 #include <NSE_MGLevel4.h>  // includes Magma_Solver.h (no include guard)
 #include <SquareMatrix3D.h>
 #include <SquareStructure3D.h>
@@ -113,6 +114,16 @@ struct Level : public TNSE_MGLevel4 {
 #endif
 };
 
+// NSTYPE-2 level (src/FE/NSE_MGLevel2.C): one velocity block A for the
+// three components; the same auxiliary vectors (:131-135)
+struct Level2 : public TNSE_MGLevel2 {
+  using TNSE_MGLevel2::TNSE_MGLevel2;
+  void release() {
+    delete[] Aux[0];
+    delete[] Aux;
+  }
+};
+
 template <class T>
 T *copy_of(const T *src, long n) {
   T *d = new T[n > 0 ? n : 1];
@@ -140,6 +151,10 @@ struct VankaLevel {
   double al[2] = {1.0, 1.0};
   alignas(Level) unsigned char level_store[sizeof(Level)];
   Level *level = nullptr;
+  alignas(Level2) unsigned char level2_store[sizeof(Level2)];
+  Level2 *level2 = nullptr;  // NSTYPE-2 levels (ref_vanka2_create)
+  TNSE_MGLevel *base = nullptr;
+  int n_blocks = 9;
   int *colour_ptr = nullptr, *cell_order = nullptr;  // colour-parallel build only
   int threads = 1;
 };
@@ -164,13 +179,19 @@ extern "C" {
 // pressure DOFs (cell_udofs, cell_pdofs), the CSR arrays as for
 // ref_level_create, and the relaxation alpha of the level (al[0] of the
 // TNSE_MGLevel4 constructor).  Returns null for an unsupported nu_loc.
-__attribute__((visibility("default"))) void *ref_vanka_create(
-    int n_u, int n_active, int n_p, int n_cells, int nu_loc, const int *cell_udofs,
-    const int *cell_pdofs, const int *a_rowptr, const int *a_col, const double *const *a,
-    const int *b_rowptr, const int *b_col, const double *const *b, const int *bt_rowptr,
-    const int *bt_col, const double *const *bt, double alpha) {
+}  // extern "C"
+
+namespace {
+
+VankaLevel *make_vanka_level(int n_blocks, int n_u, int n_active, int n_p, int n_cells,
+                             int nu_loc, const int *cell_udofs, const int *cell_pdofs,
+                             const int *a_rowptr, const int *a_col, const double *const *a,
+                             const int *b_rowptr, const int *b_col, const double *const *b,
+                             const int *bt_rowptr, const int *bt_col, const double *const *bt,
+                             double alpha) {
   if (nu_loc != 27 && nu_loc != 15) return nullptr;
   VankaLevel *V = new VankaLevel;
+  V->n_blocks = n_blocks;
   V->n_u = n_u;
   V->n_p = n_p;
   V->n = 3 * n_u + n_p;
@@ -207,7 +228,7 @@ __attribute__((visibility("default"))) void *ref_vanka_create(
                              copy_of(b_rowptr, n_p + 1L));
   V->sbt = new LevelStructure(V->oa, V->ob, V->us, V->ps, n_u, n_p, bt_nnz,
                               copy_of(bt_col, bt_nnz), copy_of(bt_rowptr, n_u + 1L));
-  for (int k = 0; k < 9; ++k) {
+  for (int k = 0; k < n_blocks; ++k) {
     V->A[k] = new (V->a_store[k]) TSquareMatrix3D(V->sa);  // allocates its entries
     std::memcpy(V->A[k]->GetEntries(), a[k], sizeof(double) * a_nnz);
   }
@@ -221,18 +242,53 @@ __attribute__((visibility("default"))) void *ref_vanka_create(
   V->u = new double[V->n]();
   V->aux = new double[V->n]();
   V->al[0] = alpha;
-  V->level = new (V->level_store)
-      Level(0, V->A[0], V->A[1], V->A[2], V->A[3], V->A[4], V->A[5], V->A[6], V->A[7], V->A[8],
-            V->B[0], V->B[1], V->B[2], V->B[3], V->B[4], V->B[5], V->f, V->u, 1, V->al, 0, 0,
-            V->coll, nullptr);
+  if (n_blocks == 9) {
+    V->level = new (V->level_store)
+        Level(0, V->A[0], V->A[1], V->A[2], V->A[3], V->A[4], V->A[5], V->A[6], V->A[7],
+              V->A[8], V->B[0], V->B[1], V->B[2], V->B[3], V->B[4], V->B[5], V->f, V->u, 1,
+              V->al, 0, 0, V->coll, nullptr);
+    V->base = V->level;
+  } else {
+    V->level2 = new (V->level2_store)
+        Level2(0, V->A[0], V->B[0], V->B[1], V->B[2], V->B[3], V->B[4], V->B[5], V->f, V->u, 1,
+               V->al, 0, 0, V->coll, nullptr);
+    V->base = V->level2;
+  }
   return V;
+}
+
+}  // namespace
+
+extern "C" {
+
+__attribute__((visibility("default"))) void *ref_vanka_create(
+    int n_u, int n_active, int n_p, int n_cells, int nu_loc, const int *cell_udofs,
+    const int *cell_pdofs, const int *a_rowptr, const int *a_col, const double *const *a,
+    const int *b_rowptr, const int *b_col, const double *const *b, const int *bt_rowptr,
+    const int *bt_col, const double *const *bt, double alpha) {
+  return make_vanka_level(9, n_u, n_active, n_p, n_cells, nu_loc, cell_udofs, cell_pdofs,
+                          a_rowptr, a_col, a, b_rowptr, b_col, b, bt_rowptr, bt_col, bt, alpha);
+}
+
+// The same level as NSTYPE 2 (TNSE_MGLevel2, src/FE/NSE_MGLevel2.C:43-146):
+// a[0] is the one velocity block of the three components; its CellVanka
+// (:336-700) builds the 85x85 (49x49) system with that block on the three
+// diagonal positions and solves it as the NSTYPE-4 one does.
+__attribute__((visibility("default"))) void *ref_vanka2_create(
+    int n_u, int n_active, int n_p, int n_cells, int nu_loc, const int *cell_udofs,
+    const int *cell_pdofs, const int *a_rowptr, const int *a_col, const double *const *a,
+    const int *b_rowptr, const int *b_col, const double *const *b, const int *bt_rowptr,
+    const int *bt_col, const double *const *bt, double alpha) {
+  return make_vanka_level(1, n_u, n_active, n_p, n_cells, nu_loc, cell_udofs, cell_pdofs,
+                          a_rowptr, a_col, a, b_rowptr, b_col, b, bt_rowptr, bt_col, bt, alpha);
 }
 
 __attribute__((visibility("default"))) void ref_vanka_destroy(void *h) {
   VankaLevel *V = static_cast<VankaLevel *>(h);
   if (!V) return;
-  V->level->release();
-  for (int k = 0; k < 9; ++k) delete[] V->A[k]->GetEntries();
+  if (V->level) V->level->release();
+  if (V->level2) V->level2->release();
+  for (int k = 0; k < V->n_blocks; ++k) delete[] V->A[k]->GetEntries();
   for (int k = 0; k < 6; ++k) delete[] V->B[k]->GetEntries();
   delete V->sa;
   delete V->sb;
@@ -265,7 +321,8 @@ __attribute__((visibility("default"))) int ref_vanka_set_colours(void *h, int n_
                                                                  const int *cell_order,
                                                                  int n_cells, int threads) {
   VankaLevel *V = static_cast<VankaLevel *>(h);
-  if (n_colours <= 0 || colour_ptr[0] != 0 || colour_ptr[n_colours] != n_cells || threads <= 0)
+  if (!V->level || n_colours <= 0 || colour_ptr[0] != 0 || colour_ptr[n_colours] != n_cells ||
+      threads <= 0)
     return -1;
   int max_cells = 0;
   for (int k = 0; k < n_colours; ++k) {
@@ -295,11 +352,11 @@ __attribute__((visibility("default"))) void ref_vanka_sweeps(void *h, double *u,
   db->SC_LARGEST_DIRECT_SOLVE = 1 << 20;
   db->INTERNAL_LOCAL_DOF = -1;
 #ifdef _HYBRID
-  if (!V->colour_ptr) return;  // no colouring set: nothing to sweep
+  if (V->level && !V->colour_ptr) return;  // no colouring set: nothing to sweep
   db->OMPNUMTHREADS = V->threads;
 #endif
   double *r = copy_of(rhs, V->n);
-  for (int s = 0; s < sweeps; ++s) V->level->CellVanka(u, r, V->aux, 0, nullptr, 2, 1);
+  for (int s = 0; s < sweeps; ++s) V->base->CellVanka(u, r, V->aux, 0, nullptr, 2, 1);
   delete[] r;
 }
 
@@ -314,7 +371,7 @@ __attribute__((visibility("default"))) void ref_vanka_solve_exact(void *h, doubl
   TDatabase::ParamDB->INTERNAL_PROJECT_PRESSURE = pin_pressure;
   TDatabase::ParamDB->INTERNAL_PRESSURE_SPACE = -11;
   double *r = copy_of(rhs, V->n);
-  V->level->SolveExact(u, r);
+  V->base->SolveExact(u, r);
   delete[] r;
 }
 

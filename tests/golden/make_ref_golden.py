@@ -12,6 +12,9 @@ oracle/build_oracle.py compiles with the reference sources where they lie:
 * tests/golden/ref_vanka_*.npz: one and two sweeps of the cell Vanka
   TNSE_MGLevel4::CellVanka (src/FE/NSE_MGLevel4.C:1653-2087, sequential
   build, damping 1, no relaxation) from u = x with right-hand side b;
+* tests/golden/ref_vanka_nse2_*.npz: the same sweeps by the reference's
+  NSTYPE-2 level (TNSE_MGLevel2::CellVanka, src/FE/NSE_MGLevel2.C:336-700)
+  built on the one velocity block A11 of these one-block problems;
 * tests/golden/ref_vanka_colour_*.npz: the same sweeps by the reference's
   colour-parallel build (-D_HYBRID: CellVanka's OpenMP colour loop,
   src/FE/NSE_MGLevel4.C:603-1651) over the level's own colouring, and two
@@ -251,6 +254,17 @@ def main() -> None:
             source=("reference src/FE/NSE_MGLevel4.C TNSE_MGLevel4::CellVanka (_SEQ) "
                     "run by oracle/ref_vanka.cpp"))
         print("wrote vanka", name, "level", level, "ndof", P.ndof(level))
+    for name, (kwargs, level) in VANKA_CASES.items():
+        P = build_problem(kwargs)
+        V = RefVankaLevel(P.arrays(level), one_block=True)
+        x, b = golden_inputs(P.ndof(level))
+        np.savez_compressed(
+            HERE / f"ref_vanka_nse2_{name}.npz",
+            problem=json.dumps(kwargs), level=level, n_cells=P.arrays(level)["n_cells"],
+            u_sweep1=V.cell_vanka(x, b, 1), u_sweep2=V.cell_vanka(x, b, 2),
+            source=("reference src/FE/NSE_MGLevel2.C TNSE_MGLevel2::CellVanka (NSTYPE 2, "
+                    "the one velocity block A11) run by oracle/ref_vanka.cpp"))
+        print("wrote NSTYPE-2 vanka", name, "level", level, "ndof", P.ndof(level))
     for name, (kwargs, _) in CASES.items():
         P = build_problem(kwargs)
         V = RefVankaLevel(P.arrays(0))

@@ -84,7 +84,7 @@ def load_case(name, kind="defect"):
     if kind == "defect":
         assert P.arrays(level)["n_udof"] == int(g["n_udof"])
         assert P.arrays(level)["n_pdof"] == int(g["n_pdof"])
-    elif kind in ("vanka", "coarse", "vanka_colour"):
+    elif kind in ("vanka", "coarse", "vanka_colour", "vanka_nse2"):
         assert P.arrays(level)["n_cells"] == int(g["n_cells"])
     elif kind in ("cycle", "cycle_colour"):
         assert level == P.n_levels - 1
@@ -243,15 +243,17 @@ def test_oracle_vanka_equals_reference_cell_vanka_bitwise(case):
         assert np.max(np.abs(u_ref - u)) > 1e-3  # the sweep did change u
 
 
-def per_cell_colours(P, levels):
-    """The problem's descriptors with every cell of each level in ``levels``
-    (one level or several) its own colour (the colour-block sweep then runs
-    the cells one by one, in index order).  Returns the descriptors and the
-    colour arrays they point at."""
+def per_cell_colours(P, levels, source=None):
+    """The problem's descriptors (or those of ``source``, e.g. its one-block
+    descriptors) with every cell of each level in ``levels`` (one level or
+    several) its own colour (the colour-block sweep then runs the cells one
+    by one, in index order).  Returns the descriptors and the colour arrays
+    they point at."""
     from to_merge_master_parmoon_gb300._lib import PmLevelDesc
+    source = P.descs if source is None else source
     descs = (PmLevelDesc * P.n_levels)()
     for l in range(P.n_levels):
-        C.pointer(descs[l])[0] = P.descs[l]
+        C.pointer(descs[l])[0] = source[l]
     colours = []
     for level in ([levels] if isinstance(levels, int) else levels):
         colours.append(np.arange(P.arrays(level)["n_cells"], dtype=np.int32))
@@ -805,3 +807,67 @@ def test_gpu_fgmres_matches_reference_colour_solve_fixture(precision):
         xp[0::4] -= xp[0::4].mean()
         rp[0::4] -= rp[0::4].mean()
         assert rel(xp, rp) < 1e-6
+
+
+# ------------------------------------------------------------ NSTYPE 2 ----
+# The reference's NSTYPE-2 level, TNSE_MGLevel2 (src/FE/NSE_MGLevel2.C), holds
+# one velocity block for the three components; its CellVanka (:336-700)
+# builds the same local system as the NSTYPE-4 one with that block on the
+# diagonal and no coupling, and forms the local residual from the one block,
+# so on these one-block problems it agrees with the oracle (which equals the
+# NSTYPE-4 CellVanka bit for bit) to rounding.  The library's one-block
+# descriptors are the NSTYPE-2 boundary.
+
+@pytest.mark.parametrize("name,kwargs,level", [
+    ("hexa", dict(n_levels=3, nu=1e-2, seed=0), 1),
+    ("hexa", dict(n_levels=3, nu=1e-2, seed=0), 2),
+    ("channel", None, 1),
+    ("tetra", None, 1),
+])
+@pytest.mark.parametrize("damp,alpha", [(1.0, 1.0), (0.8, 0.7)])
+def test_oracle_vanka_matches_the_reference_nstype2_vanka(name, kwargs, level, damp, alpha):
+    ref_lib_or_skip()
+    from oracle.pyref import RefVankaLevel
+    gm = _golden_module()
+    if kwargs is None:
+        kwargs = gm.CASES["channel"][0] if name == "channel" else gm.VANKA_CASES["tetra"][0]
+    P = gm.build_problem(kwargs)
+    assert P.is_one_block()
+    x, b = gm.golden_inputs(P.ndof(level))
+    want = RefVankaLevel(P.arrays(level), alpha=alpha, one_block=True).cell_vanka(x, b, 2, damp)
+    got = Oracle(P, vanka_mode="seq", smooth_damp=damp, alpha=alpha).cell_vanka(level, x, b, 2)
+    assert rel(got, want) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["hexa", "tetra"])
+def test_nstype2_vanka_fixtures_reproduce_from_the_reference(name):
+    ref_lib_or_skip()
+    from oracle.pyref import RefVankaLevel
+    P, level, x, b, g = load_case(name, "vanka_nse2")
+    V = RefVankaLevel(P.arrays(level), one_block=True)
+    assert np.array_equal(V.cell_vanka(x, b, 1), g["u_sweep1"])
+    assert np.array_equal(V.cell_vanka(x, b, 2), g["u_sweep2"])
+
+
+@pytest.mark.parametrize("name", ["hexa", "tetra"])
+def test_oracle_vanka_matches_reference_nstype2_fixtures(name):
+    P, level, x, b, g = load_case(name, "vanka_nse2")
+    O = Oracle(P, vanka_mode="seq")
+    assert rel(O.cell_vanka(level, x, b, 1), g["u_sweep1"]) < 1e-13
+    assert rel(O.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-13
+
+
+@pytest.mark.gpu
+def test_gpu_one_block_vanka_matches_reference_nstype2_fixture():
+    """The library's one-block (NSTYPE-2) descriptors, one cell per colour,
+    FP64 block elimination, against TNSE_MGLevel2::CellVanka."""
+    from to_merge_master_parmoon_gb300 import PmSolver
+    P, level, x, b, g = load_case("hexa", "vanka_nse2")
+    assert P.is_one_block()
+    descs, colours = per_cell_colours(P, level, source=P.descs_one_block())
+    S = PmSolver(descs, precision="fp64")
+    assert S._lib.pm_level_blocks(S._h, level) == 1
+    assert rel(S.cell_vanka(level, x, b, 1), g["u_sweep1"]) < 1e-9
+    assert rel(S.cell_vanka(level, x, b, 2), g["u_sweep2"]) < 1e-9
+    S.close()
+    del colours
