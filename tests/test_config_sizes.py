@@ -6,8 +6,8 @@ residual 1e-10.
 The oracle's FGMRES (src/FE/FgmresIte.C:250-677 over the cycle of
 src/FE/NSE_MultiGrid.C:434-1779) is the reference answer; where the
 reference tree is present, the reference's own solver (its FGMRES over its
-own cycle driver, compiled where they lie) is run on the same problem and
-the oracle checked against it.  Bars, as the
+own cycle driver, compiled where they lie; sequential and colour-parallel
+cell Vanka) is run on the same problem and the oracle checked against it.  Bars, as the
 path's correctness target states them: the GPU solution reaches 1e-10
 relative residual, its velocity and its pressure each differ from the
 oracle's by at most 1e-6 relative L2 (pressures compared after the same
@@ -88,6 +88,28 @@ def test_oracle_equals_the_whole_reference_solver(config0):
     assert it == i_s["iterations"]
     assert np.linalg.norm(xs - xr) <= 1e-13 * np.linalg.norm(xr)
     assert eu <= 1e-7 and ep <= 1e-7
+
+
+def test_colour_oracle_equals_the_colour_parallel_reference_solver(config0):
+    """The colour-ordered oracle the GPU is compared with, against the
+    reference's own solver in its colour-parallel build (CellVanka's OpenMP
+    colour loop, src/FE/NSE_MGLevel4.C:603-1651, over every level's own
+    colouring, inside its cycle driver and FGMRES): the same iterations and
+    the same solution to rounding."""
+    from oracle.pyref import ref_harness_lib, ref_transfer_lib
+    if ref_harness_lib() is None or ref_transfer_lib(hybrid=True) is None:
+        pytest.skip("reference tree not present: the harnesses are not built")
+    from oracle.pyref import RefCycle, RefLevel
+    P, b, r0, xo, io = config0
+    x0 = np.zeros_like(b)
+    O = Oracle(P, restart=20, maxit=100, res_norm_min=RTOL * r0)
+    xr, it = RefLevel(P.arrays(LEVELS - 1), threads=4).fgmres_with_reference_cycle(
+        RefCycle(P, colours=True, threads=4), O.params, x0, b)
+    print(f"config 0 colour-parallel reference solver: {it} iterations "
+          f"(oracle {io['iterations']}), rel. difference "
+          f"{np.linalg.norm(xo - xr) / np.linalg.norm(xr):.2e}")
+    assert it == io["iterations"]
+    assert np.linalg.norm(xo - xr) <= 1e-13 * np.linalg.norm(xr)
 
 
 @pytest.mark.gpu
