@@ -61,3 +61,23 @@ def test_no_device_is_reported_not_faked(monkeypatch):
     with pytest.raises(PmError) as e:
         PmSolver()
     assert e.value.status == 9  # PM_NO_DEVICE
+
+
+@pytest.mark.parametrize("opts,status", [
+    (dict(factor_fp32=2), 6),                        # PM_BADARG: not -1, 0 or 1
+    (dict(precision="fp64", factor_fp32=1), 6),      # PM_BADARG: FP32 factors need mixed
+    (dict(precision="fp64", factor_fp32=-1), 9),     # the default: valid in both precisions
+    (dict(precision="mixed", factor_fp32=0), 9),
+])
+def test_factor_precision_option_is_validated_before_the_device(opts, status):
+    """pm_create checks factor_fp32 (-1 default: FP32 block elimination and
+    FP64 85x85 LU in mixed precision; 0 all FP64; 1 all FP32, mixed only)
+    before it looks for a device, so on a host without a GPU a valid
+    setting reports PM_NO_DEVICE and an invalid one PM_BADARG."""
+    from to_merge_master_parmoon_gb300._lib import gpu_lib
+    if gpu_lib().pm_device_count() > 0:
+        pytest.skip("a GPU is present")
+    from to_merge_master_parmoon_gb300 import PmError, PmSolver
+    with pytest.raises(PmError) as e:
+        PmSolver(**opts)
+    assert e.value.status == status
